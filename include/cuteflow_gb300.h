@@ -1,0 +1,183 @@
+/*
+ * cuteflow_gb300.h -- C ABI of the GB300-native CuteFlow time step (libcfgb.so).
+ *
+ * The reference has no library API: its hot path is the body of solve_finite_volumes
+ * (finite_volumes_method.cuf:123-242), which reaches the kernels through module globals
+ * (global_data_device.cuf:8-76) filled by the host setup (data_transfer.cuf:4-100,
+ * maillage.cuf:4-166, main.cuf:124-169).  This header replaces that surface with plain
+ * C entry points a Fortran ISO_C_BINDING module (or ctypes, cgo, JNI) binds directly.
+ *
+ * Conventions
+ *  - Every call returns 0 or a negative CF_E* code; nothing calls exit().  The text of the
+ *    last error of a context is available from cf_last_error().
+ *  - Host arrays passed in are borrowed for the duration of the call only.
+ *  - Element order and indexing at the boundary are the reference's: element k of the mesh
+ *    tables is element k everywhere (any internal renumbering is undone on output), node
+ *    and element ids inside the mesh tables are 1-based, and states are element-major
+ *    (h, hu, hv) triples exactly like vdlg(3, nelt).
+ *  - A context owns all of its device memory and one CUDA stream; it is used by one host
+ *    thread at a time.  Separate contexts are independent.
+ *  - Arithmetic is IEEE FP64 throughout.
+ */
+#ifndef CUTEFLOW_GB300_H
+#define CUTEFLOW_GB300_H
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CF_MAX_IO 20
+
+/* Error codes */
+#define CF_OK 0
+#define CF_EINVAL -1     /* bad argument or inconsistent input */
+#define CF_ECUDA -2      /* CUDA runtime error (message in cf_last_error) */
+#define CF_ENOMEM -3     /* device or host allocation failed */
+#define CF_EDT -4        /* time step left the range (1e-12, 9999] (cfl_condition.cuf:129-132) */
+#define CF_ENONFINITE -5 /* a NaN or Inf appeared in the state */
+#define CF_ESTATE -6     /* call out of order (e.g. stepping before a state was set) */
+#define CF_ENOTSUP -7    /* option not implemented */
+
+/* Device status bits reported in cf_step_info.status */
+#define CF_STATUS_DT_RANGE 1u
+#define CF_STATUS_NONFINITE 2u
+
+/* Mesh tables, as lec_mail_tri reads them (maillage.cuf:196-313). */
+typedef struct cf_mesh {
+  int32_t nnt;                     /* number of nodes (nnt) */
+  int32_t nelt;                    /* number of triangles (nelt) */
+  const double* x;                 /* [nnt] coordonnees(:,1) */
+  const double* y;                 /* [nnt] coordonnees(:,2) */
+  const double* z;                 /* [nnt] coordonnees(:,3): bed elevation at the nodes */
+  const int32_t* tri;              /* [3*nelt] 1-based node ids, tri[3*k+j] = connectivite(k+1,j+1);
+                                      edge j joins node j and node j+1 (mod 3) */
+  const double* manning_elt;       /* [nelt] manning_nelt; may be NULL with is_override_manning */
+  const int32_t* ndinput;          /* [ndi] inflow nodes (ndinput) */
+  const int32_t* numero_ndinput;   /* [ndi] inlet number of each inflow node (numero_ndinput) */
+  const int32_t* ndoutput;         /* [ndo] outflow nodes (ndoutput) */
+  const int32_t* numero_ndoutput;  /* [ndo] outlet number of each outflow node (numero_ndoutput) */
+  const int32_t* ndwall;           /* [ndw] wall nodes (ndwall) */
+  int32_t ndi, ndo, ndw;
+  int32_t nombre_entrees;          /* number of inlets (nombre_entrees) */
+  int32_t nombre_sorties;          /* number of outlets (nombre_sorties) */
+  int32_t pad_;
+} cf_mesh;
+
+/* The used subset of the donnees_namelist (global_data.cuf:31-94) plus extensions. */
+typedef struct cf_params {
+  double gp;                       /* gravity (gp) */
+  double tolisec;                  /* dry threshold (tolisec) */
+  double cfl;                      /* CFL number (cfl) */
+  double tol;                      /* friction velocity floor; the reference's tol is the
+                                      single-precision literal 1e-6 (global_data.cuf:59) */
+  double override_manning;         /* (override_manning) */
+  double constant_dt;              /* (constant_dt) */
+  double debitglob[CF_MAX_IO];     /* inflow discharge per inlet, m^3/s (debitglob) */
+  double h_sortie[CF_MAX_IO];      /* water level per outlet (h_sortie) */
+  double debitglob_start[CF_MAX_IO]; /* extension: discharge at t = 0 of a linear ramp */
+  double ramp_time;                /* extension: ramp duration in s; 0 keeps debitglob constant */
+  int32_t iflux;                   /* 1 HLLC, 2 HLLC (Ata et al. star states), 3 WAF, 4 MUSCL */
+  int32_t ilimiteur;               /* limiter (ilimiteur), default 1 */
+  int32_t friction;                /* 1: Manning friction (friction) */
+  int32_t fricimplic;              /* 0 explicit, 1 (I - dt/2 J)^-1, 2 diagonal (fricimplic) */
+  int32_t is_override_manning;     /* (is_override_manning) */
+  int32_t is_dt_constant;          /* (is_dt_constant) */
+  int32_t inlet;                   /* 1 'transm', 2 'inflow', 3 'phys_inflow' (data_transfer.cuf:43-55) */
+  int32_t outlet;                  /* 1 'fixedheight', 2 'transm' (data_transfer.cuf:57-66) */
+  int32_t flux_mode;               /* extension: 0 (default) = the reference's semantics, the flux of
+                                      every (element, edge) as that element evaluates it
+                                      (flux_riemann.cuf:33-426); 1 = conservative, one evaluation
+                                      per edge with the opposite sign for the neighbour */
+  int32_t reorder;                 /* extension: 1 = space-filling-curve renumbering (default) */
+} cf_params;
+
+/* set_initial_condition inputs (initial_condition.cuf:4-80, namelist global_data.cuf:40-44). */
+typedef struct cf_ic {
+  double x1eqbar, x2eqbar, y1eqbar, y2eqbar;
+  double h_amont, u_amont, v_amont, h_aval, u_aval, v_aval;
+  double xplan, yplan, zplan, xpoint, ypoint, zpoint;
+  int32_t eqlin_barrage;
+  int32_t plan;
+} cf_ic;
+
+/* Result of cf_step. */
+typedef struct cf_step_info {
+  double t;                        /* time after the last step: t0 + sum of the dt used */
+  double dt_last;                  /* dt used by the last step */
+  double dt_next;                  /* dt the next step will use (CFL of the current state) */
+  double q_in;                     /* inflow discharge of the last step (debit_entree_sum) */
+  double q_out;                    /* outflow discharge of the last step (debit_sortie) */
+  int64_t steps;                   /* steps taken since the state was set */
+  uint32_t status;                 /* CF_STATUS_* bits latched on the device */
+  int32_t pad_;
+} cf_step_info;
+
+typedef struct cf_ctx cf_ctx;
+
+/* Fill p with the reference's namelist defaults (global_data.cuf:31-62) and the values the
+ * reference's own cases set (gp = 9.81, tolisec = 1e-5, cfl = 0.9, iflux = 1). */
+int cf_default_params(cf_params* p);
+
+/* Build a context: boundary tagging and adjacency (replaces tab_bound_tri / boundary_kind,
+ * maillage.cuf:781-1110, and set_undefined_boudaries_as_walls, :1454-1471), geometry
+ * (compute_surface_and_bathy :1284-1331, the CFL length :132-165, inlet lengths
+ * :1423-1452), upwind tables (find_upwind_cells :954-978), renumbering and upload. */
+int cf_create(const cf_mesh* mesh, const cf_params* params, cf_ctx** out);
+
+/* Destroy a context and release its device memory (NULL is accepted). */
+void cf_destroy(cf_ctx* ctx);
+
+/* Set U^0 from host memory: hu3[3*k+c] = vdlg0(c+1, k+1) (read_initial_condition,
+ * initial_condition.cuf:82-102).  Resets the time to t0 and the step count, and computes
+ * the first dt (finite_volumes_method.cuf:113-116). */
+int cf_set_state(cf_ctx* ctx, const double* hu3, double t0);
+
+/* Same with a device pointer (3*nelt doubles, reference element order). */
+int cf_set_state_device(cf_ctx* ctx, const double* d_hu3, double t0);
+
+/* Initial condition by dam line or plane (set_initial_condition, initial_condition.cuf:4-80),
+ * then as cf_set_state. */
+int cf_set_initial_condition(cf_ctx* ctx, const cf_ic* ic, double t0);
+
+/* Advance nsteps steps of the time loop (finite_volumes_method.cuf:123-242 without file
+ * output).  Each step: fluxes, sources and friction, update with the wet/dry clamp, and the
+ * CFL dt of the new state for the next step, all on the device with no host round trip.
+ * info may be NULL. */
+int cf_step(cf_ctx* ctx, int32_t nsteps, cf_step_info* info);
+
+/* Copy U^n to host memory in reference order (3*nelt doubles). */
+int cf_get_state(cf_ctx* ctx, double* hu3_out);
+
+/* Copy U^n to device memory in reference order (3*nelt doubles). */
+int cf_get_state_device(cf_ctx* ctx, double* d_hu3_out);
+
+/* Current time, dt and status without stepping. */
+int cf_get_info(cf_ctx* ctx, cf_step_info* info);
+
+/* Preprocessing results in reference order, for comparison with the reference's own
+ * boundary table file (maillage.cuf:62-68).  boundary: [nelt*3*2] int32 with
+ * boundary[(k*3+j)*2+0] = neighbour id (1-based) or -1 inflow / -2 outflow / -3 wall and
+ * boundary[(k*3+j)*2+1] = inlet/outlet number (the element's own id elsewhere).
+ * area, zm, cotemin: [nelt] each; any pointer may be NULL. */
+int cf_get_mesh_tables(cf_ctx* ctx, int32_t* boundary, double* area, double* zm, double* cotemin);
+
+/* Number of elements and edges of the context; edges counts each shared edge once. */
+int cf_get_sizes(cf_ctx* ctx, int64_t* nelt, int64_t* nedge);
+
+/* The CUDA stream (cudaStream_t) the context launches on. */
+void* cf_get_stream(cf_ctx* ctx);
+
+/* Text of the last error of ctx (or of the last failed cf_create when ctx is NULL). */
+const char* cf_last_error(const cf_ctx* ctx);
+
+/* Kernel timing of the last cf_step call: total device milliseconds of the edge-flux and
+ * cell-update kernels measured with CUDA events when timing is enabled. */
+int cf_set_timing(cf_ctx* ctx, int32_t enable);
+int cf_get_timing(cf_ctx* ctx, double* flux_ms, double* update_ms, int64_t* launches);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
