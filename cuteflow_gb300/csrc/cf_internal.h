@@ -1,0 +1,149 @@
+/*
+ * cf_internal.h -- data layout shared by the host preprocessing (cf_mesh.cpp), the C ABI
+ * (cf_api.cpp) and the sm_103a kernels (cf_kernels.cu).
+ *
+ * Device layout (all arrays in space-filling-curve order, see cf_mesh.cpp):
+ *   cells  U[2]  : double4 {h, hu, hv, z} per element, ping-pong (state n in U[n & 1])
+ *          cslot : int4 {slot of local edge 0, 1, 2, -}   (local edges in the reference's order)
+ *          cstat : double4 {area, g*n*n, cfl*L_cfl, 1/area}
+ *   edges  ecell : int2 {A, B}; B >= 0 another element, B < 0 the boundary kind (-1/-2/-3)
+ *          egeo  : double4 {nx, ny, len, 1/d_AB}, normal pointing out of A
+ *          ebid  : int32 inlet/outlet number of a boundary edge
+ *          eupw  : int4 {A-side upwind 1, 2, B-side upwind 1, 2}          (second order only)
+ *          ewts  : double4 {A weights 1, 2, B weights 1, 2}              (second order only)
+ *          edk   : double2 {1/d_mkvol, 1/d_mkvoisin}                     (second order only)
+ *   slots  Slot  : 48 bytes per (edge, side): flux*len of that side's own evaluation and
+ *                  the bed-slope source of that side.  Slot 2e is side A, 2e+1 side B.
+ * Several independent simulations ("members") can share one flat cell/edge space; each
+ * member owns whole tiles of TILE_C cells and TILE_E edges so every tile belongs to one
+ * member and the per-member dt minimum is a tile reduction plus one atomic.
+ */
+#ifndef CF_INTERNAL_H
+#define CF_INTERNAL_H
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/cuteflow_gb300.h"
+
+#include <vector_types.h>
+#include <vector_functions.h>
+
+namespace cf {
+
+constexpr int TILE_E = 128;  /* edges per tile (= edge-kernel block) */
+constexpr int TILE_C = 256;  /* cells per tile (= cell-kernel block) */
+
+/* Fortran default-real literals of the reference, rounded to single precision. */
+constexpr double EPS_HLLC = (double)1e-8f;    /* flux_riemann.cuf:926 */
+constexpr double EPS_RIADH = (double)1e-6f;   /* flux_riemann.cuf:1051 */
+constexpr double EPS_SECOND = (double)1e-16f; /* flux_riemann.cuf:555, :749 */
+constexpr double EPS_VLEER = (double)1e-12f;  /* flux_riemann.cuf:454 */
+constexpr double DT_LOW = (double)1e-12f;     /* cfl_condition.cuf:129 */
+
+struct Slot {
+  double f1, f2, f3;   /* flux*len as evaluated by this side, global frame */
+  double bx, by;       /* bed-slope source of this side (source_terms.cuf:90-97) */
+  double q;            /* boundary discharge diagnostic (boundary edges, side A) */
+};
+
+/* Per-member constants. */
+struct MemberDev {
+  double gp, tolisec, tol, constant_dt, ramp_time, dt_reset;
+  double debit_end[CF_MAX_IO];
+  double debit_start[CF_MAX_IO];
+  double long_entree[CF_MAX_IO];
+  double h_sortie[CF_MAX_IO];
+  int32_t inlet, outlet, friction, fricimplic, is_dt_constant, pad_;
+  int32_t cell_begin, cell_end;   /* real elements [begin, end) of the flat space */
+  int32_t edge_begin, edge_end;   /* real edges */
+  int32_t bedge_begin, bedge_end; /* boundary edges (a sub-range of the edges) */
+};
+
+/* Per-member mutable device state.  dt[p] and t[p] belong to the step with parity p; the
+ * step with parity p folds the next dt into dt[1-p] with an ordered-integer atomicMin. */
+struct MemberState {
+  double dt[2];
+  double t[2];
+  double q_in, q_out;
+  long long nstep;   /* steps completed since the state was set; the state is in U[nstep & 1] */
+  uint32_t status;
+  int32_t pad_;
+};
+
+/* Everything a step kernel needs, passed by value. */
+struct StepArgs {
+  const double4* Uin;
+  double4* Uout;
+  const int4* cslot;
+  const double4* cstat;
+  const int2* ecell;
+  const double4* egeo;
+  const int32_t* ebid;
+  const int4* eupw;
+  const double4* ewts;
+  const double2* edk;
+  Slot* slots;
+  const int32_t* etile_mem;
+  const int32_t* ctile_mem;
+  const MemberDev* mdev;
+  MemberState* mst;
+  int32_t n_etiles, n_ctiles;
+  int32_t parity;
+  int32_t iflux, ilimiteur, flux_mode;
+};
+
+/* ---- host preprocessing (cf_mesh.cpp) ---------------------------------------------- */
+
+struct HostEdge {
+  int32_t a, b;      /* new element ids; b < 0: boundary kind */
+  int32_t ka, kb;    /* local edge index in a and b */
+  int32_t id;        /* inlet/outlet number of a boundary edge */
+};
+
+struct Prep {
+  int32_t nelt = 0, nnt = 0;
+  /* reference-order tables */
+  std::vector<int32_t> bnd;       /* nelt*3*2 (boundary(:,:,1:2)) */
+  std::vector<int32_t> nbr_k;     /* nelt*3: local edge index in the neighbour */
+  std::vector<double> area, zm, cotemin, xc, yc;
+  double long_entree[CF_MAX_IO] = {0};
+  /* renumbering */
+  std::vector<int32_t> perm;      /* new -> old */
+  std::vector<int32_t> iperm;     /* old -> new */
+  /* device tables in new order (unpadded) */
+  std::vector<HostEdge> edges;    /* interior edges, then boundary edges */
+  int32_t n_interior = 0;
+  std::vector<int4> cslot;
+  std::vector<double4> cstat;
+  std::vector<double> zcell;      /* new order */
+  std::vector<int2> ecell;
+  std::vector<double4> egeo;
+  std::vector<int32_t> ebid;
+  std::vector<int4> eupw;
+  std::vector<double4> ewts;
+  std::vector<double2> edk;
+};
+
+/* Build every host table from the reference mesh inputs.  Returns CF_OK or CF_EINVAL with a
+ * message in err. */
+int prepare_mesh(const cf_mesh* m, const cf_params* p, Prep& out, std::string& err);
+
+/* ---- kernel launchers (cf_kernels.cu) ---------------------------------------------- */
+
+typedef struct CUstream_st* stream_t;
+
+int launch_step(const StepArgs& a, stream_t s, void* ev_mid, void* ev_end);
+int launch_cfl(const double4* U, const double4* cstat, const int32_t* ctile_mem, int32_t n_ctiles,
+               const MemberDev* mdev, MemberState* mst, int32_t slot, stream_t s);
+int launch_discharge(const Slot* slots, const int2* ecell, const MemberDev* mdev, MemberState* mst,
+                     int32_t nmembers, stream_t s);
+int launch_scatter_state(const double* hu3, const int32_t* perm_new2old, const double* zcell,
+                         double4* U, int32_t n, stream_t s);
+int launch_gather_state(const double4* U, const int32_t* iperm_old2new, double* hu3, int32_t n,
+                        stream_t s);
+
+}  // namespace cf
+
+#endif

@@ -1,0 +1,194 @@
+"""Python front end of libcfgb.so (ctypes over the C ABI of include/cuteflow_gb300.h).
+
+The reference's host side is the Fortran program main.cuf / solve_finite_volumes; this module
+offers the same operations to Python tooling: build a simulation from the reference's mesh
+inputs (cf_create), set or generate the initial state (cf_set_state,
+cf_set_initial_condition), advance a number of steps entirely on the GPU (cf_step), and read
+the state back in the reference's element order (cf_get_state).
+
+There is no CPU fallback: if the CUDA library is missing or no GPU is present, the calls
+raise.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import dataclasses
+import os
+from typing import Optional
+
+import numpy as np
+
+from . import _abi
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libcfgb.so")
+
+_lib = None
+
+
+class CFError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"cuteflow_gb300 error {code}: {msg}")
+        self.code = code
+
+
+def load(build_if_missing: bool = True):
+    """Load libcfgb.so (building it in-tree first if it is absent)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH) and build_if_missing:
+        from . import build as _b
+        _b.build()
+    if not os.path.exists(LIB_PATH):
+        raise CFError(_abi.CF_EINVAL, f"{LIB_PATH} is missing: run cuteflow_gb300/build.py")
+    L = C.CDLL(LIB_PATH)
+    vp = C.c_void_p
+    dp = C.POINTER(C.c_double)
+    L.cf_default_params.argtypes = [C.POINTER(_abi.CfParams)]
+    L.cf_create.argtypes = [C.POINTER(_abi.CfMesh), C.POINTER(_abi.CfParams), C.POINTER(vp)]
+    L.cf_destroy.argtypes = [vp]
+    L.cf_destroy.restype = None
+    L.cf_set_state.argtypes = [vp, dp, C.c_double]
+    L.cf_set_state_device.argtypes = [vp, vp, C.c_double]
+    L.cf_set_initial_condition.argtypes = [vp, C.POINTER(_abi.CfIc), C.c_double]
+    L.cf_step.argtypes = [vp, C.c_int32, C.POINTER(_abi.CfStepInfo)]
+    L.cf_get_state.argtypes = [vp, dp]
+    L.cf_get_state_device.argtypes = [vp, vp]
+    L.cf_get_info.argtypes = [vp, C.POINTER(_abi.CfStepInfo)]
+    L.cf_get_mesh_tables.argtypes = [vp, C.POINTER(C.c_int32), dp, dp, dp]
+    L.cf_mesh_tables.argtypes = [C.POINTER(_abi.CfMesh), C.POINTER(_abi.CfParams), C.POINTER(C.c_int32), dp, dp, dp]
+    L.cf_get_sizes.argtypes = [vp, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
+    L.cf_get_stream.argtypes = [vp]
+    L.cf_get_stream.restype = vp
+    L.cf_last_error.argtypes = [vp]
+    L.cf_last_error.restype = C.c_char_p
+    L.cf_set_timing.argtypes = [vp, C.c_int32]
+    L.cf_get_timing.argtypes = [vp, dp, dp, C.POINTER(C.c_int64)]
+    for name in ("cf_default_params", "cf_create", "cf_set_state", "cf_set_state_device",
+                 "cf_set_initial_condition", "cf_step", "cf_get_state", "cf_get_state_device",
+                 "cf_get_info", "cf_get_mesh_tables", "cf_mesh_tables", "cf_get_sizes", "cf_set_timing", "cf_get_timing"):
+        getattr(L, name).restype = C.c_int
+    _lib = L
+    return L
+
+
+def mesh_tables(case, params: Optional[dict] = None):
+    """Host preprocessing only (no GPU): boundary table [nelt,3,2], area, zm, cotemin."""
+    L = load()
+    ma = _abi.MeshArrays(case)
+    p = _abi.make_params({**getattr(case, "params", {}), **(params or {})})
+    n = case.nelt
+    bnd = np.zeros((n, 3, 2), dtype=np.int32)
+    area, zm, cm = np.zeros(n), np.zeros(n), np.zeros(n)
+    rc = L.cf_mesh_tables(C.byref(ma.mesh), C.byref(p), _abi.iptr(bnd), _abi.dptr(area), _abi.dptr(zm), _abi.dptr(cm))
+    if rc != 0:
+        raise CFError(rc, L.cf_last_error(None).decode())
+    return bnd, area, zm, cm
+
+
+@dataclasses.dataclass
+class StepInfo:
+    t: float
+    dt_last: float
+    dt_next: float
+    q_in: float
+    q_out: float
+    steps: int
+    status: int
+
+
+def _info(s: _abi.CfStepInfo) -> StepInfo:
+    return StepInfo(s.t, s.dt_last, s.dt_next, s.q_in, s.q_out, int(s.steps), int(s.status))
+
+
+class Solver:
+    """One simulation on the current CUDA device."""
+
+    def __init__(self, case, params: Optional[dict] = None):
+        self._L = load()
+        self._ctx = C.c_void_p()
+        self._mesh = _abi.MeshArrays(case)
+        self.params = _abi.make_params({**getattr(case, "params", {}), **(params or {})})
+        rc = self._L.cf_create(C.byref(self._mesh.mesh), C.byref(self.params), C.byref(self._ctx))
+        if rc != 0:
+            raise CFError(rc, self._L.cf_last_error(None).decode())
+        self.nelt = int(self._mesh.mesh.nelt)
+        n = C.c_int64()
+        e = C.c_int64()
+        self._L.cf_get_sizes(self._ctx, C.byref(n), C.byref(e))
+        self.nedge = int(e.value)
+
+    def _check(self, rc: int):
+        if rc != 0:
+            raise CFError(rc, self._L.cf_last_error(self._ctx).decode())
+
+    def close(self):
+        if self._ctx:
+            self._L.cf_destroy(self._ctx)
+            self._ctx = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def set_state(self, U: np.ndarray, t0: float = 0.0):
+        U = np.ascontiguousarray(U, dtype=np.float64).reshape(self.nelt, 3)
+        self._check(self._L.cf_set_state(self._ctx, _abi.dptr(U), float(t0)))
+
+    def set_state_device(self, ptr: int, t0: float = 0.0):
+        """Set the state from a device pointer of 3*nelt doubles (reference order)."""
+        self._check(self._L.cf_set_state_device(self._ctx, C.c_void_p(ptr), float(t0)))
+
+    def set_initial_condition(self, ic: dict, t0: float = 0.0):
+        c = _abi.CfIc()
+        for k, v in ic.items():
+            setattr(c, k, v)
+        self._check(self._L.cf_set_initial_condition(self._ctx, C.byref(c), float(t0)))
+
+    def step(self, nsteps: int, check: bool = True) -> StepInfo:
+        info = _abi.CfStepInfo()
+        rc = self._L.cf_step(self._ctx, int(nsteps), C.byref(info))
+        if check:
+            self._check(rc)
+        return _info(info)
+
+    def info(self) -> StepInfo:
+        s = _abi.CfStepInfo()
+        self._check(self._L.cf_get_info(self._ctx, C.byref(s)))
+        return _info(s)
+
+    def get_state(self, out: Optional[np.ndarray] = None) -> np.ndarray:
+        if out is None:
+            out = np.empty((self.nelt, 3))
+        self._check(self._L.cf_get_state(self._ctx, _abi.dptr(out)))
+        return out
+
+    def get_state_device(self, ptr: int):
+        self._check(self._L.cf_get_state_device(self._ctx, C.c_void_p(ptr)))
+
+    def mesh_tables(self):
+        bnd = np.zeros((self.nelt, 3, 2), dtype=np.int32)
+        area, zm, cm = np.zeros(self.nelt), np.zeros(self.nelt), np.zeros(self.nelt)
+        self._check(self._L.cf_get_mesh_tables(self._ctx, _abi.iptr(bnd), _abi.dptr(area),
+                                               _abi.dptr(zm), _abi.dptr(cm)))
+        return bnd, area, zm, cm
+
+    def stream(self) -> int:
+        return int(self._L.cf_get_stream(self._ctx) or 0)
+
+    def set_timing(self, on: bool):
+        self._check(self._L.cf_set_timing(self._ctx, 1 if on else 0))
+
+    def timing(self):
+        f, u, n = C.c_double(), C.c_double(), C.c_int64()
+        self._check(self._L.cf_get_timing(self._ctx, C.byref(f), C.byref(u), C.byref(n)))
+        return f.value, u.value, int(n.value)

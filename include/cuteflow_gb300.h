@@ -163,6 +163,11 @@ int cf_get_info(cf_ctx* ctx, cf_step_info* info);
  * area, zm, cotemin: [nelt] each; any pointer may be NULL. */
 int cf_get_mesh_tables(cf_ctx* ctx, int32_t* boundary, double* area, double* zm, double* cotemin);
 
+/* The same tables computed from the mesh alone, without a context or a GPU (the host
+ * preprocessing of cf_create).  Lets a caller check its inputs on a machine without a GPU. */
+int cf_mesh_tables(const cf_mesh* mesh, const cf_params* params, int32_t* boundary, double* area,
+                   double* zm, double* cotemin);
+
 /* Number of elements and edges of the context; edges counts each shared edge once. */
 int cf_get_sizes(cf_ctx* ctx, int64_t* nelt, int64_t* nedge);
 

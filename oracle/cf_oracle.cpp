@@ -19,6 +19,7 @@
 #include "cf_oracle.h"
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -832,7 +833,7 @@ int orc_initial_condition(const orc_mesh* m, const orc_params* p, const orc_ic* 
 /* The time loop of solve_finite_volumes, finite_volumes_method.cuf:113-242, for nsteps. */
 int orc_run(const orc_mesh* m, const orc_params* prm, const double* U0in, double t0, int32_t nsteps,
             double* U_out, double* dt_hist, const double* dt_replay, double* t_out, double* q_out,
-            int32_t nthreads) {
+            int32_t nthreads, double* loop_seconds) {
 #ifdef _OPENMP
   int saved = omp_get_max_threads();
   if (nthreads > 0) omp_set_num_threads(nthreads);
@@ -860,6 +861,7 @@ int orc_run(const orc_mesh* m, const orc_params* prm, const double* U0in, double
   if (dt_hist) dt_hist[0] = dt;
   double t = t0, qin = 0., qout = 0.;
   int rc = 0;
+  const auto wall0 = std::chrono::steady_clock::now();
   for (int step = 0; step < nsteps; ++step) {
     C.p.dt = dt_replay ? dt_replay[step] : dt;
     C.t = t;
@@ -900,6 +902,8 @@ int orc_run(const orc_mesh* m, const orc_params* prm, const double* U0in, double
     std::swap(U0, U);
     if (!dt_replay && (dt > 9999 || dt < DT_LOW)) { rc = -2; break; }
   }
+  if (loop_seconds)
+    *loop_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - wall0).count();
   std::memcpy(U_out, U0, 3 * (size_t)n * sizeof(double));
   if (t_out) *t_out = t;
   if (q_out) { q_out[0] = qin; q_out[1] = qout; }

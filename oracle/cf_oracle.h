@@ -86,10 +86,11 @@ int orc_initial_condition(const orc_mesh* m, const orc_params* p, const orc_ic* 
  *   t_out    : time after the last step (t0 + sum of the dt used)
  *   q_out    : 2 or NULL; inflow and outflow discharge of the last step
  *   nthreads : OpenMP threads (<=0: library default)
+ *   loop_seconds: NULL or the wall time of the time loop alone (setup excluded)
  * Returns 0, or a negative code: -1 bad input, -2 dt out of the reference's sane range. */
 int orc_run(const orc_mesh* m, const orc_params* p, const double* U0, double t0, int32_t nsteps,
             double* U_out, double* dt_hist, const double* dt_replay, double* t_out, double* q_out,
-            int32_t nthreads);
+            int32_t nthreads, double* loop_seconds);
 
 /* flux*len of edge tj (0..2) of element gi (0-based) for state U (3 doubles out). */
 int orc_edge_flux(const orc_mesh* m, const orc_params* p, const double* U, double dt, double t,

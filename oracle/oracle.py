@@ -52,7 +52,7 @@ def lib():
         L.orc_run.argtypes = [C.POINTER(_abi.CfMesh), C.POINTER(_abi.CfParams), C.POINTER(C.c_double),
                               C.c_double, C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_double),
                               C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_double),
-                              C.c_int32]
+                              C.c_int32, C.POINTER(C.c_double)]
         L.orc_run.restype = C.c_int
         L.orc_max_threads.restype = C.c_int
         L.orc_all_edge_fluxes.argtypes = [C.POINTER(_abi.CfMesh), C.POINTER(_abi.CfParams),
@@ -106,11 +106,13 @@ def run(case, nsteps: int, params: dict | None = None, U0: np.ndarray | None = N
     if dt_replay is not None:
         dt_replay = np.ascontiguousarray(dt_replay, dtype=np.float64)
         rp = _abi.dptr(dt_replay)
+    loop = C.c_double(0.0)
     rc = lib().orc_run(C.byref(ma.mesh), C.byref(p), _abi.dptr(U0), float(t0), int(nsteps),
-                       _abi.dptr(U), _abi.dptr(dt_hist), rp, C.byref(t), _abi.dptr(q), int(nthreads))
+                       _abi.dptr(U), _abi.dptr(dt_hist), rp, C.byref(t), _abi.dptr(q), int(nthreads),
+                       C.byref(loop))
     if check and rc not in (0,):
         raise RuntimeError(f"orc_run failed ({rc})")
-    return dict(U=U, dt_hist=dt_hist, t=t.value, q_in=q[0], q_out=q[1], rc=rc)
+    return dict(U=U, dt_hist=dt_hist, t=t.value, q_in=q[0], q_out=q[1], rc=rc, loop_seconds=loop.value)
 
 
 def edge_fluxes(case, U: np.ndarray, dt: float, t: float = 0.0, params: dict | None = None) -> np.ndarray:
