@@ -23,7 +23,7 @@ NVCC = os.path.join(CUDA_HOME, "bin", "nvcc") if os.path.exists(os.path.join(CUD
 
 CU_SOURCES = ["cf_kernels.cu"]
 CPP_SOURCES = ["cf_mesh.cpp", "cf_api.cpp"]
-HEADERS = ["cf_internal.h"]
+HEADERS = ["cf_internal.h", "cf_flux.h"]
 
 
 def _sources():
@@ -48,7 +48,9 @@ def build(force: bool = False, verbose: bool = False) -> str:
     for s in CU_SOURCES:
         o = os.path.join(BUILD, s + ".o")
         objs.append(o)
-        jobs.append([NVCC] + ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
+        # -fmad=false: no FMA contraction, so the kernels round exactly like the reference's
+        # sequence of FP64 operations (see csrc/cf_flux.h)
+        jobs.append([NVCC] + ARCH + ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-Xcompiler", "-fPIC",
                                      "-diag-suppress", "1444", "-Xcompiler", "-Wno-deprecated-declarations",
                                      "-c", os.path.join(CSRC, s), "-o", o] + inc)
     for s in CPP_SOURCES:

@@ -1,0 +1,605 @@
+/*
+ * cf_flux.h -- per-edge and per-element arithmetic of the step, shared by the sm_103a kernels
+ * (cf_kernels.cu) and, compiled for the host, by the CPU test harness that checks it against
+ * the oracle edge by edge.  Everything here is __host__ __device__ and FP64.
+ *
+ * Bit-exact reproduction.  The reference's WAF flux is discontinuous at the bit level: where
+ * the reconstructed depths of an edge are equal to the last bit (still water),
+ * r = dupw / (dloc + eps) (flux_riemann.cuf:876-878) changes sign with the side that
+ * evaluates it, and a one-ulp change of the state moves the limiter between its branches.
+ * A result "within round-off" of the reference therefore does not stay within 1e-9 of it.
+ * This code evaluates every expression in the reference's order of operations, with true
+ * divisions, and the kernels are compiled without FMA contraction (-fmad=false), so a step
+ * on the GPU reproduces the CPU restatement of the reference bit for bit.  The second side of
+ * an edge is obtained from the first by exact IEEE identities ((-a)*b = -(a*b),
+ * (-a)-(-b) = b-a, commutativity), never by re-rounded arithmetic.
+ */
+#ifndef CF_FLUX_H
+#define CF_FLUX_H
+
+#include <cmath>
+#include <cstring>
+
+#include "cf_internal.h"
+
+#ifdef __CUDACC__
+#define CF_HD __host__ __device__
+#define CF_INLINE __forceinline__
+#else
+#define CF_HD
+#define CF_INLINE inline
+#endif
+
+namespace cf {
+
+#ifndef __CUDACC__
+using std::copysign;
+using std::fabs;
+using std::fmax;
+using std::frexp;
+using std::ldexp;
+using std::sqrt;
+#endif
+
+/* ---- loads --------------------------------------------------------------------------- */
+
+CF_HD CF_INLINE double4 ld4(const double4* p) {
+#ifdef __CUDA_ARCH__
+  const double2* q = reinterpret_cast<const double2*>(p);
+  double2 a = __ldg(q), b = __ldg(q + 1);
+  return make_double4(a.x, a.y, b.x, b.y);
+#else
+  return *p;
+#endif
+}
+
+template <class T>
+CF_HD CF_INLINE T ldro(const T* p) {
+#ifdef __CUDA_ARCH__
+  return __ldg(p);
+#else
+  return *p;
+#endif
+}
+
+CF_HD CF_INLINE bool finite_bits(double x) {
+  long long b;
+  memcpy(&b, &x, sizeof(b));
+  return (b & 0x7ff0000000000000ll) != 0x7ff0000000000000ll;
+}
+
+CF_HD CF_INLINE double dmax(double a, double b) { return (a < b) ? b : a; } /* Fortran max */
+CF_HD CF_INLINE double dmin(double a, double b) { return (b < a) ? b : a; } /* Fortran min */
+
+/* ---- x**(-1/3) -------------------------------------------------------------------------- */
+
+/* x^(1/3) for x > 0 by Halley's iteration y <- y (y^3 + 2m) / (2 y^3 + m) on the mantissa
+ * m in [0.5, 4) (exponent split off exactly by frexp/ldexp), three iterations from the
+ * linear start 0.6 + 0.25 m; within 3 ulp of the exact root.  The same fixed sequence of
+ * IEEE operations runs in the oracle, so the Manning factor h^(-1/3)
+ * (source_terms.cuf:112-127) is reproduced exactly on both sides. */
+CF_HD CF_INLINE double cbrt_halley(double x) {
+  int e;
+  double m = frexp(x, &e);
+  int r = e % 3;
+  if (r < 0) r += 3;
+  m = ldexp(m, r);
+  e -= r;
+  double y = 0.6 + 0.25 * m;
+  for (int i = 0; i < 3; ++i) {
+    const double y3 = y * y * y;
+    y = y * (y3 + 2.0 * m) / (2.0 * y3 + m);
+  }
+  return ldexp(y, e / 3);
+}
+
+/* ---- edge-frame states ------------------------------------------------------------------ */
+
+/* Masked primitive state in the frame (n, t) of an edge (flux_riemann.cuf:105-112). */
+CF_HD CF_INLINE void to_frame(double h, double hu, double hv, double nx, double ny, double tolisec,
+                              double& hm, double& un, double& ut) {
+  if (h > tolisec) {
+    un = (hu * nx + hv * ny) / h;
+    ut = (hv * nx - hu * ny) / h;
+    hm = h;
+  } else {
+    hm = 0.0;
+    un = 0.0;
+    ut = 0.0;
+  }
+}
+
+/* Wave speeds of all solvers (flux_riemann.cuf:930-983, 753-806, 1055-1108).  Returns false
+ * when both depths are below eps: the reference then reads uninitialised speeds; the flux
+ * defined for that case is zero. */
+CF_HD CF_INLINE bool wave_speeds(double g, double eps, double hl, double ul, double hr, double ur,
+                                 double& sl, double& sr, double& set) {
+  if (hl < eps && hr < eps) return false;
+  const double al = sqrt(g * hl);
+  const double ar = sqrt(g * hr);
+  const double het = (hl + hr) / 2. - (ur - ul) * (hl + hr) / (al + ar) / 4.;
+  double pql, pqr;
+  if (het < hl) pql = 1.;
+  else pql = (hl > eps) ? sqrt(0.5 * (het + hl) * het / (hl * hl)) : 0.;
+  if (het < hr) pqr = 1.;
+  else pqr = (hr > eps) ? sqrt(0.5 * (het + hr) * het / (hr * hr)) : 0.;
+  if (hl > eps) {
+    sl = ul - al * pql;
+    if (hr > eps) {
+      sr = ur + ar * pqr;
+    } else {
+      sl = ul - al;
+      sr = ul + 2 * al;
+    }
+  } else {
+    sl = ur - 2 * ar;
+    sr = ur + ar;
+  }
+  const double denom = hr * (ur - sr) - hl * (ul - sl);
+  if (fabs(denom) < eps) set = (ul + ur) / 2. - (hr - hl) * (al + ar) / (hl + hr);
+  else set = (sl * hr * (ur - sr) - sr * hl * (ul - sl)) / denom;
+  return true;
+}
+
+struct TwoFlux {
+  /* global-frame flux of side A (normal out of A) and of side B (normal out of B) */
+  double a1, a2, a3, b1, b2, b3;
+};
+
+/* Side A's global flux from the edge-frame vector x; side B's from its vector y: B's frame
+ * normal is -n and its vector is the mirror (-y1, y2, y3), which reprojects to
+ * -(n1 y2 - n2 y3), -(n2 y2 + n1 y3) exactly. */
+CF_HD CF_INLINE void reproject_both(double nx, double ny, double x1, double x2, double x3, double y1,
+                                    double y2, double y3, TwoFlux& F) {
+  F.a1 = x1;
+  F.a2 = nx * x2 - ny * x3;
+  F.a3 = ny * x2 + nx * x3;
+  F.b1 = -y1;
+  F.b2 = -(nx * y2 - ny * y3);
+  F.b3 = -(ny * y2 + nx * y3);
+}
+
+/* First-order HLLC (IFLUX 1, flux_riemann.cuf:902-1026) and the star-state HLLC of Ata et
+ * al. (IFLUX 2, :1029-1182), for both sides.  Side B's evaluation is the mirror image
+ * (h -> h, u_n -> -u_n, u_t -> -u_t, s_L -> -s_R, s_R -> -s_L, s_* -> -s_*): it selects a
+ * region with its own tests and its vector is the mirror of an A-frame vector. */
+template <int IFLUX>
+CF_HD CF_INLINE void first_order_flux(double g, double nx, double ny, double hl, double ul, double vl,
+                                      double hr, double ur, double vr, TwoFlux& F) {
+  const double eps = (IFLUX == 1) ? EPS_HLLC : EPS_RIADH;
+  double sl, sr, set;
+  if (!wave_speeds(g, eps, hl, ul, hr, ur, sl, sr, set)) {
+    F.a1 = F.a2 = F.a3 = F.b1 = F.b2 = F.b3 = 0.0;
+    return;
+  }
+  const double fl1 = hl * ul, fl2 = hl * (ul * ul) + g * hl * hl / 2.0, fl3 = hl * ul * vl;
+  const double fr1 = hr * ur, fr2 = hr * (ur * ur) + g * hr * hr / 2.0, fr3 = hr * ur * vr;
+  double x1, x2, x3, y1, y2, y3;
+  if (IFLUX == 1) {
+    /* A: sl > 0 -> FL | sr < 0 -> FR | HLL with the tangential component of the upwind side
+     * of s*.  B: -sr > 0 -> FR | -sl < 0 -> FL | HLL, tangential by -s*. */
+    const int ra = (sl > 0) ? 0 : ((sr < 0) ? 1 : 2);
+    const int rb = (-sr > 0) ? 1 : ((-sl < 0) ? 0 : 2);
+    double h1 = 0.0, h2 = 0.0;
+    if (ra == 2 || rb == 2) {
+      h1 = (sr * fl1 - sl * fr1 + sl * sr * (hr - hl)) / (sr - sl + eps);
+      h2 = (sr * fl2 - sl * fr2 + sl * sr * (hr * ur - hl * ul)) / (sr - sl + eps);
+    }
+    if (ra == 0) { x1 = fl1; x2 = fl2; x3 = fl3; }
+    else if (ra == 1) { x1 = fr1; x2 = fr2; x3 = fr3; }
+    else { x1 = h1; x2 = h2; x3 = (set > 0) ? h1 * vl : h1 * vr; }
+    if (rb == 0) { y1 = fl1; y2 = fl2; y3 = fl3; }
+    else if (rb == 1) { y1 = fr1; y2 = fr2; y3 = fr3; }
+    else { y1 = h1; y2 = h2; y3 = (-set > 0) ? h1 * vr : h1 * vl; }
+  } else {
+    const double pl = (fabs(sl - set) > eps) ? hl * (sl - ul) / (sl - set) : 0.0;
+    const double pr = (fabs(sr - set) > eps) ? hr * (sr - ur) / (sr - set) : 0.0;
+    const double el1 = fl1 + sl * (pl - hl), el2 = fl2 + sl * (pl * set - hl * ul), el3 = fl3 + sl * (pl * vl - hl * vl);
+    const double er1 = fr1 + sr * (pr - hr), er2 = fr2 + sr * (pr * set - hr * ur), er3 = fr3 + sr * (pr * vr - hr * vr);
+    /* A: 0<sl FL | 0<s* & 0>sl EL | 0>s* & 0<sr ER | FR.
+     * B (sl'=-sr, s*'=-s*, sr'=-sl): 0<-sr FR | 0<-s* & 0>-sr ER | 0>-s* & 0<-sl EL | FL. */
+    int ra, rb;
+    if (0. < sl) ra = 0;
+    else if (0. < set && 0. > sl) ra = 2;
+    else if (0. > set && 0. < sr) ra = 3;
+    else ra = 1;
+    if (0. < -sr) rb = 1;
+    else if (0. < -set && 0. > -sr) rb = 3;
+    else if (0. > -set && 0. < -sl) rb = 2;
+    else rb = 0;
+#define CF_PICK(r, a1_, a2_, a3_)                      \
+  if (r == 0) { a1_ = fl1; a2_ = fl2; a3_ = fl3; }     \
+  else if (r == 1) { a1_ = fr1; a2_ = fr2; a3_ = fr3; } \
+  else if (r == 2) { a1_ = el1; a2_ = el2; a3_ = el3; } \
+  else { a1_ = er1; a2_ = er2; a3_ = er3; }
+    CF_PICK(ra, x1, x2, x3)
+    CF_PICK(rb, y1, y2, y3)
+#undef CF_PICK
+  }
+  reproject_both(nx, ny, x1, x2, x3, y1, y2, y3, F);
+}
+
+/* WAF limiter (flux_riemann.cuf:465-524).  The superbee gaps at r = 0.5, 1, 2 are kept. */
+CF_HD CF_INLINE double waf_limiter(int ilim, double r, double c) {
+  double A = 1.;
+  if (ilim == 1) {
+    if (r <= 0) A = 1.;
+    else if (r > 0. && r < 0.5) A = 1. - 2. * (1. - fabs(c)) * r;
+    else if (r > 0.5 && r < 1.) A = fabs(c);
+    else if (r > 1. && r < 2.) A = 1. - (1. - fabs(c)) * r;
+    else A = 2. * fabs(c) - 1.;
+  } else if (ilim == 2) {
+    if (r <= 0) A = 1.;
+    else A = 1 - 2 * (1 - fabs(c)) * r / (1 + r);
+  } else if (ilim == 3) {
+    if (r <= 0) A = 1.;
+    else A = 1. - (1. - fabs(c)) * r * (1. + r) / (1. + r * r);
+  } else if (ilim == 4) {
+    if (r <= 0) A = 1.;
+    else if (r <= 1) A = 1 - (1 - fabs(c)) * r;
+    else A = fabs(c);
+  }
+  return A;
+}
+
+CF_HD CF_INLINE double sgn1(double x) { return copysign(1.0, x); }
+
+/* Second-order WAF (IFLUX 3, flux_riemann.cuf:720-900) for both sides.  Inputs: the
+ * reconstructed, masked edge-frame states of A (left) and B (right), the upwind
+ * reconstructions (h, v) of each side, dt, and the distances d_mrl, d_mkvol (A), d_mkvoisin (B). */
+CF_HD CF_INLINE void waf_flux(double g, int ilim, double nx, double ny, double dt, double d_mrl, double d_mkvol,
+                              double d_mkvoisin, double hl, double ul, double vl, double hr, double ur,
+                              double vr, double hl_upw, double vl_upw, double hr_upw, double vr_upw, TwoFlux& F) {
+  const double eps = EPS_SECOND;
+  double sl, sr, set;
+  if (!wave_speeds(g, eps, hl, ul, hr, ur, sl, sr, set)) {
+    F.a1 = F.a2 = F.a3 = F.b1 = F.b2 = F.b3 = 0.0;
+    return;
+  }
+  const double fl1 = hl * ul, fl2 = hl * (ul * ul) + g * hl * hl / 2.0;
+  const double fr1 = hr * ur, fr2 = hr * (ur * ur) + g * hr * hr / 2.0;
+  const int ra = (sl > 0) ? 0 : ((sr < 0) ? 1 : 2);
+  const int rb = (-sr > 0) ? 1 : ((-sl < 0) ? 0 : 2);
+  double h1 = 0.0, h2 = 0.0;
+  if (ra == 2 || rb == 2) {
+    h1 = (sr * fl1 - sl * fr1 + sl * sr * (hr - hl)) / (sr - sl + eps);
+    h2 = (sr * fl2 - sl * fr2 + sl * sr * (hr * ur - hl * ul)) / (sr - sl + eps);
+  }
+  const double ha1 = (ra == 0) ? fl1 : ((ra == 1) ? fr1 : h1);
+  const double ha2 = (ra == 0) ? fl2 : ((ra == 1) ? fr2 : h2);
+  const double hb1 = (rb == 0) ? fl1 : ((rb == 1) ? fr1 : h1);
+  const double hb2 = (rb == 0) ? fl2 : ((rb == 1) ? fr2 : h2);
+
+  const double dtoverdx = dt / d_mrl;
+  const double cr = sr * dtoverdx, cl = sl * dtoverdx, cet = set * dtoverdx;
+  const double dloc = (hr - hl) / d_mrl;          /* delta_loc_l = delta_loc_r */
+  const double dloc_et = (vr - vl) / d_mrl;
+  const double upl = (hl - hl_upw) / d_mkvol;     /* upwind difference of side A */
+  const double upr = (hr_upw - hr) / d_mkvoisin;  /* upwind difference of side B */
+  const double upvl = (vl - vl_upw) / d_mkvol;
+  const double upvr = (vr_upw - vr) / d_mkvoisin;
+  const double ret_a = ((set > 0) ? upvl : upvr) / (dloc_et + eps);
+
+  /* side A (:854-899) */
+  {
+    const double rl = ((sl > 0) ? upl : upr) / (dloc + eps);
+    const double rr = ((sr > 0) ? upl : upr) / (dloc + eps);
+    const double ll = waf_limiter(ilim, rl, cl);
+    const double lr = waf_limiter(ilim, rr, cr);
+    const double le = waf_limiter(ilim, ret_a, cet);
+    const double wl = (1 + sgn1(sl) * ll) / 2.;
+    const double wlet = (1 + sgn1(set) * le) / 2.;
+    const double wlr = (sgn1(sr) * lr - sgn1(sl) * ll) / 2.;
+    const double wr = (1 - sgn1(sr) * lr) / 2.;
+    const double wret = (1 - sgn1(set) * le) / 2.;
+    const double fw1 = wl * fl1 + wlr * ha1 + wr * fr1;
+    const double fw2 = wl * fl2 + wlr * ha2 + wr * fr2;
+    const double fw3 = (wlet * vl + wret * vr) * fw1;
+    F.a1 = fw1;
+    F.a2 = nx * fw2 - ny * fw3;
+    F.a3 = ny * fw2 + nx * fw3;
+  }
+  /* side B: the same formulas on the mirrored states.  Its local difference is
+   * (hl - hr)/d = -dloc, its upwind differences are minus A's (for the wave it tests), the
+   * tangential ones coincide; its Courant numbers are -cr, -cl, -cet. */
+  {
+    const double rl = ((-sr > 0) ? -upr : -upl) / (-dloc + eps);
+    const double rr = ((-sl > 0) ? -upr : -upl) / (-dloc + eps);
+    const double ret_b = ((-set > 0) ? upvr : upvl) / (dloc_et + eps);
+    const double ll = waf_limiter(ilim, rl, -cr);
+    const double lr = waf_limiter(ilim, rr, -cl);
+    const double le = waf_limiter(ilim, ret_b, -cet);
+    const double wl = (1 + sgn1(-sr) * ll) / 2.;
+    const double wlet = (1 + sgn1(-set) * le) / 2.;
+    const double wlr = (sgn1(-sl) * lr - sgn1(-sr) * ll) / 2.;
+    const double wr = (1 - sgn1(-sl) * lr) / 2.;
+    const double wret = (1 - sgn1(-set) * le) / 2.;
+    /* mirrored physical fluxes: FL' = (-fr1, fr2), FR' = (-fl1, fl2), HLL' = (-hb1, hb2) */
+    const double fw1 = -(wl * fr1 + wlr * hb1 + wr * fl1);
+    const double fw2 = wl * fr2 + wlr * hb2 + wr * fl2;
+    const double fw3 = -(wlet * vr + wret * vl) * fw1;
+    /* B's normal is -n: (fw1, -n1 fw2 + n2 fw3, -n2 fw2 - n1 fw3) */
+    F.b1 = fw1;
+    F.b2 = -nx * fw2 + ny * fw3;
+    F.b3 = -ny * fw2 - nx * fw3;
+  }
+}
+
+/* Discharge of an inlet at time t: debitglob, or a linear ramp from debitglob_start. */
+CF_HD CF_INLINE double inlet_discharge(const MemberDev& M, int id, double t) {
+  const double q1 = M.debit_end[id - 1];
+  if (M.ramp_time > 0.0 && t < M.ramp_time) {
+    const double q0 = M.debit_start[id - 1];
+    return q0 + (q1 - q0) * (t / M.ramp_time);
+  }
+  return q1;
+}
+
+/* Boundary-edge flux of side A (flux_riemann.cuf:114-171). */
+CF_HD CF_INLINE void boundary_flux(int iflux, const MemberDev& M, int kind, int id, double t, double nx,
+                                   double ny, double h, double hu, double hv, double z, double& f1,
+                                   double& f2, double& f3, double& q) {
+  const double g = M.gp, tolisec = M.tolisec;
+  double hautl, vitul, vitvl;
+  to_frame(h, hu, hv, nx, ny, tolisec, hautl, vitul, vitvl);
+  f1 = f2 = f3 = 0.0;
+  q = 0.0;
+  if (kind == -1) {
+    if (M.inlet == 1) {
+      f1 = hautl * vitul;
+      f2 = nx * (hautl * (vitul * vitul) + g * (hautl * hautl) / 2.) - ny * hautl * vitul * vitvl;
+      f3 = ny * (hautl * (vitul * vitul) + g * (hautl * hautl) / 2.) + nx * hautl * vitul * vitvl;
+    } else if (M.inlet == 2) {
+      const double debitnorm = -inlet_discharge(M, id, t) / M.long_entree[id - 1];
+      f1 = debitnorm;
+      f2 = nx * ((debitnorm * debitnorm) / (hautl + tolisec) + g * (hautl * hautl) / 2.);
+      f3 = ny * ((debitnorm * debitnorm) / (hautl + tolisec) + g * (hautl * hautl) / 2.);
+      q = -debitnorm;
+    }
+  } else if (kind == -3) {
+    f2 = nx * g * (hautl * hautl) / 2.;
+    f3 = ny * g * (hautl * hautl) / 2.;
+  } else if (kind == -2) {
+    if (M.outlet == 1) {
+      if (vitul >= 0. && vitul / sqrt(g * hautl) < 1.0) {
+        double ho = M.h_sortie[id - 1] - z;
+        ho = dmax(0.0, ho);
+        f1 = ho * vitul;
+        f2 = nx * (ho * (vitul * vitul) + g * (ho * ho) / 2.) - ny * ho * vitul * vitvl;
+        f3 = ny * (ho * (vitul * vitul) + g * (ho * ho) / 2.) + nx * ho * vitul * vitvl;
+      } else {
+        f2 = nx * g * (hautl * hautl) / 2.;
+        f3 = ny * g * (hautl * hautl) / 2.;
+      }
+      q = f1;
+    } else {
+      /* transmissive outlet: the element is its own neighbour (:169-171), raw depth on the
+       * right (:173-181); second-order schemes use first-order HLLC here (their centroid
+       * distance to themselves is zero). */
+      const double zij = dmax(z, z);
+      double hsl = dmax(0.0, hautl + z - zij);
+      double hsr = dmax(0.0, ((iflux <= 2) ? h : hautl) + z - zij);
+      double ul = vitul, vl = vitvl, ur = vitul, vr = vitvl;
+      if (hsl < tolisec) { hsl = 0.; ul = 0.; vl = 0.; }
+      if (hsr < tolisec) { hsr = 0.; ur = 0.; vr = 0.; }
+      TwoFlux F;
+      if (iflux == 2) first_order_flux<2>(g, nx, ny, hsl, ul, vl, hsr, ur, vr, F);
+      else first_order_flux<1>(g, nx, ny, hsl, ul, vl, hsr, ur, vr, F);
+      f1 = F.a1; f2 = F.a2; f3 = F.a3;
+    }
+  }
+}
+
+/* Upwind reconstruction of one side (flux_riemann.cuf:240-366): a copy of one element's
+ * masked state when d1 < 0 (one upwind element, or the first-order fallback), else the
+ * centroid-distance weighted average of two. */
+CF_HD CF_INLINE void upwind_state(const double4* U, int i1, int i2, double d1, double d2, double nx, double ny,
+                                  double tolisec, double& hu_, double& vu_, double& zu_) {
+  const double4 A1 = ld4(U + i1);
+  double h1, u1, v1;
+  to_frame(A1.x, A1.y, A1.z, nx, ny, tolisec, h1, u1, v1);
+  if (d1 < 0.0) {
+    hu_ = h1; vu_ = v1; zu_ = A1.w;
+    return;
+  }
+  const double4 A2 = ld4(U + i2);
+  double h2, u2, v2;
+  to_frame(A2.x, A2.y, A2.z, nx, ny, tolisec, h2, u2, v2);
+  hu_ = (d1 * h1 + d2 * h2) / (d1 + d2);
+  vu_ = (d1 * v1 + d2 * v2) / (d1 + d2);
+  zu_ = (d1 * A1.w + d2 * A2.w) / (d1 + d2);
+}
+
+/* ---- one edge: the body of the edge kernel ----------------------------------------------- */
+
+/* Fluxes (times the edge length) and bed sources of edge e into its two slots, from the
+ * state U of step n. */
+template <int IFLUX>
+CF_HD CF_INLINE void edge_body(const StepArgs& a, const MemberDev& M, int e, double dt, double t) {
+  const int2 ab = ldro(a.ecell + e);
+  const double4 geo = ld4(a.egeo + e);
+  const double nx = geo.x, ny = geo.y, len = geo.z;
+  const double4 UA = ld4(a.Uin + ab.x);
+  const double g = M.gp, tolisec = M.tolisec;
+  Slot* sa = a.slots + 2 * (size_t)e;
+
+  if (ab.y < 0) {
+    double f1, f2, f3, q;
+    boundary_flux(IFLUX, M, ab.y, ldro(a.ebid + e), t, nx, ny, UA.x, UA.y, UA.z, UA.w, f1, f2, f3, q);
+    sa->f1 = f1 * len;
+    sa->f2 = f2 * len;
+    sa->f3 = f3 * len;
+    sa->bx = 0.0;
+    sa->by = 0.0;
+    sa->q = q * len;
+    return;
+  }
+
+  const double4 UB = ld4(a.Uin + ab.y);
+  const double zml = UA.w, zmr = UB.w;
+  const double zij = dmax(zml, zmr);
+  double hautl, vitul, vitvl, hautr, vitur, vitvr;
+  to_frame(UA.x, UA.y, UA.z, nx, ny, tolisec, hautl, vitul, vitvl);
+  to_frame(UB.x, UB.y, UB.z, nx, ny, tolisec, hautr, vitur, vitvr);
+  TwoFlux F;
+  if (IFLUX <= 2) {
+    /* hydrostatic reconstruction (:176-181, :200-210): A from its masked depth, B from its
+     * raw depth; the raw and masked depths differ only for 0 < h <= tolisec, where side B's
+     * own evaluation (B masked, A raw) is computed separately. */
+    double hijet = dmax(0.0, hautl + zml - zij);
+    double hjiet = dmax(0.0, UB.x + zmr - zij);
+    double ul = vitul, vl = vitvl, ur = vitur, vr = vitvr;
+    if (hijet < tolisec) { hijet = 0.; ul = 0.; vl = 0.; }
+    if (hjiet < tolisec) { hjiet = 0.; ur = 0.; vr = 0.; }
+    first_order_flux<IFLUX>(g, nx, ny, hijet, ul, vl, hjiet, ur, vr, F);
+    if (hautl != UA.x || hautr != UB.x) {
+      double bl = dmax(0.0, hautr + zmr - zij), br = dmax(0.0, UA.x + zml - zij);
+      double bul = -vitur, bvl = -vitvr, bur = -vitul, bvr = -vitvl;
+      if (bl < tolisec) { bl = 0.; bul = 0.; bvl = 0.; }
+      if (br < tolisec) { br = 0.; bur = 0.; bvr = 0.; }
+      TwoFlux G;
+      first_order_flux<IFLUX>(g, -nx, -ny, bl, bul, bvl, br, bur, bvr, G);
+      F.b1 = G.a1;
+      F.b2 = G.a2;
+      F.b3 = G.a3;
+    }
+  } else {
+    const int4 up = ldro(a.eupw + e);
+    const double4 dw = ld4(a.ewts + e);   /* d1, d2 of side A, d1, d2 of side B */
+    const double2 dk = ldro(a.edk + e);   /* d_mkvol, d_mkvoisin */
+    double hl_upw, vl_upw, zml_upw, hr_upw, vr_upw, zmr_upw;
+    upwind_state(a.Uin, up.x, up.y, dw.x, dw.y, nx, ny, tolisec, hl_upw, vl_upw, zml_upw);
+    upwind_state(a.Uin, up.z, up.w, dw.z, dw.w, nx, ny, tolisec, hr_upw, vr_upw, zmr_upw);
+    /* hydrostatic reconstruction of the four states (:370-400) */
+    double hijet = dmax(0.0, hautl + zml - zij);
+    hl_upw = dmax(0.0, hl_upw + zml_upw - zij);
+    double hjiet = dmax(0.0, hautr + zmr - zij);
+    hr_upw = dmax(0.0, hr_upw + zmr_upw - zij);
+    double ul = vitul, vl = vitvl, ur = vitur, vr = vitvr;
+    if (hijet < tolisec) { hijet = 0.; ul = 0.; vl = 0.; }
+    if (hl_upw < tolisec) { hl_upw = 0.; vl_upw = 0.; }
+    if (hjiet < tolisec) { hjiet = 0.; ur = 0.; vr = 0.; }
+    if (hr_upw < tolisec) { hr_upw = 0.; vr_upw = 0.; }
+    waf_flux(g, a.ilimiteur, nx, ny, dt, geo.w, dk.x, dk.y, hijet, ul, vl, hjiet, ur, vr, hl_upw, vl_upw,
+             hr_upw, vr_upw, F);
+  }
+  if (a.flux_mode == 1) {
+    F.b1 = -F.a1;
+    F.b2 = -F.a2;
+    F.b3 = -F.a3;
+  }
+  /* bed-slope source of both sides from the raw depths (source_terms.cuf:90-97) */
+  const double ha = dmax(0.0, UA.x + zml - zij);
+  const double hb = dmax(0.0, UB.x + zmr - zij);
+  const double ta = g / 2.0 * (ha * ha - UA.x * UA.x) * len;
+  const double tb = g / 2.0 * (hb * hb - UB.x * UB.x) * len;
+  Slot* sb = sa + 1;
+  sa->f1 = F.a1 * len;
+  sa->f2 = F.a2 * len;
+  sa->f3 = F.a3 * len;
+  sa->bx = ta * nx;
+  sa->by = ta * ny;
+  sa->q = 0.0;
+  sb->f1 = F.b1 * len;
+  sb->f2 = F.b2 * len;
+  sb->f3 = F.b3 * len;
+  sb->bx = -(tb * nx);
+  sb->by = -(tb * ny);
+  sb->q = 0.0;
+}
+
+/* ---- one element: the body of the element kernel ---------------------------------------- */
+
+/* CFL time step of one element (cfl_condition.cuf:20-37); cflL = cfl * L_cfl. */
+CF_HD CF_INLINE double cfl_dt_elem(const MemberDev& M, double cflL, double h, double hu, double hv) {
+  double d = 1000000.0;
+  if (h > M.tolisec) {
+    const double vu = hu / h, vv = hv / h;
+    const double nv = sqrt(vu * vu + vv * vv);
+    const double vmax = dmax(0.01, nv + sqrt(M.gp * fabs(h)));
+    d = dmin(cflL / vmax, 1000000.0);
+  }
+  if (M.is_dt_constant == 1) d = M.constant_dt;
+  return d;
+}
+
+/* Sources, friction and update of element c (source_terms.cuf:33-211,
+ * finite_volumes_method.cuf:283-303).  st = {area, manning n, cfl*L_cfl, -}.  Returns the
+ * new state; sets *nonfinite when it is not finite. */
+CF_HD CF_INLINE double4 element_update(const MemberDev& M, const double4 U, const double4 st, const Slot& s0,
+                                       const Slot& s1, const Slot& s2, double dt, bool& nonfinite) {
+  const double gp = M.gp, tolisec = M.tolisec, tol = M.tol;
+  const double area = st.x, manning = st.y;
+  const double q1 = U.x, q2 = U.y, q3 = U.z;
+  /* fixed-order sums over the three edges (flux_riemann.cuf:411-426, source_terms.cuf:54-100) */
+  const double rc1 = s0.f1 + s1.f1 + s2.f1;
+  const double rc2 = s0.f2 + s1.f2 + s2.f2;
+  const double rc3 = s0.f3 + s1.f3 + s2.f3;
+  const double sb2 = s0.bx + s1.bx + s2.bx;
+  const double sb3 = s0.by + s1.by + s2.by;
+  double r1, r2, r3;
+  if (M.friction == 1) {
+    double sf2 = 0., sf3 = 0.;
+    double m4 = 0., m5 = 1., m6 = 0., m7 = 0., m8 = 0., m9 = 1.;
+    if (q1 > tolisec) {
+      const double vitu = q2 / q1, vitv = q3 / q1;
+      double normvit = sqrt(vitu * vitu + vitv * vitv);
+      if (normvit < tol) normvit = tol;
+      const double p13 = 1.0 / cbrt_halley(q1);    /* q1**(-1/3) */
+      sf2 = -(gp * manning * manning * vitu * normvit * area * p13);
+      sf3 = -(gp * manning * manning * vitv * normvit * area * p13);
+      if (normvit > tol) {
+        const double p43 = p13 / q1;                /* q1**(-4/3) */
+        if (M.fricimplic == 1) {
+          const double dtgn2h = dt / 2.0 * gp * manning * manning * p43;
+          const double af21 = -(7.0 / 3.0 * dtgn2h * vitu * normvit);
+          const double af22 = 1.0 + dtgn2h * (2 * (vitu * vitu) + vitv * vitv) / normvit;
+          const double af23 = dtgn2h * vitu * vitv / normvit;
+          const double af31 = -(7.0 / 3.0 * dtgn2h * vitv * normvit);
+          const double af32 = af23;
+          const double af33 = 1.0 + dtgn2h * (vitu * vitu + 2 * (vitv * vitv)) / normvit;
+          const double detaf = af22 * af33 - af23 * af32;
+          m4 = -(af21 * af33 - af23 * af31) / detaf;
+          m5 = af33 / detaf;
+          m6 = -af23 / detaf;
+          m7 = (af21 * af32 - af22 * af31) / detaf;
+          m8 = -af32 / detaf;
+          m9 = af22 / detaf;
+        } else if (M.fricimplic == 2) {
+          const double beta = -(dt * gp * manning * manning * normvit * p43);
+          const double detaf = (1 - beta) * (1 - beta);
+          m5 = (1 - beta) / detaf;
+          m9 = (1 - beta) / detaf;
+        }
+      }
+    }
+    const double ri1 = (0. + 0. - rc1) / area;
+    const double ri2 = (sb2 + sf2 - rc2) / area;
+    const double ri3 = (sb3 + sf3 - rc3) / area;
+    if (M.fricimplic == 1 || M.fricimplic == 2) {
+      r1 = 1. * ri1 + 0. * ri2 + 0. * ri3;
+      r2 = m4 * ri1 + m5 * ri2 + m6 * ri3;
+      r3 = m7 * ri1 + m8 * ri2 + m9 * ri3;
+    } else {
+      r1 = ri1;
+      r2 = ri2;
+      r3 = ri3;
+    }
+  } else {
+    r1 = (0. - rc1) / area;
+    r2 = (sb2 - rc2) / area;
+    r3 = (sb3 - rc3) / area;
+  }
+  double h = q1 + dt * r1, hu = q2 + dt * r2, hv = q3 + dt * r3;
+  nonfinite = !(finite_bits(h) && finite_bits(hu) && finite_bits(hv));
+  if (h <= tolisec) {
+    h = 0.;
+    hu = 0.;
+    hv = 0.;
+  }
+  return make_double4(h, hu, hv, U.w);
+}
+
+}  // namespace cf
+
+#endif

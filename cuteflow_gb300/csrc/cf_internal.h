@@ -5,13 +5,13 @@
  * Device layout (all arrays in space-filling-curve order, see cf_mesh.cpp):
  *   cells  U[2]  : double4 {h, hu, hv, z} per element, ping-pong (state n in U[n & 1])
  *          cslot : int4 {slot of local edge 0, 1, 2, -}   (local edges in the reference's order)
- *          cstat : double4 {area, g*n*n, cfl*L_cfl, 1/area}
+ *          cstat : double4 {area, Manning n, cfl*L_cfl, -}
  *   edges  ecell : int2 {A, B}; B >= 0 another element, B < 0 the boundary kind (-1/-2/-3)
- *          egeo  : double4 {nx, ny, len, 1/d_AB}, normal pointing out of A
+ *          egeo  : double4 {nx, ny, len, d_AB}, normal pointing out of A, centroid distance
  *          ebid  : int32 inlet/outlet number of a boundary edge
  *          eupw  : int4 {A-side upwind 1, 2, B-side upwind 1, 2}          (second order only)
- *          ewts  : double4 {A weights 1, 2, B weights 1, 2}              (second order only)
- *          edk   : double2 {1/d_mkvol, 1/d_mkvoisin}                     (second order only)
+ *          ewts  : double4 {A distances d1, d2, B distances d1, d2}; d1 < 0: copy element 1
+ *          edk   : double2 {d_mkvol, d_mkvoisin}                         (second order only)
  *   slots  Slot  : 48 bytes per (edge, side): flux*len of that side's own evaluation and
  *                  the bed-slope source of that side.  Slot 2e is side A, 2e+1 side B.
  * Several independent simulations ("members") can share one flat cell/edge space; each

@@ -247,8 +247,7 @@ int prepare_mesh(const cf_mesh* m, const cf_params* p, Prep& P, std::string& err
   for (int c = 0; c < n; ++c) {
     int o = P.perm[c];
     double man = p->is_override_manning ? p->override_manning : m->manning_elt[o];
-    double gnn = p->gp * man * man;
-    P.cstat[c] = make_double4(P.area[o], gnn, p->cfl * P.cotemin[o], 1.0 / P.area[o]);
+    P.cstat[c] = make_double4(P.area[o], man, p->cfl * P.cotemin[o], 0.0);
     P.zcell[c] = P.zm[o];
   }
   auto set_slot = [&](int c, int k, int s) {
@@ -286,46 +285,48 @@ int prepare_mesh(const cf_mesh* m, const cf_params* p, Prep& P, std::string& err
     int oa = P.perm[E.a];
     double n1, n2, ln;
     edge_normal(m, oa, E.ka, n1, n2, ln);
-    double inv_d = 0.0;
+    double inv_d = 0.0; /* d_mrl of an interior edge */
     if (E.b >= 0) {
       int ob = P.perm[E.b];
-      inv_d = 1.0 / cdist(oa, ob);
+      inv_d = cdist(oa, ob); /* d_mrl (:195) */
       P.ecell[e] = make_int2(E.a, E.b);
       P.ebid[e] = 0;
       if (second) {
+        /* upwind reconstruction of each side (flux_riemann.cuf:302-366): d1 < 0 marks a copy
+         * of one element's state (one upwind element, or the first-order fallback of
+         * :303-316 where the element itself is copied and d_mkvol = d_mrl). */
         double dmrl = cdist(oa, ob);
         int v1 = upw(oa, E.ka, 0), v2 = upw(oa, E.ka, 1);
         int w1 = upw(ob, E.kb, 0), w2 = upw(ob, E.kb, 1);
         int ua1, ua2, ub1, ub2;
-        double wa1, wa2, wb1, wb2, dka, dkb;
+        double da1, da2, db1, db2, dka, dkb;
         if ((v1 == oa && v2 == oa) || (w1 == ob && w2 == ob)) {
-          /* first-order fallback of flux_riemann.cuf:303-316 */
-          ua1 = ua2 = oa; wa1 = 1.0; wa2 = 0.0; dka = dmrl;
-          ub1 = ub2 = ob; wb1 = 1.0; wb2 = 0.0; dkb = dmrl;
+          ua1 = ua2 = oa; da1 = -1.0; da2 = 0.0; dka = dmrl;
+          ub1 = ub2 = ob; db1 = -1.0; db2 = 0.0; dkb = dmrl;
         } else {
-          if (v1 == oa) { ua1 = ua2 = v2; wa1 = 1.0; wa2 = 0.0; dka = cdist(v2, oa); }
-          else if (v2 == oa) { ua1 = ua2 = v1; wa1 = 1.0; wa2 = 0.0; dka = cdist(v1, oa); }
+          /* one upwind element: the reference reads the distance to it uninitialised on
+           * the kvol side (Q8); it is the centroid distance, as on the kvoisin side. */
+          if (v1 == oa) { ua1 = ua2 = v2; da1 = -1.0; da2 = 0.0; dka = cdist(v2, oa); }
+          else if (v2 == oa) { ua1 = ua2 = v1; da1 = -1.0; da2 = 0.0; dka = cdist(v1, oa); }
           else {
-            double d1 = cdist(v1, oa), d2 = cdist(v2, oa);
-            ua1 = v1; ua2 = v2; wa1 = d1 / (d1 + d2); wa2 = d2 / (d1 + d2); dka = (d1 + d2) / 2.;
+            ua1 = v1; ua2 = v2; da1 = cdist(v1, oa); da2 = cdist(v2, oa); dka = (da1 + da2) / 2.;
           }
-          if (w1 == ob) { ub1 = ub2 = w2; wb1 = 1.0; wb2 = 0.0; dkb = cdist(w2, ob); }
-          else if (w2 == ob) { ub1 = ub2 = w1; wb1 = 1.0; wb2 = 0.0; dkb = cdist(w1, ob); }
+          if (w1 == ob) { ub1 = ub2 = w2; db1 = -1.0; db2 = 0.0; dkb = cdist(w2, ob); }
+          else if (w2 == ob) { ub1 = ub2 = w1; db1 = -1.0; db2 = 0.0; dkb = cdist(w1, ob); }
           else {
-            double d1 = cdist(w1, ob), d2 = cdist(w2, ob);
-            ub1 = w1; ub2 = w2; wb1 = d1 / (d1 + d2); wb2 = d2 / (d1 + d2); dkb = (d1 + d2) / 2.;
+            ub1 = w1; ub2 = w2; db1 = cdist(w1, ob); db2 = cdist(w2, ob); dkb = (db1 + db2) / 2.;
           }
         }
         P.eupw[e] = make_int4(P.iperm[ua1], P.iperm[ua2], P.iperm[ub1], P.iperm[ub2]);
-        P.ewts[e] = make_double4(wa1, wa2, wb1, wb2);
-        P.edk[e] = make_double2(1.0 / dka, 1.0 / dkb);
+        P.ewts[e] = make_double4(da1, da2, db1, db2);
+        P.edk[e] = make_double2(dka, dkb);
       }
     } else {
       P.ecell[e] = make_int2(E.a, E.b);
       P.ebid[e] = E.id;
       if (second) {
         P.eupw[e] = make_int4(E.a, E.a, E.a, E.a);
-        P.ewts[e] = make_double4(1.0, 0.0, 1.0, 0.0);
+        P.ewts[e] = make_double4(-1.0, 0.0, -1.0, 0.0);
         P.edk[e] = make_double2(0.0, 0.0);
       }
     }

@@ -196,6 +196,29 @@ bool do_setup(Setup& S, const orc_mesh* m) {
   return true;
 }
 
+/* ---- x**(-1/3) ------------------------------------------------------------------------- */
+
+/* The reference raises the depth to -1/3 and -4/3 with the compiler's pow
+ * (source_terms.cuf:112,119-120,127).  pow is not correctly rounded and differs between math
+ * libraries, so the restatement fixes one evaluation: x^(1/3) by Halley's iteration
+ * y <- y (y^3 + 2m) / (2 y^3 + m) on the mantissa m in [0.5, 4) (exponent split off exactly),
+ * three iterations from 0.6 + 0.25 m, within 3 ulp of the root; then q^(-1/3) = 1/cbrt(q)
+ * and q^(-4/3) = q^(-1/3)/q. */
+double cbrt_halley(double x) {
+  int e;
+  double m = std::frexp(x, &e);
+  int r = e % 3;
+  if (r < 0) r += 3;
+  m = std::ldexp(m, r);
+  e -= r;
+  double y = 0.6 + 0.25 * m;
+  for (int i = 0; i < 3; ++i) {
+    const double y3 = y * y * y;
+    y = y * (y3 + 2.0 * m) / (2.0 * y3 + m);
+  }
+  return std::ldexp(y, e / 3);
+}
+
 /* ---- Riemann solvers ---------------------------------------------------------------- */
 
 struct P {
@@ -668,12 +691,13 @@ void cell_update(const Ctx& C, const double* U0, const double* resc, int gi, dou
       vitv = q3 / q1;
       normvit = std::sqrt(vitu * vitu + vitv * vitv);
       if (normvit < tol) normvit = tol;
-      sf[1] = -(gp * manning * manning * vitu * normvit * area * std::pow(q1, -1.0 / 3.0));
-      sf[2] = -(gp * manning * manning * vitv * normvit * area * std::pow(q1, -1.0 / 3.0));
+      const double p13 = 1.0 / cbrt_halley(q1); /* q1**(-1/3) */
+      sf[1] = -(gp * manning * manning * vitu * normvit * area * p13);
+      sf[2] = -(gp * manning * manning * vitv * normvit * area * p13);
     }
     if (prm->fricimplic == 1) {
       if (normvit > tol && q1 > tolisec) {
-        double dtgn2h = dt / 2.0 * gp * manning * manning * std::pow(q1, -4.0 / 3.0);
+        double dtgn2h = dt / 2.0 * gp * manning * manning * (1.0 / cbrt_halley(q1) / q1);
         double af21 = -(7.0 / 3.0 * dtgn2h * vitu * normvit);
         double af22 = 1.0 + dtgn2h * (2 * (vitu * vitu) + vitv * vitv) / normvit;
         double af23 = dtgn2h * vitu * vitv / normvit;
@@ -691,7 +715,7 @@ void cell_update(const Ctx& C, const double* U0, const double* resc, int gi, dou
       }
     } else if (prm->fricimplic == 2) {
       if (normvit > tol && q1 > tolisec) {
-        double beta = -(dt * gp * manning * manning * normvit * std::pow(q1, -4.0 / 3.0));
+        double beta = -(dt * gp * manning * manning * normvit * (1.0 / cbrt_halley(q1) / q1));
         double detaf = (1 - beta) * (1 - beta);
         afm1[4] = (1 - beta) / detaf;
         afm1[8] = (1 - beta) / detaf;

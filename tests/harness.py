@@ -1,0 +1,65 @@
+"""Builds and loads tests/flux_harness.cpp (the GPU step's flux mathematics compiled for the
+CPU).  Test infrastructure only."""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+LIB = os.path.join(HERE, "_build", "libflux_harness.so")
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is not None:
+        return _lib
+    srcs = [os.path.join(HERE, "flux_harness.cpp"), os.path.join(ROOT, "cuteflow_gb300", "csrc", "cf_mesh.cpp")]
+    deps = srcs + [os.path.join(ROOT, "cuteflow_gb300", "csrc", f) for f in ("cf_flux.h", "cf_internal.h")]
+    if not os.path.exists(LIB) or any(os.path.getmtime(d) > os.path.getmtime(LIB) for d in deps):
+        os.makedirs(os.path.dirname(LIB), exist_ok=True)
+        cuda_inc = os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "include")
+        subprocess.run(["g++", "-std=c++17", "-O2", "-fPIC", "-shared", "-ffp-contract=off",
+                        "-Wno-deprecated-declarations", "-I", cuda_inc, "-I", os.path.join(ROOT, "include"),
+                        "-o", LIB] + srcs, check=True)
+    from cuteflow_gb300 import _abi
+    L = C.CDLL(LIB)
+    dp = C.POINTER(C.c_double)
+    L.harness_edge_fluxes.argtypes = [C.POINTER(_abi.CfMesh), C.POINTER(_abi.CfParams), dp, C.c_double,
+                                      C.c_double, dp, dp]
+    L.harness_edge_fluxes.restype = C.c_int
+    _lib = L
+    return L
+
+
+def edge_fluxes(case, U, dt, t=0.0, params=None):
+    from cuteflow_gb300 import _abi
+    ma = _abi.MeshArrays(case)
+    p = _abi.make_params({**case.params, **(params or {})})
+    U = np.ascontiguousarray(U, dtype=np.float64)
+    out = np.zeros((case.nelt, 3, 3))
+    bed = np.zeros((case.nelt, 3, 2))
+    rc = lib().harness_edge_fluxes(C.byref(ma.mesh), C.byref(p), _abi.dptr(U), float(dt), float(t),
+                                   _abi.dptr(out), _abi.dptr(bed))
+    assert rc == 0
+    return out, bed
+
+
+def run(case, nsteps, params=None, U0=None):
+    from cuteflow_gb300 import _abi
+    L = lib()
+    if not hasattr(L, "_run_typed"):
+        dp = C.POINTER(C.c_double)
+        L.harness_run.argtypes = [C.POINTER(_abi.CfMesh), C.POINTER(_abi.CfParams), dp, C.c_int, dp, dp, dp]
+        L.harness_run.restype = C.c_int
+        L._run_typed = True
+    ma = _abi.MeshArrays(case)
+    p = _abi.make_params({**case.params, **(params or {})})
+    U0 = np.ascontiguousarray(case.U0 if U0 is None else U0, dtype=np.float64)
+    U = np.zeros_like(U0)
+    dth = np.zeros(nsteps + 1)
+    t = C.c_double(0.0)
+    rc = L.harness_run(C.byref(ma.mesh), C.byref(p), _abi.dptr(U0), int(nsteps), _abi.dptr(U), _abi.dptr(dth), C.byref(t))
+    return dict(U=U, dt_hist=dth, t=t.value, rc=rc)

@@ -1,0 +1,65 @@
+"""The GPU step's arithmetic (cuteflow_gb300/csrc/cf_flux.h, compiled here for the CPU
+without FMA contraction, as the kernels are compiled with -fmad=false) against the oracle:
+every (element, edge) flux and every full run must agree bit for bit."""
+import numpy as np
+import pytest
+
+import harness as H
+from cuteflow_gb300 import cases
+
+
+def _state_after(oracle, case, n, params=None):
+    r = oracle.run(case, n, params=params)
+    return r["U"], r["dt_hist"][-1], r["t"]
+
+
+@pytest.mark.parametrize("iflux", [1, 2, 3])
+@pytest.mark.parametrize("flux_mode", [0, 1])
+def test_edge_fluxes_bitwise(oracle, iflux, flux_mode):
+    c = cases.flooding(60, 30, seed=4, iflux=iflux)
+    prm = dict(flux_mode=flux_mode)
+    for n in (0, 25):
+        U, dt, t = _state_after(oracle, c, n, prm) if n else (c.U0, 0.3, 0.0)
+        fo = oracle.edge_fluxes(c, U, dt, t, params=prm)
+        fh, _ = H.edge_fluxes(c, U, dt, t, params=prm)
+        if flux_mode == 0:
+            assert np.array_equal(fo, fh)
+        else:
+            # conservative mode: the element with the smaller index evaluates, the other negates
+            bnd = oracle.setup(c)[0]
+            own = (bnd[:, :, 0] <= 0) | (bnd[:, :, 0] - 1 > np.arange(c.nelt)[:, None])
+            assert np.array_equal(fo[own], fh[own])
+
+
+CASES = [
+    ("dam_hllc", lambda: cases.circular_dam_break(30, 30, seed=3, iflux=1), 150, {}),
+    ("dam_riadh", lambda: cases.circular_dam_break(30, 30, seed=3, iflux=2), 150, {}),
+    ("dam_waf", lambda: cases.circular_dam_break(30, 30, seed=3, iflux=3), 150, {}),
+    ("flood_hllc", lambda: cases.flooding(60, 30, seed=4, iflux=1), 200, {}),
+    ("flood_riadh", lambda: cases.flooding(60, 30, seed=4, iflux=2), 200, {}),
+    ("flood_waf", lambda: cases.flooding(60, 30, seed=4, iflux=3), 200, {}),
+    ("flood_waf_conservative", lambda: cases.flooding(40, 20, seed=7, iflux=3), 150, dict(flux_mode=1)),
+    ("waf_lim0", lambda: cases.flooding(40, 20, seed=6, iflux=3), 150, dict(ilimiteur=0)),
+    ("waf_lim2", lambda: cases.flooding(40, 20, seed=6, iflux=3), 150, dict(ilimiteur=2)),
+    ("waf_lim3", lambda: cases.flooding(40, 20, seed=6, iflux=3), 150, dict(ilimiteur=3)),
+    ("waf_lim4", lambda: cases.flooding(40, 20, seed=6, iflux=3), 150, dict(ilimiteur=4)),
+    ("fric_explicit", lambda: cases.flooding(40, 20, seed=8, iflux=1), 120, dict(fricimplic=0)),
+    ("fric_diag", lambda: cases.flooding(40, 20, seed=8, iflux=1), 120, dict(fricimplic=2)),
+    ("no_friction", lambda: cases.flooding(40, 20, seed=8, iflux=3), 120, dict(friction=0)),
+    ("inlet_transm_outlet_transm", lambda: cases.flooding(40, 20, seed=9, iflux=1), 120, dict(inlet=1, outlet=2)),
+    ("outlet_transm_waf", lambda: cases.flooding(40, 20, seed=9, iflux=3), 120, dict(outlet=2)),
+    ("constant_dt", lambda: cases.circular_dam_break(20, 20, seed=2, iflux=1), 60, dict(is_dt_constant=1, constant_dt=0.01)),
+    ("lake_wet", lambda: cases.lake_at_rest(30, 15, iflux=3), 100, {}),
+    ("lake_islands", lambda: cases.lake_at_rest(30, 15, iflux=3, wet=False), 100, {}),
+]
+
+
+@pytest.mark.parametrize("name,make,n,prm", CASES, ids=[c[0] for c in CASES])
+def test_full_run_bitwise(oracle, name, make, n, prm):
+    c = make()
+    r1 = oracle.run(c, n, params=prm, check=False)
+    r2 = H.run(c, n, params=prm)
+    assert r1["rc"] == r2["rc"]
+    assert np.array_equal(r1["dt_hist"], r2["dt_hist"])
+    assert np.array_equal(r1["U"], r2["U"])
+    assert r1["t"] == r2["t"]

@@ -1,88 +1,152 @@
-"""GPU step against the CPU oracle on the same seeded inputs (called through the C ABI).
+"""GPU step against the CPU oracle on the same seeded inputs, through the C ABI.
 
-Tolerance: the benchmark spec's bound, max |h - h_oracle| <= 1e-9 m and |hu|, |hv| <= 1e-9 m^2/s
-after the stated step count; the time after the steps must agree to 1e-12 relative.
+The bar stated for this path is max |h - h_ref| <= 1e-9 m and |hu|, |hv| <= 1e-9 m^2/s after
+the stated step count.  The kernels evaluate the reference's operations in its order without
+FMA contraction, so the tests require more: the GPU state, every dt and the time must equal
+the oracle's bit for bit (TOL is only reported in the failure message).
 """
 import numpy as np
 import pytest
 
-from cuteflow_gb300 import cases
+from cuteflow_gb300 import _abi, cases
 
 pytestmark = pytest.mark.gpu
 
 TOL = 1e-9
 
 
-def run_gpu(case, nsteps, params=None, U0=None, chunks=1):
+def run_gpu(case, nsteps, params=None, U0=None, chunks=(None,)):
     from cuteflow_gb300 import Solver
     with Solver(case, params) as s:
         s.set_state(case.U0 if U0 is None else U0)
-        per = nsteps // chunks
         info = None
         done = 0
+        sizes = [c for c in chunks if c] or [nsteps]
+        i = 0
         while done < nsteps:
-            k = min(per, nsteps - done)
-            info = s.step(k)
+            k = min(sizes[i % len(sizes)], nsteps - done)
+            info = s.step(k, check=False)
             done += k
+            i += 1
         return s.get_state(), info
 
 
-def compare(case, nsteps, oracle, params=None, tol=TOL, chunks=1):
+def compare_bitwise(case, nsteps, oracle, params=None, chunks=(None,)):
     U, info = run_gpu(case, nsteps, params, chunks=chunks)
-    ref = oracle.run(case, nsteps, params=params)
+    ref = oracle.run(case, nsteps, params=params, check=False)
     d = np.abs(U - ref["U"]).max(axis=0)
-    assert info.steps == nsteps
-    assert abs(info.t - ref["t"]) <= 1e-12 * max(1.0, abs(ref["t"])), (info.t, ref["t"])
-    assert d[0] <= tol and d[1] <= tol and d[2] <= tol, (case.name, d)
+    assert info.steps == nsteps or ref["rc"] != 0
+    assert np.array_equal(U, ref["U"]), f"{case.name}: max|dU| = {d} (bar {TOL})"
+    assert info.t == ref["t"], (info.t, ref["t"])
+    assert info.dt_next == ref["dt_hist"][info.steps]
     return U, ref, info
 
 
-@pytest.mark.parametrize("iflux", [1, 2])
-def test_first_order_dam_break(gpu_lib, oracle, iflux):
-    c = cases.circular_dam_break(40, 40, seed=3, iflux=iflux)
-    compare(c, 200, oracle)
+@pytest.mark.parametrize("iflux", [1, 2, 3])
+def test_dam_break(gpu_lib, oracle, iflux):
+    compare_bitwise(cases.circular_dam_break(40, 40, seed=3, iflux=iflux), 200, oracle)
 
 
 @pytest.mark.parametrize("iflux", [1, 2, 3])
 def test_flooding_wet_dry(gpu_lib, oracle, iflux):
-    c = cases.flooding(80, 40, seed=4, iflux=iflux)
-    compare(c, 300, oracle, chunks=3)
+    compare_bitwise(cases.flooding(80, 40, seed=4, iflux=iflux), 300, oracle, chunks=(7, 100, 1, 50))
 
 
 @pytest.mark.parametrize("ilim", [0, 1, 2, 3, 4])
 def test_waf_limiters(gpu_lib, oracle, ilim):
-    c = cases.flooding(60, 30, seed=6, iflux=3)
-    compare(c, 200, oracle, params=dict(ilimiteur=ilim))
+    compare_bitwise(cases.flooding(60, 30, seed=6, iflux=3), 200, oracle, params=dict(ilimiteur=ilim))
 
 
 @pytest.mark.parametrize("iflux", [1, 3])
 def test_conservative_mode(gpu_lib, oracle, iflux):
-    c = cases.flooding(60, 30, seed=7, iflux=iflux)
-    compare(c, 200, oracle, params=dict(flux_mode=1))
+    compare_bitwise(cases.flooding(60, 30, seed=7, iflux=iflux), 200, oracle, params=dict(flux_mode=1))
 
 
-@pytest.mark.parametrize("fricimplic", [0, 1, 2])
-def test_friction_modes(gpu_lib, oracle, fricimplic):
-    c = cases.flooding(50, 25, seed=8, iflux=1)
-    compare(c, 150, oracle, params=dict(fricimplic=fricimplic))
+@pytest.mark.parametrize("prm", [dict(fricimplic=2), dict(friction=0), dict(inlet=1, outlet=2),
+                                 dict(outlet=2), dict(is_dt_constant=1, constant_dt=0.05)],
+                         ids=["fric_diag", "no_friction", "transm_in_out", "transm_out", "constant_dt"])
+def test_options(gpu_lib, oracle, prm):
+    compare_bitwise(cases.flooding(50, 25, seed=8, iflux=3), 150, oracle, params=prm)
+
+
+def test_explicit_friction_stops_like_the_reference(gpu_lib, oracle):
+    """Explicit friction (fricimplic=0) is unstable on this case: dt leaves the reference's
+    sane range (cfl_condition.cuf:129-132).  Both stop at the same step with the same state."""
+    from cuteflow_gb300 import Solver
+    c = cases.flooding(40, 20, seed=8, iflux=1)
+    ref = oracle.run(c, 120, params=dict(fricimplic=0), check=False)
+    assert ref["rc"] == -2
+    with Solver(c, dict(fricimplic=0)) as s:
+        s.set_state(c.U0)
+        info = s.step(120, check=False)
+        assert info.status & _abi.CF_STATUS_DT_RANGE
+        U = s.get_state()
+        with pytest.raises(Exception):
+            s.step(1)
+    assert np.array_equal(U, ref["U"])
+    assert info.t == ref["t"]
 
 
 def test_lake_at_rest(gpu_lib, oracle):
     c = cases.lake_at_rest(40, 20, iflux=3)
-    U, ref, info = compare(c, 200, oracle)
-    from oracle import oracle as O
-    zm = O.setup(c)[2]
-    eta = U[:, 0] + zm
-    assert np.ptp(eta) < 1e-12
+    U, ref, info = compare_bitwise(c, 200, oracle)
+    zm = oracle.setup(c)[2]
+    eta0 = c.U0[:, 0] + zm
+    assert np.abs(U[:, 0] + zm - eta0).max() < 1e-12
     assert np.abs(U[:, 1:]).max() < 1e-12
 
 
+def test_state_round_trip_and_reordering(gpu_lib):
+    """cf_set_state / cf_get_state keep the reference's element order through the internal
+    space-filling-curve renumbering, with and without renumbering."""
+    from cuteflow_gb300 import Solver
+    c = cases.flooding(30, 15, seed=1, iflux=1)
+    U = np.random.default_rng(0).uniform(0.1, 2.0, (c.nelt, 3))
+    for reorder in (1, 0):
+        with Solver(c, dict(reorder=reorder)) as s:
+            s.set_state(U, t0=3.5)
+            assert np.array_equal(s.get_state(), U)
+            assert s.info().t == 3.5
+    a, _ = run_gpu(c, 50, dict(reorder=1))
+    b, _ = run_gpu(c, 50, dict(reorder=0))
+    assert np.array_equal(a, b)
+
+
+def test_initial_condition_matches_oracle(gpu_lib, oracle):
+    from cuteflow_gb300 import Solver
+    c = cases.flooding(40, 20, seed=2, iflux=1)
+    for ic in (dict(eqlin_barrage=1, x1eqbar=500.001, x2eqbar=500.0, y1eqbar=0.0, y2eqbar=1000.0,
+                    h_amont=3.0, u_amont=0.5, v_amont=0.1, h_aval=1.0),
+               dict(plan=1, xplan=0.0, yplan=0.0, zplan=1.0, xpoint=0.0, ypoint=0.0, zpoint=1.5, u_aval=0.2)):
+        ref = oracle.initial_condition(c, ic)
+        with Solver(c) as s:
+            s.set_initial_condition(ic)
+            assert np.array_equal(s.get_state(), ref)
+
+
+def test_deterministic_and_graph_equals_single_steps(gpu_lib):
+    c = cases.flooding(60, 30, seed=5, iflux=3)
+    a, ia = run_gpu(c, 120)                    # graph replay of step pairs
+    b, ib = run_gpu(c, 120, chunks=(1,))       # one launch pair per call
+    c2, _ = run_gpu(c, 120)
+    assert np.array_equal(a, b) and np.array_equal(a, c2) and ia.t == ib.t
+
+
+def test_discharge_diagnostics(gpu_lib, oracle):
+    c = cases.flooding(60, 30, seed=4, iflux=3)
+    U, info = run_gpu(c, 40)
+    ref = oracle.run(c, 40)
+    assert info.q_in == pytest.approx(ref["q_in"], rel=1e-12)
+    assert info.q_out == pytest.approx(ref["q_out"], rel=1e-12, abs=1e-12)
+    t_ramp = ref["t"] - ref["dt_hist"][39]  # time at the start of the last step
+    assert info.q_in == pytest.approx(1000.0 * (2.0 + 8.0 * t_ramp / 600.0), rel=1e-9)
+
+
 def test_config1_circular_dam_break_full(gpu_lib, oracle):
-    """80,000 triangles, HLLC, 500 steps (the CPU-runnable benchmark case)."""
+    """The CPU-runnable benchmark case: 80,000 triangles, HLLC, CFL 0.9, 500 steps."""
     c = cases.circular_dam_break(200, 200, seed=1, iflux=1)
-    U, ref, info = compare(c, 500, oracle)
-    from oracle import oracle as O
-    area = O.setup(c)[1]
+    U, ref, info = compare_bitwise(c, 500, oracle)
+    area = oracle.setup(c)[1]
     m0 = float((c.U0[:, 0] * area).sum())
     m1 = float((U[:, 0] * area).sum())
     assert abs(m1 - m0) <= 1e-12 * m0
