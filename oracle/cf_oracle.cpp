@@ -4,11 +4,14 @@
  * TEST INFRASTRUCTURE ONLY: the correctness checker and the timed CPU baseline of the GPU
  * step in cuteflow_gb300/.  Nothing in the product links, calls or falls back to it.
  *
- * Parity status: the reference ships no loadable golden vectors for this path (its meshes
- * and saved solutions are Git LFS stubs) and it cannot be built here (CUDA Fortran + MPI +
- * libcgns).  The restatement is pinned by (a) the boundary table the reference itself wrote
- * for the Divergent_Canal calibration mesh (tests/golden/), and (b) known-answer properties:
- * lake at rest, mass conservation with walls, mirror symmetry, and the 1-D dam break.
+ * Parity status: pinned against outputs of the reference itself.  Its meshes for the test
+ * cases are Git LFS stubs and it cannot be built here (CUDA Fortran + MPI + libcgns), but its
+ * calibration folders ship two real CGNS meshes, the boundary tables CuteFlow wrote for them,
+ * and the logs of three runs on a Tesla P100 (tests/golden/make_golden.py).  This restatement
+ * reproduces both boundary tables exactly and the logged outflow discharge of all three runs
+ * to the printed 16 digits at every 1000-step checkpoint (up to 30,000 steps checked).  It is
+ * further checked by known-answer properties: lake at rest, mass conservation with walls,
+ * mirror symmetry, and the 1-D dam break.
  *
  * Every routine below follows the reference file:line it cites, in the reference's own
  * order of floating-point operations (compile with -ffp-contract=off).  Fortran default-real

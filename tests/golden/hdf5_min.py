@@ -8,6 +8,7 @@ Format facts follow the public HDF5 File Format Specification (version 3.0).
 from __future__ import annotations
 
 import struct
+import zlib
 
 import numpy as np
 
@@ -116,8 +117,44 @@ class H5:
                 res[name] = raw[:size]
         return res
 
+    def _chunks(self, addr: int, rank: int, out: list):
+        """Walk a version-1 B-tree of raw-data chunks (node type 1)."""
+        b = self.b
+        if b[addr:addr + 4] != b"TREE":
+            raise ValueError("bad chunk B-tree")
+        level = b[addr + 5]
+        used = self._u(addr + 6, 2)
+        p = addr + 8 + 2 * self.so
+        keysize = 8 + 8 * (rank + 1)
+        for i in range(used):
+            csize = self._u(p, 4)
+            fmask = self._u(p + 4, 4)
+            offs = [self._u(p + 8 + 8 * k, 8) for k in range(rank)]
+            child = self._u(p + keysize, self.so)
+            if level == 0:
+                out.append((offs, child, csize, fmask))
+            else:
+                self._chunks(child, rank, out)
+            p += keysize + self.so
+
     def dataset(self, addr: int) -> np.ndarray:
         dims, dtype, layout = None, None, None
+        filters = []
+        for t, d in self.messages(addr):
+            if t == 0x0B:
+                ver, nf = d[0], d[1]
+                p = 8 if ver == 1 else 2
+                for _ in range(nf):
+                    fid = struct.unpack_from("<H", d, p)[0]
+                    if ver == 1 or fid >= 256:
+                        nlen = struct.unpack_from("<H", d, p + 2)[0]
+                        p += 2
+                    else:
+                        nlen = 0
+                    nvals = struct.unpack_from("<H", d, p + 4)[0]
+                    p += 6 + ((nlen + 7) // 8 * 8 if ver == 1 else nlen)
+                    p += 4 * nvals + (4 if (ver == 1 and nvals % 2) else 0)
+                    filters.append(fid)
         for t, d in self.messages(addr):
             if t == 0x01:
                 ver, rank, flags = d[0], d[1], d[2]
@@ -147,9 +184,35 @@ class H5:
                     a = int.from_bytes(d[2:2 + self.so], "little")
                     n = int.from_bytes(d[2 + self.so:2 + self.so + self.sl], "little")
                     layout = ("raw", self.b[a:a + n])
+                elif cls == 2:
+                    rank = d[2] - 1
+                    baddr = int.from_bytes(d[3:3 + self.so], "little")
+                    cdims = [struct.unpack_from("<I", d, 3 + self.so + 4 * k)[0] for k in range(rank)]
+                    layout = ("chunked", baddr, cdims)
                 else:
-                    raise ValueError("chunked datasets not supported")
+                    raise ValueError("virtual datasets not supported")
         count = int(np.prod(dims)) if dims else 1
+        if layout[0] == "chunked":
+            _, baddr, cdims = layout
+            full = np.zeros(dims, dtype=dtype)
+            chunks = []
+            self._chunks(baddr, len(dims), chunks)
+            for offs, caddr, csize, fmask in chunks:
+                raw = self.b[caddr:caddr + csize]
+                for k, fid in reversed(list(enumerate(filters))):
+                    if fmask & (1 << k):
+                        continue
+                    if fid == 1:
+                        raw = zlib.decompress(raw)
+                    elif fid == 2:
+                        n = len(raw) // dtype.itemsize
+                        raw = np.frombuffer(raw, np.uint8).reshape(dtype.itemsize, n).T.tobytes()
+                    else:
+                        raise ValueError(f"filter {fid} not supported")
+                blk = np.frombuffer(raw, dtype=dtype, count=int(np.prod(cdims))).reshape(cdims)
+                sl = tuple(slice(o, min(o + c, n)) for o, c, n in zip(offs, cdims, dims))
+                full[sl] = blk[tuple(slice(0, s.stop - s.start) for s in sl)]
+            return full
         arr = np.frombuffer(layout[1], dtype=dtype, count=count)
         # HDF5 stores C order; CGNS writes Fortran arrays with reversed dimensions
         return arr.reshape(dims) if dims else arr
