@@ -158,6 +158,47 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def ensemble(nmembers: int, steps: int, warmup: int, seed: int = 3):
+    """Batched ensemble vs the same members run one after another through the plain API.
+
+    Members come from the circular-dam-break generator with seeded sizes (20k-500k triangles,
+    skewed to small members), their own lognormal Manning field and inflow peak, WAF.  Both
+    forms give bit-identical states, so the comparison is at the same tolerance.  Setup (mesh
+    preprocessing, uploads) is excluded from both timings."""
+    import torch
+    from cuteflow_gb300 import Batch, Solver, cases
+    members = [cases.ensemble_member(i, seed=seed) for i in range(nmembers)]
+    tri = sum(m.nelt for m in members)
+    b = Batch(members)
+    for i, m in enumerate(members):
+        b.set_state(i, m.U0)
+    b.step(warmup)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    infos = b.step(steps)
+    torch.cuda.synchronize()
+    t_batch = time.perf_counter() - t0
+    b.close()
+    del b
+    t_seq = 0.0
+    for m in members:
+        s = Solver(m)
+        s.set_state(m.U0)
+        s.step(warmup)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        s.step(steps)
+        torch.cuda.synchronize()
+        t_seq += time.perf_counter() - t0
+        s.close()
+    sizes = sorted(m.nelt for m in members)
+    return {"members": nmembers, "steps_each": steps, "triangles_total": tri,
+            "triangles_min_median_max": [sizes[0], sizes[len(sizes) // 2], sizes[-1]],
+            "batched_value": tri * steps / t_batch, "sequential_value": tri * steps / t_seq,
+            "unit": UNIT, "speedup_vs_sequential": t_seq / t_batch,
+            "batched_s": t_batch, "sequential_s": t_seq, "stopped_members": sum(1 for i in infos if i.status)}
+
+
 def run_ours(args):
     import torch
     world, rank, local = dist_env()
@@ -263,6 +304,10 @@ def run_ours(args):
         "gpu_launches": 2 * args.steps + 1,
         "clocks": clk.summary(),
     }
+    if rank == 0 and args.batched_members > 0:
+        line["batched"] = ensemble(args.batched_members, args.batched_steps, 3)
+        line["batched"]["note"] = ("sample of the 256-member, 2000-step ensemble workload; run "
+                                   "`bench.py --config ensemble` for the full size")
     if rank == 0 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(case)
     s.close()
@@ -278,11 +323,24 @@ def main():
     ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="flooding", choices=["flooding", "dam_break"])
+    ap.add_argument("--config", default="flooding", choices=["flooding", "dam_break", "ensemble"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--batched-members", type=int, default=32, help="ensemble sample beside the plain line (0: skip)")
+    ap.add_argument("--batched-steps", type=int, default=200)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    if args.config == "ensemble":
+        import torch
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        from cuteflow_gb300 import build
+        build.build()
+        r = ensemble(args.batched_members if args.batched_members > 32 else 256, args.steps, args.warmup)
+        print(json.dumps({"metric": "batched ensemble: " + METRIC, "value": r["batched_value"], "unit": UNIT,
+                          "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+                          "dtype": "f64", "data": "synthetic", "config": {"workload": "ensemble_256_waf"},
+                          "batched": r}), flush=True)
+        return
     if args.impl == "reference":
         run_reference(args)
     else:

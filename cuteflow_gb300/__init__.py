@@ -4,4 +4,4 @@
 ``cases`` builds seeded synthetic inputs in the reference's mesh-table format.
 """
 from . import _abi, cases  # noqa: F401
-from .solver import CFError, Solver, StepInfo, load  # noqa: F401
+from .solver import Batch, CFError, Solver, StepInfo, load  # noqa: F401

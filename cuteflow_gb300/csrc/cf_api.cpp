@@ -1,40 +1,60 @@
 /*
  * cf_api.cpp -- the C ABI of include/cuteflow_gb300.h.
  *
- * A context holds one simulation (one "member" of the flat cell/edge space the kernels work
- * on), its device tables, the ping-pong state buffers and one CUDA stream.  Stepping never
- * returns to the host between steps: the next dt is produced on the device by the element
- * kernel and read by the next edge kernel.  The host only reads the small per-member state
- * record at the end of a cf_step call.  Runs of steps are replayed from a captured CUDA
- * graph of two steps (even and odd parity).
+ * A context holds one or more independent simulations ("members") packed into one flat
+ * element/edge space: member m owns the elements [cell_off, cell_off + n) and the edges
+ * [edge_off, edge_off + ne), both padded to whole tiles (TILE_C elements, TILE_E edges), so
+ * every tile, and every thread block, belongs to one member.  A step is then two kernel
+ * launches over all members together, each member with its own parameters, time, dt and
+ * status.  The plain API (cf_create, cf_set_state, ...) is the one-member case.
+ *
+ * Stepping never returns to the host between steps: the next dt of every member is produced on
+ * the device by the element kernel and read by the next edge kernel.  The host reads the small
+ * per-member records once at the end of a cf_step call.  Runs of steps are replayed from a
+ * captured CUDA graph of two steps (even and odd buffer parity).
  */
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <new>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "cf_internal.h"
 
 using namespace cf;
 
-struct cf_ctx {
-  int device = 0;
+namespace {
+
+struct Member {
   cf_params params{};
   Prep prep;
-  int32_t n = 0, n_pad = 0, ne = 0, ne_pad = 0, n_etiles = 0, n_ctiles = 0;
+  int32_t n = 0, ne = 0;
+  int32_t cell_off = 0, edge_off = 0;
+  int32_t ctile_begin = 0, ctile_end = 0;
+  MemberDev dev{};
+};
+
+}  // namespace
+
+struct cf_ctx {
+  int device = 0;
+  int32_t iflux = 1, ilimiteur = 1, flux_mode = 0;
+  std::vector<Member> mem;
+  int32_t n_pad = 0, ne_pad = 0, n_etiles = 0, n_ctiles = 0, max_n = 0;
   cudaStream_t stream = nullptr;
-  /* device memory */
+  /* device memory (flat over members) */
   double4* U[2] = {nullptr, nullptr};
   int4* cslot = nullptr;
   double4* cstat = nullptr;
   double* zcell = nullptr;
-  int32_t* perm = nullptr;   /* new -> old */
-  int32_t* iperm = nullptr;  /* old -> new */
+  int32_t* perm = nullptr;   /* new -> old, member-local */
+  int32_t* iperm = nullptr;  /* old -> new, member-local */
   int2* ecell = nullptr;
   double4* egeo = nullptr;
   int32_t* ebid = nullptr;
@@ -46,13 +66,11 @@ struct cf_ctx {
   int32_t* ctile_mem = nullptr;
   MemberDev* mdev = nullptr;
   MemberState* mst = nullptr;
-  double* staging = nullptr;      /* 3*n doubles, reference order */
-  MemberState* host_state = nullptr; /* pinned */
-  MemberDev mhost{};
+  double* staging = nullptr;           /* 3 * max_n doubles, reference order */
+  MemberState* host_state = nullptr;   /* pinned, one record per member */
   /* stepping */
-  bool have_state = false;
-  int64_t launched = 0;           /* steps launched since the state was set */
-  cudaGraphExec_t graph2 = nullptr; /* two steps: parity 0 then 1 */
+  int64_t launched = 0;                /* steps launched since creation (buffer parity) */
+  cudaGraphExec_t graph2 = nullptr;    /* two steps: parity 0 then 1 */
   bool use_graph = true;
   /* timing */
   bool timing = false;
@@ -84,11 +102,16 @@ int cuda_fail(cf_ctx* c, cudaError_t e, const char* what) {
   } while (0)
 
 template <class T>
-int upload(cf_ctx* c, T** dst, const std::vector<T>& src, size_t count_pad) {
-  size_t bytes = std::max<size_t>(1, count_pad) * sizeof(T);
+int dalloc(cf_ctx* c, T** dst, size_t count) {
+  size_t bytes = std::max<size_t>(1, count) * sizeof(T);
   CF_CUDA(c, cudaMalloc((void**)dst, bytes));
   CF_CUDA(c, cudaMemset(*dst, 0, bytes));
-  if (!src.empty()) CF_CUDA(c, cudaMemcpy(*dst, src.data(), src.size() * sizeof(T), cudaMemcpyHostToDevice));
+  return CF_OK;
+}
+
+template <class T>
+int put(cf_ctx* c, T* dst, const T* src, size_t count) {
+  if (count) CF_CUDA(c, cudaMemcpy(dst, src, count * sizeof(T), cudaMemcpyHostToDevice));
   return CF_OK;
 }
 
@@ -112,9 +135,9 @@ StepArgs step_args(const cf_ctx* c, int parity) {
   a.n_etiles = c->n_etiles;
   a.n_ctiles = c->n_ctiles;
   a.parity = parity;
-  a.iflux = c->params.iflux;
-  a.ilimiteur = c->params.ilimiteur;
-  a.flux_mode = c->params.flux_mode;
+  a.iflux = c->iflux;
+  a.ilimiteur = c->ilimiteur;
+  a.flux_mode = c->flux_mode;
   return a;
 }
 
@@ -131,31 +154,32 @@ void free_all(cf_ctx* c) {
   if (c->stream) cudaStreamDestroy(c->stream);
 }
 
-int read_state(cf_ctx* c) {
-  CF_CUDA(c, cudaMemcpyAsync(c->host_state, c->mst, sizeof(MemberState), cudaMemcpyDeviceToHost, c->stream));
+int read_states(cf_ctx* c) {
+  CF_CUDA(c, cudaMemcpyAsync(c->host_state, c->mst, c->mem.size() * sizeof(MemberState), cudaMemcpyDeviceToHost,
+                             c->stream));
   CF_CUDA(c, cudaStreamSynchronize(c->stream));
   return CF_OK;
 }
 
-void fill_info(const cf_ctx* c, cf_step_info* info) {
-  const MemberState& s = *c->host_state;
+void fill_info(const MemberState& s, cf_step_info* info) {
+  const int cur = (int)((s.base + s.nstep) & 1);
   info->steps = s.nstep;
-  info->t = s.t[s.nstep & 1];
-  info->dt_next = s.dt[s.nstep & 1];
-  info->dt_last = s.nstep > 0 ? s.dt[(s.nstep - 1) & 1] : 0.0;
+  info->t = s.t[cur];
+  info->dt_next = s.dt[cur];
+  info->dt_last = s.nstep > 0 ? s.dt[1 - cur] : 0.0;
   info->q_in = s.q_in;
   info->q_out = s.q_out;
-  info->status = s.status;
+  info->status = s.status & ~STATUS_NO_STATE;
   info->pad_ = 0;
 }
 
 int status_code(uint32_t st) {
+  if (st & STATUS_NO_STATE) return CF_ESTATE;
   if (st & CF_STATUS_NONFINITE) return CF_ENONFINITE;
   if (st & CF_STATUS_DT_RANGE) return CF_EDT;
   return CF_OK;
 }
 
-/* one step with explicit parity (also used while capturing the graph) */
 int enqueue_step(cf_ctx* c, int parity, bool timed) {
   StepArgs a = step_args(c, parity);
   int rc = launch_step(a, reinterpret_cast<stream_t>(c->stream), timed ? c->ev[1] : nullptr,
@@ -170,7 +194,10 @@ int build_graph(cf_ctx* c) {
   int rc0 = enqueue_step(c, 0, false);
   int rc1 = rc0 == CF_OK ? enqueue_step(c, 1, false) : rc0;
   cudaError_t e = cudaStreamEndCapture(c->stream, &g);
-  if (rc1 != CF_OK) { if (g) cudaGraphDestroy(g); return rc1; }
+  if (rc1 != CF_OK) {
+    if (g) cudaGraphDestroy(g);
+    return rc1;
+  }
   if (e != cudaSuccess) return cuda_fail(c, e, "cudaStreamEndCapture");
   e = cudaGraphInstantiate(&c->graph2, g, 0);
   cudaGraphDestroy(g);
@@ -178,47 +205,90 @@ int build_graph(cf_ctx* c) {
   return CF_OK;
 }
 
-}  // namespace
-
-extern "C" {
-
-int cf_default_params(cf_params* p) {
-  if (!p) return CF_EINVAL;
-  std::memset(p, 0, sizeof(*p));
-  p->gp = 9.81;
-  p->tolisec = 1e-5;
-  p->cfl = 0.9;
-  p->tol = (double)1e-6f;
-  p->iflux = 1;
-  p->ilimiteur = 1;
-  p->friction = 0;
-  p->fricimplic = 1;
-  p->inlet = 2;
-  p->outlet = 1;
-  p->flux_mode = 0;
-  p->reorder = 1;
+int check_params(const cf_params* p, std::string& why) {
+  if (p->iflux < 1 || p->iflux > 4) { why = "iflux must be 1..4"; return CF_EINVAL; }
+  if (p->iflux == 4) { why = "iflux 4 (MUSCL-Hancock) is not supported by the GPU step"; return CF_ENOTSUP; }
+  if (p->inlet == 3) { why = "inlet 'phys_inflow' is not supported"; return CF_ENOTSUP; }
+  if (p->inlet < 1 || p->inlet > 3 || p->outlet < 1 || p->outlet > 2) { why = "inlet must be 1..3 and outlet 1..2"; return CF_EINVAL; }
+  if (p->ilimiteur < 0 || p->ilimiteur > 4) { why = "ilimiteur must be 0..4"; return CF_EINVAL; }
+  if (p->flux_mode < 0 || p->flux_mode > 1) { why = "flux_mode must be 0 or 1"; return CF_EINVAL; }
+  if (p->fricimplic < 0 || p->fricimplic > 2) { why = "fricimplic must be 0..2"; return CF_EINVAL; }
+  if (!(p->gp > 0.0) || !(p->cfl > 0.0) || !(p->tolisec >= 0.0)) { why = "gp and cfl must be positive, tolisec non-negative"; return CF_EINVAL; }
+  if (p->ramp_time < 0.0) { why = "ramp_time must be non-negative"; return CF_EINVAL; }
   return CF_OK;
 }
 
-int cf_create(const cf_mesh* mesh, const cf_params* params, cf_ctx** out) {
+MemberDev member_dev(const Member& M) {
+  const cf_params* p = &M.params;
+  MemberDev D;
+  std::memset(&D, 0, sizeof(D));
+  D.gp = p->gp;
+  D.tolisec = p->tolisec;
+  D.tol = p->tol;
+  D.constant_dt = p->constant_dt;
+  D.ramp_time = p->ramp_time;
+  D.dt_reset = (M.n % 1024 != 0) ? 100000.0 : 1000000.0;
+  for (int i = 0; i < CF_MAX_IO; ++i) {
+    D.debit_end[i] = p->debitglob[i];
+    D.debit_start[i] = p->debitglob_start[i];
+    D.long_entree[i] = M.prep.long_entree[i];
+    D.h_sortie[i] = p->h_sortie[i];
+  }
+  D.inlet = p->inlet;
+  D.outlet = p->outlet;
+  D.friction = p->friction;
+  D.fricimplic = p->fricimplic;
+  D.is_dt_constant = p->is_dt_constant;
+  D.cell_begin = M.cell_off;
+  D.cell_end = M.cell_off + M.n;
+  D.edge_begin = M.edge_off;
+  D.edge_end = M.edge_off + M.ne;
+  D.bedge_begin = M.edge_off + M.prep.n_interior;
+  D.bedge_end = M.edge_off + M.ne;
+  return D;
+}
+
+/* Build a context of nm members (the meshes are preprocessed in parallel on the host). */
+int create_impl(const cf_mesh* meshes, const cf_params* params, int32_t nm, cf_ctx** out) {
   if (!out) return fail(nullptr, CF_EINVAL, "out is NULL");
   *out = nullptr;
-  if (!mesh || !params) return fail(nullptr, CF_EINVAL, "mesh or params is NULL");
-  if (params->iflux < 1 || params->iflux > 3)
-    return fail(nullptr, CF_ENOTSUP, "iflux must be 1 (HLLC), 2 (HLLC, star states) or 3 (WAF)");
-  if (params->inlet == 3) return fail(nullptr, CF_ENOTSUP, "inlet 'phys_inflow' is not supported");
-  if (params->inlet < 1 || params->inlet > 3 || params->outlet < 1 || params->outlet > 2)
-    return fail(nullptr, CF_EINVAL, "inlet must be 1..3 and outlet 1..2");
-  if (params->ilimiteur < 0 || params->ilimiteur > 4) return fail(nullptr, CF_EINVAL, "ilimiteur must be 0..4");
-  if (params->flux_mode < 0 || params->flux_mode > 1) return fail(nullptr, CF_EINVAL, "flux_mode must be 0 or 1");
-  if (!(params->gp > 0.0) || !(params->cfl > 0.0) || !(params->tolisec >= 0.0))
-    return fail(nullptr, CF_EINVAL, "gp and cfl must be positive, tolisec non-negative");
+  if (!meshes || !params || nm < 1) return fail(nullptr, CF_EINVAL, "meshes/params NULL or no member");
+  std::string why;
+  for (int i = 0; i < nm; ++i) {
+    int rc = check_params(&params[i], why);
+    if (rc != CF_OK) return fail(nullptr, rc, "member " + std::to_string(i) + ": " + why);
+    if (params[i].iflux != params[0].iflux || params[i].ilimiteur != params[0].ilimiteur ||
+        params[i].flux_mode != params[0].flux_mode)
+      return fail(nullptr, CF_EINVAL, "all members must share iflux, ilimiteur and flux_mode");
+  }
   cf_ctx* c = new (std::nothrow) cf_ctx();
   if (!c) return fail(nullptr, CF_ENOMEM, "host allocation failed");
-  c->params = *params;
-  std::string err;
-  int rc = prepare_mesh(mesh, params, c->prep, err);
-  if (rc != CF_OK) { delete c; return fail(nullptr, rc, err); }
+  c->iflux = params[0].iflux;
+  c->ilimiteur = params[0].ilimiteur;
+  c->flux_mode = params[0].flux_mode;
+  c->mem.resize(nm);
+  for (int i = 0; i < nm; ++i) c->mem[i].params = params[i];
+  /* host preprocessing, members in parallel */
+  std::vector<int> rcs(nm, CF_OK);
+  std::vector<std::string> errs(nm);
+  {
+    std::atomic<int> next(0);
+    unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+    int nth = (int)std::min<unsigned>(hw, (unsigned)nm);
+    auto work = [&]() {
+      for (int i = next++; i < nm; i = next++) rcs[i] = prepare_mesh(&meshes[i], &params[i], c->mem[i].prep, errs[i]);
+    };
+    std::vector<std::thread> th;
+    for (int t = 1; t < nth; ++t) th.emplace_back(work);
+    work();
+    for (auto& t : th) t.join();
+  }
+  for (int i = 0; i < nm; ++i)
+    if (rcs[i] != CF_OK) {
+      std::string msg = (nm > 1 ? "member " + std::to_string(i) + ": " : std::string()) + errs[i];
+      delete c;
+      return fail(nullptr, rcs[i], msg);
+    }
   auto done = [&](int code) {
     if (code != CF_OK) {
       g_create_error = c->err;
@@ -229,6 +299,25 @@ int cf_create(const cf_mesh* mesh, const cf_params* params, cf_ctx** out) {
     *out = c;
     return CF_OK;
   };
+  /* layout of the flat space */
+  int64_t noff = 0, eoff = 0;
+  for (auto& M : c->mem) {
+    M.n = M.prep.nelt;
+    M.ne = (int32_t)M.prep.edges.size();
+    M.cell_off = (int32_t)noff;
+    M.edge_off = (int32_t)eoff;
+    M.ctile_begin = (int32_t)(noff / TILE_C);
+    noff += (M.n + TILE_C - 1) / TILE_C * (int64_t)TILE_C;
+    eoff += (M.ne + TILE_E - 1) / TILE_E * (int64_t)TILE_E;
+    M.ctile_end = (int32_t)(noff / TILE_C);
+    c->max_n = std::max(c->max_n, M.n);
+    M.dev = member_dev(M);
+  }
+  if (noff > 0x7fffffffLL || 2 * eoff > 0x7fffffffLL) return done(fail(c, CF_EINVAL, "batch too large for 32-bit indices"));
+  c->n_pad = (int32_t)noff;
+  c->ne_pad = (int32_t)eoff;
+  c->n_ctiles = c->n_pad / TILE_C;
+  c->n_etiles = c->ne_pad / TILE_E;
   cudaError_t e = cudaGetDevice(&c->device);
   if (e != cudaSuccess) return done(cuda_fail(c, e, "cudaGetDevice"));
   e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
@@ -237,116 +326,116 @@ int cf_create(const cf_mesh* mesh, const cf_params* params, cf_ctx** out) {
     e = cudaEventCreate(&ev);
     if (e != cudaSuccess) return done(cuda_fail(c, e, "cudaEventCreate"));
   }
-  const Prep& P = c->prep;
-  c->n = P.nelt;
-  c->ne = (int32_t)P.edges.size();
-  c->n_ctiles = (c->n + TILE_C - 1) / TILE_C;
-  c->n_etiles = (c->ne + TILE_E - 1) / TILE_E;
-  c->n_pad = c->n_ctiles * TILE_C;
-  c->ne_pad = c->n_etiles * TILE_E;
-  if ((rc = upload(c, &c->cslot, P.cslot, c->n_pad)) || (rc = upload(c, &c->cstat, P.cstat, c->n_pad)) ||
-      (rc = upload(c, &c->zcell, P.zcell, c->n_pad)) || (rc = upload(c, &c->perm, P.perm, c->n_pad)) ||
-      (rc = upload(c, &c->iperm, P.iperm, c->n_pad)) || (rc = upload(c, &c->ecell, P.ecell, c->ne_pad)) ||
-      (rc = upload(c, &c->egeo, P.egeo, c->ne_pad)) || (rc = upload(c, &c->ebid, P.ebid, c->ne_pad)))
+  int rc;
+  const bool second = c->iflux >= 3;
+  if ((rc = dalloc(c, &c->U[0], c->n_pad)) || (rc = dalloc(c, &c->U[1], c->n_pad)) ||
+      (rc = dalloc(c, &c->cslot, c->n_pad)) || (rc = dalloc(c, &c->cstat, c->n_pad)) ||
+      (rc = dalloc(c, &c->zcell, c->n_pad)) || (rc = dalloc(c, &c->perm, c->n_pad)) ||
+      (rc = dalloc(c, &c->iperm, c->n_pad)) || (rc = dalloc(c, &c->ecell, c->ne_pad)) ||
+      (rc = dalloc(c, &c->egeo, c->ne_pad)) || (rc = dalloc(c, &c->ebid, c->ne_pad)) ||
+      (rc = dalloc(c, &c->slots, 2 * (size_t)c->ne_pad)) || (rc = dalloc(c, &c->etile_mem, c->n_etiles)) ||
+      (rc = dalloc(c, &c->ctile_mem, c->n_ctiles)) || (rc = dalloc(c, &c->mdev, (size_t)nm)) ||
+      (rc = dalloc(c, &c->mst, (size_t)nm)) || (rc = dalloc(c, &c->staging, 3 * (size_t)c->max_n)))
     return done(rc);
-  if (params->iflux >= 3) {
-    if ((rc = upload(c, &c->eupw, P.eupw, c->ne_pad)) || (rc = upload(c, &c->ewts, P.ewts, c->ne_pad)) ||
-        (rc = upload(c, &c->edk, P.edk, c->ne_pad)))
+  if (second && ((rc = dalloc(c, &c->eupw, c->ne_pad)) || (rc = dalloc(c, &c->ewts, c->ne_pad)) ||
+                 (rc = dalloc(c, &c->edk, c->ne_pad))))
+    return done(rc);
+  /* per-member uploads with the member offsets applied */
+  std::vector<int32_t> etm(c->n_etiles), ctm(c->n_ctiles);
+  std::vector<MemberDev> mdev(nm);
+  for (int i = 0; i < nm; ++i) {
+    Member& M = c->mem[i];
+    Prep& P = M.prep;
+    const int32_t co = M.cell_off, eo = M.edge_off;
+    for (int t = M.ctile_begin; t < M.ctile_end; ++t) ctm[t] = i;
+    for (int t = eo / TILE_E; t < (eo + (M.ne + TILE_E - 1) / TILE_E * TILE_E) / TILE_E; ++t) etm[t] = i;
+    std::vector<int4> cslot(P.cslot);
+    for (auto& s : cslot) { s.x += 2 * eo; s.y += 2 * eo; s.z += 2 * eo; }
+    std::vector<int2> ecell(P.ecell);
+    for (auto& e2 : ecell) { e2.x += co; if (e2.y >= 0) e2.y += co; }
+    if ((rc = put(c, c->cslot + co, cslot.data(), cslot.size())) || (rc = put(c, c->cstat + co, P.cstat.data(), P.cstat.size())) ||
+        (rc = put(c, c->zcell + co, P.zcell.data(), P.zcell.size())) || (rc = put(c, c->perm + co, P.perm.data(), P.perm.size())) ||
+        (rc = put(c, c->iperm + co, P.iperm.data(), P.iperm.size())) || (rc = put(c, c->ecell + eo, ecell.data(), ecell.size())) ||
+        (rc = put(c, c->egeo + eo, P.egeo.data(), P.egeo.size())) || (rc = put(c, c->ebid + eo, P.ebid.data(), P.ebid.size())))
       return done(rc);
+    if (second) {
+      std::vector<int4> up(P.eupw);
+      for (auto& u : up) { u.x += co; u.y += co; u.z += co; u.w += co; }
+      if ((rc = put(c, c->eupw + eo, up.data(), up.size())) || (rc = put(c, c->ewts + eo, P.ewts.data(), P.ewts.size())) ||
+          (rc = put(c, c->edk + eo, P.edk.data(), P.edk.size())))
+        return done(rc);
+      std::vector<int4>().swap(P.eupw);
+      std::vector<double4>().swap(P.ewts);
+      std::vector<double2>().swap(P.edk);
+    }
+    mdev[i] = M.dev;
+    /* the device copies are authoritative; keep the reference-order tables and the permutation */
+    std::vector<int4>().swap(P.cslot);
+    std::vector<double4>().swap(P.cstat);
+    std::vector<int2>().swap(P.ecell);
+    std::vector<double4>().swap(P.egeo);
+    std::vector<int32_t>().swap(P.ebid);
+    std::vector<HostEdge>().swap(P.edges);
   }
-  std::vector<double4> none;
-  if ((rc = upload(c, &c->U[0], none, c->n_pad)) || (rc = upload(c, &c->U[1], none, c->n_pad))) return done(rc);
-  std::vector<Slot> noslot;
-  if ((rc = upload(c, &c->slots, noslot, 2 * (size_t)c->ne_pad))) return done(rc);
-  std::vector<int32_t> tm_e(c->n_etiles, 0), tm_c(c->n_ctiles, 0);
-  if ((rc = upload(c, &c->etile_mem, tm_e, c->n_etiles)) || (rc = upload(c, &c->ctile_mem, tm_c, c->n_ctiles)))
+  if ((rc = put(c, c->etile_mem, etm.data(), etm.size())) || (rc = put(c, c->ctile_mem, ctm.data(), ctm.size())) ||
+      (rc = put(c, c->mdev, mdev.data(), mdev.size())))
     return done(rc);
-  std::vector<double> none_d;
-  if ((rc = upload(c, &c->staging, none_d, 3 * (size_t)c->n))) return done(rc);
-  /* member constants */
-  MemberDev& M = c->mhost;
-  std::memset(&M, 0, sizeof(M));
-  M.gp = params->gp;
-  M.tolisec = params->tolisec;
-  M.tol = params->tol;
-  M.constant_dt = params->constant_dt;
-  M.ramp_time = params->ramp_time;
-  M.dt_reset = (c->n % 1024 != 0) ? 100000.0 : 1000000.0;
-  for (int i = 0; i < CF_MAX_IO; ++i) {
-    M.debit_end[i] = params->debitglob[i];
-    M.debit_start[i] = params->debitglob_start[i];
-    M.long_entree[i] = P.long_entree[i];
-    M.h_sortie[i] = params->h_sortie[i];
-  }
-  M.inlet = params->inlet;
-  M.outlet = params->outlet;
-  M.friction = params->friction;
-  M.fricimplic = params->fricimplic;
-  M.is_dt_constant = params->is_dt_constant;
-  M.cell_begin = 0;
-  M.cell_end = c->n;
-  M.edge_begin = 0;
-  M.edge_end = c->ne;
-  M.bedge_begin = P.n_interior;
-  M.bedge_end = c->ne;
-  std::vector<MemberDev> mv(1, M);
-  if ((rc = upload(c, &c->mdev, mv, 1))) return done(rc);
-  std::vector<MemberState> ms(1);
-  std::memset(ms.data(), 0, sizeof(MemberState));
-  if ((rc = upload(c, &c->mst, ms, 1))) return done(rc);
-  e = cudaMallocHost((void**)&c->host_state, sizeof(MemberState));
+  e = cudaMallocHost((void**)&c->host_state, nm * sizeof(MemberState));
   if (e != cudaSuccess) return done(cuda_fail(c, e, "cudaMallocHost"));
-  std::memset(c->host_state, 0, sizeof(MemberState));
+  for (int i = 0; i < nm; ++i) {
+    std::memset(&c->host_state[i], 0, sizeof(MemberState));
+    c->host_state[i].status = STATUS_NO_STATE;
+  }
+  if ((rc = put(c, c->mst, c->host_state, (size_t)nm))) return done(rc);
   return done(CF_OK);
 }
 
-void cf_destroy(cf_ctx* c) {
-  if (!c) return;
-  cudaSetDevice(c->device);
-  cudaStreamSynchronize(c->stream);
-  free_all(c);
-  delete c;
-}
-
-static int set_state_common(cf_ctx* c, double t0) {
-  MemberState s;
-  std::memset(&s, 0, sizeof(s));
-  s.dt[0] = c->mhost.dt_reset;
-  s.t[0] = t0;
-  *c->host_state = s;
-  CF_CUDA(c, cudaMemcpyAsync(c->mst, c->host_state, sizeof(MemberState), cudaMemcpyHostToDevice, c->stream));
-  int rc = launch_scatter_state(c->staging, c->perm, c->zcell, c->U[0], c->n, reinterpret_cast<stream_t>(c->stream));
-  if (rc != CF_OK) return fail(c, rc, "state scatter launch failed");
-  rc = launch_cfl(c->U[0], c->cstat, c->ctile_mem, c->n_ctiles, c->mdev, c->mst, 0, reinterpret_cast<stream_t>(c->stream));
-  if (rc != CF_OK) return fail(c, rc, "cfl launch failed");
-  /* the host record is reused below; wait for the copy and the kernels */
-  CF_CUDA(c, cudaStreamSynchronize(c->stream));
-  c->have_state = true;
-  c->launched = 0;
+int member_ok(cf_ctx* c, int32_t m) {
+  if (!c) return CF_EINVAL;
+  if (m < 0 || m >= (int32_t)c->mem.size()) return fail(c, CF_EINVAL, "member index out of range");
   return CF_OK;
 }
 
-int cf_set_state(cf_ctx* c, const double* hu3, double t0) {
-  if (!c || !hu3) return fail(c, CF_EINVAL, "null argument");
-  CF_CUDA(c, cudaSetDevice(c->device));
-  CF_CUDA(c, cudaMemcpyAsync(c->staging, hu3, 3 * (size_t)c->n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
-  return set_state_common(c, t0);
+/* Set the state of member m from c->staging (reference order), resetting its time and steps. */
+int set_state_member(cf_ctx* c, int32_t m, double t0) {
+  const Member& M = c->mem[m];
+  const int p0 = (int)(c->launched & 1);
+  MemberState s;
+  std::memset(&s, 0, sizeof(s));
+  s.dt[p0] = M.dev.dt_reset;
+  s.t[p0] = t0;
+  s.base = p0;
+  c->host_state[m] = s;
+  CF_CUDA(c, cudaMemcpyAsync(c->mst + m, c->host_state + m, sizeof(MemberState), cudaMemcpyHostToDevice, c->stream));
+  int rc = launch_scatter_state(c->staging, c->perm + M.cell_off, c->zcell + M.cell_off, c->U[p0] + M.cell_off, M.n,
+                                reinterpret_cast<stream_t>(c->stream));
+  if (rc != CF_OK) return fail(c, rc, "state scatter launch failed");
+  rc = launch_cfl(c->U[p0], c->cstat, c->ctile_mem, M.ctile_begin, M.ctile_end - M.ctile_begin, c->mdev, c->mst, p0,
+                  reinterpret_cast<stream_t>(c->stream));
+  if (rc != CF_OK) return fail(c, rc, "cfl launch failed");
+  CF_CUDA(c, cudaStreamSynchronize(c->stream));
+  return CF_OK;
 }
 
-int cf_set_state_device(cf_ctx* c, const double* d_hu3, double t0) {
-  if (!c || !d_hu3) return fail(c, CF_EINVAL, "null argument");
+int set_state_host(cf_ctx* c, int32_t m, const double* hu3, double t0, cudaMemcpyKind kind) {
+  int rc = member_ok(c, m);
+  if (rc) return rc;
+  if (!hu3) return fail(c, CF_EINVAL, "null state");
   CF_CUDA(c, cudaSetDevice(c->device));
-  CF_CUDA(c, cudaMemcpyAsync(c->staging, d_hu3, 3 * (size_t)c->n * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
-  return set_state_common(c, t0);
+  CF_CUDA(c, cudaMemcpyAsync(c->staging, hu3, 3 * (size_t)c->mem[m].n * sizeof(double), kind, c->stream));
+  return set_state_member(c, m, t0);
 }
 
 /* set_initial_condition, initial_condition.cuf:18-79, evaluated on the host (setup only). */
-int cf_set_initial_condition(cf_ctx* c, const cf_ic* ic, double t0) {
-  if (!c || !ic) return fail(c, CF_EINVAL, "null argument");
-  const Prep& P = c->prep;
-  std::vector<double> U(3 * (size_t)c->n, 0.0);
-  const double tolisec = c->params.tolisec;
-  for (int k = 0; k < c->n; ++k) {
+int initial_condition(cf_ctx* c, int32_t m, const cf_ic* ic, double t0) {
+  int rc = member_ok(c, m);
+  if (rc) return rc;
+  if (!ic) return fail(c, CF_EINVAL, "null argument");
+  const Member& M = c->mem[m];
+  const Prep& P = M.prep;
+  std::vector<double> U(3 * (size_t)M.n, 0.0);
+  const double tolisec = M.params.tolisec;
+  for (int k = 0; k < M.n; ++k) {
     const double zmd = P.zm[k], v1 = P.xc[k], v2 = P.yc[k];
     double* u = &U[3 * (size_t)k];
     if (ic->eqlin_barrage == 1) {
@@ -373,25 +462,36 @@ int cf_set_initial_condition(cf_ctx* c, const cf_ic* ic, double t0) {
       }
     }
   }
-  return cf_set_state(c, U.data(), t0);
+  return set_state_host(c, m, U.data(), t0, cudaMemcpyHostToDevice);
 }
 
-int cf_step(cf_ctx* c, int32_t nsteps, cf_step_info* info) {
+int get_state_member(cf_ctx* c, int32_t m, double* dst, cudaMemcpyKind kind) {
+  int rc = member_ok(c, m);
+  if (rc) return rc;
+  if (!dst) return fail(c, CF_EINVAL, "null destination");
+  CF_CUDA(c, cudaSetDevice(c->device));
+  if ((rc = read_states(c))) return rc;
+  const MemberState& s = c->host_state[m];
+  if (s.status & STATUS_NO_STATE) return fail(c, CF_ESTATE, "no state set");
+  const Member& M = c->mem[m];
+  const int buf = (int)((s.base + s.nstep) & 1);
+  rc = launch_gather_state(c->U[buf] + M.cell_off, c->iperm + M.cell_off, c->staging, M.n,
+                           reinterpret_cast<stream_t>(c->stream));
+  if (rc != CF_OK) return fail(c, rc, "gather launch failed");
+  CF_CUDA(c, cudaMemcpyAsync(dst, c->staging, 3 * (size_t)M.n * sizeof(double), kind, c->stream));
+  CF_CUDA(c, cudaStreamSynchronize(c->stream));
+  return CF_OK;
+}
+
+int step_impl(cf_ctx* c, int32_t nsteps, cf_step_info* infos) {
   if (!c) return CF_EINVAL;
   if (nsteps < 0) return fail(c, CF_EINVAL, "nsteps < 0");
-  if (!c->have_state) return fail(c, CF_ESTATE, "cf_step before a state was set");
   CF_CUDA(c, cudaSetDevice(c->device));
-  if (c->host_state->status) {
-    if (info) fill_info(c, info);
-    return fail(c, status_code(c->host_state->status), "the run is stopped (status latched on the device)");
-  }
   int rc;
-  const bool timed = c->timing;
   c->flux_ms = c->update_ms = 0.0;
   c->launches = 0;
   int32_t left = nsteps;
-  if (timed) {
-    /* per-step events: edge kernel [ev0, ev1), element kernel [ev1, ev2) */
+  if (c->timing) {
     for (int32_t i = 0; i < nsteps; ++i) {
       CF_CUDA(c, cudaEventRecord(c->ev[0], c->stream));
       if ((rc = enqueue_step(c, (int)((c->launched + i) & 1), true))) return rc;
@@ -417,53 +517,112 @@ int cf_step(cf_ctx* c, int32_t nsteps, cf_step_info* info) {
       if ((rc = enqueue_step(c, (int)((c->launched + nsteps - left) & 1), false))) return rc;
       --left;
     }
+    c->launches = 2 * (int64_t)nsteps;
   }
   c->launched += nsteps;
-  rc = launch_discharge(c->slots, c->ecell, c->mdev, c->mst, 1, reinterpret_cast<stream_t>(c->stream));
+  rc = launch_discharge(c->slots, c->ecell, c->mdev, c->mst, (int32_t)c->mem.size(), reinterpret_cast<stream_t>(c->stream));
   if (rc != CF_OK) return fail(c, rc, "discharge launch failed");
-  if ((rc = read_state(c))) return rc;
-  if (info) fill_info(c, info);
-  rc = status_code(c->host_state->status);
-  if (rc != CF_OK) return fail(c, rc, rc == CF_EDT ? "dt left the range (1e-12, 9999]" : "non-finite value in the state");
+  if ((rc = read_states(c))) return rc;
+  uint32_t any = 0;
+  for (size_t i = 0; i < c->mem.size(); ++i) {
+    if (infos) fill_info(c->host_state[i], &infos[i]);
+    any |= c->host_state[i].status;
+  }
+  if (c->mem.size() == 1 && (any & STATUS_NO_STATE)) return fail(c, CF_ESTATE, "cf_step before a state was set");
+  rc = status_code(any & ~STATUS_NO_STATE);
+  if (rc != CF_OK)
+    return fail(c, rc, rc == CF_EDT ? "dt left the range (1e-12, 9999]" : "non-finite value in the state");
   return CF_OK;
 }
 
-static int gather_common(cf_ctx* c, double* dst, cudaMemcpyKind kind) {
-  if (!c->have_state) return fail(c, CF_ESTATE, "no state set");
-  int rc = read_state(c);
-  if (rc) return rc;
-  const int buf = (int)(c->host_state->nstep & 1);
-  rc = launch_gather_state(c->U[buf], c->iperm, c->staging, c->n, reinterpret_cast<stream_t>(c->stream));
-  if (rc != CF_OK) return fail(c, rc, "gather launch failed");
-  CF_CUDA(c, cudaMemcpyAsync(dst, c->staging, 3 * (size_t)c->n * sizeof(double), kind, c->stream));
-  CF_CUDA(c, cudaStreamSynchronize(c->stream));
+}  // namespace
+
+extern "C" {
+
+int cf_default_params(cf_params* p) {
+  if (!p) return CF_EINVAL;
+  std::memset(p, 0, sizeof(*p));
+  p->gp = 9.81;
+  p->tolisec = 1e-5;
+  p->cfl = 0.9;
+  p->tol = (double)1e-6f;
+  p->iflux = 1;
+  p->ilimiteur = 1;
+  p->friction = 0;
+  p->fricimplic = 1;
+  p->inlet = 2;
+  p->outlet = 1;
+  p->flux_mode = 0;
+  p->reorder = 1;
   return CF_OK;
 }
 
-int cf_get_state(cf_ctx* c, double* hu3) {
-  if (!c || !hu3) return fail(c, CF_EINVAL, "null argument");
-  CF_CUDA(c, cudaSetDevice(c->device));
-  return gather_common(c, hu3, cudaMemcpyDeviceToHost);
+int cf_create(const cf_mesh* mesh, const cf_params* params, cf_ctx** out) {
+  return create_impl(mesh, params, 1, out);
 }
 
-int cf_get_state_device(cf_ctx* c, double* d_hu3) {
-  if (!c || !d_hu3) return fail(c, CF_EINVAL, "null argument");
-  CF_CUDA(c, cudaSetDevice(c->device));
-  return gather_common(c, d_hu3, cudaMemcpyDeviceToDevice);
+int cf_create_batch(const cf_mesh* meshes, const cf_params* params, int32_t nmembers, cf_ctx** out) {
+  return create_impl(meshes, params, nmembers, out);
 }
 
-int cf_get_info(cf_ctx* c, cf_step_info* info) {
-  if (!c || !info) return fail(c, CF_EINVAL, "null argument");
-  CF_CUDA(c, cudaSetDevice(c->device));
-  int rc = read_state(c);
+void cf_destroy(cf_ctx* c) {
+  if (!c) return;
+  cudaSetDevice(c->device);
+  cudaStreamSynchronize(c->stream);
+  free_all(c);
+  delete c;
+}
+
+int cf_get_members(cf_ctx* c) { return c ? (int)c->mem.size() : CF_EINVAL; }
+
+int cf_set_state(cf_ctx* c, const double* hu3, double t0) {
+  return set_state_host(c, 0, hu3, t0, cudaMemcpyHostToDevice);
+}
+
+int cf_set_state_device(cf_ctx* c, const double* d_hu3, double t0) {
+  return set_state_host(c, 0, d_hu3, t0, cudaMemcpyDeviceToDevice);
+}
+
+int cf_member_set_state(cf_ctx* c, int32_t member, const double* hu3, double t0) {
+  return set_state_host(c, member, hu3, t0, cudaMemcpyHostToDevice);
+}
+
+int cf_set_initial_condition(cf_ctx* c, const cf_ic* ic, double t0) { return initial_condition(c, 0, ic, t0); }
+
+int cf_member_set_initial_condition(cf_ctx* c, int32_t member, const cf_ic* ic, double t0) {
+  return initial_condition(c, member, ic, t0);
+}
+
+int cf_step(cf_ctx* c, int32_t nsteps, cf_step_info* info) { return step_impl(c, nsteps, info); }
+
+int cf_get_state(cf_ctx* c, double* hu3) { return get_state_member(c, 0, hu3, cudaMemcpyDeviceToHost); }
+
+int cf_get_state_device(cf_ctx* c, double* d_hu3) { return get_state_member(c, 0, d_hu3, cudaMemcpyDeviceToDevice); }
+
+int cf_member_get_state(cf_ctx* c, int32_t member, double* hu3) {
+  return get_state_member(c, member, hu3, cudaMemcpyDeviceToHost);
+}
+
+int cf_get_info(cf_ctx* c, cf_step_info* info) { return cf_member_get_info(c, 0, info); }
+
+int cf_member_get_info(cf_ctx* c, int32_t member, cf_step_info* info) {
+  int rc = member_ok(c, member);
   if (rc) return rc;
-  fill_info(c, info);
+  if (!info) return fail(c, CF_EINVAL, "null argument");
+  CF_CUDA(c, cudaSetDevice(c->device));
+  if ((rc = read_states(c))) return rc;
+  fill_info(c->host_state[member], info);
   return CF_OK;
 }
 
 int cf_get_mesh_tables(cf_ctx* c, int32_t* boundary, double* area, double* zm, double* cotemin) {
-  if (!c) return CF_EINVAL;
-  const Prep& P = c->prep;
+  return cf_member_get_mesh_tables(c, 0, boundary, area, zm, cotemin);
+}
+
+int cf_member_get_mesh_tables(cf_ctx* c, int32_t member, int32_t* boundary, double* area, double* zm, double* cotemin) {
+  int rc = member_ok(c, member);
+  if (rc) return rc;
+  const Prep& P = c->mem[member].prep;
   const size_t n = (size_t)P.nelt;
   if (boundary) std::memcpy(boundary, P.bnd.data(), n * 6 * sizeof(int32_t));
   if (area) std::memcpy(area, P.area.data(), n * sizeof(double));
@@ -472,8 +631,8 @@ int cf_get_mesh_tables(cf_ctx* c, int32_t* boundary, double* area, double* zm, d
   return CF_OK;
 }
 
-int cf_mesh_tables(const cf_mesh* mesh, const cf_params* params, int32_t* boundary, double* area,
-                   double* zm, double* cotemin) {
+int cf_mesh_tables(const cf_mesh* mesh, const cf_params* params, int32_t* boundary, double* area, double* zm,
+                   double* cotemin) {
   Prep P;
   std::string err;
   int rc = prepare_mesh(mesh, params, P, err);
@@ -488,8 +647,13 @@ int cf_mesh_tables(const cf_mesh* mesh, const cf_params* params, int32_t* bounda
 
 int cf_get_sizes(cf_ctx* c, int64_t* nelt, int64_t* nedge) {
   if (!c) return CF_EINVAL;
-  if (nelt) *nelt = c->n;
-  if (nedge) *nedge = c->ne;
+  int64_t n = 0, e = 0;
+  for (const auto& M : c->mem) {
+    n += M.n;
+    e += M.ne;
+  }
+  if (nelt) *nelt = n;
+  if (nedge) *nedge = e;
   return CF_OK;
 }
 

@@ -67,10 +67,13 @@ struct MemberState {
   double dt[2];
   double t[2];
   double q_in, q_out;
-  long long nstep;   /* steps completed since the state was set; the state is in U[nstep & 1] */
-  uint32_t status;
-  int32_t pad_;
+  long long nstep;   /* steps completed since the state was set */
+  uint32_t status;   /* CF_STATUS_* bits; a member with a non-zero status does not step */
+  int32_t base;      /* buffer parity at which the state was set: the state is in U[(base + nstep) & 1] */
 };
+
+/* status bit of a member whose state has not been set yet */
+constexpr uint32_t STATUS_NO_STATE = 0x80000000u;
 
 /* Everything a step kernel needs, passed by value. */
 struct StepArgs {
@@ -135,10 +138,12 @@ int prepare_mesh(const cf_mesh* m, const cf_params* p, Prep& out, std::string& e
 typedef struct CUstream_st* stream_t;
 
 int launch_step(const StepArgs& a, stream_t s, void* ev_mid, void* ev_end);
-int launch_cfl(const double4* U, const double4* cstat, const int32_t* ctile_mem, int32_t n_ctiles,
-               const MemberDev* mdev, MemberState* mst, int32_t slot, stream_t s);
+int launch_cfl(const double4* U, const double4* cstat, const int32_t* ctile_mem, int32_t tile_begin,
+               int32_t n_tiles, const MemberDev* mdev, MemberState* mst, int32_t slot, stream_t s);
 int launch_discharge(const Slot* slots, const int2* ecell, const MemberDev* mdev, MemberState* mst,
                      int32_t nmembers, stream_t s);
+/* hu3 (reference order, one member) <-> U (new order); perm/iperm/zcell/U point at the member's
+ * first element, the permutations hold member-local indices. */
 int launch_scatter_state(const double* hu3, const int32_t* perm_new2old, const double* zcell,
                          double4* U, int32_t n, stream_t s);
 int launch_gather_state(const double4* U, const int32_t* iperm_old2new, double* hu3, int32_t n,

@@ -124,8 +124,8 @@ __global__ void __launch_bounds__(TILE_C) k_cells(StepArgs a) {
 
 /* CFL of a state into mst[m].dt[slot] (the initial dt, finite_volumes_method.cuf:113-116). */
 __global__ void __launch_bounds__(TILE_C) k_cfl(const double4* U, const double4* cstat, const int32_t* ctile_mem,
-                                                const MemberDev* mdev, MemberState* mst, int slot) {
-  const int tile = blockIdx.x;
+                                                int tile_begin, const MemberDev* mdev, MemberState* mst, int slot) {
+  const int tile = tile_begin + blockIdx.x;
   const int m = __ldg(ctile_mem + tile);
   const MemberDev& M = mdev[m];
   const int c = tile * TILE_C + threadIdx.x;
@@ -202,9 +202,10 @@ int launch_step(const StepArgs& a, stream_t s, void* ev_mid, void* ev_end) {
   return check(cudaGetLastError());
 }
 
-int launch_cfl(const double4* U, const double4* cstat, const int32_t* ctile_mem, int32_t n_ctiles,
-               const MemberDev* mdev, MemberState* mst, int32_t slot, stream_t s) {
-  k_cfl<<<n_ctiles, TILE_C, 0, reinterpret_cast<cudaStream_t>(s)>>>(U, cstat, ctile_mem, mdev, mst, slot);
+int launch_cfl(const double4* U, const double4* cstat, const int32_t* ctile_mem, int32_t tile_begin,
+               int32_t n_tiles, const MemberDev* mdev, MemberState* mst, int32_t slot, stream_t s) {
+  if (n_tiles <= 0) return CF_OK;
+  k_cfl<<<n_tiles, TILE_C, 0, reinterpret_cast<cudaStream_t>(s)>>>(U, cstat, ctile_mem, tile_begin, mdev, mst, slot);
   return check(cudaGetLastError());
 }
 

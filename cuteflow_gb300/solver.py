@@ -65,6 +65,17 @@ def load(build_if_missing: bool = True):
     L.cf_last_error.restype = C.c_char_p
     L.cf_set_timing.argtypes = [vp, C.c_int32]
     L.cf_get_timing.argtypes = [vp, dp, dp, C.POINTER(C.c_int64)]
+    ip = C.POINTER(C.c_int32)
+    L.cf_create_batch.argtypes = [C.POINTER(_abi.CfMesh), C.POINTER(_abi.CfParams), C.c_int32, C.POINTER(vp)]
+    L.cf_get_members.argtypes = [vp]
+    L.cf_member_set_state.argtypes = [vp, C.c_int32, dp, C.c_double]
+    L.cf_member_set_initial_condition.argtypes = [vp, C.c_int32, C.POINTER(_abi.CfIc), C.c_double]
+    L.cf_member_get_state.argtypes = [vp, C.c_int32, dp]
+    L.cf_member_get_info.argtypes = [vp, C.c_int32, C.POINTER(_abi.CfStepInfo)]
+    L.cf_member_get_mesh_tables.argtypes = [vp, C.c_int32, ip, dp, dp, dp]
+    for name in ("cf_create_batch", "cf_get_members", "cf_member_set_state", "cf_member_set_initial_condition",
+                 "cf_member_get_state", "cf_member_get_info", "cf_member_get_mesh_tables"):
+        getattr(L, name).restype = C.c_int
     for name in ("cf_default_params", "cf_create", "cf_set_state", "cf_set_state_device",
                  "cf_set_initial_condition", "cf_step", "cf_get_state", "cf_get_state_device",
                  "cf_get_info", "cf_get_mesh_tables", "cf_mesh_tables", "cf_get_sizes", "cf_set_timing", "cf_get_timing"):
@@ -181,6 +192,86 @@ class Solver:
         self._check(self._L.cf_get_mesh_tables(self._ctx, _abi.iptr(bnd), _abi.dptr(area),
                                                _abi.dptr(zm), _abi.dptr(cm)))
         return bnd, area, zm, cm
+
+    def stream(self) -> int:
+        return int(self._L.cf_get_stream(self._ctx) or 0)
+
+    def set_timing(self, on: bool):
+        self._check(self._L.cf_set_timing(self._ctx, 1 if on else 0))
+
+    def timing(self):
+        f, u, n = C.c_double(), C.c_double(), C.c_int64()
+        self._check(self._L.cf_get_timing(self._ctx, C.byref(f), C.byref(u), C.byref(n)))
+        return f.value, u.value, int(n.value)
+
+
+class Batch:
+    """Many independent simulations of uneven size stepped together (cf_create_batch)."""
+
+    def __init__(self, case_list, params_list=None):
+        self._L = load()
+        self._ctx = C.c_void_p()
+        self._meshes = [_abi.MeshArrays(c) for c in case_list]
+        n = len(case_list)
+        params_list = params_list or [None] * n
+        MeshArr = _abi.CfMesh * n
+        ParArr = _abi.CfParams * n
+        self._mesh_arr = MeshArr(*[m.mesh for m in self._meshes])
+        self._par_arr = ParArr(*[_abi.make_params({**getattr(c, "params", {}), **(p or {})})
+                                 for c, p in zip(case_list, params_list)])
+        rc = self._L.cf_create_batch(self._mesh_arr, self._par_arr, n, C.byref(self._ctx))
+        if rc != 0:
+            raise CFError(rc, self._L.cf_last_error(None).decode())
+        self.members = n
+        self.nelt = [int(m.mesh.nelt) for m in self._meshes]
+
+    def _check(self, rc: int):
+        if rc != 0:
+            raise CFError(rc, self._L.cf_last_error(self._ctx).decode())
+
+    def close(self):
+        if self._ctx:
+            self._L.cf_destroy(self._ctx)
+            self._ctx = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def set_state(self, member: int, U: np.ndarray, t0: float = 0.0):
+        U = np.ascontiguousarray(U, dtype=np.float64).reshape(self.nelt[member], 3)
+        self._check(self._L.cf_member_set_state(self._ctx, int(member), _abi.dptr(U), float(t0)))
+
+    def set_initial_condition(self, member: int, ic: dict, t0: float = 0.0):
+        c = _abi.CfIc()
+        for k, v in ic.items():
+            setattr(c, k, v)
+        self._check(self._L.cf_member_set_initial_condition(self._ctx, int(member), C.byref(c), float(t0)))
+
+    def step(self, nsteps: int, check: bool = True):
+        infos = (_abi.CfStepInfo * self.members)()
+        rc = self._L.cf_step(self._ctx, int(nsteps), infos)
+        if check:
+            self._check(rc)
+        return [_info(i) for i in infos]
+
+    def get_state(self, member: int) -> np.ndarray:
+        out = np.empty((self.nelt[member], 3))
+        self._check(self._L.cf_member_get_state(self._ctx, int(member), _abi.dptr(out)))
+        return out
+
+    def info(self, member: int) -> StepInfo:
+        s = _abi.CfStepInfo()
+        self._check(self._L.cf_member_get_info(self._ctx, int(member), C.byref(s)))
+        return _info(s)
 
     def stream(self) -> int:
         return int(self._L.cf_get_stream(self._ctx) or 0)

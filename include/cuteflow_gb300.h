@@ -144,7 +144,9 @@ int cf_set_initial_condition(cf_ctx* ctx, const cf_ic* ic, double t0);
 /* Advance nsteps steps of the time loop (finite_volumes_method.cuf:123-242 without file
  * output).  Each step: fluxes, sources and friction, update with the wet/dry clamp, and the
  * CFL dt of the new state for the next step, all on the device with no host round trip.
- * info may be NULL. */
+ * info is NULL or an array of cf_get_members(ctx) records (one for a plain context).
+ * Returns CF_EDT / CF_ENONFINITE when a member has stopped (that member no longer steps; the
+ * others do), CF_ESTATE for a plain context without a state. */
 int cf_step(cf_ctx* ctx, int32_t nsteps, cf_step_info* info);
 
 /* Copy U^n to host memory in reference order (3*nelt doubles). */
@@ -155,6 +157,21 @@ int cf_get_state_device(cf_ctx* ctx, double* d_hu3_out);
 
 /* Current time, dt and status without stepping. */
 int cf_get_info(cf_ctx* ctx, cf_step_info* info);
+
+/* ---- Batched ensembles (no reference counterpart: the reference runs ensemble members as
+ * separate processes, scripts/array.sh:8-11, Calibration_manning/scripts/calib_array.sh:8-11).
+ * A batch context holds nmembers independent simulations of uneven size in one flat
+ * element/edge space; every cf_step advances all of them in the same kernel launches, each
+ * with its own parameters, dt, time and status.  All members share iflux, ilimiteur and
+ * flux_mode.  Member indices are 0-based; the plain functions above act on member 0. */
+int cf_create_batch(const cf_mesh* meshes, const cf_params* params, int32_t nmembers, cf_ctx** out);
+int cf_get_members(cf_ctx* ctx);
+int cf_member_set_state(cf_ctx* ctx, int32_t member, const double* hu3, double t0);
+int cf_member_set_initial_condition(cf_ctx* ctx, int32_t member, const cf_ic* ic, double t0);
+int cf_member_get_state(cf_ctx* ctx, int32_t member, double* hu3_out);
+int cf_member_get_info(cf_ctx* ctx, int32_t member, cf_step_info* info);
+int cf_member_get_mesh_tables(cf_ctx* ctx, int32_t member, int32_t* boundary, double* area, double* zm,
+                              double* cotemin);
 
 /* Preprocessing results in reference order, for comparison with the reference's own
  * boundary table file (maillage.cuf:62-68).  boundary: [nelt*3*2] int32 with
@@ -168,7 +185,8 @@ int cf_get_mesh_tables(cf_ctx* ctx, int32_t* boundary, double* area, double* zm,
 int cf_mesh_tables(const cf_mesh* mesh, const cf_params* params, int32_t* boundary, double* area,
                    double* zm, double* cotemin);
 
-/* Number of elements and edges of the context; edges counts each shared edge once. */
+/* Number of elements and edges of the context (all members); edges counts each shared edge
+ * once. */
 int cf_get_sizes(cf_ctx* ctx, int64_t* nelt, int64_t* nedge);
 
 /* The CUDA stream (cudaStream_t) the context launches on. */
