@@ -60,7 +60,8 @@ struct cf_ctx {
   int32_t* ebid = nullptr;
   int4* eupw = nullptr;
   double4* ewts = nullptr;
-  double2* edk = nullptr;
+  double4* edk = nullptr;
+  double4* einv = nullptr;
   Slot* slots = nullptr;
   int32_t* etile_mem = nullptr;
   int32_t* ctile_mem = nullptr;
@@ -127,6 +128,7 @@ StepArgs step_args(const cf_ctx* c, int parity) {
   a.eupw = c->eupw;
   a.ewts = c->ewts;
   a.edk = c->edk;
+  a.einv = c->einv;
   a.slots = c->slots;
   a.etile_mem = c->etile_mem;
   a.ctile_mem = c->ctile_mem;
@@ -144,7 +146,7 @@ StepArgs step_args(const cf_ctx* c, int parity) {
 void free_all(cf_ctx* c) {
   if (c->graph2) cudaGraphExecDestroy(c->graph2);
   void* ptrs[] = {c->U[0], c->U[1], c->cslot, c->cstat, c->zcell, c->perm, c->iperm, c->ecell, c->egeo,
-                  c->ebid, c->eupw, c->ewts, c->edk, c->slots, c->etile_mem, c->ctile_mem, c->mdev,
+                  c->ebid, c->eupw, c->ewts, c->edk, c->einv, c->slots, c->etile_mem, c->ctile_mem, c->mdev,
                   c->mst, c->staging};
   for (void* p : ptrs)
     if (p) cudaFree(p);
@@ -338,7 +340,7 @@ int create_impl(const cf_mesh* meshes, const cf_params* params, int32_t nm, cf_c
       (rc = dalloc(c, &c->mst, (size_t)nm)) || (rc = dalloc(c, &c->staging, 3 * (size_t)c->max_n)))
     return done(rc);
   if (second && ((rc = dalloc(c, &c->eupw, c->ne_pad)) || (rc = dalloc(c, &c->ewts, c->ne_pad)) ||
-                 (rc = dalloc(c, &c->edk, c->ne_pad))))
+                 (rc = dalloc(c, &c->edk, c->ne_pad)) || (rc = dalloc(c, &c->einv, c->ne_pad))))
     return done(rc);
   /* per-member uploads with the member offsets applied */
   std::vector<int32_t> etm(c->n_etiles), ctm(c->n_ctiles);
@@ -362,11 +364,12 @@ int create_impl(const cf_mesh* meshes, const cf_params* params, int32_t nm, cf_c
       std::vector<int4> up(P.eupw);
       for (auto& u : up) { u.x += co; u.y += co; u.z += co; u.w += co; }
       if ((rc = put(c, c->eupw + eo, up.data(), up.size())) || (rc = put(c, c->ewts + eo, P.ewts.data(), P.ewts.size())) ||
-          (rc = put(c, c->edk + eo, P.edk.data(), P.edk.size())))
+          (rc = put(c, c->edk + eo, P.edk.data(), P.edk.size())) || (rc = put(c, c->einv + eo, P.einv.data(), P.einv.size())))
         return done(rc);
       std::vector<int4>().swap(P.eupw);
       std::vector<double4>().swap(P.ewts);
-      std::vector<double2>().swap(P.edk);
+      std::vector<double4>().swap(P.edk);
+      std::vector<double4>().swap(P.einv);
     }
     mdev[i] = M.dev;
     /* the device copies are authoritative; keep the reference-order tables and the permutation */

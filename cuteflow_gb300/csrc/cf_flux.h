@@ -35,6 +35,7 @@ namespace cf {
 #ifndef __CUDACC__
 using std::copysign;
 using std::fabs;
+using std::fma;
 using std::fmax;
 using std::frexp;
 using std::ldexp;
@@ -71,6 +72,22 @@ CF_HD CF_INLINE bool finite_bits(double x) {
 CF_HD CF_INLINE double dmax(double a, double b) { return (a < b) ? b : a; } /* Fortran max */
 CF_HD CF_INLINE double dmin(double a, double b) { return (b < a) ? b : a; } /* Fortran min */
 
+/* a / d rounded to nearest, given y = RN(1/d): q = RN(a y), r = a - d q (exact through the
+ * FMA), RN(q + r y) (Markstein's correction step; P. Markstein, "Computation of elementary
+ * functions on the IBM RISC System/6000 processor", IBM J. Res. Dev. 34, 1990).  It equals the
+ * IEEE quotient for finite non-zero a (no mismatch in 3e8 adversarial samples, see the tests);
+ * a zero numerator is returned as q = a y, which carries the quotient's sign.  Three FP64
+ * instructions instead of a full division wherever 1/d is known: for precomputed geometry,
+ * and for denominators shared by several quotients (y = 1/d computed once). */
+CF_HD CF_INLINE double div_rn(double a, double d, double y) {
+  const double q = a * y;
+  const double r = fma(-d, q, a);
+  const double q1 = fma(r, y, q);
+  long long ab;
+  memcpy(&ab, &a, sizeof(ab));
+  return ((ab << 1) == 0) ? q : q1;
+}
+
 /* ---- x**(-1/3) -------------------------------------------------------------------------- */
 
 /* x^(1/3) for x > 0 by Halley's iteration y <- y (y^3 + 2m) / (2 y^3 + m) on the mantissa
@@ -99,12 +116,25 @@ CF_HD CF_INLINE double cbrt_halley(double x) {
 CF_HD CF_INLINE void to_frame(double h, double hu, double hv, double nx, double ny, double tolisec,
                               double& hm, double& un, double& ut) {
   if (h > tolisec) {
-    un = (hu * nx + hv * ny) / h;
-    ut = (hv * nx - hu * ny) / h;
+    const double y = 1.0 / h;
+    un = div_rn(hu * nx + hv * ny, h, y);
+    ut = div_rn(hv * nx - hu * ny, h, y);
     hm = h;
   } else {
     hm = 0.0;
     un = 0.0;
+    ut = 0.0;
+  }
+}
+
+/* Only the masked depth and tangential velocity (what the WAF upwind states use). */
+CF_HD CF_INLINE void to_frame_t(double h, double hu, double hv, double nx, double ny, double tolisec, double& hm,
+                                double& ut) {
+  if (h > tolisec) {
+    ut = (hv * nx - hu * ny) / h;
+    hm = h;
+  } else {
+    hm = 0.0;
     ut = 0.0;
   }
 }
@@ -182,8 +212,9 @@ CF_HD CF_INLINE void first_order_flux(double g, double nx, double ny, double hl,
     const int rb = (-sr > 0) ? 1 : ((-sl < 0) ? 0 : 2);
     double h1 = 0.0, h2 = 0.0;
     if (ra == 2 || rb == 2) {
-      h1 = (sr * fl1 - sl * fr1 + sl * sr * (hr - hl)) / (sr - sl + eps);
-      h2 = (sr * fl2 - sl * fr2 + sl * sr * (hr * ur - hl * ul)) / (sr - sl + eps);
+      const double den = sr - sl + eps, yden = 1.0 / den;
+      h1 = div_rn(sr * fl1 - sl * fr1 + sl * sr * (hr - hl), den, yden);
+      h2 = div_rn(sr * fl2 - sl * fr2 + sl * sr * (hr * ur - hl * ul), den, yden);
     }
     if (ra == 0) { x1 = fl1; x2 = fl2; x3 = fl3; }
     else if (ra == 1) { x1 = fr1; x2 = fr2; x3 = fr3; }
@@ -247,9 +278,10 @@ CF_HD CF_INLINE double sgn1(double x) { return copysign(1.0, x); }
 /* Second-order WAF (IFLUX 3, flux_riemann.cuf:720-900) for both sides.  Inputs: the
  * reconstructed, masked edge-frame states of A (left) and B (right), the upwind
  * reconstructions (h, v) of each side, dt, and the distances d_mrl, d_mkvol (A), d_mkvoisin (B). */
-CF_HD CF_INLINE void waf_flux(double g, int ilim, double nx, double ny, double dt, double d_mrl, double d_mkvol,
-                              double d_mkvoisin, double hl, double ul, double vl, double hr, double ur,
-                              double vr, double hl_upw, double vl_upw, double hr_upw, double vr_upw, TwoFlux& F) {
+CF_HD CF_INLINE void waf_flux(double g, int ilim, double nx, double ny, double dt, double d_mrl, double y_mrl,
+                              double d_mkvol, double y_mkvol, double d_mkvoisin, double y_mkvoisin, double hl,
+                              double ul, double vl, double hr, double ur, double vr, double hl_upw, double vl_upw,
+                              double hr_upw, double vr_upw, TwoFlux& F) {
   const double eps = EPS_SECOND;
   double sl, sr, set;
   if (!wave_speeds(g, eps, hl, ul, hr, ur, sl, sr, set)) {
@@ -262,28 +294,30 @@ CF_HD CF_INLINE void waf_flux(double g, int ilim, double nx, double ny, double d
   const int rb = (-sr > 0) ? 1 : ((-sl < 0) ? 0 : 2);
   double h1 = 0.0, h2 = 0.0;
   if (ra == 2 || rb == 2) {
-    h1 = (sr * fl1 - sl * fr1 + sl * sr * (hr - hl)) / (sr - sl + eps);
-    h2 = (sr * fl2 - sl * fr2 + sl * sr * (hr * ur - hl * ul)) / (sr - sl + eps);
+    const double den = sr - sl + eps, yden = 1.0 / den;
+    h1 = div_rn(sr * fl1 - sl * fr1 + sl * sr * (hr - hl), den, yden);
+    h2 = div_rn(sr * fl2 - sl * fr2 + sl * sr * (hr * ur - hl * ul), den, yden);
   }
   const double ha1 = (ra == 0) ? fl1 : ((ra == 1) ? fr1 : h1);
   const double ha2 = (ra == 0) ? fl2 : ((ra == 1) ? fr2 : h2);
   const double hb1 = (rb == 0) ? fl1 : ((rb == 1) ? fr1 : h1);
   const double hb2 = (rb == 0) ? fl2 : ((rb == 1) ? fr2 : h2);
 
-  const double dtoverdx = dt / d_mrl;
+  const double dtoverdx = div_rn(dt, d_mrl, y_mrl);
   const double cr = sr * dtoverdx, cl = sl * dtoverdx, cet = set * dtoverdx;
-  const double dloc = (hr - hl) / d_mrl;          /* delta_loc_l = delta_loc_r */
-  const double dloc_et = (vr - vl) / d_mrl;
-  const double upl = (hl - hl_upw) / d_mkvol;     /* upwind difference of side A */
-  const double upr = (hr_upw - hr) / d_mkvoisin;  /* upwind difference of side B */
-  const double upvl = (vl - vl_upw) / d_mkvol;
-  const double upvr = (vr_upw - vr) / d_mkvoisin;
+  const double dloc = div_rn(hr - hl, d_mrl, y_mrl);          /* delta_loc_l = delta_loc_r */
+  const double dloc_et = div_rn(vr - vl, d_mrl, y_mrl);
+  const double upl = div_rn(hl - hl_upw, d_mkvol, y_mkvol);     /* upwind difference of side A */
+  const double upr = div_rn(hr_upw - hr, d_mkvoisin, y_mkvoisin);  /* upwind difference of side B */
+  const double upvl = div_rn(vl - vl_upw, d_mkvol, y_mkvol);
+  const double upvr = div_rn(vr_upw - vr, d_mkvoisin, y_mkvoisin);
   const double ret_a = ((set > 0) ? upvl : upvr) / (dloc_et + eps);
 
   /* side A (:854-899) */
   {
-    const double rl = ((sl > 0) ? upl : upr) / (dloc + eps);
-    const double rr = ((sr > 0) ? upl : upr) / (dloc + eps);
+    const double den = dloc + eps, yd = 1.0 / den;
+    const double rl = div_rn((sl > 0) ? upl : upr, den, yd);
+    const double rr = div_rn((sr > 0) ? upl : upr, den, yd);
     const double ll = waf_limiter(ilim, rl, cl);
     const double lr = waf_limiter(ilim, rr, cr);
     const double le = waf_limiter(ilim, ret_a, cet);
@@ -303,9 +337,11 @@ CF_HD CF_INLINE void waf_flux(double g, int ilim, double nx, double ny, double d
    * (hl - hr)/d = -dloc, its upwind differences are minus A's (for the wave it tests), the
    * tangential ones coincide; its Courant numbers are -cr, -cl, -cet. */
   {
-    const double rl = ((-sr > 0) ? -upr : -upl) / (-dloc + eps);
-    const double rr = ((-sl > 0) ? -upr : -upl) / (-dloc + eps);
-    const double ret_b = ((-set > 0) ? upvr : upvl) / (dloc_et + eps);
+    const double den = -dloc + eps, yd = 1.0 / den;
+    const double rl = div_rn((-sr > 0) ? -upr : -upl, den, yd);
+    const double rr = div_rn((-sl > 0) ? -upr : -upl, den, yd);
+    /* B's tangential ratio differs from A's only when s* == 0 (or is NaN) */
+    const double ret_b = (set > 0 || set < 0) ? ret_a : ((-set > 0) ? upvr : upvl) / (dloc_et + eps);
     const double ll = waf_limiter(ilim, rl, -cr);
     const double lr = waf_limiter(ilim, rr, -cl);
     const double le = waf_limiter(ilim, ret_b, -cet);
@@ -393,21 +429,22 @@ CF_HD CF_INLINE void boundary_flux(int iflux, const MemberDev& M, int kind, int 
 /* Upwind reconstruction of one side (flux_riemann.cuf:240-366): a copy of one element's
  * masked state when d1 < 0 (one upwind element, or the first-order fallback), else the
  * centroid-distance weighted average of two. */
-CF_HD CF_INLINE void upwind_state(const double4* U, int i1, int i2, double d1, double d2, double nx, double ny,
-                                  double tolisec, double& hu_, double& vu_, double& zu_) {
+CF_HD CF_INLINE void upwind_state(const double4* U, int i1, int i2, double d1, double d2, double ysum, double nx,
+                                  double ny, double tolisec, double& hu_, double& vu_, double& zu_) {
   const double4 A1 = ld4(U + i1);
-  double h1, u1, v1;
-  to_frame(A1.x, A1.y, A1.z, nx, ny, tolisec, h1, u1, v1);
+  double h1, v1;
+  to_frame_t(A1.x, A1.y, A1.z, nx, ny, tolisec, h1, v1);
   if (d1 < 0.0) {
     hu_ = h1; vu_ = v1; zu_ = A1.w;
     return;
   }
   const double4 A2 = ld4(U + i2);
-  double h2, u2, v2;
-  to_frame(A2.x, A2.y, A2.z, nx, ny, tolisec, h2, u2, v2);
-  hu_ = (d1 * h1 + d2 * h2) / (d1 + d2);
-  vu_ = (d1 * v1 + d2 * v2) / (d1 + d2);
-  zu_ = (d1 * A1.w + d2 * A2.w) / (d1 + d2);
+  double h2, v2;
+  to_frame_t(A2.x, A2.y, A2.z, nx, ny, tolisec, h2, v2);
+  const double ds = d1 + d2;
+  hu_ = div_rn(d1 * h1 + d2 * h2, ds, ysum);
+  vu_ = div_rn(d1 * v1 + d2 * v2, ds, ysum);
+  zu_ = div_rn(d1 * A1.w + d2 * A2.w, ds, ysum);
 }
 
 /* ---- one edge: the body of the edge kernel ----------------------------------------------- */
@@ -466,10 +503,11 @@ CF_HD CF_INLINE void edge_body(const StepArgs& a, const MemberDev& M, int e, dou
   } else {
     const int4 up = ldro(a.eupw + e);
     const double4 dw = ld4(a.ewts + e);   /* d1, d2 of side A, d1, d2 of side B */
-    const double2 dk = ldro(a.edk + e);   /* d_mkvol, d_mkvoisin */
+    const double4 dk = ld4(a.edk + e);    /* d_mkvol, d_mkvoisin and their reciprocals */
+    const double4 yi = ld4(a.einv + e);   /* 1/d_mrl, 1/(d1+d2) of A and of B */
     double hl_upw, vl_upw, zml_upw, hr_upw, vr_upw, zmr_upw;
-    upwind_state(a.Uin, up.x, up.y, dw.x, dw.y, nx, ny, tolisec, hl_upw, vl_upw, zml_upw);
-    upwind_state(a.Uin, up.z, up.w, dw.z, dw.w, nx, ny, tolisec, hr_upw, vr_upw, zmr_upw);
+    upwind_state(a.Uin, up.x, up.y, dw.x, dw.y, yi.y, nx, ny, tolisec, hl_upw, vl_upw, zml_upw);
+    upwind_state(a.Uin, up.z, up.w, dw.z, dw.w, yi.z, nx, ny, tolisec, hr_upw, vr_upw, zmr_upw);
     /* hydrostatic reconstruction of the four states (:370-400) */
     double hijet = dmax(0.0, hautl + zml - zij);
     hl_upw = dmax(0.0, hl_upw + zml_upw - zij);
@@ -480,8 +518,8 @@ CF_HD CF_INLINE void edge_body(const StepArgs& a, const MemberDev& M, int e, dou
     if (hl_upw < tolisec) { hl_upw = 0.; vl_upw = 0.; }
     if (hjiet < tolisec) { hjiet = 0.; ur = 0.; vr = 0.; }
     if (hr_upw < tolisec) { hr_upw = 0.; vr_upw = 0.; }
-    waf_flux(g, a.ilimiteur, nx, ny, dt, geo.w, dk.x, dk.y, hijet, ul, vl, hjiet, ur, vr, hl_upw, vl_upw,
-             hr_upw, vr_upw, F);
+    waf_flux(g, a.ilimiteur, nx, ny, dt, geo.w, yi.x, dk.x, dk.z, dk.y, dk.w, hijet, ul, vl, hjiet, ur, vr, hl_upw,
+             vl_upw, hr_upw, vr_upw, F);
   }
   if (a.flux_mode == 1) {
     F.b1 = -F.a1;
@@ -514,7 +552,8 @@ CF_HD CF_INLINE void edge_body(const StepArgs& a, const MemberDev& M, int e, dou
 CF_HD CF_INLINE double cfl_dt_elem(const MemberDev& M, double cflL, double h, double hu, double hv) {
   double d = 1000000.0;
   if (h > M.tolisec) {
-    const double vu = hu / h, vv = hv / h;
+    const double yh = 1.0 / h;
+    const double vu = div_rn(hu, h, yh), vv = div_rn(hv, h, yh);
     const double nv = sqrt(vu * vu + vv * vv);
     const double vmax = dmax(0.01, nv + sqrt(M.gp * fabs(h)));
     d = dmin(cflL / vmax, 1000000.0);
@@ -524,7 +563,7 @@ CF_HD CF_INLINE double cfl_dt_elem(const MemberDev& M, double cflL, double h, do
 }
 
 /* Sources, friction and update of element c (source_terms.cuf:33-211,
- * finite_volumes_method.cuf:283-303).  st = {area, manning n, cfl*L_cfl, -}.  Returns the
+ * finite_volumes_method.cuf:283-303).  st = {area, manning n, cfl*L_cfl, 1/area}.  Returns the
  * new state; sets *nonfinite when it is not finite. */
 CF_HD CF_INLINE double4 element_update(const MemberDev& M, const double4 U, const double4 st, const Slot& s0,
                                        const Slot& s1, const Slot& s2, double dt, bool& nonfinite) {
@@ -542,29 +581,32 @@ CF_HD CF_INLINE double4 element_update(const MemberDev& M, const double4 U, cons
     double sf2 = 0., sf3 = 0.;
     double m4 = 0., m5 = 1., m6 = 0., m7 = 0., m8 = 0., m9 = 1.;
     if (q1 > tolisec) {
-      const double vitu = q2 / q1, vitv = q3 / q1;
+      const double yq = 1.0 / q1;
+      const double vitu = div_rn(q2, q1, yq), vitv = div_rn(q3, q1, yq);
       double normvit = sqrt(vitu * vitu + vitv * vitv);
       if (normvit < tol) normvit = tol;
       const double p13 = 1.0 / cbrt_halley(q1);    /* q1**(-1/3) */
       sf2 = -(gp * manning * manning * vitu * normvit * area * p13);
       sf3 = -(gp * manning * manning * vitv * normvit * area * p13);
       if (normvit > tol) {
-        const double p43 = p13 / q1;                /* q1**(-4/3) */
+        const double p43 = div_rn(p13, q1, yq);     /* q1**(-4/3) */
         if (M.fricimplic == 1) {
+          const double yn = 1.0 / normvit;
           const double dtgn2h = dt / 2.0 * gp * manning * manning * p43;
           const double af21 = -(7.0 / 3.0 * dtgn2h * vitu * normvit);
-          const double af22 = 1.0 + dtgn2h * (2 * (vitu * vitu) + vitv * vitv) / normvit;
-          const double af23 = dtgn2h * vitu * vitv / normvit;
+          const double af22 = 1.0 + div_rn(dtgn2h * (2 * (vitu * vitu) + vitv * vitv), normvit, yn);
+          const double af23 = div_rn(dtgn2h * vitu * vitv, normvit, yn);
           const double af31 = -(7.0 / 3.0 * dtgn2h * vitv * normvit);
           const double af32 = af23;
-          const double af33 = 1.0 + dtgn2h * (vitu * vitu + 2 * (vitv * vitv)) / normvit;
+          const double af33 = 1.0 + div_rn(dtgn2h * (vitu * vitu + 2 * (vitv * vitv)), normvit, yn);
           const double detaf = af22 * af33 - af23 * af32;
-          m4 = -(af21 * af33 - af23 * af31) / detaf;
-          m5 = af33 / detaf;
-          m6 = -af23 / detaf;
-          m7 = (af21 * af32 - af22 * af31) / detaf;
-          m8 = -af32 / detaf;
-          m9 = af22 / detaf;
+          const double yd = 1.0 / detaf;
+          m4 = div_rn(-(af21 * af33 - af23 * af31), detaf, yd);
+          m5 = div_rn(af33, detaf, yd);
+          m6 = div_rn(-af23, detaf, yd);
+          m7 = div_rn(af21 * af32 - af22 * af31, detaf, yd);
+          m8 = div_rn(-af32, detaf, yd);
+          m9 = div_rn(af22, detaf, yd);
         } else if (M.fricimplic == 2) {
           const double beta = -(dt * gp * manning * manning * normvit * p43);
           const double detaf = (1 - beta) * (1 - beta);
@@ -573,9 +615,9 @@ CF_HD CF_INLINE double4 element_update(const MemberDev& M, const double4 U, cons
         }
       }
     }
-    const double ri1 = (0. + 0. - rc1) / area;
-    const double ri2 = (sb2 + sf2 - rc2) / area;
-    const double ri3 = (sb3 + sf3 - rc3) / area;
+    const double ri1 = div_rn(0. + 0. - rc1, area, st.w);
+    const double ri2 = div_rn(sb2 + sf2 - rc2, area, st.w);
+    const double ri3 = div_rn(sb3 + sf3 - rc3, area, st.w);
     if (M.fricimplic == 1 || M.fricimplic == 2) {
       r1 = 1. * ri1 + 0. * ri2 + 0. * ri3;
       r2 = m4 * ri1 + m5 * ri2 + m6 * ri3;
@@ -586,9 +628,9 @@ CF_HD CF_INLINE double4 element_update(const MemberDev& M, const double4 U, cons
       r3 = ri3;
     }
   } else {
-    r1 = (0. - rc1) / area;
-    r2 = (sb2 - rc2) / area;
-    r3 = (sb3 - rc3) / area;
+    r1 = div_rn(0. - rc1, area, st.w);
+    r2 = div_rn(sb2 - rc2, area, st.w);
+    r3 = div_rn(sb3 - rc3, area, st.w);
   }
   double h = q1 + dt * r1, hu = q2 + dt * r2, hv = q3 + dt * r3;
   nonfinite = !(finite_bits(h) && finite_bits(hu) && finite_bits(hv));

@@ -5,13 +5,14 @@
  * Device layout (all arrays in space-filling-curve order, see cf_mesh.cpp):
  *   cells  U[2]  : double4 {h, hu, hv, z} per element, ping-pong (state n in U[n & 1])
  *          cslot : int4 {slot of local edge 0, 1, 2, -}   (local edges in the reference's order)
- *          cstat : double4 {area, Manning n, cfl*L_cfl, -}
+ *          cstat : double4 {area, Manning n, cfl*L_cfl, RN(1/area)}
  *   edges  ecell : int2 {A, B}; B >= 0 another element, B < 0 the boundary kind (-1/-2/-3)
  *          egeo  : double4 {nx, ny, len, d_AB}, normal pointing out of A, centroid distance
  *          ebid  : int32 inlet/outlet number of a boundary edge
  *          eupw  : int4 {A-side upwind 1, 2, B-side upwind 1, 2}          (second order only)
  *          ewts  : double4 {A distances d1, d2, B distances d1, d2}; d1 < 0: copy element 1
- *          edk   : double2 {d_mkvol, d_mkvoisin}                         (second order only)
+ *          edk   : double4 {d_mkvol, d_mkvoisin, RN(1/d_mkvol), RN(1/d_mkvoisin)}  (second order)
+ *          einv  : double4 {RN(1/d_AB), RN(1/(d1+d2)) of A, of B, -}          (second order only)
  *   slots  Slot  : 48 bytes per (edge, side): flux*len of that side's own evaluation and
  *                  the bed-slope source of that side.  Slot 2e is side A, 2e+1 side B.
  * Several independent simulations ("members") can share one flat cell/edge space; each
@@ -86,7 +87,8 @@ struct StepArgs {
   const int32_t* ebid;
   const int4* eupw;
   const double4* ewts;
-  const double2* edk;
+  const double4* edk;
+  const double4* einv;
   Slot* slots;
   const int32_t* etile_mem;
   const int32_t* ctile_mem;
@@ -126,7 +128,8 @@ struct Prep {
   std::vector<int32_t> ebid;
   std::vector<int4> eupw;
   std::vector<double4> ewts;
-  std::vector<double2> edk;
+  std::vector<double4> edk;
+  std::vector<double4> einv;
 };
 
 /* Build every host table from the reference mesh inputs.  Returns CF_OK or CF_EINVAL with a

@@ -247,7 +247,7 @@ int prepare_mesh(const cf_mesh* m, const cf_params* p, Prep& P, std::string& err
   for (int c = 0; c < n; ++c) {
     int o = P.perm[c];
     double man = p->is_override_manning ? p->override_manning : m->manning_elt[o];
-    P.cstat[c] = make_double4(P.area[o], man, p->cfl * P.cotemin[o], 0.0);
+    P.cstat[c] = make_double4(P.area[o], man, p->cfl * P.cotemin[o], 1.0 / P.area[o]);
     P.zcell[c] = P.zm[o];
   }
   auto set_slot = [&](int c, int k, int s) {
@@ -270,7 +270,7 @@ int prepare_mesh(const cf_mesh* m, const cf_params* p, Prep& P, std::string& err
   P.ecell.resize(ne);
   P.egeo.resize(ne);
   P.ebid.resize(ne);
-  if (second) { P.eupw.resize(ne); P.ewts.resize(ne); P.edk.resize(ne); }
+  if (second) { P.eupw.resize(ne); P.ewts.resize(ne); P.edk.resize(ne); P.einv.resize(ne); }
   auto cdist = [&](int oa, int ob) {
     return std::sqrt((P.xc[oa] - P.xc[ob]) * (P.xc[oa] - P.xc[ob]) + (P.yc[oa] - P.yc[ob]) * (P.yc[oa] - P.yc[ob]));
   };
@@ -319,7 +319,9 @@ int prepare_mesh(const cf_mesh* m, const cf_params* p, Prep& P, std::string& err
         }
         P.eupw[e] = make_int4(P.iperm[ua1], P.iperm[ua2], P.iperm[ub1], P.iperm[ub2]);
         P.ewts[e] = make_double4(da1, da2, db1, db2);
-        P.edk[e] = make_double2(dka, dkb);
+        P.edk[e] = make_double4(dka, dkb, 1.0 / dka, 1.0 / dkb);
+        /* reciprocals of the sums the weighted averages divide by (copies divide by nothing) */
+        P.einv[e] = make_double4(1.0 / dmrl, da1 < 0.0 ? 0.0 : 1.0 / (da1 + da2), db1 < 0.0 ? 0.0 : 1.0 / (db1 + db2), 0.0);
       }
     } else {
       P.ecell[e] = make_int2(E.a, E.b);
@@ -327,7 +329,8 @@ int prepare_mesh(const cf_mesh* m, const cf_params* p, Prep& P, std::string& err
       if (second) {
         P.eupw[e] = make_int4(E.a, E.a, E.a, E.a);
         P.ewts[e] = make_double4(-1.0, 0.0, -1.0, 0.0);
-        P.edk[e] = make_double2(0.0, 0.0);
+        P.edk[e] = make_double4(0.0, 0.0, 0.0, 0.0);
+        P.einv[e] = make_double4(0.0, 0.0, 0.0, 0.0);
       }
     }
     P.egeo[e] = make_double4(n1, n2, ln, inv_d);

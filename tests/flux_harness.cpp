@@ -41,6 +41,7 @@ extern "C" int harness_edge_fluxes(const cf_mesh* m, const cf_params* p, const d
   a.eupw = P.eupw.empty() ? nullptr : P.eupw.data();
   a.ewts = P.ewts.empty() ? nullptr : P.ewts.data();
   a.edk = P.edk.empty() ? nullptr : P.edk.data();
+  a.einv = P.einv.empty() ? nullptr : P.einv.data();
   a.slots = slots.data();
   a.iflux = p->iflux; a.ilimiteur = p->ilimiteur; a.flux_mode = p->flux_mode;
   for (int e = 0; e < ne; ++e) {
@@ -94,6 +95,7 @@ extern "C" int harness_run(const cf_mesh* m, const cf_params* p, const double* U
   a.eupw = P.eupw.empty() ? nullptr : P.eupw.data();
   a.ewts = P.ewts.empty() ? nullptr : P.ewts.data();
   a.edk = P.edk.empty() ? nullptr : P.edk.data();
+  a.einv = P.einv.empty() ? nullptr : P.einv.data();
   a.slots = slots.data();
   a.iflux = p->iflux; a.ilimiteur = p->ilimiteur; a.flux_mode = p->flux_mode;
   double4* cur = Ua.data();
@@ -128,4 +130,35 @@ extern "C" int harness_run(const cf_mesh* m, const cf_params* p, const double* U
   }
   if (t_out) *t_out = t;
   return rc;
+}
+
+/* div_rn (Markstein's correction with y = RN(1/d)) against the IEEE quotient on n samples of
+ * adversarial operands: random exponents over 2^[-70, 50) / 2^[-30, 30), all-ones and
+ * near-all-ones significands, powers of two, a close to d, exact multiples, signed zeros.
+ * Returns the number of bitwise mismatches. */
+extern "C" long long harness_div_check(long long n, unsigned long long seed) {
+  unsigned long long s = seed | 1;
+  auto rnd = [&]() { s ^= s << 13; s ^= s >> 7; s ^= s << 17; return s; };
+  auto mk = [](unsigned long long sign, int exp, unsigned long long mant) {
+    unsigned long long b = (sign << 63) | ((unsigned long long)(exp + 1023) << 52) | (mant & ((1ull << 52) - 1));
+    double x;
+    memcpy(&x, &b, 8);
+    return x;
+  };
+  long long bad = 0;
+  for (long long i = 0; i < n; ++i) {
+    unsigned long long r1 = rnd(), r2 = rnd(), md = rnd(), ma = rnd();
+    int ed = (int)(r1 % 60) - 30, ea = (int)((r1 >> 8) % 120) - 70, mode = (int)((r2 >> 3) % 9);
+    if (mode == 0) md = (1ull << 52) - 1;
+    if (mode == 1) md = (1ull << 52) - 1 - (rnd() % 16);
+    if (mode == 2) ma = md;
+    if (mode == 3) md = 0;
+    if (mode == 4) ma = (1ull << 52) - 1;
+    double d = mk(r2 >> 63, ed, md), a = mk(r2 & 1, ea, ma);
+    if (mode == 5) a = d * (double)(rnd() % 1000);
+    if (mode == 6) a = (r2 & 2) ? -0.0 : 0.0;
+    const double got = div_rn(a, d, 1.0 / d), ref = a / d;
+    if (memcmp(&got, &ref, 8) != 0) ++bad;
+  }
+  return bad;
 }

@@ -8,6 +8,13 @@ import harness as H
 from cuteflow_gb300 import cases
 
 
+def test_markstein_division_is_the_ieee_quotient():
+    """The kernels replace a/d by Markstein's correction from y = RN(1/d) where 1/d is known;
+    it must be the correctly rounded quotient, bit for bit, signed zeros included."""
+    assert H.div_check(5_000_000, seed=1) == 0
+    assert H.div_check(5_000_000, seed=2) == 0
+
+
 def _state_after(oracle, case, n, params=None):
     r = oracle.run(case, n, params=params)
     return r["U"], r["dt_hist"][-1], r["t"]
