@@ -49,7 +49,7 @@ __global__ void __launch_bounds__(TILE_E) k_edges(StepArgs a) {
      * dt ends the run with the current state), the next time, and the start value of the
      * next dt minimum (cflcond sets dt_d = 1e6 and the block reduction pads a partial last
      * block with 1e5, cfl_condition.cuf:21,86). */
-    if (dt > 9999.0 || dt < DT_LOW) {
+    if (S->nstep > 0 && (dt > 9999.0 || dt < DT_LOW)) {   /* the initial dt is not tested (:113-116) */
       atomicOr(&S->status, CF_STATUS_DT_RANGE);
     } else {
       S->t[1 - p] = t + dt;

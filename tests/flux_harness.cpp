@@ -105,7 +105,7 @@ extern "C" int harness_run(const cf_mesh* m, const cf_params* p, const double* U
   if (dt_hist) dt_hist[0] = dt;
   double t = 0.0;
   for (int s = 0; s < nsteps; ++s) {
-    if (dt > 9999.0 || dt < DT_LOW) { rc = -2; break; }
+    if (s > 0 && (dt > 9999.0 || dt < DT_LOW)) { rc = -2; break; }
     a.Uin = cur;
     for (int e = 0; e < ne; ++e) {
       if (p->iflux == 1) edge_body<1>(a, M, e, dt, t);

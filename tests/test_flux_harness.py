@@ -57,6 +57,8 @@ CASES = [
     ("outlet_transm_waf", lambda: cases.flooding(40, 20, seed=9, iflux=3), 120, dict(outlet=2)),
     ("constant_dt", lambda: cases.circular_dam_break(20, 20, seed=2, iflux=1), 60, dict(is_dt_constant=1, constant_dt=0.01)),
     ("lake_wet", lambda: cases.lake_at_rest(30, 15, iflux=3), 100, {}),
+    # all dry at t=0: the first step runs with the 1e5 dt sentinel (the initial dt is not tested)
+    ("dry_start_inflow", lambda: cases.flooding(18, 9, seed=22, lx=360.0, ly=180.0, iflux=3), 60, {}),
     ("lake_islands", lambda: cases.lake_at_rest(30, 15, iflux=3, wet=False), 100, {}),
 ]
 
