@@ -2,7 +2,7 @@
 
 Kernels are compiled by nvcc for sm_103a only; the host translation units by g++ with
 -ffp-contract=off (the mesh geometry must round like a plain FP64 evaluation of the
-reference formulas).  The three units compile in parallel.
+reference formulas).  The units compile in parallel.
 """
 from __future__ import annotations
 
@@ -21,7 +21,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA_HOME, "bin", "nvcc") if os.path.exists(os.path.join(CUDA_HOME, "bin", "nvcc")) else "nvcc"
 
-CU_SOURCES = ["cf_kernels.cu"]
+CU_SOURCES = ["cf_kernels.cu", "cf_noalloc.cu"]
 CPP_SOURCES = ["cf_mesh.cpp", "cf_api.cpp"]
 HEADERS = ["cf_internal.h", "cf_flux.h"]
 

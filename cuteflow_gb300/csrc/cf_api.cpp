@@ -540,6 +540,54 @@ int step_impl(cf_ctx* c, int32_t nsteps, cf_step_info* infos) {
 
 }  // namespace
 
+/* ---- helpers of the static-scratch entry point (cf_noalloc.cu) ---------------------------- */
+
+int cf::ctx_set_device(cf_ctx* c) {
+  CF_CUDA(c, cudaSetDevice(c->device));
+  return CF_OK;
+}
+
+int cf::ctx_error(cf_ctx* c, int code, const std::string& msg) { return fail(c, code, msg); }
+
+int cf::step_with_slots(cf_ctx* c, int32_t nsteps, cf_step_info* infos, Slot* slots, size_t capacity) {
+  if (nsteps < 0) return fail(c, CF_EINVAL, "nsteps < 0");
+  const size_t need = 2 * (size_t)c->ne_pad;
+  if (need > capacity) {
+    char msg[256];
+    std::snprintf(msg, sizeof(msg),
+                  "the context needs %zu edge-flux slots (%zu bytes) but the static scratch holds %zu (%zu bytes)",
+                  need, need * sizeof(Slot), capacity, capacity * sizeof(Slot));
+    return fail(c, CF_EINVAL, msg);
+  }
+  int rc;
+  const stream_t s = reinterpret_cast<stream_t>(c->stream);
+  if (nsteps > 0) {
+    /* the scratch keeps whatever the previous call left: start from zero like a new context */
+    CF_CUDA(c, cudaMemsetAsync(slots, 0, need * sizeof(Slot), c->stream));
+    for (int32_t i = 0; i < nsteps; ++i) {
+      StepArgs a = step_args(c, (int)((c->launched + i) & 1));
+      a.slots = slots;
+      if ((rc = launch_step(a, s, nullptr, nullptr))) return fail(c, rc, "step launch failed");
+    }
+    c->launched += nsteps;
+    rc = launch_discharge(slots, c->ecell, c->mdev, c->mst, (int32_t)c->mem.size(), s);
+    if (rc != CF_OK) return fail(c, rc, "discharge launch failed");
+  }
+  c->flux_ms = c->update_ms = 0.0;
+  c->launches = 2 * (int64_t)nsteps;
+  if ((rc = read_states(c))) return rc;
+  uint32_t any = 0;
+  for (size_t i = 0; i < c->mem.size(); ++i) {
+    if (infos) fill_info(c->host_state[i], &infos[i]);
+    any |= c->host_state[i].status;
+  }
+  if (c->mem.size() == 1 && (any & STATUS_NO_STATE)) return fail(c, CF_ESTATE, "step before a state was set");
+  rc = status_code(any & ~STATUS_NO_STATE);
+  if (rc != CF_OK)
+    return fail(c, rc, rc == CF_EDT ? "dt left the range (1e-12, 9999]" : "non-finite value in the state");
+  return CF_OK;
+}
+
 extern "C" {
 
 int cf_default_params(cf_params* p) {

@@ -152,6 +152,14 @@ int launch_scatter_state(const double* hu3, const int32_t* perm_new2old, const d
 int launch_gather_state(const double4* U, const int32_t* iperm_old2new, double* hu3, int32_t n,
                         stream_t s);
 
+/* ---- context helpers for the static-scratch entry point (cf_api.cpp) ---------------- */
+
+int ctx_set_device(cf_ctx* c);                                /* the context's device current */
+int ctx_error(cf_ctx* c, int code, const std::string& msg);  /* record msg, return code */
+/* The steps of cf_step with the edge-flux slots at `slots` (room for `capacity` slots) in
+ * place of the context's own slot buffer: direct launches, no graph, no allocation. */
+int step_with_slots(cf_ctx* c, int32_t nsteps, cf_step_info* infos, Slot* slots, size_t capacity);
+
 }  // namespace cf
 
 #endif

@@ -53,6 +53,7 @@ def load(build_if_missing: bool = True):
     L.cf_set_state_device.argtypes = [vp, vp, C.c_double]
     L.cf_set_initial_condition.argtypes = [vp, C.POINTER(_abi.CfIc), C.c_double]
     L.cf_step.argtypes = [vp, C.c_int32, C.POINTER(_abi.CfStepInfo)]
+    L.cf_step_noalloc.argtypes = [vp, C.c_int32, C.POINTER(_abi.CfStepInfo)]
     L.cf_get_state.argtypes = [vp, dp]
     L.cf_get_state_device.argtypes = [vp, vp]
     L.cf_get_info.argtypes = [vp, C.POINTER(_abi.CfStepInfo)]
@@ -77,7 +78,7 @@ def load(build_if_missing: bool = True):
                  "cf_member_get_state", "cf_member_get_info", "cf_member_get_mesh_tables"):
         getattr(L, name).restype = C.c_int
     for name in ("cf_default_params", "cf_create", "cf_set_state", "cf_set_state_device",
-                 "cf_set_initial_condition", "cf_step", "cf_get_state", "cf_get_state_device",
+                 "cf_set_initial_condition", "cf_step", "cf_step_noalloc", "cf_get_state", "cf_get_state_device",
                  "cf_get_info", "cf_get_mesh_tables", "cf_mesh_tables", "cf_get_sizes", "cf_set_timing", "cf_get_timing"):
         getattr(L, name).restype = C.c_int
     _lib = L

@@ -200,6 +200,36 @@ const char* cf_last_error(const cf_ctx* ctx);
 int cf_set_timing(cf_ctx* ctx, int32_t enable);
 int cf_get_timing(cf_ctx* ctx, double* flux_ms, double* update_ms, int64_t* launches);
 
+/* ---- stepping without allocation (no counterpart in the reference) --------------------
+ *
+ * For callers that may not allocate device memory once their time loop runs: a coupled host
+ * model whose GPU memory is budgeted among its components at start-up, or a process under a
+ * fixed device-memory limit (a CUDA MPS client limit) where an allocation in mid-run could
+ * fail and lose the simulation.  cf_step allocates nothing per step either, but on its first
+ * call with two or more steps it instantiates a CUDA graph, which takes resources of its own.
+ *
+ * cf_step_noalloc advances exactly like cf_step (same kernels, bit-identical results), with
+ * two differences: it launches the kernels one by one, and the per-edge flux slots that the
+ * edge kernel hands to the element kernel live in one fixed array inside the library
+ * (CF_NOALLOC_SCRATCH_SLOTS slots of 48 bytes, 16 MiB, held on every GPU that loads the
+ * library until the process exits) instead of the context's buffer.  It calls no cudaMalloc,
+ * cudaFree or allocating library routine.
+ *   - Limit: contexts whose edges need at most CF_NOALLOC_SCRATCH_SLOTS slots (two per edge,
+ *     each member's edges rounded up to a multiple of 128): about 116,000 triangles in one
+ *     member.  A larger context is rejected with CF_EINVAL, the sizes in cf_last_error, and
+ *     nothing is launched.
+ *   - The first call on a device sets up that device's address of the array (which can load
+ *     the library's device code there); make that first call before any stream capture.
+ *   - Every call on a device shares the one array, which keeps the last call's contents; a
+ *     call clears the part it uses before its first step.  Calls whose work overlaps on the
+ *     GPU (contexts stepped at the same time from several host threads) race on the array:
+ *     serialise them.  A call returns after its work has finished, so calls from one host
+ *     thread never overlap.
+ *   - Kernel timing is not collected (cf_get_timing reports zero times); a member whose
+ *     status was already set before the call reports q_in = q_out = 0. */
+#define CF_NOALLOC_SCRATCH_SLOTS 349525
+int cf_step_noalloc(cf_ctx* ctx, int32_t nsteps, cf_step_info* info);
+
 #ifdef __cplusplus
 }
 #endif
