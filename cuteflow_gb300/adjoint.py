@@ -1,0 +1,169 @@
+"""Discrete adjoint of the step for Manning calibration (cf_adjoint_* of the C ABI).
+
+``Adjoint`` runs N steps from a Solver's current state, records the gauge elevations
+eta[k, g] = h + z after every step and the dt sequence, and returns the gradient of
+
+    J = sum_k sum_g w_eta[k, g] * eta[k, g] + sum_e w_state[e, :] . U^N[e, :]
+
+with respect to the initial state and the per-element Manning n, with every step's dt held at
+its recorded value.  ``gauge_run`` exposes the same run as a ``torch.autograd.Function`` of
+(manning, U0) returning (eta, U^N) on the GPU.
+
+Calibration tooling of the reference samples Manning fields and runs independent forwards; it
+has no gradients.  This module has no CPU fallback: without the CUDA library the calls raise.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import Optional, Tuple
+
+import numpy as np
+
+from .solver import CFError, Solver, load
+
+
+def _ptr(a) -> C.c_void_p:
+    if a is None:
+        return C.c_void_p()
+    if isinstance(a, int):
+        return C.c_void_p(a)
+    if hasattr(a, "data_ptr"):           # torch tensor
+        return C.c_void_p(a.data_ptr())
+    return a.ctypes.data_as(C.c_void_p)  # numpy array
+
+
+class Adjoint:
+    """Adjoint of ``nsteps`` steps of ``solver`` (a one-member context) with gauge elements
+    ``gauges`` (0-based, reference order).  ``checkpoint_interval`` 0 keeps ceil(sqrt(N))."""
+
+    def __init__(self, solver: Solver, nsteps: int, gauges, checkpoint_interval: int = 0):
+        self._L = load()
+        self.solver = solver
+        self.nsteps = int(nsteps)
+        self.gauges = np.ascontiguousarray(gauges, dtype=np.int32).ravel()
+        self._h = C.c_void_p()
+        rc = self._L.cf_adjoint_create(solver._ctx, self.nsteps, int(checkpoint_interval),
+                                       self.gauges.ctypes.data_as(C.POINTER(C.c_int32)), int(self.gauges.size),
+                                       C.byref(self._h))
+        solver._check(rc)
+        k, g = C.c_int32(), C.c_int32()
+        b = C.c_int64()
+        self._L.cf_adjoint_sizes(self._h, None, C.byref(k), C.byref(g), C.byref(b))
+        self.checkpoint_interval = int(k.value)
+        self.device_bytes = int(b.value)
+        self.generation = 0
+
+    @property
+    def ngauges(self) -> int:
+        return int(self.gauges.size)
+
+    def close(self):
+        if self._h:
+            self._L.cf_adjoint_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def forward(self, replay: bool = False, eta=None, state=None) -> Tuple[np.ndarray, np.ndarray]:
+        """Run; returns (eta [N, G], U^N [nelt, 3]) as numpy arrays, or fills the given
+        buffers (numpy arrays, torch tensors or device addresses) and returns them."""
+        ret_e = np.empty((self.nsteps, self.ngauges)) if eta is None else eta
+        ret_s = np.empty((self.solver.nelt, 3)) if state is None else state
+        self.solver._check(self._L.cf_adjoint_forward(self._h, 1 if replay else 0, _ptr(ret_e), _ptr(ret_s)))
+        self.generation += 1
+        return ret_e, ret_s
+
+    def backward(self, w_eta=None, w_state=None, g_state0=None, g_manning=None):
+        """Gradient of the last forward run: returns (dJ/dU0 [nelt, 3], dJ/dn [nelt])."""
+        if w_eta is not None and not isinstance(w_eta, int) and not hasattr(w_eta, "data_ptr"):
+            w_eta = np.ascontiguousarray(w_eta, dtype=np.float64)
+            assert w_eta.size == self.nsteps * self.ngauges
+        if w_state is not None and not isinstance(w_state, int) and not hasattr(w_state, "data_ptr"):
+            w_state = np.ascontiguousarray(w_state, dtype=np.float64)
+            assert w_state.size == 3 * self.solver.nelt
+        gs = np.empty((self.solver.nelt, 3)) if g_state0 is None else g_state0
+        gm = np.empty(self.solver.nelt) if g_manning is None else g_manning
+        self.solver._check(self._L.cf_adjoint_backward(self._h, _ptr(w_eta), _ptr(w_state), _ptr(gs), _ptr(gm)))
+        return gs, gm
+
+    def dt_history(self) -> Tuple[np.ndarray, np.ndarray]:
+        dt, t = np.empty(self.nsteps), np.empty(self.nsteps)
+        self.solver._check(self._L.cf_adjoint_get_dt(self._h, _ptr(dt), _ptr(t)))
+        return dt, t
+
+    def set_dt_history(self, dt, t):
+        dt = np.ascontiguousarray(dt, dtype=np.float64)
+        t = np.ascontiguousarray(t, dtype=np.float64)
+        assert dt.size == self.nsteps and t.size == self.nsteps
+        self.solver._check(self._L.cf_adjoint_set_dt(self._h, _ptr(dt), _ptr(t)))
+
+
+def _torch_function():
+    import torch
+
+    class GaugeRun(torch.autograd.Function):
+        """(manning [nelt], U0 [nelt, 3]) -> (eta [N, G], U^N [nelt, 3]) on the GPU, float64."""
+
+        @staticmethod
+        def forward(ctx, manning, U0, adj: Adjoint, t0: float, replay: bool):
+            for x in (manning, U0):
+                if x.dtype != torch.float64 or not x.is_cuda or not x.is_contiguous():
+                    raise CFError(-1, "manning and U0 must be contiguous float64 CUDA tensors")
+            torch.cuda.current_stream().synchronize()
+            s = adj.solver
+            s.set_manning(int(manning.data_ptr()))
+            s.set_state_device(int(U0.data_ptr()), t0)
+            eta = torch.empty((adj.nsteps, adj.ngauges), dtype=torch.float64, device=U0.device)
+            UN = torch.empty_like(U0)
+            adj.forward(replay=replay, eta=eta, state=UN)
+            ctx.adj = adj
+            ctx.generation = adj.generation
+            return eta, UN
+
+        @staticmethod
+        def backward(ctx, g_eta, g_UN):
+            adj: Adjoint = ctx.adj
+            if adj.generation != ctx.generation:
+                raise CFError(-6, "the adjoint has run another forward since this one; "
+                                  "call backward before the next forward")
+            dev = g_eta.device if g_eta is not None else g_UN.device
+            torch.cuda.current_stream().synchronize()
+            ge = g_eta.contiguous() if g_eta is not None else None
+            gs = g_UN.contiguous() if g_UN is not None else None
+            gU0 = torch.empty((adj.solver.nelt, 3), dtype=torch.float64, device=dev)
+            gn = torch.empty(adj.solver.nelt, dtype=torch.float64, device=dev)
+            adj.backward(ge, gs, gU0, gn)
+            return gn, gU0, None, None, None
+
+    return GaugeRun
+
+
+_GaugeRun = None
+
+
+def gauge_run(adj: Adjoint, manning, U0, t0: float = 0.0, replay: bool = False):
+    """torch.autograd-aware run: returns (eta [N, G], U^N [nelt, 3]); backward gives the
+    gradients with respect to manning and U0 through the discrete adjoint (dt frozen)."""
+    global _GaugeRun
+    if _GaugeRun is None:
+        _GaugeRun = _torch_function()
+    return _GaugeRun.apply(manning, U0, adj, float(t0), bool(replay))
+
+
+def zone_gradient(g_manning: np.ndarray, zones: np.ndarray, nzones: Optional[int] = None) -> np.ndarray:
+    """dJ/d(zone value) for a Manning field that is piecewise constant over zones: the sum of
+    the per-element gradients of each zone, in element order (deterministic)."""
+    nz = int(zones.max()) + 1 if nzones is None else nzones
+    out = np.zeros(nz)
+    np.add.at(out, zones, g_manning)
+    return out

@@ -1,0 +1,327 @@
+/*
+ * cf_adjoint.cu -- sm_103a kernels of the discrete adjoint of the step (dt of every step frozen).
+ *
+ * The step maps U^n to U^{n+1} in two stages: every edge computes the slot values of its two
+ * sides (flux * len and bed source) from the states of its elements (and, second order, of
+ * their upwind elements); every element then combines its state, the sums of its three slots
+ * and its Manning n.  The adjoint runs the stages backwards:
+ *
+ *   k_rep_edges  : the edge stage at U^n (the slot values the element stage needs),
+ *   k_adj_cells  : per element, the transposed local Jacobian of the element stage applied to
+ *                  lambda^{n+1}: the element's own part of lambda^n, the adjoint of its slot
+ *                  sums (mu for the fluxes, nu for the bed source) and dJ/dn += .. ,
+ *   k_adj_edges  : per edge, the transposed Jacobian of the edge stage applied to the mu, nu
+ *                  of its two elements: one contribution per side (and per upwind element),
+ *   k_adj_gather : per element, lambda^n = own part + the contributions of its three slots
+ *                  + those of the edges it is an upwind element of + the objective's weight
+ *                  on the gauges it carries, in a fixed order (deterministic, no atomics).
+ *
+ * The local Jacobians come from the step's own arithmetic (cf_flux.h) instantiated on
+ * Dual<D> numbers, whose value lane repeats the forward's IEEE operations, so every branch
+ * (wet/dry masks, hydrostatic reconstruction, wave regions, limiter cases, friction
+ * floors, the wet/dry clamp of the update) is the one the forward took.  The D derivative
+ * lanes are run in chunks over the 6 (first order) or 10 (WAF: + the upwind reconstructions)
+ * inputs of an edge and the 9 inputs of an element; D is a compile-time choice that trades
+ * registers for repeated value lanes.
+ *
+ * Replay kernels (k_rep_edges, k_rep_cells) advance a state with a recorded dt / time
+ * sequence; they run the step's own edge_body / element_update, so a replayed trajectory is
+ * bit-identical to the recorded one.
+ */
+#include <cuda_runtime.h>
+
+#include "cf_dual.h"
+
+namespace cf {
+namespace {
+
+__device__ __forceinline__ Slot load_slot_adj(const Slot* p) {
+  const double2* q = reinterpret_cast<const double2*>(p);
+  const double2 a = __ldg(q), b = __ldg(q + 1), c = __ldg(q + 2);
+  Slot s;
+  s.f1 = a.x; s.f2 = a.y; s.f3 = b.x; s.bx = b.y; s.by = c.x; s.q = c.y;
+  return s;
+}
+
+/* Dual<D> for input k of the lane chunk starting at base */
+template <int D>
+__device__ __forceinline__ Dual<D> seed(double v, int k, int base) {
+  Dual<D> r(v);
+#pragma unroll
+  for (int i = 0; i < D; ++i) r.d[i] = (k - base == i) ? 1.0 : 0.0;
+  return r;
+}
+
+/* ---- replay of the forward -------------------------------------------------------------- */
+
+template <int IFLUX>
+__global__ void __launch_bounds__(TILE_E) k_rep_edges(StepArgs a, const double* dt_hist, const double* t_hist, int n) {
+  const int tile = blockIdx.x;
+  const MemberDev& M = a.mdev[__ldg(a.etile_mem + tile)];
+  const int e = tile * TILE_E + threadIdx.x;
+  if (e >= M.edge_end) return;
+  edge_body<IFLUX>(a, M, e, __ldg(dt_hist + n), __ldg(t_hist + n));
+}
+
+__global__ void __launch_bounds__(TILE_C) k_rep_cells(StepArgs a, const double* dt_hist, int n, uint32_t* flag) {
+  const int tile = blockIdx.x;
+  const MemberDev& M = a.mdev[__ldg(a.ctile_mem + tile)];
+  const int c = tile * TILE_C + threadIdx.x;
+  if (c >= M.cell_end) return;
+  const double dt = __ldg(dt_hist + n);
+  const double4 U = ld4(a.Uin + c);
+  const double4 st = ld4(a.cstat + c);
+  const int4 sl = __ldg(a.cslot + c);
+  bool nonfinite = false;
+  const double4 V = element_update(M, U, st, load_slot_adj(a.slots + sl.x), load_slot_adj(a.slots + sl.y),
+                                   load_slot_adj(a.slots + sl.z), dt, nonfinite);
+  if (nonfinite) atomicOr(flag, CF_STATUS_NONFINITE);
+  double4* o = a.Uout + c;
+  reinterpret_cast<double2*>(o)[0] = make_double2(V.x, V.y);
+  reinterpret_cast<double2*>(o)[1] = make_double2(V.z, V.w);
+}
+
+/* After step n: the gauge elevations h + z of the new state and, when recording, the dt and
+ * start time of the step (read from the member record of parity p). */
+__global__ void k_record(const double4* Unew, const MemberState* S, int p, int n, double* dt_hist, double* t_hist,
+                         const int32_t* gcell, int G, double* eta) {
+  for (int g = threadIdx.x; g < G; g += blockDim.x) {
+    const double4 u = Unew[gcell[g]];
+    eta[(size_t)n * G + g] = u.x + u.w;
+  }
+  if (S && threadIdx.x == 0) {
+    dt_hist[n] = S->dt[p];
+    t_hist[n] = S->t[p];
+  }
+}
+
+/* ---- adjoint of the element stage --------------------------------------------------------- */
+
+template <int D>
+__global__ void __launch_bounds__(TILE_C) k_adj_cells(AdjArgs A) {
+  const StepArgs& a = A.s;
+  const int tile = blockIdx.x;
+  const MemberDev& M = a.mdev[__ldg(a.ctile_mem + tile)];
+  const int c = tile * TILE_C + threadIdx.x;
+  if (c >= M.cell_end) return;
+  const double dt = __ldg(A.dt_hist + A.n);
+  const double4 U = ld4(a.Uin + c);
+  const double4 st = ld4(a.cstat + c);
+  const int4 sl = __ldg(a.cslot + c);
+  const Slot s0 = load_slot_adj(a.slots + sl.x), s1 = load_slot_adj(a.slots + sl.y), s2 = load_slot_adj(a.slots + sl.z);
+  const double rc1 = s0.f1 + s1.f1 + s2.f1;
+  const double rc2 = s0.f2 + s1.f2 + s2.f2;
+  const double rc3 = s0.f3 + s1.f3 + s2.f3;
+  const double sb2 = s0.bx + s1.bx + s2.bx;
+  const double sb3 = s0.by + s1.by + s2.by;
+  const double4 L = ld4(A.lam_in + c);
+  double g[9];
+#pragma unroll
+  for (int base = 0; base < 9; base += D) {
+    Dual<D> h, hu, hv;
+    bool nf;
+    element_core(M, st.x, st.w, seed<D>(st.y, 8, base), seed<D>(U.x, 0, base), seed<D>(U.y, 1, base),
+                 seed<D>(U.z, 2, base), seed<D>(rc1, 3, base), seed<D>(rc2, 4, base), seed<D>(rc3, 5, base),
+                 seed<D>(sb2, 6, base), seed<D>(sb3, 7, base), dt, h, hu, hv, nf);
+#pragma unroll
+    for (int i = 0; i < D; ++i)
+      if (base + i < 9) g[base + i] = L.x * h.d[i] + L.y * hu.d[i] + L.z * hv.d[i];
+  }
+  A.lam_out[c] = make_double4(g[0], g[1], g[2], 0.0);
+  Slot w;
+  w.f1 = g[3]; w.f2 = g[4]; w.f3 = g[5]; w.bx = g[6]; w.by = g[7]; w.q = 0.0;
+  A.cadj[c] = w;
+  A.gman[c] += g[8];
+}
+
+/* ---- adjoint of the edge stage ---------------------------------------------------------- */
+
+/* lambda contributions of one upwind pair (U_i1, U_i2 -> the side's (h, v) reconstruction)
+ * given the adjoints wh, wv of that reconstruction. */
+__device__ __forceinline__ void upwind_chain(const double4* U, int i1, int i2, double d1, double d2, double ysum,
+                                             double nx, double ny, double tolisec, double wh, double wv, double4* o1,
+                                             double4* o2) {
+  const double4 A1 = ld4(U + i1);
+  const double4 A2 = (d1 < 0.0) ? make_double4(0.0, 0.0, 0.0, 0.0) : ld4(U + i2);
+  Dual<6> hu_, vu_;
+  upwind_mix(Dual<6>::var(A1.x, 0), Dual<6>::var(A1.y, 1), Dual<6>::var(A1.z, 2), Dual<6>::var(A2.x, 3),
+             Dual<6>::var(A2.y, 4), Dual<6>::var(A2.z, 5), d1, d2, ysum, nx, ny, tolisec, hu_, vu_);
+  *o1 = make_double4(wh * hu_.d[0] + wv * vu_.d[0], wh * hu_.d[1] + wv * vu_.d[1], wh * hu_.d[2] + wv * vu_.d[2], 0.0);
+  *o2 = make_double4(wh * hu_.d[3] + wv * vu_.d[3], wh * hu_.d[4] + wv * vu_.d[4], wh * hu_.d[5] + wv * vu_.d[5], 0.0);
+}
+
+template <int IFLUX, int D>
+__global__ void __launch_bounds__(TILE_E) k_adj_edges(AdjArgs A) {
+  const StepArgs& a = A.s;
+  const int tile = blockIdx.x;
+  const MemberDev& M = a.mdev[__ldg(a.etile_mem + tile)];
+  const int e = tile * TILE_E + threadIdx.x;
+  if (e >= M.edge_end) return;
+  const double dt = __ldg(A.dt_hist + A.n), t = __ldg(A.t_hist + A.n);
+  const int2 ab = ldro(a.ecell + e);
+  const double4 UA = ld4(a.Uin + ab.x);
+  const Slot wa = A.cadj[ab.x];
+
+  if (ab.y < 0) {
+    const double4 geo = ld4(a.egeo + e);
+    const int id = ldro(a.ebid + e);
+    Dual<3> f1, f2, f3, q;
+    boundary_flux(IFLUX, M, ab.y, id, t, geo.x, geo.y, Dual<3>::var(UA.x, 0), Dual<3>::var(UA.y, 1),
+                  Dual<3>::var(UA.z, 2), UA.w, f1, f2, f3, q);
+    const double len = geo.z;
+    double o[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) o[i] = (wa.f1 * f1.d[i] + wa.f2 * f2.d[i] + wa.f3 * f3.d[i]) * len;
+    A.eadj[2 * (size_t)e] = make_double4(o[0], o[1], o[2], 0.0);
+    return;
+  }
+
+  const double4 UB = ld4(a.Uin + ab.y);
+  const Slot wb = A.cadj[ab.y];
+  const EdgeGeo G = edge_geo(a, e, IFLUX >= 3);
+  double hl_upw = 0.0, vl_upw = 0.0, zl_upw = 0.0, hr_upw = 0.0, vr_upw = 0.0, zr_upw = 0.0;
+  int4 up = make_int4(0, 0, 0, 0);
+  double4 dw = make_double4(0.0, 0.0, 0.0, 0.0);
+  if (IFLUX >= 3) {
+    up = ldro(a.eupw + e);
+    dw = ld4(a.ewts + e);
+    upwind_state(a.Uin, up.x, up.y, dw.x, dw.y, G.ysum_a, G.nx, G.ny, M.tolisec, hl_upw, vl_upw, zl_upw);
+    upwind_state(a.Uin, up.z, up.w, dw.z, dw.w, G.ysum_b, G.nx, G.ny, M.tolisec, hr_upw, vr_upw, zr_upw);
+  }
+  constexpr int NDIR = (IFLUX >= 3) ? 10 : 6;
+  const double w[10] = {wa.f1, wa.f2, wa.f3, wa.bx, wa.by, wb.f1, wb.f2, wb.f3, wb.bx, wb.by};
+  double acc[NDIR];
+#pragma unroll
+  for (int base = 0; base < NDIR; base += D) {
+    Dual<D> o[10];
+    interior_edge<IFLUX>(M, a.ilimiteur, a.flux_mode, G, dt, seed<D>(UA.x, 0, base), seed<D>(UA.y, 1, base),
+                         seed<D>(UA.z, 2, base), UA.w, seed<D>(UB.x, 3, base), seed<D>(UB.y, 4, base),
+                         seed<D>(UB.z, 5, base), UB.w, seed<D>(hl_upw, 6, base), seed<D>(vl_upw, 7, base), zl_upw,
+                         seed<D>(hr_upw, 8, base), seed<D>(vr_upw, 9, base), zr_upw, o);
+#pragma unroll
+    for (int i = 0; i < D; ++i) {
+      if (base + i < NDIR) {
+        double s = 0.0;
+#pragma unroll
+        for (int k = 0; k < 10; ++k) s = fma(w[k], o[k].d[i], s);
+        acc[base + i] = s;
+      }
+    }
+  }
+  A.eadj[2 * (size_t)e] = make_double4(acc[0], acc[1], acc[2], 0.0);
+  A.eadj[2 * (size_t)e + 1] = make_double4(acc[3], acc[4], acc[5], 0.0);
+  if constexpr (IFLUX >= 3) {
+    double4 c0, c1, c2, c3;
+    upwind_chain(a.Uin, up.x, up.y, dw.x, dw.y, G.ysum_a, G.nx, G.ny, M.tolisec, acc[6], acc[7], &c0, &c1);
+    upwind_chain(a.Uin, up.z, up.w, dw.z, dw.w, G.ysum_b, G.nx, G.ny, M.tolisec, acc[8], acc[9], &c2, &c3);
+    double4* u = A.uadj + 4 * (size_t)e;
+    u[0] = c0;
+    u[1] = c1;
+    u[2] = c2;
+    u[3] = c3;
+  }
+}
+
+/* ---- gather ---------------------------------------------------------------------------- */
+
+__global__ void __launch_bounds__(TILE_C) k_adj_gather(AdjArgs A) {
+  const StepArgs& a = A.s;
+  const int tile = blockIdx.x;
+  const MemberDev& M = a.mdev[__ldg(a.ctile_mem + tile)];
+  const int c = tile * TILE_C + threadIdx.x;
+  if (c >= M.cell_end) return;
+  double4 L = A.lam_out[c];
+  const int4 sl = __ldg(a.cslot + c);
+  const double4 e0 = ld4(A.eadj + sl.x), e1 = ld4(A.eadj + sl.y), e2 = ld4(A.eadj + sl.z);
+  L.x = L.x + e0.x + e1.x + e2.x;
+  L.y = L.y + e0.y + e1.y + e2.y;
+  L.z = L.z + e0.z + e1.z + e2.z;
+  if (A.uoff) {
+    for (int j = __ldg(A.uoff + c), j1 = __ldg(A.uoff + c + 1); j < j1; ++j) {
+      const double4 u = ld4(A.uadj + __ldg(A.uidx + j));
+      L.x += u.x;
+      L.y += u.y;
+      L.z += u.z;
+    }
+  }
+  if (A.gw)
+    for (int j = __ldg(A.goff + c), j1 = __ldg(A.goff + c + 1); j < j1; ++j) L.x += __ldg(A.gw + __ldg(A.gidx + j));
+  A.lam_out[c] = L;
+}
+
+/* lambda.h += the objective's weights of the gauges an element carries (the final state's
+ * gauge terms) */
+__global__ void k_add_gauges(double4* lam, const int32_t* goff, const int32_t* gidx, const double* gw, int n) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= n) return;
+  for (int j = goff[c]; j < goff[c + 1]; ++j) lam[c].x += gw[gidx[j]];
+}
+
+__global__ void k_gather_scalar(const double* x, const int32_t* iperm, double* out, int n) {
+  const int o = blockIdx.x * blockDim.x + threadIdx.x;
+  if (o < n) out[o] = x[iperm[o]];
+}
+
+__global__ void k_set_manning(double4* cstat, const int32_t* perm, const double* nref, int n) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c < n) cstat[c].y = nref[perm[c]];
+}
+
+int chk(cudaError_t e) { return e == cudaSuccess ? CF_OK : CF_ECUDA; }
+
+}  // namespace
+
+int launch_replay_step(const StepArgs& a, const double* dt_hist, const double* t_hist, int n, uint32_t* flag,
+                       stream_t s) {
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(s);
+  switch (a.iflux) {
+    case 1: k_rep_edges<1><<<a.n_etiles, TILE_E, 0, st>>>(a, dt_hist, t_hist, n); break;
+    case 2: k_rep_edges<2><<<a.n_etiles, TILE_E, 0, st>>>(a, dt_hist, t_hist, n); break;
+    case 3: k_rep_edges<3><<<a.n_etiles, TILE_E, 0, st>>>(a, dt_hist, t_hist, n); break;
+    default: return CF_ENOTSUP;
+  }
+  if (flag) k_rep_cells<<<a.n_ctiles, TILE_C, 0, st>>>(a, dt_hist, n, flag);
+  return chk(cudaGetLastError());
+}
+
+int launch_record(const double4* Unew, const MemberState* S, int p, int n, double* dt_hist, double* t_hist,
+                  const int32_t* gcell, int G, double* eta, stream_t s) {
+  k_record<<<1, 256, 0, reinterpret_cast<cudaStream_t>(s)>>>(Unew, S, p, n, dt_hist, t_hist, gcell, G, eta);
+  return chk(cudaGetLastError());
+}
+
+int launch_adjoint_step(const AdjArgs& A, stream_t s) {
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(s);
+  const StepArgs& a = A.s;
+  int rc = launch_replay_step(a, A.dt_hist, A.t_hist, A.n, nullptr, s);   /* slots at U^n */
+  if (rc != CF_OK) return rc;
+  k_adj_cells<3><<<a.n_ctiles, TILE_C, 0, st>>>(A);
+  switch (a.iflux) {
+    case 1: k_adj_edges<1, 3><<<a.n_etiles, TILE_E, 0, st>>>(A); break;
+    case 2: k_adj_edges<2, 3><<<a.n_etiles, TILE_E, 0, st>>>(A); break;
+    case 3: k_adj_edges<3, 2><<<a.n_etiles, TILE_E, 0, st>>>(A); break;
+    default: return CF_ENOTSUP;
+  }
+  k_adj_gather<<<a.n_ctiles, TILE_C, 0, st>>>(A);
+  return chk(cudaGetLastError());
+}
+
+int launch_add_gauges(double4* lam, const int32_t* goff, const int32_t* gidx, const double* gw, int32_t n, stream_t s) {
+  if (n <= 0) return CF_OK;
+  k_add_gauges<<<(n + 255) / 256, 256, 0, reinterpret_cast<cudaStream_t>(s)>>>(lam, goff, gidx, gw, n);
+  return chk(cudaGetLastError());
+}
+
+int launch_gather_scalar(const double* x, const int32_t* iperm, double* out, int32_t n, stream_t s) {
+  if (n <= 0) return CF_OK;
+  k_gather_scalar<<<(n + 255) / 256, 256, 0, reinterpret_cast<cudaStream_t>(s)>>>(x, iperm, out, n);
+  return chk(cudaGetLastError());
+}
+
+int launch_set_manning(double4* cstat, const int32_t* perm, const double* nref, int32_t n, stream_t s) {
+  if (n <= 0) return CF_OK;
+  k_set_manning<<<(n + 255) / 256, 256, 0, reinterpret_cast<cudaStream_t>(s)>>>(cstat, perm, nref, n);
+  return chk(cudaGetLastError());
+}
+
+}  // namespace cf

@@ -1,0 +1,376 @@
+/*
+ * cf_adjoint_api.cpp -- the discrete adjoint behind the C ABI (cf_adjoint_*, cf_set_manning).
+ *
+ * Objective.  For a run of N steps from the context's current state U^0 with the Manning field
+ * n, the caller weighs the free-surface elevation eta^k_g = h + z of G gauge elements after
+ * every step k = 1..N and the final state:
+ *     J = sum_k sum_g w_eta[k-1][g] eta^k_g + sum_e w_state[e] . U^N_e .
+ * cf_adjoint_backward returns dJ/dU^0 and dJ/dn (every element), with the dt of every step held
+ * at its recorded value (the time step is not differentiated).  A caller with a non-linear
+ * misfit passes its derivative with respect to eta and U^N as the weights (chain rule).
+ *
+ * Checkpointing.  The recording forward keeps the state every K steps (K ~ sqrt(N) by default).
+ * The backward sweep walks the segments from the last: it recomputes the segment's states from
+ * its checkpoint with the recorded dt sequence (bit-identical to the recorded run) and then runs
+ * the reverse steps through them.  Memory: ceil(N/K) + max(K, 2) states; cost: one extra
+ * forward pass besides the reverse steps.
+ *
+ * Contexts with one member only.
+ */
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "cf_ctx.h"
+
+using namespace cf;
+
+struct cf_adjoint {
+  cf_ctx* ctx = nullptr;
+  int32_t N = 0, K = 1, G = 0, nseg = 0, nseg_states = 2;
+  int32_t n = 0, n_pad = 0;
+  double4* ckpt = nullptr;   /* nseg states */
+  double4* seg = nullptr;    /* nseg_states states */
+  MemberState* mst = nullptr;
+  double* dt_hist = nullptr;
+  double* t_hist = nullptr;
+  double* eta = nullptr;     /* N x G */
+  double* wbuf = nullptr;    /* N x G objective weights */
+  int32_t* gcell = nullptr;
+  int32_t* goff = nullptr;
+  int32_t* gidx = nullptr;
+  double4* lam[2] = {nullptr, nullptr};
+  Slot* cadj = nullptr;
+  double4* eadj = nullptr;
+  double4* uadj = nullptr;
+  int32_t* uoff = nullptr;
+  int32_t* uidx = nullptr;
+  double* gman = nullptr;
+  uint32_t* flag = nullptr;
+  bool recorded = false;     /* a recording forward has filled dt_hist / t_hist */
+  bool have_traj = false;    /* the checkpoints hold the last forward's trajectory */
+};
+
+namespace {
+
+void adj_free(cf_adjoint* a) {
+  void* ptrs[] = {a->ckpt, a->seg, a->mst, a->dt_hist, a->t_hist, a->eta, a->wbuf, a->gcell, a->goff, a->gidx,
+                  a->lam[0], a->lam[1], a->cadj, a->eadj, a->uadj, a->uoff, a->uidx, a->gman, a->flag};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+}
+
+template <class T>
+int get(cf_ctx* c, T* dst, const T* src, size_t count) {
+  if (count) CF_CUDA(c, cudaMemcpy(dst, src, count * sizeof(T), cudaMemcpyDeviceToHost));
+  return CF_OK;
+}
+
+/* CSR (ascending element, then ascending entry) of the pairs (element, entry) */
+void build_csr(int32_t n, const std::vector<int32_t>& elem, const std::vector<int32_t>& entry,
+               std::vector<int32_t>& off, std::vector<int32_t>& idx) {
+  off.assign((size_t)n + 1, 0);
+  for (int32_t e : elem) off[(size_t)e + 1]++;
+  for (int32_t i = 0; i < n; ++i) off[(size_t)i + 1] += off[i];
+  idx.assign(elem.size(), 0);
+  std::vector<int32_t> pos(off.begin(), off.end() - 1);
+  for (size_t k = 0; k < elem.size(); ++k) idx[(size_t)pos[elem[k]]++] = entry[k];
+}
+
+int create_impl(cf_ctx* c, int32_t nsteps, int32_t interval, const int32_t* gauges, int32_t ngauges, cf_adjoint** out) {
+  if (!out) return fail(c, CF_EINVAL, "out is NULL");
+  *out = nullptr;
+  if (c->mem.size() != 1) return fail(c, CF_ENOTSUP, "the adjoint takes a context with one member");
+  if (nsteps < 1) return fail(c, CF_EINVAL, "nsteps < 1");
+  if (ngauges < 0 || (ngauges > 0 && !gauges)) return fail(c, CF_EINVAL, "gauges NULL or ngauges < 0");
+  const Member& M = c->mem[0];
+  for (int32_t g = 0; g < ngauges; ++g)
+    if (gauges[g] < 0 || gauges[g] >= M.n) return fail(c, CF_EINVAL, "gauge element out of range");
+  CF_CUDA(c, cudaSetDevice(c->device));
+  cf_adjoint* a = new (std::nothrow) cf_adjoint();
+  if (!a) return fail(c, CF_ENOMEM, "host allocation failed");
+  auto done = [&](int rc) {
+    if (rc != CF_OK) {
+      adj_free(a);
+      delete a;
+    } else {
+      *out = a;
+    }
+    return rc;
+  };
+  a->ctx = c;
+  a->N = nsteps;
+  a->K = interval > 0 ? std::min(interval, nsteps) : std::max(1, (int32_t)std::ceil(std::sqrt((double)nsteps)));
+  a->G = ngauges;
+  a->nseg = (nsteps + a->K - 1) / a->K;
+  a->nseg_states = std::max(a->K, 2);
+  a->n = M.n;
+  a->n_pad = c->n_pad;
+  const size_t np = (size_t)c->n_pad, nep = (size_t)c->ne_pad;
+  const bool second = c->iflux >= 3;
+  int rc;
+  if ((rc = dalloc(c, &a->ckpt, (size_t)a->nseg * np)) || (rc = dalloc(c, &a->seg, (size_t)a->nseg_states * np)) ||
+      (rc = dalloc(c, &a->mst, 1)) || (rc = dalloc(c, &a->dt_hist, (size_t)nsteps)) ||
+      (rc = dalloc(c, &a->t_hist, (size_t)nsteps)) || (rc = dalloc(c, &a->eta, (size_t)nsteps * ngauges)) ||
+      (rc = dalloc(c, &a->wbuf, (size_t)nsteps * ngauges)) || (rc = dalloc(c, &a->gcell, (size_t)ngauges)) ||
+      (rc = dalloc(c, &a->goff, np + 1)) || (rc = dalloc(c, &a->gidx, (size_t)ngauges)) ||
+      (rc = dalloc(c, &a->lam[0], np)) || (rc = dalloc(c, &a->lam[1], np)) || (rc = dalloc(c, &a->cadj, np)) ||
+      (rc = dalloc(c, &a->eadj, 2 * nep)) || (rc = dalloc(c, &a->gman, np)) || (rc = dalloc(c, &a->flag, 1)))
+    return done(rc);
+  /* gauges: new order, and their CSR over the elements */
+  {
+    std::vector<int32_t> gc(ngauges), ge(ngauges), gi(ngauges), off, idx;
+    for (int32_t g = 0; g < ngauges; ++g) {
+      gc[g] = M.prep.iperm[gauges[g]];
+      ge[g] = g;
+    }
+    build_csr(c->n_pad, gc, ge, off, idx);
+    if ((rc = put(c, a->gcell, gc.data(), gc.size())) || (rc = put(c, a->goff, off.data(), off.size())) ||
+        (rc = put(c, a->gidx, idx.data(), idx.size())))
+      return done(rc);
+  }
+  /* second order: which edge entries each element is an upwind element of */
+  if (second) {
+    if ((rc = dalloc(c, &a->uadj, 4 * nep)) || (rc = dalloc(c, &a->uoff, np + 1))) return done(rc);
+    std::vector<int2> ecell(nep);
+    std::vector<int4> up(nep);
+    std::vector<double4> dw(nep);
+    if ((rc = get(c, ecell.data(), c->ecell, nep)) || (rc = get(c, up.data(), c->eupw, nep)) ||
+        (rc = get(c, dw.data(), c->ewts, nep)))
+      return done(rc);
+    std::vector<int32_t> el, en, off, idx;
+    for (int32_t e = 0; e < M.ne; ++e) {
+      if (ecell[e].y < 0) continue;
+      el.push_back(up[e].x);
+      en.push_back(4 * e);
+      if (dw[e].x >= 0.0) { el.push_back(up[e].y); en.push_back(4 * e + 1); }
+      el.push_back(up[e].z);
+      en.push_back(4 * e + 2);
+      if (dw[e].z >= 0.0) { el.push_back(up[e].w); en.push_back(4 * e + 3); }
+    }
+    build_csr(c->n_pad, el, en, off, idx);
+    if ((rc = dalloc(c, &a->uidx, idx.size())) || (rc = put(c, a->uoff, off.data(), off.size())) ||
+        (rc = put(c, a->uidx, idx.data(), idx.size())))
+      return done(rc);
+  }
+  return done(CF_OK);
+}
+
+/* copy n doubles to a caller's pointer (host or device) */
+int to_user(cf_ctx* c, double* dst, const double* src, size_t count) {
+  if (dst && count) CF_CUDA(c, cudaMemcpyAsync(dst, src, count * sizeof(double), cudaMemcpyDefault, c->stream));
+  return CF_OK;
+}
+
+int forward_impl(cf_adjoint* a, int32_t replay, double* eta_out, double* state_out) {
+  cf_ctx* c = a->ctx;
+  if (replay && !a->recorded) return fail(c, CF_ESTATE, "replay before a recording forward");
+  CF_CUDA(c, cudaSetDevice(c->device));
+  int rc;
+  if ((rc = read_states(c))) return rc;
+  const MemberState s = c->host_state[0];
+  if (s.status & STATUS_NO_STATE) return fail(c, CF_ESTATE, "no state set");
+  if (s.status) return fail(c, status_code(s.status), "the context's member is stopped");
+  const int cur = (int)((s.base + s.nstep) & 1);
+  const stream_t st = reinterpret_cast<stream_t>(c->stream);
+  const size_t np = (size_t)a->n_pad;
+  a->have_traj = false;
+  CF_CUDA(c, cudaMemcpyAsync(a->seg, c->U[cur], np * sizeof(double4), cudaMemcpyDeviceToDevice, c->stream));
+  if (!replay) CF_CUDA(c, cudaMemcpyAsync(a->mst, c->mst, sizeof(MemberState), cudaMemcpyDeviceToDevice, c->stream));
+  CF_CUDA(c, cudaMemsetAsync(a->flag, 0, sizeof(uint32_t), c->stream));
+  double4* X = a->seg;
+  double4* Y = a->seg + np;
+  int p = cur;
+  for (int32_t k = 0; k < a->N; ++k) {
+    if (k % a->K == 0)
+      CF_CUDA(c, cudaMemcpyAsync(a->ckpt + (size_t)(k / a->K) * np, X, np * sizeof(double4), cudaMemcpyDeviceToDevice,
+                                 c->stream));
+    StepArgs sa = step_args(c, p);
+    sa.Uin = X;
+    sa.Uout = Y;
+    if (!replay) {
+      sa.mst = a->mst;
+      if ((rc = launch_step(sa, st, nullptr, nullptr))) return fail(c, rc, "step launch failed");
+      rc = launch_record(Y, a->mst, p, k, a->dt_hist, a->t_hist, a->gcell, a->G, a->eta, st);
+    } else {
+      if ((rc = launch_replay_step(sa, a->dt_hist, a->t_hist, k, a->flag, st))) return fail(c, rc, "replay launch failed");
+      rc = launch_record(Y, nullptr, 0, k, a->dt_hist, a->t_hist, a->gcell, a->G, a->eta, st);
+    }
+    if (rc) return fail(c, rc, "record launch failed");
+    std::swap(X, Y);
+    p ^= 1;
+  }
+  if (state_out) {
+    if ((rc = launch_gather_state(X, c->iperm, c->staging, a->n, st))) return fail(c, rc, "gather launch failed");
+    if ((rc = to_user(c, state_out, c->staging, 3 * (size_t)a->n))) return rc;
+  }
+  if ((rc = to_user(c, eta_out, a->eta, (size_t)a->N * a->G))) return rc;
+  MemberState ms{};
+  uint32_t flag = 0;
+  CF_CUDA(c, cudaMemcpyAsync(&ms, a->mst, sizeof(ms), cudaMemcpyDeviceToHost, c->stream));
+  CF_CUDA(c, cudaMemcpyAsync(&flag, a->flag, sizeof(flag), cudaMemcpyDeviceToHost, c->stream));
+  CF_CUDA(c, cudaStreamSynchronize(c->stream));
+  const uint32_t bad = replay ? flag : ms.status;
+  if (bad) {
+    rc = status_code(bad);
+    return fail(c, rc, rc == CF_EDT ? "dt left the range (1e-12, 9999] during the run" : "non-finite value in the state");
+  }
+  if (!replay) a->recorded = true;
+  a->have_traj = true;
+  return CF_OK;
+}
+
+int backward_impl(cf_adjoint* a, const double* w_eta, const double* w_state, double* g_state0, double* g_manning) {
+  cf_ctx* c = a->ctx;
+  if (!a->have_traj) return fail(c, CF_ESTATE, "backward before a forward");
+  CF_CUDA(c, cudaSetDevice(c->device));
+  const stream_t st = reinterpret_cast<stream_t>(c->stream);
+  const size_t np = (size_t)a->n_pad;
+  const size_t nw = (size_t)a->N * a->G;
+  int rc;
+  const bool weights = w_eta && nw > 0;
+  if (weights) CF_CUDA(c, cudaMemcpyAsync(a->wbuf, w_eta, nw * sizeof(double), cudaMemcpyDefault, c->stream));
+  CF_CUDA(c, cudaMemsetAsync(a->lam[0], 0, np * sizeof(double4), c->stream));
+  CF_CUDA(c, cudaMemsetAsync(a->lam[1], 0, np * sizeof(double4), c->stream));
+  CF_CUDA(c, cudaMemsetAsync(a->gman, 0, np * sizeof(double), c->stream));
+  if (w_state) {
+    CF_CUDA(c, cudaMemcpyAsync(c->staging, w_state, 3 * (size_t)a->n * sizeof(double), cudaMemcpyDefault, c->stream));
+    if ((rc = launch_scatter_state(c->staging, c->perm, c->zcell, a->lam[0], a->n, st)))
+      return fail(c, rc, "scatter launch failed");
+  }
+  if (weights && (rc = launch_add_gauges(a->lam[0], a->goff, a->gidx, a->wbuf + (size_t)(a->N - 1) * a->G, a->n, st)))
+    return fail(c, rc, "gauge launch failed");
+  double4* Lin = a->lam[0];
+  double4* Lout = a->lam[1];
+  for (int32_t j = a->nseg - 1; j >= 0; --j) {
+    const int32_t s0 = j * a->K, s1 = std::min(a->N, s0 + a->K);
+    CF_CUDA(c, cudaMemcpyAsync(a->seg, a->ckpt + (size_t)j * np, np * sizeof(double4), cudaMemcpyDeviceToDevice,
+                               c->stream));
+    for (int32_t i = 0; i + 1 < s1 - s0; ++i) {
+      StepArgs sa = step_args(c, 0);
+      sa.Uin = a->seg + (size_t)i * np;
+      sa.Uout = a->seg + (size_t)(i + 1) * np;
+      if ((rc = launch_replay_step(sa, a->dt_hist, a->t_hist, s0 + i, a->flag, st)))
+        return fail(c, rc, "replay launch failed");
+    }
+    for (int32_t k = s1 - 1; k >= s0; --k) {
+      AdjArgs A{};
+      A.s = step_args(c, 0);
+      A.s.Uin = a->seg + (size_t)(k - s0) * np;
+      A.s.Uout = nullptr;
+      A.dt_hist = a->dt_hist;
+      A.t_hist = a->t_hist;
+      A.n = k;
+      A.lam_in = Lin;
+      A.lam_out = Lout;
+      A.cadj = a->cadj;
+      A.eadj = a->eadj;
+      A.uadj = a->uadj;
+      A.uoff = a->uoff;
+      A.uidx = a->uidx;
+      A.goff = a->goff;
+      A.gidx = a->gidx;
+      A.gw = (weights && k >= 1) ? a->wbuf + (size_t)(k - 1) * a->G : nullptr;
+      A.gman = a->gman;
+      if ((rc = launch_adjoint_step(A, st))) return fail(c, rc, "adjoint launch failed");
+      std::swap(Lin, Lout);
+    }
+  }
+  if (g_state0) {
+    if ((rc = launch_gather_state(Lin, c->iperm, c->staging, a->n, st))) return fail(c, rc, "gather launch failed");
+    if ((rc = to_user(c, g_state0, c->staging, 3 * (size_t)a->n))) return rc;
+  }
+  if (g_manning) {
+    CF_CUDA(c, cudaStreamSynchronize(c->stream));  /* staging is reused */
+    if ((rc = launch_gather_scalar(a->gman, c->iperm, c->staging, a->n, st))) return fail(c, rc, "gather launch failed");
+    if ((rc = to_user(c, g_manning, c->staging, (size_t)a->n))) return rc;
+  }
+  CF_CUDA(c, cudaStreamSynchronize(c->stream));
+  return CF_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int cf_set_manning(cf_ctx* c, const double* n_elt) {
+  if (!c) return CF_EINVAL;
+  if (!n_elt) return fail(c, CF_EINVAL, "null argument");
+  if (c->mem.size() != 1) return fail(c, CF_ENOTSUP, "cf_set_manning takes a context with one member");
+  CF_CUDA(c, cudaSetDevice(c->device));
+  const Member& M = c->mem[0];
+  CF_CUDA(c, cudaMemcpyAsync(c->staging, n_elt, (size_t)M.n * sizeof(double), cudaMemcpyDefault, c->stream));
+  int rc = launch_set_manning(c->cstat, c->perm, c->staging, M.n, reinterpret_cast<stream_t>(c->stream));
+  if (rc != CF_OK) return fail(c, rc, "manning launch failed");
+  CF_CUDA(c, cudaStreamSynchronize(c->stream));
+  return CF_OK;
+}
+
+int cf_adjoint_create(cf_ctx* ctx, int32_t nsteps, int32_t checkpoint_interval, const int32_t* gauges,
+                      int32_t ngauges, cf_adjoint** out) {
+  if (!ctx) return CF_EINVAL;
+  return create_impl(ctx, nsteps, checkpoint_interval, gauges, ngauges, out);
+}
+
+void cf_adjoint_destroy(cf_adjoint* a) {
+  if (!a) return;
+  cudaSetDevice(a->ctx->device);
+  cudaStreamSynchronize(a->ctx->stream);
+  adj_free(a);
+  delete a;
+}
+
+int cf_adjoint_forward(cf_adjoint* a, int32_t replay, double* eta, double* state) {
+  if (!a) return CF_EINVAL;
+  return forward_impl(a, replay, eta, state);
+}
+
+int cf_adjoint_backward(cf_adjoint* a, const double* w_eta, const double* w_state, double* g_state0,
+                        double* g_manning) {
+  if (!a) return CF_EINVAL;
+  return backward_impl(a, w_eta, w_state, g_state0, g_manning);
+}
+
+int cf_adjoint_get_dt(cf_adjoint* a, double* dt, double* t) {
+  if (!a) return CF_EINVAL;
+  cf_ctx* c = a->ctx;
+  if (!a->recorded) return fail(c, CF_ESTATE, "no recorded dt sequence");
+  CF_CUDA(c, cudaSetDevice(c->device));
+  int rc;
+  if ((rc = to_user(c, dt, a->dt_hist, (size_t)a->N)) || (rc = to_user(c, t, a->t_hist, (size_t)a->N))) return rc;
+  CF_CUDA(c, cudaStreamSynchronize(c->stream));
+  return CF_OK;
+}
+
+int cf_adjoint_set_dt(cf_adjoint* a, const double* dt, const double* t) {
+  if (!a || !dt || !t) return a ? fail(a->ctx, CF_EINVAL, "null argument") : CF_EINVAL;
+  cf_ctx* c = a->ctx;
+  CF_CUDA(c, cudaSetDevice(c->device));
+  CF_CUDA(c, cudaMemcpyAsync(a->dt_hist, dt, (size_t)a->N * sizeof(double), cudaMemcpyDefault, c->stream));
+  CF_CUDA(c, cudaMemcpyAsync(a->t_hist, t, (size_t)a->N * sizeof(double), cudaMemcpyDefault, c->stream));
+  CF_CUDA(c, cudaStreamSynchronize(c->stream));
+  a->recorded = true;
+  a->have_traj = false;
+  return CF_OK;
+}
+
+int cf_adjoint_sizes(cf_adjoint* a, int32_t* nsteps, int32_t* interval, int32_t* ngauges, int64_t* device_bytes) {
+  if (!a) return CF_EINVAL;
+  if (nsteps) *nsteps = a->N;
+  if (interval) *interval = a->K;
+  if (ngauges) *ngauges = a->G;
+  if (device_bytes) {
+    const int64_t np = a->n_pad, nep = a->ctx->ne_pad;
+    int64_t b = (int64_t)(a->nseg + a->nseg_states + 2) * np * (int64_t)sizeof(double4) + np * (int64_t)sizeof(Slot) +
+                2 * nep * (int64_t)sizeof(double4) + np * 8 + (int64_t)a->N * (16 + 16 * (int64_t)a->G);
+    if (a->uadj) b += 4 * nep * (int64_t)sizeof(double4);
+    *device_bytes = b;
+  }
+  return CF_OK;
+}
+
+}  // extern "C"

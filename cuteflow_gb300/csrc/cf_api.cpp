@@ -25,63 +25,11 @@
 #include <thread>
 #include <vector>
 
-#include "cf_internal.h"
+#include "cf_ctx.h"
 
 using namespace cf;
 
-namespace {
-
-struct Member {
-  cf_params params{};
-  Prep prep;
-  int32_t n = 0, ne = 0;
-  int32_t cell_off = 0, edge_off = 0;
-  int32_t ctile_begin = 0, ctile_end = 0;
-  MemberDev dev{};
-};
-
-}  // namespace
-
-struct cf_ctx {
-  int device = 0;
-  int32_t iflux = 1, ilimiteur = 1, flux_mode = 0;
-  std::vector<Member> mem;
-  int32_t n_pad = 0, ne_pad = 0, n_etiles = 0, n_ctiles = 0, max_n = 0;
-  cudaStream_t stream = nullptr;
-  /* device memory (flat over members) */
-  double4* U[2] = {nullptr, nullptr};
-  int4* cslot = nullptr;
-  double4* cstat = nullptr;
-  double* zcell = nullptr;
-  int32_t* perm = nullptr;   /* new -> old, member-local */
-  int32_t* iperm = nullptr;  /* old -> new, member-local */
-  int2* ecell = nullptr;
-  double4* egeo = nullptr;
-  int32_t* ebid = nullptr;
-  int4* eupw = nullptr;
-  double4* ewts = nullptr;
-  double4* edk = nullptr;
-  double4* einv = nullptr;
-  Slot* slots = nullptr;
-  int32_t* etile_mem = nullptr;
-  int32_t* ctile_mem = nullptr;
-  MemberDev* mdev = nullptr;
-  MemberState* mst = nullptr;
-  double* staging = nullptr;           /* 3 * max_n doubles, reference order */
-  MemberState* host_state = nullptr;   /* pinned, one record per member */
-  /* stepping */
-  int64_t launched = 0;                /* steps launched since creation (buffer parity) */
-  cudaGraphExec_t graph2 = nullptr;    /* two steps: parity 0 then 1 */
-  bool use_graph = true;
-  /* timing */
-  bool timing = false;
-  cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
-  double flux_ms = 0.0, update_ms = 0.0;
-  int64_t launches = 0;
-  std::string err;
-};
-
-namespace {
+namespace cf {
 
 thread_local std::string g_create_error;
 
@@ -94,26 +42,6 @@ int fail(cf_ctx* c, int code, const std::string& msg) {
 int cuda_fail(cf_ctx* c, cudaError_t e, const char* what) {
   std::string msg = std::string(what) + ": " + cudaGetErrorString(e);
   return fail(c, e == cudaErrorMemoryAllocation ? CF_ENOMEM : CF_ECUDA, msg);
-}
-
-#define CF_CUDA(c, call)                                     \
-  do {                                                       \
-    cudaError_t e_ = (call);                                 \
-    if (e_ != cudaSuccess) return cuda_fail((c), e_, #call); \
-  } while (0)
-
-template <class T>
-int dalloc(cf_ctx* c, T** dst, size_t count) {
-  size_t bytes = std::max<size_t>(1, count) * sizeof(T);
-  CF_CUDA(c, cudaMalloc((void**)dst, bytes));
-  CF_CUDA(c, cudaMemset(*dst, 0, bytes));
-  return CF_OK;
-}
-
-template <class T>
-int put(cf_ctx* c, T* dst, const T* src, size_t count) {
-  if (count) CF_CUDA(c, cudaMemcpy(dst, src, count * sizeof(T), cudaMemcpyHostToDevice));
-  return CF_OK;
 }
 
 StepArgs step_args(const cf_ctx* c, int parity) {

@@ -1,0 +1,101 @@
+/*
+ * cf_ctx.h -- the context object behind the C ABI and the helpers its implementation files
+ * share (cf_api.cpp: the step; cf_adjoint_api.cpp: the adjoint).  Host code only.
+ */
+#ifndef CF_CTX_H
+#define CF_CTX_H
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <string>
+#include <vector>
+
+#include "cf_internal.h"
+
+namespace cf {
+
+/* One simulation of a context: its inputs, host tables and place in the flat space. */
+struct Member {
+  cf_params params{};
+  Prep prep;
+  int32_t n = 0, ne = 0;
+  int32_t cell_off = 0, edge_off = 0;
+  int32_t ctile_begin = 0, ctile_end = 0;
+  MemberDev dev{};
+};
+
+}  // namespace cf
+
+struct cf_ctx {
+  int device = 0;
+  int32_t iflux = 1, ilimiteur = 1, flux_mode = 0;
+  std::vector<cf::Member> mem;
+  int32_t n_pad = 0, ne_pad = 0, n_etiles = 0, n_ctiles = 0, max_n = 0;
+  cudaStream_t stream = nullptr;
+  /* device memory (flat over members) */
+  double4* U[2] = {nullptr, nullptr};
+  int4* cslot = nullptr;
+  double4* cstat = nullptr;
+  double* zcell = nullptr;
+  int32_t* perm = nullptr;   /* new -> old, member-local */
+  int32_t* iperm = nullptr;  /* old -> new, member-local */
+  int2* ecell = nullptr;
+  double4* egeo = nullptr;
+  int32_t* ebid = nullptr;
+  int4* eupw = nullptr;
+  double4* ewts = nullptr;
+  double4* edk = nullptr;
+  double4* einv = nullptr;
+  cf::Slot* slots = nullptr;
+  int32_t* etile_mem = nullptr;
+  int32_t* ctile_mem = nullptr;
+  cf::MemberDev* mdev = nullptr;
+  cf::MemberState* mst = nullptr;
+  double* staging = nullptr;           /* 3 * max_n doubles, reference order */
+  cf::MemberState* host_state = nullptr;   /* pinned, one record per member */
+  /* stepping */
+  int64_t launched = 0;                /* steps launched since creation (buffer parity) */
+  cudaGraphExec_t graph2 = nullptr;    /* two steps: parity 0 then 1 */
+  bool use_graph = true;
+  /* timing */
+  bool timing = false;
+  cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+  double flux_ms = 0.0, update_ms = 0.0;
+  int64_t launches = 0;
+  std::string err;
+};
+
+namespace cf {
+
+/* record msg as the context's last error (the create error when c is NULL), return code */
+int fail(cf_ctx* c, int code, const std::string& msg);
+int cuda_fail(cf_ctx* c, cudaError_t e, const char* what);
+
+#define CF_CUDA(c, call)                                     \
+  do {                                                       \
+    cudaError_t e_ = (call);                                 \
+    if (e_ != cudaSuccess) return cf::cuda_fail((c), e_, #call); \
+  } while (0)
+
+template <class T>
+int dalloc(cf_ctx* c, T** dst, size_t count) {
+  size_t bytes = std::max<size_t>(1, count) * sizeof(T);
+  CF_CUDA(c, cudaMalloc((void**)dst, bytes));
+  CF_CUDA(c, cudaMemset(*dst, 0, bytes));
+  return CF_OK;
+}
+
+template <class T>
+int put(cf_ctx* c, T* dst, const T* src, size_t count) {
+  if (count) CF_CUDA(c, cudaMemcpy(dst, src, count * sizeof(T), cudaMemcpyHostToDevice));
+  return CF_OK;
+}
+
+StepArgs step_args(const cf_ctx* c, int parity);  /* the context's buffers for a step of this parity */
+int read_states(cf_ctx* c);                        /* mst -> host_state, synchronising the stream */
+int status_code(uint32_t status);                  /* CF_* code of a status word */
+
+}  // namespace cf
+
+#endif

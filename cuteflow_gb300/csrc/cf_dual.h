@@ -1,0 +1,199 @@
+/*
+ * cf_dual.h -- forward-mode dual numbers for the discrete adjoint.
+ *
+ * Dual<N> carries a value and N directional derivatives.  The value lane performs exactly the
+ * IEEE operations the plain FP64 forward performs (same order, no contraction: the kernels are
+ * compiled with -fmad=false), so comparisons taken on values select the same branches as the
+ * forward step, and the derivative lanes are the exact local derivatives of that branch.  The
+ * templated step arithmetic (cf_flux.h) instantiated with Dual<N> therefore yields the local
+ * Jacobians the reverse sweep needs (dt frozen).
+ */
+#ifndef CF_DUAL_H
+#define CF_DUAL_H
+
+#include "cf_flux.h"
+
+#ifdef __CUDACC__
+#define CFD_HD __host__ __device__ __forceinline__
+#else
+#define CFD_HD inline
+#endif
+
+namespace cf {
+
+#ifdef __CUDACC__
+using ::fabs;
+using ::sqrt;
+#endif
+
+template <int N>
+struct Dual {
+  double v;
+  double d[N];
+  CFD_HD Dual() : v(0.0) {
+#pragma unroll
+    for (int i = 0; i < N; ++i) d[i] = 0.0;
+  }
+  CFD_HD Dual(double x) : v(x) {  // NOLINT: constants promote implicitly
+#pragma unroll
+    for (int i = 0; i < N; ++i) d[i] = 0.0;
+  }
+  /* the i-th independent variable with value x */
+  static CFD_HD Dual var(double x, int i) {
+    Dual r(x);
+    r.d[i] = 1.0;
+    return r;
+  }
+};
+
+template <int N>
+CFD_HD double val(const Dual<N>& x) { return x.v; }
+
+template <int N>
+CFD_HD Dual<N> operator-(const Dual<N>& a) {
+  Dual<N> r;
+  r.v = -a.v;
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = -a.d[i];
+  return r;
+}
+template <int N>
+CFD_HD Dual<N> operator+(const Dual<N>& a, const Dual<N>& b) {
+  Dual<N> r;
+  r.v = a.v + b.v;
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = a.d[i] + b.d[i];
+  return r;
+}
+template <int N>
+CFD_HD Dual<N> operator-(const Dual<N>& a, const Dual<N>& b) {
+  Dual<N> r;
+  r.v = a.v - b.v;
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = a.d[i] - b.d[i];
+  return r;
+}
+template <int N>
+CFD_HD Dual<N> operator*(const Dual<N>& a, const Dual<N>& b) {
+  Dual<N> r;
+  r.v = a.v * b.v;
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = fma(a.d[i], b.v, a.v * b.d[i]);
+  return r;
+}
+template <int N>
+CFD_HD Dual<N> operator/(const Dual<N>& a, const Dual<N>& b) {
+  Dual<N> r;
+  r.v = a.v / b.v;
+  const double y = 1.0 / b.v;
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = fma(-r.v, b.d[i], a.d[i]) * y;
+  return r;
+}
+/* mixed with constants */
+template <int N> CFD_HD Dual<N> operator+(const Dual<N>& a, double b) { Dual<N> r = a; r.v = a.v + b; return r; }
+template <int N> CFD_HD Dual<N> operator+(double a, const Dual<N>& b) { Dual<N> r = b; r.v = a + b.v; return r; }
+template <int N> CFD_HD Dual<N> operator-(const Dual<N>& a, double b) { Dual<N> r = a; r.v = a.v - b; return r; }
+template <int N>
+CFD_HD Dual<N> operator-(double a, const Dual<N>& b) {
+  Dual<N> r;
+  r.v = a - b.v;
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = -b.d[i];
+  return r;
+}
+template <int N>
+CFD_HD Dual<N> operator*(const Dual<N>& a, double b) {
+  Dual<N> r;
+  r.v = a.v * b;
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = a.d[i] * b;
+  return r;
+}
+template <int N>
+CFD_HD Dual<N> operator*(double a, const Dual<N>& b) {
+  Dual<N> r;
+  r.v = a * b.v;
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = a * b.d[i];
+  return r;
+}
+template <int N>
+CFD_HD Dual<N> operator/(const Dual<N>& a, double b) {
+  Dual<N> r;
+  r.v = a.v / b;
+  const double y = 1.0 / b;
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = a.d[i] * y;
+  return r;
+}
+template <int N>
+CFD_HD Dual<N> operator/(double a, const Dual<N>& b) {
+  Dual<N> r;
+  r.v = a / b.v;
+  const double y = 1.0 / b.v;
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = -r.v * b.d[i] * y;
+  return r;
+}
+/* comparisons act on values */
+template <int N> CFD_HD bool operator<(const Dual<N>& a, const Dual<N>& b) { return a.v < b.v; }
+template <int N> CFD_HD bool operator>(const Dual<N>& a, const Dual<N>& b) { return a.v > b.v; }
+template <int N> CFD_HD bool operator<=(const Dual<N>& a, const Dual<N>& b) { return a.v <= b.v; }
+template <int N> CFD_HD bool operator>=(const Dual<N>& a, const Dual<N>& b) { return a.v >= b.v; }
+template <int N> CFD_HD bool operator<(const Dual<N>& a, double b) { return a.v < b; }
+template <int N> CFD_HD bool operator>(const Dual<N>& a, double b) { return a.v > b; }
+template <int N> CFD_HD bool operator<=(const Dual<N>& a, double b) { return a.v <= b; }
+template <int N> CFD_HD bool operator>=(const Dual<N>& a, double b) { return a.v >= b; }
+template <int N> CFD_HD bool operator<(double a, const Dual<N>& b) { return a < b.v; }
+template <int N> CFD_HD bool operator>(double a, const Dual<N>& b) { return a > b.v; }
+template <int N> CFD_HD bool operator==(const Dual<N>& a, const Dual<N>& b) { return a.v == b.v; }
+template <int N> CFD_HD bool operator!=(const Dual<N>& a, const Dual<N>& b) { return a.v != b.v; }
+
+template <int N>
+CFD_HD Dual<N> sqrt(const Dual<N>& a) {
+  Dual<N> r;
+  r.v = ::sqrt(a.v);
+  const double y = r.v > 0.0 ? 0.5 / r.v : 0.0; /* sqrt(0) only where the depth is exactly zero */
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = a.d[i] * y;
+  return r;
+}
+template <int N>
+CFD_HD Dual<N> fabs(const Dual<N>& a) {
+  return (a.v < 0.0) ? -a : a;
+}
+
+/* Quotient by a known reciprocal (div_rn in cf_flux.h): the value lane is the step's own
+ * rounding; the lanes differentiate a / d. */
+template <int N>
+CFD_HD Dual<N> div_rn(const Dual<N>& a, const Dual<N>& d, const Dual<N>& y) {
+  Dual<N> r;
+  r.v = div_rn(a.v, d.v, y.v);
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = fma(-r.v, d.d[i], a.d[i]) * y.v;
+  return r;
+}
+template <int N>
+CFD_HD Dual<N> div_rn(const Dual<N>& a, double d, double y) {
+  Dual<N> r;
+  r.v = div_rn(a.v, d, y);
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = a.d[i] * y;
+  return r;
+}
+
+/* x^(1/3): d/dx = 1 / (3 c^2) with c the cube root */
+template <int N>
+CFD_HD Dual<N> cbrt_halley(const Dual<N>& x) {
+  Dual<N> r;
+  r.v = cbrt_halley(x.v);
+  const double k = 1.0 / (3.0 * r.v * r.v);
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = x.d[i] * k;
+  return r;
+}
+
+}  // namespace cf
+
+#endif

@@ -1,7 +1,7 @@
 /*
  * cf_flux.h -- per-edge and per-element arithmetic of the step, shared by the sm_103a kernels
- * (cf_kernels.cu) and, compiled for the host, by the CPU test harness that checks it against
- * the oracle edge by edge.  Everything here is __host__ __device__ and FP64.
+ * (cf_kernels.cu, cf_adjoint.cu) and, compiled for the host, by the CPU test harness that checks
+ * it against the oracle edge by edge.  Everything here is __host__ __device__ and FP64.
  *
  * Bit-exact reproduction.  The reference's WAF flux is discontinuous at the bit level: where
  * the reconstructed depths of an edge are equal to the last bit (still water),
@@ -13,6 +13,13 @@
  * on the GPU reproduces the CPU restatement of the reference bit for bit.  The second side of
  * an edge is obtained from the first by exact IEEE identities ((-a)*b = -(a*b),
  * (-a)-(-b) = b-a, commutativity), never by re-rounded arithmetic.
+ *
+ * Scalar type.  The state-dependent arithmetic is written once, as templates on the scalar
+ * type T.  T = double is the step.  T = Dual<N> (cf_dual.h) carries N derivative lanes next to
+ * a value lane that performs the same IEEE operations in the same order, so it takes the same
+ * branches (wet/dry masks, wave regions, limiter cases) as the step and its lanes are the exact
+ * local Jacobian of that branch: the discrete adjoint is built from it.  Geometry, time and
+ * time step stay double (the adjoint holds dt fixed).
  */
 #ifndef CF_FLUX_H
 #define CF_FLUX_H
@@ -69,8 +76,13 @@ CF_HD CF_INLINE bool finite_bits(double x) {
   return (b & 0x7ff0000000000000ll) != 0x7ff0000000000000ll;
 }
 
-CF_HD CF_INLINE double dmax(double a, double b) { return (a < b) ? b : a; } /* Fortran max */
-CF_HD CF_INLINE double dmin(double a, double b) { return (b < a) ? b : a; } /* Fortran min */
+/* value of a scalar (the Dual overload is in cf_dual.h) */
+CF_HD CF_INLINE double val(double x) { return x; }
+
+template <class T>
+CF_HD CF_INLINE T dmax(const T& a, const T& b) { return (a < b) ? b : a; } /* Fortran max */
+template <class T>
+CF_HD CF_INLINE T dmin(const T& a, const T& b) { return (b < a) ? b : a; } /* Fortran min */
 
 /* a / d rounded to nearest, given y = RN(1/d): q = RN(a y), r = a - d q (exact through the
  * FMA), RN(q + r y) (Markstein's correction step; P. Markstein, "Computation of elementary
@@ -113,46 +125,46 @@ CF_HD CF_INLINE double cbrt_halley(double x) {
 /* ---- edge-frame states ------------------------------------------------------------------ */
 
 /* Masked primitive state in the frame (n, t) of an edge (flux_riemann.cuf:105-112). */
-CF_HD CF_INLINE void to_frame(double h, double hu, double hv, double nx, double ny, double tolisec,
-                              double& hm, double& un, double& ut) {
+template <class T>
+CF_HD CF_INLINE void to_frame(T h, T hu, T hv, double nx, double ny, double tolisec, T& hm, T& un, T& ut) {
   if (h > tolisec) {
-    const double y = 1.0 / h;
+    const T y = 1.0 / h;
     un = div_rn(hu * nx + hv * ny, h, y);
     ut = div_rn(hv * nx - hu * ny, h, y);
     hm = h;
   } else {
-    hm = 0.0;
-    un = 0.0;
-    ut = 0.0;
+    hm = T(0.0);
+    un = T(0.0);
+    ut = T(0.0);
   }
 }
 
 /* Only the masked depth and tangential velocity (what the WAF upwind states use). */
-CF_HD CF_INLINE void to_frame_t(double h, double hu, double hv, double nx, double ny, double tolisec, double& hm,
-                                double& ut) {
+template <class T>
+CF_HD CF_INLINE void to_frame_t(T h, T hu, T hv, double nx, double ny, double tolisec, T& hm, T& ut) {
   if (h > tolisec) {
     ut = (hv * nx - hu * ny) / h;
     hm = h;
   } else {
-    hm = 0.0;
-    ut = 0.0;
+    hm = T(0.0);
+    ut = T(0.0);
   }
 }
 
 /* Wave speeds of all solvers (flux_riemann.cuf:930-983, 753-806, 1055-1108).  Returns false
  * when both depths are below eps: the reference then reads uninitialised speeds; the flux
  * defined for that case is zero. */
-CF_HD CF_INLINE bool wave_speeds(double g, double eps, double hl, double ul, double hr, double ur,
-                                 double& sl, double& sr, double& set) {
+template <class T>
+CF_HD CF_INLINE bool wave_speeds(double g, double eps, T hl, T ul, T hr, T ur, T& sl, T& sr, T& set) {
   if (hl < eps && hr < eps) return false;
-  const double al = sqrt(g * hl);
-  const double ar = sqrt(g * hr);
-  const double het = (hl + hr) / 2. - (ur - ul) * (hl + hr) / (al + ar) / 4.;
-  double pql, pqr;
-  if (het < hl) pql = 1.;
-  else pql = (hl > eps) ? sqrt(0.5 * (het + hl) * het / (hl * hl)) : 0.;
-  if (het < hr) pqr = 1.;
-  else pqr = (hr > eps) ? sqrt(0.5 * (het + hr) * het / (hr * hr)) : 0.;
+  const T al = sqrt(g * hl);
+  const T ar = sqrt(g * hr);
+  const T het = (hl + hr) / 2. - (ur - ul) * (hl + hr) / (al + ar) / 4.;
+  T pql, pqr;
+  if (het < hl) pql = T(1.);
+  else pql = (hl > eps) ? sqrt(0.5 * (het + hl) * het / (hl * hl)) : T(0.);
+  if (het < hr) pqr = T(1.);
+  else pqr = (hr > eps) ? sqrt(0.5 * (het + hr) * het / (hr * hr)) : T(0.);
   if (hl > eps) {
     sl = ul - al * pql;
     if (hr > eps) {
@@ -165,22 +177,24 @@ CF_HD CF_INLINE bool wave_speeds(double g, double eps, double hl, double ul, dou
     sl = ur - 2 * ar;
     sr = ur + ar;
   }
-  const double denom = hr * (ur - sr) - hl * (ul - sl);
+  const T denom = hr * (ur - sr) - hl * (ul - sl);
   if (fabs(denom) < eps) set = (ul + ur) / 2. - (hr - hl) * (al + ar) / (hl + hr);
   else set = (sl * hr * (ur - sr) - sr * hl * (ul - sl)) / denom;
   return true;
 }
 
-struct TwoFlux {
+template <class T>
+struct TwoFluxT {
   /* global-frame flux of side A (normal out of A) and of side B (normal out of B) */
-  double a1, a2, a3, b1, b2, b3;
+  T a1, a2, a3, b1, b2, b3;
 };
+typedef TwoFluxT<double> TwoFlux;
 
 /* Side A's global flux from the edge-frame vector x; side B's from its vector y: B's frame
  * normal is -n and its vector is the mirror (-y1, y2, y3), which reprojects to
  * -(n1 y2 - n2 y3), -(n2 y2 + n1 y3) exactly. */
-CF_HD CF_INLINE void reproject_both(double nx, double ny, double x1, double x2, double x3, double y1,
-                                    double y2, double y3, TwoFlux& F) {
+template <class T>
+CF_HD CF_INLINE void reproject_both(double nx, double ny, T x1, T x2, T x3, T y1, T y2, T y3, TwoFluxT<T>& F) {
   F.a1 = x1;
   F.a2 = nx * x2 - ny * x3;
   F.a3 = ny * x2 + nx * x3;
@@ -193,40 +207,40 @@ CF_HD CF_INLINE void reproject_both(double nx, double ny, double x1, double x2, 
  * al. (IFLUX 2, :1029-1182), for both sides.  Side B's evaluation is the mirror image
  * (h -> h, u_n -> -u_n, u_t -> -u_t, s_L -> -s_R, s_R -> -s_L, s_* -> -s_*): it selects a
  * region with its own tests and its vector is the mirror of an A-frame vector. */
-template <int IFLUX>
-CF_HD CF_INLINE void first_order_flux(double g, double nx, double ny, double hl, double ul, double vl,
-                                      double hr, double ur, double vr, TwoFlux& F) {
+template <int IFLUX, class T>
+CF_HD CF_INLINE void first_order_flux(double g, double nx, double ny, T hl, T ul, T vl, T hr, T ur, T vr,
+                                      TwoFluxT<T>& F) {
   const double eps = (IFLUX == 1) ? EPS_HLLC : EPS_RIADH;
-  double sl, sr, set;
+  T sl, sr, set;
   if (!wave_speeds(g, eps, hl, ul, hr, ur, sl, sr, set)) {
-    F.a1 = F.a2 = F.a3 = F.b1 = F.b2 = F.b3 = 0.0;
+    F.a1 = F.a2 = F.a3 = F.b1 = F.b2 = F.b3 = T(0.0);
     return;
   }
-  const double fl1 = hl * ul, fl2 = hl * (ul * ul) + g * hl * hl / 2.0, fl3 = hl * ul * vl;
-  const double fr1 = hr * ur, fr2 = hr * (ur * ur) + g * hr * hr / 2.0, fr3 = hr * ur * vr;
-  double x1, x2, x3, y1, y2, y3;
+  const T fl1 = hl * ul, fl2 = hl * (ul * ul) + g * hl * hl / 2.0, fl3 = hl * ul * vl;
+  const T fr1 = hr * ur, fr2 = hr * (ur * ur) + g * hr * hr / 2.0, fr3 = hr * ur * vr;
+  T x1, x2, x3, y1, y2, y3;
   if (IFLUX == 1) {
     /* A: sl > 0 -> FL | sr < 0 -> FR | HLL with the tangential component of the upwind side
      * of s*.  B: -sr > 0 -> FR | -sl < 0 -> FL | HLL, tangential by -s*. */
-    const int ra = (sl > 0) ? 0 : ((sr < 0) ? 1 : 2);
-    const int rb = (-sr > 0) ? 1 : ((-sl < 0) ? 0 : 2);
-    double h1 = 0.0, h2 = 0.0;
+    const int ra = (sl > 0.) ? 0 : ((sr < 0.) ? 1 : 2);
+    const int rb = (-sr > 0.) ? 1 : ((-sl < 0.) ? 0 : 2);
+    T h1 = T(0.0), h2 = T(0.0);
     if (ra == 2 || rb == 2) {
-      const double den = sr - sl + eps, yden = 1.0 / den;
+      const T den = sr - sl + eps, yden = 1.0 / den;
       h1 = div_rn(sr * fl1 - sl * fr1 + sl * sr * (hr - hl), den, yden);
       h2 = div_rn(sr * fl2 - sl * fr2 + sl * sr * (hr * ur - hl * ul), den, yden);
     }
     if (ra == 0) { x1 = fl1; x2 = fl2; x3 = fl3; }
     else if (ra == 1) { x1 = fr1; x2 = fr2; x3 = fr3; }
-    else { x1 = h1; x2 = h2; x3 = (set > 0) ? h1 * vl : h1 * vr; }
+    else { x1 = h1; x2 = h2; x3 = (set > 0.) ? h1 * vl : h1 * vr; }
     if (rb == 0) { y1 = fl1; y2 = fl2; y3 = fl3; }
     else if (rb == 1) { y1 = fr1; y2 = fr2; y3 = fr3; }
-    else { y1 = h1; y2 = h2; y3 = (-set > 0) ? h1 * vr : h1 * vl; }
+    else { y1 = h1; y2 = h2; y3 = (-set > 0.) ? h1 * vr : h1 * vl; }
   } else {
-    const double pl = (fabs(sl - set) > eps) ? hl * (sl - ul) / (sl - set) : 0.0;
-    const double pr = (fabs(sr - set) > eps) ? hr * (sr - ur) / (sr - set) : 0.0;
-    const double el1 = fl1 + sl * (pl - hl), el2 = fl2 + sl * (pl * set - hl * ul), el3 = fl3 + sl * (pl * vl - hl * vl);
-    const double er1 = fr1 + sr * (pr - hr), er2 = fr2 + sr * (pr * set - hr * ur), er3 = fr3 + sr * (pr * vr - hr * vr);
+    const T pl = (fabs(sl - set) > eps) ? hl * (sl - ul) / (sl - set) : T(0.0);
+    const T pr = (fabs(sr - set) > eps) ? hr * (sr - ur) / (sr - set) : T(0.0);
+    const T el1 = fl1 + sl * (pl - hl), el2 = fl2 + sl * (pl * set - hl * ul), el3 = fl3 + sl * (pl * vl - hl * vl);
+    const T er1 = fr1 + sr * (pr - hr), er2 = fr2 + sr * (pr * set - hr * ur), er3 = fr3 + sr * (pr * vr - hr * vr);
     /* A: 0<sl FL | 0<s* & 0>sl EL | 0>s* & 0<sr ER | FR.
      * B (sl'=-sr, s*'=-s*, sr'=-sl): 0<-sr FR | 0<-s* & 0>-sr ER | 0>-s* & 0<-sl EL | FL. */
     int ra, rb;
@@ -251,84 +265,86 @@ CF_HD CF_INLINE void first_order_flux(double g, double nx, double ny, double hl,
 }
 
 /* WAF limiter (flux_riemann.cuf:465-524).  The superbee gaps at r = 0.5, 1, 2 are kept. */
-CF_HD CF_INLINE double waf_limiter(int ilim, double r, double c) {
-  double A = 1.;
+template <class T>
+CF_HD CF_INLINE T waf_limiter(int ilim, T r, T c) {
+  T A = T(1.);
   if (ilim == 1) {
-    if (r <= 0) A = 1.;
+    if (r <= 0.) A = T(1.);
     else if (r > 0. && r < 0.5) A = 1. - 2. * (1. - fabs(c)) * r;
     else if (r > 0.5 && r < 1.) A = fabs(c);
     else if (r > 1. && r < 2.) A = 1. - (1. - fabs(c)) * r;
     else A = 2. * fabs(c) - 1.;
   } else if (ilim == 2) {
-    if (r <= 0) A = 1.;
-    else A = 1 - 2 * (1 - fabs(c)) * r / (1 + r);
+    if (r <= 0.) A = T(1.);
+    else A = 1. - 2. * (1. - fabs(c)) * r / (1. + r);
   } else if (ilim == 3) {
-    if (r <= 0) A = 1.;
+    if (r <= 0.) A = T(1.);
     else A = 1. - (1. - fabs(c)) * r * (1. + r) / (1. + r * r);
   } else if (ilim == 4) {
-    if (r <= 0) A = 1.;
-    else if (r <= 1) A = 1 - (1 - fabs(c)) * r;
+    if (r <= 0.) A = T(1.);
+    else if (r <= 1.) A = 1. - (1. - fabs(c)) * r;
     else A = fabs(c);
   }
   return A;
 }
 
-CF_HD CF_INLINE double sgn1(double x) { return copysign(1.0, x); }
+template <class T>
+CF_HD CF_INLINE double sgn1(const T& x) { return copysign(1.0, val(x)); }
 
 /* Second-order WAF (IFLUX 3, flux_riemann.cuf:720-900) for both sides.  Inputs: the
  * reconstructed, masked edge-frame states of A (left) and B (right), the upwind
  * reconstructions (h, v) of each side, dt, and the distances d_mrl, d_mkvol (A), d_mkvoisin (B). */
+template <class T>
 CF_HD CF_INLINE void waf_flux(double g, int ilim, double nx, double ny, double dt, double d_mrl, double y_mrl,
-                              double d_mkvol, double y_mkvol, double d_mkvoisin, double y_mkvoisin, double hl,
-                              double ul, double vl, double hr, double ur, double vr, double hl_upw, double vl_upw,
-                              double hr_upw, double vr_upw, TwoFlux& F) {
+                              double d_mkvol, double y_mkvol, double d_mkvoisin, double y_mkvoisin, T hl, T ul,
+                              T vl, T hr, T ur, T vr, T hl_upw, T vl_upw, T hr_upw, T vr_upw, TwoFluxT<T>& F) {
   const double eps = EPS_SECOND;
-  double sl, sr, set;
+  T sl, sr, set;
   if (!wave_speeds(g, eps, hl, ul, hr, ur, sl, sr, set)) {
-    F.a1 = F.a2 = F.a3 = F.b1 = F.b2 = F.b3 = 0.0;
+    F.a1 = F.a2 = F.a3 = F.b1 = F.b2 = F.b3 = T(0.0);
     return;
   }
-  const double fl1 = hl * ul, fl2 = hl * (ul * ul) + g * hl * hl / 2.0;
-  const double fr1 = hr * ur, fr2 = hr * (ur * ur) + g * hr * hr / 2.0;
-  const int ra = (sl > 0) ? 0 : ((sr < 0) ? 1 : 2);
-  const int rb = (-sr > 0) ? 1 : ((-sl < 0) ? 0 : 2);
-  double h1 = 0.0, h2 = 0.0;
+  const T fl1 = hl * ul, fl2 = hl * (ul * ul) + g * hl * hl / 2.0;
+  const T fr1 = hr * ur, fr2 = hr * (ur * ur) + g * hr * hr / 2.0;
+  const int ra = (sl > 0.) ? 0 : ((sr < 0.) ? 1 : 2);
+  const int rb = (-sr > 0.) ? 1 : ((-sl < 0.) ? 0 : 2);
+  T h1 = T(0.0), h2 = T(0.0);
   if (ra == 2 || rb == 2) {
-    const double den = sr - sl + eps, yden = 1.0 / den;
+    const T den = sr - sl + eps, yden = 1.0 / den;
     h1 = div_rn(sr * fl1 - sl * fr1 + sl * sr * (hr - hl), den, yden);
     h2 = div_rn(sr * fl2 - sl * fr2 + sl * sr * (hr * ur - hl * ul), den, yden);
   }
-  const double ha1 = (ra == 0) ? fl1 : ((ra == 1) ? fr1 : h1);
-  const double ha2 = (ra == 0) ? fl2 : ((ra == 1) ? fr2 : h2);
-  const double hb1 = (rb == 0) ? fl1 : ((rb == 1) ? fr1 : h1);
-  const double hb2 = (rb == 0) ? fl2 : ((rb == 1) ? fr2 : h2);
+  const T ha1 = (ra == 0) ? fl1 : ((ra == 1) ? fr1 : h1);
+  const T ha2 = (ra == 0) ? fl2 : ((ra == 1) ? fr2 : h2);
+  const T hb1 = (rb == 0) ? fl1 : ((rb == 1) ? fr1 : h1);
+  const T hb2 = (rb == 0) ? fl2 : ((rb == 1) ? fr2 : h2);
 
   const double dtoverdx = div_rn(dt, d_mrl, y_mrl);
-  const double cr = sr * dtoverdx, cl = sl * dtoverdx, cet = set * dtoverdx;
-  const double dloc = div_rn(hr - hl, d_mrl, y_mrl);          /* delta_loc_l = delta_loc_r */
-  const double dloc_et = div_rn(vr - vl, d_mrl, y_mrl);
-  const double upl = div_rn(hl - hl_upw, d_mkvol, y_mkvol);     /* upwind difference of side A */
-  const double upr = div_rn(hr_upw - hr, d_mkvoisin, y_mkvoisin);  /* upwind difference of side B */
-  const double upvl = div_rn(vl - vl_upw, d_mkvol, y_mkvol);
-  const double upvr = div_rn(vr_upw - vr, d_mkvoisin, y_mkvoisin);
-  const double ret_a = ((set > 0) ? upvl : upvr) / (dloc_et + eps);
+  const T cr = sr * dtoverdx, cl = sl * dtoverdx, cet = set * dtoverdx;
+  const T dloc = div_rn(hr - hl, d_mrl, y_mrl);          /* delta_loc_l = delta_loc_r */
+  const T dloc_et = div_rn(vr - vl, d_mrl, y_mrl);
+  const T upl = div_rn(hl - hl_upw, d_mkvol, y_mkvol);     /* upwind difference of side A */
+  const T upr = div_rn(hr_upw - hr, d_mkvoisin, y_mkvoisin);  /* upwind difference of side B */
+  const T upvl = div_rn(vl - vl_upw, d_mkvol, y_mkvol);
+  const T upvr = div_rn(vr_upw - vr, d_mkvoisin, y_mkvoisin);
+  const T ret_a = ((set > 0.) ? upvl : upvr) / (dloc_et + eps);
 
   /* side A (:854-899) */
   {
-    const double den = dloc + eps, yd = 1.0 / den;
-    const double rl = div_rn((sl > 0) ? upl : upr, den, yd);
-    const double rr = div_rn((sr > 0) ? upl : upr, den, yd);
-    const double ll = waf_limiter(ilim, rl, cl);
-    const double lr = waf_limiter(ilim, rr, cr);
-    const double le = waf_limiter(ilim, ret_a, cet);
-    const double wl = (1 + sgn1(sl) * ll) / 2.;
-    const double wlet = (1 + sgn1(set) * le) / 2.;
-    const double wlr = (sgn1(sr) * lr - sgn1(sl) * ll) / 2.;
-    const double wr = (1 - sgn1(sr) * lr) / 2.;
-    const double wret = (1 - sgn1(set) * le) / 2.;
-    const double fw1 = wl * fl1 + wlr * ha1 + wr * fr1;
-    const double fw2 = wl * fl2 + wlr * ha2 + wr * fr2;
-    const double fw3 = (wlet * vl + wret * vr) * fw1;
+    const T den = dloc + eps, yd = 1.0 / den;
+    const T rl = div_rn((sl > 0.) ? upl : upr, den, yd);
+    const T rr = div_rn((sr > 0.) ? upl : upr, den, yd);
+    const T ll = waf_limiter(ilim, rl, cl);
+    const T lr = waf_limiter(ilim, rr, cr);
+    const T le = waf_limiter(ilim, ret_a, cet);
+    const T wl = (1. + sgn1(sl) * ll) / 2.;
+    const T wlet = (1. + sgn1(set) * le) / 2.;
+    const T wlr = (sgn1(sr) * lr - sgn1(sl) * ll) / 2.;
+    const T wr = (1. - sgn1(sr) * lr) / 2.;
+    const T wret = (1. - sgn1(set) * le) / 2.;
+    const T fw1 = wl * fl1 + wlr * ha1 + wr * fr1;
+    const T fw2 = wl * fl2 + wlr * ha2 + wr * fr2;
+    const T fw3 = (wlet * vl + wret * vr) * fw1;
     F.a1 = fw1;
     F.a2 = nx * fw2 - ny * fw3;
     F.a3 = ny * fw2 + nx * fw3;
@@ -337,23 +353,23 @@ CF_HD CF_INLINE void waf_flux(double g, int ilim, double nx, double ny, double d
    * (hl - hr)/d = -dloc, its upwind differences are minus A's (for the wave it tests), the
    * tangential ones coincide; its Courant numbers are -cr, -cl, -cet. */
   {
-    const double den = -dloc + eps, yd = 1.0 / den;
-    const double rl = div_rn((-sr > 0) ? -upr : -upl, den, yd);
-    const double rr = div_rn((-sl > 0) ? -upr : -upl, den, yd);
+    const T den = -dloc + eps, yd = 1.0 / den;
+    const T rl = div_rn((-sr > 0.) ? -upr : -upl, den, yd);
+    const T rr = div_rn((-sl > 0.) ? -upr : -upl, den, yd);
     /* B's tangential ratio differs from A's only when s* == 0 (or is NaN) */
-    const double ret_b = (set > 0 || set < 0) ? ret_a : ((-set > 0) ? upvr : upvl) / (dloc_et + eps);
-    const double ll = waf_limiter(ilim, rl, -cr);
-    const double lr = waf_limiter(ilim, rr, -cl);
-    const double le = waf_limiter(ilim, ret_b, -cet);
-    const double wl = (1 + sgn1(-sr) * ll) / 2.;
-    const double wlet = (1 + sgn1(-set) * le) / 2.;
-    const double wlr = (sgn1(-sl) * lr - sgn1(-sr) * ll) / 2.;
-    const double wr = (1 - sgn1(-sl) * lr) / 2.;
-    const double wret = (1 - sgn1(-set) * le) / 2.;
+    const T ret_b = (set > 0. || set < 0.) ? ret_a : ((-set > 0.) ? upvr : upvl) / (dloc_et + eps);
+    const T ll = waf_limiter(ilim, rl, -cr);
+    const T lr = waf_limiter(ilim, rr, -cl);
+    const T le = waf_limiter(ilim, ret_b, -cet);
+    const T wl = (1. + sgn1(-sr) * ll) / 2.;
+    const T wlet = (1. + sgn1(-set) * le) / 2.;
+    const T wlr = (sgn1(-sl) * lr - sgn1(-sr) * ll) / 2.;
+    const T wr = (1. - sgn1(-sl) * lr) / 2.;
+    const T wret = (1. - sgn1(-set) * le) / 2.;
     /* mirrored physical fluxes: FL' = (-fr1, fr2), FR' = (-fl1, fl2), HLL' = (-hb1, hb2) */
-    const double fw1 = -(wl * fr1 + wlr * hb1 + wr * fl1);
-    const double fw2 = wl * fr2 + wlr * hb2 + wr * fl2;
-    const double fw3 = -(wlet * vr + wret * vl) * fw1;
+    const T fw1 = -(wl * fr1 + wlr * hb1 + wr * fl1);
+    const T fw2 = wl * fr2 + wlr * hb2 + wr * fl2;
+    const T fw3 = -(wlet * vr + wret * vl) * fw1;
     /* B's normal is -n: (fw1, -n1 fw2 + n2 fw3, -n2 fw2 - n1 fw3) */
     F.b1 = fw1;
     F.b2 = -nx * fw2 + ny * fw3;
@@ -372,14 +388,14 @@ CF_HD CF_INLINE double inlet_discharge(const MemberDev& M, int id, double t) {
 }
 
 /* Boundary-edge flux of side A (flux_riemann.cuf:114-171). */
-CF_HD CF_INLINE void boundary_flux(int iflux, const MemberDev& M, int kind, int id, double t, double nx,
-                                   double ny, double h, double hu, double hv, double z, double& f1,
-                                   double& f2, double& f3, double& q) {
+template <class T>
+CF_HD CF_INLINE void boundary_flux(int iflux, const MemberDev& M, int kind, int id, double t, double nx, double ny,
+                                   T h, T hu, T hv, double z, T& f1, T& f2, T& f3, T& q) {
   const double g = M.gp, tolisec = M.tolisec;
-  double hautl, vitul, vitvl;
+  T hautl, vitul, vitvl;
   to_frame(h, hu, hv, nx, ny, tolisec, hautl, vitul, vitvl);
-  f1 = f2 = f3 = 0.0;
-  q = 0.0;
+  f1 = f2 = f3 = T(0.0);
+  q = T(0.0);
   if (kind == -1) {
     if (M.inlet == 1) {
       f1 = hautl * vitul;
@@ -387,10 +403,10 @@ CF_HD CF_INLINE void boundary_flux(int iflux, const MemberDev& M, int kind, int 
       f3 = ny * (hautl * (vitul * vitul) + g * (hautl * hautl) / 2.) + nx * hautl * vitul * vitvl;
     } else if (M.inlet == 2) {
       const double debitnorm = -inlet_discharge(M, id, t) / M.long_entree[id - 1];
-      f1 = debitnorm;
+      f1 = T(debitnorm);
       f2 = nx * ((debitnorm * debitnorm) / (hautl + tolisec) + g * (hautl * hautl) / 2.);
       f3 = ny * ((debitnorm * debitnorm) / (hautl + tolisec) + g * (hautl * hautl) / 2.);
-      q = -debitnorm;
+      q = T(-debitnorm);
     }
   } else if (kind == -3) {
     f2 = nx * g * (hautl * hautl) / 2.;
@@ -413,12 +429,12 @@ CF_HD CF_INLINE void boundary_flux(int iflux, const MemberDev& M, int kind, int 
        * right (:173-181); second-order schemes use first-order HLLC here (their centroid
        * distance to themselves is zero). */
       const double zij = dmax(z, z);
-      double hsl = dmax(0.0, hautl + z - zij);
-      double hsr = dmax(0.0, ((iflux <= 2) ? h : hautl) + z - zij);
-      double ul = vitul, vl = vitvl, ur = vitul, vr = vitvl;
-      if (hsl < tolisec) { hsl = 0.; ul = 0.; vl = 0.; }
-      if (hsr < tolisec) { hsr = 0.; ur = 0.; vr = 0.; }
-      TwoFlux F;
+      T hsl = dmax(T(0.0), hautl + z - zij);
+      T hsr = dmax(T(0.0), ((iflux <= 2) ? h : hautl) + z - zij);
+      T ul = vitul, vl = vitvl, ur = vitul, vr = vitvl;
+      if (hsl < tolisec) { hsl = T(0.); ul = T(0.); vl = T(0.); }
+      if (hsr < tolisec) { hsr = T(0.); ur = T(0.); vr = T(0.); }
+      TwoFluxT<T> F;
       if (iflux == 2) first_order_flux<2>(g, nx, ny, hsl, ul, vl, hsr, ur, vr, F);
       else first_order_flux<1>(g, nx, ny, hsl, ul, vl, hsr, ur, vr, F);
       f1 = F.a1; f2 = F.a2; f3 = F.a3;
@@ -426,43 +442,157 @@ CF_HD CF_INLINE void boundary_flux(int iflux, const MemberDev& M, int kind, int 
   }
 }
 
-/* Upwind reconstruction of one side (flux_riemann.cuf:240-366): a copy of one element's
- * masked state when d1 < 0 (one upwind element, or the first-order fallback), else the
- * centroid-distance weighted average of two. */
+/* Upwind reconstruction (h, v) of one side from the states of its upwind elements
+ * (flux_riemann.cuf:240-366): a copy of element 1's masked state when d1 < 0 (one upwind
+ * element, or the first-order fallback), else the centroid-distance weighted average of two. */
+template <class T>
+CF_HD CF_INLINE void upwind_mix(T h1, T hu1, T hv1, T h2, T hu2, T hv2, double d1, double d2, double ysum,
+                                double nx, double ny, double tolisec, T& hu_, T& vu_) {
+  T a, va;
+  to_frame_t(h1, hu1, hv1, nx, ny, tolisec, a, va);
+  if (d1 < 0.0) {
+    hu_ = a;
+    vu_ = va;
+    return;
+  }
+  T b, vb;
+  to_frame_t(h2, hu2, hv2, nx, ny, tolisec, b, vb);
+  const double ds = d1 + d2;
+  hu_ = div_rn(d1 * a + d2 * b, ds, ysum);
+  vu_ = div_rn(d1 * va + d2 * vb, ds, ysum);
+}
+
+/* The same, loading the elements' states, and the matching bed elevation. */
 CF_HD CF_INLINE void upwind_state(const double4* U, int i1, int i2, double d1, double d2, double ysum, double nx,
                                   double ny, double tolisec, double& hu_, double& vu_, double& zu_) {
   const double4 A1 = ld4(U + i1);
-  double h1, v1;
-  to_frame_t(A1.x, A1.y, A1.z, nx, ny, tolisec, h1, v1);
   if (d1 < 0.0) {
-    hu_ = h1; vu_ = v1; zu_ = A1.w;
+    upwind_mix(A1.x, A1.y, A1.z, 0.0, 0.0, 0.0, d1, d2, ysum, nx, ny, tolisec, hu_, vu_);
+    zu_ = A1.w;
     return;
   }
   const double4 A2 = ld4(U + i2);
-  double h2, v2;
-  to_frame_t(A2.x, A2.y, A2.z, nx, ny, tolisec, h2, v2);
-  const double ds = d1 + d2;
-  hu_ = div_rn(d1 * h1 + d2 * h2, ds, ysum);
-  vu_ = div_rn(d1 * v1 + d2 * v2, ds, ysum);
-  zu_ = div_rn(d1 * A1.w + d2 * A2.w, ds, ysum);
+  upwind_mix(A1.x, A1.y, A1.z, A2.x, A2.y, A2.z, d1, d2, ysum, nx, ny, tolisec, hu_, vu_);
+  zu_ = div_rn(d1 * A1.w + d2 * A2.w, d1 + d2, ysum);
 }
 
-/* ---- one edge: the body of the edge kernel ----------------------------------------------- */
+/* ---- one edge ------------------------------------------------------------------------- */
+
+/* Static data of an interior edge beyond its normal: length, centroid distance and, for the
+ * second-order scheme, the upwind distances and reciprocals. */
+struct EdgeGeo {
+  double nx, ny, len, d_mrl;
+  double y_mrl, d_mkvol, y_mkvol, d_mkvoisin, y_mkvoisin;
+  double ysum_a, ysum_b;  /* RN(1/(d1+d2)) of the upwind pairs of sides A and B */
+};
+
+/* Both sides' slot values of an interior edge: out[0..4] = side A {f1, f2, f3} * len and its
+ * bed source {bx, by}; out[5..9] the same for side B.  hl_upw .. vr_upw are the upwind
+ * reconstructions of sides A and B (second order only), zl_upw / zr_upw their bed elevations. */
+template <int IFLUX, class T>
+CF_HD CF_INLINE void interior_edge(const MemberDev& M, int ilim, int flux_mode, const EdgeGeo& G, double dt, T hA,
+                                   T huA, T hvA, double zml, T hB, T huB, T hvB, double zmr, T hl_upw, T vl_upw,
+                                   double zl_upw, T hr_upw, T vr_upw, double zr_upw, T out[10]) {
+  const double g = M.gp, tolisec = M.tolisec;
+  const double nx = G.nx, ny = G.ny, len = G.len;
+  const double zij = dmax(zml, zmr);
+  T hautl, vitul, vitvl, hautr, vitur, vitvr;
+  to_frame(hA, huA, hvA, nx, ny, tolisec, hautl, vitul, vitvl);
+  to_frame(hB, huB, hvB, nx, ny, tolisec, hautr, vitur, vitvr);
+  TwoFluxT<T> F;
+  if (IFLUX <= 2) {
+    /* hydrostatic reconstruction (:176-181, :200-210): A from its masked depth, B from its
+     * raw depth; the raw and masked depths differ only for 0 < h <= tolisec, where side B's
+     * own evaluation (B masked, A raw) is computed separately. */
+    T hijet = dmax(T(0.0), hautl + zml - zij);
+    T hjiet = dmax(T(0.0), hB + zmr - zij);
+    T ul = vitul, vl = vitvl, ur = vitur, vr = vitvr;
+    if (hijet < tolisec) { hijet = T(0.); ul = T(0.); vl = T(0.); }
+    if (hjiet < tolisec) { hjiet = T(0.); ur = T(0.); vr = T(0.); }
+    first_order_flux<IFLUX>(g, nx, ny, hijet, ul, vl, hjiet, ur, vr, F);
+    if (hautl != hA || hautr != hB) {
+      T bl = dmax(T(0.0), hautr + zmr - zij), br = dmax(T(0.0), hA + zml - zij);
+      T bul = -vitur, bvl = -vitvr, bur = -vitul, bvr = -vitvl;
+      if (bl < tolisec) { bl = T(0.); bul = T(0.); bvl = T(0.); }
+      if (br < tolisec) { br = T(0.); bur = T(0.); bvr = T(0.); }
+      TwoFluxT<T> Gm;
+      first_order_flux<IFLUX>(g, -nx, -ny, bl, bul, bvl, br, bur, bvr, Gm);
+      F.b1 = Gm.a1;
+      F.b2 = Gm.a2;
+      F.b3 = Gm.a3;
+    }
+  } else {
+    /* hydrostatic reconstruction of the four states (:370-400) */
+    T hijet = dmax(T(0.0), hautl + zml - zij);
+    T hlu = dmax(T(0.0), hl_upw + zl_upw - zij);
+    T hjiet = dmax(T(0.0), hautr + zmr - zij);
+    T hru = dmax(T(0.0), hr_upw + zr_upw - zij);
+    T ul = vitul, vl = vitvl, ur = vitur, vr = vitvr, vlu = vl_upw, vru = vr_upw;
+    if (hijet < tolisec) { hijet = T(0.); ul = T(0.); vl = T(0.); }
+    if (hlu < tolisec) { hlu = T(0.); vlu = T(0.); }
+    if (hjiet < tolisec) { hjiet = T(0.); ur = T(0.); vr = T(0.); }
+    if (hru < tolisec) { hru = T(0.); vru = T(0.); }
+    waf_flux(g, ilim, nx, ny, dt, G.d_mrl, G.y_mrl, G.d_mkvol, G.y_mkvol, G.d_mkvoisin, G.y_mkvoisin, hijet, ul, vl,
+             hjiet, ur, vr, hlu, vlu, hru, vru, F);
+  }
+  if (flux_mode == 1) {
+    F.b1 = -F.a1;
+    F.b2 = -F.a2;
+    F.b3 = -F.a3;
+  }
+  /* bed-slope source of both sides from the raw depths (source_terms.cuf:90-97) */
+  const T ha = dmax(T(0.0), hA + zml - zij);
+  const T hb = dmax(T(0.0), hB + zmr - zij);
+  const T ta = g / 2.0 * (ha * ha - hA * hA) * len;
+  const T tb = g / 2.0 * (hb * hb - hB * hB) * len;
+  out[0] = F.a1 * len;
+  out[1] = F.a2 * len;
+  out[2] = F.a3 * len;
+  out[3] = ta * nx;
+  out[4] = ta * ny;
+  out[5] = F.b1 * len;
+  out[6] = F.b2 * len;
+  out[7] = F.b3 * len;
+  out[8] = -(tb * nx);
+  out[9] = -(tb * ny);
+}
+
+/* Static data of edge e in the form interior_edge takes. */
+CF_HD CF_INLINE EdgeGeo edge_geo(const StepArgs& a, int e, bool second) {
+  const double4 geo = ld4(a.egeo + e);
+  EdgeGeo G;
+  G.nx = geo.x;
+  G.ny = geo.y;
+  G.len = geo.z;
+  G.d_mrl = geo.w;
+  G.y_mrl = G.d_mkvol = G.y_mkvol = G.d_mkvoisin = G.y_mkvoisin = G.ysum_a = G.ysum_b = 0.0;
+  if (second) {
+    const double4 dk = ld4(a.edk + e);    /* d_mkvol, d_mkvoisin and their reciprocals */
+    const double4 yi = ld4(a.einv + e);   /* 1/d_mrl, 1/(d1+d2) of A and of B */
+    G.y_mrl = yi.x;
+    G.d_mkvol = dk.x;
+    G.y_mkvol = dk.z;
+    G.d_mkvoisin = dk.y;
+    G.y_mkvoisin = dk.w;
+    G.ysum_a = yi.y;
+    G.ysum_b = yi.z;
+  }
+  return G;
+}
 
 /* Fluxes (times the edge length) and bed sources of edge e into its two slots, from the
- * state U of step n. */
+ * state U of step n: the body of the edge kernel. */
 template <int IFLUX>
 CF_HD CF_INLINE void edge_body(const StepArgs& a, const MemberDev& M, int e, double dt, double t) {
   const int2 ab = ldro(a.ecell + e);
-  const double4 geo = ld4(a.egeo + e);
-  const double nx = geo.x, ny = geo.y, len = geo.z;
   const double4 UA = ld4(a.Uin + ab.x);
-  const double g = M.gp, tolisec = M.tolisec;
   Slot* sa = a.slots + 2 * (size_t)e;
 
   if (ab.y < 0) {
+    const double4 geo = ld4(a.egeo + e);
+    const double len = geo.z;
     double f1, f2, f3, q;
-    boundary_flux(IFLUX, M, ab.y, ldro(a.ebid + e), t, nx, ny, UA.x, UA.y, UA.z, UA.w, f1, f2, f3, q);
+    boundary_flux(IFLUX, M, ab.y, ldro(a.ebid + e), t, geo.x, geo.y, UA.x, UA.y, UA.z, UA.w, f1, f2, f3, q);
     sa->f1 = f1 * len;
     sa->f2 = f2 * len;
     sa->f3 = f3 * len;
@@ -472,81 +602,34 @@ CF_HD CF_INLINE void edge_body(const StepArgs& a, const MemberDev& M, int e, dou
     return;
   }
 
+  const EdgeGeo G = edge_geo(a, e, IFLUX >= 3);
   const double4 UB = ld4(a.Uin + ab.y);
-  const double zml = UA.w, zmr = UB.w;
-  const double zij = dmax(zml, zmr);
-  double hautl, vitul, vitvl, hautr, vitur, vitvr;
-  to_frame(UA.x, UA.y, UA.z, nx, ny, tolisec, hautl, vitul, vitvl);
-  to_frame(UB.x, UB.y, UB.z, nx, ny, tolisec, hautr, vitur, vitvr);
-  TwoFlux F;
-  if (IFLUX <= 2) {
-    /* hydrostatic reconstruction (:176-181, :200-210): A from its masked depth, B from its
-     * raw depth; the raw and masked depths differ only for 0 < h <= tolisec, where side B's
-     * own evaluation (B masked, A raw) is computed separately. */
-    double hijet = dmax(0.0, hautl + zml - zij);
-    double hjiet = dmax(0.0, UB.x + zmr - zij);
-    double ul = vitul, vl = vitvl, ur = vitur, vr = vitvr;
-    if (hijet < tolisec) { hijet = 0.; ul = 0.; vl = 0.; }
-    if (hjiet < tolisec) { hjiet = 0.; ur = 0.; vr = 0.; }
-    first_order_flux<IFLUX>(g, nx, ny, hijet, ul, vl, hjiet, ur, vr, F);
-    if (hautl != UA.x || hautr != UB.x) {
-      double bl = dmax(0.0, hautr + zmr - zij), br = dmax(0.0, UA.x + zml - zij);
-      double bul = -vitur, bvl = -vitvr, bur = -vitul, bvr = -vitvl;
-      if (bl < tolisec) { bl = 0.; bul = 0.; bvl = 0.; }
-      if (br < tolisec) { br = 0.; bur = 0.; bvr = 0.; }
-      TwoFlux G;
-      first_order_flux<IFLUX>(g, -nx, -ny, bl, bul, bvl, br, bur, bvr, G);
-      F.b1 = G.a1;
-      F.b2 = G.a2;
-      F.b3 = G.a3;
-    }
-  } else {
+  double hl_upw = 0.0, vl_upw = 0.0, zl_upw = 0.0, hr_upw = 0.0, vr_upw = 0.0, zr_upw = 0.0;
+  if (IFLUX >= 3) {
     const int4 up = ldro(a.eupw + e);
     const double4 dw = ld4(a.ewts + e);   /* d1, d2 of side A, d1, d2 of side B */
-    const double4 dk = ld4(a.edk + e);    /* d_mkvol, d_mkvoisin and their reciprocals */
-    const double4 yi = ld4(a.einv + e);   /* 1/d_mrl, 1/(d1+d2) of A and of B */
-    double hl_upw, vl_upw, zml_upw, hr_upw, vr_upw, zmr_upw;
-    upwind_state(a.Uin, up.x, up.y, dw.x, dw.y, yi.y, nx, ny, tolisec, hl_upw, vl_upw, zml_upw);
-    upwind_state(a.Uin, up.z, up.w, dw.z, dw.w, yi.z, nx, ny, tolisec, hr_upw, vr_upw, zmr_upw);
-    /* hydrostatic reconstruction of the four states (:370-400) */
-    double hijet = dmax(0.0, hautl + zml - zij);
-    hl_upw = dmax(0.0, hl_upw + zml_upw - zij);
-    double hjiet = dmax(0.0, hautr + zmr - zij);
-    hr_upw = dmax(0.0, hr_upw + zmr_upw - zij);
-    double ul = vitul, vl = vitvl, ur = vitur, vr = vitvr;
-    if (hijet < tolisec) { hijet = 0.; ul = 0.; vl = 0.; }
-    if (hl_upw < tolisec) { hl_upw = 0.; vl_upw = 0.; }
-    if (hjiet < tolisec) { hjiet = 0.; ur = 0.; vr = 0.; }
-    if (hr_upw < tolisec) { hr_upw = 0.; vr_upw = 0.; }
-    waf_flux(g, a.ilimiteur, nx, ny, dt, geo.w, yi.x, dk.x, dk.z, dk.y, dk.w, hijet, ul, vl, hjiet, ur, vr, hl_upw,
-             vl_upw, hr_upw, vr_upw, F);
+    upwind_state(a.Uin, up.x, up.y, dw.x, dw.y, G.ysum_a, G.nx, G.ny, M.tolisec, hl_upw, vl_upw, zl_upw);
+    upwind_state(a.Uin, up.z, up.w, dw.z, dw.w, G.ysum_b, G.nx, G.ny, M.tolisec, hr_upw, vr_upw, zr_upw);
   }
-  if (a.flux_mode == 1) {
-    F.b1 = -F.a1;
-    F.b2 = -F.a2;
-    F.b3 = -F.a3;
-  }
-  /* bed-slope source of both sides from the raw depths (source_terms.cuf:90-97) */
-  const double ha = dmax(0.0, UA.x + zml - zij);
-  const double hb = dmax(0.0, UB.x + zmr - zij);
-  const double ta = g / 2.0 * (ha * ha - UA.x * UA.x) * len;
-  const double tb = g / 2.0 * (hb * hb - UB.x * UB.x) * len;
+  double o[10];
+  interior_edge<IFLUX>(M, a.ilimiteur, a.flux_mode, G, dt, UA.x, UA.y, UA.z, UA.w, UB.x, UB.y, UB.z, UB.w, hl_upw,
+                       vl_upw, zl_upw, hr_upw, vr_upw, zr_upw, o);
   Slot* sb = sa + 1;
-  sa->f1 = F.a1 * len;
-  sa->f2 = F.a2 * len;
-  sa->f3 = F.a3 * len;
-  sa->bx = ta * nx;
-  sa->by = ta * ny;
+  sa->f1 = o[0];
+  sa->f2 = o[1];
+  sa->f3 = o[2];
+  sa->bx = o[3];
+  sa->by = o[4];
   sa->q = 0.0;
-  sb->f1 = F.b1 * len;
-  sb->f2 = F.b2 * len;
-  sb->f3 = F.b3 * len;
-  sb->bx = -(tb * nx);
-  sb->by = -(tb * ny);
+  sb->f1 = o[5];
+  sb->f2 = o[6];
+  sb->f3 = o[7];
+  sb->bx = o[8];
+  sb->by = o[9];
   sb->q = 0.0;
 }
 
-/* ---- one element: the body of the element kernel ---------------------------------------- */
+/* ---- one element ------------------------------------------------------------------------ */
 
 /* CFL time step of one element (cfl_condition.cuf:20-37); cflL = cfl * L_cfl. */
 CF_HD CF_INLINE double cfl_dt_elem(const MemberDev& M, double cflL, double h, double hu, double hv) {
@@ -562,45 +645,39 @@ CF_HD CF_INLINE double cfl_dt_elem(const MemberDev& M, double cflL, double h, do
   return d;
 }
 
-/* Sources, friction and update of element c (source_terms.cuf:33-211,
- * finite_volumes_method.cuf:283-303).  st = {area, manning n, cfl*L_cfl, 1/area}.  Returns the
- * new state; sets *nonfinite when it is not finite. */
-CF_HD CF_INLINE double4 element_update(const MemberDev& M, const double4 U, const double4 st, const Slot& s0,
-                                       const Slot& s1, const Slot& s2, double dt, bool& nonfinite) {
+/* Sources, friction and update of one element (source_terms.cuf:33-211,
+ * finite_volumes_method.cuf:283-303) from its state q, the sums rc of its three edge fluxes
+ * and sb of its bed sources, its area (and RN(1/area)) and its Manning n.  The wet/dry clamp
+ * of the new depth is part of the map. */
+template <class T>
+CF_HD CF_INLINE void element_core(const MemberDev& M, double area, double yarea, T manning, T q1, T q2, T q3, T rc1,
+                                  T rc2, T rc3, T sb2, T sb3, double dt, T& h, T& hu, T& hv, bool& nonfinite) {
   const double gp = M.gp, tolisec = M.tolisec, tol = M.tol;
-  const double area = st.x, manning = st.y;
-  const double q1 = U.x, q2 = U.y, q3 = U.z;
-  /* fixed-order sums over the three edges (flux_riemann.cuf:411-426, source_terms.cuf:54-100) */
-  const double rc1 = s0.f1 + s1.f1 + s2.f1;
-  const double rc2 = s0.f2 + s1.f2 + s2.f2;
-  const double rc3 = s0.f3 + s1.f3 + s2.f3;
-  const double sb2 = s0.bx + s1.bx + s2.bx;
-  const double sb3 = s0.by + s1.by + s2.by;
-  double r1, r2, r3;
+  T r1, r2, r3;
   if (M.friction == 1) {
-    double sf2 = 0., sf3 = 0.;
-    double m4 = 0., m5 = 1., m6 = 0., m7 = 0., m8 = 0., m9 = 1.;
+    T sf2 = T(0.), sf3 = T(0.);
+    T m4 = T(0.), m5 = T(1.), m6 = T(0.), m7 = T(0.), m8 = T(0.), m9 = T(1.);
     if (q1 > tolisec) {
-      const double yq = 1.0 / q1;
-      const double vitu = div_rn(q2, q1, yq), vitv = div_rn(q3, q1, yq);
-      double normvit = sqrt(vitu * vitu + vitv * vitv);
-      if (normvit < tol) normvit = tol;
-      const double p13 = 1.0 / cbrt_halley(q1);    /* q1**(-1/3) */
+      const T yq = 1.0 / q1;
+      const T vitu = div_rn(q2, q1, yq), vitv = div_rn(q3, q1, yq);
+      T normvit = sqrt(vitu * vitu + vitv * vitv);
+      if (normvit < tol) normvit = T(tol);
+      const T p13 = 1.0 / cbrt_halley(q1);    /* q1**(-1/3) */
       sf2 = -(gp * manning * manning * vitu * normvit * area * p13);
       sf3 = -(gp * manning * manning * vitv * normvit * area * p13);
       if (normvit > tol) {
-        const double p43 = div_rn(p13, q1, yq);     /* q1**(-4/3) */
+        const T p43 = div_rn(p13, q1, yq);     /* q1**(-4/3) */
         if (M.fricimplic == 1) {
-          const double yn = 1.0 / normvit;
-          const double dtgn2h = dt / 2.0 * gp * manning * manning * p43;
-          const double af21 = -(7.0 / 3.0 * dtgn2h * vitu * normvit);
-          const double af22 = 1.0 + div_rn(dtgn2h * (2 * (vitu * vitu) + vitv * vitv), normvit, yn);
-          const double af23 = div_rn(dtgn2h * vitu * vitv, normvit, yn);
-          const double af31 = -(7.0 / 3.0 * dtgn2h * vitv * normvit);
-          const double af32 = af23;
-          const double af33 = 1.0 + div_rn(dtgn2h * (vitu * vitu + 2 * (vitv * vitv)), normvit, yn);
-          const double detaf = af22 * af33 - af23 * af32;
-          const double yd = 1.0 / detaf;
+          const T yn = 1.0 / normvit;
+          const T dtgn2h = dt / 2.0 * gp * manning * manning * p43;
+          const T af21 = -(7.0 / 3.0 * dtgn2h * vitu * normvit);
+          const T af22 = 1.0 + div_rn(dtgn2h * (2. * (vitu * vitu) + vitv * vitv), normvit, yn);
+          const T af23 = div_rn(dtgn2h * vitu * vitv, normvit, yn);
+          const T af31 = -(7.0 / 3.0 * dtgn2h * vitv * normvit);
+          const T af32 = af23;
+          const T af33 = 1.0 + div_rn(dtgn2h * (vitu * vitu + 2. * (vitv * vitv)), normvit, yn);
+          const T detaf = af22 * af33 - af23 * af32;
+          const T yd = 1.0 / detaf;
           m4 = div_rn(-(af21 * af33 - af23 * af31), detaf, yd);
           m5 = div_rn(af33, detaf, yd);
           m6 = div_rn(-af23, detaf, yd);
@@ -608,16 +685,16 @@ CF_HD CF_INLINE double4 element_update(const MemberDev& M, const double4 U, cons
           m8 = div_rn(-af32, detaf, yd);
           m9 = div_rn(af22, detaf, yd);
         } else if (M.fricimplic == 2) {
-          const double beta = -(dt * gp * manning * manning * normvit * p43);
-          const double detaf = (1 - beta) * (1 - beta);
-          m5 = (1 - beta) / detaf;
-          m9 = (1 - beta) / detaf;
+          const T beta = -(dt * gp * manning * manning * normvit * p43);
+          const T detaf = (1. - beta) * (1. - beta);
+          m5 = (1. - beta) / detaf;
+          m9 = (1. - beta) / detaf;
         }
       }
     }
-    const double ri1 = div_rn(0. + 0. - rc1, area, st.w);
-    const double ri2 = div_rn(sb2 + sf2 - rc2, area, st.w);
-    const double ri3 = div_rn(sb3 + sf3 - rc3, area, st.w);
+    const T ri1 = div_rn(0. + 0. - rc1, area, yarea);
+    const T ri2 = div_rn(sb2 + sf2 - rc2, area, yarea);
+    const T ri3 = div_rn(sb3 + sf3 - rc3, area, yarea);
     if (M.fricimplic == 1 || M.fricimplic == 2) {
       r1 = 1. * ri1 + 0. * ri2 + 0. * ri3;
       r2 = m4 * ri1 + m5 * ri2 + m6 * ri3;
@@ -628,17 +705,33 @@ CF_HD CF_INLINE double4 element_update(const MemberDev& M, const double4 U, cons
       r3 = ri3;
     }
   } else {
-    r1 = div_rn(0. - rc1, area, st.w);
-    r2 = div_rn(sb2 - rc2, area, st.w);
-    r3 = div_rn(sb3 - rc3, area, st.w);
+    r1 = div_rn(0. - rc1, area, yarea);
+    r2 = div_rn(sb2 - rc2, area, yarea);
+    r3 = div_rn(sb3 - rc3, area, yarea);
   }
-  double h = q1 + dt * r1, hu = q2 + dt * r2, hv = q3 + dt * r3;
-  nonfinite = !(finite_bits(h) && finite_bits(hu) && finite_bits(hv));
+  h = q1 + dt * r1;
+  hu = q2 + dt * r2;
+  hv = q3 + dt * r3;
+  nonfinite = !(finite_bits(val(h)) && finite_bits(val(hu)) && finite_bits(val(hv)));
   if (h <= tolisec) {
-    h = 0.;
-    hu = 0.;
-    hv = 0.;
+    h = T(0.);
+    hu = T(0.);
+    hv = T(0.);
   }
+}
+
+/* The element kernel's body: st = {area, manning n, cfl*L_cfl, 1/area}.  Returns the new
+ * state; sets *nonfinite when it is not finite. */
+CF_HD CF_INLINE double4 element_update(const MemberDev& M, const double4 U, const double4 st, const Slot& s0,
+                                       const Slot& s1, const Slot& s2, double dt, bool& nonfinite) {
+  /* fixed-order sums over the three edges (flux_riemann.cuf:411-426, source_terms.cuf:54-100) */
+  const double rc1 = s0.f1 + s1.f1 + s2.f1;
+  const double rc2 = s0.f2 + s1.f2 + s2.f2;
+  const double rc3 = s0.f3 + s1.f3 + s2.f3;
+  const double sb2 = s0.bx + s1.bx + s2.bx;
+  const double sb3 = s0.by + s1.by + s2.by;
+  double h, hu, hv;
+  element_core(M, st.x, st.w, st.y, U.x, U.y, U.z, rc1, rc2, rc3, sb2, sb3, dt, h, hu, hv, nonfinite);
   return make_double4(h, hu, hv, U.w);
 }
 

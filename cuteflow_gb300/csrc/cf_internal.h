@@ -152,6 +152,39 @@ int launch_scatter_state(const double* hu3, const int32_t* perm_new2old, const d
 int launch_gather_state(const double4* U, const int32_t* iperm_old2new, double* hu3, int32_t n,
                         stream_t s);
 
+/* ---- discrete adjoint (cf_adjoint.cu) ------------------------------------------------- */
+
+/* One reverse step n: s holds the step's buffers with s.Uin = U^n (s.slots is overwritten). */
+struct AdjArgs {
+  StepArgs s;
+  const double* dt_hist;   /* dt of every step (frozen) */
+  const double* t_hist;    /* start time of every step */
+  int32_t n;
+  const double4* lam_in;   /* lambda^{n+1} = dJ/dU^{n+1} (x, y, z used) */
+  double4* lam_out;        /* lambda^n */
+  Slot* cadj;              /* per element: adjoint of its flux sums (f1..f3) and bed sums (bx, by) */
+  double4* eadj;           /* per edge side: contribution to the side's element */
+  double4* uadj;           /* per edge, 4: contributions to the upwind elements (second order) */
+  const int32_t* uoff;     /* per element: its entries in uidx (second order; NULL otherwise) */
+  const int32_t* uidx;
+  const int32_t* goff;     /* per element: its gauges in gidx */
+  const int32_t* gidx;
+  const double* gw;        /* objective weights of the gauge elevations after step n, or NULL */
+  double* gman;            /* dJ/dn, accumulated */
+};
+
+/* edge and element stages of step n with the recorded dt / time (flag: element stage too,
+ * non-finite results OR-ed into *flag; NULL: edge stage only) */
+int launch_replay_step(const StepArgs& a, const double* dt_hist, const double* t_hist, int n, uint32_t* flag,
+                       stream_t s);
+/* gauge elevations of Unew into eta row n; with S, also dt / t of parity p into the histories */
+int launch_record(const double4* Unew, const MemberState* S, int p, int n, double* dt_hist, double* t_hist,
+                  const int32_t* gcell, int G, double* eta, stream_t s);
+int launch_adjoint_step(const AdjArgs& A, stream_t s);
+int launch_add_gauges(double4* lam, const int32_t* goff, const int32_t* gidx, const double* gw, int32_t n, stream_t s);
+int launch_gather_scalar(const double* x, const int32_t* iperm, double* out, int32_t n, stream_t s);
+int launch_set_manning(double4* cstat, const int32_t* perm, const double* nref, int32_t n, stream_t s);
+
 /* ---- context helpers for the static-scratch entry point (cf_api.cpp) ---------------- */
 
 int ctx_set_device(cf_ctx* c);                                /* the context's device current */

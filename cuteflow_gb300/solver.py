@@ -74,6 +74,19 @@ def load(build_if_missing: bool = True):
     L.cf_member_get_state.argtypes = [vp, C.c_int32, dp]
     L.cf_member_get_info.argtypes = [vp, C.c_int32, C.POINTER(_abi.CfStepInfo)]
     L.cf_member_get_mesh_tables.argtypes = [vp, C.c_int32, ip, dp, dp, dp]
+    vpp = C.POINTER(vp)
+    L.cf_set_manning.argtypes = [vp, vp]
+    L.cf_adjoint_create.argtypes = [vp, C.c_int32, C.c_int32, ip, C.c_int32, vpp]
+    L.cf_adjoint_destroy.argtypes = [vp]
+    L.cf_adjoint_destroy.restype = None
+    L.cf_adjoint_forward.argtypes = [vp, C.c_int32, vp, vp]
+    L.cf_adjoint_backward.argtypes = [vp, vp, vp, vp, vp]
+    L.cf_adjoint_get_dt.argtypes = [vp, vp, vp]
+    L.cf_adjoint_set_dt.argtypes = [vp, vp, vp]
+    L.cf_adjoint_sizes.argtypes = [vp, ip, ip, ip, C.POINTER(C.c_int64)]
+    for name in ("cf_set_manning", "cf_adjoint_create", "cf_adjoint_forward", "cf_adjoint_backward",
+                 "cf_adjoint_get_dt", "cf_adjoint_set_dt", "cf_adjoint_sizes"):
+        getattr(L, name).restype = C.c_int
     for name in ("cf_create_batch", "cf_get_members", "cf_member_set_state", "cf_member_set_initial_condition",
                  "cf_member_get_state", "cf_member_get_info", "cf_member_get_mesh_tables"):
         getattr(L, name).restype = C.c_int
@@ -159,6 +172,16 @@ class Solver:
     def set_state_device(self, ptr: int, t0: float = 0.0):
         """Set the state from a device pointer of 3*nelt doubles (reference order)."""
         self._check(self._L.cf_set_state_device(self._ctx, C.c_void_p(ptr), float(t0)))
+
+    def set_manning(self, n):
+        """Per-element Manning n [nelt] (reference order): a numpy array, or an int device
+        address of nelt doubles."""
+        if isinstance(n, int):
+            self._check(self._L.cf_set_manning(self._ctx, C.c_void_p(n)))
+        else:
+            n = np.ascontiguousarray(n, dtype=np.float64)
+            assert n.shape == (self.nelt,)
+            self._check(self._L.cf_set_manning(self._ctx, n.ctypes.data_as(C.c_void_p)))
 
     def set_initial_condition(self, ic: dict, t0: float = 0.0):
         c = _abi.CfIc()

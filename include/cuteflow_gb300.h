@@ -200,6 +200,46 @@ const char* cf_last_error(const cf_ctx* ctx);
 int cf_set_timing(cf_ctx* ctx, int32_t enable);
 int cf_get_timing(cf_ctx* ctx, double* flux_ms, double* update_ms, int64_t* launches);
 
+/* ---- discrete adjoint (new: the reference has no gradients) ----------------------------
+ *
+ * For Manning calibration: gradients of an objective on gauge elevations and on the final
+ * state with respect to the per-element Manning n and the initial state, by the discrete
+ * adjoint of the step (the dt of every step held at its recorded value).  Contexts with one
+ * member.
+ *
+ *   J = sum_{k=1..N} sum_g w_eta[(k-1)*G + g] * eta^k_g  +  sum_e w_state[3e..3e+2] . U^N_e
+ *
+ * eta^k_g = h + z of gauge element g (0-based, reference order) after step k of a run of N
+ * steps from the context's current state.  Pointers of the run functions may be host or
+ * device memory. */
+typedef struct cf_adjoint cf_adjoint;
+
+/* Per-element Manning n [nelt], reference order (replaces the mesh's values and the override). */
+int cf_set_manning(cf_ctx* ctx, const double* n_elt);
+
+/* An adjoint of N steps with G gauges; checkpoint_interval K (0: ceil(sqrt(N))): the state is
+ * kept every K steps, ceil(N/K) + max(K, 2) states of device memory. */
+int cf_adjoint_create(cf_ctx* ctx, int32_t nsteps, int32_t checkpoint_interval, const int32_t* gauges,
+                      int32_t ngauges, cf_adjoint** out);
+void cf_adjoint_destroy(cf_adjoint* adj);
+
+/* N steps from the context's current state (which is left unchanged).  replay 0: the dt of
+ * every step comes from the CFL condition, as in cf_step (bit-identical results), and is
+ * recorded; replay 1: the recorded dt and times are used (for finite differences at frozen
+ * dt).  eta [N*G] and state [nelt*3] (the state after step N) may be NULL. */
+int cf_adjoint_forward(cf_adjoint* adj, int32_t replay, double* eta, double* state);
+
+/* dJ/dU^0 [nelt*3] and dJ/dn [nelt] of the last forward run; w_eta [N*G] and w_state
+ * [nelt*3] may be NULL (zero), g_state0 and g_manning may be NULL (not returned). */
+int cf_adjoint_backward(cf_adjoint* adj, const double* w_eta, const double* w_state, double* g_state0,
+                        double* g_manning);
+
+/* The recorded dt and start time of every step [N]; set_dt installs a sequence to replay. */
+int cf_adjoint_get_dt(cf_adjoint* adj, double* dt, double* t);
+int cf_adjoint_set_dt(cf_adjoint* adj, const double* dt, const double* t);
+int cf_adjoint_sizes(cf_adjoint* adj, int32_t* nsteps, int32_t* checkpoint_interval, int32_t* ngauges,
+                     int64_t* device_bytes);
+
 /* ---- stepping without allocation (no counterpart in the reference) --------------------
  *
  * For callers that may not allocate device memory once their time loop runs: a coupled host

@@ -162,3 +162,113 @@ extern "C" long long harness_div_check(long long n, unsigned long long seed) {
   }
   return bad;
 }
+
+/* ---- tangent-linear run: the discrete step differentiated in forward mode -------------------- */
+
+#include "../cuteflow_gb300/csrc/cf_dual.h"
+
+typedef Dual<1> D1;
+
+/* nsteps steps from U0 with Manning n, replaying the dt / start-time sequence, carrying the
+ * tangent of the direction (dU0, dn) along (every branch is the one the values take: the same
+ * templated arithmetic as the GPU step).  Outputs (reference order): the gauge elevations
+ * eta [nsteps][G] and their tangents, the final state and its tangent. */
+extern "C" int harness_tangent(const cf_mesh* m, const cf_params* p, const double* U0, const double* dU0,
+                               const double* nman, const double* dn, int nsteps, const double* dt_seq,
+                               const double* t_seq, const int32_t* gauges, int G, double* eta, double* deta,
+                               double* U_out, double* dU_out) {
+  Prep P;
+  std::string err;
+  int rc = prepare_mesh(m, p, P, err);
+  if (rc != CF_OK) return rc;
+  const int n = P.nelt;
+  MemberDev M;
+  std::memset(&M, 0, sizeof(M));
+  M.gp = p->gp; M.tolisec = p->tolisec; M.tol = p->tol; M.constant_dt = p->constant_dt;
+  M.ramp_time = p->ramp_time;
+  for (int i = 0; i < CF_MAX_IO; ++i) {
+    M.debit_end[i] = p->debitglob[i]; M.debit_start[i] = p->debitglob_start[i];
+    M.long_entree[i] = P.long_entree[i]; M.h_sortie[i] = p->h_sortie[i];
+  }
+  M.inlet = p->inlet; M.outlet = p->outlet; M.friction = p->friction; M.fricimplic = p->fricimplic;
+  std::vector<D1> h(n), hu(n), hv(n), nm(n), nh(n), nhu(n), nhv(n);
+  std::vector<double> z(n);
+  for (int c = 0; c < n; ++c) {
+    const int o = P.perm[c];
+    h[c] = D1(U0[3 * o]); h[c].d[0] = dU0[3 * o];
+    hu[c] = D1(U0[3 * o + 1]); hu[c].d[0] = dU0[3 * o + 1];
+    hv[c] = D1(U0[3 * o + 2]); hv[c].d[0] = dU0[3 * o + 2];
+    nm[c] = D1(nman[o]); nm[c].d[0] = dn[o];
+    z[c] = P.zcell[c];
+  }
+  const int ne = (int)P.edges.size();
+  std::vector<D1> slot(10 * (size_t)ne);   /* per slot s: 5 values at 5 s */
+  const bool second = p->iflux >= 3;
+  for (int s = 0; s < nsteps; ++s) {
+    const double dt = dt_seq[s], t = t_seq[s];
+    for (int e = 0; e < ne; ++e) {
+      const int2 ab = P.ecell[e];
+      const double4 geo = P.egeo[e];
+      D1* sa = &slot[10 * (size_t)e];
+      if (ab.y < 0) {
+        D1 f1, f2, f3, q;
+        boundary_flux(p->iflux, M, ab.y, P.ebid[e], t, geo.x, geo.y, h[ab.x], hu[ab.x], hv[ab.x], z[ab.x], f1, f2, f3,
+                      q);
+        sa[0] = f1 * geo.z; sa[1] = f2 * geo.z; sa[2] = f3 * geo.z; sa[3] = D1(0.0); sa[4] = D1(0.0);
+        continue;
+      }
+      EdgeGeo Gm;
+      Gm.nx = geo.x; Gm.ny = geo.y; Gm.len = geo.z; Gm.d_mrl = geo.w;
+      Gm.y_mrl = Gm.d_mkvol = Gm.y_mkvol = Gm.d_mkvoisin = Gm.y_mkvoisin = Gm.ysum_a = Gm.ysum_b = 0.0;
+      D1 hlu(0.0), vlu(0.0), hru(0.0), vru(0.0);
+      double zlu = 0.0, zru = 0.0;
+      if (second) {
+        const double4 dk = P.edk[e], yi = P.einv[e], dw = P.ewts[e];
+        const int4 up = P.eupw[e];
+        Gm.y_mrl = yi.x; Gm.d_mkvol = dk.x; Gm.y_mkvol = dk.z; Gm.d_mkvoisin = dk.y; Gm.y_mkvoisin = dk.w;
+        Gm.ysum_a = yi.y; Gm.ysum_b = yi.z;
+        const int a2 = dw.x < 0.0 ? up.x : up.y, b2 = dw.z < 0.0 ? up.z : up.w;
+        upwind_mix(h[up.x], hu[up.x], hv[up.x], h[a2], hu[a2], hv[a2], dw.x, dw.y, yi.y, geo.x, geo.y, M.tolisec, hlu,
+                   vlu);
+        upwind_mix(h[up.z], hu[up.z], hv[up.z], h[b2], hu[b2], hv[b2], dw.z, dw.w, yi.z, geo.x, geo.y, M.tolisec, hru,
+                   vru);
+        zlu = dw.x < 0.0 ? z[up.x] : div_rn(dw.x * z[up.x] + dw.y * z[up.y], dw.x + dw.y, yi.y);
+        zru = dw.z < 0.0 ? z[up.z] : div_rn(dw.z * z[up.z] + dw.w * z[up.w], dw.z + dw.w, yi.z);
+      }
+      if (p->iflux == 1)
+        interior_edge<1>(M, p->ilimiteur, p->flux_mode, Gm, dt, h[ab.x], hu[ab.x], hv[ab.x], z[ab.x], h[ab.y],
+                         hu[ab.y], hv[ab.y], z[ab.y], hlu, vlu, zlu, hru, vru, zru, sa);
+      else if (p->iflux == 2)
+        interior_edge<2>(M, p->ilimiteur, p->flux_mode, Gm, dt, h[ab.x], hu[ab.x], hv[ab.x], z[ab.x], h[ab.y],
+                         hu[ab.y], hv[ab.y], z[ab.y], hlu, vlu, zlu, hru, vru, zru, sa);
+      else
+        interior_edge<3>(M, p->ilimiteur, p->flux_mode, Gm, dt, h[ab.x], hu[ab.x], hv[ab.x], z[ab.x], h[ab.y],
+                         hu[ab.y], hv[ab.y], z[ab.y], hlu, vlu, zlu, hru, vru, zru, sa);
+    }
+    for (int c = 0; c < n; ++c) {
+      const int* sl = &P.cslot[c].x;
+      const D1* s0 = &slot[5 * (size_t)sl[0]];
+      const D1* s1 = &slot[5 * (size_t)sl[1]];
+      const D1* s2 = &slot[5 * (size_t)sl[2]];
+      const D1 rc1 = s0[0] + s1[0] + s2[0], rc2 = s0[1] + s1[1] + s2[1], rc3 = s0[2] + s1[2] + s2[2];
+      const D1 sb2 = s0[3] + s1[3] + s2[3], sb3 = s0[4] + s1[4] + s2[4];
+      bool nf = false;
+      element_core(M, P.cstat[c].x, P.cstat[c].w, nm[c], h[c], hu[c], hv[c], rc1, rc2, rc3, sb2, sb3, dt, nh[c],
+                   nhu[c], nhv[c], nf);
+    }
+    h.swap(nh);
+    hu.swap(nhu);
+    hv.swap(nhv);
+    for (int g = 0; g < G; ++g) {
+      const int c = P.iperm[gauges[g]];
+      eta[(size_t)s * G + g] = h[c].v + z[c];
+      deta[(size_t)s * G + g] = h[c].d[0];
+    }
+  }
+  for (int c = 0; c < n; ++c) {
+    const int o = P.perm[c];
+    U_out[3 * o] = h[c].v; U_out[3 * o + 1] = hu[c].v; U_out[3 * o + 2] = hv[c].v;
+    dU_out[3 * o] = h[c].d[0]; dU_out[3 * o + 1] = hu[c].d[0]; dU_out[3 * o + 2] = hv[c].d[0];
+  }
+  return 0;
+}

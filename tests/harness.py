@@ -17,7 +17,7 @@ def lib():
     if _lib is not None:
         return _lib
     srcs = [os.path.join(HERE, "flux_harness.cpp"), os.path.join(ROOT, "cuteflow_gb300", "csrc", "cf_mesh.cpp")]
-    deps = srcs + [os.path.join(ROOT, "cuteflow_gb300", "csrc", f) for f in ("cf_flux.h", "cf_internal.h")]
+    deps = srcs + [os.path.join(ROOT, "cuteflow_gb300", "csrc", f) for f in ("cf_flux.h", "cf_internal.h", "cf_dual.h")]
     if not os.path.exists(LIB) or any(os.path.getmtime(d) > os.path.getmtime(LIB) for d in deps):
         os.makedirs(os.path.dirname(LIB), exist_ok=True)
         cuda_inc = os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "include")
@@ -73,3 +73,30 @@ def div_check(n, seed=12345):
     L.harness_div_check.argtypes = [C.c_longlong, C.c_ulonglong]
     L.harness_div_check.restype = C.c_longlong
     return int(L.harness_div_check(int(n), int(seed)))
+
+
+def tangent(case, params, U0, dU0, manning, dn, dt, t, gauges):
+    """Tangent-linear run (forward mode along (dU0, dn)) replaying dt / t: returns
+    (eta, deta, U_N, dU_N)."""
+    from cuteflow_gb300 import _abi
+    L = lib()
+    if not hasattr(L, "_tan_typed"):
+        dp = C.POINTER(C.c_double)
+        ip = C.POINTER(C.c_int32)
+        L.harness_tangent.argtypes = [C.POINTER(_abi.CfMesh), C.POINTER(_abi.CfParams), dp, dp, dp, dp, C.c_int, dp,
+                                      dp, ip, C.c_int, dp, dp, dp, dp]
+        L.harness_tangent.restype = C.c_int
+        L._tan_typed = True
+    ma = _abi.MeshArrays(case)
+    p = _abi.make_params({**case.params, **(params or {})})
+    f = lambda a: np.ascontiguousarray(a, dtype=np.float64)
+    U0, dU0, manning, dn, dt, t = f(U0), f(dU0), f(manning), f(dn), f(dt), f(t)
+    g = np.ascontiguousarray(gauges, dtype=np.int32)
+    N, G = len(dt), len(g)
+    eta, deta = np.zeros((N, G)), np.zeros((N, G))
+    U, dU = np.zeros_like(U0), np.zeros_like(U0)
+    rc = L.harness_tangent(C.byref(ma.mesh), C.byref(p), _abi.dptr(U0), _abi.dptr(dU0), _abi.dptr(manning),
+                           _abi.dptr(dn), N, _abi.dptr(dt), _abi.dptr(t), g.ctypes.data_as(C.POINTER(C.c_int32)), G,
+                           _abi.dptr(eta), _abi.dptr(deta), _abi.dptr(U), _abi.dptr(dU))
+    assert rc == 0
+    return eta, deta, U, dU

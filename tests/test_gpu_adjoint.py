@@ -1,0 +1,177 @@
+"""Discrete adjoint (dt frozen) against central finite differences of the GPU forward and of
+the CPU oracle forward, both replaying the recorded dt sequence.
+
+Objective: J = <w_eta, eta> + <w_state, U^N> with seeded weights; eta = h + z of the gauge
+elements after every step.  Checks: the recording forward is the plain step bit for bit; the
+replayed forward repeats it; the gradient does not depend on the checkpoint interval; the
+directional derivative along seeded Manning and initial-state directions and single-element
+Manning derivatives agree with central differences to 1e-5 relative.
+"""
+import numpy as np
+import pytest
+
+import adjoint_cases as AC
+
+pytestmark = pytest.mark.gpu
+
+RTOL = 1e-5
+
+
+def _setup(kind, nsteps=30, ngauges=7, interval=0):
+    from cuteflow_gb300 import Solver
+    from cuteflow_gb300.adjoint import Adjoint
+    c, extra = AC.make(kind)
+    s = Solver(c, extra)
+    rng = np.random.default_rng(7)
+    wet = np.flatnonzero(c.U0[:, 0] > 0.05)
+    gauges = rng.choice(wet, ngauges, replace=False)
+    adj = Adjoint(s, nsteps, gauges, interval)
+    w_eta = rng.standard_normal((nsteps, ngauges))
+    w_state = 0.01 * rng.standard_normal((c.nelt, 3))
+    return c, extra, s, adj, w_eta, w_state
+
+
+_J = AC.objective
+KINDS = AC.KINDS
+
+
+@pytest.mark.parametrize("kind", AC.ALL_KINDS)
+def test_record_forward_is_the_step(gpu_lib, kind):
+    c, extra, s, adj, w_eta, w_state = _setup(kind)
+    with s, adj:
+        s.set_state(c.U0)
+        eta, UN = adj.forward()
+        eta2, UN2 = adj.forward(replay=True)
+        s.step(adj.nsteps)
+        ref = s.get_state()
+        zm = s.mesh_tables()[2]
+    assert np.array_equal(UN, ref)
+    assert np.array_equal(UN2, UN) and np.array_equal(eta2, eta)
+    assert np.array_equal(eta[-1], ref[adj.gauges, 0] + zm[adj.gauges])
+
+
+@pytest.mark.parametrize("kind", AC.FD_KINDS)
+def test_gradient_matches_central_differences_gpu(gpu_lib, kind):
+    c, extra, s, adj, w_eta, w_state = _setup(kind)
+    rng = np.random.default_rng(11)
+    n0 = c.manning.copy()
+    with s, adj:
+        s.set_manning(n0)
+        s.set_state(c.U0)
+        adj.forward()
+        gU, gn = adj.backward(w_eta, w_state)
+
+        def J(n, U0):
+            s.set_manning(n)
+            s.set_state(U0)
+            return _J(*adj.forward(replay=True), w_eta, w_state)
+
+        # Manning direction
+        vn = n0 * rng.uniform(-1.0, 1.0, c.nelt)
+        eps = 1e-6
+        fd = (J(n0 + eps * vn, c.U0) - J(n0 - eps * vn, c.U0)) / (2 * eps)
+        ad = float(np.dot(gn, vn))
+        assert abs(fd - ad) <= RTOL * abs(ad), (fd, ad)
+        # initial-state direction: depth and discharges of the clearly wet elements
+        wet = c.U0[:, 0] > 0.05
+        vU = np.zeros_like(c.U0)
+        vU[wet, 0] = 0.01 * rng.uniform(-1.0, 1.0, wet.sum())
+        vU[wet, 1:] = 0.01 * rng.uniform(-1.0, 1.0, (wet.sum(), 2))
+        fd = (J(n0, c.U0 + eps * vU) - J(n0, c.U0 - eps * vU)) / (2 * eps)
+        ad = float(np.sum(gU * vU))
+        assert abs(fd - ad) <= RTOL * abs(ad), (fd, ad)
+        # single elements: the largest Manning sensitivities
+        for e in np.argsort(-np.abs(gn))[:4]:
+            d = np.zeros(c.nelt)
+            d[e] = n0[e]
+            fd = (J(n0 + eps * d, c.U0) - J(n0 - eps * d, c.U0)) / (2 * eps)
+            assert abs(fd - gn[e] * n0[e]) <= RTOL * abs(gn[e] * n0[e]), (e, fd, gn[e] * n0[e])
+
+
+@pytest.mark.parametrize("kind", ["hllc_dam", "waf_flood"])
+def test_gradient_matches_central_differences_oracle(gpu_lib, oracle, kind):
+    c, extra, s, adj, w_eta, w_state = _setup(kind, nsteps=20)
+    rng = np.random.default_rng(5)
+    n0 = c.manning.copy()
+    with s, adj:
+        s.set_manning(n0)
+        s.set_state(c.U0)
+        eta_g, UN_g = adj.forward()
+        _, gn = adj.backward(w_eta, w_state)
+        dt, t = adj.dt_history()
+        zm = s.mesh_tables()[2]
+    eta_o, UN_o = AC.oracle_run(oracle, c, extra, c.U0, n0, dt, t, adj.gauges, zm)
+    assert np.array_equal(eta_o, eta_g) and np.array_equal(UN_o, UN_g)
+    vn = n0 * rng.uniform(-1.0, 1.0, c.nelt)
+    eps = 1e-6
+    Jp = _J(*AC.oracle_run(oracle, c, extra, c.U0, n0 + eps * vn, dt, t, adj.gauges, zm), w_eta, w_state)
+    Jm = _J(*AC.oracle_run(oracle, c, extra, c.U0, n0 - eps * vn, dt, t, adj.gauges, zm), w_eta, w_state)
+    fd = (Jp - Jm) / (2 * eps)
+    ad = float(np.dot(gn, vn))
+    assert abs(fd - ad) <= RTOL * abs(ad), (fd, ad)
+
+
+@pytest.mark.parametrize("kind", AC.ALL_KINDS)
+def test_adjoint_is_the_transpose_of_the_tangent(gpu_lib, kind):
+    """<dJ/dU0, dU0> + <dJ/dn, dn> from the adjoint equals the tangent-linear derivative of J
+    along (dU0, dn) (CPU, same branches): exact up to summation order, on every case,
+    including those whose WAF limiter or wet/dry switches make central differences
+    unreliable."""
+    import harness as H
+    c, extra, s, adj, w_eta, w_state = _setup(kind)
+    rng = np.random.default_rng(21)
+    wet = c.U0[:, 0] > 0.05
+    dU = np.zeros_like(c.U0)
+    dU[wet] = 0.01 * rng.uniform(-1.0, 1.0, (wet.sum(), 3))
+    dn = c.manning * rng.uniform(-1.0, 1.0, c.nelt)
+    with s, adj:
+        s.set_manning(c.manning)
+        s.set_state(c.U0)
+        eta, UN = adj.forward()
+        gU, gn = adj.backward(w_eta, w_state)
+        dt, t = adj.dt_history()
+    eta_t, deta, UN_t, dUN = H.tangent(c, extra, c.U0, dU, c.manning, dn, dt, t, adj.gauges)
+    assert np.array_equal(eta_t, eta) and np.array_equal(UN_t, UN)
+    terms = np.concatenate([(w_eta * deta).ravel(), (w_state * dUN).ravel()])
+    tl = float(terms.sum())
+    ad = float(np.sum(gU * dU) + np.sum(gn * dn))
+    assert abs(ad - tl) <= 1e-9 * np.abs(terms).sum(), (ad, tl)
+
+
+def test_gradient_independent_of_checkpoint_interval(gpu_lib):
+    from cuteflow_gb300.adjoint import Adjoint
+    c, extra, s, adj, w_eta, w_state = _setup("waf_flood", nsteps=23)
+    out = []
+    with s:
+        adj.close()
+        for k in (1, 4, 23, 0):
+            with Adjoint(s, 23, adj.gauges, k) as a:
+                s.set_state(c.U0)
+                a.forward()
+                out.append(a.backward(w_eta, w_state))
+    for gU, gn in out[1:]:
+        assert np.array_equal(gU, out[0][0]) and np.array_equal(gn, out[0][1])
+
+
+def test_torch_function(gpu_lib):
+    torch = pytest.importorskip("torch")
+    from cuteflow_gb300.adjoint import gauge_run
+    c, extra, s, adj, w_eta, w_state = _setup("waf_flood", nsteps=15)
+    dev = torch.device("cuda:0")
+    with s, adj:
+        n = torch.tensor(c.manning, dtype=torch.float64, device=dev, requires_grad=True)
+        U0 = torch.tensor(c.U0, dtype=torch.float64, device=dev, requires_grad=True)
+        obs = torch.tensor(w_eta, dtype=torch.float64, device=dev)
+        eta, UN = gauge_run(adj, n, U0)
+        loss = ((eta - obs) ** 2).sum() + (UN[:, 0] ** 2).sum()
+        loss.backward()
+        # the same through the numpy interface
+        s.set_manning(c.manning)
+        s.set_state(c.U0)
+        e2, U2 = adj.forward()
+        w_s = np.zeros_like(U2)
+        w_s[:, 0] = 2 * U2[:, 0]
+        gU, gn = adj.backward(2 * (e2 - w_eta), w_s)
+    assert np.array_equal(eta.detach().cpu().numpy(), e2)
+    assert np.array_equal(n.grad.cpu().numpy(), gn)
+    assert np.array_equal(U0.grad.cpu().numpy(), gU)
