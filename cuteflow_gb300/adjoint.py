@@ -53,6 +53,12 @@ class Adjoint:
         self.device_bytes = int(b.value)
         self.generation = 0
 
+    def set_linearization(self, freeze_limiter_ratios: bool):
+        """WAF only: hold the limiter ratios constant in the linearization, an approximate
+        gradient for long runs over which the WAF objective is not differentiable (bounded with
+        the van Albada limiter; the superbee linearization still grows)."""
+        self.solver._check(self._L.cf_adjoint_set_linearization(self._h, 1 if freeze_limiter_ratios else 0))
+
     @property
     def ngauges(self) -> int:
         return int(self.gauges.size)

@@ -6,23 +6,24 @@
  * their upwind elements); every element then combines its state, the sums of its three slots
  * and its Manning n.  The adjoint runs the stages backwards:
  *
- *   k_rep_edges  : the edge stage at U^n (the slot values the element stage needs),
- *   k_adj_cells  : per element, the transposed local Jacobian of the element stage applied to
- *                  lambda^{n+1}: the element's own part of lambda^n, the adjoint of its slot
- *                  sums (mu for the fluxes, nu for the bed source) and dJ/dn += .. ,
- *   k_adj_edges  : per edge, the transposed Jacobian of the edge stage applied to the mu, nu
- *                  of its two elements: one contribution per side (and per upwind element),
- *   k_adj_gather : per element, lambda^n = own part + the contributions of its three slots
- *                  + those of the edges it is an upwind element of + the objective's weight
- *                  on the gauges it carries, in a fixed order (deterministic, no atomics).
+ *   k_adj_cells  : per element, lambda^{n+1} gathered (its own part of the previous reverse
+ *                  step, the contributions of its three edge slots and of the edges it is
+ *                  an upwind element of, the objective's weights on its gauges; fixed order,
+ *                  no atomics), then the transposed local Jacobian of the element stage
+ *                  applied to it: its own part of lambda^n, the adjoint of its flux and bed
+ *                  sums (cadj) and dJ/dn += .. ,
+ *   k_adj_edges  : per edge, the transposed Jacobian of the edge stage applied to the cadj of
+ *                  its two elements: one contribution per side (and per upwind element).
+ * The flux and bed sums at U^n come from the replay of the checkpoint segment (k_rep_cells
+ * stores them), so a reverse step recomputes no edge fluxes.
  *
  * The local Jacobians come from the step's own arithmetic (cf_flux.h) instantiated on
  * Dual<D> numbers, whose value lane repeats the forward's IEEE operations, so every branch
  * (wet/dry masks, hydrostatic reconstruction, wave regions, limiter cases, friction
- * floors, the wet/dry clamp of the update) is the one the forward took.  The D derivative
- * lanes are run in chunks over the 6 (first order) or 10 (WAF: + the upwind reconstructions)
- * inputs of an edge and the 9 inputs of an element; D is a compile-time choice that trades
- * registers for repeated value lanes.
+ * floors, the wet/dry clamp of the update) is the one the forward took.  For an edge the D
+ * derivative lanes run in chunks over its 6 (first order) or 10 (WAF: + the upwind
+ * reconstructions) inputs; D trades registers for repeated value lanes.  The element stage
+ * is linear in the sums and is transposed by hand around a Dual<4> friction block.
  *
  * Replay kernels (k_rep_edges, k_rep_cells) advance a state with a recorded dt / time
  * sequence; they run the step's own edge_body / element_update, so a replayed trajectory is
@@ -63,7 +64,8 @@ __global__ void __launch_bounds__(TILE_E) k_rep_edges(StepArgs a, const double* 
   edge_body<IFLUX>(a, M, e, __ldg(dt_hist + n), __ldg(t_hist + n));
 }
 
-__global__ void __launch_bounds__(TILE_C) k_rep_cells(StepArgs a, const double* dt_hist, int n, uint32_t* flag) {
+__global__ void __launch_bounds__(TILE_C) k_rep_cells(StepArgs a, const double* dt_hist, int n, uint32_t* flag,
+                                                      Slot* sums) {
   const int tile = blockIdx.x;
   const MemberDev& M = a.mdev[__ldg(a.ctile_mem + tile)];
   const int c = tile * TILE_C + threadIdx.x;
@@ -72,13 +74,22 @@ __global__ void __launch_bounds__(TILE_C) k_rep_cells(StepArgs a, const double* 
   const double4 U = ld4(a.Uin + c);
   const double4 st = ld4(a.cstat + c);
   const int4 sl = __ldg(a.cslot + c);
+  const Slot s0 = load_slot_adj(a.slots + sl.x), s1 = load_slot_adj(a.slots + sl.y), s2 = load_slot_adj(a.slots + sl.z);
   bool nonfinite = false;
-  const double4 V = element_update(M, U, st, load_slot_adj(a.slots + sl.x), load_slot_adj(a.slots + sl.y),
-                                   load_slot_adj(a.slots + sl.z), dt, nonfinite);
+  const double4 V = element_update(M, U, st, s0, s1, s2, dt, nonfinite);
   if (nonfinite) atomicOr(flag, CF_STATUS_NONFINITE);
-  double4* o = a.Uout + c;
-  reinterpret_cast<double2*>(o)[0] = make_double2(V.x, V.y);
-  reinterpret_cast<double2*>(o)[1] = make_double2(V.z, V.w);
+  if (a.Uout) {
+    double4* o = a.Uout + c;
+    reinterpret_cast<double2*>(o)[0] = make_double2(V.x, V.y);
+    reinterpret_cast<double2*>(o)[1] = make_double2(V.z, V.w);
+  }
+  if (sums) {
+    /* the sums element_update forms (same expressions, same values) */
+    double2* q = reinterpret_cast<double2*>(sums + c);
+    q[0] = make_double2(s0.f1 + s1.f1 + s2.f1, s0.f2 + s1.f2 + s2.f2);
+    q[1] = make_double2(s0.f3 + s1.f3 + s2.f3, s0.bx + s1.bx + s2.bx);
+    q[2] = make_double2(s0.by + s1.by + s2.by, 0.0);
+  }
 }
 
 /* After step n: the gauge elevations h + z of the new state and, when recording, the dt and
@@ -97,41 +108,106 @@ __global__ void k_record(const double4* Unew, const MemberState* S, int p, int n
 
 /* ---- adjoint of the element stage --------------------------------------------------------- */
 
-template <int D>
+/* lambda^{n+1} of element c: its own part plus the contributions the edge adjoint of step n+1
+ * left in its three slots and in the upwind entries it belongs to, plus the objective's
+ * weights of the gauges it carries; fixed order. */
+__device__ __forceinline__ double4 gather_lambda(const AdjArgs& A, int c, const double* gw) {
+  double4 L = ld4(A.lam_own + c);
+  const int4 sl = __ldg(A.s.cslot + c);
+  const double4 e0 = ld4(A.eadj + sl.x), e1 = ld4(A.eadj + sl.y), e2 = ld4(A.eadj + sl.z);
+  L.x = L.x + e0.x + e1.x + e2.x;
+  L.y = L.y + e0.y + e1.y + e2.y;
+  L.z = L.z + e0.z + e1.z + e2.z;
+  if (A.uoff) {
+    for (int j = __ldg(A.uoff + c), j1 = __ldg(A.uoff + c + 1); j < j1; ++j) {
+      const double4 u = ld4(A.uadj + __ldg(A.uidx + j));
+      L.x += u.x;
+      L.y += u.y;
+      L.z += u.z;
+    }
+  }
+  if (gw)
+    for (int j = __ldg(A.goff + c), j1 = __ldg(A.goff + c + 1); j < j1; ++j) L.x += __ldg(gw + __ldg(A.gidx + j));
+  return L;
+}
+
+/* The element update is linear in its flux and bed sums: U^{n+1} = q + dt R (S + sf(q, n) - rc)
+ * / area (R = I, or the semi-implicit matrix of rows (1, 0, 0), (m4, m5, m6), (m7, m8, m9)),
+ * then the wet/dry clamp.  Its transpose is applied by hand; only the friction block
+ * (q1, q2, q3, n) -> (sf2, sf3, m4..m9) is differentiated with Dual<4> numbers of the step's own
+ * friction_terms. */
 __global__ void __launch_bounds__(TILE_C) k_adj_cells(AdjArgs A) {
   const StepArgs& a = A.s;
   const int tile = blockIdx.x;
   const MemberDev& M = a.mdev[__ldg(a.ctile_mem + tile)];
   const int c = tile * TILE_C + threadIdx.x;
   if (c >= M.cell_end) return;
+  const double4 L = A.gather ? gather_lambda(A, c, A.gw) : ld4(A.lam_init + c);
   const double dt = __ldg(A.dt_hist + A.n);
   const double4 U = ld4(a.Uin + c);
   const double4 st = ld4(a.cstat + c);
-  const int4 sl = __ldg(a.cslot + c);
-  const Slot s0 = load_slot_adj(a.slots + sl.x), s1 = load_slot_adj(a.slots + sl.y), s2 = load_slot_adj(a.slots + sl.z);
-  const double rc1 = s0.f1 + s1.f1 + s2.f1;
-  const double rc2 = s0.f2 + s1.f2 + s2.f2;
-  const double rc3 = s0.f3 + s1.f3 + s2.f3;
-  const double sb2 = s0.bx + s1.bx + s2.bx;
-  const double sb3 = s0.by + s1.by + s2.by;
-  const double4 L = ld4(A.lam_in + c);
-  double g[9];
-#pragma unroll
-  for (int base = 0; base < 9; base += D) {
-    Dual<D> h, hu, hv;
-    bool nf;
-    element_core(M, st.x, st.w, seed<D>(st.y, 8, base), seed<D>(U.x, 0, base), seed<D>(U.y, 1, base),
-                 seed<D>(U.z, 2, base), seed<D>(rc1, 3, base), seed<D>(rc2, 4, base), seed<D>(rc3, 5, base),
-                 seed<D>(sb2, 6, base), seed<D>(sb3, 7, base), dt, h, hu, hv, nf);
-#pragma unroll
-    for (int i = 0; i < D; ++i)
-      if (base + i < 9) g[base + i] = L.x * h.d[i] + L.y * hu.d[i] + L.z * hv.d[i];
+  const double2* sp = reinterpret_cast<const double2*>(A.sums + c);
+  const double2 sa = __ldg(sp), sb = __ldg(sp + 1), sc = __ldg(sp + 2);
+  const double rc1 = sa.x, rc2 = sa.y, rc3 = sb.x, sb2 = sb.y, sb3 = sc.x;
+  const double area = st.x, y = st.w;
+  const bool fric = M.friction == 1;
+  const bool impl = fric && (M.fricimplic == 1 || M.fricimplic == 2);
+  Dual<4> sf2(0.0), sf3(0.0), m[6];
+  double r1, ri1, ri2, ri3;
+  if (fric) {
+    friction_terms(M, area, dt, Dual<4>::var(st.y, 3), Dual<4>::var(U.x, 0), Dual<4>::var(U.y, 1),
+                   Dual<4>::var(U.z, 2), sf2, sf3, m);
+    ri1 = div_rn(0. + 0. - rc1, area, y);
+    ri2 = div_rn(sb2 + sf2.v - rc2, area, y);
+    ri3 = div_rn(sb3 + sf3.v - rc3, area, y);
+    r1 = impl ? 1. * ri1 + 0. * ri2 + 0. * ri3 : ri1;
+  } else {
+    ri1 = div_rn(0. - rc1, area, y);
+    ri2 = div_rn(sb2 - rc2, area, y);
+    ri3 = div_rn(sb3 - rc3, area, y);
+    r1 = ri1;
   }
-  A.lam_out[c] = make_double4(g[0], g[1], g[2], 0.0);
+  const double h = U.x + dt * r1;
+  double4 own = make_double4(0.0, 0.0, 0.0, 0.0);
   Slot w;
-  w.f1 = g[3]; w.f2 = g[4]; w.f3 = g[5]; w.bx = g[6]; w.by = g[7]; w.q = 0.0;
+  w.f1 = w.f2 = w.f3 = w.bx = w.by = w.q = 0.0;
+  double nb = 0.0;
+  if (!(h <= M.tolisec)) {   /* a clamped element is a constant of its inputs */
+    own = make_double4(L.x, L.y, L.z, 0.0);
+    const double r1b = dt * L.x, r2b = dt * L.y, r3b = dt * L.z;
+    double ri1b = r1b, ri2b = r2b, ri3b = r3b;
+    if (impl) {
+      ri1b = r1b + r2b * m[0].v + r3b * m[3].v;
+      ri2b = r2b * m[1].v + r3b * m[4].v;
+      ri3b = r2b * m[2].v + r3b * m[5].v;
+    }
+    w.f1 = -ri1b * y;
+    w.f2 = -ri2b * y;
+    w.f3 = -ri3b * y;
+    w.bx = ri2b * y;
+    w.by = ri3b * y;
+    if (fric) {
+      const double sf2b = ri2b * y, sf3b = ri3b * y;
+      const double mb[6] = {r2b * ri1, r2b * ri2, r2b * ri3, r3b * ri1, r3b * ri2, r3b * ri3};
+      double g[4];
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        double v = sf2b * sf2.d[k] + sf3b * sf3.d[k];
+        if (impl) {
+#pragma unroll
+          for (int j = 0; j < 6; ++j) v = fma(mb[j], m[j].d[k], v);
+        }
+        g[k] = v;
+      }
+      own.x += g[0];
+      own.y += g[1];
+      own.z += g[2];
+      nb = g[3];
+    }
+  }
+  A.lam_own[c] = own;
   A.cadj[c] = w;
-  A.gman[c] += g[8];
+  A.gman[c] += nb;
 }
 
 /* ---- adjoint of the edge stage ---------------------------------------------------------- */
@@ -197,7 +273,7 @@ __global__ void __launch_bounds__(TILE_E) k_adj_edges(AdjArgs A) {
     interior_edge<IFLUX>(M, a.ilimiteur, a.flux_mode, G, dt, seed<D>(UA.x, 0, base), seed<D>(UA.y, 1, base),
                          seed<D>(UA.z, 2, base), UA.w, seed<D>(UB.x, 3, base), seed<D>(UB.y, 4, base),
                          seed<D>(UB.z, 5, base), UB.w, seed<D>(hl_upw, 6, base), seed<D>(vl_upw, 7, base), zl_upw,
-                         seed<D>(hr_upw, 8, base), seed<D>(vr_upw, 9, base), zr_upw, o);
+                         seed<D>(hr_upw, 8, base), seed<D>(vr_upw, 9, base), zr_upw, o, A.freeze_r != 0);
 #pragma unroll
     for (int i = 0; i < D; ++i) {
       if (base + i < NDIR) {
@@ -222,31 +298,14 @@ __global__ void __launch_bounds__(TILE_E) k_adj_edges(AdjArgs A) {
   }
 }
 
-/* ---- gather ---------------------------------------------------------------------------- */
+/* ---- lambda^0 -------------------------------------------------------------------------- */
 
-__global__ void __launch_bounds__(TILE_C) k_adj_gather(AdjArgs A) {
-  const StepArgs& a = A.s;
+__global__ void __launch_bounds__(TILE_C) k_adj_final(AdjArgs A) {
   const int tile = blockIdx.x;
-  const MemberDev& M = a.mdev[__ldg(a.ctile_mem + tile)];
+  const MemberDev& M = A.s.mdev[__ldg(A.s.ctile_mem + tile)];
   const int c = tile * TILE_C + threadIdx.x;
   if (c >= M.cell_end) return;
-  double4 L = A.lam_out[c];
-  const int4 sl = __ldg(a.cslot + c);
-  const double4 e0 = ld4(A.eadj + sl.x), e1 = ld4(A.eadj + sl.y), e2 = ld4(A.eadj + sl.z);
-  L.x = L.x + e0.x + e1.x + e2.x;
-  L.y = L.y + e0.y + e1.y + e2.y;
-  L.z = L.z + e0.z + e1.z + e2.z;
-  if (A.uoff) {
-    for (int j = __ldg(A.uoff + c), j1 = __ldg(A.uoff + c + 1); j < j1; ++j) {
-      const double4 u = ld4(A.uadj + __ldg(A.uidx + j));
-      L.x += u.x;
-      L.y += u.y;
-      L.z += u.z;
-    }
-  }
-  if (A.gw)
-    for (int j = __ldg(A.goff + c), j1 = __ldg(A.goff + c + 1); j < j1; ++j) L.x += __ldg(A.gw + __ldg(A.gidx + j));
-  A.lam_out[c] = L;
+  A.lam_own[c] = gather_lambda(A, c, nullptr);
 }
 
 /* lambda.h += the objective's weights of the gauges an element carries (the final state's
@@ -272,7 +331,7 @@ int chk(cudaError_t e) { return e == cudaSuccess ? CF_OK : CF_ECUDA; }
 }  // namespace
 
 int launch_replay_step(const StepArgs& a, const double* dt_hist, const double* t_hist, int n, uint32_t* flag,
-                       stream_t s) {
+                       Slot* sums, stream_t s) {
   cudaStream_t st = reinterpret_cast<cudaStream_t>(s);
   switch (a.iflux) {
     case 1: k_rep_edges<1><<<a.n_etiles, TILE_E, 0, st>>>(a, dt_hist, t_hist, n); break;
@@ -280,7 +339,7 @@ int launch_replay_step(const StepArgs& a, const double* dt_hist, const double* t
     case 3: k_rep_edges<3><<<a.n_etiles, TILE_E, 0, st>>>(a, dt_hist, t_hist, n); break;
     default: return CF_ENOTSUP;
   }
-  if (flag) k_rep_cells<<<a.n_ctiles, TILE_C, 0, st>>>(a, dt_hist, n, flag);
+  k_rep_cells<<<a.n_ctiles, TILE_C, 0, st>>>(a, dt_hist, n, flag, sums);
   return chk(cudaGetLastError());
 }
 
@@ -293,16 +352,18 @@ int launch_record(const double4* Unew, const MemberState* S, int p, int n, doubl
 int launch_adjoint_step(const AdjArgs& A, stream_t s) {
   cudaStream_t st = reinterpret_cast<cudaStream_t>(s);
   const StepArgs& a = A.s;
-  int rc = launch_replay_step(a, A.dt_hist, A.t_hist, A.n, nullptr, s);   /* slots at U^n */
-  if (rc != CF_OK) return rc;
-  k_adj_cells<3><<<a.n_ctiles, TILE_C, 0, st>>>(A);
+  k_adj_cells<<<a.n_ctiles, TILE_C, 0, st>>>(A);
   switch (a.iflux) {
     case 1: k_adj_edges<1, 3><<<a.n_etiles, TILE_E, 0, st>>>(A); break;
     case 2: k_adj_edges<2, 3><<<a.n_etiles, TILE_E, 0, st>>>(A); break;
     case 3: k_adj_edges<3, 2><<<a.n_etiles, TILE_E, 0, st>>>(A); break;
     default: return CF_ENOTSUP;
   }
-  k_adj_gather<<<a.n_ctiles, TILE_C, 0, st>>>(A);
+  return chk(cudaGetLastError());
+}
+
+int launch_adjoint_final(const AdjArgs& A, stream_t s) {
+  k_adj_final<<<A.s.n_ctiles, TILE_C, 0, reinterpret_cast<cudaStream_t>(s)>>>(A);
   return chk(cudaGetLastError());
 }
 

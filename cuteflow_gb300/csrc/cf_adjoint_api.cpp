@@ -11,9 +11,10 @@
  *
  * Checkpointing.  The recording forward keeps the state every K steps (K ~ sqrt(N) by default).
  * The backward sweep walks the segments from the last: it recomputes the segment's states from
- * its checkpoint with the recorded dt sequence (bit-identical to the recorded run) and then runs
- * the reverse steps through them.  Memory: ceil(N/K) + max(K, 2) states; cost: one extra
- * forward pass besides the reverse steps.
+ * its checkpoint with the recorded dt sequence (bit-identical to the recorded run), keeping
+ * every step's per-element flux and bed sums, and then runs the reverse steps through them.
+ * Memory: ceil(N/K) + max(K, 2) states and max(K, 2) sum records (48 B per element each);
+ * cost: one extra forward pass besides the reverse steps.
  *
  * Contexts with one member only.
  */
@@ -43,7 +44,8 @@ struct cf_adjoint {
   int32_t* gcell = nullptr;
   int32_t* goff = nullptr;
   int32_t* gidx = nullptr;
-  double4* lam[2] = {nullptr, nullptr};
+  double4* lam[2] = {nullptr, nullptr};   /* lambda^N (terminal weights); own part of lambda^n */
+  Slot* sums = nullptr;      /* nseg_states x n_pad: flux and bed sums of every step of a segment */
   Slot* cadj = nullptr;
   double4* eadj = nullptr;
   double4* uadj = nullptr;
@@ -51,6 +53,7 @@ struct cf_adjoint {
   int32_t* uidx = nullptr;
   double* gman = nullptr;
   uint32_t* flag = nullptr;
+  int32_t freeze_r = 0;      /* linearization of the WAF limiter ratios: 0 exact, 1 held */
   bool recorded = false;     /* a recording forward has filled dt_hist / t_hist */
   bool have_traj = false;    /* the checkpoints hold the last forward's trajectory */
 };
@@ -59,7 +62,7 @@ namespace {
 
 void adj_free(cf_adjoint* a) {
   void* ptrs[] = {a->ckpt, a->seg, a->mst, a->dt_hist, a->t_hist, a->eta, a->wbuf, a->gcell, a->goff, a->gidx,
-                  a->lam[0], a->lam[1], a->cadj, a->eadj, a->uadj, a->uoff, a->uidx, a->gman, a->flag};
+                  a->lam[0], a->lam[1], a->sums, a->cadj, a->eadj, a->uadj, a->uoff, a->uidx, a->gman, a->flag};
   for (void* p : ptrs)
     if (p) cudaFree(p);
 }
@@ -119,6 +122,7 @@ int create_impl(cf_ctx* c, int32_t nsteps, int32_t interval, const int32_t* gaug
       (rc = dalloc(c, &a->wbuf, (size_t)nsteps * ngauges)) || (rc = dalloc(c, &a->gcell, (size_t)ngauges)) ||
       (rc = dalloc(c, &a->goff, np + 1)) || (rc = dalloc(c, &a->gidx, (size_t)ngauges)) ||
       (rc = dalloc(c, &a->lam[0], np)) || (rc = dalloc(c, &a->lam[1], np)) || (rc = dalloc(c, &a->cadj, np)) ||
+      (rc = dalloc(c, &a->sums, (size_t)a->nseg_states * np)) ||
       (rc = dalloc(c, &a->eadj, 2 * nep)) || (rc = dalloc(c, &a->gman, np)) || (rc = dalloc(c, &a->flag, 1)))
     return done(rc);
   /* gauges: new order, and their CSR over the elements */
@@ -197,7 +201,8 @@ int forward_impl(cf_adjoint* a, int32_t replay, double* eta_out, double* state_o
       if ((rc = launch_step(sa, st, nullptr, nullptr))) return fail(c, rc, "step launch failed");
       rc = launch_record(Y, a->mst, p, k, a->dt_hist, a->t_hist, a->gcell, a->G, a->eta, st);
     } else {
-      if ((rc = launch_replay_step(sa, a->dt_hist, a->t_hist, k, a->flag, st))) return fail(c, rc, "replay launch failed");
+      if ((rc = launch_replay_step(sa, a->dt_hist, a->t_hist, k, a->flag, nullptr, st)))
+        return fail(c, rc, "replay launch failed");
       rc = launch_record(Y, nullptr, 0, k, a->dt_hist, a->t_hist, a->gcell, a->G, a->eta, st);
     }
     if (rc) return fail(c, rc, "record launch failed");
@@ -244,29 +249,34 @@ int backward_impl(cf_adjoint* a, const double* w_eta, const double* w_state, dou
   }
   if (weights && (rc = launch_add_gauges(a->lam[0], a->goff, a->gidx, a->wbuf + (size_t)(a->N - 1) * a->G, a->n, st)))
     return fail(c, rc, "gauge launch failed");
-  double4* Lin = a->lam[0];
-  double4* Lout = a->lam[1];
+  /* lam[0] = lambda^N; lam[1] = the own part of lambda^k, carried from reverse step to reverse
+   * step (the edge contributions are gathered by the next reverse step, or the final pass). */
+  bool first = true;
+  AdjArgs A{};
   for (int32_t j = a->nseg - 1; j >= 0; --j) {
     const int32_t s0 = j * a->K, s1 = std::min(a->N, s0 + a->K);
     CF_CUDA(c, cudaMemcpyAsync(a->seg, a->ckpt + (size_t)j * np, np * sizeof(double4), cudaMemcpyDeviceToDevice,
                                c->stream));
-    for (int32_t i = 0; i + 1 < s1 - s0; ++i) {
+    /* replay the segment: its states and, for every step, the flux and bed sums at U^k */
+    for (int32_t i = 0; i < s1 - s0; ++i) {
       StepArgs sa = step_args(c, 0);
       sa.Uin = a->seg + (size_t)i * np;
-      sa.Uout = a->seg + (size_t)(i + 1) * np;
-      if ((rc = launch_replay_step(sa, a->dt_hist, a->t_hist, s0 + i, a->flag, st)))
+      sa.Uout = (i + 1 < s1 - s0) ? a->seg + (size_t)(i + 1) * np : nullptr;
+      if ((rc = launch_replay_step(sa, a->dt_hist, a->t_hist, s0 + i, a->flag, a->sums + (size_t)i * np, st)))
         return fail(c, rc, "replay launch failed");
     }
     for (int32_t k = s1 - 1; k >= s0; --k) {
-      AdjArgs A{};
+      A = AdjArgs{};
       A.s = step_args(c, 0);
       A.s.Uin = a->seg + (size_t)(k - s0) * np;
       A.s.Uout = nullptr;
       A.dt_hist = a->dt_hist;
       A.t_hist = a->t_hist;
       A.n = k;
-      A.lam_in = Lin;
-      A.lam_out = Lout;
+      A.gather = first ? 0 : 1;
+      A.sums = a->sums + (size_t)(k - s0) * np;
+      A.lam_init = a->lam[0];
+      A.lam_own = a->lam[1];
       A.cadj = a->cadj;
       A.eadj = a->eadj;
       A.uadj = a->uadj;
@@ -274,12 +284,16 @@ int backward_impl(cf_adjoint* a, const double* w_eta, const double* w_state, dou
       A.uidx = a->uidx;
       A.goff = a->goff;
       A.gidx = a->gidx;
-      A.gw = (weights && k >= 1) ? a->wbuf + (size_t)(k - 1) * a->G : nullptr;
+      /* the gauges of U^{k+1} (row k); those of U^N are already in lambda^N */
+      A.gw = (weights && k + 1 < a->N) ? a->wbuf + (size_t)k * a->G : nullptr;
       A.gman = a->gman;
+      A.freeze_r = a->freeze_r;
       if ((rc = launch_adjoint_step(A, st))) return fail(c, rc, "adjoint launch failed");
-      std::swap(Lin, Lout);
+      first = false;
     }
   }
+  if ((rc = launch_adjoint_final(A, st))) return fail(c, rc, "adjoint launch failed");
+  double4* Lin = a->lam[1];
   if (g_state0) {
     if ((rc = launch_gather_state(Lin, c->iperm, c->staging, a->n, st))) return fail(c, rc, "gather launch failed");
     if ((rc = to_user(c, g_state0, c->staging, 3 * (size_t)a->n))) return rc;
@@ -358,6 +372,13 @@ int cf_adjoint_set_dt(cf_adjoint* a, const double* dt, const double* t) {
   return CF_OK;
 }
 
+int cf_adjoint_set_linearization(cf_adjoint* a, int32_t mode) {
+  if (!a) return CF_EINVAL;
+  if (mode < 0 || mode > 1) return fail(a->ctx, CF_EINVAL, "linearization mode must be 0 or 1");
+  a->freeze_r = mode;
+  return CF_OK;
+}
+
 int cf_adjoint_sizes(cf_adjoint* a, int32_t* nsteps, int32_t* interval, int32_t* ngauges, int64_t* device_bytes) {
   if (!a) return CF_EINVAL;
   if (nsteps) *nsteps = a->N;
@@ -365,7 +386,8 @@ int cf_adjoint_sizes(cf_adjoint* a, int32_t* nsteps, int32_t* interval, int32_t*
   if (ngauges) *ngauges = a->G;
   if (device_bytes) {
     const int64_t np = a->n_pad, nep = a->ctx->ne_pad;
-    int64_t b = (int64_t)(a->nseg + a->nseg_states + 2) * np * (int64_t)sizeof(double4) + np * (int64_t)sizeof(Slot) +
+    int64_t b = (int64_t)(a->nseg + a->nseg_states + 2) * np * (int64_t)sizeof(double4) +
+                (int64_t)(a->nseg_states + 1) * np * (int64_t)sizeof(Slot) +
                 2 * nep * (int64_t)sizeof(double4) + np * 8 + (int64_t)a->N * (16 + 16 * (int64_t)a->G);
     if (a->uadj) b += 4 * nep * (int64_t)sizeof(double4);
     *device_bytes = b;

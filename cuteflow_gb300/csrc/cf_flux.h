@@ -291,13 +291,21 @@ CF_HD CF_INLINE T waf_limiter(int ilim, T r, T c) {
 template <class T>
 CF_HD CF_INLINE double sgn1(const T& x) { return copysign(1.0, val(x)); }
 
+/* x, or (freeze) its value taken as a constant of the linearization; the same number either way. */
+template <class T>
+CF_HD CF_INLINE T held(const T& x, bool freeze) { return freeze ? T(val(x)) : x; }
+
 /* Second-order WAF (IFLUX 3, flux_riemann.cuf:720-900) for both sides.  Inputs: the
  * reconstructed, masked edge-frame states of A (left) and B (right), the upwind
- * reconstructions (h, v) of each side, dt, and the distances d_mrl, d_mkvol (A), d_mkvoisin (B). */
+ * reconstructions (h, v) of each side, dt, and the distances d_mrl, d_mkvol (A), d_mkvoisin (B).
+ * freeze_r (linearizations only) holds the limiter ratios r constant: r = dupw / (dloc + eps)
+ * divides differences that are at round-off level in still water, and its derivative there
+ * (~1/eps) carries no information. */
 template <class T>
 CF_HD CF_INLINE void waf_flux(double g, int ilim, double nx, double ny, double dt, double d_mrl, double y_mrl,
                               double d_mkvol, double y_mkvol, double d_mkvoisin, double y_mkvoisin, T hl, T ul,
-                              T vl, T hr, T ur, T vr, T hl_upw, T vl_upw, T hr_upw, T vr_upw, TwoFluxT<T>& F) {
+                              T vl, T hr, T ur, T vr, T hl_upw, T vl_upw, T hr_upw, T vr_upw, TwoFluxT<T>& F,
+                              bool freeze_r = false) {
   const double eps = EPS_SECOND;
   T sl, sr, set;
   if (!wave_speeds(g, eps, hl, ul, hr, ur, sl, sr, set)) {
@@ -327,13 +335,13 @@ CF_HD CF_INLINE void waf_flux(double g, int ilim, double nx, double ny, double d
   const T upr = div_rn(hr_upw - hr, d_mkvoisin, y_mkvoisin);  /* upwind difference of side B */
   const T upvl = div_rn(vl - vl_upw, d_mkvol, y_mkvol);
   const T upvr = div_rn(vr_upw - vr, d_mkvoisin, y_mkvoisin);
-  const T ret_a = ((set > 0.) ? upvl : upvr) / (dloc_et + eps);
+  const T ret_a = held(((set > 0.) ? upvl : upvr) / (dloc_et + eps), freeze_r);
 
   /* side A (:854-899) */
   {
     const T den = dloc + eps, yd = 1.0 / den;
-    const T rl = div_rn((sl > 0.) ? upl : upr, den, yd);
-    const T rr = div_rn((sr > 0.) ? upl : upr, den, yd);
+    const T rl = held(div_rn((sl > 0.) ? upl : upr, den, yd), freeze_r);
+    const T rr = held(div_rn((sr > 0.) ? upl : upr, den, yd), freeze_r);
     const T ll = waf_limiter(ilim, rl, cl);
     const T lr = waf_limiter(ilim, rr, cr);
     const T le = waf_limiter(ilim, ret_a, cet);
@@ -354,10 +362,10 @@ CF_HD CF_INLINE void waf_flux(double g, int ilim, double nx, double ny, double d
    * tangential ones coincide; its Courant numbers are -cr, -cl, -cet. */
   {
     const T den = -dloc + eps, yd = 1.0 / den;
-    const T rl = div_rn((-sr > 0.) ? -upr : -upl, den, yd);
-    const T rr = div_rn((-sl > 0.) ? -upr : -upl, den, yd);
+    const T rl = held(div_rn((-sr > 0.) ? -upr : -upl, den, yd), freeze_r);
+    const T rr = held(div_rn((-sl > 0.) ? -upr : -upl, den, yd), freeze_r);
     /* B's tangential ratio differs from A's only when s* == 0 (or is NaN) */
-    const T ret_b = (set > 0. || set < 0.) ? ret_a : ((-set > 0.) ? upvr : upvl) / (dloc_et + eps);
+    const T ret_b = (set > 0. || set < 0.) ? ret_a : held(((-set > 0.) ? upvr : upvl) / (dloc_et + eps), freeze_r);
     const T ll = waf_limiter(ilim, rl, -cr);
     const T lr = waf_limiter(ilim, rr, -cl);
     const T le = waf_limiter(ilim, ret_b, -cet);
@@ -492,7 +500,8 @@ struct EdgeGeo {
 template <int IFLUX, class T>
 CF_HD CF_INLINE void interior_edge(const MemberDev& M, int ilim, int flux_mode, const EdgeGeo& G, double dt, T hA,
                                    T huA, T hvA, double zml, T hB, T huB, T hvB, double zmr, T hl_upw, T vl_upw,
-                                   double zl_upw, T hr_upw, T vr_upw, double zr_upw, T out[10]) {
+                                   double zl_upw, T hr_upw, T vr_upw, double zr_upw, T out[10],
+                                   bool freeze_r = false) {
   const double g = M.gp, tolisec = M.tolisec;
   const double nx = G.nx, ny = G.ny, len = G.len;
   const double zij = dmax(zml, zmr);
@@ -533,7 +542,7 @@ CF_HD CF_INLINE void interior_edge(const MemberDev& M, int ilim, int flux_mode, 
     if (hjiet < tolisec) { hjiet = T(0.); ur = T(0.); vr = T(0.); }
     if (hru < tolisec) { hru = T(0.); vru = T(0.); }
     waf_flux(g, ilim, nx, ny, dt, G.d_mrl, G.y_mrl, G.d_mkvol, G.y_mkvol, G.d_mkvoisin, G.y_mkvoisin, hijet, ul, vl,
-             hjiet, ur, vr, hlu, vlu, hru, vru, F);
+             hjiet, ur, vr, hlu, vlu, hru, vru, F, freeze_r);
   }
   if (flux_mode == 1) {
     F.b1 = -F.a1;
@@ -645,6 +654,54 @@ CF_HD CF_INLINE double cfl_dt_elem(const MemberDev& M, double cflL, double h, do
   return d;
 }
 
+/* Manning friction of one element (source_terms.cuf:102-210): the source (sf2, sf3) of its
+ * state q and the entries m = {m4, m5, m6, m7, m8, m9} of the rows 2 and 3 of the
+ * semi-implicit matrix (I - dt/2 J)^-1 (row 1 is (1, 0, 0)).  A dry element, or
+ * fricimplic 0, gives m = {0, 1, 0, 0, 0, 1}. */
+template <class T>
+CF_HD CF_INLINE void friction_terms(const MemberDev& M, double area, double dt, T manning, T q1, T q2, T q3, T& sf2,
+                                    T& sf3, T m[6]) {
+  const double gp = M.gp, tolisec = M.tolisec, tol = M.tol;
+  sf2 = T(0.);
+  sf3 = T(0.);
+  m[0] = T(0.); m[1] = T(1.); m[2] = T(0.); m[3] = T(0.); m[4] = T(0.); m[5] = T(1.);
+  if (q1 > tolisec) {
+    const T yq = 1.0 / q1;
+    const T vitu = div_rn(q2, q1, yq), vitv = div_rn(q3, q1, yq);
+    T normvit = sqrt(vitu * vitu + vitv * vitv);
+    if (normvit < tol) normvit = T(tol);
+    const T p13 = 1.0 / cbrt_halley(q1);    /* q1**(-1/3) */
+    sf2 = -(gp * manning * manning * vitu * normvit * area * p13);
+    sf3 = -(gp * manning * manning * vitv * normvit * area * p13);
+    if (normvit > tol) {
+      const T p43 = div_rn(p13, q1, yq);     /* q1**(-4/3) */
+      if (M.fricimplic == 1) {
+        const T yn = 1.0 / normvit;
+        const T dtgn2h = dt / 2.0 * gp * manning * manning * p43;
+        const T af21 = -(7.0 / 3.0 * dtgn2h * vitu * normvit);
+        const T af22 = 1.0 + div_rn(dtgn2h * (2. * (vitu * vitu) + vitv * vitv), normvit, yn);
+        const T af23 = div_rn(dtgn2h * vitu * vitv, normvit, yn);
+        const T af31 = -(7.0 / 3.0 * dtgn2h * vitv * normvit);
+        const T af32 = af23;
+        const T af33 = 1.0 + div_rn(dtgn2h * (vitu * vitu + 2. * (vitv * vitv)), normvit, yn);
+        const T detaf = af22 * af33 - af23 * af32;
+        const T yd = 1.0 / detaf;
+        m[0] = div_rn(-(af21 * af33 - af23 * af31), detaf, yd);
+        m[1] = div_rn(af33, detaf, yd);
+        m[2] = div_rn(-af23, detaf, yd);
+        m[3] = div_rn(af21 * af32 - af22 * af31, detaf, yd);
+        m[4] = div_rn(-af32, detaf, yd);
+        m[5] = div_rn(af22, detaf, yd);
+      } else if (M.fricimplic == 2) {
+        const T beta = -(dt * gp * manning * manning * normvit * p43);
+        const T detaf = (1. - beta) * (1. - beta);
+        m[1] = (1. - beta) / detaf;
+        m[5] = (1. - beta) / detaf;
+      }
+    }
+  }
+}
+
 /* Sources, friction and update of one element (source_terms.cuf:33-211,
  * finite_volumes_method.cuf:283-303) from its state q, the sums rc of its three edge fluxes
  * and sb of its bed sources, its area (and RN(1/area)) and its Manning n.  The wet/dry clamp
@@ -652,53 +709,17 @@ CF_HD CF_INLINE double cfl_dt_elem(const MemberDev& M, double cflL, double h, do
 template <class T>
 CF_HD CF_INLINE void element_core(const MemberDev& M, double area, double yarea, T manning, T q1, T q2, T q3, T rc1,
                                   T rc2, T rc3, T sb2, T sb3, double dt, T& h, T& hu, T& hv, bool& nonfinite) {
-  const double gp = M.gp, tolisec = M.tolisec, tol = M.tol;
   T r1, r2, r3;
   if (M.friction == 1) {
-    T sf2 = T(0.), sf3 = T(0.);
-    T m4 = T(0.), m5 = T(1.), m6 = T(0.), m7 = T(0.), m8 = T(0.), m9 = T(1.);
-    if (q1 > tolisec) {
-      const T yq = 1.0 / q1;
-      const T vitu = div_rn(q2, q1, yq), vitv = div_rn(q3, q1, yq);
-      T normvit = sqrt(vitu * vitu + vitv * vitv);
-      if (normvit < tol) normvit = T(tol);
-      const T p13 = 1.0 / cbrt_halley(q1);    /* q1**(-1/3) */
-      sf2 = -(gp * manning * manning * vitu * normvit * area * p13);
-      sf3 = -(gp * manning * manning * vitv * normvit * area * p13);
-      if (normvit > tol) {
-        const T p43 = div_rn(p13, q1, yq);     /* q1**(-4/3) */
-        if (M.fricimplic == 1) {
-          const T yn = 1.0 / normvit;
-          const T dtgn2h = dt / 2.0 * gp * manning * manning * p43;
-          const T af21 = -(7.0 / 3.0 * dtgn2h * vitu * normvit);
-          const T af22 = 1.0 + div_rn(dtgn2h * (2. * (vitu * vitu) + vitv * vitv), normvit, yn);
-          const T af23 = div_rn(dtgn2h * vitu * vitv, normvit, yn);
-          const T af31 = -(7.0 / 3.0 * dtgn2h * vitv * normvit);
-          const T af32 = af23;
-          const T af33 = 1.0 + div_rn(dtgn2h * (vitu * vitu + 2. * (vitv * vitv)), normvit, yn);
-          const T detaf = af22 * af33 - af23 * af32;
-          const T yd = 1.0 / detaf;
-          m4 = div_rn(-(af21 * af33 - af23 * af31), detaf, yd);
-          m5 = div_rn(af33, detaf, yd);
-          m6 = div_rn(-af23, detaf, yd);
-          m7 = div_rn(af21 * af32 - af22 * af31, detaf, yd);
-          m8 = div_rn(-af32, detaf, yd);
-          m9 = div_rn(af22, detaf, yd);
-        } else if (M.fricimplic == 2) {
-          const T beta = -(dt * gp * manning * manning * normvit * p43);
-          const T detaf = (1. - beta) * (1. - beta);
-          m5 = (1. - beta) / detaf;
-          m9 = (1. - beta) / detaf;
-        }
-      }
-    }
+    T sf2, sf3, m[6];
+    friction_terms(M, area, dt, manning, q1, q2, q3, sf2, sf3, m);
     const T ri1 = div_rn(0. + 0. - rc1, area, yarea);
     const T ri2 = div_rn(sb2 + sf2 - rc2, area, yarea);
     const T ri3 = div_rn(sb3 + sf3 - rc3, area, yarea);
     if (M.fricimplic == 1 || M.fricimplic == 2) {
       r1 = 1. * ri1 + 0. * ri2 + 0. * ri3;
-      r2 = m4 * ri1 + m5 * ri2 + m6 * ri3;
-      r3 = m7 * ri1 + m8 * ri2 + m9 * ri3;
+      r2 = m[0] * ri1 + m[1] * ri2 + m[2] * ri3;
+      r3 = m[3] * ri1 + m[4] * ri2 + m[5] * ri3;
     } else {
       r1 = ri1;
       r2 = ri2;
@@ -713,7 +734,7 @@ CF_HD CF_INLINE void element_core(const MemberDev& M, double area, double yarea,
   hu = q2 + dt * r2;
   hv = q3 + dt * r3;
   nonfinite = !(finite_bits(val(h)) && finite_bits(val(hu)) && finite_bits(val(hv)));
-  if (h <= tolisec) {
+  if (h <= M.tolisec) {
     h = T(0.);
     hu = T(0.);
     hv = T(0.);

@@ -154,14 +154,16 @@ int launch_gather_state(const double4* U, const int32_t* iperm_old2new, double* 
 
 /* ---- discrete adjoint (cf_adjoint.cu) ------------------------------------------------- */
 
-/* One reverse step n: s holds the step's buffers with s.Uin = U^n (s.slots is overwritten). */
+/* One reverse step n: s holds the step's buffers with s.Uin = U^n. */
 struct AdjArgs {
   StepArgs s;
   const double* dt_hist;   /* dt of every step (frozen) */
   const double* t_hist;    /* start time of every step */
   int32_t n;
-  const double4* lam_in;   /* lambda^{n+1} = dJ/dU^{n+1} (x, y, z used) */
-  double4* lam_out;        /* lambda^n */
+  int32_t gather;          /* 1: lambda^{n+1} = lam_own + the edge contributions; 0: lam_init */
+  const Slot* sums;        /* per element: its flux sums (f1..f3) and bed sums (bx, by) at U^n */
+  const double4* lam_init; /* lambda^N */
+  double4* lam_own;        /* in: the element's own part of lambda^{n+1}; out: of lambda^n */
   Slot* cadj;              /* per element: adjoint of its flux sums (f1..f3) and bed sums (bx, by) */
   double4* eadj;           /* per edge side: contribution to the side's element */
   double4* uadj;           /* per edge, 4: contributions to the upwind elements (second order) */
@@ -169,18 +171,22 @@ struct AdjArgs {
   const int32_t* uidx;
   const int32_t* goff;     /* per element: its gauges in gidx */
   const int32_t* gidx;
-  const double* gw;        /* objective weights of the gauge elevations after step n, or NULL */
+  const double* gw;        /* objective weights of the gauge elevations after step n+1, or NULL */
   double* gman;            /* dJ/dn, accumulated */
+  int32_t freeze_r;        /* 1: WAF limiter ratios held constant in the linearization */
 };
 
-/* edge and element stages of step n with the recorded dt / time (flag: element stage too,
- * non-finite results OR-ed into *flag; NULL: edge stage only) */
+/* Step n with the recorded dt / time: edge stage, then element stage writing a.Uout (if not
+ * NULL) and, if sums is not NULL, every element's flux and bed sums; non-finite results are
+ * OR-ed into *flag. */
 int launch_replay_step(const StepArgs& a, const double* dt_hist, const double* t_hist, int n, uint32_t* flag,
-                       stream_t s);
+                       Slot* sums, stream_t s);
 /* gauge elevations of Unew into eta row n; with S, also dt / t of parity p into the histories */
 int launch_record(const double4* Unew, const MemberState* S, int p, int n, double* dt_hist, double* t_hist,
                   const int32_t* gcell, int G, double* eta, stream_t s);
 int launch_adjoint_step(const AdjArgs& A, stream_t s);
+/* lambda^0 = lam_own + the edge contributions of the last reverse step, into lam_own */
+int launch_adjoint_final(const AdjArgs& A, stream_t s);
 int launch_add_gauges(double4* lam, const int32_t* goff, const int32_t* gidx, const double* gw, int32_t n, stream_t s);
 int launch_gather_scalar(const double* x, const int32_t* iperm, double* out, int32_t n, stream_t s);
 int launch_set_manning(double4* cstat, const int32_t* perm, const double* nref, int32_t n, stream_t s);

@@ -84,8 +84,9 @@ def load(build_if_missing: bool = True):
     L.cf_adjoint_get_dt.argtypes = [vp, vp, vp]
     L.cf_adjoint_set_dt.argtypes = [vp, vp, vp]
     L.cf_adjoint_sizes.argtypes = [vp, ip, ip, ip, C.POINTER(C.c_int64)]
+    L.cf_adjoint_set_linearization.argtypes = [vp, C.c_int32]
     for name in ("cf_set_manning", "cf_adjoint_create", "cf_adjoint_forward", "cf_adjoint_backward",
-                 "cf_adjoint_get_dt", "cf_adjoint_set_dt", "cf_adjoint_sizes"):
+                 "cf_adjoint_get_dt", "cf_adjoint_set_dt", "cf_adjoint_sizes", "cf_adjoint_set_linearization"):
         getattr(L, name).restype = C.c_int
     for name in ("cf_create_batch", "cf_get_members", "cf_member_set_state", "cf_member_set_initial_condition",
                  "cf_member_get_state", "cf_member_get_info", "cf_member_get_mesh_tables"):

@@ -237,6 +237,16 @@ int cf_adjoint_backward(cf_adjoint* adj, const double* w_eta, const double* w_st
 /* The recorded dt and start time of every step [N]; set_dt installs a sequence to replay. */
 int cf_adjoint_get_dt(cf_adjoint* adj, double* dt, double* t);
 int cf_adjoint_set_dt(cf_adjoint* adj, const double* dt, const double* t);
+/* Linearization of the WAF limiter (iflux 3): mode 0 (default) differentiates everything, the
+ * exact derivative of the step along the branches the forward took; mode 1 holds the limiter
+ * ratios r = dupw / (dloc + eps) constant.  Over long runs the WAF objective is not
+ * differentiable (the limiter jumps when dloc changes sign, superbee also at r = 0.5, 1, 2,
+ * and r divides round-off in still water, where its exact derivative ~1/eps overflows).
+ * Mode 1 is an approximate gradient for those runs: on a 10,000-triangle flooding case over
+ * 2000 steps its tangent stays bounded with the van Albada limiter (ilimiteur 3), while the
+ * exact one grows by 1e133; with superbee (ilimiteur 1), whose frozen weights are
+ * anti-diffusive, it still grows (1e18 against 1e290).  First-order schemes need neither. */
+int cf_adjoint_set_linearization(cf_adjoint* adj, int32_t mode);
 int cf_adjoint_sizes(cf_adjoint* adj, int32_t* nsteps, int32_t* checkpoint_interval, int32_t* ngauges,
                      int64_t* device_bytes);
 

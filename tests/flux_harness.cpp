@@ -176,7 +176,7 @@ typedef Dual<1> D1;
 extern "C" int harness_tangent(const cf_mesh* m, const cf_params* p, const double* U0, const double* dU0,
                                const double* nman, const double* dn, int nsteps, const double* dt_seq,
                                const double* t_seq, const int32_t* gauges, int G, double* eta, double* deta,
-                               double* U_out, double* dU_out) {
+                               double* U_out, double* dU_out, int freeze_r) {
   Prep P;
   std::string err;
   int rc = prepare_mesh(m, p, P, err);
@@ -243,7 +243,7 @@ extern "C" int harness_tangent(const cf_mesh* m, const cf_params* p, const doubl
                          hu[ab.y], hv[ab.y], z[ab.y], hlu, vlu, zlu, hru, vru, zru, sa);
       else
         interior_edge<3>(M, p->ilimiteur, p->flux_mode, Gm, dt, h[ab.x], hu[ab.x], hv[ab.x], z[ab.x], h[ab.y],
-                         hu[ab.y], hv[ab.y], z[ab.y], hlu, vlu, zlu, hru, vru, zru, sa);
+                         hu[ab.y], hv[ab.y], z[ab.y], hlu, vlu, zlu, hru, vru, zru, sa, freeze_r != 0);
     }
     for (int c = 0; c < n; ++c) {
       const int* sl = &P.cslot[c].x;

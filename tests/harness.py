@@ -75,7 +75,7 @@ def div_check(n, seed=12345):
     return int(L.harness_div_check(int(n), int(seed)))
 
 
-def tangent(case, params, U0, dU0, manning, dn, dt, t, gauges):
+def tangent(case, params, U0, dU0, manning, dn, dt, t, gauges, freeze_r=False):
     """Tangent-linear run (forward mode along (dU0, dn)) replaying dt / t: returns
     (eta, deta, U_N, dU_N)."""
     from cuteflow_gb300 import _abi
@@ -84,7 +84,7 @@ def tangent(case, params, U0, dU0, manning, dn, dt, t, gauges):
         dp = C.POINTER(C.c_double)
         ip = C.POINTER(C.c_int32)
         L.harness_tangent.argtypes = [C.POINTER(_abi.CfMesh), C.POINTER(_abi.CfParams), dp, dp, dp, dp, C.c_int, dp,
-                                      dp, ip, C.c_int, dp, dp, dp, dp]
+                                      dp, ip, C.c_int, dp, dp, dp, dp, C.c_int]
         L.harness_tangent.restype = C.c_int
         L._tan_typed = True
     ma = _abi.MeshArrays(case)
@@ -97,6 +97,6 @@ def tangent(case, params, U0, dU0, manning, dn, dt, t, gauges):
     U, dU = np.zeros_like(U0), np.zeros_like(U0)
     rc = L.harness_tangent(C.byref(ma.mesh), C.byref(p), _abi.dptr(U0), _abi.dptr(dU0), _abi.dptr(manning),
                            _abi.dptr(dn), N, _abi.dptr(dt), _abi.dptr(t), g.ctypes.data_as(C.POINTER(C.c_int32)), G,
-                           _abi.dptr(eta), _abi.dptr(deta), _abi.dptr(U), _abi.dptr(dU))
+                           _abi.dptr(eta), _abi.dptr(deta), _abi.dptr(U), _abi.dptr(dU), int(bool(freeze_r)))
     assert rc == 0
     return eta, deta, U, dU

@@ -111,8 +111,9 @@ def test_gradient_matches_central_differences_oracle(gpu_lib, oracle, kind):
     assert abs(fd - ad) <= RTOL * abs(ad), (fd, ad)
 
 
-@pytest.mark.parametrize("kind", AC.ALL_KINDS)
-def test_adjoint_is_the_transpose_of_the_tangent(gpu_lib, kind):
+@pytest.mark.parametrize("kind,frozen", [(k, False) for k in AC.ALL_KINDS] +
+                         [("waf_flood", True), ("waf_superbee", True)])
+def test_adjoint_is_the_transpose_of_the_tangent(gpu_lib, kind, frozen):
     """<dJ/dU0, dU0> + <dJ/dn, dn> from the adjoint equals the tangent-linear derivative of J
     along (dU0, dn) (CPU, same branches): exact up to summation order, on every case,
     including those whose WAF limiter or wet/dry switches make central differences
@@ -125,12 +126,13 @@ def test_adjoint_is_the_transpose_of_the_tangent(gpu_lib, kind):
     dU[wet] = 0.01 * rng.uniform(-1.0, 1.0, (wet.sum(), 3))
     dn = c.manning * rng.uniform(-1.0, 1.0, c.nelt)
     with s, adj:
+        adj.set_linearization(frozen)
         s.set_manning(c.manning)
         s.set_state(c.U0)
         eta, UN = adj.forward()
         gU, gn = adj.backward(w_eta, w_state)
         dt, t = adj.dt_history()
-    eta_t, deta, UN_t, dUN = H.tangent(c, extra, c.U0, dU, c.manning, dn, dt, t, adj.gauges)
+    eta_t, deta, UN_t, dUN = H.tangent(c, extra, c.U0, dU, c.manning, dn, dt, t, adj.gauges, freeze_r=frozen)
     assert np.array_equal(eta_t, eta) and np.array_equal(UN_t, UN)
     terms = np.concatenate([(w_eta * deta).ravel(), (w_state * dUN).ravel()])
     tl = float(terms.sum())
