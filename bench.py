@@ -107,6 +107,8 @@ def build_case(name: str):
     from cuteflow_gb300 import cases
     if name == "flooding":
         return cases.flooding(1000, 500, seed=2, iflux=3), ALG_BYTES_WAF
+    if name == "flooding_muscl":
+        return cases.flooding(1000, 500, seed=2, iflux=4), ALG_BYTES_WAF
     if name == "dam_break":
         return cases.circular_dam_break(200, 200, seed=1, iflux=1), ALG_BYTES_HLLC
     raise SystemExit(f"unknown config {name}")
@@ -152,7 +154,7 @@ def run_reference(args):
             "warmup": args.warmup, "ms_per_step": 1e3 * r["loop_seconds"] / k, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "impl": "reference",
-            "config": {"workload": case.name, "triangles": case.nelt, "scheme": "WAF" if case.params["iflux"] == 3 else "HLLC"},
+            "config": {"workload": case.name, "triangles": case.nelt, "scheme": {1: "HLLC", 2: "HLLC-Ata", 3: "WAF", 4: "MUSCL-Hancock"}[case.params["iflux"]]},
             "cpu_baseline": {"value": rate, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
             "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -197,6 +199,72 @@ def ensemble(nmembers: int, steps: int, warmup: int, seed: int = 3):
             "batched_value": tri * steps / t_batch, "sequential_value": tri * steps / t_seq,
             "unit": UNIT, "speedup_vs_sequential": t_seq / t_batch,
             "batched_s": t_batch, "sequential_s": t_seq, "stopped_members": sum(1 for i in infos if i.status)}
+
+
+def adjoint_leg(steps: int, warmup: int, obs_every: float = 10.0):
+    """Adjoint Manning calibration: cost of one gradient against one forward.
+
+    Case: 500x200 quads (200,000 triangles) over the flooding bathymetry and boundaries,
+    first-order HLLC, true Manning field piecewise constant on 12 seeded Voronoi zones, 40
+    seeded gauges observed every 10 s of simulated time.  The gradient is taken at the
+    calibration's initial guess n = 0.035 with the objective sum (eta - eta_obs)^2 over the
+    observations; ~sqrt(N) checkpoints.  Timed with CUDA events on the solver's stream:
+      forward   : N plain steps (cf_step),
+      record    : the recording forward (cf_adjoint_forward: steps + gauges + checkpoints),
+      backward  : cf_adjoint_backward (segment replays + reverse steps).
+    ratio = (record + backward) / forward, the cost of a gradient in forward runs."""
+    import torch
+    from cuteflow_gb300 import Solver, cases
+    from cuteflow_gb300.adjoint import Adjoint, zone_gradient
+    c, zones, nz_true, gauges = cases.calibration()
+    n0 = np.full(c.nelt, 0.035)
+    s = Solver(c)
+    stream = torch.cuda.ExternalStream(s.stream())
+    adj = Adjoint(s, steps, gauges, 0)
+
+    def timed(fn):
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        out = fn()
+        b.record(stream)
+        torch.cuda.synchronize()
+        return out, a.elapsed_time(b)
+
+    # observations from the true field
+    s.set_manning(c.manning)
+    s.set_state(c.U0)
+    eta_obs, _ = adj.forward()
+    dt, t = adj.dt_history()
+    obs = cases.observation_steps(t, dt, obs_every)
+    # calibration guess: warm-up, then the timed legs
+    s.set_manning(n0)
+    s.set_state(c.U0)
+    s.step(warmup)
+    s.set_state(c.U0)
+    _, fwd_ms = timed(lambda: s.step(steps))
+    s.set_state(c.U0)
+    adj.forward()
+    s.set_state(c.U0)
+    (eta, _), rec_ms = timed(lambda: adj.forward())
+    w = np.zeros_like(eta)
+    w[obs] = 2.0 * (eta[obs] - eta_obs[obs])
+    misfit = float(np.sum((eta[obs] - eta_obs[obs]) ** 2))
+    adj.backward(w)
+    (gU, gn), bwd_ms = timed(lambda: adj.backward(w))
+    gz = zone_gradient(gn, zones, nz_true.size)
+    ok = bool(np.isfinite(gn).all() and np.isfinite(gU).all())
+    out = {"workload": c.name, "triangles": c.nelt, "scheme": "HLLC", "steps": steps,
+           "checkpoint_interval": adj.checkpoint_interval, "gauges": int(gauges.size),
+           "observations": int(obs.size), "device_bytes": adj.device_bytes,
+           "forward_ms": fwd_ms, "record_ms": rec_ms, "backward_ms": bwd_ms,
+           "ratio": (rec_ms + bwd_ms) / fwd_ms, "ratio_target": 5.0,
+           "forward_value": c.nelt * steps / (fwd_ms * 1e-3),
+           "gradient_value": c.nelt * steps / ((rec_ms + bwd_ms) * 1e-3), "unit": UNIT,
+           "misfit": misfit, "zone_gradient": [float(x) for x in gz], "finite": ok}
+    adj.close()
+    s.close()
+    return out
 
 
 def run_ours(args):
@@ -289,7 +357,7 @@ def run_ours(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded generator with the benchmark case's shapes and distributions)",
         "config": {"workload": case.name, "triangles": n, "edges": s.nedge,
-                   "scheme": "WAF" if case.params["iflux"] == 3 else "HLLC",
+                   "scheme": {1: "HLLC", 2: "HLLC-Ata", 3: "WAF", 4: "MUSCL-Hancock"}[case.params["iflux"]],
                    "l2": "working set > L2 (no flush needed)", "parallelism": f"replicas x{world}",
                    "time_steps_ran": info.steps},
         "roofline": {"bound": "hbm", "kernel": "one time step (k_edges + k_cells)",
@@ -308,6 +376,8 @@ def run_ours(args):
         line["batched"] = ensemble(args.batched_members, args.batched_steps, 3)
         line["batched"]["note"] = ("sample of the 256-member, 2000-step ensemble workload; run "
                                    "`bench.py --config ensemble` for the full size")
+    if rank == 0 and args.adjoint_steps > 0:
+        line["adjoint"] = adjoint_leg(args.adjoint_steps, 10)
     if rank == 0 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(case)
     s.close()
@@ -323,10 +393,12 @@ def main():
     ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="flooding", choices=["flooding", "dam_break", "ensemble"])
+    ap.add_argument("--config", default="flooding", choices=["flooding", "flooding_muscl", "dam_break", "ensemble"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--batched-members", type=int, default=32, help="ensemble sample beside the plain line (0: skip)")
     ap.add_argument("--batched-steps", type=int, default=200)
+    ap.add_argument("--adjoint-steps", type=int, default=3000,
+                    help="adjoint calibration leg beside the plain line (0: skip)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -354,7 +354,7 @@ int launch_adjoint_step(const AdjArgs& A, stream_t s) {
   const StepArgs& a = A.s;
   k_adj_cells<<<a.n_ctiles, TILE_C, 0, st>>>(A);
   switch (a.iflux) {
-    case 1: k_adj_edges<1, 3><<<a.n_etiles, TILE_E, 0, st>>>(A); break;
+    case 1: k_adj_edges<1, 6><<<a.n_etiles, TILE_E, 0, st>>>(A); break;
     case 2: k_adj_edges<2, 3><<<a.n_etiles, TILE_E, 0, st>>>(A); break;
     case 3: k_adj_edges<3, 2><<<a.n_etiles, TILE_E, 0, st>>>(A); break;
     default: return CF_ENOTSUP;

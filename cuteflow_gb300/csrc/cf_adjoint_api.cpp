@@ -88,6 +88,7 @@ int create_impl(cf_ctx* c, int32_t nsteps, int32_t interval, const int32_t* gaug
   if (!out) return fail(c, CF_EINVAL, "out is NULL");
   *out = nullptr;
   if (c->mem.size() != 1) return fail(c, CF_ENOTSUP, "the adjoint takes a context with one member");
+  if (c->iflux > 3) return fail(c, CF_ENOTSUP, "the adjoint covers iflux 1..3");
   if (nsteps < 1) return fail(c, CF_EINVAL, "nsteps < 1");
   if (ngauges < 0 || (ngauges > 0 && !gauges)) return fail(c, CF_EINVAL, "gauges NULL or ngauges < 0");
   const Member& M = c->mem[0];

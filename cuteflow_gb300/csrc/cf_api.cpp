@@ -137,7 +137,6 @@ int build_graph(cf_ctx* c) {
 
 int check_params(const cf_params* p, std::string& why) {
   if (p->iflux < 1 || p->iflux > 4) { why = "iflux must be 1..4"; return CF_EINVAL; }
-  if (p->iflux == 4) { why = "iflux 4 (MUSCL-Hancock) is not supported by the GPU step"; return CF_ENOTSUP; }
   if (p->inlet == 3) { why = "inlet 'phys_inflow' is not supported"; return CF_ENOTSUP; }
   if (p->inlet < 1 || p->inlet > 3 || p->outlet < 1 || p->outlet > 2) { why = "inlet must be 1..3 and outlet 1..2"; return CF_EINVAL; }
   if (p->ilimiteur < 0 || p->ilimiteur > 4) { why = "ilimiteur must be 0..4"; return CF_EINVAL; }

@@ -81,11 +81,15 @@ CFD_HD Dual<N> operator*(const Dual<N>& a, const Dual<N>& b) {
   for (int i = 0; i < N; ++i) r.d[i] = fma(a.d[i], b.v, a.v * b.d[i]);
   return r;
 }
+/* a / b: one reciprocal serves the value lane (Markstein's correction, the IEEE quotient) and
+ * the derivative lanes; a zero, infinite or subnormal b divides directly. */
 template <int N>
 CFD_HD Dual<N> operator/(const Dual<N>& a, const Dual<N>& b) {
   Dual<N> r;
-  r.v = a.v / b.v;
   const double y = 1.0 / b.v;
+  long long yb;
+  memcpy(&yb, &y, sizeof(yb));
+  r.v = ((yb << 1) != 0 && finite_bits(y)) ? div_rn(a.v, b.v, y) : a.v / b.v;
 #pragma unroll
   for (int i = 0; i < N; ++i) r.d[i] = fma(-r.v, b.d[i], a.d[i]) * y;
   return r;
@@ -121,7 +125,7 @@ CFD_HD Dual<N> operator*(double a, const Dual<N>& b) {
 template <int N>
 CFD_HD Dual<N> operator/(const Dual<N>& a, double b) {
   Dual<N> r;
-  r.v = a.v / b;
+  r.v = a.v / b;  /* mostly constants (/ 2, / 4), which the compiler folds */
   const double y = 1.0 / b;
 #pragma unroll
   for (int i = 0; i < N; ++i) r.d[i] = a.d[i] * y;

@@ -385,6 +385,102 @@ CF_HD CF_INLINE void waf_flux(double g, int ilim, double nx, double ny, double d
   }
 }
 
+/* ---- MUSCL-Hancock (IFLUX 4) ----------------------------------------------------------- */
+
+/* simple_limiter (flux_riemann.cuf:431-463) of an upwind slope r1 and a local slope r2:
+ * 0 none, 1 superbee (Fortran's three-argument max / min as two nested ones), 2 van Leer,
+ * 3 minmod.  Other ilimiteur values leave the reference's result unset; defined as 0. */
+template <class T>
+CF_HD CF_INLINE T simple_limiter(int ilim, T r1, T r2) {
+  if (ilim == 1) {
+    if (r2 > 0.) return dmax(T(0.), dmax(dmin(2. * r1, r2), dmin(r1, 2. * r2)));
+    return dmin(T(0.), dmin(dmax(2. * r1, r2), dmax(r1, 2. * r2)));
+  }
+  if (ilim == 2) return (r1 * r2 + fabs(r1 * r2)) / (r1 + r2 + EPS_VLEER);
+  if (ilim == 3) {
+    if (r2 > 0.) return dmax(T(0.), dmin(r1, r2));
+    return dmin(T(0.), dmax(r1, r2));
+  }
+  return T(0.);
+}
+
+/* Edge-frame MUSCL-Hancock flux of the side whose element is on the left
+ * (solver_Riemann_muscl, flux_riemann.cuf:526-718): limited slopes of the left state (upwind
+ * difference over d_up_l, local over d_mrl) and of the right state (local, upwind over
+ * d_up_r), face values, the half-step predictor, then HLLC with eps = 1e-16 (single
+ * precision).  Inputs are the hydrostatically reconstructed, masked states of both elements
+ * and the upwind reconstructions of both sides, all in this side's frame. */
+template <class T>
+CF_HD CF_INLINE void muscl_side(double g, double tolisec, int ilim, double dtoverdx, double d_mrl, double y_mrl,
+                                double d_up_l, double y_up_l, double d_up_r, double y_up_r, T hl, T ul, T vl, T hr,
+                                T ur, T vr, T hl_upw, T ul_upw, T vl_upw, T hr_upw, T ur_upw, T vr_upw, T& x1, T& x2,
+                                T& x3) {
+  const double eps = EPS_SECOND;
+  /* data reconstruction I (:560-609) */
+  const T dloc1 = div_rn(hr - hl, d_mrl, y_mrl);
+  const T dloc2 = div_rn(ur - ul, d_mrl, y_mrl);
+  const T dloc3 = div_rn(vr - vl, d_mrl, y_mrl);
+  const T dhl = simple_limiter(ilim, div_rn(hl - hl_upw, d_up_l, y_up_l), dloc1);
+  const T hll = dmax(T(0.), hl - 0.5 * dhl * d_mrl);
+  const T hlr = dmax(T(0.), hl + 0.5 * dhl * d_mrl);
+  T ull, vll, ulr, vlr;
+  if (hlr < tolisec || hll < tolisec) {
+    ulr = vlr = ull = vll = T(0.);
+  } else {
+    const T dul = simple_limiter(ilim, div_rn(ul - ul_upw, d_up_l, y_up_l), dloc2);
+    const T dvl = simple_limiter(ilim, div_rn(vl - vl_upw, d_up_l, y_up_l), dloc3);
+    ull = ul - 0.5 * dul * d_mrl;
+    vll = vl - 0.5 * dvl * d_mrl;
+    ulr = ul + 0.5 * dul * d_mrl;
+    vlr = vl + 0.5 * dvl * d_mrl;
+  }
+  const T dhr = simple_limiter(ilim, dloc1, div_rn(hr_upw - hr, d_up_r, y_up_r));
+  const T hrr = dmax(T(0.), hr + 0.5 * dhr * d_mrl);
+  const T hrl = dmax(T(0.), hr - 0.5 * dhr * d_mrl);
+  T url, vrl, urr, vrr;
+  if (hrl < tolisec || hrr < tolisec) {
+    url = vrl = urr = vrr = T(0.);
+  } else {
+    const T dur = simple_limiter(ilim, dloc2, div_rn(ur_upw - ur, d_up_r, y_up_r));
+    const T dvr = simple_limiter(ilim, dloc3, div_rn(vr_upw - vr, d_up_r, y_up_r));
+    urr = ur + 0.5 * dur * d_mrl;
+    vrr = vr + 0.5 * dvr * d_mrl;
+    url = ur - 0.5 * dur * d_mrl;
+    vrl = vr - 0.5 * dvr * d_mrl;
+  }
+  /* data reconstruction II (:615-621) */
+  const T h1 = hlr + 0.5 * dtoverdx * (hll * ull - hlr * ulr);
+  const T u1 = ulr + 0.5 * dtoverdx *
+                         (hll * (ull * ull) + 0.5 * g * (hll * hll) - (hlr * (ulr * ulr) + 0.5 * g * (hlr * hlr)));
+  const T v1 = vlr + 0.5 * dtoverdx * (hll * ull * vll - hlr * ulr * vlr);
+  const T h2 = hrl + 0.5 * dtoverdx * (hrl * url - hrr * urr);
+  const T u2 = url + 0.5 * dtoverdx *
+                         (hrl * (url * url) + 0.5 * g * (hrl * hrl) - (hrr * (urr * urr) + 0.5 * g * (hrr * hrr)));
+  const T v2 = vrl + 0.5 * dtoverdx * (hrl * url * vrl - hrr * urr * vrr);
+  /* HLLC (:623-714) */
+  T sl, sr, set;
+  if (!wave_speeds(g, eps, h1, u1, h2, u2, sl, sr, set)) {
+    x1 = x2 = x3 = T(0.);
+    return;
+  }
+  if (sl > 0.) {
+    x1 = h1 * u1;
+    x2 = h1 * (u1 * u1) + g * h1 * h1 / 2.0;
+    x3 = h1 * u1 * v1;
+  } else if (sr < 0.) {
+    x1 = h2 * u2;
+    x2 = h2 * (u2 * u2) + g * h2 * h2 / 2.0;
+    x3 = h2 * u2 * v2;
+  } else {
+    const T fl1 = h1 * u1, fl2 = h1 * (u1 * u1) + g * h1 * h1 / 2.0;
+    const T fr1 = h2 * u2, fr2 = h2 * (u2 * u2) + g * h2 * h2 / 2.0;
+    const T den = sr - sl + eps, yden = 1.0 / den;
+    x1 = div_rn(sr * fl1 - sl * fr1 + sl * sr * (h2 - h1), den, yden);
+    x2 = div_rn(sr * fl2 - sl * fr2 + sl * sr * (h2 * u2 - h1 * u1), den, yden);
+    x3 = (set > 0.) ? x1 * v1 : x1 * v2;
+  }
+}
+
 /* Discharge of an inlet at time t: debitglob, or a linear ramp from debitglob_start. */
 CF_HD CF_INLINE double inlet_discharge(const MemberDev& M, int id, double t) {
   const double q1 = M.debit_end[id - 1];
@@ -484,6 +580,30 @@ CF_HD CF_INLINE void upwind_state(const double4* U, int i1, int i2, double d1, d
   zu_ = div_rn(d1 * A1.w + d2 * A2.w, d1 + d2, ysum);
 }
 
+/* The MUSCL form: (h, u_n, u_t) of one side's upwind reconstruction and its bed elevation
+ * (flux_riemann.cuf:240-366 with the normal velocity as well). */
+CF_HD CF_INLINE void upwind_state3(const double4* U, int i1, int i2, double d1, double d2, double ysum, double nx,
+                                   double ny, double tolisec, double& hu_, double& uu_, double& vu_, double& zu_) {
+  const double4 A1 = ld4(U + i1);
+  double a, ua, va;
+  to_frame(A1.x, A1.y, A1.z, nx, ny, tolisec, a, ua, va);
+  if (d1 < 0.0) {
+    hu_ = a;
+    uu_ = ua;
+    vu_ = va;
+    zu_ = A1.w;
+    return;
+  }
+  const double4 A2 = ld4(U + i2);
+  double b, ub, vb;
+  to_frame(A2.x, A2.y, A2.z, nx, ny, tolisec, b, ub, vb);
+  const double ds = d1 + d2;
+  hu_ = div_rn(d1 * a + d2 * b, ds, ysum);
+  uu_ = div_rn(d1 * ua + d2 * ub, ds, ysum);
+  vu_ = div_rn(d1 * va + d2 * vb, ds, ysum);
+  zu_ = div_rn(d1 * A1.w + d2 * A2.w, ds, ysum);
+}
+
 /* ---- one edge ------------------------------------------------------------------------- */
 
 /* Static data of an interior edge beyond its normal: length, centroid distance and, for the
@@ -566,6 +686,71 @@ CF_HD CF_INLINE void interior_edge(const MemberDev& M, int ilim, int flux_mode, 
   out[9] = -(tb * ny);
 }
 
+/* interior_edge for MUSCL-Hancock (IFLUX 4): the reference evaluates the edge from each of its
+ * elements in that element's frame.  Side B's frame normal is -n, so its inputs are A's
+ * frame values with the elements swapped and the velocities negated, which is what B's own
+ * masking and upwind averaging produce; each side's limited reconstruction is evaluated in
+ * full (its slopes are not mirror images of the other side's).  upA / upB: (h, u_n, u_t) of
+ * the upwind reconstructions of sides A and B in A's frame, zl_upw / zr_upw their beds. */
+CF_HD CF_INLINE void interior_edge_muscl(const MemberDev& M, int ilim, int flux_mode, const EdgeGeo& G, double dt,
+                                         double hA, double huA, double hvA, double zml, double hB, double huB,
+                                         double hvB, double zmr, const double upA[3], double zl_upw,
+                                         const double upB[3], double zr_upw, double out[10]) {
+  const double g = M.gp, tolisec = M.tolisec;
+  const double nx = G.nx, ny = G.ny, len = G.len;
+  const double zij = dmax(zml, zmr);
+  double hautl, vitul, vitvl, hautr, vitur, vitvr;
+  to_frame(hA, huA, hvA, nx, ny, tolisec, hautl, vitul, vitvl);
+  to_frame(hB, huB, hvB, nx, ny, tolisec, hautr, vitur, vitvr);
+  /* hydrostatic reconstruction of the four states (:370-400) */
+  double hijet = dmax(0.0, hautl + zml - zij);
+  double hlu = dmax(0.0, upA[0] + zl_upw - zij);
+  double hjiet = dmax(0.0, hautr + zmr - zij);
+  double hru = dmax(0.0, upB[0] + zr_upw - zij);
+  double ul = vitul, vl = vitvl, ur = vitur, vr = vitvr;
+  double ulu = upA[1], vlu = upA[2], uru = upB[1], vru = upB[2];
+  if (hijet < tolisec) { hijet = 0.; ul = 0.; vl = 0.; }
+  if (hlu < tolisec) { hlu = 0.; ulu = 0.; vlu = 0.; }
+  if (hjiet < tolisec) { hjiet = 0.; ur = 0.; vr = 0.; }
+  if (hru < tolisec) { hru = 0.; uru = 0.; vru = 0.; }
+  const double dtoverdx = div_rn(dt, G.d_mrl, G.y_mrl);
+  TwoFlux F;
+  double x1, x2, x3;
+  muscl_side(g, tolisec, ilim, dtoverdx, G.d_mrl, G.y_mrl, G.d_mkvol, G.y_mkvol, G.d_mkvoisin, G.y_mkvoisin, hijet,
+             ul, vl, hjiet, ur, vr, hlu, ulu, vlu, hru, uru, vru, x1, x2, x3);
+  F.a1 = x1;
+  F.a2 = nx * x2 - ny * x3;
+  F.a3 = ny * x2 + nx * x3;
+  if (flux_mode == 1) {
+    F.b1 = -F.a1;
+    F.b2 = -F.a2;
+    F.b3 = -F.a3;
+  } else {
+    double y1, y2, y3;
+    muscl_side(g, tolisec, ilim, dtoverdx, G.d_mrl, G.y_mrl, G.d_mkvoisin, G.y_mkvoisin, G.d_mkvol, G.y_mkvol,
+               hjiet, -ur, -vr, hijet, -ul, -vl, hru, -uru, -vru, hlu, -ulu, -vlu, y1, y2, y3);
+    const double mx = -nx, my = -ny;
+    F.b1 = y1;
+    F.b2 = mx * y2 - my * y3;
+    F.b3 = my * y2 + mx * y3;
+  }
+  /* bed-slope source of both sides from the raw depths (source_terms.cuf:90-97) */
+  const double ha = dmax(0.0, hA + zml - zij);
+  const double hb = dmax(0.0, hB + zmr - zij);
+  const double ta = g / 2.0 * (ha * ha - hA * hA) * len;
+  const double tb = g / 2.0 * (hb * hb - hB * hB) * len;
+  out[0] = F.a1 * len;
+  out[1] = F.a2 * len;
+  out[2] = F.a3 * len;
+  out[3] = ta * nx;
+  out[4] = ta * ny;
+  out[5] = F.b1 * len;
+  out[6] = F.b2 * len;
+  out[7] = F.b3 * len;
+  out[8] = -(tb * nx);
+  out[9] = -(tb * ny);
+}
+
 /* Static data of edge e in the form interior_edge takes. */
 CF_HD CF_INLINE EdgeGeo edge_geo(const StepArgs& a, int e, bool second) {
   const double4 geo = ld4(a.egeo + e);
@@ -587,6 +772,23 @@ CF_HD CF_INLINE EdgeGeo edge_geo(const StepArgs& a, int e, bool second) {
     G.ysum_b = yi.z;
   }
   return G;
+}
+
+/* The two slots of an interior edge from interior_edge's out[10]. */
+CF_HD CF_INLINE void write_slots(Slot* sa, const double o[10]) {
+  Slot* sb = sa + 1;
+  sa->f1 = o[0];
+  sa->f2 = o[1];
+  sa->f3 = o[2];
+  sa->bx = o[3];
+  sa->by = o[4];
+  sa->q = 0.0;
+  sb->f1 = o[5];
+  sb->f2 = o[6];
+  sb->f3 = o[7];
+  sb->bx = o[8];
+  sb->by = o[9];
+  sb->q = 0.0;
 }
 
 /* Fluxes (times the edge length) and bed sources of edge e into its two slots, from the
@@ -613,29 +815,28 @@ CF_HD CF_INLINE void edge_body(const StepArgs& a, const MemberDev& M, int e, dou
 
   const EdgeGeo G = edge_geo(a, e, IFLUX >= 3);
   const double4 UB = ld4(a.Uin + ab.y);
+  double o[10];
+  if (IFLUX == 4) {
+    const int4 up = ldro(a.eupw + e);
+    const double4 dw = ld4(a.ewts + e);
+    double upA[3], upB[3], zl_upw, zr_upw;
+    upwind_state3(a.Uin, up.x, up.y, dw.x, dw.y, G.ysum_a, G.nx, G.ny, M.tolisec, upA[0], upA[1], upA[2], zl_upw);
+    upwind_state3(a.Uin, up.z, up.w, dw.z, dw.w, G.ysum_b, G.nx, G.ny, M.tolisec, upB[0], upB[1], upB[2], zr_upw);
+    interior_edge_muscl(M, a.ilimiteur, a.flux_mode, G, dt, UA.x, UA.y, UA.z, UA.w, UB.x, UB.y, UB.z, UB.w, upA,
+                        zl_upw, upB, zr_upw, o);
+    write_slots(sa, o);
+    return;
+  }
   double hl_upw = 0.0, vl_upw = 0.0, zl_upw = 0.0, hr_upw = 0.0, vr_upw = 0.0, zr_upw = 0.0;
-  if (IFLUX >= 3) {
+  if (IFLUX == 3) {
     const int4 up = ldro(a.eupw + e);
     const double4 dw = ld4(a.ewts + e);   /* d1, d2 of side A, d1, d2 of side B */
     upwind_state(a.Uin, up.x, up.y, dw.x, dw.y, G.ysum_a, G.nx, G.ny, M.tolisec, hl_upw, vl_upw, zl_upw);
     upwind_state(a.Uin, up.z, up.w, dw.z, dw.w, G.ysum_b, G.nx, G.ny, M.tolisec, hr_upw, vr_upw, zr_upw);
   }
-  double o[10];
-  interior_edge<IFLUX>(M, a.ilimiteur, a.flux_mode, G, dt, UA.x, UA.y, UA.z, UA.w, UB.x, UB.y, UB.z, UB.w, hl_upw,
-                       vl_upw, zl_upw, hr_upw, vr_upw, zr_upw, o);
-  Slot* sb = sa + 1;
-  sa->f1 = o[0];
-  sa->f2 = o[1];
-  sa->f3 = o[2];
-  sa->bx = o[3];
-  sa->by = o[4];
-  sa->q = 0.0;
-  sb->f1 = o[5];
-  sb->f2 = o[6];
-  sb->f3 = o[7];
-  sb->bx = o[8];
-  sb->by = o[9];
-  sb->q = 0.0;
+  interior_edge<(IFLUX == 4 ? 3 : IFLUX)>(M, a.ilimiteur, a.flux_mode, G, dt, UA.x, UA.y, UA.z, UA.w, UB.x, UB.y,
+                                          UB.z, UB.w, hl_upw, vl_upw, zl_upw, hr_upw, vr_upw, zr_upw, o);
+  write_slots(sa, o);
 }
 
 /* ---- one element ------------------------------------------------------------------------ */

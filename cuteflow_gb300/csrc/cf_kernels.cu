@@ -194,6 +194,7 @@ int launch_step(const StepArgs& a, stream_t s, void* ev_mid, void* ev_end) {
     case 1: k_edges<1><<<a.n_etiles, TILE_E, 0, st>>>(a); break;
     case 2: k_edges<2><<<a.n_etiles, TILE_E, 0, st>>>(a); break;
     case 3: k_edges<3><<<a.n_etiles, TILE_E, 0, st>>>(a); break;
+    case 4: k_edges<4><<<a.n_etiles, TILE_E, 0, st>>>(a); break;
     default: return CF_ENOTSUP;
   }
   if (ev_mid) cudaEventRecord(reinterpret_cast<cudaEvent_t>(ev_mid), st);

@@ -47,7 +47,8 @@ extern "C" int harness_edge_fluxes(const cf_mesh* m, const cf_params* p, const d
   for (int e = 0; e < ne; ++e) {
     if (p->iflux == 1) edge_body<1>(a, M, e, dt, t);
     else if (p->iflux == 2) edge_body<2>(a, M, e, dt, t);
-    else edge_body<3>(a, M, e, dt, t);
+    else if (p->iflux == 3) edge_body<3>(a, M, e, dt, t);
+      else edge_body<4>(a, M, e, dt, t);
   }
   for (int c = 0; c < n; ++c) {
     int o = P.perm[c];
@@ -110,7 +111,8 @@ extern "C" int harness_run(const cf_mesh* m, const cf_params* p, const double* U
     for (int e = 0; e < ne; ++e) {
       if (p->iflux == 1) edge_body<1>(a, M, e, dt, t);
       else if (p->iflux == 2) edge_body<2>(a, M, e, dt, t);
-      else edge_body<3>(a, M, e, dt, t);
+      else if (p->iflux == 3) edge_body<3>(a, M, e, dt, t);
+      else edge_body<4>(a, M, e, dt, t);
     }
     double next = M.dt_reset;
     for (int c = 0; c < n; ++c) {

@@ -20,7 +20,7 @@ def _state_after(oracle, case, n, params=None):
     return r["U"], r["dt_hist"][-1], r["t"]
 
 
-@pytest.mark.parametrize("iflux", [1, 2, 3])
+@pytest.mark.parametrize("iflux", [1, 2, 3, 4])
 @pytest.mark.parametrize("flux_mode", [0, 1])
 def test_edge_fluxes_bitwise(oracle, iflux, flux_mode):
     c = cases.flooding(60, 30, seed=4, iflux=iflux)
@@ -50,6 +50,15 @@ CASES = [
     ("waf_lim2", lambda: cases.flooding(40, 20, seed=6, iflux=3), 150, dict(ilimiteur=2)),
     ("waf_lim3", lambda: cases.flooding(40, 20, seed=6, iflux=3), 150, dict(ilimiteur=3)),
     ("waf_lim4", lambda: cases.flooding(40, 20, seed=6, iflux=3), 150, dict(ilimiteur=4)),
+    ("dam_muscl", lambda: cases.circular_dam_break(30, 30, seed=3, iflux=4), 150, {}),
+    ("flood_muscl", lambda: cases.flooding(60, 30, seed=4, iflux=4), 200, {}),
+    ("muscl_lim0", lambda: cases.flooding(40, 20, seed=6, iflux=4), 150, dict(ilimiteur=0)),
+    ("muscl_lim2", lambda: cases.flooding(40, 20, seed=6, iflux=4), 150, dict(ilimiteur=2)),
+    ("muscl_lim3", lambda: cases.flooding(40, 20, seed=6, iflux=4), 150, dict(ilimiteur=3)),
+    ("muscl_lim4_unset", lambda: cases.flooding(40, 20, seed=6, iflux=4), 100, dict(ilimiteur=4)),
+    ("muscl_conservative", lambda: cases.flooding(40, 20, seed=7, iflux=4), 150, dict(flux_mode=1)),
+    ("muscl_outlet_transm", lambda: cases.flooding(40, 20, seed=9, iflux=4), 120, dict(outlet=2)),
+    ("lake_muscl", lambda: cases.lake_at_rest(30, 15, iflux=4), 100, {}),
     ("fric_explicit", lambda: cases.flooding(40, 20, seed=8, iflux=1), 120, dict(fricimplic=0)),
     ("fric_diag", lambda: cases.flooding(40, 20, seed=8, iflux=1), 120, dict(fricimplic=2)),
     ("no_friction", lambda: cases.flooding(40, 20, seed=8, iflux=3), 120, dict(friction=0)),

@@ -42,12 +42,12 @@ def compare_bitwise(case, nsteps, oracle, params=None, chunks=(None,)):
     return U, ref, info
 
 
-@pytest.mark.parametrize("iflux", [1, 2, 3])
+@pytest.mark.parametrize("iflux", [1, 2, 3, 4])
 def test_dam_break(gpu_lib, oracle, iflux):
     compare_bitwise(cases.circular_dam_break(40, 40, seed=3, iflux=iflux), 200, oracle)
 
 
-@pytest.mark.parametrize("iflux", [1, 2, 3])
+@pytest.mark.parametrize("iflux", [1, 2, 3, 4])
 def test_flooding_wet_dry(gpu_lib, oracle, iflux):
     compare_bitwise(cases.flooding(80, 40, seed=4, iflux=iflux), 300, oracle, chunks=(7, 100, 1, 50))
 
@@ -57,7 +57,14 @@ def test_waf_limiters(gpu_lib, oracle, ilim):
     compare_bitwise(cases.flooding(60, 30, seed=6, iflux=3), 200, oracle, params=dict(ilimiteur=ilim))
 
 
-@pytest.mark.parametrize("iflux", [1, 3])
+@pytest.mark.parametrize("ilim", [0, 1, 2, 3, 4])
+def test_muscl_limiters(gpu_lib, oracle, ilim):
+    """MUSCL-Hancock (iflux 4) with every simple_limiter; ilimiteur 4 leaves the reference's
+    slope unset, defined as no slope on both sides."""
+    compare_bitwise(cases.flooding(60, 30, seed=6, iflux=4), 200, oracle, params=dict(ilimiteur=ilim))
+
+
+@pytest.mark.parametrize("iflux", [1, 3, 4])
 def test_conservative_mode(gpu_lib, oracle, iflux):
     compare_bitwise(cases.flooding(60, 30, seed=7, iflux=iflux), 200, oracle, params=dict(flux_mode=1))
 
@@ -65,8 +72,9 @@ def test_conservative_mode(gpu_lib, oracle, iflux):
 @pytest.mark.parametrize("prm", [dict(fricimplic=2), dict(friction=0), dict(inlet=1, outlet=2),
                                  dict(outlet=2), dict(is_dt_constant=1, constant_dt=0.05)],
                          ids=["fric_diag", "no_friction", "transm_in_out", "transm_out", "constant_dt"])
-def test_options(gpu_lib, oracle, prm):
-    compare_bitwise(cases.flooding(50, 25, seed=8, iflux=3), 150, oracle, params=prm)
+@pytest.mark.parametrize("iflux", [3, 4])
+def test_options(gpu_lib, oracle, prm, iflux):
+    compare_bitwise(cases.flooding(50, 25, seed=8, iflux=iflux), 150, oracle, params=prm)
 
 
 def test_explicit_friction_stops_like_the_reference(gpu_lib, oracle):
@@ -87,8 +95,9 @@ def test_explicit_friction_stops_like_the_reference(gpu_lib, oracle):
     assert info.t == ref["t"]
 
 
-def test_lake_at_rest(gpu_lib, oracle):
-    c = cases.lake_at_rest(40, 20, iflux=3)
+@pytest.mark.parametrize("iflux", [3, 4])
+def test_lake_at_rest(gpu_lib, oracle, iflux):
+    c = cases.lake_at_rest(40, 20, iflux=iflux)
     U, ref, info = compare_bitwise(c, 200, oracle)
     zm = oracle.setup(c)[2]
     eta0 = c.U0[:, 0] + zm
