@@ -18,6 +18,7 @@ CF_ENOTSUP = -7
 
 CF_STATUS_DT_RANGE = 1
 CF_STATUS_NONFINITE = 2
+CF_STATUS_STEADY = 4
 
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int32)
@@ -46,7 +47,8 @@ class CfParams(C.Structure):
         ("iflux", C.c_int32), ("ilimiteur", C.c_int32), ("friction", C.c_int32),
         ("fricimplic", C.c_int32), ("is_override_manning", C.c_int32),
         ("is_dt_constant", C.c_int32), ("inlet", C.c_int32), ("outlet", C.c_int32),
-        ("flux_mode", C.c_int32), ("reorder", C.c_int32),
+        ("flux_mode", C.c_int32), ("reorder", C.c_int32), ("pad_", C.c_int32),
+        ("tol_reg_perm", C.c_double), ("steady_count", C.c_int32), ("pad2_", C.c_int32),
     ]
 
 
@@ -86,6 +88,8 @@ def default_params() -> CfParams:
     p.outlet = 1
     p.flux_mode = 0
     p.reorder = 1
+    p.tol_reg_perm = 0.0
+    p.steady_count = 1000
     return p
 
 

@@ -205,6 +205,29 @@ def flooding(nx: int = 1000, ny: int = 500, seed: int = 2, lx: float = 2000.0, l
                 nombre_sorties=1, params=params, U0=U0, name=f"flooding_{nx}x{ny}", nx=nx, ny=ny)
 
 
+def channel(nx: int = 60, ny: int = 12, seed: int = 6, lx: float = 600.0, ly: float = 120.0, iflux: int = 1,
+            q: float = 1.0, slope: float = 0.001, out_level: float = 1.0, manning: float = 0.03,
+            inlet: int = 2, tolisec: float = 1e-4) -> Case:
+    """A sloping rectangular channel that settles towards a steady flow: bed z = slope * (lx - x),
+    inflow of q m^2/s over the left edge (inlet 2 'inflow' or 3 'phys_inflow'), fixed level
+    out_level at the right edge, walls top and bottom, uniform Manning n, still water at level
+    out_level at t = 0 (dry where the bed is above it)."""
+    x, y, tri = grid_mesh(nx, ny, lx, ly, seed)
+    z = slope * (lx - x)
+    zc = cell_bed(x, y, z, tri)
+    h = out_level - zc
+    U0 = np.zeros((tri.shape[0], 3))
+    U0[:, 0] = np.where(h > tolisec, h, 0.0)
+    left, right, bottom, top = side_nodes(nx, ny)
+    walls = np.unique(np.concatenate([bottom, top])).astype(np.int32)
+    params = dict(iflux=iflux, ilimiteur=1, tolisec=tolisec, cfl=0.9, friction=1, fricimplic=1,
+                  is_override_manning=0, inlet=inlet, outlet=1, debitglob=[q * ly], h_sortie=[out_level])
+    return Case(x=x, y=y, z=z, tri=tri, manning=np.full(tri.shape[0], manning), ndinput=left,
+                numero_ndinput=np.ones_like(left), ndoutput=right, numero_ndoutput=np.ones_like(right),
+                ndwall=walls, nombre_entrees=1, nombre_sorties=1, params=params, U0=U0,
+                name=f"channel_{nx}x{ny}", nx=nx, ny=ny)
+
+
 def lake_at_rest(nx: int = 40, ny: int = 20, seed: int = 5, depth: float = 0.5, iflux: int = 3,
                  wet: bool = True) -> Case:
     """Still water over the flooding bathymetry with walls only (well-balancedness).

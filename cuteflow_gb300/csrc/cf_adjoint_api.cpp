@@ -89,6 +89,7 @@ int create_impl(cf_ctx* c, int32_t nsteps, int32_t interval, const int32_t* gaug
   *out = nullptr;
   if (c->mem.size() != 1) return fail(c, CF_ENOTSUP, "the adjoint takes a context with one member");
   if (c->iflux > 3) return fail(c, CF_ENOTSUP, "the adjoint covers iflux 1..3");
+  if (c->any_phys_inflow) return fail(c, CF_ENOTSUP, "the adjoint does not cover inlet 3 (phys_inflow)");
   if (nsteps < 1) return fail(c, CF_EINVAL, "nsteps < 1");
   if (ngauges < 0 || (ngauges > 0 && !gauges)) return fail(c, CF_EINVAL, "gauges NULL or ngauges < 0");
   const Member& M = c->mem[0];
@@ -197,6 +198,7 @@ int forward_impl(cf_adjoint* a, int32_t replay, double* eta_out, double* state_o
     StepArgs sa = step_args(c, p);
     sa.Uin = X;
     sa.Uout = Y;
+    sa.steady = 0;   /* the adjoint's run has N steps: no steady-state stop */
     if (!replay) {
       sa.mst = a->mst;
       if ((rc = launch_step(sa, st, nullptr, nullptr))) return fail(c, rc, "step launch failed");

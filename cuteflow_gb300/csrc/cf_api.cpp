@@ -68,6 +68,11 @@ StepArgs step_args(const cf_ctx* c, int parity) {
   a.iflux = c->iflux;
   a.ilimiteur = c->ilimiteur;
   a.flux_mode = c->flux_mode;
+  a.inl_cell = c->inl_cell;
+  a.inl_len = c->inl_len;
+  a.nmembers = (int32_t)c->mem.size();
+  a.phys_inflow = c->any_phys_inflow ? 1 : 0;
+  a.steady = c->any_steady ? 1 : 0;
   return a;
 }
 
@@ -75,7 +80,7 @@ void free_all(cf_ctx* c) {
   if (c->graph2) cudaGraphExecDestroy(c->graph2);
   void* ptrs[] = {c->U[0], c->U[1], c->cslot, c->cstat, c->zcell, c->perm, c->iperm, c->ecell, c->egeo,
                   c->ebid, c->eupw, c->ewts, c->edk, c->einv, c->slots, c->etile_mem, c->ctile_mem, c->mdev,
-                  c->mst, c->staging};
+                  c->mst, c->staging, c->inl_cell, c->inl_len};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (c->host_state) cudaFreeHost(c->host_state);
@@ -137,13 +142,13 @@ int build_graph(cf_ctx* c) {
 
 int check_params(const cf_params* p, std::string& why) {
   if (p->iflux < 1 || p->iflux > 4) { why = "iflux must be 1..4"; return CF_EINVAL; }
-  if (p->inlet == 3) { why = "inlet 'phys_inflow' is not supported"; return CF_ENOTSUP; }
   if (p->inlet < 1 || p->inlet > 3 || p->outlet < 1 || p->outlet > 2) { why = "inlet must be 1..3 and outlet 1..2"; return CF_EINVAL; }
   if (p->ilimiteur < 0 || p->ilimiteur > 4) { why = "ilimiteur must be 0..4"; return CF_EINVAL; }
   if (p->flux_mode < 0 || p->flux_mode > 1) { why = "flux_mode must be 0 or 1"; return CF_EINVAL; }
   if (p->fricimplic < 0 || p->fricimplic > 2) { why = "fricimplic must be 0..2"; return CF_EINVAL; }
   if (!(p->gp > 0.0) || !(p->cfl > 0.0) || !(p->tolisec >= 0.0)) { why = "gp and cfl must be positive, tolisec non-negative"; return CF_EINVAL; }
   if (p->ramp_time < 0.0) { why = "ramp_time must be non-negative"; return CF_EINVAL; }
+  if (!(p->tol_reg_perm >= 0.0)) { why = "tol_reg_perm must be non-negative"; return CF_EINVAL; }
   return CF_OK;
 }
 
@@ -174,6 +179,11 @@ MemberDev member_dev(const Member& M) {
   D.edge_end = M.edge_off + M.ne;
   D.bedge_begin = M.edge_off + M.prep.n_interior;
   D.bedge_end = M.edge_off + M.ne;
+  D.inl_begin = M.inl_off;
+  D.inl_count = (int32_t)M.prep.inl_cell.size();
+  D.nin = M.prep.nin;
+  D.tol_reg_perm = p->tol_reg_perm;
+  D.steady_count = p->steady_count > 0 ? p->steady_count : 1000;
   return D;
 }
 
@@ -229,8 +239,12 @@ int create_impl(const cf_mesh* meshes, const cf_params* params, int32_t nm, cf_c
     return CF_OK;
   };
   /* layout of the flat space */
-  int64_t noff = 0, eoff = 0;
+  int64_t noff = 0, eoff = 0, ioff = 0;
   for (auto& M : c->mem) {
+    M.inl_off = (int32_t)ioff;
+    ioff += (int64_t)M.prep.inl_cell.size();
+    c->any_phys_inflow |= M.params.inlet == 3;
+    c->any_steady |= M.params.tol_reg_perm > 0.0;
     M.n = M.prep.nelt;
     M.ne = (int32_t)M.prep.edges.size();
     M.cell_off = (int32_t)noff;
@@ -266,6 +280,12 @@ int create_impl(const cf_mesh* meshes, const cf_params* params, int32_t nm, cf_c
       (rc = dalloc(c, &c->ctile_mem, c->n_ctiles)) || (rc = dalloc(c, &c->mdev, (size_t)nm)) ||
       (rc = dalloc(c, &c->mst, (size_t)nm)) || (rc = dalloc(c, &c->staging, 3 * (size_t)c->max_n)))
     return done(rc);
+  c->n_inl = ioff;
+  if (c->any_phys_inflow) {
+    size_t nl = 0;
+    for (auto& M : c->mem) nl += M.prep.inl_len.size();
+    if ((rc = dalloc(c, &c->inl_cell, (size_t)ioff)) || (rc = dalloc(c, &c->inl_len, nl))) return done(rc);
+  }
   if (second && ((rc = dalloc(c, &c->eupw, c->ne_pad)) || (rc = dalloc(c, &c->ewts, c->ne_pad)) ||
                  (rc = dalloc(c, &c->edk, c->ne_pad)) || (rc = dalloc(c, &c->einv, c->ne_pad))))
     return done(rc);
@@ -297,6 +317,17 @@ int create_impl(const cf_mesh* meshes, const cf_params* params, int32_t nm, cf_c
       std::vector<double4>().swap(P.ewts);
       std::vector<double4>().swap(P.edk);
       std::vector<double4>().swap(P.einv);
+    }
+    if (!P.inl_cell.empty()) {
+      /* entry lengths are stored per member with that member's inlet count */
+      std::vector<int32_t> cells(P.inl_cell);
+      for (auto& x : cells) x += co;
+      size_t loff = 0;
+      for (int j = 0; j < i; ++j) loff += c->mem[j].prep.inl_len.size();
+      M.dev.inl_len_off = (int32_t)loff;
+      if ((rc = put(c, c->inl_cell + M.inl_off, cells.data(), cells.size())) ||
+          (rc = put(c, c->inl_len + loff, P.inl_len.data(), P.inl_len.size())))
+        return done(rc);
     }
     mdev[i] = M.dev;
     /* the device copies are authoritative; keep the reference-order tables and the permutation */
@@ -532,6 +563,8 @@ int cf_default_params(cf_params* p) {
   p->outlet = 1;
   p->flux_mode = 0;
   p->reorder = 1;
+  p->tol_reg_perm = 0.0;
+  p->steady_count = 1000;
   return CF_OK;
 }
 

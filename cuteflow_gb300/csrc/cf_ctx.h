@@ -22,6 +22,7 @@ struct Member {
   int32_t n = 0, ne = 0;
   int32_t cell_off = 0, edge_off = 0;
   int32_t ctile_begin = 0, ctile_end = 0;
+  int32_t inl_off = 0;      /* first phys_inflow entry of the member */
   MemberDev dev{};
 };
 
@@ -53,6 +54,11 @@ struct cf_ctx {
   cf::MemberDev* mdev = nullptr;
   cf::MemberState* mst = nullptr;
   double* staging = nullptr;           /* 3 * max_n doubles, reference order */
+  int32_t* inl_cell = nullptr;         /* phys_inflow entries of all members */
+  double* inl_len = nullptr;
+  int64_t n_inl = 0;
+  bool any_phys_inflow = false;        /* some member has inlet 3 */
+  bool any_steady = false;             /* some member tests for steady state */
   cf::MemberState* host_state = nullptr;   /* pinned, one record per member */
   /* stepping */
   int64_t launched = 0;                /* steps launched since creation (buffer parity) */

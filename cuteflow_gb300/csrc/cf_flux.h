@@ -491,10 +491,11 @@ CF_HD CF_INLINE double inlet_discharge(const MemberDev& M, int id, double t) {
   return q1;
 }
 
-/* Boundary-edge flux of side A (flux_riemann.cuf:114-171). */
+/* Boundary-edge flux of side A (flux_riemann.cuf:114-171).  surf: for phys_inflow (inlet 3),
+ * calcul_surf_entree's sum of length * depth over the edge's inlet at the step's start. */
 template <class T>
 CF_HD CF_INLINE void boundary_flux(int iflux, const MemberDev& M, int kind, int id, double t, double nx, double ny,
-                                   T h, T hu, T hv, double z, T& f1, T& f2, T& f3, T& q) {
+                                   T h, T hu, T hv, double z, T& f1, T& f2, T& f3, T& q, double surf = 0.0) {
   const double g = M.gp, tolisec = M.tolisec;
   T hautl, vitul, vitvl;
   to_frame(h, hu, hv, nx, ny, tolisec, hautl, vitul, vitvl);
@@ -511,6 +512,14 @@ CF_HD CF_INLINE void boundary_flux(int iflux, const MemberDev& M, int kind, int 
       f2 = nx * ((debitnorm * debitnorm) / (hautl + tolisec) + g * (hautl * hautl) / 2.);
       f3 = ny * ((debitnorm * debitnorm) / (hautl + tolisec) + g * (hautl * hautl) / 2.);
       q = T(-debitnorm);
+    } else if (M.inlet == 3) {
+      /* the inlet's discharge shared in proportion to depth (:127-138); the threshold is the
+       * single-precision literal 1e-8 */
+      const T debitnorm = (surf > (double)1e-8f) ? -(inlet_discharge(M, id, t) * hautl / surf) : T(0.0);
+      f1 = debitnorm;
+      f2 = nx * ((debitnorm * debitnorm) / (hautl + tolisec) + g * (hautl * hautl) / 2.);
+      f3 = ny * ((debitnorm * debitnorm) / (hautl + tolisec) + g * (hautl * hautl) / 2.);
+      q = -debitnorm;
     }
   } else if (kind == -3) {
     f2 = nx * g * (hautl * hautl) / 2.;
@@ -794,7 +803,8 @@ CF_HD CF_INLINE void write_slots(Slot* sa, const double o[10]) {
 /* Fluxes (times the edge length) and bed sources of edge e into its two slots, from the
  * state U of step n: the body of the edge kernel. */
 template <int IFLUX>
-CF_HD CF_INLINE void edge_body(const StepArgs& a, const MemberDev& M, int e, double dt, double t) {
+CF_HD CF_INLINE void edge_body(const StepArgs& a, const MemberDev& M, int e, double dt, double t,
+                               const double* surf = nullptr) {
   const int2 ab = ldro(a.ecell + e);
   const double4 UA = ld4(a.Uin + ab.x);
   Slot* sa = a.slots + 2 * (size_t)e;
@@ -802,8 +812,10 @@ CF_HD CF_INLINE void edge_body(const StepArgs& a, const MemberDev& M, int e, dou
   if (ab.y < 0) {
     const double4 geo = ld4(a.egeo + e);
     const double len = geo.z;
+    const int id = ldro(a.ebid + e);
+    const double sf = (surf && ab.y == -1 && M.inlet == 3 && id >= 1 && id <= M.nin) ? surf[id - 1] : 0.0;
     double f1, f2, f3, q;
-    boundary_flux(IFLUX, M, ab.y, ldro(a.ebid + e), t, geo.x, geo.y, UA.x, UA.y, UA.z, UA.w, f1, f2, f3, q);
+    boundary_flux(IFLUX, M, ab.y, id, t, geo.x, geo.y, UA.x, UA.y, UA.z, UA.w, f1, f2, f3, q, sf);
     sa->f1 = f1 * len;
     sa->f2 = f2 * len;
     sa->f3 = f3 * len;

@@ -15,6 +15,9 @@
  *          einv  : double4 {RN(1/d_AB), RN(1/(d1+d2)) of A, of B, -}          (second order only)
  *   slots  Slot  : 48 bytes per (edge, side): flux*len of that side's own evaluation and
  *                  the bed-slope source of that side.  Slot 2e is side A, 2e+1 side B.
+ *   inlet  inl_cell, inl_len : phys_inflow only, the entries of the reference's list of inflow
+ *                  elements (one per (element, inflow edge), reference order) with, per inlet
+ *                  number, the length the entry contributes to calcul_surf_entree.
  * Several independent simulations ("members") can share one flat cell/edge space; each
  * member owns whole tiles of TILE_C cells and TILE_E edges so every tile belongs to one
  * member and the per-member dt minimum is a tile reduction plus one atomic.
@@ -60,6 +63,12 @@ struct MemberDev {
   int32_t cell_begin, cell_end;   /* real elements [begin, end) of the flat space */
   int32_t edge_begin, edge_end;   /* real edges */
   int32_t bedge_begin, bedge_end; /* boundary edges (a sub-range of the edges) */
+  int32_t inl_begin, inl_count;   /* phys_inflow entries [begin, begin + count) */
+  int32_t inl_len_off;            /* first entry length: inl_len[inl_len_off + entry * nin + id - 1] */
+  int32_t nin;                    /* inlets (nombre_entrees) of the entry table */
+  int32_t steady_count;           /* steady-state stop after more than this many qualifying steps */
+  int32_t pad2_;
+  double tol_reg_perm;            /* steady-state tolerance; 0: no test */
 };
 
 /* Per-member mutable device state.  dt[p] and t[p] belong to the step with parity p; the
@@ -71,6 +80,9 @@ struct MemberState {
   long long nstep;   /* steps completed since the state was set */
   uint32_t status;   /* CF_STATUS_* bits; a member with a non-zero status does not step */
   int32_t base;      /* buffer parity at which the state was set: the state is in U[(base + nstep) & 1] */
+  int32_t steady_iter;  /* consecutive steps that met the steady-state test */
+  int32_t pad_;
+  double surf[CF_MAX_IO];  /* phys_inflow: sum of length * depth over each inlet, at the step's start */
 };
 
 /* status bit of a member whose state has not been set yet */
@@ -94,9 +106,14 @@ struct StepArgs {
   const int32_t* ctile_mem;
   const MemberDev* mdev;
   MemberState* mst;
+  const int32_t* inl_cell;   /* phys_inflow entry tables (NULL without phys_inflow) */
+  const double* inl_len;
   int32_t n_etiles, n_ctiles;
   int32_t parity;
   int32_t iflux, ilimiteur, flux_mode;
+  int32_t nmembers;
+  int32_t phys_inflow;       /* some member uses inlet 3: k_surf runs before the edges */
+  int32_t steady;            /* some member tests for steady state: k_steady runs after the cells */
 };
 
 /* ---- host preprocessing (cf_mesh.cpp) ---------------------------------------------- */
@@ -130,6 +147,13 @@ struct Prep {
   std::vector<double4> ewts;
   std::vector<double4> edk;
   std::vector<double4> einv;
+  /* phys_inflow: one entry per (element, inflow edge) in reference order (compute_input_elems,
+   * maillage.cuf:1333-1363): its element (new order) and, per inlet number 1..nin, the length
+   * of the element's last inflow edge of that number (0 if none), as calcul_surf_entree
+   * (maillage.cuf:1368-1421) weighs the element's depth */
+  std::vector<int32_t> inl_cell;
+  std::vector<double> inl_len;    /* [entries * nin] */
+  int32_t nin = 0;
 };
 
 /* Build every host table from the reference mesh inputs.  Returns CF_OK or CF_EINVAL with a
@@ -145,6 +169,8 @@ int launch_cfl(const double4* U, const double4* cstat, const int32_t* ctile_mem,
                int32_t n_tiles, const MemberDev* mdev, MemberState* mst, int32_t slot, stream_t s);
 int launch_discharge(const Slot* slots, const int2* ecell, const MemberDev* mdev, MemberState* mst,
                      int32_t nmembers, stream_t s);
+/* phys_inflow inlet sums of the state U into mst[m].surf (every member with inlet 3) */
+int launch_surf(const StepArgs& a, const double4* U, stream_t s);
 /* hu3 (reference order, one member) <-> U (new order); perm/iperm/zcell/U point at the member's
  * first element, the permutations hold member-local indices. */
 int launch_scatter_state(const double* hu3, const int32_t* perm_new2old, const double* zcell,

@@ -58,7 +58,34 @@ __global__ void __launch_bounds__(TILE_E) k_edges(StepArgs a) {
     }
   }
   if (e >= M.edge_end) return;
-  edge_body<IFLUX>(a, M, e, dt, t);
+  edge_body<IFLUX>(a, M, e, dt, t, S->surf);
+}
+
+/* phys_inflow: per member (one warp) and inlet, calcul_surf_entree (maillage.cuf:1368-1421)
+ * on the state at the step's start: the entries' length * depth in blocks of 32 in list
+ * order, each block summed by the reference's tree (s(t) += s(t + i), i = 16 .. 1), the
+ * block sums added in block order (the reference adds them with atomicAdd, in whatever order
+ * the blocks finish; entries past the end of the list count 0, where the reference reads
+ * beyond its list). */
+__global__ void __launch_bounds__(32) k_surf(StepArgs a) {
+  const int m = blockIdx.x;
+  const MemberDev& M = a.mdev[m];
+  MemberState* S = a.mst + m;
+  if (M.inlet != 3 || S->status) return;
+  const int lane = threadIdx.x;
+  for (int id = 0; id < M.nin; ++id) {
+    double total = 0.0;
+    for (int b = 0; b < M.inl_count; b += 32) {
+      const int j = b + lane;
+      double v = 0.0;
+      if (j < M.inl_count)
+        v = a.inl_len[M.inl_len_off + (size_t)j * M.nin + id] * a.Uin[a.inl_cell[M.inl_begin + j]].x;
+      #pragma unroll
+      for (int i = 16; i > 0; i >>= 1) v = v + __shfl_down_sync(0xffffffffu, v, i);
+      total = total + v;   /* lane 0 holds the block's tree sum */
+    }
+    if (lane == 0) S->surf[id] = total;
+  }
 }
 
 /* ---- the element kernel ----------------------------------------------------------------- */
@@ -139,9 +166,13 @@ __global__ void __launch_bounds__(TILE_C) k_cfl(const double4* U, const double4*
 
 /* Discharge diagnostics of the last step (debit_entree_sum, debit_sortie,
  * finite_volumes_method.cuf:197-214): per member, fixed-order sums over its boundary edges
- * (deterministic: each thread sums a fixed stride, then a fixed tree). */
+ * (deterministic: each thread sums a fixed stride, then a fixed tree).  With steady set (the
+ * launch at the end of every step of a context that tests for steady state) it also applies
+ * check_steady_state (finite_volumes_method.cuf:370-393) to the members that stepped:
+ * Q_in > 1e-8 (single precision) and |Q_in - Q_out| / Q_in < tol_reg_perm counts a step, any
+ * other step resets the count, and more than steady_count stops the member. */
 __global__ void __launch_bounds__(256) k_discharge(const Slot* slots, const int2* ecell, const MemberDev* mdev,
-                                                    MemberState* mst) {
+                                                    MemberState* mst, int steady) {
   __shared__ double si[256], so[256];
   const int m = blockIdx.x;
   const MemberDev& M = mdev[m];
@@ -163,8 +194,18 @@ __global__ void __launch_bounds__(256) k_discharge(const Slot* slots, const int2
     __syncthreads();
   }
   if (threadIdx.x == 0) {
-    mst[m].q_in = si[0];
-    mst[m].q_out = so[0];
+    MemberState* S = mst + m;
+    S->q_in = si[0];
+    S->q_out = so[0];
+    if (steady && M.tol_reg_perm > 0.0 && S->status == 0) {
+      const double qi = si[0], qo = so[0];
+      if (qi > (double)1e-8f && fabs(qi - qo) / qi < M.tol_reg_perm) {
+        S->steady_iter += 1;
+        if (S->steady_iter > M.steady_count) S->status |= CF_STATUS_STEADY;
+      } else {
+        S->steady_iter = 0;
+      }
+    }
   }
 }
 
@@ -190,6 +231,7 @@ int check(cudaError_t e) { return e == cudaSuccess ? CF_OK : CF_ECUDA; }
 
 int launch_step(const StepArgs& a, stream_t s, void* ev_mid, void* ev_end) {
   cudaStream_t st = reinterpret_cast<cudaStream_t>(s);
+  if (a.phys_inflow) k_surf<<<a.nmembers, 32, 0, st>>>(a);
   switch (a.iflux) {
     case 1: k_edges<1><<<a.n_etiles, TILE_E, 0, st>>>(a); break;
     case 2: k_edges<2><<<a.n_etiles, TILE_E, 0, st>>>(a); break;
@@ -199,6 +241,7 @@ int launch_step(const StepArgs& a, stream_t s, void* ev_mid, void* ev_end) {
   }
   if (ev_mid) cudaEventRecord(reinterpret_cast<cudaEvent_t>(ev_mid), st);
   k_cells<<<a.n_ctiles, TILE_C, 0, st>>>(a);
+  if (a.steady) k_discharge<<<a.nmembers, 256, 0, st>>>(a.slots, a.ecell, a.mdev, a.mst, 1);
   if (ev_end) cudaEventRecord(reinterpret_cast<cudaEvent_t>(ev_end), st);
   return check(cudaGetLastError());
 }
@@ -212,7 +255,7 @@ int launch_cfl(const double4* U, const double4* cstat, const int32_t* ctile_mem,
 
 int launch_discharge(const Slot* slots, const int2* ecell, const MemberDev* mdev, MemberState* mst, int32_t nmembers,
                      stream_t s) {
-  k_discharge<<<nmembers, 256, 0, reinterpret_cast<cudaStream_t>(s)>>>(slots, ecell, mdev, mst);
+  k_discharge<<<nmembers, 256, 0, reinterpret_cast<cudaStream_t>(s)>>>(slots, ecell, mdev, mst, 0);
   return check(cudaGetLastError());
 }
 

@@ -204,6 +204,31 @@ int prepare_mesh(const cf_mesh* m, const cf_params* p, Prep& P, std::string& err
   }
   for (int i = 0; i < n; ++i) P.iperm[P.perm[i]] = i;
 
+  /* -- phys_inflow entry list (compute_input_elems, maillage.cuf:1333-1363): one entry per
+   * (element, inflow edge) in reference order; calcul_surf_entree (:1368-1421) gives each
+   * entry, for inlet number id, length * depth of the element's last inflow edge of that
+   * number (the same value for every entry of an element) ------------------------------- */
+  P.inl_cell.clear();
+  P.inl_len.clear();
+  P.nin = 0;
+  if (p->inlet == 3) {
+    P.nin = std::max(0, std::min<int32_t>(m->nombre_entrees, CF_MAX_IO));
+    for (int e = 0; e < n; ++e)
+      for (int k = 0; k < 3; ++k) {
+        if (P.bnd[(e * 3 + k) * 2] != -1) continue;
+        P.inl_cell.push_back(P.iperm[e]);
+        for (int id = 1; id <= P.nin; ++id) {
+          double len = 0.0;
+          for (int kf = 0; kf < 3; ++kf)
+            if (P.bnd[(e * 3 + kf) * 2] == -1 && P.bnd[(e * 3 + kf) * 2 + 1] == id) {
+              int a = nd(m, e, kf), b = nd(m, e, (kf + 1) % 3);
+              len = std::sqrt((m->x[a] - m->x[b]) * (m->x[a] - m->x[b]) + (m->y[a] - m->y[b]) * (m->y[a] - m->y[b]));
+            }
+          P.inl_len.push_back(len);
+        }
+      }
+  }
+
   /* -- edges: interior edges at their first element in the new order, then boundary ------- */
   P.edges.clear();
   P.edges.reserve((size_t)n * 3 / 2 + 16);

@@ -43,6 +43,8 @@ extern "C" {
 /* Device status bits reported in cf_step_info.status */
 #define CF_STATUS_DT_RANGE 1u
 #define CF_STATUS_NONFINITE 2u
+#define CF_STATUS_STEADY 4u      /* steady state reached (check_steady_state,
+                                    finite_volumes_method.cuf:370-393): the member stops, no error */
 
 /* Mesh tables, as lec_mail_tri reads them (maillage.cuf:196-313). */
 typedef struct cf_mesh {
@@ -84,13 +86,23 @@ typedef struct cf_params {
   int32_t fricimplic;              /* 0 explicit, 1 (I - dt/2 J)^-1, 2 diagonal (fricimplic) */
   int32_t is_override_manning;     /* (is_override_manning) */
   int32_t is_dt_constant;          /* (is_dt_constant) */
-  int32_t inlet;                   /* 1 'transm', 2 'inflow', 3 'phys_inflow' (data_transfer.cuf:43-55) */
+  int32_t inlet;                   /* 1 'transm', 2 'inflow', 3 'phys_inflow' (data_transfer.cuf:43-55):
+                                      3 spreads debitglob over the inlet in proportion to the
+                                      depth of its elements (flux_riemann.cuf:127-138,
+                                      calcul_surf_entree maillage.cuf:1368-1421) */
   int32_t outlet;                  /* 1 'fixedheight', 2 'transm' (data_transfer.cuf:57-66) */
   int32_t flux_mode;               /* extension: 0 (default) = the reference's semantics, the flux of
                                       every (element, edge) as that element evaluates it
                                       (flux_riemann.cuf:33-426); 1 = conservative, one evaluation
                                       per edge with the opposite sign for the neighbour */
   int32_t reorder;                 /* extension: 1 = space-filling-curve renumbering (default) */
+  int32_t pad_;
+  double tol_reg_perm;             /* steady-state stop (tol_reg_perm): after a step whose inflow
+                                      Q_in > 1e-8 and |Q_in - Q_out| / Q_in < tol_reg_perm for
+                                      more than steady_count consecutive steps the member stops
+                                      with CF_STATUS_STEADY; 0 (default) disables the test */
+  int32_t steady_count;            /* 1000 in the reference (finite_volumes_method.cuf:380) */
+  int32_t pad2_;
 } cf_params;
 
 /* set_initial_condition inputs (initial_condition.cuf:4-80, namelist global_data.cuf:40-44). */

@@ -480,6 +480,7 @@ struct Ctx {
   const orc_params* prm;
   P p;
   double t;  /* time at the start of the step (inflow ramp) */
+  double surf[ORC_MAX_IO];  /* phys_inflow: calcul_surf_entree of the step's start state */
 };
 
 inline double inlet_discharge(const orc_params* prm, int id, double t) {
@@ -540,8 +541,16 @@ void cell_edge_flux(const Ctx& C, const double* U0, int gi, int tj, double flux[
       flux[1] = n1 * ((debitnorm * debitnorm) / (hautl + tolisec) + gp * (hautl * hautl) / 2.);
       flux[2] = n2 * ((debitnorm * debitnorm) / (hautl + tolisec) + gp * (hautl * hautl) / 2.);
       qin += (-debitnorm) * ln;
+    } else if (prm->inlet == 3) {
+      /* phys_inflow, flux_riemann.cuf:127-138: the discharge shared in proportion to depth;
+       * 1e-8 is a single-precision literal */
+      double surf = (id >= 1 && id <= ORC_MAX_IO) ? C.surf[id - 1] : 0.0;
+      double debitnorm = (surf > (double)1e-8f) ? -(inlet_discharge(prm, id, C.t) * hautl / surf) : 0.;
+      flux[0] = debitnorm;
+      flux[1] = n1 * ((debitnorm * debitnorm) / (hautl + tolisec) + gp * (hautl * hautl) / 2.);
+      flux[2] = n2 * ((debitnorm * debitnorm) / (hautl + tolisec) + gp * (hautl * hautl) / 2.);
+      qin += (-debitnorm) * ln;
     }
-    /* inlet 3 (phys_inflow) needs the calcul_surf_entree reduction; not restated here. */
   }
   if (kvoisin == -3) {
     flux[0] = 0.;
@@ -655,6 +664,46 @@ void cell_edge_flux(const Ctx& C, const double* U0, int gi, int tj, double flux[
               ur_upw, vr_upw, d_mrl, d_mkvol, d_mkvoisin, flux);
       }
     }
+  }
+}
+
+/* calcul_surf_entree, maillage.cuf:1368-1421, on state U: the list of compute_input_elems
+ * (:1333-1363) holds an element once per inflow edge, in element order; for inlet id each
+ * list entry contributes the element's depth times the length of its last inflow edge of
+ * that id (the loop over its edges overwrites s(ti)), 0 when it has none.  Entries are
+ * summed in blocks of 32 threads by the tree s(t) = s(t) + s(t+i), i = 16, 8, .., 1, and the
+ * block sums added with atomicAdd.  Defined here: blocks are added in block order (the
+ * reference's order is whatever order its blocks finish in), and the threads of the last
+ * block beyond the list, which read past its end in the reference (the bound tested is
+ * nelt, not the list length), contribute 0. */
+void surf_entree(const Setup& S, const orc_mesh* m, const double* U, double* surf) {
+  std::vector<int> list;
+  for (int gi = 0; gi < S.nelt; ++gi)
+    for (int j = 0; j < 3; ++j)
+      if (Bc(S, gi, j, 0) == -1) list.push_back(gi);
+  const int nin = std::max(0, std::min(m->nombre_entrees, ORC_MAX_IO));
+  for (int id = 1; id <= ORC_MAX_IO; ++id) surf[id - 1] = 0.0;
+  for (int id = 1; id <= nin; ++id) {
+    double acc = 0.0;
+    for (size_t b0 = 0; b0 < list.size(); b0 += 32) {
+      double s[32];
+      for (int ti = 0; ti < 32; ++ti) {
+        s[ti] = 0.0;
+        if (b0 + ti >= list.size()) continue;
+        const int kvol = list[b0 + ti];
+        for (int kfac = 0; kfac < 3; ++kfac) {
+          if (Bc(S, kvol, kfac, 0) == -1 && Bc(S, kvol, kfac, 1) == id) {
+            const int n1 = node(S, kvol, kfac), n2 = node(S, kvol, (kfac + 1) % 3);
+            s[ti] = std::sqrt((S.x[n1] - S.x[n2]) * (S.x[n1] - S.x[n2]) + (S.y[n1] - S.y[n2]) * (S.y[n1] - S.y[n2])) *
+                    U[3 * kvol];
+          }
+        }
+      }
+      for (int i = 16; i >= 1; i /= 2)
+        for (int ti = 0; ti < i; ++ti) s[ti] = s[ti] + s[ti + i];
+      acc = acc + s[0];
+    }
+    surf[id - 1] = acc;
   }
 }
 
@@ -779,6 +828,7 @@ int orc_edge_flux(const orc_mesh* m, const orc_params* prm, const double* U, dou
   C.p.gp = prm->gp; C.p.tolisec = prm->tolisec; C.p.cfl = prm->cfl; C.p.tol = prm->tol;
   C.p.iflux = prm->iflux; C.p.ilimiteur = prm->ilimiteur; C.p.dt = dt;
   C.t = t;
+  surf_entree(S, m, U, C.surf);
   double f[3], ln, qi = 0., qo = 0.;
   cell_edge_flux(C, U, gi, tj, f, ln, qi, qo);
   for (int c = 0; c < 3; ++c) fl_out[c] = f[c] * ln;
@@ -795,6 +845,7 @@ int orc_all_edge_fluxes(const orc_mesh* m, const orc_params* prm, const double* 
   C.p.gp = prm->gp; C.p.tolisec = prm->tolisec; C.p.cfl = prm->cfl; C.p.tol = prm->tol;
   C.p.iflux = prm->iflux; C.p.ilimiteur = prm->ilimiteur; C.p.dt = dt;
   C.t = t;
+  surf_entree(S, m, U, C.surf);
   for (int gi = 0; gi < m->nelt; ++gi)
     for (int tj = 0; tj < 3; ++tj) {
       double f[3], ln, qi = 0., qo = 0.;
@@ -860,7 +911,7 @@ int orc_initial_condition(const orc_mesh* m, const orc_params* p, const orc_ic* 
 /* The time loop of solve_finite_volumes, finite_volumes_method.cuf:113-242, for nsteps. */
 int orc_run(const orc_mesh* m, const orc_params* prm, const double* U0in, double t0, int32_t nsteps,
             double* U_out, double* dt_hist, const double* dt_replay, double* t_out, double* q_out,
-            int32_t nthreads, double* loop_seconds) {
+            int32_t nthreads, double* loop_seconds, int32_t* steps_out) {
 #ifdef _OPENMP
   int saved = omp_get_max_threads();
   if (nthreads > 0) omp_set_num_threads(nthreads);
@@ -887,23 +938,43 @@ int orc_run(const orc_mesh* m, const orc_params* prm, const double* U0in, double
   double dt = cfl_dt(S, prm, U0);
   if (dt_hist) dt_hist[0] = dt;
   double t = t0, qin = 0., qout = 0.;
-  int rc = 0;
+  int rc = 0, done = 0, steady_iter = 0;
+  /* boundary (cell, edge) pairs in reference order: their discharges are summed in this
+   * order after every step (finite_volumes_method.cuf:197-214), so that the sums do not
+   * depend on the thread count */
+  std::vector<int> bpos(3 * (size_t)n, -1);
+  int nb = 0;
+  for (int gi = 0; gi < n; ++gi)
+    for (int tj = 0; tj < 3; ++tj)
+      if (Bc(S, gi, tj, 0) < 0) bpos[gi * 3 + tj] = nb++;
+  std::vector<double> bq_in((size_t)nb, 0.0), bq_out((size_t)nb, 0.0);
+  for (int i = 0; i < ORC_MAX_IO; ++i) C.surf[i] = 0.0;
   const auto wall0 = std::chrono::steady_clock::now();
   for (int step = 0; step < nsteps; ++step) {
     C.p.dt = dt_replay ? dt_replay[step] : dt;
     C.t = t;
-    qin = 0.; qout = 0.;
+    if (prm->inlet == 3) surf_entree(S, m, U0, C.surf);
     /* compute_flux: per (cell, edge); in the once-per-edge mode the cell with the larger
      * index takes the negated flux of its neighbour instead of evaluating it. */
-#pragma omp parallel for schedule(static) reduction(+ : qin, qout)
+#pragma omp parallel for schedule(static)
     for (int gi = 0; gi < n; ++gi)
       for (int tj = 0; tj < 3; ++tj) {
         int kv = Bc(S, gi, tj, 0);
         if (!two_sided && kv > 0 && kv - 1 < gi) continue;
-        double f[3], ln;
-        cell_edge_flux(C, U0, gi, tj, f, ln, qin, qout);
+        double f[3], ln, qi = 0., qo = 0.;
+        cell_edge_flux(C, U0, gi, tj, f, ln, qi, qo);
         for (int c = 0; c < 3; ++c) fl[(gi * 3 + tj) * 3 + c] = f[c] * ln;
+        if (kv < 0) {
+          bq_in[bpos[gi * 3 + tj]] = qi;
+          bq_out[bpos[gi * 3 + tj]] = qo;
+        }
       }
+    qin = 0.;
+    qout = 0.;
+    for (int i = 0; i < nb; ++i) {
+      qin += bq_in[i];
+      qout += bq_out[i];
+    }
     if (!two_sided) {
 #pragma omp parallel for schedule(static)
       for (int gi = 0; gi < n; ++gi)
@@ -927,8 +998,19 @@ int orc_run(const orc_mesh* m, const orc_params* prm, const double* U0in, double
     if (dt_hist) dt_hist[step + 1] = dt;
     t = t + C.p.dt;
     std::swap(U0, U);
+    ++done;
+    /* check_steady_state, finite_volumes_method.cuf:370-393 (1e-8 single precision) */
+    if (prm->tol_reg_perm > 0.0) {
+      const int count = prm->steady_count > 0 ? prm->steady_count : 1000;
+      if (qin > (double)1e-8f && std::fabs(qin - qout) / qin < prm->tol_reg_perm) {
+        if (++steady_iter > count) { rc = 1; break; }
+      } else {
+        steady_iter = 0;
+      }
+    }
     if (!dt_replay && (dt > 9999 || dt < DT_LOW)) { rc = -2; break; }
   }
+  if (steps_out) *steps_out = done;
   if (loop_seconds)
     *loop_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - wall0).count();
   std::memcpy(U_out, U0, 3 * (size_t)n * sizeof(double));

@@ -59,6 +59,10 @@ typedef struct orc_params {
   int32_t outlet;                  /* 1 fixedheight, 2 transm */
   int32_t flux_mode;               /* 0: per (cell, edge) like the reference; 1: once per edge */
   int32_t reorder;                 /* ignored by the oracle */
+  int32_t pad_;
+  double tol_reg_perm;             /* steady-state stop; 0 disables */
+  int32_t steady_count;            /* consecutive qualifying steps before the stop (1000) */
+  int32_t pad2_;
 } orc_params;
 
 typedef struct orc_ic {
@@ -87,10 +91,12 @@ int orc_initial_condition(const orc_mesh* m, const orc_params* p, const orc_ic* 
  *   q_out    : 2 or NULL; inflow and outflow discharge of the last step
  *   nthreads : OpenMP threads (<=0: library default)
  *   loop_seconds: NULL or the wall time of the time loop alone (setup excluded)
- * Returns 0, or a negative code: -1 bad input, -2 dt out of the reference's sane range. */
+ *   steps_out: NULL or the number of steps taken
+ * Returns 0, 1 when the steady-state test stopped the run (tol_reg_perm > 0), or a negative
+ * code: -1 bad input, -2 dt out of the reference's sane range. */
 int orc_run(const orc_mesh* m, const orc_params* p, const double* U0, double t0, int32_t nsteps,
             double* U_out, double* dt_hist, const double* dt_replay, double* t_out, double* q_out,
-            int32_t nthreads, double* loop_seconds);
+            int32_t nthreads, double* loop_seconds, int32_t* steps_out);
 
 /* flux*len of edge tj (0..2) of element gi (0-based) for state U (3 doubles out). */
 int orc_edge_flux(const orc_mesh* m, const orc_params* p, const double* U, double dt, double t,

@@ -52,7 +52,7 @@ def lib():
         L.orc_run.argtypes = [C.POINTER(_abi.CfMesh), C.POINTER(_abi.CfParams), C.POINTER(C.c_double),
                               C.c_double, C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_double),
                               C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_double),
-                              C.c_int32, C.POINTER(C.c_double)]
+                              C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_int32)]
         L.orc_run.restype = C.c_int
         L.orc_max_threads.restype = C.c_int
         L.orc_all_edge_fluxes.argtypes = [C.POINTER(_abi.CfMesh), C.POINTER(_abi.CfParams),
@@ -107,12 +107,14 @@ def run(case, nsteps: int, params: dict | None = None, U0: np.ndarray | None = N
         dt_replay = np.ascontiguousarray(dt_replay, dtype=np.float64)
         rp = _abi.dptr(dt_replay)
     loop = C.c_double(0.0)
+    steps = C.c_int32(0)
     rc = lib().orc_run(C.byref(ma.mesh), C.byref(p), _abi.dptr(U0), float(t0), int(nsteps),
                        _abi.dptr(U), _abi.dptr(dt_hist), rp, C.byref(t), _abi.dptr(q), int(nthreads),
-                       C.byref(loop))
-    if check and rc not in (0,):
+                       C.byref(loop), C.byref(steps))
+    if check and rc not in (0, 1):
         raise RuntimeError(f"orc_run failed ({rc})")
-    return dict(U=U, dt_hist=dt_hist, t=t.value, q_in=q[0], q_out=q[1], rc=rc, loop_seconds=loop.value)
+    return dict(U=U, dt_hist=dt_hist, t=t.value, q_in=q[0], q_out=q[1], rc=rc, loop_seconds=loop.value,
+                steps=steps.value)
 
 
 def edge_fluxes(case, U: np.ndarray, dt: float, t: float = 0.0, params: dict | None = None) -> np.ndarray:

@@ -10,6 +10,60 @@
 
 using namespace cf;
 
+/* The member constants of a one-member context, as cf_api.cpp builds them. */
+static void fill_member(MemberDev& M, const cf_params* p, const Prep& P) {
+  std::memset(&M, 0, sizeof(M));
+  M.gp = p->gp; M.tolisec = p->tolisec; M.tol = p->tol; M.constant_dt = p->constant_dt;
+  M.ramp_time = p->ramp_time; M.dt_reset = (P.nelt % 1024 != 0) ? 100000.0 : 1000000.0;
+  for (int i = 0; i < CF_MAX_IO; ++i) {
+    M.debit_end[i] = p->debitglob[i]; M.debit_start[i] = p->debitglob_start[i];
+    M.long_entree[i] = P.long_entree[i]; M.h_sortie[i] = p->h_sortie[i];
+  }
+  M.inlet = p->inlet; M.outlet = p->outlet; M.friction = p->friction; M.fricimplic = p->fricimplic;
+  M.is_dt_constant = p->is_dt_constant;
+  M.inl_begin = 0;
+  M.inl_count = (int32_t)P.inl_cell.size();
+  M.inl_len_off = 0;
+  M.nin = P.nin;
+  M.tol_reg_perm = p->tol_reg_perm;
+  M.steady_count = p->steady_count > 0 ? p->steady_count : 1000;
+}
+
+/* k_surf on the CPU: per inlet, blocks of 32 entries summed by the tree s[t] += s[t + i]
+ * (i = 16 .. 1), block sums added in order. */
+static void surf_sums(const Prep& P, const MemberDev& M, const double4* U, double* surf) {
+  for (int id = 0; id < M.nin; ++id) {
+    double total = 0.0;
+    for (int b = 0; b < M.inl_count; b += 32) {
+      double s[32];
+      for (int l = 0; l < 32; ++l) {
+        const int j = b + l;
+        s[l] = j < M.inl_count ? P.inl_len[(size_t)j * M.nin + id] * U[P.inl_cell[j]].x : 0.0;
+      }
+      for (int i = 16; i > 0; i >>= 1)
+        for (int l = 0; l < i; ++l) s[l] = s[l] + s[l + i];
+      total = total + s[0];
+    }
+    surf[id] = total;
+  }
+}
+
+/* k_discharge on the CPU: 256 strided partial sums over the boundary edges, then a tree. */
+static void discharge(const Prep& P, const std::vector<Slot>& slots, double& qin, double& qout) {
+  double si[256] = {0}, so[256] = {0};
+  const int ne = (int)P.edges.size();
+  for (int t = 0; t < 256; ++t)
+    for (int e = P.n_interior + t; e < ne; e += 256) {
+      const int kind = P.ecell[e].y;
+      if (kind == -1) si[t] += slots[2 * (size_t)e].q;
+      else if (kind == -2) so[t] += slots[2 * (size_t)e].q;
+    }
+  for (int w = 128; w > 0; w >>= 1)
+    for (int t = 0; t < w; ++t) { si[t] += si[t + w]; so[t] += so[t + w]; }
+  qin = si[0];
+  qout = so[0];
+}
+
 extern "C" int harness_edge_fluxes(const cf_mesh* m, const cf_params* p, const double* U, double dt, double t,
                                    double* out /* [nelt][3][3] flux*len, reference order */,
                                    double* bed /* [nelt][3][2] bed source per (element, edge), or NULL */) {
@@ -24,14 +78,7 @@ extern "C" int harness_edge_fluxes(const cf_mesh* m, const cf_params* p, const d
     Un[c] = make_double4(U[3 * o], U[3 * o + 1], U[3 * o + 2], P.zcell[c]);
   }
   MemberDev M;
-  std::memset(&M, 0, sizeof(M));
-  M.gp = p->gp; M.tolisec = p->tolisec; M.tol = p->tol; M.constant_dt = p->constant_dt;
-  M.ramp_time = p->ramp_time;
-  for (int i = 0; i < CF_MAX_IO; ++i) {
-    M.debit_end[i] = p->debitglob[i]; M.debit_start[i] = p->debitglob_start[i];
-    M.long_entree[i] = P.long_entree[i]; M.h_sortie[i] = p->h_sortie[i];
-  }
-  M.inlet = p->inlet; M.outlet = p->outlet; M.friction = p->friction; M.fricimplic = p->fricimplic;
+  fill_member(M, p, P);
   const int ne = (int)P.edges.size();
   std::vector<Slot> slots(2 * (size_t)ne);
   StepArgs a;
@@ -44,11 +91,13 @@ extern "C" int harness_edge_fluxes(const cf_mesh* m, const cf_params* p, const d
   a.einv = P.einv.empty() ? nullptr : P.einv.data();
   a.slots = slots.data();
   a.iflux = p->iflux; a.ilimiteur = p->ilimiteur; a.flux_mode = p->flux_mode;
+  double surf[CF_MAX_IO] = {0};
+  surf_sums(P, M, Un.data(), surf);
   for (int e = 0; e < ne; ++e) {
-    if (p->iflux == 1) edge_body<1>(a, M, e, dt, t);
-    else if (p->iflux == 2) edge_body<2>(a, M, e, dt, t);
-    else if (p->iflux == 3) edge_body<3>(a, M, e, dt, t);
-      else edge_body<4>(a, M, e, dt, t);
+    if (p->iflux == 1) edge_body<1>(a, M, e, dt, t, surf);
+    else if (p->iflux == 2) edge_body<2>(a, M, e, dt, t, surf);
+    else if (p->iflux == 3) edge_body<3>(a, M, e, dt, t, surf);
+    else edge_body<4>(a, M, e, dt, t, surf);
   }
   for (int c = 0; c < n; ++c) {
     int o = P.perm[c];
@@ -67,7 +116,8 @@ extern "C" int harness_edge_fluxes(const cf_mesh* m, const cf_params* p, const d
 /* The whole GPU step algorithm on the CPU: edge pass, element pass, device dt rule, for
  * nsteps steps from U (reference order); U_out and dt_hist (nsteps+1) like the oracle. */
 extern "C" int harness_run(const cf_mesh* m, const cf_params* p, const double* U, int nsteps, double* U_out,
-                           double* dt_hist, double* t_out) {
+                           double* dt_hist, double* t_out, int* steps_out) {
+  int done = 0, steady_iter = 0;
   Prep P;
   std::string err;
   int rc = prepare_mesh(m, p, P, err);
@@ -79,15 +129,7 @@ extern "C" int harness_run(const cf_mesh* m, const cf_params* p, const double* U
     Ua[c] = make_double4(U[3 * o], U[3 * o + 1], U[3 * o + 2], P.zcell[c]);
   }
   MemberDev M;
-  std::memset(&M, 0, sizeof(M));
-  M.gp = p->gp; M.tolisec = p->tolisec; M.tol = p->tol; M.constant_dt = p->constant_dt;
-  M.ramp_time = p->ramp_time; M.dt_reset = (n % 1024 != 0) ? 100000.0 : 1000000.0;
-  for (int i = 0; i < CF_MAX_IO; ++i) {
-    M.debit_end[i] = p->debitglob[i]; M.debit_start[i] = p->debitglob_start[i];
-    M.long_entree[i] = P.long_entree[i]; M.h_sortie[i] = p->h_sortie[i];
-  }
-  M.inlet = p->inlet; M.outlet = p->outlet; M.friction = p->friction; M.fricimplic = p->fricimplic;
-  M.is_dt_constant = p->is_dt_constant;
+  fill_member(M, p, P);
   const int ne = (int)P.edges.size();
   std::vector<Slot> slots(2 * (size_t)ne);
   StepArgs a;
@@ -108,11 +150,13 @@ extern "C" int harness_run(const cf_mesh* m, const cf_params* p, const double* U
   for (int s = 0; s < nsteps; ++s) {
     if (s > 0 && (dt > 9999.0 || dt < DT_LOW)) { rc = -2; break; }
     a.Uin = cur;
+    double surf[CF_MAX_IO] = {0};
+    surf_sums(P, M, cur, surf);
     for (int e = 0; e < ne; ++e) {
-      if (p->iflux == 1) edge_body<1>(a, M, e, dt, t);
-      else if (p->iflux == 2) edge_body<2>(a, M, e, dt, t);
-      else if (p->iflux == 3) edge_body<3>(a, M, e, dt, t);
-      else edge_body<4>(a, M, e, dt, t);
+      if (p->iflux == 1) edge_body<1>(a, M, e, dt, t, surf);
+      else if (p->iflux == 2) edge_body<2>(a, M, e, dt, t, surf);
+      else if (p->iflux == 3) edge_body<3>(a, M, e, dt, t, surf);
+      else edge_body<4>(a, M, e, dt, t, surf);
     }
     double next = M.dt_reset;
     for (int c = 0; c < n; ++c) {
@@ -125,7 +169,18 @@ extern "C" int harness_run(const cf_mesh* m, const cf_params* p, const double* U
     dt = next;
     if (dt_hist) dt_hist[s + 1] = dt;
     std::swap(cur, nxt);
+    ++done;
+    if (M.tol_reg_perm > 0.0) {   /* check_steady_state, as k_discharge applies it */
+      double qi, qo;
+      discharge(P, slots, qi, qo);
+      if (qi > (double)1e-8f && std::fabs(qi - qo) / qi < M.tol_reg_perm) {
+        if (++steady_iter > M.steady_count) { rc = 1; break; }
+      } else {
+        steady_iter = 0;
+      }
+    }
   }
+  if (steps_out) *steps_out = done;
   for (int c = 0; c < n; ++c) {
     int o = P.perm[c];
     U_out[3 * o] = cur[c].x; U_out[3 * o + 1] = cur[c].y; U_out[3 * o + 2] = cur[c].z;
@@ -185,14 +240,7 @@ extern "C" int harness_tangent(const cf_mesh* m, const cf_params* p, const doubl
   if (rc != CF_OK) return rc;
   const int n = P.nelt;
   MemberDev M;
-  std::memset(&M, 0, sizeof(M));
-  M.gp = p->gp; M.tolisec = p->tolisec; M.tol = p->tol; M.constant_dt = p->constant_dt;
-  M.ramp_time = p->ramp_time;
-  for (int i = 0; i < CF_MAX_IO; ++i) {
-    M.debit_end[i] = p->debitglob[i]; M.debit_start[i] = p->debitglob_start[i];
-    M.long_entree[i] = P.long_entree[i]; M.h_sortie[i] = p->h_sortie[i];
-  }
-  M.inlet = p->inlet; M.outlet = p->outlet; M.friction = p->friction; M.fricimplic = p->fricimplic;
+  fill_member(M, p, P);
   std::vector<D1> h(n), hu(n), hv(n), nm(n), nh(n), nhu(n), nhv(n);
   std::vector<double> z(n);
   for (int c = 0; c < n; ++c) {

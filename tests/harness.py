@@ -55,7 +55,8 @@ def run(case, nsteps, params=None, U0=None):
     L = lib()
     if not hasattr(L, "_run_typed"):
         dp = C.POINTER(C.c_double)
-        L.harness_run.argtypes = [C.POINTER(_abi.CfMesh), C.POINTER(_abi.CfParams), dp, C.c_int, dp, dp, dp]
+        L.harness_run.argtypes = [C.POINTER(_abi.CfMesh), C.POINTER(_abi.CfParams), dp, C.c_int, dp, dp, dp,
+                                  C.POINTER(C.c_int)]
         L.harness_run.restype = C.c_int
         L._run_typed = True
     ma = _abi.MeshArrays(case)
@@ -64,8 +65,10 @@ def run(case, nsteps, params=None, U0=None):
     U = np.zeros_like(U0)
     dth = np.zeros(nsteps + 1)
     t = C.c_double(0.0)
-    rc = L.harness_run(C.byref(ma.mesh), C.byref(p), _abi.dptr(U0), int(nsteps), _abi.dptr(U), _abi.dptr(dth), C.byref(t))
-    return dict(U=U, dt_hist=dth, t=t.value, rc=rc)
+    steps = C.c_int(0)
+    rc = L.harness_run(C.byref(ma.mesh), C.byref(p), _abi.dptr(U0), int(nsteps), _abi.dptr(U), _abi.dptr(dth),
+                       C.byref(t), C.byref(steps))
+    return dict(U=U, dt_hist=dth, t=t.value, rc=rc, steps=steps.value)
 
 
 def div_check(n, seed=12345):

@@ -151,7 +151,8 @@ def test_unsupported_options_are_rejected(lib):
     c = cases.circular_dam_break(6, 6, seed=1)
     m = _abi.MeshArrays(c)
     ctx = C.c_void_p()
-    for over, code in ((dict(iflux=5), _abi.CF_EINVAL), (dict(inlet=3), _abi.CF_ENOTSUP),
+    for over, code in ((dict(iflux=5), _abi.CF_EINVAL), (dict(inlet=4), _abi.CF_EINVAL),
+                       (dict(tol_reg_perm=-1.0), _abi.CF_EINVAL),
                        (dict(ilimiteur=7), _abi.CF_EINVAL), (dict(flux_mode=2), _abi.CF_EINVAL),
                        (dict(cfl=0.0), _abi.CF_EINVAL)):
         p = _abi.make_params({**c.params, **over})

@@ -59,6 +59,14 @@ CASES = [
     ("muscl_conservative", lambda: cases.flooding(40, 20, seed=7, iflux=4), 150, dict(flux_mode=1)),
     ("muscl_outlet_transm", lambda: cases.flooding(40, 20, seed=9, iflux=4), 120, dict(outlet=2)),
     ("lake_muscl", lambda: cases.lake_at_rest(30, 15, iflux=4), 100, {}),
+    ("phys_inflow_hllc", lambda: cases.flooding(40, 20, seed=9, iflux=1), 150, dict(inlet=3)),
+    ("phys_inflow_waf", lambda: cases.flooding(40, 20, seed=9, iflux=3), 150, dict(inlet=3)),
+    ("phys_inflow_muscl", lambda: cases.flooding(40, 20, seed=9, iflux=4), 120, dict(inlet=3)),
+    ("phys_inflow_dry_start", lambda: cases.flooding(18, 9, seed=22, lx=360.0, ly=180.0, iflux=3), 60,
+     dict(inlet=3)),
+    ("steady_stop_any", lambda: cases.channel(), 400, dict(tol_reg_perm=1.5, steady_count=30)),
+    ("steady_stop_half", lambda: cases.channel(), 900, dict(tol_reg_perm=0.5, steady_count=20)),
+    ("steady_stop_phys_inflow", lambda: cases.channel(inlet=3), 900, dict(tol_reg_perm=0.05, steady_count=50)),
     ("fric_explicit", lambda: cases.flooding(40, 20, seed=8, iflux=1), 120, dict(fricimplic=0)),
     ("fric_diag", lambda: cases.flooding(40, 20, seed=8, iflux=1), 120, dict(fricimplic=2)),
     ("no_friction", lambda: cases.flooding(40, 20, seed=8, iflux=3), 120, dict(friction=0)),
@@ -78,6 +86,7 @@ def test_full_run_bitwise(oracle, name, make, n, prm):
     r1 = oracle.run(c, n, params=prm, check=False)
     r2 = H.run(c, n, params=prm)
     assert r1["rc"] == r2["rc"]
+    assert r1["steps"] == r2["steps"]
     assert np.array_equal(r1["dt_hist"], r2["dt_hist"])
     assert np.array_equal(r1["U"], r2["U"])
     assert r1["t"] == r2["t"]

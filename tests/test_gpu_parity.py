@@ -159,3 +159,34 @@ def test_config1_circular_dam_break_full(gpu_lib, oracle):
     m0 = float((c.U0[:, 0] * area).sum())
     m1 = float((U[:, 0] * area).sum())
     assert abs(m1 - m0) <= 1e-12 * m0
+
+
+@pytest.mark.parametrize("iflux", [1, 3, 4])
+def test_phys_inflow(gpu_lib, oracle, iflux):
+    """inlet 3 (phys_inflow): the per-step inlet sums of calcul_surf_entree on the device."""
+    c = cases.flooding(50, 25, seed=9, iflux=iflux)
+    U, ref, info = compare_bitwise(c, 150, oracle, params=dict(inlet=3), chunks=(7, 60, 1))
+    assert abs(info.q_in - ref["q_in"]) <= 1e-12 * abs(ref["q_in"])
+
+
+@pytest.mark.parametrize("tol,count", [(1.5, 30), (0.5, 20), (0.05, 50)])
+@pytest.mark.parametrize("inlet", [2, 3])
+def test_steady_state_stop(gpu_lib, oracle, tol, count, inlet):
+    """The steady-state test runs on the device after every step; the member stops at the
+    oracle's step with CF_STATUS_STEADY, cf_step reports success, and further calls do not
+    step it."""
+    from cuteflow_gb300 import Solver
+    c = cases.channel(inlet=inlet)
+    prm = dict(tol_reg_perm=tol, steady_count=count)
+    ref = oracle.run(c, 1200, params=prm, check=False)
+    assert ref["rc"] == 1
+    with Solver(c, prm) as s:
+        s.set_state(c.U0)
+        info = s.step(1200)
+        assert info.status & _abi.CF_STATUS_STEADY
+        assert info.steps == ref["steps"]
+        U = s.get_state()
+        again = s.step(5)
+        assert again.steps == info.steps and np.array_equal(s.get_state(), U)
+    assert np.array_equal(U, ref["U"])
+    assert info.t == ref["t"]

@@ -150,3 +150,47 @@ def test_dam_break_converges_to_stoker(oracle):
         errs.append((np.abs(r["U"][:, 0] - h_ex) * area).sum() / area.sum())
     assert errs[1] < 0.75 * errs[0]
     assert errs[1] < 0.02
+
+
+@pytest.mark.parametrize("iflux", [1, 3])
+def test_phys_inflow_delivers_the_discharge(oracle, iflux):
+    """phys_inflow (flux_riemann.cuf:127-138) gives each inflow edge Q * h len / sum(h len):
+    with one inflow edge per element the edges carry Q in total, spread in proportion to depth
+    (calcul_surf_entree, maillage.cuf:1368-1421)."""
+    c = cases.channel(iflux=iflux, inlet=3, q=1.5)
+    Q = 1.5 * 120.0
+    for n in (1, 40, 200):
+        r = oracle.run(c, n)
+        assert abs(r["q_in"] - Q) <= 1e-12 * Q, (n, r["q_in"])
+
+
+def test_phys_inflow_shares_by_depth(oracle):
+    """Against inlet 2 (uniform unit discharge Q/L), phys_inflow puts more of the same Q
+    through the deeper inflow elements: on a cross-slope the deep side's momentum grows faster."""
+    c = cases.channel(inlet=2, q=1.0)
+    c.z = c.z + 0.004 * c.y          # deeper at small y
+    from cuteflow_gb300.cases import cell_bed
+    zc = cell_bed(c.x, c.y, c.z, c.tri)
+    c.U0[:, 0] = np.where(1.0 - zc > 1e-4, 1.0 - zc, 0.0)
+    a = oracle.run(c, 30)
+    b = oracle.run(c, 30, params=dict(inlet=3))
+    assert abs(a["q_in"] - b["q_in"]) <= 1e-12 * a["q_in"]
+    xc, yc = cases.cell_centroids(c.x, c.y, c.tri)
+    left = xc < 10.0
+    deep, shallow = left & (yc < 30.0), left & (yc > 90.0)
+    assert b["U"][deep, 1].mean() > a["U"][deep, 1].mean()
+    assert b["U"][shallow, 1].mean() < a["U"][shallow, 1].mean()
+
+
+def test_steady_state_stop(oracle):
+    """check_steady_state (finite_volumes_method.cuf:370-393): the run stops after more than
+    steady_count consecutive steps with |Q_in - Q_out| / Q_in < tol_reg_perm; a tolerance
+    above 1 qualifies every step with inflow; 0 never stops."""
+    c = cases.channel()
+    r = oracle.run(c, 200, params=dict(tol_reg_perm=1.5, steady_count=30))
+    assert r["rc"] == 1 and r["steps"] == 31
+    r = oracle.run(c, 900, params=dict(tol_reg_perm=0.5, steady_count=20))
+    assert r["rc"] == 1 and 20 < r["steps"] < 900
+    assert abs(r["q_in"] - r["q_out"]) < 0.5 * r["q_in"]
+    r = oracle.run(c, 300)
+    assert r["rc"] == 0 and r["steps"] == 300
