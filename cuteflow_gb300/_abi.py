@@ -19,6 +19,7 @@ CF_ENOTSUP = -7
 CF_STATUS_DT_RANGE = 1
 CF_STATUS_NONFINITE = 2
 CF_STATUS_STEADY = 4
+CF_STATUS_END = 8
 
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int32)

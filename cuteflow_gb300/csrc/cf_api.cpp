@@ -365,6 +365,8 @@ int set_state_member(cf_ctx* c, int32_t m, double t0) {
   std::memset(&s, 0, sizeof(s));
   s.dt[p0] = M.dev.dt_reset;
   s.t[p0] = t0;
+  s.tc = t0;
+  s.ts = INFINITY;
   s.base = p0;
   c->host_state[m] = s;
   CF_CUDA(c, cudaMemcpyAsync(c->mst + m, c->host_state + m, sizeof(MemberState), cudaMemcpyHostToDevice, c->stream));
@@ -496,6 +498,54 @@ int step_impl(cf_ctx* c, int32_t nsteps, cf_step_info* infos) {
   return CF_OK;
 }
 
+/* The reference's time loop until its end test on ts (finite_volumes_method.cuf:123), the
+ * steady-state stop or max_steps: steps in chunks, the device stopping each member at its
+ * own step; the host looks between chunks whether any member is still running. */
+int run_impl(cf_ctx* c, double ts, int64_t max_steps, cf_step_info* infos) {
+  if (!(ts == ts)) return fail(c, CF_EINVAL, "ts is NaN");
+  if (max_steps < 0) return fail(c, CF_EINVAL, "max_steps < 0");
+  CF_CUDA(c, cudaSetDevice(c->device));
+  int rc;
+  if ((rc = read_states(c))) return rc;
+  const size_t nm = c->mem.size();
+  for (size_t i = 0; i < nm; ++i) {
+    MemberState& s = c->host_state[i];
+    if (s.status & STATUS_NO_STATE) {
+      if (nm == 1) return fail(c, CF_ESTATE, "cf_run before a state was set");
+      continue;
+    }
+    if ((s.status & ~CF_STATUS_END) != 0) continue;  /* stopped for another reason */
+    if (s.status & CF_STATUS_END) {
+      /* steps launched while the member stood still have moved the launch parity: move its
+       * state (and dt, t) to the buffer the next launch reads */
+      const int cur = (int)((s.base + s.nstep) & 1), want = (int)(c->launched & 1);
+      if (cur != want) {
+        const Member& M = c->mem[i];
+        CF_CUDA(c, cudaMemcpyAsync(c->U[want] + M.cell_off, c->U[cur] + M.cell_off, (size_t)M.n * sizeof(double4),
+                                   cudaMemcpyDeviceToDevice, c->stream));
+        s.dt[want] = s.dt[cur];
+        s.t[want] = s.t[cur];
+        s.base ^= 1;
+      }
+    }
+    s.status &= ~CF_STATUS_END;                      /* a later end time continues the run */
+    s.ts = ts;
+    CF_CUDA(c, cudaMemcpyAsync(c->mst + i, &s, sizeof(MemberState), cudaMemcpyHostToDevice, c->stream));
+  }
+  const int64_t chunk = 256;
+  int64_t done = 0;
+  while (done < max_steps) {
+    const int32_t k = (int32_t)std::min<int64_t>(chunk, max_steps - done);
+    if ((rc = step_impl(c, k, infos)) != CF_OK) return rc;
+    done += k;
+    bool running = false;
+    for (size_t i = 0; i < nm; ++i) running |= c->host_state[i].status == 0;
+    if (!running) break;
+  }
+  if (done == 0 && (rc = step_impl(c, 0, infos)) != CF_OK) return rc;
+  return CF_OK;
+}
+
 }  // namespace
 
 /* ---- helpers of the static-scratch entry point (cf_noalloc.cu) ---------------------------- */
@@ -547,6 +597,11 @@ int cf::step_with_slots(cf_ctx* c, int32_t nsteps, cf_step_info* infos, Slot* sl
 }
 
 extern "C" {
+
+int cf_run(cf_ctx* ctx, double ts, int64_t max_steps, cf_step_info* info) {
+  if (!ctx) return CF_EINVAL;
+  return run_impl(ctx, ts, max_steps, info);
+}
 
 int cf_default_params(cf_params* p) {
   if (!p) return CF_EINVAL;

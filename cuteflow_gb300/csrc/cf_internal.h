@@ -45,6 +45,7 @@ constexpr double EPS_RIADH = (double)1e-6f;   /* flux_riemann.cuf:1051 */
 constexpr double EPS_SECOND = (double)1e-16f; /* flux_riemann.cuf:555, :749 */
 constexpr double EPS_VLEER = (double)1e-12f;  /* flux_riemann.cuf:454 */
 constexpr double DT_LOW = (double)1e-12f;     /* cfl_condition.cuf:129 */
+constexpr double TOL_LOOP = (double)1e-6f;    /* tol, global_data.cuf:59, in the loop test :123 */
 
 struct Slot {
   double f1, f2, f3;   /* flux*len as evaluated by this side, global frame */
@@ -83,6 +84,8 @@ struct MemberState {
   int32_t steady_iter;  /* consecutive steps that met the steady-state test */
   int32_t pad_;
   double surf[CF_MAX_IO];  /* phys_inflow: sum of length * depth over each inlet, at the step's start */
+  double tc;         /* the reference's loop time: t0, then + the dt computed after every step */
+  double ts;         /* cf_run's end time; the member stops when (tc - ts + 2 tol) < tol fails */
 };
 
 /* status bit of a member whose state has not been set yet */

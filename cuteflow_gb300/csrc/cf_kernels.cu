@@ -51,7 +51,14 @@ __global__ void __launch_bounds__(TILE_E) k_edges(StepArgs a) {
      * block with 1e5, cfl_condition.cuf:21,86). */
     if (S->nstep > 0 && (dt > 9999.0 || dt < DT_LOW)) {   /* the initial dt is not tested (:113-116) */
       atomicOr(&S->status, CF_STATUS_DT_RANGE);
+    } else if (S->nstep > 0 && !((S->tc + dt) - S->ts + 2.0 * TOL_LOOP < TOL_LOOP)) {
+      /* the time loop's test (finite_volumes_method.cuf:123) on tc = tc + dt (:232); tc keeps
+       * its value, so that a later cf_run adds this dt once and tests again */
+      atomicOr(&S->status, CF_STATUS_END);
+    } else if (S->nstep == 0 && !(S->tc - S->ts + 2.0 * TOL_LOOP < TOL_LOOP)) {
+      atomicOr(&S->status, CF_STATUS_END);
     } else {
+      if (S->nstep > 0) S->tc = S->tc + dt;
       S->t[1 - p] = t + dt;
       S->dt[1 - p] = M.dt_reset;
       S->nstep += 1;

@@ -54,6 +54,7 @@ def load(build_if_missing: bool = True):
     L.cf_set_initial_condition.argtypes = [vp, C.POINTER(_abi.CfIc), C.c_double]
     L.cf_step.argtypes = [vp, C.c_int32, C.POINTER(_abi.CfStepInfo)]
     L.cf_step_noalloc.argtypes = [vp, C.c_int32, C.POINTER(_abi.CfStepInfo)]
+    L.cf_run.argtypes = [vp, C.c_double, C.c_int64, C.POINTER(_abi.CfStepInfo)]
     L.cf_get_state.argtypes = [vp, dp]
     L.cf_get_state_device.argtypes = [vp, vp]
     L.cf_get_info.argtypes = [vp, C.POINTER(_abi.CfStepInfo)]
@@ -92,7 +93,7 @@ def load(build_if_missing: bool = True):
                  "cf_member_get_state", "cf_member_get_info", "cf_member_get_mesh_tables"):
         getattr(L, name).restype = C.c_int
     for name in ("cf_default_params", "cf_create", "cf_set_state", "cf_set_state_device",
-                 "cf_set_initial_condition", "cf_step", "cf_step_noalloc", "cf_get_state", "cf_get_state_device",
+                 "cf_set_initial_condition", "cf_step", "cf_step_noalloc", "cf_run", "cf_get_state", "cf_get_state_device",
                  "cf_get_info", "cf_get_mesh_tables", "cf_mesh_tables", "cf_get_sizes", "cf_set_timing", "cf_get_timing"):
         getattr(L, name).restype = C.c_int
     _lib = L
@@ -197,6 +198,15 @@ class Solver:
             self._check(rc)
         return _info(info)
 
+    def run(self, ts: float, max_steps: int = 1 << 40, check: bool = True) -> StepInfo:
+        """The reference's time loop up to time ts (cf_run): stops with CF_STATUS_END, or at a
+        steady state, or after max_steps steps."""
+        info = _abi.CfStepInfo()
+        rc = self._L.cf_run(self._ctx, float(ts), int(max_steps), C.byref(info))
+        if check:
+            self._check(rc)
+        return _info(info)
+
     def info(self) -> StepInfo:
         s = _abi.CfStepInfo()
         self._check(self._L.cf_get_info(self._ctx, C.byref(s)))
@@ -284,6 +294,14 @@ class Batch:
     def step(self, nsteps: int, check: bool = True):
         infos = (_abi.CfStepInfo * self.members)()
         rc = self._L.cf_step(self._ctx, int(nsteps), infos)
+        if check:
+            self._check(rc)
+        return [_info(i) for i in infos]
+
+    def run(self, ts: float, max_steps: int = 1 << 40, check: bool = True):
+        """Every member up to time ts (cf_run), each stopping at its own step."""
+        infos = (_abi.CfStepInfo * self.members)()
+        rc = self._L.cf_run(self._ctx, float(ts), int(max_steps), infos)
         if check:
             self._check(rc)
         return [_info(i) for i in infos]

@@ -45,6 +45,7 @@ extern "C" {
 #define CF_STATUS_NONFINITE 2u
 #define CF_STATUS_STEADY 4u      /* steady state reached (check_steady_state,
                                     finite_volumes_method.cuf:370-393): the member stops, no error */
+#define CF_STATUS_END 8u         /* cf_run reached its end time ts: the member stops, no error */
 
 /* Mesh tables, as lec_mail_tri reads them (maillage.cuf:196-313). */
 typedef struct cf_mesh {
@@ -161,6 +162,14 @@ int cf_set_initial_condition(cf_ctx* ctx, const cf_ic* ic, double t0);
  * others do), CF_ESTATE for a plain context without a state. */
 int cf_step(cf_ctx* ctx, int32_t nsteps, cf_step_info* info);
 
+/* The reference's time loop (solve_finite_volumes, finite_volumes_method.cuf:123-242): steps
+ * every member until the loop test (tc - ts + 2 tol) < tol fails (tol = 1e-6 in single
+ * precision, tc = the state's t0 plus the dt computed after every step, :232), the
+ * steady-state test stops it (tol_reg_perm), or max_steps steps have run.  Members that
+ * reach ts stop with CF_STATUS_END; a later cf_run with a larger ts continues them.  The
+ * test runs on the device, so every member stops at its own step.  Returns as cf_step. */
+int cf_run(cf_ctx* ctx, double ts, int64_t max_steps, cf_step_info* info);
+
 /* Copy U^n to host memory in reference order (3*nelt doubles). */
 int cf_get_state(cf_ctx* ctx, double* hu3_out);
 
@@ -169,6 +178,30 @@ int cf_get_state_device(cf_ctx* ctx, double* d_hu3_out);
 
 /* Current time, dt and status without stepping. */
 int cf_get_info(cf_ctx* ctx, cf_step_info* info);
+
+/* ---- The reference's input files -------------------------------------------------------
+ * A case directory as the reference's main program reads it (main.cuf:48-182): the
+ * donnees_namelist file (lec_donnees, maillage.cuf:168-193; keys of global_data.cuf:65-94,
+ * unknown keys are an error as in a Fortran namelist read), the ASCII mesh it names
+ * (meshfile_path // meshfile, lec_mail_tri, maillage.cuf:196-313; is_cgns = 1 gives
+ * CF_ENOTSUP) and, with solinit = 1, the element initial-condition file fich_sol_init
+ * (read_initial_condition, initial_condition.cuf:82-102).  Relative paths are taken from dir.
+ * The mesh and params pointers stay valid until cf_case_free. */
+typedef struct cf_case cf_case;
+int cf_case_read(const char* dir, const char* namelist_file /* NULL: "donnees.f" */, cf_case** out);
+void cf_case_free(cf_case* c);
+/* Text of the last failed cf_case_* / cf_write_state_file call of this thread. */
+const char* cf_case_last_error(void);
+/* Mesh and parameters for cf_create, the dam line / plane of the namelist (cf_ic), its end time
+ * ts and solinit; any pointer may be NULL. */
+int cf_case_get(const cf_case* c, const cf_mesh** mesh, const cf_params** params, cf_ic* ic, double* ts,
+                int32_t* solinit);
+/* solinit = 1: the state of fich_sol_init (3*nelt doubles) and the time written on its first
+ * line (which the reference reads but does not use: main.cuf:182 starts at tc = 0). */
+int cf_case_initial_state(const cf_case* c, double* hu3, double* t_file);
+/* Write a state in the layout of save_sol_for_restart (pre_post_traitement.cuf:498-512): the
+ * time, then h, hu, hv of every element in fields '(4f16.6)', which keep 6 decimals. */
+int cf_write_state_file(const char* path, const double* hu3, int32_t nelt, double t);
 
 /* ---- Batched ensembles (no reference counterpart: the reference runs ensemble members as
  * separate processes, scripts/array.sh:8-11, Calibration_manning/scripts/calib_array.sh:8-11).

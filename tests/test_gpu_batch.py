@@ -79,3 +79,28 @@ def test_batch_mixed_first_order_schemes_rejected(gpu_lib):
     b = cases.circular_dam_break(10, 10, seed=2, iflux=3)
     with pytest.raises(CFError):
         Batch([a, b])
+
+
+def test_batch_run_until_ts(gpu_lib, oracle):
+    """cf_run on a batch: every member stops at its own step (its own dt sequence), the others
+    going on in the same launches."""
+    from cuteflow_gb300 import Batch
+    ms = [cases.channel(nx=40 + 10 * i, ny=10, seed=30 + i, q=0.5 + 0.4 * i) for i in range(3)]
+    tol = float(np.float32(1e-6))
+    want = []
+    for c in ms:
+        r = oracle.run(c, 1500)
+        tc, k = 0.0, 0
+        while tc - 50.0 + 2 * tol < tol:
+            k += 1
+            tc = tc + r["dt_hist"][k]
+        want.append(k)
+    with Batch(ms) as b:
+        for i, c in enumerate(ms):
+            b.set_state(i, c.U0)
+        infos = b.run(50.0)
+        got = [b.get_state(i) for i in range(len(ms))]
+    assert len(set(want)) > 1
+    for i, c in enumerate(ms):
+        assert infos[i].steps == want[i] and infos[i].status & _abi.CF_STATUS_END
+        assert np.array_equal(got[i], oracle.run(c, want[i])["U"])

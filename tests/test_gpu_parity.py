@@ -190,3 +190,56 @@ def test_steady_state_stop(gpu_lib, oracle, tol, count, inlet):
         assert again.steps == info.steps and np.array_equal(s.get_state(), U)
     assert np.array_equal(U, ref["U"])
     assert info.t == ref["t"]
+
+
+def _steps_to(dt_hist, ts, tc=0.0):
+    """Steps the reference's loop (finite_volumes_method.cuf:123, :232) takes to reach ts:
+    tc starts at t0 and adds the dt computed after every step."""
+    tol = float(np.float32(1e-6))
+    if not (tc - ts + 2 * tol < tol):
+        return 0
+    for k in range(1, len(dt_hist)):
+        tc = tc + dt_hist[k]
+        if not (tc - ts + 2 * tol < tol):
+            return k
+    raise AssertionError("ts not reached")
+
+
+@pytest.mark.parametrize("iflux", [1, 3])
+def test_run_until_ts(gpu_lib, oracle, iflux):
+    """cf_run stops every member at the step where the reference's time loop ends, and a later
+    cf_run with a larger ts continues from there."""
+    from cuteflow_gb300 import Solver
+    c = cases.channel(iflux=iflux)
+    full = oracle.run(c, 1500)
+    k1, k2 = _steps_to(full["dt_hist"], 60.0), _steps_to(full["dt_hist"], 97.5)
+    assert 0 < k1 < k2 < 1500
+    with Solver(c) as s:
+        s.set_state(c.U0)
+        info = s.run(60.0)
+        assert info.status & _abi.CF_STATUS_END and info.steps == k1
+        assert np.array_equal(s.get_state(), oracle.run(c, k1)["U"])
+        info = s.run(97.5)
+        assert info.status & _abi.CF_STATUS_END and info.steps == k2
+        assert np.array_equal(s.get_state(), oracle.run(c, k2)["U"])
+        info = s.run(97.5)
+        assert info.steps == k2
+        info = s.run(1e9, max_steps=10)
+        assert info.steps == k2 + 10 and not info.status
+
+
+def test_case_directory_runs_to_ts(gpu_lib, oracle, tmp_path):
+    """A case directory in the reference's formats (namelist, ASCII mesh, initial condition
+    file) read through cf_case_read and run to its ts equals the oracle on the same steps."""
+    from cuteflow_gb300 import Solver, case_files
+    c = cases.channel(inlet=3, iflux=3)
+    case_files.write_case(c, str(tmp_path), ts=45.0)
+    r = case_files.read_case(str(tmp_path))
+    with Solver(r, r.params) as s:
+        s.set_state(r.U0)
+        info = s.run(r.ts)
+        U = s.get_state()
+    full = oracle.run(c, 1000)
+    k = _steps_to(full["dt_hist"], 45.0)
+    assert info.steps == k and info.status & _abi.CF_STATUS_END
+    assert np.array_equal(U, oracle.run(c, k)["U"])
