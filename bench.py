@@ -37,6 +37,11 @@ UNIT = "tri-updates/s"
 # statics, neighbour ids, per-edge geometry at E/N = 1.5, centroids): see the design doc.
 ALG_BYTES_WAF = 144.0
 ALG_BYTES_HLLC = 128.0
+# DRAM bytes (read + write) of one 1M-triangle WAF step from one ncu capture of this command's
+# kernels (k_edges<3> 368.0 MB + k_cells 247.4 MB, profiles/step_kernels_flooding_1M_WAF.md), and
+# the FP64-pipe activity the same capture reports; used for the default workload only.
+NCU_TRAFFIC_FLOODING_1M = 615.4e6
+NCU_FP64_PIPE_FLOODING_1M = {"k_edges": 0.853, "k_cells": 0.802}
 
 
 def peaks():
@@ -363,10 +368,14 @@ def run_ours(args):
         "roofline": {"bound": "hbm", "kernel": "one time step (k_edges + k_cells)",
                      "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "peak_source": f"MEASURED_PEAKS.json hbm_gbs ({hbm_src})",
-                     "alg_bytes_per_tri": alg_bytes, "traffic": None,
+                     "alg_bytes_per_tri": alg_bytes,
+                     "traffic": NCU_TRAFFIC_FLOODING_1M if args.config == "flooding" else None,
+                     "traffic_note": "ncu dram__bytes_read.sum + dram__bytes_write.sum per step "
+                                     "(k_edges + k_cells) of the 1M WAF step",
                      "k_edges_ms": k_edges_ms, "k_cells_ms": k_cells_ms},
         "fp64": {"note": "the step is FP64-pipe bound; peak measured by a DFMA probe on this pool",
-                 "peak_tflops": fp64_peak},
+                 "peak_tflops": fp64_peak,
+                 "pipe_active_ncu": NCU_FP64_PIPE_FLOODING_1M if args.config == "flooding" else None},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 24 * n, "d2h_bytes_per_step": 24 * n,
                 "steps": e2e_steps},
         "gpu_launches": 2 * args.steps + 1,
