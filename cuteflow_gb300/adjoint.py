@@ -33,19 +33,32 @@ def _ptr(a) -> C.c_void_p:
 
 
 class Adjoint:
-    """Adjoint of ``nsteps`` steps of ``solver`` (a one-member context) with gauge elements
-    ``gauges`` (0-based, reference order).  ``checkpoint_interval`` 0 keeps ceil(sqrt(N))."""
+    """Adjoint of ``nsteps`` steps of ``solver`` with gauge elements ``gauges`` (0-based,
+    reference order).  ``solver`` is a Solver, or a Batch with ``gauge_member`` giving each
+    gauge's member; states and gradients of a batch are concatenated in member order.
+    ``checkpoint_interval`` 0 keeps ceil(sqrt(N))."""
 
-    def __init__(self, solver: Solver, nsteps: int, gauges, checkpoint_interval: int = 0):
+    def __init__(self, solver, nsteps: int, gauges, checkpoint_interval: int = 0, gauge_member=None):
         self._L = load()
         self.solver = solver
         self.nsteps = int(nsteps)
         self.gauges = np.ascontiguousarray(gauges, dtype=np.int32).ravel()
         self._h = C.c_void_p()
-        rc = self._L.cf_adjoint_create(solver._ctx, self.nsteps, int(checkpoint_interval),
-                                       self.gauges.ctypes.data_as(C.POINTER(C.c_int32)), int(self.gauges.size),
-                                       C.byref(self._h))
+        ip = C.POINTER(C.c_int32)
+        if gauge_member is None:
+            rc = self._L.cf_adjoint_create(solver._ctx, self.nsteps, int(checkpoint_interval),
+                                           self.gauges.ctypes.data_as(ip), int(self.gauges.size), C.byref(self._h))
+            self.gauge_member = np.zeros_like(self.gauges)
+        else:
+            self.gauge_member = np.ascontiguousarray(gauge_member, dtype=np.int32).ravel()
+            assert self.gauge_member.size == self.gauges.size
+            rc = self._L.cf_adjoint_create_batch(solver._ctx, self.nsteps, int(checkpoint_interval),
+                                                 self.gauge_member.ctypes.data_as(ip),
+                                                 self.gauges.ctypes.data_as(ip), int(self.gauges.size),
+                                                 C.byref(self._h))
         solver._check(rc)
+        self.members = int(getattr(solver, "members", 1))
+        self.nelt_total = int(sum(solver.nelt)) if isinstance(solver.nelt, (list, tuple)) else int(solver.nelt)
         k, g = C.c_int32(), C.c_int32()
         b = C.c_int64()
         self._L.cf_adjoint_sizes(self._h, None, C.byref(k), C.byref(g), C.byref(b))
@@ -84,7 +97,7 @@ class Adjoint:
         """Run; returns (eta [N, G], U^N [nelt, 3]) as numpy arrays, or fills the given
         buffers (numpy arrays, torch tensors or device addresses) and returns them."""
         ret_e = np.empty((self.nsteps, self.ngauges)) if eta is None else eta
-        ret_s = np.empty((self.solver.nelt, 3)) if state is None else state
+        ret_s = np.empty((self.nelt_total, 3)) if state is None else state
         self.solver._check(self._L.cf_adjoint_forward(self._h, 1 if replay else 0, _ptr(ret_e), _ptr(ret_s)))
         self.generation += 1
         return ret_e, ret_s
@@ -96,21 +109,24 @@ class Adjoint:
             assert w_eta.size == self.nsteps * self.ngauges
         if w_state is not None and not isinstance(w_state, int) and not hasattr(w_state, "data_ptr"):
             w_state = np.ascontiguousarray(w_state, dtype=np.float64)
-            assert w_state.size == 3 * self.solver.nelt
-        gs = np.empty((self.solver.nelt, 3)) if g_state0 is None else g_state0
-        gm = np.empty(self.solver.nelt) if g_manning is None else g_manning
+            assert w_state.size == 3 * self.nelt_total
+        gs = np.empty((self.nelt_total, 3)) if g_state0 is None else g_state0
+        gm = np.empty(self.nelt_total) if g_manning is None else g_manning
         self.solver._check(self._L.cf_adjoint_backward(self._h, _ptr(w_eta), _ptr(w_state), _ptr(gs), _ptr(gm)))
         return gs, gm
 
     def dt_history(self) -> Tuple[np.ndarray, np.ndarray]:
-        dt, t = np.empty(self.nsteps), np.empty(self.nsteps)
+        """The recorded dt and start time of every step: [N] for one member, [N, members] for a
+        batch."""
+        shape = (self.nsteps,) if self.members == 1 else (self.nsteps, self.members)
+        dt, t = np.empty(shape), np.empty(shape)
         self.solver._check(self._L.cf_adjoint_get_dt(self._h, _ptr(dt), _ptr(t)))
         return dt, t
 
     def set_dt_history(self, dt, t):
         dt = np.ascontiguousarray(dt, dtype=np.float64)
         t = np.ascontiguousarray(t, dtype=np.float64)
-        assert dt.size == self.nsteps and t.size == self.nsteps
+        assert dt.size == self.nsteps * self.members and t.size == self.nsteps * self.members
         self.solver._check(self._L.cf_adjoint_set_dt(self._h, _ptr(dt), _ptr(t)))
 
 
@@ -164,6 +180,56 @@ def gauge_run(adj: Adjoint, manning, U0, t0: float = 0.0, replay: bool = False):
     if _GaugeRun is None:
         _GaugeRun = _torch_function()
     return _GaugeRun.apply(manning, U0, adj, float(t0), bool(replay))
+
+
+class Zones:
+    """Manning zones of a context (cf_zones_*): ``zone_of_elem`` gives every element's zone
+    (concatenated in member order for a batch; -1: not a parameter).  ``set`` writes zone
+    values into n; ``gradient(adj)`` sums the adjoint's last dJ/dn per zone on the device in a
+    fixed order; ``descend(lr, lo, hi)`` steps the values on the device and writes the new n."""
+
+    def __init__(self, solver, zone_of_elem, nzones: int):
+        self._L = load()
+        self.solver = solver
+        self.nzones = int(nzones)
+        z = np.ascontiguousarray(zone_of_elem, dtype=np.int32).ravel()
+        self._h = C.c_void_p()
+        solver._check(self._L.cf_zones_create(solver._ctx, z.ctypes.data_as(C.POINTER(C.c_int32)), self.nzones,
+                                              C.byref(self._h)))
+
+    def close(self):
+        if self._h:
+            self._L.cf_zones_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def set(self, values):
+        v = values if hasattr(values, "data_ptr") else np.ascontiguousarray(values, dtype=np.float64)
+        self.solver._check(self._L.cf_zones_set(self._h, _ptr(v)))
+
+    def get(self) -> Tuple[np.ndarray, np.ndarray]:
+        v, g = np.empty(self.nzones), np.empty(self.nzones)
+        self.solver._check(self._L.cf_zones_get(self._h, _ptr(v), _ptr(g)))
+        return v, g
+
+    def gradient(self, adj: "Adjoint", out=None) -> np.ndarray:
+        g = np.empty(self.nzones) if out is None else out
+        self.solver._check(self._L.cf_zones_gradient(self._h, adj._h, _ptr(g)))
+        return g
+
+    def descend(self, lr: float, lo: float, hi: float):
+        self.solver._check(self._L.cf_zones_descend(self._h, float(lr), float(lo), float(hi)))
 
 
 def zone_gradient(g_manning: np.ndarray, zones: np.ndarray, nzones: Optional[int] = None) -> np.ndarray:

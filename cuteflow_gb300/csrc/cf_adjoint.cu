@@ -55,22 +55,28 @@ __device__ __forceinline__ Dual<D> seed(double v, int k, int base) {
 
 /* ---- replay of the forward -------------------------------------------------------------- */
 
+/* The recorded dt and start time of step n of member m: histories are [N][members]. */
+__device__ __forceinline__ size_t hidx(int n, int m, int nm) { return (size_t)n * nm + m; }
+
 template <int IFLUX>
 __global__ void __launch_bounds__(TILE_E) k_rep_edges(StepArgs a, const double* dt_hist, const double* t_hist, int n) {
   const int tile = blockIdx.x;
-  const MemberDev& M = a.mdev[__ldg(a.etile_mem + tile)];
+  const int m = __ldg(a.etile_mem + tile);
+  const MemberDev& M = a.mdev[m];
   const int e = tile * TILE_E + threadIdx.x;
   if (e >= M.edge_end) return;
-  edge_body<IFLUX>(a, M, e, __ldg(dt_hist + n), __ldg(t_hist + n));
+  const size_t h = hidx(n, m, a.nmembers);
+  edge_body<IFLUX>(a, M, e, __ldg(dt_hist + h), __ldg(t_hist + h));
 }
 
 __global__ void __launch_bounds__(TILE_C) k_rep_cells(StepArgs a, const double* dt_hist, int n, uint32_t* flag,
                                                       Slot* sums) {
   const int tile = blockIdx.x;
-  const MemberDev& M = a.mdev[__ldg(a.ctile_mem + tile)];
+  const int m = __ldg(a.ctile_mem + tile);
+  const MemberDev& M = a.mdev[m];
   const int c = tile * TILE_C + threadIdx.x;
   if (c >= M.cell_end) return;
-  const double dt = __ldg(dt_hist + n);
+  const double dt = __ldg(dt_hist + hidx(n, m, a.nmembers));
   const double4 U = ld4(a.Uin + c);
   const double4 st = ld4(a.cstat + c);
   const int4 sl = __ldg(a.cslot + c);
@@ -92,18 +98,19 @@ __global__ void __launch_bounds__(TILE_C) k_rep_cells(StepArgs a, const double* 
   }
 }
 
-/* After step n: the gauge elevations h + z of the new state and, when recording, the dt and
- * start time of the step (read from the member record of parity p). */
-__global__ void k_record(const double4* Unew, const MemberState* S, int p, int n, double* dt_hist, double* t_hist,
-                         const int32_t* gcell, int G, double* eta) {
+/* After step n: the gauge elevations h + z of the new state and, when recording, every
+ * member's dt and start time of the step (read from its record of parity p). */
+__global__ void k_record(const double4* Unew, const MemberState* S, int nm, int p, int n, double* dt_hist,
+                         double* t_hist, const int32_t* gcell, int G, double* eta) {
   for (int g = threadIdx.x; g < G; g += blockDim.x) {
     const double4 u = Unew[gcell[g]];
     eta[(size_t)n * G + g] = u.x + u.w;
   }
-  if (S && threadIdx.x == 0) {
-    dt_hist[n] = S->dt[p];
-    t_hist[n] = S->t[p];
-  }
+  if (S)
+    for (int m = threadIdx.x; m < nm; m += blockDim.x) {
+      dt_hist[hidx(n, m, nm)] = S[m].dt[p];
+      t_hist[hidx(n, m, nm)] = S[m].t[p];
+    }
 }
 
 /* ---- adjoint of the element stage --------------------------------------------------------- */
@@ -139,11 +146,12 @@ __device__ __forceinline__ double4 gather_lambda(const AdjArgs& A, int c, const 
 __global__ void __launch_bounds__(TILE_C) k_adj_cells(AdjArgs A) {
   const StepArgs& a = A.s;
   const int tile = blockIdx.x;
-  const MemberDev& M = a.mdev[__ldg(a.ctile_mem + tile)];
+  const int mem = __ldg(a.ctile_mem + tile);
+  const MemberDev& M = a.mdev[mem];
   const int c = tile * TILE_C + threadIdx.x;
   if (c >= M.cell_end) return;
   const double4 L = A.gather ? gather_lambda(A, c, A.gw) : ld4(A.lam_init + c);
-  const double dt = __ldg(A.dt_hist + A.n);
+  const double dt = __ldg(A.dt_hist + hidx(A.n, mem, a.nmembers));
   const double4 U = ld4(a.Uin + c);
   const double4 st = ld4(a.cstat + c);
   const double2* sp = reinterpret_cast<const double2*>(A.sums + c);
@@ -230,10 +238,12 @@ template <int IFLUX, int D>
 __global__ void __launch_bounds__(TILE_E) k_adj_edges(AdjArgs A) {
   const StepArgs& a = A.s;
   const int tile = blockIdx.x;
-  const MemberDev& M = a.mdev[__ldg(a.etile_mem + tile)];
+  const int m = __ldg(a.etile_mem + tile);
+  const MemberDev& M = a.mdev[m];
   const int e = tile * TILE_E + threadIdx.x;
   if (e >= M.edge_end) return;
-  const double dt = __ldg(A.dt_hist + A.n), t = __ldg(A.t_hist + A.n);
+  const size_t h = hidx(A.n, m, a.nmembers);
+  const double dt = __ldg(A.dt_hist + h), t = __ldg(A.t_hist + h);
   const int2 ab = ldro(a.ecell + e);
   const double4 UA = ld4(a.Uin + ab.x);
   const Slot wa = A.cadj[ab.x];
@@ -326,6 +336,37 @@ __global__ void k_set_manning(double4* cstat, const int32_t* perm, const double*
   if (c < n) cstat[c].y = nref[perm[c]];
 }
 
+/* ---- Manning zones (calibration parameters) ------------------------------------------------ */
+
+/* dJ/d(zone value) = the sum of dJ/dn over the zone's elements, in the fixed order of the
+ * zone's element list (one block per zone: strided partial sums, then a tree). */
+__global__ void __launch_bounds__(256) k_zone_sum(const double* gman, const int32_t* zoff, const int32_t* zidx,
+                                                  double* gz) {
+  __shared__ double s[256];
+  const int z = blockIdx.x;
+  double v = 0.0;
+  for (int j = zoff[z] + threadIdx.x; j < zoff[z + 1]; j += 256) v += gman[zidx[j]];
+  s[threadIdx.x] = v;
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if (threadIdx.x < w) s[threadIdx.x] += s[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) gz[z] = s[0];
+}
+
+/* projected gradient step on the zone values: v = min(hi, max(lo, v - lr g)) */
+__global__ void k_zone_step(double* v, const double* g, int nz, double lr, double lo, double hi) {
+  const int z = blockIdx.x * blockDim.x + threadIdx.x;
+  if (z < nz) v[z] = fmin(hi, fmax(lo, v[z] - lr * g[z]));
+}
+
+/* the Manning n of every element of a zone (elements without a zone keep theirs) */
+__global__ void k_zone_apply(double4* cstat, const int32_t* zone_of, const double* v, int n) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c < n && zone_of[c] >= 0) cstat[c].y = v[zone_of[c]];
+}
+
 int chk(cudaError_t e) { return e == cudaSuccess ? CF_OK : CF_ECUDA; }
 
 }  // namespace
@@ -343,9 +384,9 @@ int launch_replay_step(const StepArgs& a, const double* dt_hist, const double* t
   return chk(cudaGetLastError());
 }
 
-int launch_record(const double4* Unew, const MemberState* S, int p, int n, double* dt_hist, double* t_hist,
+int launch_record(const double4* Unew, const MemberState* S, int nm, int p, int n, double* dt_hist, double* t_hist,
                   const int32_t* gcell, int G, double* eta, stream_t s) {
-  k_record<<<1, 256, 0, reinterpret_cast<cudaStream_t>(s)>>>(Unew, S, p, n, dt_hist, t_hist, gcell, G, eta);
+  k_record<<<1, 256, 0, reinterpret_cast<cudaStream_t>(s)>>>(Unew, S, nm, p, n, dt_hist, t_hist, gcell, G, eta);
   return chk(cudaGetLastError());
 }
 
@@ -382,6 +423,24 @@ int launch_gather_scalar(const double* x, const int32_t* iperm, double* out, int
 int launch_set_manning(double4* cstat, const int32_t* perm, const double* nref, int32_t n, stream_t s) {
   if (n <= 0) return CF_OK;
   k_set_manning<<<(n + 255) / 256, 256, 0, reinterpret_cast<cudaStream_t>(s)>>>(cstat, perm, nref, n);
+  return chk(cudaGetLastError());
+}
+
+int launch_zone_sum(const double* gman, const int32_t* zoff, const int32_t* zidx, double* gz, int32_t nz, stream_t s) {
+  if (nz <= 0) return CF_OK;
+  k_zone_sum<<<nz, 256, 0, reinterpret_cast<cudaStream_t>(s)>>>(gman, zoff, zidx, gz);
+  return chk(cudaGetLastError());
+}
+
+int launch_zone_step(double* v, const double* g, int32_t nz, double lr, double lo, double hi, stream_t s) {
+  if (nz <= 0) return CF_OK;
+  k_zone_step<<<(nz + 255) / 256, 256, 0, reinterpret_cast<cudaStream_t>(s)>>>(v, g, nz, lr, lo, hi);
+  return chk(cudaGetLastError());
+}
+
+int launch_zone_apply(double4* cstat, const int32_t* zone_of, const double* v, int32_t n, stream_t s) {
+  if (n <= 0) return CF_OK;
+  k_zone_apply<<<(n + 255) / 256, 256, 0, reinterpret_cast<cudaStream_t>(s)>>>(cstat, zone_of, v, n);
   return chk(cudaGetLastError());
 }
 

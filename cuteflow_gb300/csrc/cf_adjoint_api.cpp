@@ -16,7 +16,11 @@
  * Memory: ceil(N/K) + max(K, 2) states and max(K, 2) sum records (48 B per element each);
  * cost: one extra forward pass besides the reverse steps.
  *
- * Contexts with one member only.
+ * Batches.  On a context of several members the run, the checkpoints, the replay and the reverse
+ * steps cover every member in the same launches, each with its own recorded dt (histories are
+ * [N][members]); gauges are (member, element) pairs; states and gradients are concatenated in
+ * member order.  cf_zones_* sums dJ/dn over Manning zones in a fixed order and steps the zone
+ * values on the device, for gradient-descent calibration without host round trips.
  */
 #include <cuda_runtime.h>
 
@@ -33,7 +37,9 @@ using namespace cf;
 struct cf_adjoint {
   cf_ctx* ctx = nullptr;
   int32_t N = 0, K = 1, G = 0, nseg = 0, nseg_states = 2;
-  int32_t n = 0, n_pad = 0;
+  int32_t nm = 1;            /* members */
+  int64_t n_all = 0;         /* elements of all members */
+  int32_t n_pad = 0;
   double4* ckpt = nullptr;   /* nseg states */
   double4* seg = nullptr;    /* nseg_states states */
   MemberState* mst = nullptr;
@@ -56,6 +62,18 @@ struct cf_adjoint {
   int32_t freeze_r = 0;      /* linearization of the WAF limiter ratios: 0 exact, 1 held */
   bool recorded = false;     /* a recording forward has filled dt_hist / t_hist */
   bool have_traj = false;    /* the checkpoints hold the last forward's trajectory */
+};
+
+/* Manning zones of a context: every element's zone (flat new order, -1: none), the CSR zone ->
+ * elements, the zone values and the last zone gradient (device memory). */
+struct cf_zones {
+  cf_ctx* ctx = nullptr;
+  int32_t nz = 0;
+  int32_t* zoff = nullptr;
+  int32_t* zidx = nullptr;
+  int32_t* zone_of = nullptr;
+  double* gz = nullptr;
+  double* vals = nullptr;
 };
 
 namespace {
@@ -84,17 +102,20 @@ void build_csr(int32_t n, const std::vector<int32_t>& elem, const std::vector<in
   for (size_t k = 0; k < elem.size(); ++k) idx[(size_t)pos[elem[k]]++] = entry[k];
 }
 
-int create_impl(cf_ctx* c, int32_t nsteps, int32_t interval, const int32_t* gauges, int32_t ngauges, cf_adjoint** out) {
+int create_impl(cf_ctx* c, int32_t nsteps, int32_t interval, const int32_t* gauge_member, const int32_t* gauges,
+                int32_t ngauges, cf_adjoint** out) {
   if (!out) return fail(c, CF_EINVAL, "out is NULL");
   *out = nullptr;
-  if (c->mem.size() != 1) return fail(c, CF_ENOTSUP, "the adjoint takes a context with one member");
   if (c->iflux > 3) return fail(c, CF_ENOTSUP, "the adjoint covers iflux 1..3");
   if (c->any_phys_inflow) return fail(c, CF_ENOTSUP, "the adjoint does not cover inlet 3 (phys_inflow)");
   if (nsteps < 1) return fail(c, CF_EINVAL, "nsteps < 1");
   if (ngauges < 0 || (ngauges > 0 && !gauges)) return fail(c, CF_EINVAL, "gauges NULL or ngauges < 0");
-  const Member& M = c->mem[0];
-  for (int32_t g = 0; g < ngauges; ++g)
-    if (gauges[g] < 0 || gauges[g] >= M.n) return fail(c, CF_EINVAL, "gauge element out of range");
+  const int32_t nm = (int32_t)c->mem.size();
+  for (int32_t g = 0; g < ngauges; ++g) {
+    const int32_t m = gauge_member ? gauge_member[g] : 0;
+    if (m < 0 || m >= nm) return fail(c, CF_EINVAL, "gauge member out of range");
+    if (gauges[g] < 0 || gauges[g] >= c->mem[m].n) return fail(c, CF_EINVAL, "gauge element out of range");
+  }
   CF_CUDA(c, cudaSetDevice(c->device));
   cf_adjoint* a = new (std::nothrow) cf_adjoint();
   if (!a) return fail(c, CF_ENOMEM, "host allocation failed");
@@ -113,14 +134,15 @@ int create_impl(cf_ctx* c, int32_t nsteps, int32_t interval, const int32_t* gaug
   a->G = ngauges;
   a->nseg = (nsteps + a->K - 1) / a->K;
   a->nseg_states = std::max(a->K, 2);
-  a->n = M.n;
+  a->nm = nm;
+  for (const Member& M : c->mem) a->n_all += M.n;
   a->n_pad = c->n_pad;
   const size_t np = (size_t)c->n_pad, nep = (size_t)c->ne_pad;
   const bool second = c->iflux >= 3;
   int rc;
   if ((rc = dalloc(c, &a->ckpt, (size_t)a->nseg * np)) || (rc = dalloc(c, &a->seg, (size_t)a->nseg_states * np)) ||
-      (rc = dalloc(c, &a->mst, 1)) || (rc = dalloc(c, &a->dt_hist, (size_t)nsteps)) ||
-      (rc = dalloc(c, &a->t_hist, (size_t)nsteps)) || (rc = dalloc(c, &a->eta, (size_t)nsteps * ngauges)) ||
+      (rc = dalloc(c, &a->mst, (size_t)nm)) || (rc = dalloc(c, &a->dt_hist, (size_t)nsteps * nm)) ||
+      (rc = dalloc(c, &a->t_hist, (size_t)nsteps * nm)) || (rc = dalloc(c, &a->eta, (size_t)nsteps * ngauges)) ||
       (rc = dalloc(c, &a->wbuf, (size_t)nsteps * ngauges)) || (rc = dalloc(c, &a->gcell, (size_t)ngauges)) ||
       (rc = dalloc(c, &a->goff, np + 1)) || (rc = dalloc(c, &a->gidx, (size_t)ngauges)) ||
       (rc = dalloc(c, &a->lam[0], np)) || (rc = dalloc(c, &a->lam[1], np)) || (rc = dalloc(c, &a->cadj, np)) ||
@@ -131,7 +153,8 @@ int create_impl(cf_ctx* c, int32_t nsteps, int32_t interval, const int32_t* gaug
   {
     std::vector<int32_t> gc(ngauges), ge(ngauges), gi(ngauges), off, idx;
     for (int32_t g = 0; g < ngauges; ++g) {
-      gc[g] = M.prep.iperm[gauges[g]];
+      const Member& M = c->mem[gauge_member ? gauge_member[g] : 0];
+      gc[g] = M.cell_off + M.prep.iperm[gauges[g]];
       ge[g] = g;
     }
     build_csr(c->n_pad, gc, ge, off, idx);
@@ -149,15 +172,16 @@ int create_impl(cf_ctx* c, int32_t nsteps, int32_t interval, const int32_t* gaug
         (rc = get(c, dw.data(), c->ewts, nep)))
       return done(rc);
     std::vector<int32_t> el, en, off, idx;
-    for (int32_t e = 0; e < M.ne; ++e) {
-      if (ecell[e].y < 0) continue;
-      el.push_back(up[e].x);
-      en.push_back(4 * e);
-      if (dw[e].x >= 0.0) { el.push_back(up[e].y); en.push_back(4 * e + 1); }
-      el.push_back(up[e].z);
-      en.push_back(4 * e + 2);
-      if (dw[e].z >= 0.0) { el.push_back(up[e].w); en.push_back(4 * e + 3); }
-    }
+    for (const Member& M : c->mem)   /* the members' real edges (not the tile padding) */
+      for (int32_t e = M.edge_off; e < M.edge_off + M.ne; ++e) {
+        if (ecell[e].y < 0) continue;
+        el.push_back(up[e].x);
+        en.push_back(4 * e);
+        if (dw[e].x >= 0.0) { el.push_back(up[e].y); en.push_back(4 * e + 1); }
+        el.push_back(up[e].z);
+        en.push_back(4 * e + 2);
+        if (dw[e].z >= 0.0) { el.push_back(up[e].w); en.push_back(4 * e + 3); }
+      }
     build_csr(c->n_pad, el, en, off, idx);
     if ((rc = dalloc(c, &a->uidx, idx.size())) || (rc = put(c, a->uoff, off.data(), off.size())) ||
         (rc = put(c, a->uidx, idx.data(), idx.size())))
@@ -172,25 +196,63 @@ int to_user(cf_ctx* c, double* dst, const double* src, size_t count) {
   return CF_OK;
 }
 
+/* Per member, a device state (comps = 3: double4 states, h hu hv out) or scalar field (comps = 1)
+ * in the flat new order -> dst in member order, reference element order within a member. */
+int gather_members(cf_adjoint* a, const void* src, double* dst, int comps) {
+  cf_ctx* c = a->ctx;
+  const stream_t st = reinterpret_cast<stream_t>(c->stream);
+  int rc;
+  size_t off = 0;
+  for (const Member& M : c->mem) {
+    if (comps == 3)
+      rc = launch_gather_state(static_cast<const double4*>(src) + M.cell_off, c->iperm + M.cell_off, c->staging, M.n, st);
+    else
+      rc = launch_gather_scalar(static_cast<const double*>(src) + M.cell_off, c->iperm + M.cell_off, c->staging, M.n, st);
+    if (rc) return fail(c, rc, "gather launch failed");
+    if ((rc = to_user(c, dst + off, c->staging, (size_t)comps * M.n))) return rc;
+    off += (size_t)comps * M.n;
+  }
+  return CF_OK;
+}
+
 int forward_impl(cf_adjoint* a, int32_t replay, double* eta_out, double* state_out) {
   cf_ctx* c = a->ctx;
   if (replay && !a->recorded) return fail(c, CF_ESTATE, "replay before a recording forward");
   CF_CUDA(c, cudaSetDevice(c->device));
   int rc;
   if ((rc = read_states(c))) return rc;
-  const MemberState s = c->host_state[0];
-  if (s.status & STATUS_NO_STATE) return fail(c, CF_ESTATE, "no state set");
-  if (s.status) return fail(c, status_code(s.status), "the context's member is stopped");
-  const int cur = (int)((s.base + s.nstep) & 1);
   const stream_t st = reinterpret_cast<stream_t>(c->stream);
   const size_t np = (size_t)a->n_pad;
+  /* every member's current state into the first segment state, and the adjoint's own member
+   * records, all at one buffer parity p0 (members set at different times may differ) */
+  const int p0 = (int)(c->launched & 1);
+  std::vector<MemberState> ms(c->host_state, c->host_state + a->nm);
   a->have_traj = false;
-  CF_CUDA(c, cudaMemcpyAsync(a->seg, c->U[cur], np * sizeof(double4), cudaMemcpyDeviceToDevice, c->stream));
-  if (!replay) CF_CUDA(c, cudaMemcpyAsync(a->mst, c->mst, sizeof(MemberState), cudaMemcpyDeviceToDevice, c->stream));
+  for (int32_t i = 0; i < a->nm; ++i) {
+    MemberState& s = ms[i];
+    const std::string who = a->nm > 1 ? "member " + std::to_string(i) + ": " : std::string();
+    if (s.status & STATUS_NO_STATE) return fail(c, CF_ESTATE, who + "no state set");
+    if (s.status) {
+      const int code = status_code(s.status);
+      return fail(c, code != CF_OK ? code : CF_ESTATE, who + "the member is stopped");
+    }
+    const Member& M = c->mem[i];
+    const int cur = (int)((s.base + s.nstep) & 1);
+    CF_CUDA(c, cudaMemcpyAsync(a->seg + M.cell_off, c->U[cur] + M.cell_off, (size_t)M.n * sizeof(double4),
+                               cudaMemcpyDeviceToDevice, c->stream));
+    if (cur != p0) {
+      std::swap(s.dt[0], s.dt[1]);
+      std::swap(s.t[0], s.t[1]);
+      s.base ^= 1;
+    }
+    s.ts = INFINITY;   /* the adjoint's run has N steps: no end time */
+  }
+  if (!replay) CF_CUDA(c, cudaMemcpyAsync(a->mst, ms.data(), ms.size() * sizeof(MemberState), cudaMemcpyHostToDevice,
+                                          c->stream));
   CF_CUDA(c, cudaMemsetAsync(a->flag, 0, sizeof(uint32_t), c->stream));
   double4* X = a->seg;
   double4* Y = a->seg + np;
-  int p = cur;
+  int p = p0;
   for (int32_t k = 0; k < a->N; ++k) {
     if (k % a->K == 0)
       CF_CUDA(c, cudaMemcpyAsync(a->ckpt + (size_t)(k / a->K) * np, X, np * sizeof(double4), cudaMemcpyDeviceToDevice,
@@ -202,27 +264,25 @@ int forward_impl(cf_adjoint* a, int32_t replay, double* eta_out, double* state_o
     if (!replay) {
       sa.mst = a->mst;
       if ((rc = launch_step(sa, st, nullptr, nullptr))) return fail(c, rc, "step launch failed");
-      rc = launch_record(Y, a->mst, p, k, a->dt_hist, a->t_hist, a->gcell, a->G, a->eta, st);
+      rc = launch_record(Y, a->mst, a->nm, p, k, a->dt_hist, a->t_hist, a->gcell, a->G, a->eta, st);
     } else {
       if ((rc = launch_replay_step(sa, a->dt_hist, a->t_hist, k, a->flag, nullptr, st)))
         return fail(c, rc, "replay launch failed");
-      rc = launch_record(Y, nullptr, 0, k, a->dt_hist, a->t_hist, a->gcell, a->G, a->eta, st);
+      rc = launch_record(Y, nullptr, a->nm, 0, k, a->dt_hist, a->t_hist, a->gcell, a->G, a->eta, st);
     }
     if (rc) return fail(c, rc, "record launch failed");
     std::swap(X, Y);
     p ^= 1;
   }
-  if (state_out) {
-    if ((rc = launch_gather_state(X, c->iperm, c->staging, a->n, st))) return fail(c, rc, "gather launch failed");
-    if ((rc = to_user(c, state_out, c->staging, 3 * (size_t)a->n))) return rc;
-  }
+  if (state_out && (rc = gather_members(a, X, state_out, 3))) return rc;
   if ((rc = to_user(c, eta_out, a->eta, (size_t)a->N * a->G))) return rc;
-  MemberState ms{};
   uint32_t flag = 0;
-  CF_CUDA(c, cudaMemcpyAsync(&ms, a->mst, sizeof(ms), cudaMemcpyDeviceToHost, c->stream));
+  CF_CUDA(c, cudaMemcpyAsync(ms.data(), a->mst, ms.size() * sizeof(MemberState), cudaMemcpyDeviceToHost, c->stream));
   CF_CUDA(c, cudaMemcpyAsync(&flag, a->flag, sizeof(flag), cudaMemcpyDeviceToHost, c->stream));
   CF_CUDA(c, cudaStreamSynchronize(c->stream));
-  const uint32_t bad = replay ? flag : ms.status;
+  uint32_t bad = flag;
+  if (!replay)
+    for (const MemberState& s : ms) bad |= s.status;
   if (bad) {
     rc = status_code(bad);
     return fail(c, rc, rc == CF_EDT ? "dt left the range (1e-12, 9999] during the run" : "non-finite value in the state");
@@ -246,11 +306,17 @@ int backward_impl(cf_adjoint* a, const double* w_eta, const double* w_state, dou
   CF_CUDA(c, cudaMemsetAsync(a->lam[1], 0, np * sizeof(double4), c->stream));
   CF_CUDA(c, cudaMemsetAsync(a->gman, 0, np * sizeof(double), c->stream));
   if (w_state) {
-    CF_CUDA(c, cudaMemcpyAsync(c->staging, w_state, 3 * (size_t)a->n * sizeof(double), cudaMemcpyDefault, c->stream));
-    if ((rc = launch_scatter_state(c->staging, c->perm, c->zcell, a->lam[0], a->n, st)))
-      return fail(c, rc, "scatter launch failed");
+    size_t off = 0;
+    for (const Member& M : c->mem) {
+      CF_CUDA(c, cudaMemcpyAsync(c->staging, w_state + off, 3 * (size_t)M.n * sizeof(double), cudaMemcpyDefault,
+                                 c->stream));
+      if ((rc = launch_scatter_state(c->staging, c->perm + M.cell_off, c->zcell + M.cell_off, a->lam[0] + M.cell_off,
+                                     M.n, st)))
+        return fail(c, rc, "scatter launch failed");
+      off += 3 * (size_t)M.n;
+    }
   }
-  if (weights && (rc = launch_add_gauges(a->lam[0], a->goff, a->gidx, a->wbuf + (size_t)(a->N - 1) * a->G, a->n, st)))
+  if (weights && (rc = launch_add_gauges(a->lam[0], a->goff, a->gidx, a->wbuf + (size_t)(a->N - 1) * a->G, a->n_pad, st)))
     return fail(c, rc, "gauge launch failed");
   /* lam[0] = lambda^N; lam[1] = the own part of lambda^k, carried from reverse step to reverse
    * step (the edge contributions are gathered by the next reverse step, or the final pass). */
@@ -297,15 +363,8 @@ int backward_impl(cf_adjoint* a, const double* w_eta, const double* w_state, dou
   }
   if ((rc = launch_adjoint_final(A, st))) return fail(c, rc, "adjoint launch failed");
   double4* Lin = a->lam[1];
-  if (g_state0) {
-    if ((rc = launch_gather_state(Lin, c->iperm, c->staging, a->n, st))) return fail(c, rc, "gather launch failed");
-    if ((rc = to_user(c, g_state0, c->staging, 3 * (size_t)a->n))) return rc;
-  }
-  if (g_manning) {
-    CF_CUDA(c, cudaStreamSynchronize(c->stream));  /* staging is reused */
-    if ((rc = launch_gather_scalar(a->gman, c->iperm, c->staging, a->n, st))) return fail(c, rc, "gather launch failed");
-    if ((rc = to_user(c, g_manning, c->staging, (size_t)a->n))) return rc;
-  }
+  if (g_state0 && (rc = gather_members(a, Lin, g_state0, 3))) return rc;
+  if (g_manning && (rc = gather_members(a, a->gman, g_manning, 1))) return rc;
   CF_CUDA(c, cudaStreamSynchronize(c->stream));
   return CF_OK;
 }
@@ -314,23 +373,37 @@ int backward_impl(cf_adjoint* a, const double* w_eta, const double* w_state, dou
 
 extern "C" {
 
-int cf_set_manning(cf_ctx* c, const double* n_elt) {
+int cf_member_set_manning(cf_ctx* c, int32_t member, const double* n_elt) {
   if (!c) return CF_EINVAL;
   if (!n_elt) return fail(c, CF_EINVAL, "null argument");
-  if (c->mem.size() != 1) return fail(c, CF_ENOTSUP, "cf_set_manning takes a context with one member");
+  if (member < 0 || member >= (int32_t)c->mem.size()) return fail(c, CF_EINVAL, "member index out of range");
   CF_CUDA(c, cudaSetDevice(c->device));
-  const Member& M = c->mem[0];
+  const Member& M = c->mem[member];
   CF_CUDA(c, cudaMemcpyAsync(c->staging, n_elt, (size_t)M.n * sizeof(double), cudaMemcpyDefault, c->stream));
-  int rc = launch_set_manning(c->cstat, c->perm, c->staging, M.n, reinterpret_cast<stream_t>(c->stream));
+  int rc = launch_set_manning(c->cstat + M.cell_off, c->perm + M.cell_off, c->staging, M.n,
+                              reinterpret_cast<stream_t>(c->stream));
   if (rc != CF_OK) return fail(c, rc, "manning launch failed");
   CF_CUDA(c, cudaStreamSynchronize(c->stream));
   return CF_OK;
 }
 
+int cf_set_manning(cf_ctx* c, const double* n_elt) {
+  if (!c) return CF_EINVAL;
+  if (c->mem.size() != 1) return fail(c, CF_ENOTSUP, "cf_set_manning takes a context with one member");
+  return cf_member_set_manning(c, 0, n_elt);
+}
+
 int cf_adjoint_create(cf_ctx* ctx, int32_t nsteps, int32_t checkpoint_interval, const int32_t* gauges,
                       int32_t ngauges, cf_adjoint** out) {
   if (!ctx) return CF_EINVAL;
-  return create_impl(ctx, nsteps, checkpoint_interval, gauges, ngauges, out);
+  return create_impl(ctx, nsteps, checkpoint_interval, nullptr, gauges, ngauges, out);
+}
+
+int cf_adjoint_create_batch(cf_ctx* ctx, int32_t nsteps, int32_t checkpoint_interval, const int32_t* gauge_member,
+                            const int32_t* gauges, int32_t ngauges, cf_adjoint** out) {
+  if (!ctx) return CF_EINVAL;
+  if (ngauges > 0 && !gauge_member) return fail(ctx, CF_EINVAL, "gauge_member is NULL");
+  return create_impl(ctx, nsteps, checkpoint_interval, gauge_member, gauges, ngauges, out);
 }
 
 void cf_adjoint_destroy(cf_adjoint* a) {
@@ -358,7 +431,8 @@ int cf_adjoint_get_dt(cf_adjoint* a, double* dt, double* t) {
   if (!a->recorded) return fail(c, CF_ESTATE, "no recorded dt sequence");
   CF_CUDA(c, cudaSetDevice(c->device));
   int rc;
-  if ((rc = to_user(c, dt, a->dt_hist, (size_t)a->N)) || (rc = to_user(c, t, a->t_hist, (size_t)a->N))) return rc;
+  const size_t nh = (size_t)a->N * a->nm;
+  if ((rc = to_user(c, dt, a->dt_hist, nh)) || (rc = to_user(c, t, a->t_hist, nh))) return rc;
   CF_CUDA(c, cudaStreamSynchronize(c->stream));
   return CF_OK;
 }
@@ -367,8 +441,9 @@ int cf_adjoint_set_dt(cf_adjoint* a, const double* dt, const double* t) {
   if (!a || !dt || !t) return a ? fail(a->ctx, CF_EINVAL, "null argument") : CF_EINVAL;
   cf_ctx* c = a->ctx;
   CF_CUDA(c, cudaSetDevice(c->device));
-  CF_CUDA(c, cudaMemcpyAsync(a->dt_hist, dt, (size_t)a->N * sizeof(double), cudaMemcpyDefault, c->stream));
-  CF_CUDA(c, cudaMemcpyAsync(a->t_hist, t, (size_t)a->N * sizeof(double), cudaMemcpyDefault, c->stream));
+  const size_t nh = (size_t)a->N * a->nm;
+  CF_CUDA(c, cudaMemcpyAsync(a->dt_hist, dt, nh * sizeof(double), cudaMemcpyDefault, c->stream));
+  CF_CUDA(c, cudaMemcpyAsync(a->t_hist, t, nh * sizeof(double), cudaMemcpyDefault, c->stream));
   CF_CUDA(c, cudaStreamSynchronize(c->stream));
   a->recorded = true;
   a->have_traj = false;
@@ -391,10 +466,105 @@ int cf_adjoint_sizes(cf_adjoint* a, int32_t* nsteps, int32_t* interval, int32_t*
     const int64_t np = a->n_pad, nep = a->ctx->ne_pad;
     int64_t b = (int64_t)(a->nseg + a->nseg_states + 2) * np * (int64_t)sizeof(double4) +
                 (int64_t)(a->nseg_states + 1) * np * (int64_t)sizeof(Slot) +
-                2 * nep * (int64_t)sizeof(double4) + np * 8 + (int64_t)a->N * (16 + 16 * (int64_t)a->G);
+                2 * nep * (int64_t)sizeof(double4) + np * 8 + (int64_t)a->N * (16 * (int64_t)a->nm + 16 * (int64_t)a->G);
     if (a->uadj) b += 4 * nep * (int64_t)sizeof(double4);
     *device_bytes = b;
   }
+  return CF_OK;
+}
+
+/* ---- Manning zones ------------------------------------------------------------------------ */
+
+int cf_zones_create(cf_ctx* c, const int32_t* zone_of_elem, int32_t nzones, cf_zones** out) {
+  if (!c) return CF_EINVAL;
+  if (!out || !zone_of_elem || nzones < 1) return fail(c, CF_EINVAL, "null argument or nzones < 1");
+  *out = nullptr;
+  CF_CUDA(c, cudaSetDevice(c->device));
+  /* zone of every element in the flat new order; CSR zone -> elements in ascending new order */
+  std::vector<int32_t> zone_new((size_t)c->n_pad, -1), el, zn;
+  size_t off = 0;
+  for (const Member& M : c->mem) {
+    for (int32_t o = 0; o < M.n; ++o) {
+      const int32_t z = zone_of_elem[off + o];
+      if (z < -1 || z >= nzones) return fail(c, CF_EINVAL, "zone id out of range");
+      zone_new[(size_t)M.cell_off + M.prep.iperm[o]] = z;
+    }
+    off += (size_t)M.n;
+  }
+  for (int32_t i = 0; i < c->n_pad; ++i)
+    if (zone_new[i] >= 0) { zn.push_back(zone_new[i]); el.push_back(i); }
+  std::vector<int32_t> zoff, zidx;
+  build_csr(nzones, zn, el, zoff, zidx);
+  cf_zones* z = new (std::nothrow) cf_zones();
+  if (!z) return fail(c, CF_ENOMEM, "host allocation failed");
+  z->ctx = c;
+  z->nz = nzones;
+  int rc;
+  if ((rc = dalloc(c, &z->zoff, zoff.size())) || (rc = dalloc(c, &z->zidx, zidx.size())) ||
+      (rc = dalloc(c, &z->zone_of, zone_new.size())) || (rc = dalloc(c, &z->gz, (size_t)nzones)) ||
+      (rc = dalloc(c, &z->vals, (size_t)nzones)) || (rc = put(c, z->zoff, zoff.data(), zoff.size())) ||
+      (rc = put(c, z->zidx, zidx.data(), zidx.size())) || (rc = put(c, z->zone_of, zone_new.data(), zone_new.size()))) {
+    cf_zones_destroy(z);
+    return rc;
+  }
+  *out = z;
+  return CF_OK;
+}
+
+void cf_zones_destroy(cf_zones* z) {
+  if (!z) return;
+  cudaSetDevice(z->ctx->device);
+  cudaStreamSynchronize(z->ctx->stream);
+  void* ptrs[] = {z->zoff, z->zidx, z->zone_of, z->gz, z->vals};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  delete z;
+}
+
+int cf_zones_set(cf_zones* z, const double* values) {
+  if (!z) return CF_EINVAL;
+  cf_ctx* c = z->ctx;
+  if (!values) return fail(c, CF_EINVAL, "null argument");
+  CF_CUDA(c, cudaSetDevice(c->device));
+  CF_CUDA(c, cudaMemcpyAsync(z->vals, values, (size_t)z->nz * sizeof(double), cudaMemcpyDefault, c->stream));
+  int rc = launch_zone_apply(c->cstat, z->zone_of, z->vals, c->n_pad, reinterpret_cast<stream_t>(c->stream));
+  if (rc) return fail(c, rc, "zone launch failed");
+  CF_CUDA(c, cudaStreamSynchronize(c->stream));
+  return CF_OK;
+}
+
+int cf_zones_get(cf_zones* z, double* values, double* gradient) {
+  if (!z) return CF_EINVAL;
+  cf_ctx* c = z->ctx;
+  CF_CUDA(c, cudaSetDevice(c->device));
+  int rc;
+  if ((rc = to_user(c, values, z->vals, (size_t)z->nz)) || (rc = to_user(c, gradient, z->gz, (size_t)z->nz))) return rc;
+  CF_CUDA(c, cudaStreamSynchronize(c->stream));
+  return CF_OK;
+}
+
+int cf_zones_gradient(cf_zones* z, cf_adjoint* a, double* gradient) {
+  if (!z || !a) return CF_EINVAL;
+  cf_ctx* c = z->ctx;
+  if (a->ctx != c) return fail(c, CF_EINVAL, "the zones and the adjoint belong to different contexts");
+  CF_CUDA(c, cudaSetDevice(c->device));
+  int rc = launch_zone_sum(a->gman, z->zoff, z->zidx, z->gz, z->nz, reinterpret_cast<stream_t>(c->stream));
+  if (rc) return fail(c, rc, "zone launch failed");
+  if ((rc = to_user(c, gradient, z->gz, (size_t)z->nz))) return rc;
+  CF_CUDA(c, cudaStreamSynchronize(c->stream));
+  return CF_OK;
+}
+
+int cf_zones_descend(cf_zones* z, double lr, double lo, double hi) {
+  if (!z) return CF_EINVAL;
+  cf_ctx* c = z->ctx;
+  if (!(lo <= hi)) return fail(c, CF_EINVAL, "lo > hi");
+  CF_CUDA(c, cudaSetDevice(c->device));
+  const stream_t st = reinterpret_cast<stream_t>(c->stream);
+  int rc = launch_zone_step(z->vals, z->gz, z->nz, lr, lo, hi, st);
+  if (rc == CF_OK) rc = launch_zone_apply(c->cstat, z->zone_of, z->vals, c->n_pad, st);
+  if (rc) return fail(c, rc, "zone launch failed");
+  CF_CUDA(c, cudaStreamSynchronize(c->stream));
   return CF_OK;
 }
 

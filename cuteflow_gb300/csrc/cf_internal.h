@@ -186,8 +186,8 @@ int launch_gather_state(const double4* U, const int32_t* iperm_old2new, double* 
 /* One reverse step n: s holds the step's buffers with s.Uin = U^n. */
 struct AdjArgs {
   StepArgs s;
-  const double* dt_hist;   /* dt of every step (frozen) */
-  const double* t_hist;    /* start time of every step */
+  const double* dt_hist;   /* dt of every step and member (frozen), [N][members] */
+  const double* t_hist;    /* start time of every step and member */
   int32_t n;
   int32_t gather;          /* 1: lambda^{n+1} = lam_own + the edge contributions; 0: lam_init */
   const Slot* sums;        /* per element: its flux sums (f1..f3) and bed sums (bx, by) at U^n */
@@ -211,7 +211,7 @@ struct AdjArgs {
 int launch_replay_step(const StepArgs& a, const double* dt_hist, const double* t_hist, int n, uint32_t* flag,
                        Slot* sums, stream_t s);
 /* gauge elevations of Unew into eta row n; with S, also dt / t of parity p into the histories */
-int launch_record(const double4* Unew, const MemberState* S, int p, int n, double* dt_hist, double* t_hist,
+int launch_record(const double4* Unew, const MemberState* S, int nm, int p, int n, double* dt_hist, double* t_hist,
                   const int32_t* gcell, int G, double* eta, stream_t s);
 int launch_adjoint_step(const AdjArgs& A, stream_t s);
 /* lambda^0 = lam_own + the edge contributions of the last reverse step, into lam_own */
@@ -219,6 +219,11 @@ int launch_adjoint_final(const AdjArgs& A, stream_t s);
 int launch_add_gauges(double4* lam, const int32_t* goff, const int32_t* gidx, const double* gw, int32_t n, stream_t s);
 int launch_gather_scalar(const double* x, const int32_t* iperm, double* out, int32_t n, stream_t s);
 int launch_set_manning(double4* cstat, const int32_t* perm, const double* nref, int32_t n, stream_t s);
+/* Manning zones: fixed-order zone sums of dJ/dn (CSR zone -> elements, new order), a projected
+ * gradient step on the zone values, and the zone values into every element's n */
+int launch_zone_sum(const double* gman, const int32_t* zoff, const int32_t* zidx, double* gz, int32_t nz, stream_t s);
+int launch_zone_step(double* v, const double* g, int32_t nz, double lr, double lo, double hi, stream_t s);
+int launch_zone_apply(double4* cstat, const int32_t* zone_of, const double* v, int32_t n, stream_t s);
 
 /* ---- context helpers for the static-scratch entry point (cf_api.cpp) ---------------- */
 

@@ -86,6 +86,18 @@ def load(build_if_missing: bool = True):
     L.cf_adjoint_set_dt.argtypes = [vp, vp, vp]
     L.cf_adjoint_sizes.argtypes = [vp, ip, ip, ip, C.POINTER(C.c_int64)]
     L.cf_adjoint_set_linearization.argtypes = [vp, C.c_int32]
+    L.cf_adjoint_create_batch.argtypes = [vp, C.c_int32, C.c_int32, ip, ip, C.c_int32, vpp]
+    L.cf_member_set_manning.argtypes = [vp, C.c_int32, vp]
+    L.cf_zones_create.argtypes = [vp, ip, C.c_int32, vpp]
+    L.cf_zones_destroy.argtypes = [vp]
+    L.cf_zones_destroy.restype = None
+    L.cf_zones_set.argtypes = [vp, vp]
+    L.cf_zones_get.argtypes = [vp, vp, vp]
+    L.cf_zones_gradient.argtypes = [vp, vp, vp]
+    L.cf_zones_descend.argtypes = [vp, C.c_double, C.c_double, C.c_double]
+    for name in ("cf_adjoint_create_batch", "cf_member_set_manning", "cf_zones_create", "cf_zones_set",
+                 "cf_zones_get", "cf_zones_gradient", "cf_zones_descend"):
+        getattr(L, name).restype = C.c_int
     for name in ("cf_set_manning", "cf_adjoint_create", "cf_adjoint_forward", "cf_adjoint_backward",
                  "cf_adjoint_get_dt", "cf_adjoint_set_dt", "cf_adjoint_sizes", "cf_adjoint_set_linearization"):
         getattr(L, name).restype = C.c_int
@@ -305,6 +317,15 @@ class Batch:
         if check:
             self._check(rc)
         return [_info(i) for i in infos]
+
+    def set_manning(self, member: int, n):
+        """Per-element Manning n of one member (reference order; host array or device address)."""
+        if isinstance(n, int):
+            self._check(self._L.cf_member_set_manning(self._ctx, int(member), C.c_void_p(n)))
+            return
+        n = np.ascontiguousarray(n, dtype=np.float64)
+        assert n.shape == (self.nelt[member],)
+        self._check(self._L.cf_member_set_manning(self._ctx, int(member), n.ctypes.data_as(C.c_void_p)))
 
     def get_state(self, member: int) -> np.ndarray:
         out = np.empty((self.nelt[member], 3))

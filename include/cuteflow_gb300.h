@@ -250,7 +250,7 @@ int cf_get_timing(cf_ctx* ctx, double* flux_ms, double* update_ms, int64_t* laun
  * For Manning calibration: gradients of an objective on gauge elevations and on the final
  * state with respect to the per-element Manning n and the initial state, by the discrete
  * adjoint of the step (the dt of every step held at its recorded value).  Contexts with one
- * member.
+ * member, or the members of a batch (cf_adjoint_create_batch).
  *
  *   J = sum_{k=1..N} sum_g w_eta[(k-1)*G + g] * eta^k_g  +  sum_e w_state[3e..3e+2] . U^N_e
  *
@@ -259,13 +259,21 @@ int cf_get_timing(cf_ctx* ctx, double* flux_ms, double* update_ms, int64_t* laun
  * device memory. */
 typedef struct cf_adjoint cf_adjoint;
 
-/* Per-element Manning n [nelt], reference order (replaces the mesh's values and the override). */
+/* Per-element Manning n [nelt], reference order (replaces the mesh's values and the override);
+ * cf_set_manning for a one-member context, cf_member_set_manning for member m of a batch. */
 int cf_set_manning(cf_ctx* ctx, const double* n_elt);
+int cf_member_set_manning(cf_ctx* ctx, int32_t member, const double* n_elt);
 
 /* An adjoint of N steps with G gauges; checkpoint_interval K (0: ceil(sqrt(N))): the state is
  * kept every K steps, ceil(N/K) + max(K, 2) states of device memory. */
 int cf_adjoint_create(cf_ctx* ctx, int32_t nsteps, int32_t checkpoint_interval, const int32_t* gauges,
                       int32_t ngauges, cf_adjoint** out);
+/* The adjoint of a batch: every member runs the same N steps with its own dt, in the same
+ * launches.  Gauge g is element gauges[g] (0-based, reference order) of member gauge_member[g].
+ * States, weights and gradients of the run functions are concatenated in member order
+ * ([sum of nelt] elements); the dt / time histories are [N][members]. */
+int cf_adjoint_create_batch(cf_ctx* ctx, int32_t nsteps, int32_t checkpoint_interval, const int32_t* gauge_member,
+                            const int32_t* gauges, int32_t ngauges, cf_adjoint** out);
 void cf_adjoint_destroy(cf_adjoint* adj);
 
 /* N steps from the context's current state (which is left unchanged).  replay 0: the dt of
@@ -294,6 +302,21 @@ int cf_adjoint_set_dt(cf_adjoint* adj, const double* dt, const double* t);
 int cf_adjoint_set_linearization(cf_adjoint* adj, int32_t mode);
 int cf_adjoint_sizes(cf_adjoint* adj, int32_t* nsteps, int32_t* checkpoint_interval, int32_t* ngauges,
                      int64_t* device_bytes);
+
+/* Manning zones for calibration on the device.  zone_of_elem [sum of nelt] (member order,
+ * reference order within a member) gives every element's zone in 0..nzones-1, or -1 for an
+ * element whose n is not a parameter.  cf_zones_set writes zone values (host or device
+ * memory) into every zoned element's n; cf_zones_gradient sums the adjoint's last dJ/dn over
+ * each zone in a fixed order (deterministic); cf_zones_descend takes the projected gradient
+ * step v = min(hi, max(lo, v - lr g)) on the device and writes the new n, so that a
+ * calibration loop (forward, backward, gradient, descend) needs no host round trip. */
+typedef struct cf_zones cf_zones;
+int cf_zones_create(cf_ctx* ctx, const int32_t* zone_of_elem, int32_t nzones, cf_zones** out);
+void cf_zones_destroy(cf_zones* z);
+int cf_zones_set(cf_zones* z, const double* values);
+int cf_zones_get(cf_zones* z, double* values, double* gradient);
+int cf_zones_gradient(cf_zones* z, cf_adjoint* adj, double* gradient /* may be NULL */);
+int cf_zones_descend(cf_zones* z, double lr, double lo, double hi);
 
 /* ---- stepping without allocation (no counterpart in the reference) --------------------
  *
