@@ -293,6 +293,11 @@ def run_ours(args):
         if pg is not None:
             pg.barrier()
 
+    # ---- autotuner: how the edge kernel shares FP64 work with the integer pipes (identical
+    # results in every setting); the trials run on the initial state, which is restored ----
+    s.set_state(case.U0)
+    tune = s.autotune(30) if not args.no_tune else (0, 0, None)
+
     # ---- device-resident throughput (value) ----
     s.set_state(case.U0)
     s.step(args.warmup)
@@ -364,7 +369,8 @@ def run_ours(args):
         "config": {"workload": case.name, "triangles": n, "edges": s.nedge,
                    "scheme": {1: "HLLC", 2: "HLLC-Ata", 3: "WAF", 4: "MUSCL-Hancock"}[case.params["iflux"]],
                    "l2": "working set > L2 (no flush needed)", "parallelism": f"replicas x{world}",
-                   "time_steps_ran": info.steps},
+                   "time_steps_ran": info.steps,
+                   "tuning": {"int_compare": tune[0], "int_mul_warps": tune[1], "trial_ms_per_step": tune[2]}},
         "roofline": {"bound": "hbm", "kernel": "one time step (k_edges + k_cells)",
                      "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "peak_source": f"MEASURED_PEAKS.json hbm_gbs ({hbm_src})",
@@ -404,6 +410,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="flooding", choices=["flooding", "flooding_muscl", "dam_break", "ensemble"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (every operation on the FP64 pipe)")
     ap.add_argument("--batched-members", type=int, default=32, help="ensemble sample beside the plain line (0: skip)")
     ap.add_argument("--batched-steps", type=int, default=200)
     ap.add_argument("--adjoint-steps", type=int, default=3000,

@@ -23,7 +23,7 @@ NVCC = os.path.join(CUDA_HOME, "bin", "nvcc") if os.path.exists(os.path.join(CUD
 
 CU_SOURCES = ["cf_kernels.cu", "cf_noalloc.cu", "cf_adjoint.cu"]
 CPP_SOURCES = ["cf_mesh.cpp", "cf_api.cpp", "cf_adjoint_api.cpp", "cf_io.cpp"]
-HEADERS = ["cf_internal.h", "cf_flux.h", "cf_dual.h", "cf_ctx.h"]
+HEADERS = ["cf_internal.h", "cf_flux.h", "cf_dual.h", "cf_ctx.h", "cf_xd.h"]
 
 
 def _sources():

@@ -73,6 +73,8 @@ StepArgs step_args(const cf_ctx* c, int parity) {
   a.nmembers = (int32_t)c->mem.size();
   a.phys_inflow = c->any_phys_inflow ? 1 : 0;
   a.steady = c->any_steady ? 1 : 0;
+  a.xd_cmp = c->xd_cmp;
+  a.xd_mul_mask = c->xd_mul_mask;
   return a;
 }
 
@@ -601,6 +603,97 @@ extern "C" {
 int cf_run(cf_ctx* ctx, double ts, int64_t max_steps, cf_step_info* info) {
   if (!ctx) return CF_EINVAL;
   return run_impl(ctx, ts, max_steps, info);
+}
+
+int cf_set_tuning(cf_ctx* ctx, int32_t int_compare, int32_t int_mul_warps) {
+  if (!ctx) return CF_EINVAL;
+  if (int_compare < 0 || int_compare > 1 || int_mul_warps < 0 || int_mul_warps > 0xf)
+    return fail(ctx, CF_EINVAL, "int_compare must be 0/1 and int_mul_warps a 4-bit warp mask");
+  if (int_mul_warps && !int_compare) return fail(ctx, CF_EINVAL, "integer products need int_compare = 1");
+  if (ctx->xd_cmp != int_compare || ctx->xd_mul_mask != int_mul_warps) {
+    ctx->xd_cmp = int_compare;
+    ctx->xd_mul_mask = int_mul_warps;
+    if (ctx->graph2) {   /* the captured steps hold the old arguments */
+      CF_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+      cudaGraphExecDestroy(ctx->graph2);
+      ctx->graph2 = nullptr;
+    }
+  }
+  return CF_OK;
+}
+
+int cf_get_tuning(cf_ctx* ctx, int32_t* int_compare, int32_t* int_mul_warps) {
+  if (!ctx) return CF_EINVAL;
+  if (int_compare) *int_compare = ctx->xd_cmp;
+  if (int_mul_warps) *int_mul_warps = ctx->xd_mul_mask;
+  return CF_OK;
+}
+
+int cf_autotune(cf_ctx* ctx, int32_t steps_per_trial, int32_t* int_compare, int32_t* int_mul_warps, double* ms_per_step) {
+  if (!ctx) return CF_EINVAL;
+  cf_ctx* c = ctx;
+  if (steps_per_trial < 2) return fail(c, CF_EINVAL, "steps_per_trial < 2");
+  CF_CUDA(c, cudaSetDevice(c->device));
+  int rc;
+  if ((rc = read_states(c))) return rc;
+  for (size_t i = 0; i < c->mem.size(); ++i)
+    if (c->host_state[i].status) return fail(c, CF_ESTATE, "cf_autotune needs every member set and running");
+  /* the trials step the context's own state; it is restored after each one (both buffers,
+   * the member records and the launch count), so tuning leaves the simulation unchanged */
+  const size_t np = (size_t)c->n_pad, nm = c->mem.size();
+  double4* saved = nullptr;
+  CF_CUDA(c, cudaMalloc((void**)&saved, 2 * np * sizeof(double4)));
+  std::vector<MemberState> ms(c->host_state, c->host_state + nm);
+  const int64_t launched0 = c->launched;
+  const int32_t cmp0 = c->xd_cmp, mul0 = c->xd_mul_mask;
+  auto restore = [&]() -> int {
+    CF_CUDA(c, cudaMemcpyAsync(c->U[0], saved, np * sizeof(double4), cudaMemcpyDeviceToDevice, c->stream));
+    CF_CUDA(c, cudaMemcpyAsync(c->U[1], saved + np, np * sizeof(double4), cudaMemcpyDeviceToDevice, c->stream));
+    CF_CUDA(c, cudaMemcpyAsync(c->mst, ms.data(), nm * sizeof(MemberState), cudaMemcpyHostToDevice, c->stream));
+    CF_CUDA(c, cudaStreamSynchronize(c->stream));
+    c->launched = launched0;
+    return CF_OK;
+  };
+  cudaError_t e = cudaMemcpyAsync(saved, c->U[0], np * sizeof(double4), cudaMemcpyDeviceToDevice, c->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(saved + np, c->U[1], np * sizeof(double4), cudaMemcpyDeviceToDevice, c->stream);
+  if (e != cudaSuccess) {
+    cudaFree(saved);
+    return cuda_fail(c, e, "cudaMemcpyAsync");
+  }
+  /* candidates: all on the FP64 pipe; comparisons on the integer pipes; comparisons and all
+   * products; comparisons and the products of half the warps */
+  const int32_t cand[4][2] = {{0, 0}, {1, 0}, {1, 0xf}, {1, 0x5}};
+  double best = 1e300;
+  int32_t bc = 0, bm = 0;
+  rc = CF_OK;
+  for (const auto& k : cand) {
+    if ((rc = cf_set_tuning(c, k[0], k[1]))) break;
+    if ((rc = step_impl(c, 2, nullptr))) break;  /* warm-up (and graph build) */
+    CF_CUDA(c, cudaEventRecord(c->ev[0], c->stream));
+    if ((rc = step_impl(c, steps_per_trial, nullptr))) break;
+    CF_CUDA(c, cudaEventRecord(c->ev[1], c->stream));
+    CF_CUDA(c, cudaEventSynchronize(c->ev[1]));
+    float t = 0.f;
+    cudaEventElapsedTime(&t, c->ev[0], c->ev[1]);
+    if ((rc = restore())) break;
+    const double per = t / steps_per_trial;
+    if (per < best) {
+      best = per;
+      bc = k[0];
+      bm = k[1];
+    }
+  }
+  cudaFree(saved);
+  if (rc != CF_OK) {
+    cf_set_tuning(c, cmp0, mul0);
+    restore();
+    return rc;
+  }
+  if ((rc = cf_set_tuning(c, bc, bm))) return rc;
+  if (int_compare) *int_compare = bc;
+  if (int_mul_warps) *int_mul_warps = bm;
+  if (ms_per_step) *ms_per_step = best;
+  return CF_OK;
 }
 
 int cf_default_params(cf_params* p) {

@@ -802,7 +802,7 @@ CF_HD CF_INLINE void write_slots(Slot* sa, const double o[10]) {
 
 /* Fluxes (times the edge length) and bed sources of edge e into its two slots, from the
  * state U of step n: the body of the edge kernel. */
-template <int IFLUX>
+template <int IFLUX, class S = double>
 CF_HD CF_INLINE void edge_body(const StepArgs& a, const MemberDev& M, int e, double dt, double t,
                                const double* surf = nullptr) {
   const int2 ab = ldro(a.ecell + e);
@@ -846,8 +846,12 @@ CF_HD CF_INLINE void edge_body(const StepArgs& a, const MemberDev& M, int e, dou
     upwind_state(a.Uin, up.x, up.y, dw.x, dw.y, G.ysum_a, G.nx, G.ny, M.tolisec, hl_upw, vl_upw, zl_upw);
     upwind_state(a.Uin, up.z, up.w, dw.z, dw.w, G.ysum_b, G.nx, G.ny, M.tolisec, hr_upw, vr_upw, zr_upw);
   }
-  interior_edge<(IFLUX == 4 ? 3 : IFLUX)>(M, a.ilimiteur, a.flux_mode, G, dt, UA.x, UA.y, UA.z, UA.w, UB.x, UB.y,
-                                          UB.z, UB.w, hl_upw, vl_upw, zl_upw, hr_upw, vr_upw, zr_upw, o);
+  S os[10];
+  interior_edge<(IFLUX == 4 ? 3 : IFLUX)>(M, a.ilimiteur, a.flux_mode, G, dt, S(UA.x), S(UA.y), S(UA.z), UA.w,
+                                          S(UB.x), S(UB.y), S(UB.z), UB.w, S(hl_upw), S(vl_upw), zl_upw, S(hr_upw),
+                                          S(vr_upw), zr_upw, os);
+#pragma unroll
+  for (int i = 0; i < 10; ++i) o[i] = val(os[i]);
   write_slots(sa, o);
 }
 

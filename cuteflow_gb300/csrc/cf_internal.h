@@ -117,6 +117,9 @@ struct StepArgs {
   int32_t nmembers;
   int32_t phys_inflow;       /* some member uses inlet 3: k_surf runs before the edges */
   int32_t steady;            /* some member tests for steady state: k_steady runs after the cells */
+  int32_t xd_cmp;            /* edge kernel: 1 = comparisons on integer keys (cf_xd.h) */
+  int32_t xd_mul_mask;       /* edge kernel, with xd_cmp: warps w of a block with bit w set multiply
+                                on the integer pipes */
 };
 
 /* ---- host preprocessing (cf_mesh.cpp) ---------------------------------------------- */

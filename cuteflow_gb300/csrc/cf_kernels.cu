@@ -29,6 +29,7 @@
 #include <cstdio>
 
 #include "cf_flux.h"
+#include "cf_xd.h"
 
 namespace cf {
 namespace {
@@ -65,7 +66,14 @@ __global__ void __launch_bounds__(TILE_E) k_edges(StepArgs a) {
     }
   }
   if (e >= M.edge_end) return;
-  edge_body<IFLUX>(a, M, e, dt, t, S->surf);
+  if (IFLUX <= 3 && a.xd_cmp) {
+    /* the same arithmetic with exact integer comparisons and, in the warps of xd_mul_mask,
+     * exact integer products: the FP64 pipe and the integer pipes share the work */
+    if ((a.xd_mul_mask >> (threadIdx.x >> 5)) & 1) edge_body<IFLUX, XD<true>>(a, M, e, dt, t, S->surf);
+    else edge_body<IFLUX, XD<false>>(a, M, e, dt, t, S->surf);
+  } else {
+    edge_body<IFLUX>(a, M, e, dt, t, S->surf);
+  }
 }
 
 /* phys_inflow: per member (one warp) and inlet, calcul_surf_entree (maillage.cuf:1368-1421)

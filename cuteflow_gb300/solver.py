@@ -55,6 +55,9 @@ def load(build_if_missing: bool = True):
     L.cf_step.argtypes = [vp, C.c_int32, C.POINTER(_abi.CfStepInfo)]
     L.cf_step_noalloc.argtypes = [vp, C.c_int32, C.POINTER(_abi.CfStepInfo)]
     L.cf_run.argtypes = [vp, C.c_double, C.c_int64, C.POINTER(_abi.CfStepInfo)]
+    L.cf_set_tuning.argtypes = [vp, C.c_int32, C.c_int32]
+    L.cf_get_tuning.argtypes = [vp, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
+    L.cf_autotune.argtypes = [vp, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_int32), dp]
     L.cf_get_state.argtypes = [vp, dp]
     L.cf_get_state_device.argtypes = [vp, vp]
     L.cf_get_info.argtypes = [vp, C.POINTER(_abi.CfStepInfo)]
@@ -105,7 +108,8 @@ def load(build_if_missing: bool = True):
                  "cf_member_get_state", "cf_member_get_info", "cf_member_get_mesh_tables"):
         getattr(L, name).restype = C.c_int
     for name in ("cf_default_params", "cf_create", "cf_set_state", "cf_set_state_device",
-                 "cf_set_initial_condition", "cf_step", "cf_step_noalloc", "cf_run", "cf_get_state", "cf_get_state_device",
+                 "cf_set_initial_condition", "cf_step", "cf_step_noalloc", "cf_run", "cf_set_tuning",
+                 "cf_get_tuning", "cf_autotune", "cf_get_state", "cf_get_state_device",
                  "cf_get_info", "cf_get_mesh_tables", "cf_mesh_tables", "cf_get_sizes", "cf_set_timing", "cf_get_timing"):
         getattr(L, name).restype = C.c_int
     _lib = L
@@ -210,6 +214,23 @@ class Solver:
             self._check(rc)
         return _info(info)
 
+    def set_tuning(self, int_compare: int, int_mul_warps: int):
+        """cf_set_tuning: share the edge kernel's FP64 work with the integer pipes (results
+        identical in every setting)."""
+        self._check(self._L.cf_set_tuning(self._ctx, int(int_compare), int(int_mul_warps)))
+
+    def tuning(self):
+        a, b = C.c_int32(), C.c_int32()
+        self._check(self._L.cf_get_tuning(self._ctx, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
+    def autotune(self, steps_per_trial: int = 50):
+        """cf_autotune: time each setting on the current state (restored afterwards) and keep
+        the fastest; returns (int_compare, int_mul_warps, ms_per_step)."""
+        a, b, t = C.c_int32(), C.c_int32(), C.c_double()
+        self._check(self._L.cf_autotune(self._ctx, int(steps_per_trial), C.byref(a), C.byref(b), C.byref(t)))
+        return a.value, b.value, t.value
+
     def run(self, ts: float, max_steps: int = 1 << 40, check: bool = True) -> StepInfo:
         """The reference's time loop up to time ts (cf_run): stops with CF_STATUS_END, or at a
         steady state, or after max_steps steps."""
@@ -309,6 +330,12 @@ class Batch:
         if check:
             self._check(rc)
         return [_info(i) for i in infos]
+
+    def autotune(self, steps_per_trial: int = 50):
+        """cf_autotune on the batch (every member set and running); the state is restored."""
+        a, b, t = C.c_int32(), C.c_int32(), C.c_double()
+        self._check(self._L.cf_autotune(self._ctx, int(steps_per_trial), C.byref(a), C.byref(b), C.byref(t)))
+        return a.value, b.value, t.value
 
     def run(self, ts: float, max_steps: int = 1 << 40, check: bool = True):
         """Every member up to time ts (cf_run), each stopping at its own step."""

@@ -240,6 +240,20 @@ void* cf_get_stream(cf_ctx* ctx);
 /* Text of the last error of ctx (or of the last failed cf_create when ctx is NULL). */
 const char* cf_last_error(const cf_ctx* ctx);
 
+/* How the edge kernel shares its FP64 work between GB300's FP64 pipe and its integer pipes
+ * (results are identical bit for bit in every setting): int_compare 1 evaluates comparisons
+ * on integer keys of the bit patterns; int_mul_warps is a mask over the 4 warps of an edge
+ * block, and the warps whose bit is set form products by exact integer multiplication of the
+ * significands.  Default (0, 0): every operation on the FP64 pipe.  cf_autotune picks a
+ * setting by timing. */
+int cf_set_tuning(cf_ctx* ctx, int32_t int_compare, int32_t int_mul_warps);
+int cf_get_tuning(cf_ctx* ctx, int32_t* int_compare, int32_t* int_mul_warps);
+/* Autotuner: times steps_per_trial steps of every setting on the context's own state and keeps
+ * the fastest (the state, time and step count are restored after each trial, so the simulation
+ * is unchanged).  Every member must have a state and be running.  Outputs may be NULL. */
+int cf_autotune(cf_ctx* ctx, int32_t steps_per_trial, int32_t* int_compare, int32_t* int_mul_warps,
+                double* ms_per_step);
+
 /* Kernel timing of the last cf_step call: total device milliseconds of the edge-flux and
  * cell-update kernels measured with CUDA events when timing is enabled. */
 int cf_set_timing(cf_ctx* ctx, int32_t enable);

@@ -5,6 +5,7 @@
  * per-(element, edge) evaluation of the reference.  Not part of the product library.
  */
 #include "../cuteflow_gb300/csrc/cf_flux.h"
+#include "../cuteflow_gb300/csrc/cf_xd.h"
 
 #include <vector>
 
@@ -27,6 +28,18 @@ static void fill_member(MemberDev& M, const cf_params* p, const Prep& P) {
   M.nin = P.nin;
   M.tol_reg_perm = p->tol_reg_perm;
   M.steady_count = p->steady_count > 0 ? p->steady_count : 1000;
+}
+
+/* The edge kernel's arithmetic type: 0 double, 1 integer comparisons (XD<false>), 2 integer
+ * comparisons and products (XD<true>); results must not depend on it. */
+static int g_xd = 0;
+extern "C" void harness_set_xd(int mode) { g_xd = mode; }
+
+template <int IFLUX>
+static void edge_xd(const StepArgs& a, const MemberDev& M, int e, double dt, double t, const double* surf) {
+  if (IFLUX <= 3 && g_xd == 1) edge_body<IFLUX, XD<false>>(a, M, e, dt, t, surf);
+  else if (IFLUX <= 3 && g_xd == 2) edge_body<IFLUX, XD<true>>(a, M, e, dt, t, surf);
+  else edge_body<IFLUX>(a, M, e, dt, t, surf);
 }
 
 /* k_surf on the CPU: per inlet, blocks of 32 entries summed by the tree s[t] += s[t + i]
@@ -94,10 +107,10 @@ extern "C" int harness_edge_fluxes(const cf_mesh* m, const cf_params* p, const d
   double surf[CF_MAX_IO] = {0};
   surf_sums(P, M, Un.data(), surf);
   for (int e = 0; e < ne; ++e) {
-    if (p->iflux == 1) edge_body<1>(a, M, e, dt, t, surf);
-    else if (p->iflux == 2) edge_body<2>(a, M, e, dt, t, surf);
-    else if (p->iflux == 3) edge_body<3>(a, M, e, dt, t, surf);
-    else edge_body<4>(a, M, e, dt, t, surf);
+    if (p->iflux == 1) edge_xd<1>(a, M, e, dt, t, surf);
+    else if (p->iflux == 2) edge_xd<2>(a, M, e, dt, t, surf);
+    else if (p->iflux == 3) edge_xd<3>(a, M, e, dt, t, surf);
+    else edge_xd<4>(a, M, e, dt, t, surf);
   }
   for (int c = 0; c < n; ++c) {
     int o = P.perm[c];
@@ -153,10 +166,10 @@ extern "C" int harness_run(const cf_mesh* m, const cf_params* p, const double* U
     double surf[CF_MAX_IO] = {0};
     surf_sums(P, M, cur, surf);
     for (int e = 0; e < ne; ++e) {
-      if (p->iflux == 1) edge_body<1>(a, M, e, dt, t, surf);
-      else if (p->iflux == 2) edge_body<2>(a, M, e, dt, t, surf);
-      else if (p->iflux == 3) edge_body<3>(a, M, e, dt, t, surf);
-      else edge_body<4>(a, M, e, dt, t, surf);
+      if (p->iflux == 1) edge_xd<1>(a, M, e, dt, t, surf);
+      else if (p->iflux == 2) edge_xd<2>(a, M, e, dt, t, surf);
+      else if (p->iflux == 3) edge_xd<3>(a, M, e, dt, t, surf);
+      else edge_xd<4>(a, M, e, dt, t, surf);
     }
     double next = M.dt_reset;
     for (int c = 0; c < n; ++c) {
@@ -216,6 +229,43 @@ extern "C" long long harness_div_check(long long n, unsigned long long seed) {
     if (mode == 6) a = (r2 & 2) ? -0.0 : 0.0;
     const double got = div_rn(a, d, 1.0 / d), ref = a / d;
     if (memcmp(&got, &ref, 8) != 0) ++bad;
+  }
+  return bad;
+}
+
+/* em_mul and the integer comparisons of cf_xd.h against the hardware on n adversarial operand
+ * pairs: exponents over the whole range (subnormals, near overflow and underflow), all-ones and
+ * near-all-ones significands, signed zeros, infinities and NaN.  Returns the mismatches. */
+extern "C" long long harness_xd_check(long long n, unsigned long long seed) {
+  unsigned long long s = seed | 1;
+  auto rnd = [&]() { s ^= s << 13; s ^= s >> 7; s ^= s << 17; return s; };
+  auto mk = [&](int emin, int emax) {
+    unsigned long long m = rnd() & ((1ull << 52) - 1);
+    const int mode = (int)(rnd() % 8);
+    if (mode == 0) m = (1ull << 52) - 1;
+    if (mode == 1) m = 0;
+    if (mode == 2) m = rnd() % 16;
+    if (mode == 3) m = ((1ull << 52) - 1) ^ (rnd() % 16);
+    const int e = emin + (int)(rnd() % (unsigned long long)(emax - emin + 1));
+    const unsigned long long b = ((rnd() & 1) << 63) | ((unsigned long long)e << 52) | m;
+    double x;
+    memcpy(&x, &b, 8);
+    return x;
+  };
+  long long bad = 0;
+  for (long long i = 0; i < n; ++i) {
+    const int mode = (int)(rnd() % 5);
+    double a, b;
+    if (mode == 0) { a = mk(1, 2046); b = mk(1, 2046); }              /* any normal */
+    else if (mode == 1) { a = mk(0, 2047); b = mk(0, 2047); }         /* incl. subnormal, inf, NaN */
+    else if (mode == 2) { a = mk(1000, 1050); b = mk(1000, 1050); }   /* the step's range */
+    else if (mode == 3) { a = mk(1, 30); b = mk(990, 1030); }         /* underflow edge */
+    else { a = mk(2000, 2046); b = mk(1000, 1100); }                  /* overflow edge */
+    const double p1 = em_mul(a, b), p2 = a * b;
+    if (memcmp(&p1, &p2, 8) != 0 && !(p1 != p1 && p2 != p2)) ++bad;
+    if (xlt(a, b) != (a < b) || xle(a, b) != (a <= b) || xeq(a, b) != (a == b)) ++bad;
+    const double z = (rnd() & 1) ? -0.0 : 0.0;
+    if (xlt(a, z) != (a < z) || xlt(z, a) != (z < a) || xle(a, z) != (a <= z) || xeq(a, z) != (a == z)) ++bad;
   }
   return bad;
 }

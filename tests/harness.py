@@ -17,7 +17,7 @@ def lib():
     if _lib is not None:
         return _lib
     srcs = [os.path.join(HERE, "flux_harness.cpp"), os.path.join(ROOT, "cuteflow_gb300", "csrc", "cf_mesh.cpp")]
-    deps = srcs + [os.path.join(ROOT, "cuteflow_gb300", "csrc", f) for f in ("cf_flux.h", "cf_internal.h", "cf_dual.h")]
+    deps = srcs + [os.path.join(ROOT, "cuteflow_gb300", "csrc", f) for f in ("cf_flux.h", "cf_internal.h", "cf_dual.h", "cf_xd.h")]
     if not os.path.exists(LIB) or any(os.path.getmtime(d) > os.path.getmtime(LIB) for d in deps):
         os.makedirs(os.path.dirname(LIB), exist_ok=True)
         cuda_inc = os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "include")
@@ -69,6 +69,22 @@ def run(case, nsteps, params=None, U0=None):
     rc = L.harness_run(C.byref(ma.mesh), C.byref(p), _abi.dptr(U0), int(nsteps), _abi.dptr(U), _abi.dptr(dth),
                        C.byref(t), C.byref(steps))
     return dict(U=U, dt_hist=dth, t=t.value, rc=rc, steps=steps.value)
+
+
+def set_xd(mode: int):
+    """The edge arithmetic type of the harness: 0 double, 1 integer comparisons, 2 integer
+    comparisons and products."""
+    L = lib()
+    L.harness_set_xd.argtypes = [C.c_int]
+    L.harness_set_xd.restype = None
+    L.harness_set_xd(int(mode))
+
+
+def mul_check(n, seed=12345):
+    L = lib()
+    L.harness_xd_check.argtypes = [C.c_longlong, C.c_ulonglong]
+    L.harness_xd_check.restype = C.c_longlong
+    return int(L.harness_xd_check(int(n), int(seed)))
 
 
 def div_check(n, seed=12345):

@@ -90,3 +90,32 @@ def test_full_run_bitwise(oracle, name, make, n, prm):
     assert np.array_equal(r1["dt_hist"], r2["dt_hist"])
     assert np.array_equal(r1["U"], r2["U"])
     assert r1["t"] == r2["t"]
+
+
+XD_CASES = [c for c in CASES if c[0] in ("dam_hllc", "dam_riadh", "dam_waf", "flood_hllc", "flood_riadh", "flood_waf",
+                                          "flood_waf_conservative", "waf_lim2", "waf_lim3", "outlet_transm_waf",
+                                          "lake_wet", "dry_start_inflow", "phys_inflow_waf", "steady_stop_half")]
+
+
+@pytest.mark.parametrize("mode", [1, 2])
+@pytest.mark.parametrize("name,make,n,prm", XD_CASES, ids=[c[0] for c in XD_CASES])
+def test_full_run_bitwise_integer_pipes(oracle, name, make, n, prm, mode):
+    """The edge arithmetic on GB300's integer pipes (exact integer comparisons, and exact integer
+    products of the significands) runs the same IEEE operations: bit-identical runs."""
+    c = make()
+    r1 = oracle.run(c, n, params=prm, check=False)
+    H.set_xd(mode)
+    try:
+        r2 = H.run(c, n, params=prm)
+    finally:
+        H.set_xd(0)
+    assert r1["rc"] == r2["rc"] and r1["steps"] == r2["steps"]
+    assert np.array_equal(r1["dt_hist"], r2["dt_hist"])
+    assert np.array_equal(r1["U"], r2["U"])
+    assert r1["t"] == r2["t"]
+
+
+def test_integer_product_is_the_ieee_product():
+    """em_mul (cf_xd.h) against the hardware product on adversarial operands: normal and
+    near-overflow/underflow exponents, all-ones and near-all-ones significands, ties."""
+    assert H.mul_check(2_000_000, seed=3) == 0

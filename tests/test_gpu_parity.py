@@ -243,3 +243,42 @@ def test_case_directory_runs_to_ts(gpu_lib, oracle, tmp_path):
     k = _steps_to(full["dt_hist"], 45.0)
     assert info.steps == k and info.status & _abi.CF_STATUS_END
     assert np.array_equal(U, oracle.run(c, k)["U"])
+
+
+@pytest.mark.parametrize("iflux", [1, 2, 3])
+def test_integer_pipe_settings_are_bit_identical(gpu_lib, oracle, iflux):
+    """Every setting of cf_set_tuning (comparisons and products on the integer pipes, in some or
+    all warps) gives the oracle's run bit for bit."""
+    from cuteflow_gb300 import Solver
+    c = cases.flooding(60, 30, seed=4, iflux=iflux)
+    ref = oracle.run(c, 120)
+    with Solver(c) as s:
+        for cmp_, mask in ((1, 0), (1, 0xF), (1, 0x5), (1, 0x2), (0, 0)):
+            s.set_tuning(cmp_, mask)
+            assert s.tuning() == (cmp_, mask)
+            s.set_state(c.U0)
+            info = s.step(120)
+            assert np.array_equal(s.get_state(), ref["U"]), (cmp_, mask)
+            assert info.t == ref["t"]
+        with pytest.raises(Exception):
+            s.set_tuning(0, 0xF)
+
+
+def test_autotune_leaves_the_run_unchanged(gpu_lib, oracle):
+    """cf_autotune times the settings on the current state and restores it: the run continues
+    exactly as without tuning."""
+    from cuteflow_gb300 import Solver
+    c = cases.flooding(60, 30, seed=5, iflux=3)
+    ref = oracle.run(c, 90)
+    with Solver(c) as s:
+        s.set_state(c.U0)
+        s.step(40)
+        before = s.get_state()
+        info0 = s.info()
+        cmp_, mask, ms = s.autotune(20)
+        assert (cmp_, mask) == s.tuning() and ms > 0
+        assert np.array_equal(s.get_state(), before)
+        info1 = s.info()
+        assert info1.steps == info0.steps and info1.t == info0.t and info1.dt_next == info0.dt_next
+        info = s.step(50)
+        assert np.array_equal(s.get_state(), ref["U"]) and info.t == ref["t"] and info.steps == 90
