@@ -960,6 +960,7 @@ CF_HD CF_INLINE void element_core(const MemberDev& M, double area, double yarea,
 
 /* The element kernel's body: st = {area, manning n, cfl*L_cfl, 1/area}.  Returns the new
  * state; sets *nonfinite when it is not finite. */
+template <class S = double>
 CF_HD CF_INLINE double4 element_update(const MemberDev& M, const double4 U, const double4 st, const Slot& s0,
                                        const Slot& s1, const Slot& s2, double dt, bool& nonfinite) {
   /* fixed-order sums over the three edges (flux_riemann.cuf:411-426, source_terms.cuf:54-100) */
@@ -968,9 +969,10 @@ CF_HD CF_INLINE double4 element_update(const MemberDev& M, const double4 U, cons
   const double rc3 = s0.f3 + s1.f3 + s2.f3;
   const double sb2 = s0.bx + s1.bx + s2.bx;
   const double sb3 = s0.by + s1.by + s2.by;
-  double h, hu, hv;
-  element_core(M, st.x, st.w, st.y, U.x, U.y, U.z, rc1, rc2, rc3, sb2, sb3, dt, h, hu, hv, nonfinite);
-  return make_double4(h, hu, hv, U.w);
+  S h, hu, hv;
+  element_core(M, st.x, st.w, S(st.y), S(U.x), S(U.y), S(U.z), S(rc1), S(rc2), S(rc3), S(sb2), S(sb3), dt, h, hu,
+               hv, nonfinite);
+  return make_double4(val(h), val(hu), val(hv), U.w);
 }
 
 }  // namespace cf

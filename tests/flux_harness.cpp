@@ -175,7 +175,9 @@ extern "C" int harness_run(const cf_mesh* m, const cf_params* p, const double* U
     for (int c = 0; c < n; ++c) {
       const int* sl = &P.cslot[c].x;
       bool nf = false;
-      nxt[c] = element_update(M, cur[c], P.cstat[c], slots[sl[0]], slots[sl[1]], slots[sl[2]], dt, nf);
+      nxt[c] = g_xd == 0 ? element_update(M, cur[c], P.cstat[c], slots[sl[0]], slots[sl[1]], slots[sl[2]], dt, nf)
+               : g_xd == 1 ? element_update<XD<false>>(M, cur[c], P.cstat[c], slots[sl[0]], slots[sl[1]], slots[sl[2]], dt, nf)
+                           : element_update<XD<true>>(M, cur[c], P.cstat[c], slots[sl[0]], slots[sl[1]], slots[sl[2]], dt, nf);
       next = dmin(next, cfl_dt_elem(M, P.cstat[c].z, nxt[c].x, nxt[c].y, nxt[c].z));
     }
     t = t + dt;
