@@ -272,6 +272,95 @@ def adjoint_leg(steps: int, warmup: int, obs_every: float = 10.0):
     return out
 
 
+def calibration_batch_leg(ninst: int, steps: int, iters: int, obs_every: float = 10.0):
+    """Batched adjoint calibration (a sample of the 64-instance workload): ninst instances of the
+    calibration case with seeded sizes, zone fields and gauges, in one batch context; every
+    gradient-descent iteration runs one recording forward and one backward for all instances in
+    the same launches, sums dJ/dn per zone and steps the zone values on the device.  Timed
+    against the same instances' one-member adjoints run one after another (forward, backward,
+    zone gradient and step each).  Misfit: sum of squared gauge misfits every obs_every s."""
+    import torch
+    from cuteflow_gb300 import Batch, Solver, cases
+    from cuteflow_gb300.adjoint import Adjoint, Zones
+    inst = []
+    for i in range(ninst):
+        nx = int(100 + (i * 37) % 120)
+        ny = int(40 + (i * 23) % 50)
+        c, zones, nz, gauges = cases.calibration(nx, ny, seed=10 + i, nzones=8 + i % 9, ngauges=20 + (i * 7) % 41)
+        inst.append((c, zones, nz, gauges))
+    tri = sum(c.nelt for c, *_ in inst)
+    zoff = np.cumsum([0] + [len(nz) for _, _, nz, _ in inst])
+    zone_all = np.concatenate([z + zoff[i] for i, (_, z, _, _) in enumerate(inst)]).astype(np.int32)
+    true_vals = np.concatenate([nz for _, _, nz, _ in inst])
+    gm = np.concatenate([np.full(len(g), i, np.int32) for i, (_, _, _, g) in enumerate(inst)])
+    gg = np.concatenate([g for *_, g in inst]).astype(np.int32)
+    b = Batch([c for c, *_ in inst])
+    adj = Adjoint(b, steps, gg, 0, gauge_member=gm)
+    zs = Zones(b, zone_all, int(zoff[-1]))
+
+    def start():
+        for i, (c, *_) in enumerate(inst):
+            b.set_state(i, c.U0)
+
+    zs.set(true_vals)
+    start()
+    eta_obs, _ = adj.forward()
+    dt, t = adj.dt_history()
+    obs = [cases.observation_steps(t[:, i], dt[:, i], obs_every) for i in range(ninst)]
+    col = np.cumsum([0] + [len(g) for *_, g in inst])
+    mask = np.zeros_like(eta_obs)
+    for i in range(ninst):
+        mask[obs[i], col[i]:col[i + 1]] = 1.0
+    vals0 = np.full(int(zoff[-1]), 0.035)
+    zs.set(vals0)
+    misfits, lr = [], None
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for it in range(iters):
+        start()
+        eta, _ = adj.forward()
+        r = (eta - eta_obs) * mask
+        misfits.append(float(np.sum(r * r)))
+        adj.backward(2.0 * r)
+        g = zs.gradient(adj)
+        if lr is None:
+            lr = 0.004 / max(np.abs(g).max(), 1e-300)
+        zs.descend(lr, 0.01, 0.1)
+    torch.cuda.synchronize()
+    t_batch = (time.perf_counter() - t0) / iters
+    start()
+    eta, _ = adj.forward()
+    r = (eta - eta_obs) * mask
+    misfits.append(float(np.sum(r * r)))
+    vals, _ = zs.get()
+    zs.close(); adj.close(); b.close()
+    # the same iteration, instance by instance
+    t_seq = 0.0
+    for i, (c, zones, nz, gauges) in enumerate(inst):
+        s = Solver(c)
+        a1 = Adjoint(s, steps, gauges, 0)
+        z1 = Zones(s, zones, len(nz))
+        z1.set(vals0[zoff[i]:zoff[i + 1]])
+        obs_i, mask_i = eta_obs[:, col[i]:col[i + 1]], mask[:, col[i]:col[i + 1]]
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        for it in range(iters):
+            s.set_state(c.U0)
+            eta_i, _ = a1.forward()
+            a1.backward(2.0 * (eta_i - obs_i) * mask_i)
+            z1.gradient(a1)
+            z1.descend(lr, 0.01, 0.1)
+        torch.cuda.synchronize()
+        t_seq += (time.perf_counter() - t1) / iters
+        z1.close(); a1.close(); s.close()
+    return {"instances": ninst, "triangles_total": tri, "steps": steps, "iterations": iters,
+            "zones_total": int(zoff[-1]), "gauges_total": int(gg.size),
+            "batched_s_per_iteration": t_batch, "sequential_s_per_iteration": t_seq,
+            "speedup_vs_sequential": t_seq / t_batch, "misfit_per_iteration": misfits,
+            "zone_error_start": float(np.abs(vals0 - true_vals).mean()),
+            "zone_error_end": float(np.abs(vals - true_vals).mean())}
+
+
 def run_ours(args):
     import torch
     world, rank, local = dist_env()
@@ -393,6 +482,10 @@ def run_ours(args):
                                    "`bench.py --config ensemble` for the full size")
     if rank == 0 and args.adjoint_steps > 0:
         line["adjoint"] = adjoint_leg(args.adjoint_steps, 10)
+    if rank == 0 and args.calib_instances > 0:
+        line["batched_adjoint"] = calibration_batch_leg(args.calib_instances, args.calib_steps, args.calib_iters)
+        line["batched_adjoint"]["note"] = ("sample of the 64-instance calibration workload (50k-300k triangles, "
+                                           "3000 steps, 10 iterations)")
     if rank == 0 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(case)
     s.close()
@@ -413,6 +506,9 @@ def main():
     ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (every operation on the FP64 pipe)")
     ap.add_argument("--batched-members", type=int, default=32, help="ensemble sample beside the plain line (0: skip)")
     ap.add_argument("--batched-steps", type=int, default=200)
+    ap.add_argument("--calib-instances", type=int, default=8, help="batched calibration leg (0: skip)")
+    ap.add_argument("--calib-steps", type=int, default=400)
+    ap.add_argument("--calib-iters", type=int, default=3)
     ap.add_argument("--adjoint-steps", type=int, default=3000,
                     help="adjoint calibration leg beside the plain line (0: skip)")
     args = ap.parse_args()

@@ -296,7 +296,10 @@ def calibration(nx: int = 500, ny: int = 200, seed: int = 4, nzones: int = 12, n
     Returns (case with the true field, zones [nelt] zone id of every element, true zone values
     [nzones], gauges [ngauges] element ids)."""
     lx, ly = 2.0 * nx, 2.0 * ny
-    c = flooding(nx, ny, seed=seed, lx=lx, ly=ly, iflux=iflux, nbumps=8)
+    # 8 bumps on the 1000 m x 400 m case, proportionally fewer on smaller domains (bumps 30-150 m
+    # wide would otherwise cover a small domain and leave it dry)
+    nbumps = int(round(8 * (lx * ly) / (1000.0 * 400.0)))
+    c = flooding(nx, ny, seed=seed, lx=lx, ly=ly, iflux=iflux, nbumps=nbumps)
     xc, yc = cell_centroids(c.x, c.y, c.tri)
     sx = uniform(seed, 30, nzones, 0.0, lx)
     sy = uniform(seed, 31, nzones, 0.0, ly)
