@@ -49,7 +49,8 @@ class CfParams(C.Structure):
         ("fricimplic", C.c_int32), ("is_override_manning", C.c_int32),
         ("is_dt_constant", C.c_int32), ("inlet", C.c_int32), ("outlet", C.c_int32),
         ("flux_mode", C.c_int32), ("reorder", C.c_int32), ("pad_", C.c_int32),
-        ("tol_reg_perm", C.c_double), ("steady_count", C.c_int32), ("pad2_", C.c_int32),
+        ("tol_reg_perm", C.c_double), ("steady_count", C.c_int32), ("dt_reset_nelt", C.c_int32),
+        ("long_entree", C.c_double * CF_MAX_IO),
     ]
 
 
@@ -97,7 +98,7 @@ def default_params() -> CfParams:
 def make_params(overrides: dict | None = None) -> CfParams:
     p = default_params()
     for k, v in (overrides or {}).items():
-        if k in ("debitglob", "h_sortie", "debitglob_start"):
+        if k in ("debitglob", "h_sortie", "debitglob_start", "long_entree"):
             arr = getattr(p, k)
             for i, val in enumerate(v):
                 arr[i] = float(val)

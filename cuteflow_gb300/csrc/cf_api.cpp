@@ -82,7 +82,7 @@ void free_all(cf_ctx* c) {
   if (c->graph2) cudaGraphExecDestroy(c->graph2);
   void* ptrs[] = {c->U[0], c->U[1], c->cslot, c->cstat, c->zcell, c->perm, c->iperm, c->ecell, c->egeo,
                   c->ebid, c->eupw, c->ewts, c->edk, c->einv, c->slots, c->etile_mem, c->ctile_mem, c->mdev,
-                  c->mst, c->staging, c->inl_cell, c->inl_len};
+                  c->mst, c->staging, c->inl_cell, c->inl_len, c->ids};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (c->host_state) cudaFreeHost(c->host_state);
@@ -163,7 +163,7 @@ MemberDev member_dev(const Member& M) {
   D.tol = p->tol;
   D.constant_dt = p->constant_dt;
   D.ramp_time = p->ramp_time;
-  D.dt_reset = (M.n % 1024 != 0) ? 100000.0 : 1000000.0;
+  D.dt_reset = ((p->dt_reset_nelt > 0 ? p->dt_reset_nelt : M.n) % 1024 != 0) ? 100000.0 : 1000000.0;
   for (int i = 0; i < CF_MAX_IO; ++i) {
     D.debit_end[i] = p->debitglob[i];
     D.debit_start[i] = p->debitglob_start[i];
@@ -693,6 +693,85 @@ int cf_autotune(cf_ctx* ctx, int32_t steps_per_trial, int32_t* int_compare, int3
   if (int_compare) *int_compare = bc;
   if (int_mul_warps) *int_mul_warps = bm;
   if (ms_per_step) *ms_per_step = best;
+  return CF_OK;
+}
+
+/* ---- pieces of a decomposed mesh: halo exchange and the global dt ------------------------- */
+
+namespace {
+
+int elements_prep(cf_ctx* c, int32_t member, const int32_t* ids, int32_t n, const void* vals) {
+  int rc = member_ok(c, member);
+  if (rc) return rc;
+  const Member& M = c->mem[member];
+  if (n < 0 || n > M.n || (n > 0 && (!ids || !vals))) return fail(c, CF_EINVAL, "bad element list");
+  for (int32_t i = 0; i < n; ++i)
+    if (ids[i] < 0 || ids[i] >= M.n) return fail(c, CF_EINVAL, "element id out of range");
+  CF_CUDA(c, cudaSetDevice(c->device));
+  if (!c->ids && (rc = dalloc(c, &c->ids, (size_t)c->max_n))) return rc;
+  if ((rc = read_states(c))) return rc;
+  if (c->host_state[member].status & STATUS_NO_STATE) return fail(c, CF_ESTATE, "no state set");
+  CF_CUDA(c, cudaMemcpyAsync(c->ids, ids, (size_t)n * sizeof(int32_t), cudaMemcpyHostToDevice, c->stream));
+  return CF_OK;
+}
+
+}  // namespace
+
+int cf_get_elements(cf_ctx* ctx, int32_t member, const int32_t* ids, int32_t n, double* hu3_out) {
+  if (!ctx) return CF_EINVAL;
+  cf_ctx* c = ctx;
+  int rc = elements_prep(c, member, ids, n, hu3_out);
+  if (rc || n == 0) return rc;
+  const Member& M = c->mem[member];
+  const MemberState& s = c->host_state[member];
+  const int cur = (int)((s.base + s.nstep) & 1);
+  rc = launch_gather_ids(c->U[cur] + M.cell_off, c->iperm + M.cell_off, c->ids, c->staging, n,
+                         reinterpret_cast<stream_t>(c->stream));
+  if (rc) return fail(c, rc, "gather launch failed");
+  CF_CUDA(c, cudaMemcpyAsync(hu3_out, c->staging, 3 * (size_t)n * sizeof(double), cudaMemcpyDefault, c->stream));
+  CF_CUDA(c, cudaStreamSynchronize(c->stream));
+  return CF_OK;
+}
+
+int cf_set_elements(cf_ctx* ctx, int32_t member, const int32_t* ids, int32_t n, const double* hu3) {
+  if (!ctx) return CF_EINVAL;
+  cf_ctx* c = ctx;
+  int rc = elements_prep(c, member, ids, n, hu3);
+  if (rc) return rc;
+  const Member& M = c->mem[member];
+  MemberState s = c->host_state[member];
+  const int cur = (int)((s.base + s.nstep) & 1);
+  const stream_t st = reinterpret_cast<stream_t>(c->stream);
+  if (n > 0) {
+    CF_CUDA(c, cudaMemcpyAsync(c->staging, hu3, 3 * (size_t)n * sizeof(double), cudaMemcpyDefault, c->stream));
+    if ((rc = launch_scatter_ids(c->U[cur] + M.cell_off, c->iperm + M.cell_off, c->ids, c->staging, n, st)))
+      return fail(c, rc, "scatter launch failed");
+  }
+  /* the next dt is the CFL of the state as it now is (as cf_set_state computes it) */
+  s.dt[cur] = M.dev.dt_reset;
+  c->host_state[member] = s;
+  CF_CUDA(c, cudaMemcpyAsync(c->mst + member, &c->host_state[member], sizeof(MemberState), cudaMemcpyHostToDevice,
+                             c->stream));
+  if ((rc = launch_cfl(c->U[cur], c->cstat, c->ctile_mem, M.ctile_begin, M.ctile_end - M.ctile_begin, c->mdev, c->mst,
+                       cur, st)))
+    return fail(c, rc, "cfl launch failed");
+  CF_CUDA(c, cudaStreamSynchronize(c->stream));
+  return CF_OK;
+}
+
+int cf_set_dt(cf_ctx* ctx, int32_t member, double dt) {
+  if (!ctx) return CF_EINVAL;
+  cf_ctx* c = ctx;
+  int rc = member_ok(c, member);
+  if (rc) return rc;
+  if (!(dt > 0.0)) return fail(c, CF_EINVAL, "dt must be positive");
+  CF_CUDA(c, cudaSetDevice(c->device));
+  if ((rc = read_states(c))) return rc;
+  MemberState& s = c->host_state[member];
+  if (s.status & STATUS_NO_STATE) return fail(c, CF_ESTATE, "no state set");
+  s.dt[(s.base + s.nstep) & 1] = dt;
+  CF_CUDA(c, cudaMemcpyAsync(c->mst + member, &s, sizeof(MemberState), cudaMemcpyHostToDevice, c->stream));
+  CF_CUDA(c, cudaStreamSynchronize(c->stream));
   return CF_OK;
 }
 

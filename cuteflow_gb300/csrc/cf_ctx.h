@@ -59,6 +59,7 @@ struct cf_ctx {
   int64_t n_inl = 0;
   bool any_phys_inflow = false;        /* some member has inlet 3 */
   bool any_steady = false;             /* some member tests for steady state */
+  int32_t* ids = nullptr;              /* max_n element ids (cf_get_elements / cf_set_elements) */
   int32_t xd_cmp = 0;                  /* edge kernel: integer comparisons (cf_set_tuning) */
   int32_t xd_mul_mask = 0;             /* edge kernel: warps multiplying on the integer pipes */
   cf::MemberState* host_state = nullptr;   /* pinned, one record per member */

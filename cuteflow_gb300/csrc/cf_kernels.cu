@@ -242,6 +242,24 @@ __global__ void k_gather(const double4* U, const int32_t* iperm, double* hu3, in
   hu3[3 * (size_t)o + 2] = u.z;
 }
 
+/* (h, hu, hv) of the listed elements (member-local reference ids) out of / into U */
+__global__ void k_gather_ids(const double4* U, const int32_t* iperm, const int32_t* ids, double* out, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double4 u = U[iperm[ids[i]]];
+  out[3 * (size_t)i] = u.x;
+  out[3 * (size_t)i + 1] = u.y;
+  out[3 * (size_t)i + 2] = u.z;
+}
+
+__global__ void k_scatter_ids(double4* U, const int32_t* iperm, const int32_t* ids, const double* in, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double4* u = U + iperm[ids[i]];
+  reinterpret_cast<double2*>(u)[0] = make_double2(in[3 * (size_t)i], in[3 * (size_t)i + 1]);
+  u->z = in[3 * (size_t)i + 2];
+}
+
 int check(cudaError_t e) { return e == cudaSuccess ? CF_OK : CF_ECUDA; }
 
 }  // namespace
@@ -278,6 +296,18 @@ int launch_discharge(const Slot* slots, const int2* ecell, const MemberDev* mdev
 
 int launch_scatter_state(const double* hu3, const int32_t* perm, const double* zcell, double4* U, int32_t n, stream_t s) {
   k_scatter<<<(n + 255) / 256, 256, 0, reinterpret_cast<cudaStream_t>(s)>>>(hu3, perm, zcell, U, n);
+  return check(cudaGetLastError());
+}
+
+int launch_gather_ids(const double4* U, const int32_t* iperm, const int32_t* ids, double* out, int32_t n, stream_t s) {
+  if (n <= 0) return CF_OK;
+  k_gather_ids<<<(n + 255) / 256, 256, 0, reinterpret_cast<cudaStream_t>(s)>>>(U, iperm, ids, out, n);
+  return check(cudaGetLastError());
+}
+
+int launch_scatter_ids(double4* U, const int32_t* iperm, const int32_t* ids, const double* in, int32_t n, stream_t s) {
+  if (n <= 0) return CF_OK;
+  k_scatter_ids<<<(n + 255) / 256, 256, 0, reinterpret_cast<cudaStream_t>(s)>>>(U, iperm, ids, in, n);
   return check(cudaGetLastError());
 }
 

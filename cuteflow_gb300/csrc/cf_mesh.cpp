@@ -174,6 +174,8 @@ int prepare_mesh(const cf_mesh* m, const cf_params* p, Prep& P, std::string& err
         P.long_entree[id - 1] += std::sqrt((m->x[a] - m->x[b]) * (m->x[a] - m->x[b]) +
                                            (m->y[a] - m->y[b]) * (m->y[a] - m->y[b]));
       }
+  for (int i = 0; i < CF_MAX_IO; ++i)
+    if (p->long_entree[i] > 0.0) P.long_entree[i] = p->long_entree[i];   /* a part of a decomposed mesh */
   if (p->inlet == 2)
     for (int e = 0; e < n; ++e)
       for (int k = 0; k < 3; ++k)

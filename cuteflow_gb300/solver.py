@@ -56,6 +56,9 @@ def load(build_if_missing: bool = True):
     L.cf_step_noalloc.argtypes = [vp, C.c_int32, C.POINTER(_abi.CfStepInfo)]
     L.cf_run.argtypes = [vp, C.c_double, C.c_int64, C.POINTER(_abi.CfStepInfo)]
     L.cf_set_tuning.argtypes = [vp, C.c_int32, C.c_int32]
+    L.cf_get_elements.argtypes = [vp, C.c_int32, C.POINTER(C.c_int32), C.c_int32, dp]
+    L.cf_set_elements.argtypes = [vp, C.c_int32, C.POINTER(C.c_int32), C.c_int32, dp]
+    L.cf_set_dt.argtypes = [vp, C.c_int32, C.c_double]
     L.cf_get_tuning.argtypes = [vp, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
     L.cf_autotune.argtypes = [vp, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_int32), dp]
     L.cf_get_state.argtypes = [vp, dp]
@@ -109,7 +112,7 @@ def load(build_if_missing: bool = True):
         getattr(L, name).restype = C.c_int
     for name in ("cf_default_params", "cf_create", "cf_set_state", "cf_set_state_device",
                  "cf_set_initial_condition", "cf_step", "cf_step_noalloc", "cf_run", "cf_set_tuning",
-                 "cf_get_tuning", "cf_autotune", "cf_get_state", "cf_get_state_device",
+                 "cf_get_tuning", "cf_autotune", "cf_get_elements", "cf_set_elements", "cf_set_dt", "cf_get_state", "cf_get_state_device",
                  "cf_get_info", "cf_get_mesh_tables", "cf_mesh_tables", "cf_get_sizes", "cf_set_timing", "cf_get_timing"):
         getattr(L, name).restype = C.c_int
     _lib = L
@@ -213,6 +216,25 @@ class Solver:
         if check:
             self._check(rc)
         return _info(info)
+
+    def get_elements(self, ids) -> np.ndarray:
+        """(h, hu, hv) of the listed elements (0-based, reference order) of the current state."""
+        ids = np.ascontiguousarray(ids, dtype=np.int32)
+        out = np.empty((ids.size, 3))
+        self._check(self._L.cf_get_elements(self._ctx, 0, ids.ctypes.data_as(C.POINTER(C.c_int32)), int(ids.size),
+                                            _abi.dptr(out)))
+        return out
+
+    def set_elements(self, ids, values):
+        """Write (h, hu, hv) of the listed elements; the next dt becomes the CFL of the new state."""
+        ids = np.ascontiguousarray(ids, dtype=np.int32)
+        v = np.ascontiguousarray(values, dtype=np.float64).reshape(ids.size, 3)
+        self._check(self._L.cf_set_elements(self._ctx, 0, ids.ctypes.data_as(C.POINTER(C.c_int32)), int(ids.size),
+                                            _abi.dptr(v)))
+
+    def set_dt(self, dt: float):
+        """The dt of the next step (a decomposed mesh applies the minimum over its parts)."""
+        self._check(self._L.cf_set_dt(self._ctx, 0, float(dt)))
 
     def set_tuning(self, int_compare: int, int_mul_warps: int):
         """cf_set_tuning: share the edge kernel's FP64 work with the integer pipes (results

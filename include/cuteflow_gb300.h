@@ -103,7 +103,11 @@ typedef struct cf_params {
                                       more than steady_count consecutive steps the member stops
                                       with CF_STATUS_STEADY; 0 (default) disables the test */
   int32_t steady_count;            /* 1000 in the reference (finite_volumes_method.cuf:380) */
-  int32_t pad2_;
+  int32_t dt_reset_nelt;           /* extension: the element count whose remainder mod 1024 selects the
+                                      dt minimum's start value 1e5 / 1e6 (cfl_condition.cuf:86); 0 = the
+                                      mesh's own (a part of a decomposed mesh passes the whole mesh's) */
+  double long_entree[CF_MAX_IO];   /* extension: inlet lengths; 0 = measured on the mesh (a part of a
+                                      decomposed mesh passes the whole mesh's, calcul_long_entree) */
 } cf_params;
 
 /* set_initial_condition inputs (initial_condition.cuf:4-80, namelist global_data.cuf:40-44). */
@@ -239,6 +243,20 @@ void* cf_get_stream(cf_ctx* ctx);
 
 /* Text of the last error of ctx (or of the last failed cf_create when ctx is NULL). */
 const char* cf_last_error(const cf_ctx* ctx);
+
+/* ---- Pieces of a decomposed mesh (the reference's MPI decomposition, memory_exchange_functions.cuf,
+ * finite_volumes_method.cuf:141-171): each part is its own context over its elements and a halo of
+ * the neighbours' elements (one ring of neighbours; two for iflux 3 and 4, whose upwind states read
+ * the neighbours' neighbours).  After every step the caller copies the owners' states into the
+ * halos and applies the minimum dt over all parts (the reference's MPI_ALLREDUCE MIN).  With the
+ * whole mesh's inlet lengths and element count in cf_params (long_entree, dt_reset_nelt), every
+ * element evolves bit for bit as in the undivided mesh.
+ * cf_get_elements / cf_set_elements read / write (h, hu, hv) of listed elements (0-based, member-local
+ * reference order) of the current state; cf_set_elements then recomputes the member's next dt from
+ * the CFL of the state as it now is.  cf_set_dt sets the member's next dt. */
+int cf_get_elements(cf_ctx* ctx, int32_t member, const int32_t* ids, int32_t n, double* hu3_out);
+int cf_set_elements(cf_ctx* ctx, int32_t member, const int32_t* ids, int32_t n, const double* hu3);
+int cf_set_dt(cf_ctx* ctx, int32_t member, double dt);
 
 /* How the edge kernel shares its FP64 work between GB300's FP64 pipe and its integer pipes
  * (results are identical bit for bit in every setting): int_compare 1 evaluates comparisons

@@ -187,6 +187,13 @@ void build_geometry(Setup& S, const orc_mesh* m) {
       }
 }
 
+/* the inlet lengths a caller passes (a part of a decomposed mesh takes the whole mesh's) */
+void apply_overrides(Setup& S, const orc_params* prm) {
+  if (!prm) return;
+  for (int i = 0; i < ORC_MAX_IO && i < (int)S.long_entree.size(); ++i)
+    if (prm->long_entree[i] > 0.0) S.long_entree[i] = prm->long_entree[i];
+}
+
 bool do_setup(Setup& S, const orc_mesh* m) {
   if (!m || m->nelt <= 0 || m->nnt <= 0 || !m->x || !m->y || !m->z || !m->tri) return false;
   S.nnt = m->nnt; S.nelt = m->nelt; S.x = m->x; S.y = m->y; S.z = m->z; S.tri = m->tri;
@@ -809,7 +816,7 @@ double cfl_dt(const Setup& S, const orc_params* prm, const double* U) {
     if (prm->is_dt_constant == 1) d = prm->constant_dt;
     dtmin = std::min(dtmin, d);
   }
-  if (n % 1024 != 0) dtmin = std::min(dtmin, 100000.0);
+  if (((prm->dt_reset_nelt > 0) ? prm->dt_reset_nelt : n) % 1024 != 0) dtmin = std::min(dtmin, 100000.0);
   return dtmin;
 }
 
@@ -823,6 +830,7 @@ int orc_edge_flux(const orc_mesh* m, const orc_params* prm, const double* U, dou
                   int32_t gi, int32_t tj, double* fl_out) {
   Setup S;
   if (!prm || !U || !fl_out || !do_setup(S, m) || gi < 0 || gi >= m->nelt || tj < 0 || tj > 2) return -1;
+  apply_overrides(S, prm);
   Ctx C;
   C.S = &S; C.m = m; C.prm = prm;
   C.p.gp = prm->gp; C.p.tolisec = prm->tolisec; C.p.cfl = prm->cfl; C.p.tol = prm->tol;
@@ -840,6 +848,7 @@ int orc_all_edge_fluxes(const orc_mesh* m, const orc_params* prm, const double* 
                         double t, double* fl_out) {
   Setup S;
   if (!prm || !U || !fl_out || !do_setup(S, m)) return -1;
+  apply_overrides(S, prm);
   Ctx C;
   C.S = &S; C.m = m; C.prm = prm;
   C.p.gp = prm->gp; C.p.tolisec = prm->tolisec; C.p.cfl = prm->cfl; C.p.tol = prm->tol;
@@ -924,6 +933,7 @@ int orc_run(const orc_mesh* m, const orc_params* prm, const double* U0in, double
 #endif
     return -1;
   }
+  apply_overrides(S, prm);
   const int n = S.nelt;
   const bool two_sided = prm->flux_mode == 0;
   std::vector<double> Ua(U0in, U0in + 3 * (size_t)n), Ub(3 * (size_t)n, 0.0);

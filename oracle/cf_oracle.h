@@ -62,7 +62,8 @@ typedef struct orc_params {
   int32_t pad_;
   double tol_reg_perm;             /* steady-state stop; 0 disables */
   int32_t steady_count;            /* consecutive qualifying steps before the stop (1000) */
-  int32_t pad2_;
+  int32_t dt_reset_nelt;           /* element count selecting the dt sentinel (0: the mesh's) */
+  double long_entree[ORC_MAX_IO];  /* inlet lengths (0: measured on the mesh) */
 } orc_params;
 
 typedef struct orc_ic {

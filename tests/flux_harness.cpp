@@ -15,7 +15,8 @@ using namespace cf;
 static void fill_member(MemberDev& M, const cf_params* p, const Prep& P) {
   std::memset(&M, 0, sizeof(M));
   M.gp = p->gp; M.tolisec = p->tolisec; M.tol = p->tol; M.constant_dt = p->constant_dt;
-  M.ramp_time = p->ramp_time; M.dt_reset = (P.nelt % 1024 != 0) ? 100000.0 : 1000000.0;
+  M.ramp_time = p->ramp_time;
+  M.dt_reset = ((p->dt_reset_nelt > 0 ? p->dt_reset_nelt : P.nelt) % 1024 != 0) ? 100000.0 : 1000000.0;
   for (int i = 0; i < CF_MAX_IO; ++i) {
     M.debit_end[i] = p->debitglob[i]; M.debit_start[i] = p->debitglob_start[i];
     M.long_entree[i] = P.long_entree[i]; M.h_sortie[i] = p->h_sortie[i];
