@@ -100,11 +100,11 @@ __global__ void __launch_bounds__(TILE_C) k_rep_cells(StepArgs a, const double* 
 
 /* After step n: the gauge elevations h + z of the new state and, when recording, every
  * member's dt and start time of the step (read from its record of parity p). */
-__global__ void k_record(const double4* Unew, const MemberState* S, int nm, int p, int n, double* dt_hist,
-                         double* t_hist, const int32_t* gcell, int G, double* eta) {
+__global__ void k_record(const double4* Unew, const double* zcell, const MemberState* S, int nm, int p, int n,
+                         double* dt_hist, double* t_hist, const int32_t* gcell, int G, double* eta) {
   for (int g = threadIdx.x; g < G; g += blockDim.x) {
-    const double4 u = Unew[gcell[g]];
-    eta[(size_t)n * G + g] = u.x + u.w;
+    const int c = gcell[g];
+    eta[(size_t)n * G + g] = Unew[c].x + zcell[c];
   }
   if (S)
     for (int m = threadIdx.x; m < nm; m += blockDim.x) {
@@ -164,7 +164,7 @@ __global__ void __launch_bounds__(TILE_C) k_adj_cells(AdjArgs A) {
   double r1, ri1, ri2, ri3;
   if (fric) {
     friction_terms(M, area, dt, Dual<4>::var(st.y, 3), Dual<4>::var(U.x, 0), Dual<4>::var(U.y, 1),
-                   Dual<4>::var(U.z, 2), sf2, sf3, m);
+                   Dual<4>::var(U.z, 2), sf2, sf3, m, U.w);
     ri1 = div_rn(0. + 0. - rc1, area, y);
     ri2 = div_rn(sb2 + sf2.v - rc2, area, y);
     ri3 = div_rn(sb3 + sf3.v - rc3, area, y);
@@ -228,8 +228,8 @@ __device__ __forceinline__ void upwind_chain(const double4* U, int i1, int i2, d
   const double4 A1 = ld4(U + i1);
   const double4 A2 = (d1 < 0.0) ? make_double4(0.0, 0.0, 0.0, 0.0) : ld4(U + i2);
   Dual<6> hu_, vu_;
-  upwind_mix(Dual<6>::var(A1.x, 0), Dual<6>::var(A1.y, 1), Dual<6>::var(A1.z, 2), Dual<6>::var(A2.x, 3),
-             Dual<6>::var(A2.y, 4), Dual<6>::var(A2.z, 5), d1, d2, ysum, nx, ny, tolisec, hu_, vu_);
+  upwind_mix(Dual<6>::var(A1.x, 0), Dual<6>::var(A1.y, 1), Dual<6>::var(A1.z, 2), A1.w, Dual<6>::var(A2.x, 3),
+             Dual<6>::var(A2.y, 4), Dual<6>::var(A2.z, 5), A2.w, d1, d2, ysum, nx, ny, tolisec, hu_, vu_);
   *o1 = make_double4(wh * hu_.d[0] + wv * vu_.d[0], wh * hu_.d[1] + wv * vu_.d[1], wh * hu_.d[2] + wv * vu_.d[2], 0.0);
   *o2 = make_double4(wh * hu_.d[3] + wv * vu_.d[3], wh * hu_.d[4] + wv * vu_.d[4], wh * hu_.d[5] + wv * vu_.d[5], 0.0);
 }
@@ -246,6 +246,7 @@ __global__ void __launch_bounds__(TILE_E) k_adj_edges(AdjArgs A) {
   const double dt = __ldg(A.dt_hist + h), t = __ldg(A.t_hist + h);
   const int2 ab = ldro(a.ecell + e);
   const double4 UA = ld4(a.Uin + ab.x);
+  const double4 ez = ld4(a.ez + e);
   const Slot wa = A.cadj[ab.x];
 
   if (ab.y < 0) {
@@ -253,7 +254,7 @@ __global__ void __launch_bounds__(TILE_E) k_adj_edges(AdjArgs A) {
     const int id = ldro(a.ebid + e);
     Dual<3> f1, f2, f3, q;
     boundary_flux(IFLUX, M, ab.y, id, t, geo.x, geo.y, Dual<3>::var(UA.x, 0), Dual<3>::var(UA.y, 1),
-                  Dual<3>::var(UA.z, 2), UA.w, f1, f2, f3, q);
+                  Dual<3>::var(UA.z, 2), UA.w, ez.x, f1, f2, f3, q);
     const double len = geo.z;
     double o[3];
 #pragma unroll
@@ -265,14 +266,14 @@ __global__ void __launch_bounds__(TILE_E) k_adj_edges(AdjArgs A) {
   const double4 UB = ld4(a.Uin + ab.y);
   const Slot wb = A.cadj[ab.y];
   const EdgeGeo G = edge_geo(a, e, IFLUX >= 3);
-  double hl_upw = 0.0, vl_upw = 0.0, zl_upw = 0.0, hr_upw = 0.0, vr_upw = 0.0, zr_upw = 0.0;
+  double hl_upw = 0.0, vl_upw = 0.0, hr_upw = 0.0, vr_upw = 0.0;
   int4 up = make_int4(0, 0, 0, 0);
   double4 dw = make_double4(0.0, 0.0, 0.0, 0.0);
   if (IFLUX >= 3) {
     up = ldro(a.eupw + e);
     dw = ld4(a.ewts + e);
-    upwind_state(a.Uin, up.x, up.y, dw.x, dw.y, G.ysum_a, G.nx, G.ny, M.tolisec, hl_upw, vl_upw, zl_upw);
-    upwind_state(a.Uin, up.z, up.w, dw.z, dw.w, G.ysum_b, G.nx, G.ny, M.tolisec, hr_upw, vr_upw, zr_upw);
+    upwind_state(a.Uin, up.x, up.y, dw.x, dw.y, G.ysum_a, G.nx, G.ny, M.tolisec, hl_upw, vl_upw);
+    upwind_state(a.Uin, up.z, up.w, dw.z, dw.w, G.ysum_b, G.nx, G.ny, M.tolisec, hr_upw, vr_upw);
   }
   constexpr int NDIR = (IFLUX >= 3) ? 10 : 6;
   const double w[10] = {wa.f1, wa.f2, wa.f3, wa.bx, wa.by, wb.f1, wb.f2, wb.f3, wb.bx, wb.by};
@@ -281,9 +282,9 @@ __global__ void __launch_bounds__(TILE_E) k_adj_edges(AdjArgs A) {
   for (int base = 0; base < NDIR; base += D) {
     Dual<D> o[10];
     interior_edge<IFLUX>(M, a.ilimiteur, a.flux_mode, G, dt, seed<D>(UA.x, 0, base), seed<D>(UA.y, 1, base),
-                         seed<D>(UA.z, 2, base), UA.w, seed<D>(UB.x, 3, base), seed<D>(UB.y, 4, base),
-                         seed<D>(UB.z, 5, base), UB.w, seed<D>(hl_upw, 6, base), seed<D>(vl_upw, 7, base), zl_upw,
-                         seed<D>(hr_upw, 8, base), seed<D>(vr_upw, 9, base), zr_upw, o, A.freeze_r != 0);
+                         seed<D>(UA.z, 2, base), ez.x, UA.w, seed<D>(UB.x, 3, base), seed<D>(UB.y, 4, base),
+                         seed<D>(UB.z, 5, base), ez.y, UB.w, seed<D>(hl_upw, 6, base), seed<D>(vl_upw, 7, base), ez.z,
+                         seed<D>(hr_upw, 8, base), seed<D>(vr_upw, 9, base), ez.w, o, A.freeze_r != 0);
 #pragma unroll
     for (int i = 0; i < D; ++i) {
       if (base + i < NDIR) {
@@ -384,9 +385,9 @@ int launch_replay_step(const StepArgs& a, const double* dt_hist, const double* t
   return chk(cudaGetLastError());
 }
 
-int launch_record(const double4* Unew, const MemberState* S, int nm, int p, int n, double* dt_hist, double* t_hist,
-                  const int32_t* gcell, int G, double* eta, stream_t s) {
-  k_record<<<1, 256, 0, reinterpret_cast<cudaStream_t>(s)>>>(Unew, S, nm, p, n, dt_hist, t_hist, gcell, G, eta);
+int launch_record(const double4* Unew, const double* zcell, const MemberState* S, int nm, int p, int n, double* dt_hist,
+                  double* t_hist, const int32_t* gcell, int G, double* eta, stream_t s) {
+  k_record<<<1, 256, 0, reinterpret_cast<cudaStream_t>(s)>>>(Unew, zcell, S, nm, p, n, dt_hist, t_hist, gcell, G, eta);
   return chk(cudaGetLastError());
 }
 

@@ -264,11 +264,11 @@ int forward_impl(cf_adjoint* a, int32_t replay, double* eta_out, double* state_o
     if (!replay) {
       sa.mst = a->mst;
       if ((rc = launch_step(sa, st, nullptr, nullptr))) return fail(c, rc, "step launch failed");
-      rc = launch_record(Y, a->mst, a->nm, p, k, a->dt_hist, a->t_hist, a->gcell, a->G, a->eta, st);
+      rc = launch_record(Y, c->zcell, a->mst, a->nm, p, k, a->dt_hist, a->t_hist, a->gcell, a->G, a->eta, st);
     } else {
       if ((rc = launch_replay_step(sa, a->dt_hist, a->t_hist, k, a->flag, nullptr, st)))
         return fail(c, rc, "replay launch failed");
-      rc = launch_record(Y, nullptr, a->nm, 0, k, a->dt_hist, a->t_hist, a->gcell, a->G, a->eta, st);
+      rc = launch_record(Y, c->zcell, nullptr, a->nm, 0, k, a->dt_hist, a->t_hist, a->gcell, a->G, a->eta, st);
     }
     if (rc) return fail(c, rc, "record launch failed");
     std::swap(X, Y);

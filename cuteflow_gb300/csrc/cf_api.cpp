@@ -53,6 +53,7 @@ StepArgs step_args(const cf_ctx* c, int parity) {
   a.ecell = c->ecell;
   a.egeo = c->egeo;
   a.ebid = c->ebid;
+  a.ez = c->ez;
   a.eupw = c->eupw;
   a.ewts = c->ewts;
   a.edk = c->edk;
@@ -80,7 +81,7 @@ StepArgs step_args(const cf_ctx* c, int parity) {
 
 void free_all(cf_ctx* c) {
   if (c->graph2) cudaGraphExecDestroy(c->graph2);
-  void* ptrs[] = {c->U[0], c->U[1], c->cslot, c->cstat, c->zcell, c->perm, c->iperm, c->ecell, c->egeo,
+  void* ptrs[] = {c->U[0], c->U[1], c->cslot, c->cstat, c->zcell, c->perm, c->iperm, c->ecell, c->egeo, c->ez,
                   c->ebid, c->eupw, c->ewts, c->edk, c->einv, c->slots, c->etile_mem, c->ctile_mem, c->mdev,
                   c->mst, c->staging, c->inl_cell, c->inl_len, c->ids};
   for (void* p : ptrs)
@@ -278,6 +279,7 @@ int create_impl(const cf_mesh* meshes, const cf_params* params, int32_t nm, cf_c
       (rc = dalloc(c, &c->zcell, c->n_pad)) || (rc = dalloc(c, &c->perm, c->n_pad)) ||
       (rc = dalloc(c, &c->iperm, c->n_pad)) || (rc = dalloc(c, &c->ecell, c->ne_pad)) ||
       (rc = dalloc(c, &c->egeo, c->ne_pad)) || (rc = dalloc(c, &c->ebid, c->ne_pad)) ||
+      (rc = dalloc(c, &c->ez, c->ne_pad)) ||
       (rc = dalloc(c, &c->slots, 2 * (size_t)c->ne_pad)) || (rc = dalloc(c, &c->etile_mem, c->n_etiles)) ||
       (rc = dalloc(c, &c->ctile_mem, c->n_ctiles)) || (rc = dalloc(c, &c->mdev, (size_t)nm)) ||
       (rc = dalloc(c, &c->mst, (size_t)nm)) || (rc = dalloc(c, &c->staging, 3 * (size_t)c->max_n)))
@@ -307,7 +309,8 @@ int create_impl(const cf_mesh* meshes, const cf_params* params, int32_t nm, cf_c
     if ((rc = put(c, c->cslot + co, cslot.data(), cslot.size())) || (rc = put(c, c->cstat + co, P.cstat.data(), P.cstat.size())) ||
         (rc = put(c, c->zcell + co, P.zcell.data(), P.zcell.size())) || (rc = put(c, c->perm + co, P.perm.data(), P.perm.size())) ||
         (rc = put(c, c->iperm + co, P.iperm.data(), P.iperm.size())) || (rc = put(c, c->ecell + eo, ecell.data(), ecell.size())) ||
-        (rc = put(c, c->egeo + eo, P.egeo.data(), P.egeo.size())) || (rc = put(c, c->ebid + eo, P.ebid.data(), P.ebid.size())))
+        (rc = put(c, c->egeo + eo, P.egeo.data(), P.egeo.size())) || (rc = put(c, c->ebid + eo, P.ebid.data(), P.ebid.size())) ||
+        (rc = put(c, c->ez + eo, P.ez.data(), P.ez.size())))
       return done(rc);
     if (second) {
       std::vector<int4> up(P.eupw);
@@ -337,6 +340,7 @@ int create_impl(const cf_mesh* meshes, const cf_params* params, int32_t nm, cf_c
     std::vector<double4>().swap(P.cstat);
     std::vector<int2>().swap(P.ecell);
     std::vector<double4>().swap(P.egeo);
+    std::vector<double4>().swap(P.ez);
     std::vector<int32_t>().swap(P.ebid);
     std::vector<HostEdge>().swap(P.edges);
   }

@@ -43,6 +43,7 @@ struct cf_ctx {
   int32_t* iperm = nullptr;  /* old -> new, member-local */
   int2* ecell = nullptr;
   double4* egeo = nullptr;
+  double4* ez = nullptr;   /* per edge: the beds it reads */
   int32_t* ebid = nullptr;
   int4* eupw = nullptr;
   double4* ewts = nullptr;

@@ -168,6 +168,10 @@ CFD_HD Dual<N> fabs(const Dual<N>& a) {
   return (a.v < 0.0) ? -a : a;
 }
 
+/* the reciprocal of a depth with its derivative (the stored RN(1/h) carries none) */
+template <int N>
+CFD_HD Dual<N> recip_h(const Dual<N>& h, double) { return 1.0 / h; }
+
 /* Quotient by a known reciprocal (div_rn in cf_flux.h): the value lane is the step's own
  * rounding; the lanes differentiate a / d. */
 template <int N>

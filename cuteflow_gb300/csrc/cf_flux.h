@@ -124,11 +124,18 @@ CF_HD CF_INLINE double cbrt_halley(double x) {
 
 /* ---- edge-frame states ------------------------------------------------------------------ */
 
-/* Masked primitive state in the frame (n, t) of an edge (flux_riemann.cuf:105-112). */
+/* RN(1/h) of an element's depth: the state carries it (the element kernel stores it with the
+ * new depth), so the quotients by h below are Markstein's exact three-instruction form.  A
+ * linearization computes it from h (cf_dual.h overloads this for its dual numbers). */
 template <class T>
-CF_HD CF_INLINE void to_frame(T h, T hu, T hv, double nx, double ny, double tolisec, T& hm, T& un, T& ut) {
+CF_HD CF_INLINE T recip_h(const T&, double yh) { return T(yh); }
+
+/* Masked primitive state in the frame (n, t) of an edge (flux_riemann.cuf:105-112); yh = RN(1/h). */
+template <class T>
+CF_HD CF_INLINE void to_frame(T h, T hu, T hv, double yh, double nx, double ny, double tolisec, T& hm, T& un,
+                              T& ut) {
   if (h > tolisec) {
-    const T y = 1.0 / h;
+    const T y = recip_h(h, yh);
     un = div_rn(hu * nx + hv * ny, h, y);
     ut = div_rn(hv * nx - hu * ny, h, y);
     hm = h;
@@ -141,9 +148,9 @@ CF_HD CF_INLINE void to_frame(T h, T hu, T hv, double nx, double ny, double toli
 
 /* Only the masked depth and tangential velocity (what the WAF upwind states use). */
 template <class T>
-CF_HD CF_INLINE void to_frame_t(T h, T hu, T hv, double nx, double ny, double tolisec, T& hm, T& ut) {
+CF_HD CF_INLINE void to_frame_t(T h, T hu, T hv, double yh, double nx, double ny, double tolisec, T& hm, T& ut) {
   if (h > tolisec) {
-    ut = (hv * nx - hu * ny) / h;
+    ut = div_rn(hv * nx - hu * ny, h, recip_h(h, yh));
     hm = h;
   } else {
     hm = T(0.0);
@@ -495,10 +502,11 @@ CF_HD CF_INLINE double inlet_discharge(const MemberDev& M, int id, double t) {
  * calcul_surf_entree's sum of length * depth over the edge's inlet at the step's start. */
 template <class T>
 CF_HD CF_INLINE void boundary_flux(int iflux, const MemberDev& M, int kind, int id, double t, double nx, double ny,
-                                   T h, T hu, T hv, double z, T& f1, T& f2, T& f3, T& q, double surf = 0.0) {
+                                   T h, T hu, T hv, double yh, double z, T& f1, T& f2, T& f3, T& q,
+                                   double surf = 0.0) {
   const double g = M.gp, tolisec = M.tolisec;
   T hautl, vitul, vitvl;
-  to_frame(h, hu, hv, nx, ny, tolisec, hautl, vitul, vitvl);
+  to_frame(h, hu, hv, yh, nx, ny, tolisec, hautl, vitul, vitvl);
   f1 = f2 = f3 = T(0.0);
   q = T(0.0);
   if (kind == -1) {
@@ -559,58 +567,60 @@ CF_HD CF_INLINE void boundary_flux(int iflux, const MemberDev& M, int kind, int 
  * (flux_riemann.cuf:240-366): a copy of element 1's masked state when d1 < 0 (one upwind
  * element, or the first-order fallback), else the centroid-distance weighted average of two. */
 template <class T>
-CF_HD CF_INLINE void upwind_mix(T h1, T hu1, T hv1, T h2, T hu2, T hv2, double d1, double d2, double ysum,
-                                double nx, double ny, double tolisec, T& hu_, T& vu_) {
+CF_HD CF_INLINE void upwind_mix(T h1, T hu1, T hv1, double yh1, T h2, T hu2, T hv2, double yh2, double d1,
+                                double d2, double ysum, double nx, double ny, double tolisec, T& hu_, T& vu_) {
   T a, va;
-  to_frame_t(h1, hu1, hv1, nx, ny, tolisec, a, va);
+  to_frame_t(h1, hu1, hv1, yh1, nx, ny, tolisec, a, va);
   if (d1 < 0.0) {
     hu_ = a;
     vu_ = va;
     return;
   }
   T b, vb;
-  to_frame_t(h2, hu2, hv2, nx, ny, tolisec, b, vb);
+  to_frame_t(h2, hu2, hv2, yh2, nx, ny, tolisec, b, vb);
   const double ds = d1 + d2;
   hu_ = div_rn(d1 * a + d2 * b, ds, ysum);
   vu_ = div_rn(d1 * va + d2 * vb, ds, ysum);
 }
 
-/* The same, loading the elements' states, and the matching bed elevation. */
+/* The bed elevation of an upwind reconstruction (flux_riemann.cuf:320-366): static, so the host
+ * preprocessing evaluates it once per edge side. */
+CF_HD CF_INLINE double upwind_bed(double z1, double z2, double d1, double d2, double ysum) {
+  return (d1 < 0.0) ? z1 : div_rn(d1 * z1 + d2 * z2, d1 + d2, ysum);
+}
+
+/* The same, loading the elements' states (w = RN(1/h)). */
 CF_HD CF_INLINE void upwind_state(const double4* U, int i1, int i2, double d1, double d2, double ysum, double nx,
-                                  double ny, double tolisec, double& hu_, double& vu_, double& zu_) {
+                                  double ny, double tolisec, double& hu_, double& vu_) {
   const double4 A1 = ld4(U + i1);
   if (d1 < 0.0) {
-    upwind_mix(A1.x, A1.y, A1.z, 0.0, 0.0, 0.0, d1, d2, ysum, nx, ny, tolisec, hu_, vu_);
-    zu_ = A1.w;
+    upwind_mix(A1.x, A1.y, A1.z, A1.w, 0.0, 0.0, 0.0, 0.0, d1, d2, ysum, nx, ny, tolisec, hu_, vu_);
     return;
   }
   const double4 A2 = ld4(U + i2);
-  upwind_mix(A1.x, A1.y, A1.z, A2.x, A2.y, A2.z, d1, d2, ysum, nx, ny, tolisec, hu_, vu_);
-  zu_ = div_rn(d1 * A1.w + d2 * A2.w, d1 + d2, ysum);
+  upwind_mix(A1.x, A1.y, A1.z, A1.w, A2.x, A2.y, A2.z, A2.w, d1, d2, ysum, nx, ny, tolisec, hu_, vu_);
 }
 
-/* The MUSCL form: (h, u_n, u_t) of one side's upwind reconstruction and its bed elevation
- * (flux_riemann.cuf:240-366 with the normal velocity as well). */
+/* The MUSCL form: (h, u_n, u_t) of one side's upwind reconstruction (flux_riemann.cuf:240-366
+ * with the normal velocity as well). */
 CF_HD CF_INLINE void upwind_state3(const double4* U, int i1, int i2, double d1, double d2, double ysum, double nx,
-                                   double ny, double tolisec, double& hu_, double& uu_, double& vu_, double& zu_) {
+                                   double ny, double tolisec, double& hu_, double& uu_, double& vu_) {
   const double4 A1 = ld4(U + i1);
   double a, ua, va;
-  to_frame(A1.x, A1.y, A1.z, nx, ny, tolisec, a, ua, va);
+  to_frame(A1.x, A1.y, A1.z, A1.w, nx, ny, tolisec, a, ua, va);
   if (d1 < 0.0) {
     hu_ = a;
     uu_ = ua;
     vu_ = va;
-    zu_ = A1.w;
     return;
   }
   const double4 A2 = ld4(U + i2);
   double b, ub, vb;
-  to_frame(A2.x, A2.y, A2.z, nx, ny, tolisec, b, ub, vb);
+  to_frame(A2.x, A2.y, A2.z, A2.w, nx, ny, tolisec, b, ub, vb);
   const double ds = d1 + d2;
   hu_ = div_rn(d1 * a + d2 * b, ds, ysum);
   uu_ = div_rn(d1 * ua + d2 * ub, ds, ysum);
   vu_ = div_rn(d1 * va + d2 * vb, ds, ysum);
-  zu_ = div_rn(d1 * A1.w + d2 * A2.w, ds, ysum);
 }
 
 /* ---- one edge ------------------------------------------------------------------------- */
@@ -628,15 +638,15 @@ struct EdgeGeo {
  * reconstructions of sides A and B (second order only), zl_upw / zr_upw their bed elevations. */
 template <int IFLUX, class T>
 CF_HD CF_INLINE void interior_edge(const MemberDev& M, int ilim, int flux_mode, const EdgeGeo& G, double dt, T hA,
-                                   T huA, T hvA, double zml, T hB, T huB, T hvB, double zmr, T hl_upw, T vl_upw,
-                                   double zl_upw, T hr_upw, T vr_upw, double zr_upw, T out[10],
+                                   T huA, T hvA, double zml, double yhA, T hB, T huB, T hvB, double zmr, double yhB,
+                                   T hl_upw, T vl_upw, double zl_upw, T hr_upw, T vr_upw, double zr_upw, T out[10],
                                    bool freeze_r = false) {
   const double g = M.gp, tolisec = M.tolisec;
   const double nx = G.nx, ny = G.ny, len = G.len;
   const double zij = dmax(zml, zmr);
   T hautl, vitul, vitvl, hautr, vitur, vitvr;
-  to_frame(hA, huA, hvA, nx, ny, tolisec, hautl, vitul, vitvl);
-  to_frame(hB, huB, hvB, nx, ny, tolisec, hautr, vitur, vitvr);
+  to_frame(hA, huA, hvA, yhA, nx, ny, tolisec, hautl, vitul, vitvl);
+  to_frame(hB, huB, hvB, yhB, nx, ny, tolisec, hautr, vitur, vitvr);
   TwoFluxT<T> F;
   if (IFLUX <= 2) {
     /* hydrostatic reconstruction (:176-181, :200-210): A from its masked depth, B from its
@@ -702,15 +712,15 @@ CF_HD CF_INLINE void interior_edge(const MemberDev& M, int ilim, int flux_mode, 
  * full (its slopes are not mirror images of the other side's).  upA / upB: (h, u_n, u_t) of
  * the upwind reconstructions of sides A and B in A's frame, zl_upw / zr_upw their beds. */
 CF_HD CF_INLINE void interior_edge_muscl(const MemberDev& M, int ilim, int flux_mode, const EdgeGeo& G, double dt,
-                                         double hA, double huA, double hvA, double zml, double hB, double huB,
-                                         double hvB, double zmr, const double upA[3], double zl_upw,
-                                         const double upB[3], double zr_upw, double out[10]) {
+                                         double hA, double huA, double hvA, double zml, double yhA, double hB,
+                                         double huB, double hvB, double zmr, double yhB, const double upA[3],
+                                         double zl_upw, const double upB[3], double zr_upw, double out[10]) {
   const double g = M.gp, tolisec = M.tolisec;
   const double nx = G.nx, ny = G.ny, len = G.len;
   const double zij = dmax(zml, zmr);
   double hautl, vitul, vitvl, hautr, vitur, vitvr;
-  to_frame(hA, huA, hvA, nx, ny, tolisec, hautl, vitul, vitvl);
-  to_frame(hB, huB, hvB, nx, ny, tolisec, hautr, vitur, vitvr);
+  to_frame(hA, huA, hvA, yhA, nx, ny, tolisec, hautl, vitul, vitvl);
+  to_frame(hB, huB, hvB, yhB, nx, ny, tolisec, hautr, vitur, vitvr);
   /* hydrostatic reconstruction of the four states (:370-400) */
   double hijet = dmax(0.0, hautl + zml - zij);
   double hlu = dmax(0.0, upA[0] + zl_upw - zij);
@@ -806,7 +816,8 @@ template <int IFLUX, class S = double>
 CF_HD CF_INLINE void edge_body(const StepArgs& a, const MemberDev& M, int e, double dt, double t,
                                const double* surf = nullptr) {
   const int2 ab = ldro(a.ecell + e);
-  const double4 UA = ld4(a.Uin + ab.x);
+  const double4 UA = ld4(a.Uin + ab.x);   /* {h, hu, hv, RN(1/h)} */
+  const double4 ez = ld4(a.ez + e);       /* bed of A, of B, of A's and B's upwind reconstructions */
   Slot* sa = a.slots + 2 * (size_t)e;
 
   if (ab.y < 0) {
@@ -815,7 +826,7 @@ CF_HD CF_INLINE void edge_body(const StepArgs& a, const MemberDev& M, int e, dou
     const int id = ldro(a.ebid + e);
     const double sf = (surf && ab.y == -1 && M.inlet == 3 && id >= 1 && id <= M.nin) ? surf[id - 1] : 0.0;
     double f1, f2, f3, q;
-    boundary_flux(IFLUX, M, ab.y, id, t, geo.x, geo.y, UA.x, UA.y, UA.z, UA.w, f1, f2, f3, q, sf);
+    boundary_flux(IFLUX, M, ab.y, id, t, geo.x, geo.y, UA.x, UA.y, UA.z, UA.w, ez.x, f1, f2, f3, q, sf);
     sa->f1 = f1 * len;
     sa->f2 = f2 * len;
     sa->f3 = f3 * len;
@@ -831,25 +842,25 @@ CF_HD CF_INLINE void edge_body(const StepArgs& a, const MemberDev& M, int e, dou
   if (IFLUX == 4) {
     const int4 up = ldro(a.eupw + e);
     const double4 dw = ld4(a.ewts + e);
-    double upA[3], upB[3], zl_upw, zr_upw;
-    upwind_state3(a.Uin, up.x, up.y, dw.x, dw.y, G.ysum_a, G.nx, G.ny, M.tolisec, upA[0], upA[1], upA[2], zl_upw);
-    upwind_state3(a.Uin, up.z, up.w, dw.z, dw.w, G.ysum_b, G.nx, G.ny, M.tolisec, upB[0], upB[1], upB[2], zr_upw);
-    interior_edge_muscl(M, a.ilimiteur, a.flux_mode, G, dt, UA.x, UA.y, UA.z, UA.w, UB.x, UB.y, UB.z, UB.w, upA,
-                        zl_upw, upB, zr_upw, o);
+    double upA[3], upB[3];
+    upwind_state3(a.Uin, up.x, up.y, dw.x, dw.y, G.ysum_a, G.nx, G.ny, M.tolisec, upA[0], upA[1], upA[2]);
+    upwind_state3(a.Uin, up.z, up.w, dw.z, dw.w, G.ysum_b, G.nx, G.ny, M.tolisec, upB[0], upB[1], upB[2]);
+    interior_edge_muscl(M, a.ilimiteur, a.flux_mode, G, dt, UA.x, UA.y, UA.z, ez.x, UA.w, UB.x, UB.y, UB.z, ez.y,
+                        UB.w, upA, ez.z, upB, ez.w, o);
     write_slots(sa, o);
     return;
   }
-  double hl_upw = 0.0, vl_upw = 0.0, zl_upw = 0.0, hr_upw = 0.0, vr_upw = 0.0, zr_upw = 0.0;
+  double hl_upw = 0.0, vl_upw = 0.0, hr_upw = 0.0, vr_upw = 0.0;
   if (IFLUX == 3) {
     const int4 up = ldro(a.eupw + e);
     const double4 dw = ld4(a.ewts + e);   /* d1, d2 of side A, d1, d2 of side B */
-    upwind_state(a.Uin, up.x, up.y, dw.x, dw.y, G.ysum_a, G.nx, G.ny, M.tolisec, hl_upw, vl_upw, zl_upw);
-    upwind_state(a.Uin, up.z, up.w, dw.z, dw.w, G.ysum_b, G.nx, G.ny, M.tolisec, hr_upw, vr_upw, zr_upw);
+    upwind_state(a.Uin, up.x, up.y, dw.x, dw.y, G.ysum_a, G.nx, G.ny, M.tolisec, hl_upw, vl_upw);
+    upwind_state(a.Uin, up.z, up.w, dw.z, dw.w, G.ysum_b, G.nx, G.ny, M.tolisec, hr_upw, vr_upw);
   }
   S os[10];
-  interior_edge<(IFLUX == 4 ? 3 : IFLUX)>(M, a.ilimiteur, a.flux_mode, G, dt, S(UA.x), S(UA.y), S(UA.z), UA.w,
-                                          S(UB.x), S(UB.y), S(UB.z), UB.w, S(hl_upw), S(vl_upw), zl_upw, S(hr_upw),
-                                          S(vr_upw), zr_upw, os);
+  interior_edge<(IFLUX == 4 ? 3 : IFLUX)>(M, a.ilimiteur, a.flux_mode, G, dt, S(UA.x), S(UA.y), S(UA.z), ez.x,
+                                          UA.w, S(UB.x), S(UB.y), S(UB.z), ez.y, UB.w, S(hl_upw), S(vl_upw), ez.z,
+                                          S(hr_upw), S(vr_upw), ez.w, os);
 #pragma unroll
   for (int i = 0; i < 10; ++i) o[i] = val(os[i]);
   write_slots(sa, o);
@@ -858,10 +869,9 @@ CF_HD CF_INLINE void edge_body(const StepArgs& a, const MemberDev& M, int e, dou
 /* ---- one element ------------------------------------------------------------------------ */
 
 /* CFL time step of one element (cfl_condition.cuf:20-37); cflL = cfl * L_cfl. */
-CF_HD CF_INLINE double cfl_dt_elem(const MemberDev& M, double cflL, double h, double hu, double hv) {
+CF_HD CF_INLINE double cfl_dt_elem(const MemberDev& M, double cflL, double h, double hu, double hv, double yh) {
   double d = 1000000.0;
   if (h > M.tolisec) {
-    const double yh = 1.0 / h;
     const double vu = div_rn(hu, h, yh), vv = div_rn(hv, h, yh);
     const double nv = sqrt(vu * vu + vv * vv);
     const double vmax = dmax(0.01, nv + sqrt(M.gp * fabs(h)));
@@ -877,13 +887,13 @@ CF_HD CF_INLINE double cfl_dt_elem(const MemberDev& M, double cflL, double h, do
  * fricimplic 0, gives m = {0, 1, 0, 0, 0, 1}. */
 template <class T>
 CF_HD CF_INLINE void friction_terms(const MemberDev& M, double area, double dt, T manning, T q1, T q2, T q3, T& sf2,
-                                    T& sf3, T m[6]) {
+                                    T& sf3, T m[6], double yq1) {
   const double gp = M.gp, tolisec = M.tolisec, tol = M.tol;
   sf2 = T(0.);
   sf3 = T(0.);
   m[0] = T(0.); m[1] = T(1.); m[2] = T(0.); m[3] = T(0.); m[4] = T(0.); m[5] = T(1.);
   if (q1 > tolisec) {
-    const T yq = 1.0 / q1;
+    const T yq = recip_h(q1, yq1);
     const T vitu = div_rn(q2, q1, yq), vitv = div_rn(q3, q1, yq);
     T normvit = sqrt(vitu * vitu + vitv * vitv);
     if (normvit < tol) normvit = T(tol);
@@ -925,11 +935,12 @@ CF_HD CF_INLINE void friction_terms(const MemberDev& M, double area, double dt, 
  * of the new depth is part of the map. */
 template <class T>
 CF_HD CF_INLINE void element_core(const MemberDev& M, double area, double yarea, T manning, T q1, T q2, T q3, T rc1,
-                                  T rc2, T rc3, T sb2, T sb3, double dt, T& h, T& hu, T& hv, bool& nonfinite) {
+                                  T rc2, T rc3, T sb2, T sb3, double dt, T& h, T& hu, T& hv, bool& nonfinite,
+                                  double yq1) {
   T r1, r2, r3;
   if (M.friction == 1) {
     T sf2, sf3, m[6];
-    friction_terms(M, area, dt, manning, q1, q2, q3, sf2, sf3, m);
+    friction_terms(M, area, dt, manning, q1, q2, q3, sf2, sf3, m, yq1);
     const T ri1 = div_rn(0. + 0. - rc1, area, yarea);
     const T ri2 = div_rn(sb2 + sf2 - rc2, area, yarea);
     const T ri3 = div_rn(sb3 + sf3 - rc3, area, yarea);
@@ -971,8 +982,10 @@ CF_HD CF_INLINE double4 element_update(const MemberDev& M, const double4 U, cons
   const double sb3 = s0.by + s1.by + s2.by;
   S h, hu, hv;
   element_core(M, st.x, st.w, S(st.y), S(U.x), S(U.y), S(U.z), S(rc1), S(rc2), S(rc3), S(sb2), S(sb3), dt, h, hu,
-               hv, nonfinite);
-  return make_double4(val(h), val(hu), val(hv), U.w);
+               hv, nonfinite, U.w);
+  /* the new state carries RN(1/h) for the next step's quotients by h */
+  const double hn = val(h);
+  return make_double4(hn, val(hu), val(hv), hn > 0.0 ? 1.0 / hn : 0.0);
 }
 
 }  // namespace cf

@@ -3,7 +3,8 @@
  * (cf_api.cpp) and the sm_103a kernels (cf_kernels.cu).
  *
  * Device layout (all arrays in space-filling-curve order, see cf_mesh.cpp):
- *   cells  U[2]  : double4 {h, hu, hv, z} per element, ping-pong (state n in U[n & 1])
+ *   cells  U[2]  : double4 {h, hu, hv, RN(1/h) (0 where h = 0)} per element, ping-pong (state n in
+ *                  U[n & 1]); the bed elevations live in zcell and, per edge, in ez
  *          cslot : int4 {slot of local edge 0, 1, 2, -}   (local edges in the reference's order)
  *          cstat : double4 {area, Manning n, cfl*L_cfl, RN(1/area)}
  *   edges  ecell : int2 {A, B}; B >= 0 another element, B < 0 the boundary kind (-1/-2/-3)
@@ -97,6 +98,7 @@ struct StepArgs {
   double4* Uout;
   const int4* cslot;
   const double4* cstat;
+  const double4* ez;       /* per edge: bed of A, of B, of the upwind reconstructions of A and B */
   const int2* ecell;
   const double4* egeo;
   const int32_t* ebid;
@@ -153,6 +155,7 @@ struct Prep {
   std::vector<double4> ewts;
   std::vector<double4> edk;
   std::vector<double4> einv;
+  std::vector<double4> ez;        /* per edge: zA, zB, upwind bed of A and of B (second order) */
   /* phys_inflow: one entry per (element, inflow edge) in reference order (compute_input_elems,
    * maillage.cuf:1333-1363): its element (new order) and, per inlet number 1..nin, the length
    * of the element's last inflow edge of that number (0 if none), as calcul_surf_entree
@@ -216,9 +219,9 @@ struct AdjArgs {
  * OR-ed into *flag. */
 int launch_replay_step(const StepArgs& a, const double* dt_hist, const double* t_hist, int n, uint32_t* flag,
                        Slot* sums, stream_t s);
-/* gauge elevations of Unew into eta row n; with S, also dt / t of parity p into the histories */
-int launch_record(const double4* Unew, const MemberState* S, int nm, int p, int n, double* dt_hist, double* t_hist,
-                  const int32_t* gcell, int G, double* eta, stream_t s);
+/* gauge elevations h + z of Unew into eta row n; with S, also dt / t of parity p into the histories */
+int launch_record(const double4* Unew, const double* zcell, const MemberState* S, int nm, int p, int n, double* dt_hist,
+                  double* t_hist, const int32_t* gcell, int G, double* eta, stream_t s);
 int launch_adjoint_step(const AdjArgs& A, stream_t s);
 /* lambda^0 = lam_own + the edge contributions of the last reverse step, into lam_own */
 int launch_adjoint_final(const AdjArgs& A, stream_t s);

@@ -161,7 +161,7 @@ __global__ void __launch_bounds__(TILE_C) k_cells(StepArgs a) {
     double4* o = a.Uout + c;
     reinterpret_cast<double2*>(o)[0] = make_double2(V.x, V.y);
     reinterpret_cast<double2*>(o)[1] = make_double2(V.z, V.w);
-    dti = cfl_dt_elem(M, st.z, V.x, V.y, V.z);
+    dti = cfl_dt_elem(M, st.z, V.x, V.y, V.z, V.w);
   }
   block_min_atomic(dti, &S->dt[1 - p]);
 }
@@ -176,7 +176,7 @@ __global__ void __launch_bounds__(TILE_C) k_cfl(const double4* U, const double4*
   double dti = 1.0e300;
   if (c < M.cell_end) {
     const double4 u = ld4(U + c);
-    dti = cfl_dt_elem(M, ld4(cstat + c).z, u.x, u.y, u.z);
+    dti = cfl_dt_elem(M, ld4(cstat + c).z, u.x, u.y, u.z, u.w);
   }
   block_min_atomic(dti, &mst[m].dt[slot]);
 }
@@ -230,7 +230,8 @@ __global__ void k_scatter(const double* hu3, const int32_t* perm, const double* 
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= n) return;
   const int o = perm[c];
-  U[c] = make_double4(hu3[3 * (size_t)o], hu3[3 * (size_t)o + 1], hu3[3 * (size_t)o + 2], zcell[c]);
+  const double h = hu3[3 * (size_t)o];
+  U[c] = make_double4(h, hu3[3 * (size_t)o + 1], hu3[3 * (size_t)o + 2], h > 0.0 ? 1.0 / h : 0.0);
 }
 
 __global__ void k_gather(const double4* U, const int32_t* iperm, double* hu3, int n) {
@@ -256,8 +257,9 @@ __global__ void k_scatter_ids(double4* U, const int32_t* iperm, const int32_t* i
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   double4* u = U + iperm[ids[i]];
-  reinterpret_cast<double2*>(u)[0] = make_double2(in[3 * (size_t)i], in[3 * (size_t)i + 1]);
-  u->z = in[3 * (size_t)i + 2];
+  const double h = in[3 * (size_t)i];
+  reinterpret_cast<double2*>(u)[0] = make_double2(h, in[3 * (size_t)i + 1]);
+  reinterpret_cast<double2*>(u)[1] = make_double2(in[3 * (size_t)i + 2], h > 0.0 ? 1.0 / h : 0.0);
 }
 
 int check(cudaError_t e) { return e == cudaSuccess ? CF_OK : CF_ECUDA; }

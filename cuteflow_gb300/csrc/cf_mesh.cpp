@@ -17,6 +17,7 @@
 #include <cstring>
 #include <numeric>
 
+#include "cf_flux.h"
 #include "cf_internal.h"
 
 namespace cf {
@@ -361,6 +362,20 @@ int prepare_mesh(const cf_mesh* m, const cf_params* p, Prep& P, std::string& err
       }
     }
     P.egeo[e] = make_double4(n1, n2, ln, inv_d);
+  }
+  /* the beds an edge reads: its elements' and, second order, its upwind reconstructions' (the
+   * distance-weighted bed of two upwind elements, flux_riemann.cuf:320-366; static) */
+  P.ez.resize(ne);
+  for (size_t e = 0; e < ne; ++e) {
+    const HostEdge& E = P.edges[e];
+    double4 z = make_double4(P.zcell[E.a], E.b >= 0 ? P.zcell[E.b] : 0.0, 0.0, 0.0);
+    if (second && E.b >= 0) {
+      const int4 u = P.eupw[e];
+      const double4 w = P.ewts[e], yi = P.einv[e];
+      z.z = upwind_bed(P.zcell[u.x], P.zcell[u.y], w.x, w.y, yi.y);
+      z.w = upwind_bed(P.zcell[u.z], P.zcell[u.w], w.z, w.w, yi.z);
+    }
+    P.ez[e] = z;
   }
   return CF_OK;
 }

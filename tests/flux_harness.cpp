@@ -89,7 +89,7 @@ extern "C" int harness_edge_fluxes(const cf_mesh* m, const cf_params* p, const d
   std::vector<double4> Un(n);
   for (int c = 0; c < n; ++c) {
     int o = P.perm[c];
-    Un[c] = make_double4(U[3 * o], U[3 * o + 1], U[3 * o + 2], P.zcell[c]);
+    Un[c] = make_double4(U[3 * o], U[3 * o + 1], U[3 * o + 2], U[3 * o] > 0.0 ? 1.0 / U[3 * o] : 0.0);
   }
   MemberDev M;
   fill_member(M, p, P);
@@ -98,7 +98,7 @@ extern "C" int harness_edge_fluxes(const cf_mesh* m, const cf_params* p, const d
   StepArgs a;
   std::memset(&a, 0, sizeof(a));
   a.Uin = Un.data();
-  a.ecell = P.ecell.data(); a.egeo = P.egeo.data(); a.ebid = P.ebid.data();
+  a.ecell = P.ecell.data(); a.egeo = P.egeo.data(); a.ebid = P.ebid.data(); a.ez = P.ez.data();
   a.eupw = P.eupw.empty() ? nullptr : P.eupw.data();
   a.ewts = P.ewts.empty() ? nullptr : P.ewts.data();
   a.edk = P.edk.empty() ? nullptr : P.edk.data();
@@ -140,7 +140,7 @@ extern "C" int harness_run(const cf_mesh* m, const cf_params* p, const double* U
   std::vector<double4> Ua(n), Ub(n);
   for (int c = 0; c < n; ++c) {
     int o = P.perm[c];
-    Ua[c] = make_double4(U[3 * o], U[3 * o + 1], U[3 * o + 2], P.zcell[c]);
+    Ua[c] = make_double4(U[3 * o], U[3 * o + 1], U[3 * o + 2], U[3 * o] > 0.0 ? 1.0 / U[3 * o] : 0.0);
   }
   MemberDev M;
   fill_member(M, p, P);
@@ -148,7 +148,7 @@ extern "C" int harness_run(const cf_mesh* m, const cf_params* p, const double* U
   std::vector<Slot> slots(2 * (size_t)ne);
   StepArgs a;
   std::memset(&a, 0, sizeof(a));
-  a.ecell = P.ecell.data(); a.egeo = P.egeo.data(); a.ebid = P.ebid.data();
+  a.ecell = P.ecell.data(); a.egeo = P.egeo.data(); a.ebid = P.ebid.data(); a.ez = P.ez.data();
   a.eupw = P.eupw.empty() ? nullptr : P.eupw.data();
   a.ewts = P.ewts.empty() ? nullptr : P.ewts.data();
   a.edk = P.edk.empty() ? nullptr : P.edk.data();
@@ -158,7 +158,7 @@ extern "C" int harness_run(const cf_mesh* m, const cf_params* p, const double* U
   double4* cur = Ua.data();
   double4* nxt = Ub.data();
   double dt = M.dt_reset;
-  for (int c = 0; c < n; ++c) dt = dmin(dt, cfl_dt_elem(M, P.cstat[c].z, cur[c].x, cur[c].y, cur[c].z));
+  for (int c = 0; c < n; ++c) dt = dmin(dt, cfl_dt_elem(M, P.cstat[c].z, cur[c].x, cur[c].y, cur[c].z, cur[c].w));
   if (dt_hist) dt_hist[0] = dt;
   double t = 0.0;
   for (int s = 0; s < nsteps; ++s) {
@@ -179,7 +179,7 @@ extern "C" int harness_run(const cf_mesh* m, const cf_params* p, const double* U
       nxt[c] = g_xd == 0 ? element_update(M, cur[c], P.cstat[c], slots[sl[0]], slots[sl[1]], slots[sl[2]], dt, nf)
                : g_xd == 1 ? element_update<XD<false>>(M, cur[c], P.cstat[c], slots[sl[0]], slots[sl[1]], slots[sl[2]], dt, nf)
                            : element_update<XD<true>>(M, cur[c], P.cstat[c], slots[sl[0]], slots[sl[1]], slots[sl[2]], dt, nf);
-      next = dmin(next, cfl_dt_elem(M, P.cstat[c].z, nxt[c].x, nxt[c].y, nxt[c].z));
+      next = dmin(next, cfl_dt_elem(M, P.cstat[c].z, nxt[c].x, nxt[c].y, nxt[c].z, nxt[c].w));
     }
     t = t + dt;
     dt = next;
@@ -315,8 +315,8 @@ extern "C" int harness_tangent(const cf_mesh* m, const cf_params* p, const doubl
       D1* sa = &slot[10 * (size_t)e];
       if (ab.y < 0) {
         D1 f1, f2, f3, q;
-        boundary_flux(p->iflux, M, ab.y, P.ebid[e], t, geo.x, geo.y, h[ab.x], hu[ab.x], hv[ab.x], z[ab.x], f1, f2, f3,
-                      q);
+        boundary_flux(p->iflux, M, ab.y, P.ebid[e], t, geo.x, geo.y, h[ab.x], hu[ab.x], hv[ab.x], 0.0, z[ab.x], f1, f2,
+                      f3, q);
         sa[0] = f1 * geo.z; sa[1] = f2 * geo.z; sa[2] = f3 * geo.z; sa[3] = D1(0.0); sa[4] = D1(0.0);
         continue;
       }
@@ -331,22 +331,22 @@ extern "C" int harness_tangent(const cf_mesh* m, const cf_params* p, const doubl
         Gm.y_mrl = yi.x; Gm.d_mkvol = dk.x; Gm.y_mkvol = dk.z; Gm.d_mkvoisin = dk.y; Gm.y_mkvoisin = dk.w;
         Gm.ysum_a = yi.y; Gm.ysum_b = yi.z;
         const int a2 = dw.x < 0.0 ? up.x : up.y, b2 = dw.z < 0.0 ? up.z : up.w;
-        upwind_mix(h[up.x], hu[up.x], hv[up.x], h[a2], hu[a2], hv[a2], dw.x, dw.y, yi.y, geo.x, geo.y, M.tolisec, hlu,
-                   vlu);
-        upwind_mix(h[up.z], hu[up.z], hv[up.z], h[b2], hu[b2], hv[b2], dw.z, dw.w, yi.z, geo.x, geo.y, M.tolisec, hru,
-                   vru);
+        upwind_mix(h[up.x], hu[up.x], hv[up.x], 0.0, h[a2], hu[a2], hv[a2], 0.0, dw.x, dw.y, yi.y, geo.x, geo.y,
+                   M.tolisec, hlu, vlu);
+        upwind_mix(h[up.z], hu[up.z], hv[up.z], 0.0, h[b2], hu[b2], hv[b2], 0.0, dw.z, dw.w, yi.z, geo.x, geo.y,
+                   M.tolisec, hru, vru);
         zlu = dw.x < 0.0 ? z[up.x] : div_rn(dw.x * z[up.x] + dw.y * z[up.y], dw.x + dw.y, yi.y);
         zru = dw.z < 0.0 ? z[up.z] : div_rn(dw.z * z[up.z] + dw.w * z[up.w], dw.z + dw.w, yi.z);
       }
       if (p->iflux == 1)
-        interior_edge<1>(M, p->ilimiteur, p->flux_mode, Gm, dt, h[ab.x], hu[ab.x], hv[ab.x], z[ab.x], h[ab.y],
-                         hu[ab.y], hv[ab.y], z[ab.y], hlu, vlu, zlu, hru, vru, zru, sa);
+        interior_edge<1>(M, p->ilimiteur, p->flux_mode, Gm, dt, h[ab.x], hu[ab.x], hv[ab.x], z[ab.x], 0.0, h[ab.y],
+                         hu[ab.y], hv[ab.y], z[ab.y], 0.0, hlu, vlu, zlu, hru, vru, zru, sa);
       else if (p->iflux == 2)
-        interior_edge<2>(M, p->ilimiteur, p->flux_mode, Gm, dt, h[ab.x], hu[ab.x], hv[ab.x], z[ab.x], h[ab.y],
-                         hu[ab.y], hv[ab.y], z[ab.y], hlu, vlu, zlu, hru, vru, zru, sa);
+        interior_edge<2>(M, p->ilimiteur, p->flux_mode, Gm, dt, h[ab.x], hu[ab.x], hv[ab.x], z[ab.x], 0.0, h[ab.y],
+                         hu[ab.y], hv[ab.y], z[ab.y], 0.0, hlu, vlu, zlu, hru, vru, zru, sa);
       else
-        interior_edge<3>(M, p->ilimiteur, p->flux_mode, Gm, dt, h[ab.x], hu[ab.x], hv[ab.x], z[ab.x], h[ab.y],
-                         hu[ab.y], hv[ab.y], z[ab.y], hlu, vlu, zlu, hru, vru, zru, sa, freeze_r != 0);
+        interior_edge<3>(M, p->ilimiteur, p->flux_mode, Gm, dt, h[ab.x], hu[ab.x], hv[ab.x], z[ab.x], 0.0, h[ab.y],
+                         hu[ab.y], hv[ab.y], z[ab.y], 0.0, hlu, vlu, zlu, hru, vru, zru, sa, freeze_r != 0);
     }
     for (int c = 0; c < n; ++c) {
       const int* sl = &P.cslot[c].x;
@@ -357,7 +357,7 @@ extern "C" int harness_tangent(const cf_mesh* m, const cf_params* p, const doubl
       const D1 sb2 = s0[3] + s1[3] + s2[3], sb3 = s0[4] + s1[4] + s2[4];
       bool nf = false;
       element_core(M, P.cstat[c].x, P.cstat[c].w, nm[c], h[c], hu[c], hv[c], rc1, rc2, rc3, sb2, sb3, dt, nh[c],
-                   nhu[c], nhv[c], nf);
+                   nhu[c], nhv[c], nf, 0.0);
     }
     h.swap(nh);
     hu.swap(nhu);
