@@ -191,12 +191,12 @@ CFD_HD Dual<N> div_rn(const Dual<N>& a, double d, double y) {
   return r;
 }
 
-/* x^(1/3): d/dx = 1 / (3 c^2) with c the cube root */
+/* x^(-1/3): d/dx = -r / (3 x) with r = x^(-1/3) */
 template <int N>
-CFD_HD Dual<N> cbrt_halley(const Dual<N>& x) {
+CFD_HD Dual<N> rcbrt(const Dual<N>& x) {
   Dual<N> r;
-  r.v = cbrt_halley(x.v);
-  const double k = 1.0 / (3.0 * r.v * r.v);
+  r.v = rcbrt(x.v);
+  const double k = -(r.v / (3.0 * x.v));
 #pragma unroll
   for (int i = 0; i < N; ++i) r.d[i] = x.d[i] * k;
   return r;

@@ -102,24 +102,74 @@ CF_HD CF_INLINE double div_rn(double a, double d, double y) {
 
 /* ---- x**(-1/3) -------------------------------------------------------------------------- */
 
-/* x^(1/3) for x > 0 by Halley's iteration y <- y (y^3 + 2m) / (2 y^3 + m) on the mantissa
- * m in [0.5, 4) (exponent split off exactly by frexp/ldexp), three iterations from the
- * linear start 0.6 + 0.25 m; within 3 ulp of the exact root.  The same fixed sequence of
- * IEEE operations runs in the oracle, so the Manning factor h^(-1/3)
- * (source_terms.cuf:112-127) is reproduced exactly on both sides. */
-CF_HD CF_INLINE double cbrt_halley(double x) {
-  int e;
-  double m = frexp(x, &e);
-  int r = e % 3;
-  if (r < 0) r += 3;
-  m = ldexp(m, r);
-  e -= r;
-  double y = 0.6 + 0.25 * m;
-  for (int i = 0; i < 3; ++i) {
-    const double y3 = y * y * y;
-    y = y * (y3 + 2.0 * m) / (2.0 * y3 + m);
+/* x^(-1/3), the Manning factor h^(-1/3) (source_terms.cuf:112-127; the reference calls pow, which
+ * is not correctly rounded and differs between math libraries), as one fixed sequence of IEEE and
+ * integer operations that the oracle repeats exactly, with no division:
+ *   x = m 2^(3k), m in [1, 8): the exponent split in integer arithmetic (Kahan, "Computing a real
+ *       cube root", 1991, splits the exponent by three the same way);
+ *   a single-precision seed for m^(-1/3): a cubic in the leading mantissa bits u = 1 + f
+ *       (least-squares fit of u^(-1/3) on [1, 2), relative error 2.5e-4) times 2^(-r/3), then one
+ *       Newton step y <- y + y (1 - m y^3) / 3 (relative error ~2e-7);
+ *   one third-order step in double precision, y <- y + y (e/3 + 2 e^2/9) with e = 1 - m y^3 (the
+ *       series of (1 - e)^(-1/3) to second order; the truncation is below 1e-19 relative);
+ *   y 2^(-k) by an exponent shift.
+ * Rounding bound 1.2 ulp (the two products forming y^3 give e an error of 2^-52, a third of it
+ * reaches y; then the final rounding); measured within 1 ulp of the exact value (tests).  Seven
+ * FP64-pipe instructions.  Zero, subnormal, infinite, negative and NaN x (never reached by the
+ * step, whose depths here exceed tolisec > 0) take rcbrt_special. */
+CF_HD CF_INLINE double rcbrt_core(uint64_t b) {
+  const uint32_t ex = (uint32_t)(b >> 52);
+  const uint32_t ep = ex + 177u;            /* unbiased exponent + 1200 */
+  const uint32_t k3 = ep / 3u;
+  const uint32_t r = ep - 3u * k3;          /* exponent = 3 (k3 - 400) + r */
+  const uint64_t frac = b & ((1ull << 52) - 1);
+  const uint64_t mb = frac | ((uint64_t)(1023u + r) << 52);
+  const uint32_t ub = (127u << 23) | (uint32_t)(frac >> 29);
+  const uint32_t mfb = ub + (r << 23);
+  double m;
+  float u, mf;
+  memcpy(&m, &mb, sizeof(m));
+  memcpy(&u, &ub, sizeof(u));
+  memcpy(&mf, &mfb, sizeof(mf));
+  float y = fmaf(fmaf(fmaf(-0x1.99153cp-5f, u, 0x1.45621ap-2f), u, -0x1.9eb31ap-1f), u, 0x1.8ab91ap+0f);
+  y = y * (r == 0u ? 1.0f : (r == 1u ? 0x1.965feap-1f : 0x1.428a30p-1f));
+  const float e32 = fmaf(-mf, y * y * y, 1.0f);
+  y = fmaf(y, e32 * 0x1.555556p-2f, y);
+  const double yd = (double)y;
+  const double e = fma(-m, yd * yd * yd, 1.0);
+  const double c = e * fma(e, 2.0 / 9.0, 1.0 / 3.0);
+  const double res = fma(yd, c, yd);
+  uint64_t rb;
+  memcpy(&rb, &res, sizeof(rb));
+  rb = (uint64_t)((int64_t)rb - ((int64_t)k3 - 400) * (int64_t)(1ull << 52));
+  double out;
+  memcpy(&out, &rb, sizeof(out));
+  return out;
+}
+
+/* x^(-1/3) outside the normal positive numbers: +0 -> +inf, subnormal -> scaled by 2^54 into the
+ * normal range (x^(-1/3) = (2^54 x)^(-1/3) 2^18, exact scalings), +inf -> 0, negative or NaN ->
+ * NaN (Fortran's real power of a negative base). */
+CF_HD CF_INLINE double rcbrt_special(double x) {
+  if (!(x >= 0.0)) {
+    const uint64_t qnan = 0x7ff8000000000000ull;
+    double n;
+    memcpy(&n, &qnan, sizeof(n));
+    return (x != x) ? x : n;
   }
-  return ldexp(y, e / 3);
+  if (x == 0.0) return 1.0 / x;
+  if (x > 1.0) return 0.0;
+  const double s = x * 0x1p54;
+  uint64_t b;
+  memcpy(&b, &s, sizeof(b));
+  return rcbrt_core(b) * 0x1p18;
+}
+
+CF_HD CF_INLINE double rcbrt(double x) {
+  uint64_t b;
+  memcpy(&b, &x, sizeof(b));
+  if ((uint32_t)(b >> 52) - 1u >= 2046u) return rcbrt_special(x);
+  return rcbrt_core(b);
 }
 
 /* ---- edge-frame states ------------------------------------------------------------------ */
@@ -897,7 +947,7 @@ CF_HD CF_INLINE void friction_terms(const MemberDev& M, double area, double dt, 
     const T vitu = div_rn(q2, q1, yq), vitv = div_rn(q3, q1, yq);
     T normvit = sqrt(vitu * vitu + vitv * vitv);
     if (normvit < tol) normvit = T(tol);
-    const T p13 = 1.0 / cbrt_halley(q1);    /* q1**(-1/3) */
+    const T p13 = rcbrt(q1);                /* q1**(-1/3) */
     sf2 = -(gp * manning * manning * vitu * normvit * area * p13);
     sf3 = -(gp * manning * manning * vitv * normvit * area * p13);
     if (normvit > tol) {

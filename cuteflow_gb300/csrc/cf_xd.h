@@ -137,7 +137,7 @@ CF_XD_CMP(!=, !xeq(x, y))
 #undef CF_XD_CMP
 
 template <bool MUL> XD_HD XD<MUL> sqrt(const XD<MUL>& a) { return XD<MUL>(::sqrt(a.v)); }
-template <bool MUL> XD_HD XD<MUL> cbrt_halley(const XD<MUL>& a) { return XD<MUL>(cbrt_halley(a.v)); }
+template <bool MUL> XD_HD XD<MUL> rcbrt(const XD<MUL>& a) { return XD<MUL>(rcbrt(a.v)); }
 template <bool MUL> XD_HD XD<MUL> fabs(const XD<MUL>& a) { return XD<MUL>(xdbl(xbits(a.v) & 0x7fffffffffffffffull)); }
 
 /* Markstein's quotient (div_rn in cf_flux.h) with the product on the chosen path */

@@ -25,12 +25,29 @@
 #include <chrono>
 #include <cmath>
 #include <cstring>
+#include <limits>
 #include <vector>
 #ifdef _OPENMP
 #include <omp.h>
 #endif
 
 namespace {
+
+uint64_t double_bits(double x) {
+  uint64_t b;
+  std::memcpy(&b, &x, sizeof(b));
+  return b;
+}
+double bits_double(uint64_t b) {
+  double x;
+  std::memcpy(&x, &b, sizeof(x));
+  return x;
+}
+float bits_float(uint32_t b) {
+  float x;
+  std::memcpy(&x, &b, sizeof(x));
+  return x;
+}
 
 /* Fortran default-real literals of the reference, rounded to single precision. */
 const double EPS_HLLC = (double)1e-8f;    /* flux_riemann.cuf:926 */
@@ -210,23 +227,42 @@ bool do_setup(Setup& S, const orc_mesh* m) {
 
 /* The reference raises the depth to -1/3 and -4/3 with the compiler's pow
  * (source_terms.cuf:112,119-120,127).  pow is not correctly rounded and differs between math
- * libraries, so the restatement fixes one evaluation: x^(1/3) by Halley's iteration
- * y <- y (y^3 + 2m) / (2 y^3 + m) on the mantissa m in [0.5, 4) (exponent split off exactly),
- * three iterations from 0.6 + 0.25 m, within 3 ulp of the root; then q^(-1/3) = 1/cbrt(q)
- * and q^(-4/3) = q^(-1/3)/q. */
-double cbrt_halley(double x) {
-  int e;
-  double m = std::frexp(x, &e);
-  int r = e % 3;
-  if (r < 0) r += 3;
-  m = std::ldexp(m, r);
-  e -= r;
-  double y = 0.6 + 0.25 * m;
-  for (int i = 0; i < 3; ++i) {
-    const double y3 = y * y * y;
-    y = y * (y3 + 2.0 * m) / (2.0 * y3 + m);
-  }
-  return std::ldexp(y, e / 3);
+ * libraries, so the restatement fixes one evaluation of q^(-1/3), with no division:
+ *   q = m 2^(3k), m in [1, 8), by integer arithmetic on the exponent field;
+ *   a float seed for m^(-1/3): the cubic c0 + u (c1 + u (c2 + u c3)) in u = 1 + f (the leading 23
+ *   mantissa bits; c = least-squares fit of u^(-1/3) on [1, 2)), times the float 2^(-r/3), then
+ *   y <- y + y (1 - mf y^3) (1/3) in float with mf = u 2^r;
+ *   in double: e = 1 - m y^3, y <- y + y e (1/3 + 2e/9), then y 2^(-k).
+ * Every step is a named IEEE operation (fma / fmaf where written), within 1.2 ulp of the exact
+ * power.  q^(-4/3) = q^(-1/3) / q. */
+double rcbrt_normal(uint64_t b) {
+  const uint32_t ex = (uint32_t)(b >> 52);
+  const uint32_t k3 = (ex + 177u) / 3u;        /* exponent - 1023 + 1200 = 3 k3 + r */
+  const uint32_t r = ex + 177u - 3u * k3;
+  const uint64_t frac = b & 0x000fffffffffffffull;
+  const double m = bits_double(frac | ((uint64_t)(1023u + r) << 52));
+  const float u = bits_float((127u << 23) | (uint32_t)(frac >> 29));
+  const float mf = bits_float(((127u + r) << 23) | (uint32_t)(frac >> 29));
+  const float c0 = 0x1.8ab91ap+0f, c1 = -0x1.9eb31ap-1f, c2 = 0x1.45621ap-2f, c3 = -0x1.99153cp-5f;
+  const float s_r[3] = {1.0f, 0x1.965feap-1f, 0x1.428a30p-1f};   /* 2^(-1/3), 2^(-2/3) as floats */
+  float y = std::fma(std::fma(std::fma(c3, u, c2), u, c1), u, c0) * s_r[r];
+  const float y3 = y * y * y;
+  y = std::fma(y, std::fma(-mf, y3, 1.0f) * 0x1.555556p-2f, y);
+  const double yd = y;
+  const double e = std::fma(-m, yd * yd * yd, 1.0);
+  const double v = std::fma(yd, e * std::fma(e, 2.0 / 9.0, 1.0 / 3.0), yd);
+  return bits_double(double_bits(v) - (uint64_t)((int64_t)k3 - 400) * (1ull << 52));
+}
+
+double rcbrt(double q) {
+  const uint64_t b = double_bits(q);
+  const uint32_t ex = (uint32_t)(b >> 52);
+  if (ex >= 1u && ex <= 2046u) return rcbrt_normal(b);
+  if (std::isnan(q)) return q;
+  if (q < 0.0) return std::numeric_limits<double>::quiet_NaN();
+  if (q == 0.0) return 1.0 / q;
+  if (std::isinf(q)) return 0.0;
+  return rcbrt_normal(double_bits(q * 0x1p54)) * 0x1p18;      /* subnormal */
 }
 
 /* ---- Riemann solvers ---------------------------------------------------------------- */
@@ -750,13 +786,13 @@ void cell_update(const Ctx& C, const double* U0, const double* resc, int gi, dou
       vitv = q3 / q1;
       normvit = std::sqrt(vitu * vitu + vitv * vitv);
       if (normvit < tol) normvit = tol;
-      const double p13 = 1.0 / cbrt_halley(q1); /* q1**(-1/3) */
+      const double p13 = rcbrt(q1); /* q1**(-1/3) */
       sf[1] = -(gp * manning * manning * vitu * normvit * area * p13);
       sf[2] = -(gp * manning * manning * vitv * normvit * area * p13);
     }
     if (prm->fricimplic == 1) {
       if (normvit > tol && q1 > tolisec) {
-        double dtgn2h = dt / 2.0 * gp * manning * manning * (1.0 / cbrt_halley(q1) / q1);
+        double dtgn2h = dt / 2.0 * gp * manning * manning * (rcbrt(q1) / q1);
         double af21 = -(7.0 / 3.0 * dtgn2h * vitu * normvit);
         double af22 = 1.0 + dtgn2h * (2 * (vitu * vitu) + vitv * vitv) / normvit;
         double af23 = dtgn2h * vitu * vitv / normvit;
@@ -774,7 +810,7 @@ void cell_update(const Ctx& C, const double* U0, const double* resc, int gi, dou
       }
     } else if (prm->fricimplic == 2) {
       if (normvit > tol && q1 > tolisec) {
-        double beta = -(dt * gp * manning * manning * normvit * (1.0 / cbrt_halley(q1) / q1));
+        double beta = -(dt * gp * manning * manning * normvit * (rcbrt(q1) / q1));
         double detaf = (1 - beta) * (1 - beta);
         afm1[4] = (1 - beta) / detaf;
         afm1[8] = (1 - beta) / detaf;
@@ -862,6 +898,11 @@ int orc_all_edge_fluxes(const orc_mesh* m, const orc_params* prm, const double* 
       for (int c = 0; c < 3; ++c) fl_out[(gi * 3 + tj) * 3 + c] = f[c] * ln;
     }
   return 0;
+}
+
+/* x^(-1/3) of the friction term, elementwise (the restatement's fixed evaluation). */
+void orc_rcbrt(const double* x, double* y, int64_t n) {
+  for (int64_t i = 0; i < n; ++i) y[i] = rcbrt(x[i]);
 }
 
 int orc_max_threads(void) {

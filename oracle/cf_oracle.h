@@ -108,6 +108,8 @@ int orc_all_edge_fluxes(const orc_mesh* m, const orc_params* p, const double* U,
                         double t, double* fl_out);
 
 /* Number of OpenMP threads the library would use by default. */
+/* x^(-1/3) as the friction term evaluates it, elementwise. */
+void orc_rcbrt(const double* x, double* y, int64_t n);
 int orc_max_threads(void);
 
 #ifdef __cplusplus

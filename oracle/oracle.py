@@ -67,6 +67,18 @@ def max_threads() -> int:
     return int(lib().orc_max_threads())
 
 
+def rcbrt(x) -> np.ndarray:
+    """x^(-1/3) as the restated friction term evaluates it, elementwise."""
+    L = lib()
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    y = np.empty_like(x)
+    dp = C.POINTER(C.c_double)
+    L.orc_rcbrt.argtypes = [dp, dp, C.c_int64]
+    L.orc_rcbrt.restype = None
+    L.orc_rcbrt(x.ctypes.data_as(dp), y.ctypes.data_as(dp), x.size)
+    return y
+
+
 def setup(case):
     """Boundary table [nelt,3,2], area, zm, cotemin, xc, yc in reference order."""
     ma = _abi.MeshArrays(case)

@@ -236,6 +236,11 @@ extern "C" long long harness_div_check(long long n, unsigned long long seed) {
   return bad;
 }
 
+/* cf::rcbrt (the kernels' x^(-1/3)) elementwise, on the host. */
+extern "C" void harness_rcbrt(const double* x, double* y, long long n) {
+  for (long long i = 0; i < n; ++i) y[i] = cf::rcbrt(x[i]);
+}
+
 /* em_mul and the integer comparisons of cf_xd.h against the hardware on n adversarial operand
  * pairs: exponents over the whole range (subnormals, near overflow and underflow), all-ones and
  * near-all-ones significands, signed zeros, infinities and NaN.  Returns the mismatches. */

@@ -87,6 +87,17 @@ def mul_check(n, seed=12345):
     return int(L.harness_xd_check(int(n), int(seed)))
 
 
+def rcbrt(x):
+    """cf::rcbrt of the kernels, evaluated on the host, elementwise."""
+    L = lib()
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    y = np.empty_like(x)
+    dp = C.POINTER(C.c_double)
+    L.harness_rcbrt.argtypes = [dp, dp, C.c_longlong]
+    L.harness_rcbrt(x.ctypes.data_as(dp), y.ctypes.data_as(dp), x.size)
+    return y
+
+
 def div_check(n, seed=12345):
     L = lib()
     L.harness_div_check.argtypes = [C.c_longlong, C.c_ulonglong]

@@ -15,6 +15,34 @@ def test_markstein_division_is_the_ieee_quotient():
     assert H.div_check(5_000_000, seed=2) == 0
 
 
+def test_inverse_cube_root_is_the_oracles_and_within_an_ulp(oracle):
+    """The friction term's h^(-1/3): the kernels' rcbrt (run here on the host) equals the
+    oracle's bit for bit, and both are within 1 ulp of the exact power (mpmath, 130 bits) over
+    the whole normal range, the depths a run meets, binade edges and the special values."""
+    mpmath = pytest.importorskip("mpmath")
+    rng = np.random.default_rng(11)
+    n = 60_000
+    bits = rng.integers(0, 1 << 52, n, dtype=np.uint64) | (
+        rng.integers(1, 2047, n).astype(np.uint64) << np.uint64(52))
+    x = np.concatenate([bits.view(np.float64), 10.0 ** rng.uniform(-7, 3, n),
+                        2.0 ** np.arange(-1022, 1024, 1.0), np.nextafter(2.0 ** np.arange(-1000, 1000, 1.0), 0),
+                        np.array([5e-324, 2.2e-308, 1e-310, 1.0, 8.0, 27.0, 0.125])])
+    yk, yo = H.rcbrt(x), oracle.rcbrt(x)
+    assert np.array_equal(yk.view(np.uint64), yo.view(np.uint64))
+    mpmath.mp.prec = 130
+    third = mpmath.mpf(-1) / 3
+    worst = 0.0
+    for xi, yi in zip(x[::3], yk[::3]):
+        ex = mpmath.mpf(float(xi)) ** third
+        worst = max(worst, float(abs(mpmath.mpf(float(yi)) - ex)) / np.spacing(float(ex)))
+    assert worst <= 1.0, worst
+    sp = np.array([0.0, -0.0, np.inf, -1.0, -np.inf, np.nan])
+    for f in (H.rcbrt, oracle.rcbrt):
+        got = f(sp)
+        assert got[0] == np.inf and got[1] == -np.inf and got[2] == 0.0
+        assert np.isnan(got[3:]).all()
+
+
 def _state_after(oracle, case, n, params=None):
     r = oracle.run(case, n, params=params)
     return r["U"], r["dt_hist"][-1], r["t"]
