@@ -621,7 +621,7 @@ CF_HD CF_INLINE void upwind_mix(T h1, T hu1, T hv1, double yh1, T h2, T hu2, T h
                                 double d2, double ysum, double nx, double ny, double tolisec, T& hu_, T& vu_) {
   T a, va;
   to_frame_t(h1, hu1, hv1, yh1, nx, ny, tolisec, a, va);
-  if (d1 < 0.0) {
+  if (T(d1) < 0.0) {
     hu_ = a;
     vu_ = va;
     return;
@@ -639,16 +639,19 @@ CF_HD CF_INLINE double upwind_bed(double z1, double z2, double d1, double d2, do
   return (d1 < 0.0) ? z1 : div_rn(d1 * z1 + d2 * z2, d1 + d2, ysum);
 }
 
-/* The same, loading the elements' states (w = RN(1/h)). */
+/* The same, loading the elements' states (w = RN(1/h)), in the edge's arithmetic type T. */
+template <class T>
 CF_HD CF_INLINE void upwind_state(const double4* U, int i1, int i2, double d1, double d2, double ysum, double nx,
-                                  double ny, double tolisec, double& hu_, double& vu_) {
+                                  double ny, double tolisec, T& hu_, T& vu_) {
   const double4 A1 = ld4(U + i1);
-  if (d1 < 0.0) {
-    upwind_mix(A1.x, A1.y, A1.z, A1.w, 0.0, 0.0, 0.0, 0.0, d1, d2, ysum, nx, ny, tolisec, hu_, vu_);
+  if (T(d1) < 0.0) {
+    upwind_mix(T(A1.x), T(A1.y), T(A1.z), A1.w, T(0.0), T(0.0), T(0.0), 0.0, d1, d2, ysum, nx, ny, tolisec, hu_,
+               vu_);
     return;
   }
   const double4 A2 = ld4(U + i2);
-  upwind_mix(A1.x, A1.y, A1.z, A1.w, A2.x, A2.y, A2.z, A2.w, d1, d2, ysum, nx, ny, tolisec, hu_, vu_);
+  upwind_mix(T(A1.x), T(A1.y), T(A1.z), A1.w, T(A2.x), T(A2.y), T(A2.z), A2.w, d1, d2, ysum, nx, ny, tolisec, hu_,
+             vu_);
 }
 
 /* The MUSCL form: (h, u_n, u_t) of one side's upwind reconstruction (flux_riemann.cuf:240-366
@@ -693,7 +696,7 @@ CF_HD CF_INLINE void interior_edge(const MemberDev& M, int ilim, int flux_mode, 
                                    bool freeze_r = false) {
   const double g = M.gp, tolisec = M.tolisec;
   const double nx = G.nx, ny = G.ny, len = G.len;
-  const double zij = dmax(zml, zmr);
+  const double zij = val(dmax(T(zml), T(zmr)));
   T hautl, vitul, vitvl, hautr, vitur, vitvr;
   to_frame(hA, huA, hvA, yhA, nx, ny, tolisec, hautl, vitul, vitvl);
   to_frame(hB, huB, hvB, yhB, nx, ny, tolisec, hautr, vitur, vitvr);
@@ -900,7 +903,7 @@ CF_HD CF_INLINE void edge_body(const StepArgs& a, const MemberDev& M, int e, dou
     write_slots(sa, o);
     return;
   }
-  double hl_upw = 0.0, vl_upw = 0.0, hr_upw = 0.0, vr_upw = 0.0;
+  S hl_upw = S(0.0), vl_upw = S(0.0), hr_upw = S(0.0), vr_upw = S(0.0);
   if (IFLUX == 3) {
     const int4 up = ldro(a.eupw + e);
     const double4 dw = ld4(a.ewts + e);   /* d1, d2 of side A, d1, d2 of side B */
@@ -909,8 +912,8 @@ CF_HD CF_INLINE void edge_body(const StepArgs& a, const MemberDev& M, int e, dou
   }
   S os[10];
   interior_edge<(IFLUX == 4 ? 3 : IFLUX)>(M, a.ilimiteur, a.flux_mode, G, dt, S(UA.x), S(UA.y), S(UA.z), ez.x,
-                                          UA.w, S(UB.x), S(UB.y), S(UB.z), ez.y, UB.w, S(hl_upw), S(vl_upw), ez.z,
-                                          S(hr_upw), S(vr_upw), ez.w, os);
+                                          UA.w, S(UB.x), S(UB.y), S(UB.z), ez.y, UB.w, hl_upw, vl_upw, ez.z, hr_upw,
+                                          vr_upw, ez.w, os);
 #pragma unroll
   for (int i = 0; i < 10; ++i) o[i] = val(os[i]);
   write_slots(sa, o);

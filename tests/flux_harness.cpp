@@ -262,14 +262,18 @@ extern "C" long long harness_xd_check(long long n, unsigned long long seed) {
   };
   long long bad = 0;
   for (long long i = 0; i < n; ++i) {
-    const int mode = (int)(rnd() % 5);
+    const int mode = (int)(rnd() % 7);
     double a, b;
     if (mode == 0) { a = mk(1, 2046); b = mk(1, 2046); }              /* any normal */
     else if (mode == 1) { a = mk(0, 2047); b = mk(0, 2047); }         /* incl. subnormal, inf, NaN */
     else if (mode == 2) { a = mk(1000, 1050); b = mk(1000, 1050); }   /* the step's range */
     else if (mode == 3) { a = mk(1, 30); b = mk(990, 1030); }         /* underflow edge */
-    else { a = mk(2000, 2046); b = mk(1000, 1100); }                  /* overflow edge */
+    else if (mode == 4) { a = mk(2000, 2046); b = mk(1000, 1100); }   /* overflow edge */
+    else { a = (rnd() & 1) ? -0.0 : 0.0; b = mk(0, 2047); }           /* signed zero times anything */
+    if (mode == 6) std::swap(a, b);
     const double p1 = em_mul(a, b), p2 = a * b;
+    const double n1 = val(-XD<true>(a)), n2 = -a;
+    if (memcmp(&n1, &n2, 8) != 0) ++bad;
     if (memcmp(&p1, &p2, 8) != 0 && !(p1 != p1 && p2 != p2)) ++bad;
     if (xlt(a, b) != (a < b) || xle(a, b) != (a <= b) || xeq(a, b) != (a == b)) ++bad;
     const double z = (rnd() & 1) ? -0.0 : 0.0;
