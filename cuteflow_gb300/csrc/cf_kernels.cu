@@ -115,21 +115,94 @@ __device__ __forceinline__ Slot load_slot(const Slot* p) {
   return s;
 }
 
-/* Minimum over the block, folded into *target with one atomic (positive doubles order
- * like their bit patterns). */
+/* Minimum over the block, folded into *target with one atomic.  The values are positive (or
+ * NaN, which the minimum ignores as fmin would), so they order like their bit patterns: the
+ * reduction is integer work. */
 __device__ __forceinline__ void block_min_atomic(double v, double* target) {
-  __shared__ double red[TILE_C / 32];
+  __shared__ unsigned long long red[TILE_C / 32];
+  unsigned long long b = dbits(v);
   #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
+  for (int o = 16; o > 0; o >>= 1) b = min(b, __shfl_xor_sync(0xffffffffu, b, o));
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) red[wid] = b;
+  __syncthreads();
+  if (wid == 0) {
+    b = (lane < TILE_C / 32) ? red[lane] : dbits(1.0e300);
+    #pragma unroll
+    for (int o = 16; o > 0; o >>= 1) b = min(b, __shfl_xor_sync(0xffffffffu, b, o));
+    if (lane == 0) atomicMin(reinterpret_cast<unsigned long long*>(target), b);
+  }
+}
+
+/* Minimum over the block of a float, returned to every thread. */
+__device__ __forceinline__ float block_min_f32(float v) {
+  __shared__ float red[TILE_C / 32];
+  #pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fminf(v, __shfl_xor_sync(0xffffffffu, v, o));
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   if (lane == 0) red[wid] = v;
   __syncthreads();
-  if (wid == 0) {
-    v = (lane < TILE_C / 32) ? red[lane] : 1.0e300;
-    #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
-    if (lane == 0) atomicMin(reinterpret_cast<unsigned long long*>(target), dbits(v));
+  v = red[0];
+  #pragma unroll
+  for (int w = 1; w < TILE_C / 32; ++w) v = fminf(v, red[w]);
+  return v;
+}
+
+/* x truncated to float by integer operations (relative error below 2^-23); false when x is
+ * outside float's normal range, infinite or NaN.  Zero converts exactly. */
+__device__ __forceinline__ bool f32_trunc(double x, float& f) {
+  const unsigned long long b = dbits(x);
+  const unsigned sign = (unsigned)(b >> 32) & 0x80000000u;
+  if ((b << 1) == 0) {
+    f = __uint_as_float(sign);
+    return true;
   }
+  const int e = (int)((b >> 52) & 0x7ff) - 1023;
+  if (e < -126 || e > 127) return false;
+  f = __uint_as_float(sign | ((unsigned)(e + 127) << 23) | (unsigned)((b >> 29) & 0x7fffffu));
+  return true;
+}
+
+/* cfl_dt_elem of a wet element (h > tolisec) in single precision: the inputs truncated to float,
+ * every operation correctly rounded.  Relative to the FP64 value it is within
+ *   2^-23 (truncation of hu or hv, and of h) x 2 + 2^-24 for u = hu/h; twice that + 2^-24 for u^2;
+ *   + 2^-24 for the sum of squares (positive terms); half of it + 2^-24 for the root;
+ *   below that for sqrt(g h); + 2^-24 for the sum; 2^-23 (cfl L) + 2^-24 for the last quotient
+ * = 7e-7 (the max with 0.01 and the min with 1e6 are monotone and add nothing; the FP64 value's
+ * own rounding is ~1e-15).  Returns false (the caller takes the FP64 value) where an input is out
+ * of float's range or the result is not in (1e-30, 1e6]. */
+__device__ __forceinline__ bool cfl_dt_f32(const MemberDev& M, double cflL, double h, double hu, double hv,
+                                           float& d) {
+  float hf, huf, hvf, lf, gf;
+  if (!(f32_trunc(h, hf) & f32_trunc(hu, huf) & f32_trunc(hv, hvf) & f32_trunc(cflL, lf) & f32_trunc(M.gp, gf)))
+    return false;
+  const float vu = __fdiv_rn(huf, hf), vv = __fdiv_rn(hvf, hf);
+  const float nv = __fsqrt_rn(__fadd_rn(__fmul_rn(vu, vu), __fmul_rn(vv, vv)));
+  const float c = __fsqrt_rn(__fmul_rn(gf, hf));
+  const float vmax = fmaxf(0.01f, __fadd_rn(nv, c));
+  d = fminf(__fdiv_rn(lf, vmax), 1.0e6f);
+  return d > 1.0e-30f && d <= 1.0e6f;
+}
+
+/* The minimum of cfl_dt_elem over the block's elements with the FP64 evaluation only where it
+ * can be the minimum.  RN is monotone, so the block minimum of the FP64 values is the FP64 value
+ * of an element whose single-precision value lies within the error bound of the block's
+ * single-precision minimum: m_f >= (1 - 7e-7) d_min and d_f(argmin) <= (1 + 7e-7) d_min, so the
+ * element of the minimum passes d_f <= 1.000004 m_f.  Elements without a single-precision value
+ * (dry ones, constant dt, out-of-range inputs) take their FP64 value directly. */
+__device__ __forceinline__ void block_cfl_min(const MemberDev& M, bool active, double cflL, const double4& V,
+                                              double* target) {
+  double dti = 1.0e300;
+  float df = __int_as_float(0x7f800000);
+  bool pending = false;
+  if (active) {
+    if (M.is_dt_constant == 1 || !(V.x > M.tolisec)) dti = cfl_dt_elem(M, cflL, V.x, V.y, V.z, V.w);
+    else if (cfl_dt_f32(M, cflL, V.x, V.y, V.z, df)) pending = true;
+    else dti = cfl_dt_elem(M, cflL, V.x, V.y, V.z, V.w);
+  }
+  const float mf = block_min_f32(df);
+  if (pending && df <= mf * 1.000004f) dti = cfl_dt_elem(M, cflL, V.x, V.y, V.z, V.w);
+  block_min_atomic(dti, target);
 }
 
 __global__ void __launch_bounds__(TILE_C) k_cells(StepArgs a) {
@@ -145,7 +218,8 @@ __global__ void __launch_bounds__(TILE_C) k_cells(StepArgs a) {
   if (s_stop) return;
   const double dt = S->dt[p];
   const int c = tile * TILE_C + threadIdx.x;
-  double dti = 1.0e300;
+  double4 V = make_double4(0.0, 0.0, 0.0, 0.0);
+  double cflL = 0.0;
   if (c < M.cell_end) {
     const double4 U = ld4(a.Uin + c);
     const double4 st = ld4(a.cstat + c);   /* area, manning n, cfl L, - */
@@ -154,16 +228,16 @@ __global__ void __launch_bounds__(TILE_C) k_cells(StepArgs a) {
     const Slot s1 = load_slot(a.slots + sl.y);
     const Slot s2 = load_slot(a.slots + sl.z);
     bool nonfinite = false;
-    /* FP64 pipe only: on GB300 the integer-pipe arithmetic of cf_xd.h is slower for this kernel
-     * (0.207 -> 0.214-0.218 ms per 1M elements) */
-    const double4 V = element_update(M, U, st, s0, s1, s2, dt, nonfinite);
+    /* FP64 pipe only: the integer-pipe arithmetic of cf_xd.h does not pay here (1M elements:
+     * 0.180 ms; integer comparisons 0.180 ms, comparisons and products 0.197 ms) */
+    V = element_update(M, U, st, s0, s1, s2, dt, nonfinite);
     if (nonfinite) atomicOr(&S->status, CF_STATUS_NONFINITE);
     double4* o = a.Uout + c;
     reinterpret_cast<double2*>(o)[0] = make_double2(V.x, V.y);
     reinterpret_cast<double2*>(o)[1] = make_double2(V.z, V.w);
-    dti = cfl_dt_elem(M, st.z, V.x, V.y, V.z, V.w);
+    cflL = st.z;
   }
-  block_min_atomic(dti, &S->dt[1 - p]);
+  block_cfl_min(M, c < M.cell_end, cflL, V, &S->dt[1 - p]);
 }
 
 /* CFL of a state into mst[m].dt[slot] (the initial dt, finite_volumes_method.cuf:113-116). */
