@@ -247,12 +247,13 @@ __global__ void __launch_bounds__(TILE_C) k_cfl(const double4* U, const double4*
   const int m = __ldg(ctile_mem + tile);
   const MemberDev& M = mdev[m];
   const int c = tile * TILE_C + threadIdx.x;
-  double dti = 1.0e300;
+  double4 u = make_double4(0.0, 0.0, 0.0, 0.0);
+  double cflL = 0.0;
   if (c < M.cell_end) {
-    const double4 u = ld4(U + c);
-    dti = cfl_dt_elem(M, ld4(cstat + c).z, u.x, u.y, u.z, u.w);
+    u = ld4(U + c);
+    cflL = ld4(cstat + c).z;
   }
-  block_min_atomic(dti, &mst[m].dt[slot]);
+  block_cfl_min(M, c < M.cell_end, cflL, u, &mst[m].dt[slot]);
 }
 
 /* Discharge diagnostics of the last step (debit_entree_sum, debit_sortie,
