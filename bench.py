@@ -33,15 +33,19 @@ sys.path.insert(0, ROOT)
 
 METRIC = "FP64 triangle-updates/s @1M tris: plain vs batched; adjoint/forward cost ratio"
 UNIT = "tri-updates/s"
-# Compulsory HBM bytes per triangle-update of one WAF step (state in/out, per-element
-# statics, neighbour ids, per-edge geometry at E/N = 1.5, centroids): see the design doc.
+# Compulsory HBM bytes per triangle-update of one WAF step: state in and out 48, per-element
+# statics 32, neighbour ids 12, per-edge geometry 24 x E/N = 36 (E/N = 1.5), centroids 16.
 ALG_BYTES_WAF = 144.0
 ALG_BYTES_HLLC = 128.0
-# DRAM bytes (read + write) of one 1M-triangle WAF step from one ncu capture of this command's
-# kernels (k_edges<3> 368.0 MB + k_cells 247.4 MB, profiles/step_kernels_flooding_1M_WAF.md), and
-# the FP64-pipe activity the same capture reports; used for the default workload only.
-NCU_TRAFFIC_FLOODING_1M = 615.4e6
-NCU_FP64_PIPE_FLOODING_1M = {"k_edges": 0.853, "k_cells": 0.802}
+# DRAM bytes (read + write) of one 1M-triangle WAF step from one ncu capture of this workload's
+# kernels with the tuned setting (k_edges<3> 421.8 MB + k_cells 246.0 MB), and the FP64-pipe
+# activity the same capture reports; used for the default workload only.
+NCU_TRAFFIC_FLOODING_1M = 667.8e6
+NCU_FP64_PIPE_FLOODING_1M = {"k_edges": 0.786, "k_cells": 0.813}
+# FP64-pipe instructions (DADD + DMUL + DFMA + DSETP, thread-level, ncu sass__inst_executed_per_opcode)
+# of the same step: per edge in k_edges<3> by tuning setting (int_compare, int_mul_warps), per element
+# in k_cells.
+NCU_FP64_INSTR_FLOODING_1M = {"per_edge": {(1, 15): 176.4, (0, 0): 238.2}, "per_element": 73.7}
 
 
 def peaks():
@@ -385,7 +389,12 @@ def run_ours(args):
     # ---- autotuner: how the edge kernel shares FP64 work with the integer pipes (identical
     # results in every setting); the trials run on the initial state, which is restored ----
     s.set_state(case.U0)
-    tune = s.autotune(30) if not args.no_tune else (0, 0, None)
+    if args.tuning:
+        cmp_, mask = (int(v) for v in args.tuning.split(","))
+        s.set_tuning(cmp_, mask)
+        tune = (cmp_, mask, None)
+    else:
+        tune = s.autotune(30) if not args.no_tune else (0, 0, None)
 
     # ---- device-resident throughput (value) ----
     s.set_state(case.U0)
@@ -446,10 +455,34 @@ def run_ours(args):
         pg.all_reduce(t, op=pg.ReduceOp.MAX)
         e2e_ms = float(t.item())
     e2e_value = world * n * e2e_steps / (e2e_ms * 1e-3)
+    # the host link's own rate for the same bytes (plain pinned copies, no kernels): the floor of
+    # the end-to-end step's copy time
+    dbuf = torch.empty(hin.numel(), dtype=torch.float64, device="cuda")
+    hv, ho = hin.view(-1), hout.view(-1)
+
+    def link_ms(fn, k=10):
+        fn()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        for _ in range(k):
+            fn()
+        b.record()
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / k
+
+    h2d_ms = link_ms(lambda: dbuf.copy_(hv, non_blocking=True))
+    d2h_ms = link_ms(lambda: ho.copy_(dbuf, non_blocking=True))
+    del dbuf
 
     hbm, hbm_src = peaks()
     achieved = alg_bytes * n / (step_kernel_ms * 1e-3) / 1e9
-    fp64_peak = float(os.environ.get("CF_FP64_PEAK_TFLOPS", "1.19"))
+    fp64_rate = s.probe_fp64()
+    fp64_instr = None
+    if args.config == "flooding" and (tune[0], tune[1]) in NCU_FP64_INSTR_FLOODING_1M["per_edge"]:
+        fp64_instr = (NCU_FP64_INSTR_FLOODING_1M["per_edge"][(tune[0], tune[1])] * s.nedge
+                      + NCU_FP64_INSTR_FLOODING_1M["per_element"] * n)
+    fp64_achieved = fp64_instr / (step_kernel_ms * 1e-3) if fp64_instr else None
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
@@ -468,11 +501,19 @@ def run_ours(args):
                      "traffic_note": "ncu dram__bytes_read.sum + dram__bytes_write.sum per step "
                                      "(k_edges + k_cells) of the 1M WAF step",
                      "k_edges_ms": k_edges_ms, "k_cells_ms": k_cells_ms},
-        "fp64": {"note": "the step is FP64-pipe bound; peak measured by a DFMA probe on this pool",
-                 "peak_tflops": fp64_peak,
+        "fp64": {"bound": "fp64 pipe (the step's limit; HBM runs at 10-21 % of peak)",
+                 "peak_instr_per_s": fp64_rate,
+                 "peak_source": "cf_probe_fp64, measured live: independent FMA chains on every SM",
+                 "instr_per_step": fp64_instr,
+                 "instr_source": "ncu sass__inst_executed_per_opcode of the same step (DADD+DMUL+DFMA+DSETP)",
+                 "achieved_instr_per_s": fp64_achieved,
+                 "frac": fp64_achieved / fp64_rate if fp64_achieved else None,
                  "pipe_active_ncu": NCU_FP64_PIPE_FLOODING_1M if args.config == "flooding" else None},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 24 * n, "d2h_bytes_per_step": 24 * n,
-                "steps": e2e_steps},
+                "steps": e2e_steps, "ms_per_step": e2e_ms / e2e_steps,
+                "link_h2d_gbs": 24 * n / (h2d_ms * 1e-3) / 1e9, "link_d2h_gbs": 24 * n / (d2h_ms * 1e-3) / 1e9,
+                "note": "per step: cf_set_state from pinned host memory, cf_step, cf_get_state into pinned "
+                        "host memory; link_*: plain pinned copies of the same bytes"},
         "gpu_launches": 2 * args.steps + 1,
         "clocks": clk.summary(),
     }
@@ -504,6 +545,8 @@ def main():
     ap.add_argument("--config", default="flooding", choices=["flooding", "flooding_muscl", "dam_break", "ensemble"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (every operation on the FP64 pipe)")
+    ap.add_argument("--tuning", default=None, metavar="CMP,MASK",
+                    help="fix the edge kernel's integer-pipe setting instead of autotuning (e.g. 1,15)")
     ap.add_argument("--batched-members", type=int, default=32, help="ensemble sample beside the plain line (0: skip)")
     ap.add_argument("--batched-steps", type=int, default=200)
     ap.add_argument("--calib-instances", type=int, default=8, help="batched calibration leg (0: skip)")

@@ -626,6 +626,36 @@ int cf_set_tuning(cf_ctx* ctx, int32_t int_compare, int32_t int_mul_warps) {
   return CF_OK;
 }
 
+int cf_probe_fp64(cf_ctx* ctx, double* instr_per_s) {
+  if (!ctx || !instr_per_s) return CF_EINVAL;
+  cf_ctx* c = ctx;
+  CF_CUDA(c, cudaSetDevice(c->device));
+  int sms = 0;
+  CF_CUDA(c, cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device));
+  const int32_t nblocks = 8 * sms;
+  const int64_t iters = 4096;
+  double* out = nullptr;
+  int rc = dalloc(c, &out, (size_t)nblocks * 256);
+  if (rc) return rc;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  float ms = 0.0f;
+  cudaError_t err = cudaEventCreate(&e0);
+  if (err == cudaSuccess) err = cudaEventCreate(&e1);
+  if (err == cudaSuccess) rc = launch_probe_fp64(out, nblocks, iters, reinterpret_cast<stream_t>(c->stream));
+  if (err == cudaSuccess && rc == CF_OK) err = cudaEventRecord(e0, c->stream);
+  if (err == cudaSuccess && rc == CF_OK) rc = launch_probe_fp64(out, nblocks, iters, reinterpret_cast<stream_t>(c->stream));
+  if (err == cudaSuccess && rc == CF_OK) err = cudaEventRecord(e1, c->stream);
+  if (err == cudaSuccess && rc == CF_OK) err = cudaEventSynchronize(e1);
+  if (err == cudaSuccess && rc == CF_OK) err = cudaEventElapsedTime(&ms, e0, e1);
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  cudaFree(out);
+  if (err != cudaSuccess) return cuda_fail(c, err, "cf_probe_fp64");
+  if (rc != CF_OK) return fail(c, rc, "cf_probe_fp64 launch failed");
+  *instr_per_s = (double)nblocks * 256.0 * 8.0 * (double)iters / (ms * 1e-3);
+  return CF_OK;
+}
+
 int cf_get_tuning(cf_ctx* ctx, int32_t* int_compare, int32_t* int_mul_warps) {
   if (!ctx) return CF_EINVAL;
   if (int_compare) *int_compare = ctx->xd_cmp;

@@ -174,6 +174,7 @@ int prepare_mesh(const cf_mesh* m, const cf_params* p, Prep& out, std::string& e
 typedef struct CUstream_st* stream_t;
 
 int launch_step(const StepArgs& a, stream_t s, void* ev_mid, void* ev_end);
+int launch_probe_fp64(double* out, int32_t nblocks, int64_t iters, stream_t s);  /* nblocks x 256 outputs */
 int launch_cfl(const double4* U, const double4* cstat, const int32_t* ctile_mem, int32_t tile_begin,
                int32_t n_tiles, const MemberDev* mdev, MemberState* mst, int32_t slot, stream_t s);
 int launch_discharge(const Slot* slots, const int2* ecell, const MemberDev* mdev, MemberState* mst,

@@ -337,9 +337,31 @@ __global__ void k_scatter_ids(double4* U, const int32_t* iperm, const int32_t* i
   reinterpret_cast<double2*>(u)[1] = make_double2(in[3 * (size_t)i + 2], h > 0.0 ? 1.0 / h : 0.0);
 }
 
+/* Throughput probe of the FP64 pipe: eight independent FMA chains per thread, x <- x a + b with
+ * a = 1 - 2^-20 and b = 2^-20, so every value stays a normal number near 1. */
+__global__ void __launch_bounds__(256) k_probe_fp64(double* out, long long iters) {
+  const double a = 1.0 - 0x1p-20, b = 0x1p-20;
+  double x[8];
+  #pragma unroll
+  for (int k = 0; k < 8; ++k) x[k] = 0.5 + 0.01 * k + 1e-6 * threadIdx.x;
+  for (long long i = 0; i < iters; ++i) {
+    #pragma unroll
+    for (int k = 0; k < 8; ++k) x[k] = fma(x[k], a, b);
+  }
+  double sum = 0.0;
+  #pragma unroll
+  for (int k = 0; k < 8; ++k) sum += x[k];
+  out[blockIdx.x * (size_t)blockDim.x + threadIdx.x] = sum;
+}
+
 int check(cudaError_t e) { return e == cudaSuccess ? CF_OK : CF_ECUDA; }
 
 }  // namespace
+
+int launch_probe_fp64(double* out, int32_t nblocks, int64_t iters, stream_t s) {
+  k_probe_fp64<<<nblocks, 256, 0, reinterpret_cast<cudaStream_t>(s)>>>(out, (long long)iters);
+  return check(cudaGetLastError());
+}
 
 int launch_step(const StepArgs& a, stream_t s, void* ev_mid, void* ev_end) {
   cudaStream_t st = reinterpret_cast<cudaStream_t>(s);

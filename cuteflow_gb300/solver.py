@@ -56,6 +56,7 @@ def load(build_if_missing: bool = True):
     L.cf_step_noalloc.argtypes = [vp, C.c_int32, C.POINTER(_abi.CfStepInfo)]
     L.cf_run.argtypes = [vp, C.c_double, C.c_int64, C.POINTER(_abi.CfStepInfo)]
     L.cf_set_tuning.argtypes = [vp, C.c_int32, C.c_int32]
+    L.cf_probe_fp64.argtypes = [vp, dp]
     L.cf_get_elements.argtypes = [vp, C.c_int32, C.POINTER(C.c_int32), C.c_int32, dp]
     L.cf_set_elements.argtypes = [vp, C.c_int32, C.POINTER(C.c_int32), C.c_int32, dp]
     L.cf_set_dt.argtypes = [vp, C.c_int32, C.c_double]
@@ -113,7 +114,8 @@ def load(build_if_missing: bool = True):
     for name in ("cf_default_params", "cf_create", "cf_set_state", "cf_set_state_device",
                  "cf_set_initial_condition", "cf_step", "cf_step_noalloc", "cf_run", "cf_set_tuning",
                  "cf_get_tuning", "cf_autotune", "cf_get_elements", "cf_set_elements", "cf_set_dt", "cf_get_state", "cf_get_state_device",
-                 "cf_get_info", "cf_get_mesh_tables", "cf_mesh_tables", "cf_get_sizes", "cf_set_timing", "cf_get_timing"):
+                 "cf_get_info", "cf_get_mesh_tables", "cf_mesh_tables", "cf_get_sizes", "cf_set_timing", "cf_get_timing",
+                 "cf_probe_fp64"):
         getattr(L, name).restype = C.c_int
     _lib = L
     return L
@@ -252,6 +254,12 @@ class Solver:
         a, b, t = C.c_int32(), C.c_int32(), C.c_double()
         self._check(self._L.cf_autotune(self._ctx, int(steps_per_trial), C.byref(a), C.byref(b), C.byref(t)))
         return a.value, b.value, t.value
+
+    def probe_fp64(self) -> float:
+        """cf_probe_fp64: the FP64 pipe's throughput on this device, FP64 instructions per second."""
+        r = C.c_double()
+        self._check(self._L.cf_probe_fp64(self._ctx, C.byref(r)))
+        return r.value
 
     def run(self, ts: float, max_steps: int = 1 << 40, check: bool = True) -> StepInfo:
         """The reference's time loop up to time ts (cf_run): stops with CF_STATUS_END, or at a

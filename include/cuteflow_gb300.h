@@ -272,6 +272,12 @@ int cf_get_tuning(cf_ctx* ctx, int32_t* int_compare, int32_t* int_mul_warps);
 int cf_autotune(cf_ctx* ctx, int32_t steps_per_trial, int32_t* int_compare, int32_t* int_mul_warps,
                 double* ms_per_step);
 
+/* Diagnostic: the FP64 pipe's throughput on the context's device in FP64 instructions per second
+ * (independent FMA chains on every SM, timed with CUDA events), the denominator of the step's
+ * roofline: the step is bound by FP64 instruction issue, not by HBM.  Allocates and frees a
+ * scratch buffer of 2 KB per block. */
+int cf_probe_fp64(cf_ctx* ctx, double* instr_per_s);
+
 /* Kernel timing of the last cf_step call: total device milliseconds of the edge-flux and
  * cell-update kernels measured with CUDA events when timing is enabled. */
 int cf_set_timing(cf_ctx* ctx, int32_t enable);

@@ -284,6 +284,19 @@ def test_autotune_leaves_the_run_unchanged(gpu_lib, oracle):
         assert np.array_equal(s.get_state(), ref["U"]) and info.t == ref["t"] and info.steps == 90
 
 
+def test_fp64_probe_reports_a_plausible_rate(gpu_lib):
+    """cf_probe_fp64 (the step's roofline denominator): GB300 issues ~2 FP64 instructions per
+    clock per SM, ~6e11/s over 152 SMs at 2 GHz; the probe must land in that range and leave the
+    context usable."""
+    from cuteflow_gb300 import Solver
+    c = cases.flooding(20, 10, seed=1, iflux=1)
+    with Solver(c) as s:
+        r = s.probe_fp64()
+        assert 1e11 < r < 5e12, r
+        s.set_state(c.U0)
+        assert s.step(3).status == 0
+
+
 @pytest.mark.parametrize("iflux,nparts", [(1, 3), (3, 2), (3, 4), (4, 3)])
 def test_decomposed_mesh_equals_the_whole(gpu_lib, oracle, iflux, nparts):
     """A mesh cut into parts (separate contexts, halos exchanged and the minimum dt applied after
