@@ -656,20 +656,21 @@ CF_HD CF_INLINE void upwind_state(const double4* U, int i1, int i2, double d1, d
 
 /* The MUSCL form: (h, u_n, u_t) of one side's upwind reconstruction (flux_riemann.cuf:240-366
  * with the normal velocity as well). */
+template <class T>
 CF_HD CF_INLINE void upwind_state3(const double4* U, int i1, int i2, double d1, double d2, double ysum, double nx,
-                                   double ny, double tolisec, double& hu_, double& uu_, double& vu_) {
+                                   double ny, double tolisec, T& hu_, T& uu_, T& vu_) {
   const double4 A1 = ld4(U + i1);
-  double a, ua, va;
-  to_frame(A1.x, A1.y, A1.z, A1.w, nx, ny, tolisec, a, ua, va);
-  if (d1 < 0.0) {
+  T a, ua, va;
+  to_frame(T(A1.x), T(A1.y), T(A1.z), A1.w, nx, ny, tolisec, a, ua, va);
+  if (T(d1) < 0.0) {
     hu_ = a;
     uu_ = ua;
     vu_ = va;
     return;
   }
   const double4 A2 = ld4(U + i2);
-  double b, ub, vb;
-  to_frame(A2.x, A2.y, A2.z, A2.w, nx, ny, tolisec, b, ub, vb);
+  T b, ub, vb;
+  to_frame(T(A2.x), T(A2.y), T(A2.z), A2.w, nx, ny, tolisec, b, ub, vb);
   const double ds = d1 + d2;
   hu_ = div_rn(d1 * a + d2 * b, ds, ysum);
   uu_ = div_rn(d1 * ua + d2 * ub, ds, ysum);
@@ -764,30 +765,31 @@ CF_HD CF_INLINE void interior_edge(const MemberDev& M, int ilim, int flux_mode, 
  * masking and upwind averaging produce; each side's limited reconstruction is evaluated in
  * full (its slopes are not mirror images of the other side's).  upA / upB: (h, u_n, u_t) of
  * the upwind reconstructions of sides A and B in A's frame, zl_upw / zr_upw their beds. */
+template <class T>
 CF_HD CF_INLINE void interior_edge_muscl(const MemberDev& M, int ilim, int flux_mode, const EdgeGeo& G, double dt,
-                                         double hA, double huA, double hvA, double zml, double yhA, double hB,
-                                         double huB, double hvB, double zmr, double yhB, const double upA[3],
-                                         double zl_upw, const double upB[3], double zr_upw, double out[10]) {
+                                         T hA, T huA, T hvA, double zml, double yhA, T hB, T huB, T hvB, double zmr,
+                                         double yhB, const T upA[3], double zl_upw, const T upB[3], double zr_upw,
+                                         T out[10]) {
   const double g = M.gp, tolisec = M.tolisec;
   const double nx = G.nx, ny = G.ny, len = G.len;
-  const double zij = dmax(zml, zmr);
-  double hautl, vitul, vitvl, hautr, vitur, vitvr;
+  const double zij = val(dmax(T(zml), T(zmr)));
+  T hautl, vitul, vitvl, hautr, vitur, vitvr;
   to_frame(hA, huA, hvA, yhA, nx, ny, tolisec, hautl, vitul, vitvl);
   to_frame(hB, huB, hvB, yhB, nx, ny, tolisec, hautr, vitur, vitvr);
   /* hydrostatic reconstruction of the four states (:370-400) */
-  double hijet = dmax(0.0, hautl + zml - zij);
-  double hlu = dmax(0.0, upA[0] + zl_upw - zij);
-  double hjiet = dmax(0.0, hautr + zmr - zij);
-  double hru = dmax(0.0, upB[0] + zr_upw - zij);
-  double ul = vitul, vl = vitvl, ur = vitur, vr = vitvr;
-  double ulu = upA[1], vlu = upA[2], uru = upB[1], vru = upB[2];
-  if (hijet < tolisec) { hijet = 0.; ul = 0.; vl = 0.; }
-  if (hlu < tolisec) { hlu = 0.; ulu = 0.; vlu = 0.; }
-  if (hjiet < tolisec) { hjiet = 0.; ur = 0.; vr = 0.; }
-  if (hru < tolisec) { hru = 0.; uru = 0.; vru = 0.; }
+  T hijet = dmax(T(0.0), hautl + zml - zij);
+  T hlu = dmax(T(0.0), upA[0] + zl_upw - zij);
+  T hjiet = dmax(T(0.0), hautr + zmr - zij);
+  T hru = dmax(T(0.0), upB[0] + zr_upw - zij);
+  T ul = vitul, vl = vitvl, ur = vitur, vr = vitvr;
+  T ulu = upA[1], vlu = upA[2], uru = upB[1], vru = upB[2];
+  if (hijet < tolisec) { hijet = T(0.); ul = T(0.); vl = T(0.); }
+  if (hlu < tolisec) { hlu = T(0.); ulu = T(0.); vlu = T(0.); }
+  if (hjiet < tolisec) { hjiet = T(0.); ur = T(0.); vr = T(0.); }
+  if (hru < tolisec) { hru = T(0.); uru = T(0.); vru = T(0.); }
   const double dtoverdx = div_rn(dt, G.d_mrl, G.y_mrl);
-  TwoFlux F;
-  double x1, x2, x3;
+  TwoFluxT<T> F;
+  T x1, x2, x3;
   muscl_side(g, tolisec, ilim, dtoverdx, G.d_mrl, G.y_mrl, G.d_mkvol, G.y_mkvol, G.d_mkvoisin, G.y_mkvoisin, hijet,
              ul, vl, hjiet, ur, vr, hlu, ulu, vlu, hru, uru, vru, x1, x2, x3);
   F.a1 = x1;
@@ -798,7 +800,7 @@ CF_HD CF_INLINE void interior_edge_muscl(const MemberDev& M, int ilim, int flux_
     F.b2 = -F.a2;
     F.b3 = -F.a3;
   } else {
-    double y1, y2, y3;
+    T y1, y2, y3;
     muscl_side(g, tolisec, ilim, dtoverdx, G.d_mrl, G.y_mrl, G.d_mkvoisin, G.y_mkvoisin, G.d_mkvol, G.y_mkvol,
                hjiet, -ur, -vr, hijet, -ul, -vl, hru, -uru, -vru, hlu, -ulu, -vlu, y1, y2, y3);
     const double mx = -nx, my = -ny;
@@ -807,10 +809,10 @@ CF_HD CF_INLINE void interior_edge_muscl(const MemberDev& M, int ilim, int flux_
     F.b3 = my * y2 + mx * y3;
   }
   /* bed-slope source of both sides from the raw depths (source_terms.cuf:90-97) */
-  const double ha = dmax(0.0, hA + zml - zij);
-  const double hb = dmax(0.0, hB + zmr - zij);
-  const double ta = g / 2.0 * (ha * ha - hA * hA) * len;
-  const double tb = g / 2.0 * (hb * hb - hB * hB) * len;
+  const T ha = dmax(T(0.0), hA + zml - zij);
+  const T hb = dmax(T(0.0), hB + zmr - zij);
+  const T ta = g / 2.0 * (ha * ha - hA * hA) * len;
+  const T tb = g / 2.0 * (hb * hb - hB * hB) * len;
   out[0] = F.a1 * len;
   out[1] = F.a2 * len;
   out[2] = F.a3 * len;
@@ -895,11 +897,13 @@ CF_HD CF_INLINE void edge_body(const StepArgs& a, const MemberDev& M, int e, dou
   if (IFLUX == 4) {
     const int4 up = ldro(a.eupw + e);
     const double4 dw = ld4(a.ewts + e);
-    double upA[3], upB[3];
+    S upA[3], upB[3], om[10];
     upwind_state3(a.Uin, up.x, up.y, dw.x, dw.y, G.ysum_a, G.nx, G.ny, M.tolisec, upA[0], upA[1], upA[2]);
     upwind_state3(a.Uin, up.z, up.w, dw.z, dw.w, G.ysum_b, G.nx, G.ny, M.tolisec, upB[0], upB[1], upB[2]);
-    interior_edge_muscl(M, a.ilimiteur, a.flux_mode, G, dt, UA.x, UA.y, UA.z, ez.x, UA.w, UB.x, UB.y, UB.z, ez.y,
-                        UB.w, upA, ez.z, upB, ez.w, o);
+    interior_edge_muscl(M, a.ilimiteur, a.flux_mode, G, dt, S(UA.x), S(UA.y), S(UA.z), ez.x, UA.w, S(UB.x), S(UB.y),
+                        S(UB.z), ez.y, UB.w, upA, ez.z, upB, ez.w, om);
+#pragma unroll
+    for (int i = 0; i < 10; ++i) o[i] = val(om[i]);
     write_slots(sa, o);
     return;
   }

@@ -66,7 +66,7 @@ __global__ void __launch_bounds__(TILE_E) k_edges(StepArgs a) {
     }
   }
   if (e >= M.edge_end) return;
-  if (IFLUX <= 3 && a.xd_cmp) {
+  if (a.xd_cmp) {
     /* the same arithmetic with exact integer comparisons and, in the warps of xd_mul_mask,
      * exact integer products: the FP64 pipe and the integer pipes share the work */
     if ((a.xd_mul_mask >> (threadIdx.x >> 5)) & 1) edge_body<IFLUX, XD<true>>(a, M, e, dt, t, S->surf);

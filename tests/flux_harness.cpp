@@ -38,8 +38,8 @@ extern "C" void harness_set_xd(int mode) { g_xd = mode; }
 
 template <int IFLUX>
 static void edge_xd(const StepArgs& a, const MemberDev& M, int e, double dt, double t, const double* surf) {
-  if (IFLUX <= 3 && g_xd == 1) edge_body<IFLUX, XD<false>>(a, M, e, dt, t, surf);
-  else if (IFLUX <= 3 && g_xd == 2) edge_body<IFLUX, XD<true>>(a, M, e, dt, t, surf);
+  if (g_xd == 1) edge_body<IFLUX, XD<false>>(a, M, e, dt, t, surf);
+  else if (g_xd == 2) edge_body<IFLUX, XD<true>>(a, M, e, dt, t, surf);
   else edge_body<IFLUX>(a, M, e, dt, t, surf);
 }
 

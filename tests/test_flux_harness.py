@@ -122,7 +122,9 @@ def test_full_run_bitwise(oracle, name, make, n, prm):
 
 XD_CASES = [c for c in CASES if c[0] in ("dam_hllc", "dam_riadh", "dam_waf", "flood_hllc", "flood_riadh", "flood_waf",
                                           "flood_waf_conservative", "waf_lim2", "waf_lim3", "outlet_transm_waf",
-                                          "lake_wet", "dry_start_inflow", "phys_inflow_waf", "steady_stop_half")]
+                                          "lake_wet", "dry_start_inflow", "phys_inflow_waf", "steady_stop_half",
+                                          "dam_muscl", "flood_muscl", "muscl_lim2", "muscl_lim3",
+                                          "muscl_conservative", "lake_muscl")]
 
 
 @pytest.mark.parametrize("mode", [1, 2])

@@ -161,6 +161,24 @@ def test_config1_circular_dam_break_full(gpu_lib, oracle):
     assert abs(m1 - m0) <= 1e-12 * m0
 
 
+def test_config2_flooding_1M_5000_steps(gpu_lib, oracle):
+    """The benchmark workload at full size and length: 1,000,000 triangles, WAF, inflow ramp and
+    fixed-level outflow, 5000 steps from the initial state, with the edge kernel's integer-pipe
+    setting the bench runs (int_compare 1, all warps multiplying on the integer pipes).  Bit for
+    bit the oracle's state, time and next dt (the tolerance of the target is 1e-9 m)."""
+    from cuteflow_gb300 import Solver
+    c = cases.flooding(1000, 500, seed=2, iflux=3)
+    ref = oracle.run(c, 5000, check=False)
+    with Solver(c) as s:
+        s.set_tuning(1, 0xF)
+        s.set_state(c.U0)
+        info = s.step(5000)
+        U = s.get_state()
+    assert info.steps == 5000 and info.status == 0
+    assert np.array_equal(U, ref["U"]), np.abs(U - ref["U"]).max(axis=0)
+    assert info.t == ref["t"] and info.dt_next == ref["dt_hist"][5000]
+
+
 @pytest.mark.parametrize("iflux", [1, 3, 4])
 def test_phys_inflow(gpu_lib, oracle, iflux):
     """inlet 3 (phys_inflow): the per-step inlet sums of calcul_surf_entree on the device."""
