@@ -183,6 +183,7 @@ def ensemble(nmembers: int, steps: int, warmup: int, seed: int = 3):
     b = Batch(members)
     for i, m in enumerate(members):
         b.set_state(i, m.U0)
+    tune = b.autotune(20)   # the same setting runs in both forms below (results identical in any)
     b.step(warmup)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -194,6 +195,7 @@ def ensemble(nmembers: int, steps: int, warmup: int, seed: int = 3):
     t_seq = 0.0
     for m in members:
         s = Solver(m)
+        s.set_tuning(tune[0], tune[1])
         s.set_state(m.U0)
         s.step(warmup)
         torch.cuda.synchronize()
@@ -207,7 +209,8 @@ def ensemble(nmembers: int, steps: int, warmup: int, seed: int = 3):
             "triangles_min_median_max": [sizes[0], sizes[len(sizes) // 2], sizes[-1]],
             "batched_value": tri * steps / t_batch, "sequential_value": tri * steps / t_seq,
             "unit": UNIT, "speedup_vs_sequential": t_seq / t_batch,
-            "batched_s": t_batch, "sequential_s": t_seq, "stopped_members": sum(1 for i in infos if i.status)}
+            "batched_s": t_batch, "sequential_s": t_seq, "stopped_members": sum(1 for i in infos if i.status),
+            "tuning": {"int_compare": tune[0], "int_mul_warps": tune[1]}}
 
 
 def adjoint_leg(steps: int, warmup: int, obs_every: float = 10.0):
