@@ -495,7 +495,7 @@ int cf_case_read(const char* dir, const char* namelist_file, cf_case** out) {
   int rc = parse_namelist(ss.str(), "donnees_namelist", nml);
   if (rc == CF_OK) rc = apply_namelist(nml, *C);
   if (rc == CF_OK && C->is_cgns)
-    rc = io_fail(CF_ENOTSUP, "is_cgns = 1: CGNS meshes need libcgns, which this build does not use");
+    rc = io_fail(CF_ENOTSUP, "is_cgns = 1: CGNS meshes need libcgns, which this library does not link");
   if (rc == CF_OK) {
     /* trim(adjustl(meshfile_path)) // trim(adjustl(meshfile)), maillage.cuf:208 */
     const std::string mpath = trim(C->meshfile_path), mfile = trim(C->meshfile);

@@ -1,5 +1,5 @@
 """Build the golden fixtures of tests/golden/ from the reference checkout (run here, once; the
-outputs are committed and the GPU machine never reads the reference).
+outputs are committed, so the tests never read the reference at run time).
 
 Sources, all produced by the reference itself on a Tesla P100 and shipped in its repository:
   Calibration_manning/docs_calibration/River_piers/Froude/
