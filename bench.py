@@ -279,20 +279,23 @@ def adjoint_leg(steps: int, warmup: int, obs_every: float = 10.0):
     return out
 
 
-def calibration_batch_leg(ninst: int, steps: int, iters: int, obs_every: float = 10.0):
+def calibration_batch_leg(ninst: int, steps: int, iters: int, obs_every: float = 10.0, full: bool = False):
     """Batched adjoint calibration (a sample of the 64-instance workload): ninst instances of the
     calibration case with seeded sizes, zone fields and gauges, in one batch context; every
     gradient-descent iteration runs one recording forward and one backward for all instances in
     the same launches, sums dJ/dn per zone and steps the zone values on the device.  Timed
     against the same instances' one-member adjoints run one after another (forward, backward,
-    zone gradient and step each).  Misfit: sum of squared gauge misfits every obs_every s."""
+    zone gradient and step each).  Misfit: sum of squared gauge misfits every obs_every s.
+    Instance meshes: 8k-39k triangles for the sample, 50k-273k with full (the workload's sizes)."""
     import torch
     from cuteflow_gb300 import Batch, Solver, cases
     from cuteflow_gb300.adjoint import Adjoint, Zones
     inst = []
     for i in range(ninst):
-        nx = int(100 + (i * 37) % 120)
-        ny = int(40 + (i * 23) % 50)
+        if full:
+            nx, ny = int(250 + (i * 37) % 300), int(100 + (i * 23) % 180)
+        else:
+            nx, ny = int(100 + (i * 37) % 120), int(40 + (i * 23) % 50)
         c, zones, nz, gauges = cases.calibration(nx, ny, seed=10 + i, nzones=8 + i % 9, ngauges=20 + (i * 7) % 41)
         inst.append((c, zones, nz, gauges))
     tri = sum(c.nelt for c, *_ in inst)
@@ -527,9 +530,12 @@ def run_ours(args):
     if rank == 0 and args.adjoint_steps > 0:
         line["adjoint"] = adjoint_leg(args.adjoint_steps, 10)
     if rank == 0 and args.calib_instances > 0:
-        line["batched_adjoint"] = calibration_batch_leg(args.calib_instances, args.calib_steps, args.calib_iters)
-        line["batched_adjoint"]["note"] = ("sample of the 64-instance calibration workload (50k-300k triangles, "
-                                           "3000 steps, 10 iterations)")
+        line["batched_adjoint"] = calibration_batch_leg(args.calib_instances, args.calib_steps, args.calib_iters,
+                                                        full=args.calib_full)
+        line["batched_adjoint"]["note"] = (
+            "the 64-instance calibration workload's instance sizes (50k-273k triangles)" if args.calib_full else
+            "sample of the 64-instance calibration workload (50k-300k triangles, 3000 steps, 10 iterations); "
+            "`--calib-instances 64 --calib-steps 3000 --calib-full` runs its sizes")
     if rank == 0 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(case)
     s.close()
@@ -555,6 +561,7 @@ def main():
     ap.add_argument("--calib-instances", type=int, default=8, help="batched calibration leg (0: skip)")
     ap.add_argument("--calib-steps", type=int, default=400)
     ap.add_argument("--calib-iters", type=int, default=3)
+    ap.add_argument("--calib-full", action="store_true", help="calibration instances at the workload's sizes")
     ap.add_argument("--adjoint-steps", type=int, default=3000,
                     help="adjoint calibration leg beside the plain line (0: skip)")
     args = ap.parse_args()
