@@ -169,7 +169,7 @@ def circular_dam_break(nx: int = 200, ny: int = 200, seed: int = 1, lx: Optional
 
 def flooding(nx: int = 1000, ny: int = 500, seed: int = 2, lx: float = 2000.0, ly: float = 1000.0,
              iflux: int = 3, q0: float = 2.0, q1: float = 10.0, ramp: float = 600.0,
-             out_level: float = 1.0, tolisec: float = 1e-4, nbumps: int = 8) -> Case:
+             out_level: float = 1.0, tolisec: float = 1e-4, nbumps: int = 8, bump_scale: float = 1.0) -> Case:
     """Wet/dry flooding over seeded bathymetry.
 
     The benchmark case is 2 km x 1 km, 1000x500 quads (1,000,000 triangles),
@@ -177,13 +177,14 @@ def flooding(nx: int = 1000, ny: int = 500, seed: int = 2, lx: float = 2000.0, l
     per-element lognormal Manning (median 0.03, sigma_log 0.3, clipped to [0.01, 0.1]),
     still water at level 1.0 m where z < 1 m and dry elsewhere (dry threshold 1e-4 m),
     left-edge inflow ramping q = 2 -> 10 m^2/s over 600 s, fixed level 1.0 m at the right
-    edge, walls top and bottom, CFL 0.9, second-order WAF.
+    edge, walls top and bottom, CFL 0.9, second-order WAF.  bump_scale multiplies the bump
+    widths (smaller domains with the same bathymetry statistics per area).
     """
     x, y, tri = grid_mesh(nx, ny, lx, ly, seed)
     cx = uniform(seed, 10, nbumps, 0.0, lx)
     cy = uniform(seed, 11, nbumps, 0.0, ly)
     amp = uniform(seed, 12, nbumps, 0.5, 3.0)
-    wid = uniform(seed, 13, nbumps, 30.0, 150.0)
+    wid = uniform(seed, 13, nbumps, 30.0, 150.0) * bump_scale
     z = 0.001 * x
     for k in range(nbumps):
         z = z + amp[k] * np.exp(-((x - cx[k]) ** 2 + (y - cy[k]) ** 2) / (2.0 * wid[k] ** 2))
@@ -254,29 +255,24 @@ def lake_at_rest(nx: int = 40, ny: int = 20, seed: int = 5, depth: float = 0.5, 
 
 def ensemble_member(index: int, seed: int = 3, n_min: int = 20000, n_max: int = 500000,
                     iflux: int = 3) -> Case:
-    """One member of the batched ensemble: the circular-dam-break generator with its own
-    size (triangle count drawn unevenly in [n_min, n_max]), lognormal Manning field, and a
-    left-edge inflow ramping to a peak q ~ U(2, 15) m^2/s over 600 s with a fixed 1 m level
-    at the right edge."""
+    """One member of the batched ensemble: the flooding generator (seeded bathymetry, lognormal
+    Manning field, still water at 1 m, inflow ramp on the left edge, fixed 1 m level on the right)
+    with its own size (triangle count drawn unevenly in [n_min, n_max], aspect U(0.5, 2)) at the
+    benchmark case's 2 m spacing, its own seed for the bumps and the Manning field, bumps in
+    proportion to the area (8 per 2 km^2, at least one) with widths scaled by the square root of
+    the area ratio (the benchmark's bumps on the benchmark's domain keep their size; a small domain
+    is not covered by one hill and left dry), and an inflow ramping from 2 m^2/s to its own peak
+    q ~ U(2, 15) m^2/s over 600 s."""
     u = uniform(seed, 100, index + 1)[index]
     target = n_min * (n_max / n_min) ** (u ** 1.5)       # uneven, skewed towards small members
     aspect = uniform(seed, 101, index + 1, 0.5, 2.0)[index]
     ny = max(8, int(round(np.sqrt(target / 2.0 / aspect))))
     nx = max(8, int(round(target / 2.0 / ny)))
-    c = circular_dam_break(nx, ny, seed=seed * 1000 + index, iflux=iflux, tolisec=1e-4)
-    c.manning = _lognormal_manning(seed * 1000 + index, 20, c.nelt)
-    peak = uniform(seed, 102, index + 1, 2.0, 15.0)[index]
-    left, right, bottom, top = side_nodes(nx, ny)
-    c.ndinput = left
-    c.numero_ndinput = np.ones_like(left)
-    c.ndoutput = right
-    c.numero_ndoutput = np.ones_like(right)
-    c.ndwall = np.unique(np.concatenate([bottom, top])).astype(np.int32)
-    c.nombre_entrees = c.nombre_sorties = 1
-    ly = float(ny)
-    c.params = dict(iflux=iflux, ilimiteur=1, tolisec=1e-4, cfl=0.9, friction=1, fricimplic=1,
-                    is_override_manning=0, inlet=2, outlet=1, ramp_time=600.0,
-                    debitglob=[peak * ly], debitglob_start=[0.0], h_sortie=[1.0])
+    peak = float(uniform(seed, 102, index + 1, 2.0, 15.0)[index])
+    lx, ly = 2.0 * nx, 2.0 * ny
+    nbumps = max(1, int(round(8.0 * lx * ly / 2.0e6)))
+    c = flooding(nx, ny, seed=seed * 1000 + index, lx=lx, ly=ly, iflux=iflux, q0=2.0, q1=peak, nbumps=nbumps,
+                 bump_scale=min(1.0, float(np.sqrt(lx * ly / 2.0e6))))
     c.name = f"member_{index}_{nx}x{ny}"
     return c
 

@@ -32,6 +32,7 @@
 #include <cuda_runtime.h>
 
 #include "cf_dual.h"
+#include "cf_xd.h"
 
 namespace cf {
 namespace {
@@ -66,7 +67,13 @@ __global__ void __launch_bounds__(TILE_E) k_rep_edges(StepArgs a, const double* 
   const int e = tile * TILE_E + threadIdx.x;
   if (e >= M.edge_end) return;
   const size_t h = hidx(n, m, a.nmembers);
-  edge_body<IFLUX>(a, M, e, __ldg(dt_hist + h), __ldg(t_hist + h));
+  const double dt = __ldg(dt_hist + h), t = __ldg(t_hist + h);
+  if (a.xd_cmp) {   /* the context's integer-pipe setting, as the step's edge kernel (same results) */
+    if ((a.xd_mul_mask >> (threadIdx.x >> 5)) & 1) edge_body<IFLUX, XD<true>>(a, M, e, dt, t);
+    else edge_body<IFLUX, XD<false>>(a, M, e, dt, t);
+  } else {
+    edge_body<IFLUX>(a, M, e, dt, t);
+  }
 }
 
 __global__ void __launch_bounds__(TILE_C) k_rep_cells(StepArgs a, const double* dt_hist, int n, uint32_t* flag,

@@ -25,10 +25,10 @@
 
 #ifdef __CUDACC__
 #define XD_HD __host__ __device__ __forceinline__
-#define XD_NOINLINE __host__ __device__ __noinline__
+#define XD_NOINLINE static __host__ __device__ __noinline__
 #else
 #define XD_HD inline
-#define XD_NOINLINE __attribute__((noinline))
+#define XD_NOINLINE static __attribute__((noinline))
 #endif
 
 namespace cf {

@@ -45,6 +45,20 @@ def test_flooding_inputs_follow_the_spec():
     assert c.params["debitglob"][0] == 10.0 * 1000.0 and c.params["debitglob_start"][0] == 2.0 * 1000.0
 
 
+def test_ensemble_members_are_flooding_cases():
+    """Ensemble members come from the flooding generator: bathymetry (not flat), still water at
+    1 m, an inflow ramp from 2 m^2/s to the member's peak in [2, 15] m^2/s, the fixed 1 m outflow."""
+    for i in (0, 5, 17):
+        c = cases.ensemble_member(i)
+        ly = 2.0 * c.ny
+        assert np.ptp(np.asarray(c.z)) > 0.1
+        assert c.params["debitglob_start"][0] == 2.0 * ly
+        assert 2.0 * ly <= c.params["debitglob"][0] <= 15.0 * ly
+        assert c.params["h_sortie"] == [1.0] and c.params["iflux"] == 3
+        h = c.U0[:, 0]
+        assert h.max() <= 1.0 and (h > 0).any()
+
+
 def test_ensemble_sizes_span_range():
     n = [cases.ensemble_member(i).nelt for i in range(0, 256, 16)]
     assert min(n) >= 15000 and max(n) <= 560000

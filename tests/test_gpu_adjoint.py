@@ -155,6 +155,25 @@ def test_gradient_independent_of_checkpoint_interval(gpu_lib):
         assert np.array_equal(gU, out[0][0]) and np.array_equal(gn, out[0][1])
 
 
+@pytest.mark.parametrize("case", ["waf_flood", "hllc_dam"])
+def test_gradient_independent_of_integer_pipe_setting(gpu_lib, case):
+    """The recording forward and the segment replays run the step's edge kernel in the context's
+    integer-pipe setting; every setting rounds identically, so the gradient is the same bit for bit."""
+    from cuteflow_gb300.adjoint import Adjoint
+    c, extra, s, adj, w_eta, w_state = _setup(case, nsteps=23)
+    out = []
+    with s:
+        adj.close()
+        for tuning in ((0, 0), (1, 0), (1, 0xF), (1, 0x5)):
+            s.set_tuning(*tuning)
+            with Adjoint(s, 23, adj.gauges, 4) as a:
+                s.set_state(c.U0)
+                a.forward()
+                out.append(a.backward(w_eta, w_state))
+    for gU, gn in out[1:]:
+        assert np.array_equal(gU, out[0][0]) and np.array_equal(gn, out[0][1])
+
+
 def test_torch_function(gpu_lib):
     torch = pytest.importorskip("torch")
     from cuteflow_gb300.adjoint import gauge_run
