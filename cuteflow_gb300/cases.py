@@ -15,6 +15,7 @@ may differ in the last bit between machines).
 from __future__ import annotations
 
 import dataclasses
+import math
 from typing import Optional
 
 import numpy as np
@@ -40,12 +41,72 @@ def uniform(seed: int, stream: int, n: int, lo: float = 0.0, hi: float = 1.0) ->
     return lo + (hi - lo) * u
 
 
+# ---- elementary functions as fixed sequences of float64 operations --------------------------
+#
+# numpy's exp, log and cos are not correctly rounded and differ between its x86-64 and aarch64
+# builds, so the same seed would give different inputs on different machines.  The generators use
+# these instead: range reduction that is exact, then a truncated Taylor or atanh series by Horner's
+# rule in plain IEEE additions and multiplications (a few ulp from the true value, identical on every
+# machine).
+
+_LN2_HI = float.fromhex("0x1.62e42fee00000p-1")   # ln 2 truncated to 32 bits: k * _LN2_HI is exact
+_LN2_LO = float.fromhex("0x1.a39ef35793c76p-33")  # ln 2 - _LN2_HI
+_INV_LN2 = float.fromhex("0x1.71547652b82fep+0")
+_TWO_PI = float.fromhex("0x1.921fb54442d18p+2")
+_INV_FACT = [1.0 / float(math.factorial(i)) for i in range(23)]
+
+
+def det_exp(x) -> np.ndarray:
+    """e^x: x = k ln 2 + r (Cody-Waite, |r| <= ln2 / 2), e^r by its Taylor series to r^13, 2^k exactly."""
+    x = np.asarray(x, dtype=np.float64)
+    k = np.rint(x * _INV_LN2)
+    r = (x - k * _LN2_HI) - k * _LN2_LO
+    p = np.full_like(r, _INV_FACT[13])
+    for i in range(12, -1, -1):
+        p = p * r + _INV_FACT[i]
+    return np.ldexp(p, np.clip(k, -2000, 2000).astype(np.int64))
+
+
+def det_log(x) -> np.ndarray:
+    """ln x for x > 0: x = m 2^e with m in [1/sqrt 2, sqrt 2), ln m = 2 atanh(s) with
+    s = (m - 1) / (m + 1) (|s| <= 0.172) by its series to s^23."""
+    m, e = np.frexp(np.asarray(x, dtype=np.float64))
+    low = m < 0.7071067811865476
+    m = np.where(low, m * 2.0, m)
+    e = np.where(low, e - 1, e).astype(np.float64)
+    s = (m - 1.0) / (m + 1.0)
+    s2 = s * s
+    p = np.full_like(s, 1.0 / 23.0)
+    for j in range(21, 0, -2):
+        p = p * s2 + 1.0 / j
+    return e * _LN2_HI + (e * _LN2_LO + 2.0 * s * p)
+
+
+def det_cos2pi(u) -> np.ndarray:
+    """cos(2 pi u) for u in [0, 1): folded by symmetry (exact subtractions) to an angle in
+    [0, pi/4], where the Taylor series of cos (to x^20) or of sin (to x^21) is summed."""
+    u = np.asarray(u, dtype=np.float64)
+    w = np.where(u > 0.5, 1.0 - u, u)                  # cos(2 pi u) = cos(2 pi (1 - u))
+    neg = w > 0.25
+    w = np.where(neg, 0.5 - w, w)                      # cos(2 pi w) = -cos(2 pi (1/2 - w))
+    use_sin = w > 0.125
+    a = _TWO_PI * np.where(use_sin, 0.25 - w, w)       # cos(2 pi w) = sin(2 pi (1/4 - w))
+    a2 = a * a
+    c = np.full_like(a, _INV_FACT[20])
+    sn = np.full_like(a, _INV_FACT[21])
+    for i in range(18, -1, -2):
+        c = c * a2 * (-1.0) + _INV_FACT[i]
+        sn = sn * a2 * (-1.0) + _INV_FACT[i + 1]
+    v = np.where(use_sin, a * sn, c)
+    return np.where(neg, -v, v)
+
+
 def normal(seed: int, stream: int, n: int) -> np.ndarray:
     """Box-Muller standard normals."""
     u1 = uniform(seed, stream, n)
     u2 = uniform(seed, stream + 1000003, n)
     u1 = np.maximum(u1, 1e-300)
-    return np.sqrt(-2.0 * np.log(u1)) * np.cos(2.0 * np.pi * u2)
+    return np.sqrt(-2.0 * det_log(u1)) * det_cos2pi(u2)
 
 
 @dataclasses.dataclass
@@ -135,7 +196,7 @@ def cell_bed(x, y, z, tri):
 
 
 def _lognormal_manning(seed: int, stream: int, n: int, median=0.03, sigma=0.3, lo=0.01, hi=0.1):
-    return np.clip(median * np.exp(sigma * normal(seed, stream, n)), lo, hi)
+    return np.clip(median * det_exp(sigma * normal(seed, stream, n)), lo, hi)
 
 
 def circular_dam_break(nx: int = 200, ny: int = 200, seed: int = 1, lx: Optional[float] = None,
@@ -187,7 +248,7 @@ def flooding(nx: int = 1000, ny: int = 500, seed: int = 2, lx: float = 2000.0, l
     wid = uniform(seed, 13, nbumps, 30.0, 150.0) * bump_scale
     z = 0.001 * x
     for k in range(nbumps):
-        z = z + amp[k] * np.exp(-((x - cx[k]) ** 2 + (y - cy[k]) ** 2) / (2.0 * wid[k] ** 2))
+        z = z + amp[k] * det_exp(-((x - cx[k]) ** 2 + (y - cy[k]) ** 2) / (2.0 * wid[k] ** 2))
     manning = _lognormal_manning(seed, 20, tri.shape[0])
     zc = cell_bed(x, y, z, tri)
     h = 1.0 - zc
@@ -264,7 +325,7 @@ def ensemble_member(index: int, seed: int = 3, n_min: int = 20000, n_max: int = 
     is not covered by one hill and left dry), and an inflow ramping from 2 m^2/s to its own peak
     q ~ U(2, 15) m^2/s over 600 s."""
     u = uniform(seed, 100, index + 1)[index]
-    target = n_min * (n_max / n_min) ** (u ** 1.5)       # uneven, skewed towards small members
+    target = n_min * float(det_exp(u * np.sqrt(u) * det_log(n_max / n_min)))   # uneven, skewed to small members
     aspect = uniform(seed, 101, index + 1, 0.5, 2.0)[index]
     ny = max(8, int(round(np.sqrt(target / 2.0 / aspect))))
     nx = max(8, int(round(target / 2.0 / ny)))

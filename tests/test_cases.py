@@ -1,5 +1,6 @@
 """The seeded case generator: sizes of the benchmark workloads, determinism, orientation."""
 import numpy as np
+import pytest
 
 from cuteflow_gb300 import cases
 
@@ -63,3 +64,23 @@ def test_ensemble_sizes_span_range():
     n = [cases.ensemble_member(i).nelt for i in range(0, 256, 16)]
     assert min(n) >= 15000 and max(n) <= 560000
     assert max(n) / min(n) > 5
+
+
+def test_generator_functions_are_accurate_fixed_sequences():
+    """det_exp / det_log / det_cos2pi (the generators' elementary functions: plain float64 operation
+    sequences, so every machine builds the same inputs from a seed) within 4 ulp of the exact values
+    (mpmath) over the ranges the generators use."""
+    mpmath = pytest.importorskip("mpmath")
+    mpmath.mp.prec = 120
+    rng = np.random.default_rng(3)
+    xe = np.concatenate([rng.uniform(-700.0, 0.0, 3000), rng.uniform(-3.0, 3.0, 3000)])
+    xl = np.concatenate([10.0 ** rng.uniform(-300, 0, 3000), rng.uniform(0.5, 30.0, 3000)])
+    xc = rng.uniform(0.0, 1.0, 6000)
+    for f, xs, ref in ((cases.det_exp, xe, mpmath.exp), (cases.det_log, xl, mpmath.log),
+                       (cases.det_cos2pi, xc, lambda u: mpmath.cos(2 * mpmath.pi * u))):
+        got = f(xs)
+        for x, g in zip(xs, got):
+            r = float(ref(mpmath.mpf(float(x))))
+            assert abs(g - r) <= 4 * np.spacing(max(abs(r), 1e-300)) + (1e-16 if f is cases.det_cos2pi else 0.0), (f, x, g, r)
+    # the same value for an element wherever it sits in the array
+    assert np.array_equal(cases.det_exp(xe)[::7], cases.det_exp(xe[::7].copy()))
