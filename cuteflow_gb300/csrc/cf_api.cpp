@@ -376,13 +376,16 @@ int set_state_member(cf_ctx* c, int32_t m, double t0) {
   s.base = p0;
   c->host_state[m] = s;
   CF_CUDA(c, cudaMemcpyAsync(c->mst + m, c->host_state + m, sizeof(MemberState), cudaMemcpyHostToDevice, c->stream));
+  CF_CUDA(c, cudaEventRecord(c->ev[3], c->stream));   /* the host inputs (caller's state, member record) read */
   int rc = launch_scatter_state(c->staging, c->perm + M.cell_off, c->zcell + M.cell_off, c->U[p0] + M.cell_off, M.n,
                                 reinterpret_cast<stream_t>(c->stream));
   if (rc != CF_OK) return fail(c, rc, "state scatter launch failed");
   rc = launch_cfl(c->U[p0], c->cstat, c->ctile_mem, M.ctile_begin, M.ctile_end - M.ctile_begin, c->mdev, c->mst, p0,
                   reinterpret_cast<stream_t>(c->stream));
   if (rc != CF_OK) return fail(c, rc, "cfl launch failed");
-  CF_CUDA(c, cudaStreamSynchronize(c->stream));
+  /* return once the host buffers are consumed; the scatter and the initial dt run on the stream
+   * ahead of the next call's work (which every later call orders after) */
+  CF_CUDA(c, cudaEventSynchronize(c->ev[3]));
   return CF_OK;
 }
 

@@ -70,7 +70,7 @@ struct cf_ctx {
   bool use_graph = true;
   /* timing */
   bool timing = false;
-  cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};   /* 0-2 timing, 3: inputs of cf_set_state consumed */
   double flux_ms = 0.0, update_ms = 0.0;
   int64_t launches = 0;
   std::string err;
