@@ -148,7 +148,8 @@ void cf_destroy(cf_ctx* ctx);
 
 /* Set U^0 from host memory: hu3[3*k+c] = vdlg0(c+1, k+1) (read_initial_condition,
  * initial_condition.cuf:82-102).  Resets the time to t0 and the step count, and computes
- * the first dt (finite_volumes_method.cuf:113-116). */
+ * the first dt (finite_volumes_method.cuf:113-116).  Returns once hu3 has been read (the
+ * caller may reuse it); the state's device-side setup runs ahead of the context's next call. */
 int cf_set_state(cf_ctx* ctx, const double* hu3, double t0);
 
 /* Same with a device pointer (3*nelt doubles, reference element order). */
