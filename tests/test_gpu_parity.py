@@ -302,6 +302,23 @@ def test_autotune_leaves_the_run_unchanged(gpu_lib, oracle):
         assert np.array_equal(s.get_state(), ref["U"]) and info.t == ref["t"] and info.steps == 90
 
 
+def test_set_state_consumes_a_pinned_buffer_before_returning(gpu_lib, oracle):
+    """cf_set_state from pinned host memory (an asynchronous copy) returns once the buffer has been
+    read: the caller overwrites it at once, and the run is still the oracle's."""
+    import ctypes
+    torch = pytest.importorskip("torch")
+    from cuteflow_gb300 import Solver
+    c = cases.flooding(60, 30, seed=3, iflux=3)
+    ref = oracle.run(c, 40)
+    buf = torch.from_numpy(np.ascontiguousarray(c.U0, dtype=np.float64)).pin_memory()
+    with Solver(c) as s:
+        rc = s._L.cf_set_state(s._ctx, ctypes.cast(buf.data_ptr(), ctypes.POINTER(ctypes.c_double)), 0.0)
+        assert rc == 0
+        buf.fill_(float("nan"))
+        info = s.step(40)
+        assert np.array_equal(s.get_state(), ref["U"]) and info.t == ref["t"]
+
+
 def test_fp64_probe_reports_a_plausible_rate(gpu_lib):
     """cf_probe_fp64 (the step's roofline denominator): GB300 issues ~2 FP64 instructions per
     clock per SM, ~6e11/s over 152 SMs at 2 GHz; the probe must land in that range and leave the
