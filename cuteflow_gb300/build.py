@@ -22,7 +22,7 @@ CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA_HOME, "bin", "nvcc") if os.path.exists(os.path.join(CUDA_HOME, "bin", "nvcc")) else "nvcc"
 
 CU_SOURCES = ["cf_kernels.cu", "cf_noalloc.cu", "cf_adjoint.cu"]
-CPP_SOURCES = ["cf_mesh.cpp", "cf_api.cpp", "cf_adjoint_api.cpp", "cf_io.cpp"]
+CPP_SOURCES = ["cf_mesh.cpp", "cf_api.cpp", "cf_adjoint_api.cpp", "cf_io.cpp", "cf_cgns.cpp"]
 HEADERS = ["cf_internal.h", "cf_flux.h", "cf_dual.h", "cf_ctx.h", "cf_xd.h"]
 
 

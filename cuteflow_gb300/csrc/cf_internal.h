@@ -243,6 +243,17 @@ int ctx_error(cf_ctx* c, int code, const std::string& msg);  /* record msg, retu
  * place of the context's own slot buffer: direct launches, no graph, no allocation. */
 int step_with_slots(cf_ctx* c, int32_t nsteps, cf_step_info* infos, Slot* slots, size_t capacity);
 
+/* lec_mail_cgns (maillage.cuf:398-778) for one process, without libcgns (cf_cgns.cpp): a CGNS/HDF5
+ * triangle mesh with its inflow/outflow node lists (numbered by inlet_name / outlet_name) and, when
+ * want_manning, the per-element "Manning" user data.  Returns a CF_* code; err says why. */
+struct CgnsMesh {
+  std::vector<double> x, y, z, manning_elt;
+  std::vector<int32_t> tri, ndinput, numero_ndinput, ndoutput, numero_ndoutput;
+  bool has_manning = false;
+};
+int read_cgns_mesh(const std::string& path, const std::vector<std::string>& inlet_names,
+                   const std::vector<std::string>& outlet_names, bool want_manning, CgnsMesh& M, std::string& err);
+
 }  // namespace cf
 
 #endif

@@ -10,7 +10,8 @@
  *                 initial_condition.cuf:82-102), and the same layout written back
  *                 (save_sol_for_restart, pre_post_traitement.cuf:498-512).
  *
- * CGNS meshes (is_cgns = 1, maillage.cuf:398-778) need libcgns/HDF5 and are not read here.
+ *   CGNS mesh     is_cgns = 1 (lec_mail_cgns, maillage.cuf:398-778), read by cf_cgns.cpp from the
+ *                 HDF5 container directly (no libcgns).
  * Host code only; nothing here touches the GPU.
  */
 #include <cctype>
@@ -41,6 +42,7 @@ struct cf_case {
   std::vector<double> U0;  /* solinit = 1: the state of fich_sol_init */
   double tc_init = 0.0;    /* the first value of fich_sol_init (read, not used: main.cuf:182) */
   std::string meshfile_path = "./", meshfile, fich_sol_init;
+  std::vector<std::string> inlet_name, outlet_name;   /* CGNS boundary names of the inlets / outlets */
 };
 
 namespace {
@@ -293,6 +295,15 @@ int apply_namelist(const std::vector<std::pair<std::string, NmlValue>>& nml, cf_
     else if (k == "is_cgns") rc = int1(C.is_cgns);
     else if (k == "meshfile_path") C.meshfile_path = v.items[0];
     else if (k == "meshfile") C.meshfile = v.items[0];
+    else if (k == "inlet_name" || k == "outlet_name") {
+      auto& names = (k == "inlet_name") ? C.inlet_name : C.outlet_name;
+      for (size_t i = 0; i < v.items.size(); ++i) {
+        const int64_t at = v.index - 1 + (int64_t)i;
+        if (at < 0 || at >= CF_MAX_IO) return io_fail(CF_EINVAL, "namelist: '" + k + "' has more than 20 values");
+        if ((int64_t)names.size() <= at) names.resize((size_t)at + 1);
+        names[(size_t)at] = v.items[i];
+      }
+    }
     else if (k == "nombre_entrees") rc = int1(C.mesh.nombre_entrees);
     else if (k == "nombre_sorties") rc = int1(C.mesh.nombre_sorties);
     else if (k == "eqlin_barrage") rc = int1(ic.eqlin_barrage);
@@ -437,6 +448,35 @@ int read_mesh(const std::string& path, cf_case& C) {
   return CF_OK;
 }
 
+/* lec_mail_cgns (maillage.cuf:398-778), one process: the mesh, its inflow/outflow node lists and
+ * its per-element Manning n (unless is_override_manning, which the step applies itself); no wall
+ * nodes are listed (every unmatched boundary edge is a wall, maillage.cuf:1454-1471). */
+int read_cgns(const std::string& path, cf_case& C) {
+  cf::CgnsMesh M;
+  std::string err;
+  const bool want_manning = C.params.is_override_manning != 1;
+  const int rc = cf::read_cgns_mesh(path, C.inlet_name, C.outlet_name, want_manning, M, err);
+  if (rc != CF_OK) return io_fail(rc, "CGNS mesh " + path + ": " + err);
+  if (want_manning && !M.has_manning)
+    return io_fail(CF_EINVAL, "CGNS mesh " + path + " has no Manning user data and is_override_manning = 0");
+  if (!M.ndinput.empty() && C.mesh.nombre_entrees < 1)
+    return io_fail(CF_EINVAL, "CGNS mesh " + path + " has inflow nodes but nombre_entrees = 0");
+  if (!M.ndoutput.empty() && C.mesh.nombre_sorties < 1)
+    return io_fail(CF_EINVAL, "CGNS mesh " + path + " has outflow nodes but nombre_sorties = 0");
+  C.x = std::move(M.x);
+  C.y = std::move(M.y);
+  C.z = std::move(M.z);
+  C.manning_nd.assign(C.x.size(), 0.0);
+  C.tri = std::move(M.tri);
+  C.manning_elt = want_manning ? std::move(M.manning_elt) : std::vector<double>(C.tri.size() / 3, C.params.override_manning);
+  C.ndinput = std::move(M.ndinput);
+  C.numero_ndinput = std::move(M.numero_ndinput);
+  C.ndoutput = std::move(M.ndoutput);
+  C.numero_ndoutput = std::move(M.numero_ndoutput);
+  C.ndwall.clear();
+  return CF_OK;
+}
+
 /* read_initial_condition (initial_condition.cuf:82-102) */
 int read_state_file(const std::string& path, int64_t nelt, std::vector<double>& U, double& t0) {
   std::ifstream f(path);
@@ -494,13 +534,12 @@ int cf_case_read(const char* dir, const char* namelist_file, cf_case** out) {
   std::vector<std::pair<std::string, NmlValue>> nml;
   int rc = parse_namelist(ss.str(), "donnees_namelist", nml);
   if (rc == CF_OK) rc = apply_namelist(nml, *C);
-  if (rc == CF_OK && C->is_cgns)
-    rc = io_fail(CF_ENOTSUP, "is_cgns = 1: CGNS meshes need libcgns, which this library does not link");
   if (rc == CF_OK) {
     /* trim(adjustl(meshfile_path)) // trim(adjustl(meshfile)), maillage.cuf:208 */
     const std::string mpath = trim(C->meshfile_path), mfile = trim(C->meshfile);
     if (mfile.empty()) rc = io_fail(CF_EINVAL, "namelist: no meshfile");
-    else rc = read_mesh(join_path(d, mpath + mfile), *C);
+    else if (!C->is_cgns) rc = read_mesh(join_path(d, mpath + mfile), *C);
+    else rc = read_cgns(join_path(d, mpath + mfile), *C);
   }
   if (rc == CF_OK) fill_mesh(*C);
   if (rc == CF_OK && C->solinit == 1)

@@ -61,6 +61,11 @@ def read_table(path):
     return np.stack([a[:, 0:3], a[:, 3:6]], axis=2).astype(np.int32)  # boundary(k, j, 1:2), before walls
 
 
+# where the reference checkout is read from when no path is given (tests that read its case
+# directories directly, on a machine that has it, use the same default)
+DEFAULT_REFERENCE = "/root/reference"
+
+
 def main(ref):
     cal = os.path.join(ref, "Calibration_manning", "docs_calibration")
     rp = os.path.join(cal, "River_piers", "Froude")
@@ -87,4 +92,4 @@ def main(ref):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    main(sys.argv[1] if len(sys.argv) > 1 else DEFAULT_REFERENCE)

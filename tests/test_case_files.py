@@ -115,7 +115,7 @@ def test_namelist_and_mesh_syntax(tmp_path):
 
 @pytest.mark.parametrize("change,code,words", [
     (("GP=9.81,", "GP=9.81, bogus_key=3,"), _abi.CF_EINVAL, "unknown key"),
-    (("is_cgns=0", "is_cgns=1"), _abi.CF_ENOTSUP, "CGNS"),
+    (("is_cgns=0", "is_cgns=1"), _abi.CF_EINVAL, "not an HDF5 file"),   # an ASCII mesh named as CGNS
     (('meshfile="m.txt"', 'meshfile="missing.txt"'), _abi.CF_EINVAL, "cannot open"),
     (("IFLUX=3", "IFLUX=three"), _abi.CF_EINVAL, "iflux"),
     (("inlet='phys_inflow'", "inlet='sideways'"), _abi.CF_EINVAL, "inlet"),
@@ -156,3 +156,64 @@ def test_restart_file_layout(tmp_path):
     r = case_files.read_case(str(tmp_path))
     assert r.t_file == 12.25
     assert np.abs(r.U0 - U).max() <= 5e-7
+
+
+def _reference_case_dir(sub):
+    """A case directory of the reference checkout, where this machine has one (the path the golden
+    fixtures were made from); None elsewhere."""
+    import os
+    import sys
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden"))
+    import make_golden
+    d = os.path.join(make_golden.DEFAULT_REFERENCE, "Calibration_manning", "docs_calibration", sub)
+    return d if os.path.isfile(os.path.join(d, "donnees.f")) else None
+
+
+@pytest.mark.parametrize("name,sub", [("river_piers", "River_piers/Froude"),
+                                      ("divergent_canal", "Divergent_Canal/Froude")])
+def test_cgns_case_directories_of_the_reference(tmp_path, name, sub):
+    """is_cgns = 1: the reference's own case directories (donnees.f + CGNS/HDF5 mesh) read through
+    cf_case_read give the mesh, boundary node lists and parameters of the golden fixtures (which a
+    separate Python HDF5 reader decoded from the same files), and the boundary table CuteFlow wrote;
+    with is_override_manning = 0 the per-element Manning n comes from the mesh's user data."""
+    d = _reference_case_dir(sub)
+    if d is None:
+        pytest.skip("the reference checkout is not on this machine")
+    import os
+    import golden_cases as G
+    g = G.load(name)
+    r = case_files.read_case(d)
+    assert r.nelt == g["tri"].shape[0]
+    for k in ("x", "y", "z", "ndinput", "ndoutput"):
+        assert np.array_equal(np.asarray(getattr(r, k)), g[k]), k
+    assert np.array_equal(np.asarray(r.tri).reshape(-1, 3), g["tri"])
+    assert set(np.asarray(r.numero_ndinput).tolist()) == {1} and len(r.ndwall) == 0
+    for k in ("iflux", "ilimiteur", "fricimplic", "tolisec", "cfl", "gp"):
+        assert r.params[k] == g[k].item(), k
+    assert r.params["is_override_manning"] == 1
+    assert np.array_equal(solver.mesh_tables(r, r.params)[0], G.reference_table(g))
+    # the same case with the mesh's own Manning field
+    text = open(os.path.join(d, "donnees.f")).read()
+    text = text.replace("is_override_manning=1", "is_override_manning=0")
+    text = text.replace("meshfile_path='./'", f"meshfile_path='{d}/'")
+    (tmp_path / "donnees.f").write_text(text)
+    r0 = case_files.read_case(str(tmp_path))
+    assert r0.params["is_override_manning"] == 0
+    assert np.array_equal(np.asarray(r0.manning), g["manning"])
+
+
+def test_cgns_errors_are_reported(tmp_path):
+    """A CGNS mesh that is not HDF5, or is cut short, is an error code with a message."""
+    (tmp_path / "mesh.cgns").write_bytes(b"not an hdf5 file at all" * 10)
+    (tmp_path / "donnees.f").write_text("&donnees_namelist\n is_cgns=1, meshfile='mesh.cgns',\n/\n")
+    with pytest.raises(Exception) as e:
+        case_files.read_case(str(tmp_path))
+    assert "HDF5" in str(e.value)
+    d = _reference_case_dir("River_piers/Froude")
+    if d is not None:
+        import os
+        raw = open(os.path.join(d, "manning_River_wth_piers.cgns"), "rb").read()
+        for cut in (100, 2000, len(raw) // 2):
+            (tmp_path / "mesh.cgns").write_bytes(raw[:cut])
+            with pytest.raises(Exception):
+                case_files.read_case(str(tmp_path))
