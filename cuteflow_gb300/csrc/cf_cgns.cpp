@@ -13,8 +13,9 @@
  * (version 3.0): superblock versions 2 and 3, version-2 object headers with continuation blocks,
  * link messages of compact groups, attribute messages, and datasets with compact, contiguous or
  * chunked (version-1 B-tree index) layout of integers, floats and strings.  Filtered (compressed)
- * datasets, dense link storage and other layouts are reported as not supported.  Every read is
- * bounds-checked: a malformed file gives an error, never a crash.  Host code only.
+ * datasets, dense link storage and other layouts are reported as not supported.  The checksums of
+ * the superblock and of every object header are verified, and every read is bounds-checked: a
+ * malformed file gives an error, never a crash.  Host code only.
  */
 #include <algorithm>
 #include <cstdint>
@@ -43,6 +44,44 @@ struct Msg {
   int type;
   size_t off, len;
 };
+
+/* Bob Jenkins' lookup3 hash of bytes (hashlittle, public domain, 2006), which HDF5 stores as the
+ * checksum of its version-2 superblocks and object headers (initial value 0). */
+uint32_t lookup3(const uint8_t* k, size_t length, uint32_t initval) {
+  auto rot = [](uint32_t x, int r) { return (x << r) | (x >> (32 - r)); };
+  uint32_t a, b, c;
+  a = b = c = 0xdeadbeefu + (uint32_t)length + initval;
+  auto word = [&](size_t i) {
+    return (uint32_t)k[i] | ((uint32_t)k[i + 1] << 8) | ((uint32_t)k[i + 2] << 16) | ((uint32_t)k[i + 3] << 24);
+  };
+  while (length > 12) {
+    a += word(0);
+    b += word(4);
+    c += word(8);
+    a -= c; a ^= rot(c, 4);  c += b;
+    b -= a; b ^= rot(a, 6);  a += c;
+    c -= b; c ^= rot(b, 8);  b += a;
+    a -= c; a ^= rot(c, 16); c += b;
+    b -= a; b ^= rot(a, 19); a += c;
+    c -= b; c ^= rot(b, 4);  b += a;
+    length -= 12;
+    k += 12;
+  }
+  if (length == 0) return c;
+  uint8_t tail[12] = {0};
+  std::memcpy(tail, k, length);
+  a += (uint32_t)tail[0] | ((uint32_t)tail[1] << 8) | ((uint32_t)tail[2] << 16) | ((uint32_t)tail[3] << 24);
+  b += (uint32_t)tail[4] | ((uint32_t)tail[5] << 8) | ((uint32_t)tail[6] << 16) | ((uint32_t)tail[7] << 24);
+  c += (uint32_t)tail[8] | ((uint32_t)tail[9] << 8) | ((uint32_t)tail[10] << 16) | ((uint32_t)tail[11] << 24);
+  c ^= b; c -= rot(b, 14);
+  a ^= c; a -= rot(c, 11);
+  b ^= a; b -= rot(a, 25);
+  c ^= b; c -= rot(b, 16);
+  a ^= c; a -= rot(c, 4);
+  b ^= a; b -= rot(a, 14);
+  c ^= b; c -= rot(b, 24);
+  return c;
+}
 
 struct Data {
   int cls = -1;            /* 0 integer, 1 float, 3 string */
@@ -75,6 +114,7 @@ class H5 {
     p += so_;          /* superblock extension */
     p += so_;          /* end of file */
     root_ = u(p, so_);
+    checksum(0, p + so_, "superblock");
   }
 
   uint64_t root() const { return root_; }
@@ -98,6 +138,8 @@ class H5 {
     const uint64_t size0 = u(p, csize);
     p += csize;
     const bool track = (flags & 0x04) != 0;
+    need(p, size0 + 4);
+    checksum(addr, (size_t)(p - addr + size0), "object header");
     std::vector<std::pair<size_t, size_t>> chunks{{p, p + (size_t)size0}};
     std::vector<Msg> out;
     for (size_t ci = 0; ci < chunks.size(); ++ci) {
@@ -113,7 +155,10 @@ class H5 {
         if (mtype == 0x10) {   /* continuation */
           const uint64_t caddr = u(q, so_), clen = u(q + so_, sl_);
           need(caddr, clen);
-          if (clen >= 8 && std::memcmp(&b_[caddr], "OCHK", 4) == 0) chunks.emplace_back(caddr + 4, caddr + clen - 4);
+          if (clen >= 8 && std::memcmp(&b_[caddr], "OCHK", 4) == 0) {
+            checksum(caddr, (size_t)clen - 4, "object header continuation");
+            chunks.emplace_back(caddr + 4, caddr + clen - 4);
+          }
         } else if (mtype != 0) {
           out.push_back({mtype, q, msize});
         }
@@ -241,6 +286,13 @@ class H5 {
  private:
   void need(uint64_t p, uint64_t n) const {
     if (p > b_.size() || n > b_.size() - p) h5fail(CF_EINVAL, "HDF5 structure outside the file");
+  }
+
+  /* the lookup3 checksum stored after the n bytes at p */
+  void checksum(uint64_t p, size_t n, const char* what) const {
+    need(p, (uint64_t)n + 4);
+    if (lookup3(&b_[p], n, 0) != (uint32_t)u(p + n, 4))
+      h5fail(CF_EINVAL, std::string("HDF5 ") + what + " checksum mismatch (corrupted file)");
   }
 
   /* a version-1 B-tree of raw-data chunks: copy every chunk into out.raw */

@@ -217,3 +217,11 @@ def test_cgns_errors_are_reported(tmp_path):
             (tmp_path / "mesh.cgns").write_bytes(raw[:cut])
             with pytest.raises(Exception):
                 case_files.read_case(str(tmp_path))
+        # one changed byte in an object header fails its checksum
+        bad = bytearray(raw)
+        at = bad.find(b"OHDR", 64)
+        bad[at + 9] ^= 0x01
+        (tmp_path / "mesh.cgns").write_bytes(bytes(bad))
+        with pytest.raises(Exception) as e:
+            case_files.read_case(str(tmp_path))
+        assert "checksum" in str(e.value)
