@@ -202,6 +202,30 @@ def test_cgns_case_directories_of_the_reference(tmp_path, name, sub):
     assert np.array_equal(np.asarray(r0.manning), g["manning"])
 
 
+def test_cgns_mesh_without_boundary_lists(tmp_path):
+    """A CGNS mesh of the reference's calibration example (32-bit connectivity, no ZoneBC, no Manning
+    data): read with an override Manning n, every node of it as the independent Python HDF5 reader
+    of the golden-fixture script decodes it, and no inflow or outflow node."""
+    import os
+    d = _reference_case_dir("River_piers/Froude")
+    if d is None:
+        pytest.skip("the reference checkout is not on this machine")
+    import make_golden
+    from hdf5_min import H5
+    mesh = os.path.join(make_golden.DEFAULT_REFERENCE, "Calibration_manning", "Exemple2", "base_files", "mesh_6072.cgns")
+    (tmp_path / "donnees.f").write_text(
+        f"&donnees_namelist\n is_cgns=1, meshfile_path='{os.path.dirname(mesh)}/', meshfile='mesh_6072.cgns',\n"
+        " is_override_manning=1, override_manning=0.03,\n/\n")
+    r = case_files.read_case(str(tmp_path))
+    h = H5(mesh)
+    Z = ["Base", "Zone"]
+    for k, name in (("x", "CoordinateX"), ("y", "CoordinateY"), ("z", "CoordinateZ")):
+        assert np.array_equal(np.asarray(getattr(r, k)), h.cgns_data(Z + ["GridCoordinates", name])), k
+    conn = h.cgns_data(Z + ["Elements", "ElementConnectivity"]).reshape(-1, 3)
+    assert r.nelt == 6072 and np.array_equal(np.asarray(r.tri).reshape(-1, 3), conn)
+    assert len(r.ndinput) == 0 and len(r.ndoutput) == 0 and np.all(np.asarray(r.manning) == 0.03)
+
+
 def test_cgns_errors_are_reported(tmp_path):
     """A CGNS mesh that is not HDF5, or is cut short, is an error code with a message."""
     (tmp_path / "mesh.cgns").write_bytes(b"not an hdf5 file at all" * 10)
