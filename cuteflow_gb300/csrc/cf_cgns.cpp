@@ -83,6 +83,13 @@ uint32_t lookup3(const uint8_t* k, size_t length, uint32_t initval) {
   return c;
 }
 
+/* a * b, or an error when the product leaves 2^40 (no array of a mesh file comes near it) */
+uint64_t mul_checked(uint64_t a, uint64_t b) {
+  const uint64_t lim = (uint64_t)1 << 40;
+  if (a > lim || b > lim || (a != 0 && b > lim / a)) h5fail(CF_EINVAL, "HDF5 dataset dimensions too large");
+  return a * b;
+}
+
 struct Data {
   int cls = -1;            /* 0 integer, 1 float, 3 string */
   bool is_signed = true;
@@ -91,7 +98,7 @@ struct Data {
   std::vector<uint8_t> raw;
   uint64_t count() const {
     uint64_t n = 1;
-    for (uint64_t d : dims) n *= d;
+    for (uint64_t d : dims) n = mul_checked(n, d);
     return n;
   }
 };
@@ -265,8 +272,8 @@ class H5 {
       }
     }
     if (out.cls < 0 || lclass < 0) h5fail(CF_EINVAL, "HDF5 dataset without type or layout");
-    const uint64_t n = out.count(), nbytes = n * out.size;
-    if (out.size == 0 || n > ((uint64_t)1 << 40) / out.size) h5fail(CF_EINVAL, "bad HDF5 dataset size");
+    if (out.size == 0) h5fail(CF_EINVAL, "bad HDF5 element size");
+    const uint64_t n = out.count(), nbytes = mul_checked(n, out.size);
     if (lclass == 0) {
       if (compact.size() < nbytes) h5fail(CF_EINVAL, "short HDF5 compact dataset");
       out.raw.assign(compact.begin(), compact.begin() + (size_t)nbytes);
@@ -314,7 +321,7 @@ class H5 {
       } else {
         if (fmask != 0) h5fail(CF_ENOTSUP, "filtered HDF5 chunks are not supported");
         uint64_t per = out.size;
-        for (size_t k = 0; k < rank; ++k) per *= cdims[k];
+        for (size_t k = 0; k < rank; ++k) per = mul_checked(per, cdims[k]);
         if (csize < per) h5fail(CF_EINVAL, "short HDF5 chunk");
         need(child, per);
         copy_chunk(&b_[child], offs, cdims, out);
@@ -330,7 +337,7 @@ class H5 {
     std::vector<uint64_t> idx(rank, 0);
     const uint64_t es = out.size;
     uint64_t total = 1;
-    for (size_t k = 0; k < rank; ++k) total *= cdims[k];
+    for (size_t k = 0; k < rank; ++k) total = mul_checked(total, cdims[k]);
     for (uint64_t e = 0; e < total; ++e) {
       uint64_t lin = 0;
       bool inside = true;
