@@ -15,6 +15,7 @@
  * Host code only; nothing here touches the GPU.
  */
 #include <cctype>
+#include <climits>
 #include <cerrno>
 #include <cmath>
 #include <cstdio>
@@ -22,8 +23,10 @@
 #include <cstring>
 #include <fstream>
 #include <map>
+#include <memory>
 #include <new>
 #include <sstream>
+#include <stdexcept>
 #include <string>
 #include <vector>
 
@@ -386,7 +389,7 @@ int read_mesh(const std::string& path, cf_case& C) {
   };
   int64_t v = 0;
   if (!r.skip_title()) return bad("missing the node table title");
-  if (!r.read(1, t) || !parse_int(t[0], v) || v < 1) return bad("bad node count");
+  if (!r.read(1, t) || !parse_int(t[0], v) || v < 1 || v > INT32_MAX) return bad("bad node count");
   const int64_t nnt = v;
   C.x.resize(nnt); C.y.resize(nnt); C.z.resize(nnt); C.manning_nd.resize(nnt);
   for (int64_t i = 0; i < nnt; ++i) {
@@ -396,7 +399,7 @@ int read_mesh(const std::string& path, cf_case& C) {
     C.x[i] = a; C.y[i] = b; C.z[i] = c; C.manning_nd[i] = d;
   }
   if (!r.skip_title()) return bad("missing the connectivity title");
-  if (!r.read(1, t) || !parse_int(t[0], v) || v < 1) return bad("bad element count");
+  if (!r.read(1, t) || !parse_int(t[0], v) || v < 1 || v > INT32_MAX / 3) return bad("bad element count");
   const int64_t nelt = v;
   C.tri.resize(3 * nelt);
   C.manning_elt.resize(nelt);
@@ -416,9 +419,10 @@ int read_mesh(const std::string& path, cf_case& C) {
     int64_t n = 0, nb = 0;
     const bool numbered = nbr != 1;   /* the namelist's count selects the layout */
     if (!numbered) {
-      if (!r.read(1, t) || !parse_int(t[0], n) || n < 0) return bad("bad inflow/outflow node count");
+      if (!r.read(1, t) || !parse_int(t[0], n) || n < 0 || n > INT32_MAX) return bad("bad inflow/outflow node count");
     } else {
-      if (!r.read(2, t) || !parse_int(t[0], n) || !parse_int(t[1], nb) || n < 0 || nb < 0 || nb > CF_MAX_IO)
+      if (!r.read(2, t) || !parse_int(t[0], n) || !parse_int(t[1], nb) || n < 0 || n > INT32_MAX || nb < 0 ||
+          nb > CF_MAX_IO)
         return bad("bad inflow/outflow counts");
       nbr = (int32_t)nb;
     }
@@ -438,7 +442,7 @@ int read_mesh(const std::string& path, cf_case& C) {
   if ((rc = io_table(C.mesh.nombre_entrees, C.ndinput, C.numero_ndinput))) return rc;
   if ((rc = io_table(C.mesh.nombre_sorties, C.ndoutput, C.numero_ndoutput))) return rc;
   if (!r.skip_title()) return bad("missing the wall title");
-  if (!r.read(1, t) || !parse_int(t[0], v) || v < 0) return bad("bad wall node count");
+  if (!r.read(1, t) || !parse_int(t[0], v) || v < 0 || v > INT32_MAX) return bad("bad wall node count");
   C.ndwall.resize(v);
   for (int64_t i = 0; i < v; ++i) {
     int64_t a;
@@ -516,7 +520,22 @@ void fill_mesh(cf_case& C) {
 
 extern "C" {
 
+static int case_read_impl(const char* dir, const char* namelist_file, cf_case** out);
+
 int cf_case_read(const char* dir, const char* namelist_file, cf_case** out) {
+  /* no C++ exception crosses the C ABI: a file whose counts outrun host memory is an error */
+  try {
+    return case_read_impl(dir, namelist_file, out);
+  } catch (const std::bad_alloc&) {
+    if (out) *out = nullptr;
+    return io_fail(CF_ENOMEM, "host allocation failed reading the case (counts in the files too large?)");
+  } catch (const std::length_error&) {
+    if (out) *out = nullptr;
+    return io_fail(CF_EINVAL, "counts in the case files too large");
+  }
+}
+
+static int case_read_impl(const char* dir, const char* namelist_file, cf_case** out) {
   if (!out) return io_fail(CF_EINVAL, "out is NULL");
   *out = nullptr;
   const std::string d = dir ? dir : ".";
@@ -525,7 +544,7 @@ int cf_case_read(const char* dir, const char* namelist_file, cf_case** out) {
   if (!f) return io_fail(CF_EINVAL, "cannot open the namelist file " + nml_path);
   std::stringstream ss;
   ss << f.rdbuf();
-  cf_case* C = new (std::nothrow) cf_case();
+  std::unique_ptr<cf_case> C(new (std::nothrow) cf_case());
   if (!C) return io_fail(CF_ENOMEM, "host allocation failed");
   cf_default_params(&C->params);
   C->params.friction = 0;          /* friction=0 is the namelist's initial value (global_data.cuf:31) */
@@ -544,11 +563,8 @@ int cf_case_read(const char* dir, const char* namelist_file, cf_case** out) {
   if (rc == CF_OK) fill_mesh(*C);
   if (rc == CF_OK && C->solinit == 1)
     rc = read_state_file(join_path(d, trim(C->fich_sol_init)), C->mesh.nelt, C->U0, C->tc_init);
-  if (rc != CF_OK) {
-    delete C;
-    return rc;
-  }
-  *out = C;
+  if (rc != CF_OK) return rc;
+  *out = C.release();
   return CF_OK;
 }
 

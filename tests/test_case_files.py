@@ -139,6 +139,11 @@ def test_mesh_errors(tmp_path):
     (tmp_path / "m.txt").write_text(MESH[:120])
     with pytest.raises(solver.CFError):
         case_files.read_case(str(tmp_path))
+    # a count beyond the mesh tables' int32 range is an error, not an allocation of it
+    (tmp_path / "m.txt").write_text(MESH.replace("Table des coordonnees\n4\n", "Table des coordonnees\n1000000000000\n", 1))
+    with pytest.raises(solver.CFError) as ei:
+        case_files.read_case(str(tmp_path))
+    assert "node count" in str(ei.value)
 
 
 def test_restart_file_layout(tmp_path):
