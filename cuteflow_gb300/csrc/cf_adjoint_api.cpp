@@ -396,14 +396,14 @@ int cf_set_manning(cf_ctx* c, const double* n_elt) {
 int cf_adjoint_create(cf_ctx* ctx, int32_t nsteps, int32_t checkpoint_interval, const int32_t* gauges,
                       int32_t ngauges, cf_adjoint** out) {
   if (!ctx) return CF_EINVAL;
-  return create_impl(ctx, nsteps, checkpoint_interval, nullptr, gauges, ngauges, out);
+  return abi_guard(ctx, [&] { return create_impl(ctx, nsteps, checkpoint_interval, nullptr, gauges, ngauges, out); });
 }
 
 int cf_adjoint_create_batch(cf_ctx* ctx, int32_t nsteps, int32_t checkpoint_interval, const int32_t* gauge_member,
                             const int32_t* gauges, int32_t ngauges, cf_adjoint** out) {
   if (!ctx) return CF_EINVAL;
   if (ngauges > 0 && !gauge_member) return fail(ctx, CF_EINVAL, "gauge_member is NULL");
-  return create_impl(ctx, nsteps, checkpoint_interval, gauge_member, gauges, ngauges, out);
+  return abi_guard(ctx, [&] { return create_impl(ctx, nsteps, checkpoint_interval, gauge_member, gauges, ngauges, out); });
 }
 
 void cf_adjoint_destroy(cf_adjoint* a) {
@@ -475,8 +475,14 @@ int cf_adjoint_sizes(cf_adjoint* a, int32_t* nsteps, int32_t* interval, int32_t*
 
 /* ---- Manning zones ------------------------------------------------------------------------ */
 
+static int zones_create_impl(cf_ctx* c, const int32_t* zone_of_elem, int32_t nzones, cf_zones** out);
+
 int cf_zones_create(cf_ctx* c, const int32_t* zone_of_elem, int32_t nzones, cf_zones** out) {
   if (!c) return CF_EINVAL;
+  return abi_guard(c, [&] { return zones_create_impl(c, zone_of_elem, nzones, out); });
+}
+
+static int zones_create_impl(cf_ctx* c, const int32_t* zone_of_elem, int32_t nzones, cf_zones** out) {
   if (!out || !zone_of_elem || nzones < 1) return fail(c, CF_EINVAL, "null argument or nzones < 1");
   *out = nullptr;
   CF_CUDA(c, cudaSetDevice(c->device));

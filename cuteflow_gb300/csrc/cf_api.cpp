@@ -833,11 +833,11 @@ int cf_default_params(cf_params* p) {
 }
 
 int cf_create(const cf_mesh* mesh, const cf_params* params, cf_ctx** out) {
-  return create_impl(mesh, params, 1, out);
+  return abi_guard(nullptr, [&] { return create_impl(mesh, params, 1, out); });
 }
 
 int cf_create_batch(const cf_mesh* meshes, const cf_params* params, int32_t nmembers, cf_ctx** out) {
-  return create_impl(meshes, params, nmembers, out);
+  return abi_guard(nullptr, [&] { return create_impl(meshes, params, nmembers, out); });
 }
 
 void cf_destroy(cf_ctx* c) {
@@ -862,10 +862,12 @@ int cf_member_set_state(cf_ctx* c, int32_t member, const double* hu3, double t0)
   return set_state_host(c, member, hu3, t0, cudaMemcpyHostToDevice);
 }
 
-int cf_set_initial_condition(cf_ctx* c, const cf_ic* ic, double t0) { return initial_condition(c, 0, ic, t0); }
+int cf_set_initial_condition(cf_ctx* c, const cf_ic* ic, double t0) {
+  return abi_guard(c, [&] { return initial_condition(c, 0, ic, t0); });
+}
 
 int cf_member_set_initial_condition(cf_ctx* c, int32_t member, const cf_ic* ic, double t0) {
-  return initial_condition(c, member, ic, t0);
+  return abi_guard(c, [&] { return initial_condition(c, member, ic, t0); });
 }
 
 int cf_step(cf_ctx* c, int32_t nsteps, cf_step_info* info) { return step_impl(c, nsteps, info); }
@@ -906,8 +908,16 @@ int cf_member_get_mesh_tables(cf_ctx* c, int32_t member, int32_t* boundary, doub
   return CF_OK;
 }
 
+static int mesh_tables_impl(const cf_mesh* mesh, const cf_params* params, int32_t* boundary, double* area,
+                            double* zm, double* cotemin);
+
 int cf_mesh_tables(const cf_mesh* mesh, const cf_params* params, int32_t* boundary, double* area, double* zm,
                    double* cotemin) {
+  return abi_guard(nullptr, [&] { return mesh_tables_impl(mesh, params, boundary, area, zm, cotemin); });
+}
+
+static int mesh_tables_impl(const cf_mesh* mesh, const cf_params* params, int32_t* boundary, double* area, double* zm,
+                            double* cotemin) {
   Prep P;
   std::string err;
   int rc = prepare_mesh(mesh, params, P, err);

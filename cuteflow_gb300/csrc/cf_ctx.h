@@ -11,6 +11,9 @@
 #include <string>
 #include <vector>
 
+#include <exception>
+#include <new>
+
 #include "cf_internal.h"
 
 namespace cf {
@@ -80,6 +83,20 @@ namespace cf {
 
 /* record msg as the context's last error (the create error when c is NULL), return code */
 int fail(cf_ctx* c, int code, const std::string& msg);
+
+/* Runs the body of a C ABI entry point: a C++ exception of the host preprocessing (an allocation
+ * beyond host memory for an enormous input) becomes an error code with a message, recorded on c (or
+ * as the creation error when c is NULL), instead of crossing the C ABI. */
+template <class F>
+int abi_guard(cf_ctx* c, F&& body) {
+  try {
+    return body();
+  } catch (const std::bad_alloc&) {
+    return fail(c, CF_ENOMEM, "host allocation failed (input too large for host memory?)");
+  } catch (const std::exception& e) {
+    return fail(c, CF_EINVAL, std::string("host error: ") + e.what());
+  }
+}
 int cuda_fail(cf_ctx* c, cudaError_t e, const char* what);
 
 #define CF_CUDA(c, call)                                     \
