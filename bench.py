@@ -8,8 +8,9 @@ for the reference's real-river meshes, which are not available).
 A step is one time step of the whole mesh.  `value` is device-timed throughput with the
 state resident in HBM (CUDA events on the solver's stream around K steps replayed from a
 CUDA graph); `e2e` times the same metric through the public C ABI with the state copied in
-from pinned host memory and read back every step.  The working set (~0.5 GB) is larger than
-L2, so no flush is needed between steps.
+from pinned host memory and read back every step (cf_advance; the three-call sequence
+cf_set_state + cf_step + cf_get_state is reported beside it).  The working set (~0.55 GB) is
+larger than L2, so no flush is needed between steps.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
@@ -463,12 +464,23 @@ def run_ours(args):
             raise SystemExit("C ABI call failed during the e2e loop")
     f1.record(stream)
     barrier()
+    three_ms = f0.elapsed_time(f1)
+    # the same per step through cf_advance: state in, one step, state out, one wait
+    lib.cf_advance(s._ctx, pin_in, 0.0, 1, pin_out, ctypes.byref(stepinfo))
+    barrier()
+    f0.record(stream)
+    for _ in range(e2e_steps):
+        if lib.cf_advance(s._ctx, pin_in, 0.0, 1, pin_out, ctypes.byref(stepinfo)):
+            raise SystemExit("C ABI call failed during the e2e loop")
+    f1.record(stream)
+    barrier()
     e2e_ms = f0.elapsed_time(f1)
     if pg is not None:
-        t = torch.tensor([e2e_ms], device="cuda", dtype=torch.float64)
+        t = torch.tensor([e2e_ms, three_ms], device="cuda", dtype=torch.float64)
         pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        e2e_ms = float(t.item())
+        e2e_ms, three_ms = float(t[0].item()), float(t[1].item())
     e2e_value = world * n * e2e_steps / (e2e_ms * 1e-3)
+    three_value = world * n * e2e_steps / (three_ms * 1e-3)
     # the host link's own rate for the same bytes (plain pinned copies, no kernels): the floor of
     # the end-to-end step's copy time
     dbuf = torch.empty(hin.numel(), dtype=torch.float64, device="cuda")
@@ -526,8 +538,10 @@ def run_ours(args):
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 24 * n, "d2h_bytes_per_step": 24 * n,
                 "steps": e2e_steps, "ms_per_step": e2e_ms / e2e_steps,
                 "link_h2d_gbs": 24 * n / (h2d_ms * 1e-3) / 1e9, "link_d2h_gbs": 24 * n / (d2h_ms * 1e-3) / 1e9,
-                "note": "per step: cf_set_state from pinned host memory, cf_step, cf_get_state into pinned "
-                        "host memory; link_*: plain pinned copies of the same bytes"},
+                "three_calls_value": three_value, "three_calls_ms_per_step": three_ms / e2e_steps,
+                "note": "per step: cf_advance (the state from pinned host memory, one step, the state back "
+                        "into pinned host memory, one wait); three_calls: the same as cf_set_state + "
+                        "cf_step + cf_get_state; link_*: plain pinned copies of the same bytes"},
         "gpu_launches": 2 * args.steps + 1,
         "clocks": clk.summary(),
     }

@@ -364,7 +364,8 @@ int member_ok(cf_ctx* c, int32_t m) {
 }
 
 /* Set the state of member m from c->staging (reference order), resetting its time and steps. */
-int set_state_member(cf_ctx* c, int32_t m, double t0) {
+/* the device work of setting member m's state from the staging buffer (stream-ordered, no wait) */
+int enqueue_set_state(cf_ctx* c, int32_t m, double t0) {
   const Member& M = c->mem[m];
   const int p0 = (int)(c->launched & 1);
   MemberState s;
@@ -383,6 +384,12 @@ int set_state_member(cf_ctx* c, int32_t m, double t0) {
   rc = launch_cfl(c->U[p0], c->cstat, c->ctile_mem, M.ctile_begin, M.ctile_end - M.ctile_begin, c->mdev, c->mst, p0,
                   reinterpret_cast<stream_t>(c->stream));
   if (rc != CF_OK) return fail(c, rc, "cfl launch failed");
+  return CF_OK;
+}
+
+int set_state_member(cf_ctx* c, int32_t m, double t0) {
+  const int rc = enqueue_set_state(c, m, t0);
+  if (rc != CF_OK) return rc;
   /* return once the host buffers are consumed; the scatter and the initial dt run on the stream
    * ahead of the next call's work (which every later call orders after) */
   CF_CUDA(c, cudaEventSynchronize(c->ev[3]));
@@ -455,8 +462,8 @@ int get_state_member(cf_ctx* c, int32_t m, double* dst, cudaMemcpyKind kind) {
   return CF_OK;
 }
 
-int step_impl(cf_ctx* c, int32_t nsteps, cf_step_info* infos) {
-  if (!c) return CF_EINVAL;
+/* the launches of nsteps steps and the discharge diagnostics (stream-ordered, no wait) */
+int enqueue_steps(cf_ctx* c, int32_t nsteps) {
   if (nsteps < 0) return fail(c, CF_EINVAL, "nsteps < 0");
   CF_CUDA(c, cudaSetDevice(c->device));
   int rc;
@@ -494,6 +501,12 @@ int step_impl(cf_ctx* c, int32_t nsteps, cf_step_info* infos) {
   c->launched += nsteps;
   rc = launch_discharge(c->slots, c->ecell, c->mdev, c->mst, (int32_t)c->mem.size(), reinterpret_cast<stream_t>(c->stream));
   if (rc != CF_OK) return fail(c, rc, "discharge launch failed");
+  return CF_OK;
+}
+
+/* wait for the stream, read the member records back and report them (info, status code) */
+int finish_steps(cf_ctx* c, cf_step_info* infos) {
+  int rc;
   if ((rc = read_states(c))) return rc;
   uint32_t any = 0;
   for (size_t i = 0; i < c->mem.size(); ++i) {
@@ -505,6 +518,13 @@ int step_impl(cf_ctx* c, int32_t nsteps, cf_step_info* infos) {
   if (rc != CF_OK)
     return fail(c, rc, rc == CF_EDT ? "dt left the range (1e-12, 9999]" : "non-finite value in the state");
   return CF_OK;
+}
+
+int step_impl(cf_ctx* c, int32_t nsteps, cf_step_info* infos) {
+  if (!c) return CF_EINVAL;
+  const int rc = enqueue_steps(c, nsteps);
+  if (rc != CF_OK) return rc;
+  return finish_steps(c, infos);
 }
 
 /* The reference's time loop until its end test on ts (finite_volumes_method.cuf:123), the
@@ -871,6 +891,34 @@ int cf_member_set_initial_condition(cf_ctx* c, int32_t member, const cf_ic* ic, 
 }
 
 int cf_step(cf_ctx* c, int32_t nsteps, cf_step_info* info) { return step_impl(c, nsteps, info); }
+
+int cf_advance(cf_ctx* c, const double* hu3_in, double t0, int32_t nsteps, double* hu3_out, cf_step_info* info) {
+  if (!c) return CF_EINVAL;
+  if (c->mem.size() != 1) return fail(c, CF_EINVAL, "cf_advance: a context with one member");
+  if (!hu3_in || !hu3_out) return fail(c, CF_EINVAL, "null state");
+  if (nsteps < 0) return fail(c, CF_EINVAL, "nsteps < 0");
+  CF_CUDA(c, cudaSetDevice(c->device));
+  const Member& M = c->mem[0];
+  const size_t bytes = 3 * (size_t)M.n * sizeof(double);
+  const stream_t st = reinterpret_cast<stream_t>(c->stream);
+  /* one stream-ordered sequence, one wait: state in, initial dt, the steps, the current state out
+   * (its buffer chosen on the device, so a member that stopped early returns where it stopped) */
+  CF_CUDA(c, cudaMemcpyAsync(c->staging, hu3_in, bytes, cudaMemcpyDefault, c->stream));
+  int rc = enqueue_set_state(c, 0, t0);
+  if (rc == CF_OK) rc = enqueue_steps(c, nsteps);
+  if (rc != CF_OK) {
+    cudaStreamSynchronize(c->stream);
+    return rc;
+  }
+  rc = launch_gather_current(c->U[0] + M.cell_off, c->U[1] + M.cell_off, c->mst, 0, c->iperm + M.cell_off, c->staging,
+                             M.n, st);
+  if (rc != CF_OK) {
+    cudaStreamSynchronize(c->stream);
+    return fail(c, rc, "gather launch failed");
+  }
+  CF_CUDA(c, cudaMemcpyAsync(hu3_out, c->staging, bytes, cudaMemcpyDefault, c->stream));
+  return finish_steps(c, info);
+}
 
 int cf_get_state(cf_ctx* c, double* hu3) { return get_state_member(c, 0, hu3, cudaMemcpyDeviceToHost); }
 

@@ -187,6 +187,9 @@ int launch_scatter_state(const double* hu3, const int32_t* perm_new2old, const d
                          double4* U, int32_t n, stream_t s);
 int launch_gather_state(const double4* U, const int32_t* iperm_old2new, double* hu3, int32_t n,
                         stream_t s);
+/* launch_gather_state out of member m's current buffer, chosen on the device from mst[m] */
+int launch_gather_current(const double4* U0, const double4* U1, const MemberState* mst, int32_t m,
+                          const int32_t* iperm, double* hu3, int32_t n, stream_t s);
 /* (h, hu, hv) of listed elements (member-local reference ids, iperm member-local) */
 int launch_gather_ids(const double4* U, const int32_t* iperm, const int32_t* ids, double* out, int32_t n, stream_t s);
 int launch_scatter_ids(double4* U, const int32_t* iperm, const int32_t* ids, const double* in, int32_t n, stream_t s);

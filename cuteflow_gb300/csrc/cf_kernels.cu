@@ -318,6 +318,20 @@ __global__ void k_gather(const double4* U, const int32_t* iperm, double* hu3, in
   hu3[3 * (size_t)o + 2] = u.z;
 }
 
+/* The same, out of the buffer that holds member m's current state, chosen on the device from its
+ * record (U[(base + nstep) & 1]): correct after steps whose count the host has not read back. */
+__global__ void k_gather_current(const double4* U0, const double4* U1, const MemberState* mst, int m,
+                                 const int32_t* iperm, double* hu3, int n) {
+  const int o = blockIdx.x * blockDim.x + threadIdx.x;
+  if (o >= n) return;
+  const MemberState& s = mst[m];
+  const double4* U = ((s.base + s.nstep) & 1) ? U1 : U0;
+  const double4 u = U[iperm[o]];
+  hu3[3 * (size_t)o] = u.x;
+  hu3[3 * (size_t)o + 1] = u.y;
+  hu3[3 * (size_t)o + 2] = u.z;
+}
+
 /* (h, hu, hv) of the listed elements (member-local reference ids) out of / into U */
 __global__ void k_gather_ids(const double4* U, const int32_t* iperm, const int32_t* ids, double* out, int n) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -407,6 +421,12 @@ int launch_gather_ids(const double4* U, const int32_t* iperm, const int32_t* ids
 int launch_scatter_ids(double4* U, const int32_t* iperm, const int32_t* ids, const double* in, int32_t n, stream_t s) {
   if (n <= 0) return CF_OK;
   k_scatter_ids<<<(n + 255) / 256, 256, 0, reinterpret_cast<cudaStream_t>(s)>>>(U, iperm, ids, in, n);
+  return check(cudaGetLastError());
+}
+
+int launch_gather_current(const double4* U0, const double4* U1, const MemberState* mst, int32_t m,
+                          const int32_t* iperm, double* hu3, int32_t n, stream_t s) {
+  k_gather_current<<<(n + 255) / 256, 256, 0, reinterpret_cast<cudaStream_t>(s)>>>(U0, U1, mst, m, iperm, hu3, n);
   return check(cudaGetLastError());
 }
 

@@ -57,6 +57,7 @@ def load(build_if_missing: bool = True):
     L.cf_run.argtypes = [vp, C.c_double, C.c_int64, C.POINTER(_abi.CfStepInfo)]
     L.cf_set_tuning.argtypes = [vp, C.c_int32, C.c_int32]
     L.cf_probe_fp64.argtypes = [vp, dp]
+    L.cf_advance.argtypes = [vp, dp, C.c_double, C.c_int32, dp, C.POINTER(_abi.CfStepInfo)]
     L.cf_get_elements.argtypes = [vp, C.c_int32, C.POINTER(C.c_int32), C.c_int32, dp]
     L.cf_set_elements.argtypes = [vp, C.c_int32, C.POINTER(C.c_int32), C.c_int32, dp]
     L.cf_set_dt.argtypes = [vp, C.c_int32, C.c_double]
@@ -115,7 +116,7 @@ def load(build_if_missing: bool = True):
                  "cf_set_initial_condition", "cf_step", "cf_step_noalloc", "cf_run", "cf_set_tuning",
                  "cf_get_tuning", "cf_autotune", "cf_get_elements", "cf_set_elements", "cf_set_dt", "cf_get_state", "cf_get_state_device",
                  "cf_get_info", "cf_get_mesh_tables", "cf_mesh_tables", "cf_get_sizes", "cf_set_timing", "cf_get_timing",
-                 "cf_probe_fp64"):
+                 "cf_probe_fp64", "cf_advance"):
         getattr(L, name).restype = C.c_int
     _lib = L
     return L
@@ -254,6 +255,19 @@ class Solver:
         a, b, t = C.c_int32(), C.c_int32(), C.c_double()
         self._check(self._L.cf_autotune(self._ctx, int(steps_per_trial), C.byref(a), C.byref(b), C.byref(t)))
         return a.value, b.value, t.value
+
+    def advance(self, U: np.ndarray, t0: float, nsteps: int, check: bool = True):
+        """cf_advance: the host state U (reference order, [nelt, 3]) at time t0 advanced by nsteps
+        steps in one call; returns (the new state, StepInfo)."""
+        src = np.ascontiguousarray(U, dtype=np.float64)
+        out = np.empty_like(src)
+        info = _abi.CfStepInfo()
+        dp = C.POINTER(C.c_double)
+        rc = self._L.cf_advance(self._ctx, src.ctypes.data_as(dp), float(t0), int(nsteps), out.ctypes.data_as(dp),
+                                C.byref(info))
+        if check:
+            self._check(rc)
+        return out, _info(info)
 
     def probe_fp64(self) -> float:
         """cf_probe_fp64: the FP64 pipe's throughput on this device, FP64 instructions per second."""

@@ -167,6 +167,13 @@ int cf_set_initial_condition(cf_ctx* ctx, const cf_ic* ic, double t0);
  * others do), CF_ESTATE for a plain context without a state. */
 int cf_step(cf_ctx* ctx, int32_t nsteps, cf_step_info* info);
 
+/* A host-held state advanced by nsteps steps in one call: cf_set_state(hu3_in, t0), cf_step(nsteps),
+ * cf_get_state(hu3_out), with the copies, the steps and the read-back in one stream-ordered sequence
+ * and a single wait (for a caller that keeps the state itself, e.g. a coupled model exchanging it
+ * every step).  hu3_in and hu3_out may be the same buffer.  Contexts with one member; the result
+ * and the return code are those of the three calls. */
+int cf_advance(cf_ctx* ctx, const double* hu3_in, double t0, int32_t nsteps, double* hu3_out, cf_step_info* info);
+
 /* The reference's time loop (solve_finite_volumes, finite_volumes_method.cuf:123-242): steps
  * every member until the loop test (tc - ts + 2 tol) < tol fails (tol = 1e-6 in single
  * precision, tc = the state's t0 plus the dt computed after every step, :232), the

@@ -5,6 +5,8 @@ the stated step count.  The kernels evaluate the reference's operations in its o
 FMA contraction, so the tests require more: the GPU state, every dt and the time must equal
 the oracle's bit for bit (TOL is only reported in the failure message).
 """
+import ctypes as C
+
 import numpy as np
 import pytest
 
@@ -93,6 +95,36 @@ def test_explicit_friction_stops_like_the_reference(gpu_lib, oracle):
             s.step(1)
     assert np.array_equal(U, ref["U"])
     assert info.t == ref["t"]
+
+
+def test_advance_chained_is_the_continuous_run(gpu_lib, oracle):
+    """cf_advance (state in, steps, state out, one wait), chained as a coupling host would chain it
+    (each call from the returned state at the returned time, in place or not): the continuous run,
+    bit for bit."""
+    from cuteflow_gb300 import Solver
+    c = cases.flooding(60, 30, seed=8, iflux=3)
+    ref = oracle.run(c, 30)
+    with Solver(c) as s:
+        U, t = np.array(c.U0), 0.0
+        for k in (7, 0, 13, 10):
+            U, info = s.advance(U, t, k)
+            t = info.t
+        assert np.array_equal(U, ref["U"]) and t == ref["t"] and info.steps == 10
+
+
+def test_advance_returns_a_stopped_state_like_the_three_calls(gpu_lib, oracle):
+    """A member that stops inside cf_advance (the reference's dt-range test) returns the state where
+    it stopped and the same code as cf_set_state + cf_step + cf_get_state: the state's buffer is
+    chosen on the device."""
+    from cuteflow_gb300 import Solver
+    c = cases.flooding(40, 20, seed=8, iflux=1)
+    ref = oracle.run(c, 120, params=dict(fricimplic=0), check=False)
+    with Solver(c, dict(fricimplic=0)) as s:
+        U, info = s.advance(c.U0, 0.0, 120, check=False)
+        rc = s._L.cf_advance(s._ctx, np.ascontiguousarray(c.U0).ctypes.data_as(C.POINTER(C.c_double)), 0.0, 120,
+                             np.empty_like(c.U0).ctypes.data_as(C.POINTER(C.c_double)), None)
+    assert rc == _abi.CF_EDT and info.status & _abi.CF_STATUS_DT_RANGE
+    assert np.array_equal(U, ref["U"]) and info.t == ref["t"]
 
 
 @pytest.mark.parametrize("iflux", [3, 4])
