@@ -348,6 +348,20 @@ CF_HD CF_INLINE T waf_limiter(int ilim, T r, T c) {
 template <class T>
 CF_HD CF_INLINE double sgn1(const T& x) { return copysign(1.0, val(x)); }
 
+/* sgn1(x) * y, the reference's dsign(1.d0, x) * y: for every y that is not NaN the IEEE product
+ * of +-1 and y is y with the sign of x multiplied in, a sign-bit flip (no FP64 instruction). */
+CF_HD CF_INLINE double sgnmul(double x, double y) {
+  uint64_t bx, by;
+  memcpy(&bx, &x, sizeof(bx));
+  memcpy(&by, &y, sizeof(by));
+  by ^= bx & 0x8000000000000000ull;
+  double r;
+  memcpy(&r, &by, sizeof(r));
+  return r;
+}
+template <class T>
+CF_HD CF_INLINE T sgnmul(const T& x, const T& y) { return sgn1(x) * y; }
+
 /* x, or (freeze) its value taken as a constant of the linearization; the same number either way. */
 template <class T>
 CF_HD CF_INLINE T held(const T& x, bool freeze) { return freeze ? T(val(x)) : x; }
@@ -402,11 +416,11 @@ CF_HD CF_INLINE void waf_flux(double g, int ilim, double nx, double ny, double d
     const T ll = waf_limiter(ilim, rl, cl);
     const T lr = waf_limiter(ilim, rr, cr);
     const T le = waf_limiter(ilim, ret_a, cet);
-    const T wl = (1. + sgn1(sl) * ll) / 2.;
-    const T wlet = (1. + sgn1(set) * le) / 2.;
-    const T wlr = (sgn1(sr) * lr - sgn1(sl) * ll) / 2.;
-    const T wr = (1. - sgn1(sr) * lr) / 2.;
-    const T wret = (1. - sgn1(set) * le) / 2.;
+    const T wl = (1. + sgnmul(sl, ll)) / 2.;
+    const T wlet = (1. + sgnmul(set, le)) / 2.;
+    const T wlr = (sgnmul(sr, lr) - sgnmul(sl, ll)) / 2.;
+    const T wr = (1. - sgnmul(sr, lr)) / 2.;
+    const T wret = (1. - sgnmul(set, le)) / 2.;
     const T fw1 = wl * fl1 + wlr * ha1 + wr * fr1;
     const T fw2 = wl * fl2 + wlr * ha2 + wr * fr2;
     const T fw3 = (wlet * vl + wret * vr) * fw1;
@@ -426,11 +440,11 @@ CF_HD CF_INLINE void waf_flux(double g, int ilim, double nx, double ny, double d
     const T ll = waf_limiter(ilim, rl, -cr);
     const T lr = waf_limiter(ilim, rr, -cl);
     const T le = waf_limiter(ilim, ret_b, -cet);
-    const T wl = (1. + sgn1(-sr) * ll) / 2.;
-    const T wlet = (1. + sgn1(-set) * le) / 2.;
-    const T wlr = (sgn1(-sl) * lr - sgn1(-sr) * ll) / 2.;
-    const T wr = (1. - sgn1(-sl) * lr) / 2.;
-    const T wret = (1. - sgn1(-set) * le) / 2.;
+    const T wl = (1. + sgnmul(-sr, ll)) / 2.;
+    const T wlet = (1. + sgnmul(-set, le)) / 2.;
+    const T wlr = (sgnmul(-sl, lr) - sgnmul(-sr, ll)) / 2.;
+    const T wr = (1. - sgnmul(-sl, lr)) / 2.;
+    const T wret = (1. - sgnmul(-set, le)) / 2.;
     /* mirrored physical fluxes: FL' = (-fr1, fr2), FR' = (-fl1, fl2), HLL' = (-hb1, hb2) */
     const T fw1 = -(wl * fr1 + wlr * hb1 + wr * fl1);
     const T fw2 = wl * fr2 + wlr * hb2 + wr * fl2;

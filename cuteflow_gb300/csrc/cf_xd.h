@@ -142,6 +142,9 @@ CF_XD_CMP(!=, !xeq(x, y))
 template <bool MUL> XD_HD XD<MUL> sqrt(const XD<MUL>& a) { return XD<MUL>(::sqrt(a.v)); }
 template <bool MUL> XD_HD XD<MUL> rcbrt(const XD<MUL>& a) { return XD<MUL>(rcbrt(a.v)); }
 template <bool MUL> XD_HD XD<MUL> fabs(const XD<MUL>& a) { return XD<MUL>(xdbl(xbits(a.v) & 0x7fffffffffffffffull)); }
+template <bool MUL> XD_HD XD<MUL> sgnmul(const XD<MUL>& x, const XD<MUL>& y) {
+  return XD<MUL>(xdbl(xbits(y.v) ^ (xbits(x.v) & 0x8000000000000000ull)));
+}
 
 /* Markstein's quotient (div_rn in cf_flux.h) with the product on the chosen path */
 template <bool MUL>
