@@ -89,7 +89,9 @@ __global__ void __launch_bounds__(TILE_C) k_rep_cells(StepArgs a, const double* 
   const int4 sl = __ldg(a.cslot + c);
   const Slot s0 = load_slot_adj(a.slots + sl.x), s1 = load_slot_adj(a.slots + sl.y), s2 = load_slot_adj(a.slots + sl.z);
   bool nonfinite = false;
-  const double4 V = element_update(M, U, st, s0, s1, s2, dt, nonfinite);
+  const double4 V = (a.xd_cmp && (a.xd_mul_mask & XD_CELLS))
+                        ? element_update<XD<true>>(M, U, st, s0, s1, s2, dt, nonfinite)
+                        : element_update(M, U, st, s0, s1, s2, dt, nonfinite);
   if (nonfinite) atomicOr(flag, CF_STATUS_NONFINITE);
   if (a.Uout) {
     double4* o = a.Uout + c;

@@ -634,8 +634,8 @@ int cf_run(cf_ctx* ctx, double ts, int64_t max_steps, cf_step_info* info) {
 
 int cf_set_tuning(cf_ctx* ctx, int32_t int_compare, int32_t int_mul_warps) {
   if (!ctx) return CF_EINVAL;
-  if (int_compare < 0 || int_compare > 1 || int_mul_warps < 0 || int_mul_warps > 0xf)
-    return fail(ctx, CF_EINVAL, "int_compare must be 0/1 and int_mul_warps a 4-bit warp mask");
+  if (int_compare < 0 || int_compare > 1 || int_mul_warps < 0 || int_mul_warps > 0x1f)
+    return fail(ctx, CF_EINVAL, "int_compare must be 0/1 and int_mul_warps a 4-bit warp mask plus bit 4");
   if (int_mul_warps && !int_compare) return fail(ctx, CF_EINVAL, "integer products need int_compare = 1");
   if (ctx->xd_cmp != int_compare || ctx->xd_mul_mask != int_mul_warps) {
     ctx->xd_cmp = int_compare;
@@ -679,6 +679,27 @@ int cf_probe_fp64(cf_ctx* ctx, double* instr_per_s) {
   return CF_OK;
 }
 
+int cf_selftest_xd(cf_ctx* ctx, int64_t n, uint64_t seed, int64_t* mismatches) {
+  if (!ctx || !mismatches || n < 0) return CF_EINVAL;
+  cf_ctx* c = ctx;
+  CF_CUDA(c, cudaSetDevice(c->device));
+  int sms = 0;
+  CF_CUDA(c, cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device));
+  unsigned long long* bad = nullptr;
+  int rc = dalloc(c, &bad, 1);
+  if (rc) return rc;
+  unsigned long long h = 0;
+  cudaError_t err = cudaMemsetAsync(bad, 0, sizeof(*bad), c->stream);
+  if (err == cudaSuccess) rc = launch_selftest_xd(n, seed, bad, 4 * sms, reinterpret_cast<stream_t>(c->stream));
+  if (err == cudaSuccess && rc == CF_OK) err = cudaMemcpyAsync(&h, bad, sizeof(h), cudaMemcpyDeviceToHost, c->stream);
+  if (err == cudaSuccess && rc == CF_OK) err = cudaStreamSynchronize(c->stream);
+  cudaFree(bad);
+  if (err != cudaSuccess) return cuda_fail(c, err, "cf_selftest_xd");
+  if (rc != CF_OK) return fail(c, rc, "cf_selftest_xd launch failed");
+  *mismatches = (int64_t)h;
+  return CF_OK;
+}
+
 int cf_get_tuning(cf_ctx* ctx, int32_t* int_compare, int32_t* int_mul_warps) {
   if (!ctx) return CF_EINVAL;
   if (int_compare) *int_compare = ctx->xd_cmp;
@@ -717,9 +738,9 @@ int cf_autotune(cf_ctx* ctx, int32_t steps_per_trial, int32_t* int_compare, int3
     cudaFree(saved);
     return cuda_fail(c, e, "cudaMemcpyAsync");
   }
-  /* candidates: all on the FP64 pipe; comparisons on the integer pipes; comparisons and all
-   * products; comparisons and the products of half the warps */
-  const int32_t cand[4][2] = {{0, 0}, {1, 0}, {1, 0xf}, {1, 0x5}};
+  /* candidates: all on the FP64 pipe; comparisons on the integer pipes; comparisons and the
+   * arithmetic of all edge warps, of half of them, and of all edge warps and the elements */
+  const int32_t cand[5][2] = {{0, 0}, {1, 0}, {1, 0xf}, {1, 0x5}, {1, 0x1f}};
   double best = 1e300;
   int32_t bc = 0, bm = 0;
   rc = CF_OK;

@@ -84,6 +84,16 @@ CF_HD CF_INLINE T dmax(const T& a, const T& b) { return (a < b) ? b : a; } /* Fo
 template <class T>
 CF_HD CF_INLINE T dmin(const T& a, const T& b) { return (b < a) ? b : a; } /* Fortran min */
 
+/* x / 2, x / 4 and 2 x.  A scaling by a power of two rounds once whichever way it is written, so
+ * these give the bits of the quotient or product they stand for; the integer-product type (cf_xd.h)
+ * overloads them with an exponent change. */
+template <class T>
+CF_HD CF_INLINE T halve(const T& x) { return x * 0.5; }
+template <class T>
+CF_HD CF_INLINE T quarter(const T& x) { return x * 0.25; }
+template <class T>
+CF_HD CF_INLINE T twice(const T& x) { return x * 2.0; }
+
 /* a / d rounded to nearest, given y = RN(1/d): q = RN(a y), r = a - d q (exact through the
  * FMA), RN(q + r y) (Markstein's correction step; P. Markstein, "Computation of elementary
  * functions on the IBM RISC System/6000 processor", IBM J. Res. Dev. 34, 1990).  It equals the
@@ -216,26 +226,26 @@ CF_HD CF_INLINE bool wave_speeds(double g, double eps, T hl, T ul, T hr, T ur, T
   if (hl < eps && hr < eps) return false;
   const T al = sqrt(g * hl);
   const T ar = sqrt(g * hr);
-  const T het = (hl + hr) / 2. - (ur - ul) * (hl + hr) / (al + ar) / 4.;
+  const T het = halve(hl + hr) - quarter((ur - ul) * (hl + hr) / (al + ar));
   T pql, pqr;
   if (het < hl) pql = T(1.);
-  else pql = (hl > eps) ? sqrt(0.5 * (het + hl) * het / (hl * hl)) : T(0.);
+  else pql = (hl > eps) ? sqrt(halve(het + hl) * het / (hl * hl)) : T(0.);
   if (het < hr) pqr = T(1.);
-  else pqr = (hr > eps) ? sqrt(0.5 * (het + hr) * het / (hr * hr)) : T(0.);
+  else pqr = (hr > eps) ? sqrt(halve(het + hr) * het / (hr * hr)) : T(0.);
   if (hl > eps) {
     sl = ul - al * pql;
     if (hr > eps) {
       sr = ur + ar * pqr;
     } else {
       sl = ul - al;
-      sr = ul + 2 * al;
+      sr = ul + twice(al);
     }
   } else {
-    sl = ur - 2 * ar;
+    sl = ur - twice(ar);
     sr = ur + ar;
   }
   const T denom = hr * (ur - sr) - hl * (ul - sl);
-  if (fabs(denom) < eps) set = (ul + ur) / 2. - (hr - hl) * (al + ar) / (hl + hr);
+  if (fabs(denom) < eps) set = halve(ul + ur) - (hr - hl) * (al + ar) / (hl + hr);
   else set = (sl * hr * (ur - sr) - sr * hl * (ul - sl)) / denom;
   return true;
 }
@@ -273,8 +283,8 @@ CF_HD CF_INLINE void first_order_flux(double g, double nx, double ny, T hl, T ul
     F.a1 = F.a2 = F.a3 = F.b1 = F.b2 = F.b3 = T(0.0);
     return;
   }
-  const T fl1 = hl * ul, fl2 = hl * (ul * ul) + g * hl * hl / 2.0, fl3 = hl * ul * vl;
-  const T fr1 = hr * ur, fr2 = hr * (ur * ur) + g * hr * hr / 2.0, fr3 = hr * ur * vr;
+  const T fl1 = hl * ul, fl2 = hl * (ul * ul) + halve(g * hl * hl), fl3 = hl * ul * vl;
+  const T fr1 = hr * ur, fr2 = hr * (ur * ur) + halve(g * hr * hr), fr3 = hr * ur * vr;
   T x1, x2, x3, y1, y2, y3;
   if (IFLUX == 1) {
     /* A: sl > 0 -> FL | sr < 0 -> FR | HLL with the tangential component of the upwind side
@@ -327,13 +337,13 @@ CF_HD CF_INLINE T waf_limiter(int ilim, T r, T c) {
   T A = T(1.);
   if (ilim == 1) {
     if (r <= 0.) A = T(1.);
-    else if (r > 0. && r < 0.5) A = 1. - 2. * (1. - fabs(c)) * r;
+    else if (r > 0. && r < 0.5) A = 1. - twice(1. - fabs(c)) * r;
     else if (r > 0.5 && r < 1.) A = fabs(c);
     else if (r > 1. && r < 2.) A = 1. - (1. - fabs(c)) * r;
-    else A = 2. * fabs(c) - 1.;
+    else A = twice(fabs(c)) - 1.;
   } else if (ilim == 2) {
     if (r <= 0.) A = T(1.);
-    else A = 1. - 2. * (1. - fabs(c)) * r / (1. + r);
+    else A = 1. - twice(1. - fabs(c)) * r / (1. + r);
   } else if (ilim == 3) {
     if (r <= 0.) A = T(1.);
     else A = 1. - (1. - fabs(c)) * r * (1. + r) / (1. + r * r);
@@ -383,8 +393,8 @@ CF_HD CF_INLINE void waf_flux(double g, int ilim, double nx, double ny, double d
     F.a1 = F.a2 = F.a3 = F.b1 = F.b2 = F.b3 = T(0.0);
     return;
   }
-  const T fl1 = hl * ul, fl2 = hl * (ul * ul) + g * hl * hl / 2.0;
-  const T fr1 = hr * ur, fr2 = hr * (ur * ur) + g * hr * hr / 2.0;
+  const T fl1 = hl * ul, fl2 = hl * (ul * ul) + halve(g * hl * hl);
+  const T fr1 = hr * ur, fr2 = hr * (ur * ur) + halve(g * hr * hr);
   const int ra = (sl > 0.) ? 0 : ((sr < 0.) ? 1 : 2);
   const int rb = (-sr > 0.) ? 1 : ((-sl < 0.) ? 0 : 2);
   T h1 = T(0.0), h2 = T(0.0);
@@ -416,11 +426,11 @@ CF_HD CF_INLINE void waf_flux(double g, int ilim, double nx, double ny, double d
     const T ll = waf_limiter(ilim, rl, cl);
     const T lr = waf_limiter(ilim, rr, cr);
     const T le = waf_limiter(ilim, ret_a, cet);
-    const T wl = (1. + sgnmul(sl, ll)) / 2.;
-    const T wlet = (1. + sgnmul(set, le)) / 2.;
-    const T wlr = (sgnmul(sr, lr) - sgnmul(sl, ll)) / 2.;
-    const T wr = (1. - sgnmul(sr, lr)) / 2.;
-    const T wret = (1. - sgnmul(set, le)) / 2.;
+    const T wl = halve(1. + sgnmul(sl, ll));
+    const T wlet = halve(1. + sgnmul(set, le));
+    const T wlr = halve(sgnmul(sr, lr) - sgnmul(sl, ll));
+    const T wr = halve(1. - sgnmul(sr, lr));
+    const T wret = halve(1. - sgnmul(set, le));
     const T fw1 = wl * fl1 + wlr * ha1 + wr * fr1;
     const T fw2 = wl * fl2 + wlr * ha2 + wr * fr2;
     const T fw3 = (wlet * vl + wret * vr) * fw1;
@@ -440,11 +450,11 @@ CF_HD CF_INLINE void waf_flux(double g, int ilim, double nx, double ny, double d
     const T ll = waf_limiter(ilim, rl, -cr);
     const T lr = waf_limiter(ilim, rr, -cl);
     const T le = waf_limiter(ilim, ret_b, -cet);
-    const T wl = (1. + sgnmul(-sr, ll)) / 2.;
-    const T wlet = (1. + sgnmul(-set, le)) / 2.;
-    const T wlr = (sgnmul(-sl, lr) - sgnmul(-sr, ll)) / 2.;
-    const T wr = (1. - sgnmul(-sl, lr)) / 2.;
-    const T wret = (1. - sgnmul(-set, le)) / 2.;
+    const T wl = halve(1. + sgnmul(-sr, ll));
+    const T wlet = halve(1. + sgnmul(-set, le));
+    const T wlr = halve(sgnmul(-sl, lr) - sgnmul(-sr, ll));
+    const T wr = halve(1. - sgnmul(-sl, lr));
+    const T wret = halve(1. - sgnmul(-set, le));
     /* mirrored physical fluxes: FL' = (-fr1, fr2), FR' = (-fl1, fl2), HLL' = (-hb1, hb2) */
     const T fw1 = -(wl * fr1 + wlr * hb1 + wr * fl1);
     const T fw2 = wl * fr2 + wlr * hb2 + wr * fl2;
@@ -464,8 +474,8 @@ CF_HD CF_INLINE void waf_flux(double g, int ilim, double nx, double ny, double d
 template <class T>
 CF_HD CF_INLINE T simple_limiter(int ilim, T r1, T r2) {
   if (ilim == 1) {
-    if (r2 > 0.) return dmax(T(0.), dmax(dmin(2. * r1, r2), dmin(r1, 2. * r2)));
-    return dmin(T(0.), dmin(dmax(2. * r1, r2), dmax(r1, 2. * r2)));
+    if (r2 > 0.) return dmax(T(0.), dmax(dmin(twice(r1), r2), dmin(r1, twice(r2))));
+    return dmin(T(0.), dmin(dmax(twice(r1), r2), dmax(r1, twice(r2))));
   }
   if (ilim == 2) return (r1 * r2 + fabs(r1 * r2)) / (r1 + r2 + EPS_VLEER);
   if (ilim == 3) {
@@ -492,32 +502,32 @@ CF_HD CF_INLINE void muscl_side(double g, double tolisec, int ilim, double dtove
   const T dloc2 = div_rn(ur - ul, d_mrl, y_mrl);
   const T dloc3 = div_rn(vr - vl, d_mrl, y_mrl);
   const T dhl = simple_limiter(ilim, div_rn(hl - hl_upw, d_up_l, y_up_l), dloc1);
-  const T hll = dmax(T(0.), hl - 0.5 * dhl * d_mrl);
-  const T hlr = dmax(T(0.), hl + 0.5 * dhl * d_mrl);
+  const T hll = dmax(T(0.), hl - halve(dhl) * d_mrl);
+  const T hlr = dmax(T(0.), hl + halve(dhl) * d_mrl);
   T ull, vll, ulr, vlr;
   if (hlr < tolisec || hll < tolisec) {
     ulr = vlr = ull = vll = T(0.);
   } else {
     const T dul = simple_limiter(ilim, div_rn(ul - ul_upw, d_up_l, y_up_l), dloc2);
     const T dvl = simple_limiter(ilim, div_rn(vl - vl_upw, d_up_l, y_up_l), dloc3);
-    ull = ul - 0.5 * dul * d_mrl;
-    vll = vl - 0.5 * dvl * d_mrl;
-    ulr = ul + 0.5 * dul * d_mrl;
-    vlr = vl + 0.5 * dvl * d_mrl;
+    ull = ul - halve(dul) * d_mrl;
+    vll = vl - halve(dvl) * d_mrl;
+    ulr = ul + halve(dul) * d_mrl;
+    vlr = vl + halve(dvl) * d_mrl;
   }
   const T dhr = simple_limiter(ilim, dloc1, div_rn(hr_upw - hr, d_up_r, y_up_r));
-  const T hrr = dmax(T(0.), hr + 0.5 * dhr * d_mrl);
-  const T hrl = dmax(T(0.), hr - 0.5 * dhr * d_mrl);
+  const T hrr = dmax(T(0.), hr + halve(dhr) * d_mrl);
+  const T hrl = dmax(T(0.), hr - halve(dhr) * d_mrl);
   T url, vrl, urr, vrr;
   if (hrl < tolisec || hrr < tolisec) {
     url = vrl = urr = vrr = T(0.);
   } else {
     const T dur = simple_limiter(ilim, dloc2, div_rn(ur_upw - ur, d_up_r, y_up_r));
     const T dvr = simple_limiter(ilim, dloc3, div_rn(vr_upw - vr, d_up_r, y_up_r));
-    urr = ur + 0.5 * dur * d_mrl;
-    vrr = vr + 0.5 * dvr * d_mrl;
-    url = ur - 0.5 * dur * d_mrl;
-    vrl = vr - 0.5 * dvr * d_mrl;
+    urr = ur + halve(dur) * d_mrl;
+    vrr = vr + halve(dvr) * d_mrl;
+    url = ur - halve(dur) * d_mrl;
+    vrl = vr - halve(dvr) * d_mrl;
   }
   /* data reconstruction II (:615-621) */
   const T h1 = hlr + 0.5 * dtoverdx * (hll * ull - hlr * ulr);
@@ -536,15 +546,15 @@ CF_HD CF_INLINE void muscl_side(double g, double tolisec, int ilim, double dtove
   }
   if (sl > 0.) {
     x1 = h1 * u1;
-    x2 = h1 * (u1 * u1) + g * h1 * h1 / 2.0;
+    x2 = h1 * (u1 * u1) + halve(g * h1 * h1);
     x3 = h1 * u1 * v1;
   } else if (sr < 0.) {
     x1 = h2 * u2;
-    x2 = h2 * (u2 * u2) + g * h2 * h2 / 2.0;
+    x2 = h2 * (u2 * u2) + halve(g * h2 * h2);
     x3 = h2 * u2 * v2;
   } else {
-    const T fl1 = h1 * u1, fl2 = h1 * (u1 * u1) + g * h1 * h1 / 2.0;
-    const T fr1 = h2 * u2, fr2 = h2 * (u2 * u2) + g * h2 * h2 / 2.0;
+    const T fl1 = h1 * u1, fl2 = h1 * (u1 * u1) + halve(g * h1 * h1);
+    const T fr1 = h2 * u2, fr2 = h2 * (u2 * u2) + halve(g * h2 * h2);
     const T den = sr - sl + eps, yden = 1.0 / den;
     x1 = div_rn(sr * fl1 - sl * fr1 + sl * sr * (h2 - h1), den, yden);
     x2 = div_rn(sr * fl2 - sl * fr2 + sl * sr * (h2 * u2 - h1 * u1), den, yden);
@@ -576,37 +586,37 @@ CF_HD CF_INLINE void boundary_flux(int iflux, const MemberDev& M, int kind, int 
   if (kind == -1) {
     if (M.inlet == 1) {
       f1 = hautl * vitul;
-      f2 = nx * (hautl * (vitul * vitul) + g * (hautl * hautl) / 2.) - ny * hautl * vitul * vitvl;
-      f3 = ny * (hautl * (vitul * vitul) + g * (hautl * hautl) / 2.) + nx * hautl * vitul * vitvl;
+      f2 = nx * (hautl * (vitul * vitul) + halve(g * (hautl * hautl))) - ny * hautl * vitul * vitvl;
+      f3 = ny * (hautl * (vitul * vitul) + halve(g * (hautl * hautl))) + nx * hautl * vitul * vitvl;
     } else if (M.inlet == 2) {
       const double debitnorm = -inlet_discharge(M, id, t) / M.long_entree[id - 1];
       f1 = T(debitnorm);
-      f2 = nx * ((debitnorm * debitnorm) / (hautl + tolisec) + g * (hautl * hautl) / 2.);
-      f3 = ny * ((debitnorm * debitnorm) / (hautl + tolisec) + g * (hautl * hautl) / 2.);
+      f2 = nx * ((debitnorm * debitnorm) / (hautl + tolisec) + halve(g * (hautl * hautl)));
+      f3 = ny * ((debitnorm * debitnorm) / (hautl + tolisec) + halve(g * (hautl * hautl)));
       q = T(-debitnorm);
     } else if (M.inlet == 3) {
       /* the inlet's discharge shared in proportion to depth (:127-138); the threshold is the
        * single-precision literal 1e-8 */
       const T debitnorm = (surf > (double)1e-8f) ? -(inlet_discharge(M, id, t) * hautl / surf) : T(0.0);
       f1 = debitnorm;
-      f2 = nx * ((debitnorm * debitnorm) / (hautl + tolisec) + g * (hautl * hautl) / 2.);
-      f3 = ny * ((debitnorm * debitnorm) / (hautl + tolisec) + g * (hautl * hautl) / 2.);
+      f2 = nx * ((debitnorm * debitnorm) / (hautl + tolisec) + halve(g * (hautl * hautl)));
+      f3 = ny * ((debitnorm * debitnorm) / (hautl + tolisec) + halve(g * (hautl * hautl)));
       q = -debitnorm;
     }
   } else if (kind == -3) {
-    f2 = nx * g * (hautl * hautl) / 2.;
-    f3 = ny * g * (hautl * hautl) / 2.;
+    f2 = halve(nx * g * (hautl * hautl));
+    f3 = halve(ny * g * (hautl * hautl));
   } else if (kind == -2) {
     if (M.outlet == 1) {
       if (vitul >= 0. && vitul / sqrt(g * hautl) < 1.0) {
         double ho = M.h_sortie[id - 1] - z;
         ho = dmax(0.0, ho);
         f1 = ho * vitul;
-        f2 = nx * (ho * (vitul * vitul) + g * (ho * ho) / 2.) - ny * ho * vitul * vitvl;
-        f3 = ny * (ho * (vitul * vitul) + g * (ho * ho) / 2.) + nx * ho * vitul * vitvl;
+        f2 = nx * (ho * (vitul * vitul) + halve(g * (ho * ho))) - ny * ho * vitul * vitvl;
+        f3 = ny * (ho * (vitul * vitul) + halve(g * (ho * ho))) + nx * ho * vitul * vitvl;
       } else {
-        f2 = nx * g * (hautl * hautl) / 2.;
-        f3 = ny * g * (hautl * hautl) / 2.;
+        f2 = halve(nx * g * (hautl * hautl));
+        f3 = halve(ny * g * (hautl * hautl));
       }
       q = f1;
     } else {
@@ -977,11 +987,11 @@ CF_HD CF_INLINE void friction_terms(const MemberDev& M, double area, double dt, 
         const T yn = 1.0 / normvit;
         const T dtgn2h = dt / 2.0 * gp * manning * manning * p43;
         const T af21 = -(7.0 / 3.0 * dtgn2h * vitu * normvit);
-        const T af22 = 1.0 + div_rn(dtgn2h * (2. * (vitu * vitu) + vitv * vitv), normvit, yn);
+        const T af22 = 1.0 + div_rn(dtgn2h * (twice(vitu * vitu) + vitv * vitv), normvit, yn);
         const T af23 = div_rn(dtgn2h * vitu * vitv, normvit, yn);
         const T af31 = -(7.0 / 3.0 * dtgn2h * vitv * normvit);
         const T af32 = af23;
-        const T af33 = 1.0 + div_rn(dtgn2h * (vitu * vitu + 2. * (vitv * vitv)), normvit, yn);
+        const T af33 = 1.0 + div_rn(dtgn2h * (vitu * vitu + twice(vitv * vitv)), normvit, yn);
         const T detaf = af22 * af33 - af23 * af32;
         const T yd = 1.0 / detaf;
         m[0] = div_rn(-(af21 * af33 - af23 * af31), detaf, yd);
@@ -1056,7 +1066,7 @@ CF_HD CF_INLINE double4 element_update(const MemberDev& M, const double4 U, cons
                hv, nonfinite, U.w);
   /* the new state carries RN(1/h) for the next step's quotients by h */
   const double hn = val(h);
-  return make_double4(hn, val(hu), val(hv), hn > 0.0 ? 1.0 / hn : 0.0);
+  return make_double4(hn, val(hu), val(hv), hn > 0.0 ? val(S(1.0) / h) : 0.0);
 }
 
 }  // namespace cf

@@ -39,6 +39,7 @@ namespace cf {
 
 constexpr int TILE_E = 128;  /* edges per tile (= edge-kernel block) */
 constexpr int TILE_C = 256;  /* cells per tile (= cell-kernel block) */
+constexpr int32_t XD_CELLS = 0x10;  /* tuning-mask bit of the element kernel */
 
 /* Fortran default-real literals of the reference, rounded to single precision. */
 constexpr double EPS_HLLC = (double)1e-8f;    /* flux_riemann.cuf:926 */
@@ -120,8 +121,9 @@ struct StepArgs {
   int32_t phys_inflow;       /* some member uses inlet 3: k_surf runs before the edges */
   int32_t steady;            /* some member tests for steady state: k_steady runs after the cells */
   int32_t xd_cmp;            /* edge kernel: 1 = comparisons on integer keys (cf_xd.h) */
-  int32_t xd_mul_mask;       /* edge kernel, with xd_cmp: warps w of a block with bit w set multiply
-                                on the integer pipes */
+  int32_t xd_mul_mask;       /* with xd_cmp: warps w (0-3) of an edge block with bit w set, and with
+                                bit 4 (XD_CELLS) the element kernel, form products, quotients and
+                                roots on the integer pipes */
 };
 
 /* ---- host preprocessing (cf_mesh.cpp) ---------------------------------------------- */
@@ -175,6 +177,7 @@ typedef struct CUstream_st* stream_t;
 
 int launch_step(const StepArgs& a, stream_t s, void* ev_mid, void* ev_end);
 int launch_probe_fp64(double* out, int32_t nblocks, int64_t iters, stream_t s);  /* nblocks x 256 outputs */
+int launch_selftest_xd(int64_t n, uint64_t seed, unsigned long long* bad, int32_t nblocks, stream_t s);
 int launch_cfl(const double4* U, const double4* cstat, const int32_t* ctile_mem, int32_t tile_begin,
                int32_t n_tiles, const MemberDev* mdev, MemberState* mst, int32_t slot, stream_t s);
 int launch_discharge(const Slot* slots, const int2* ecell, const MemberDev* mdev, MemberState* mst,

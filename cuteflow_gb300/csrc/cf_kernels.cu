@@ -228,9 +228,9 @@ __global__ void __launch_bounds__(TILE_C) k_cells(StepArgs a) {
     const Slot s1 = load_slot(a.slots + sl.y);
     const Slot s2 = load_slot(a.slots + sl.z);
     bool nonfinite = false;
-    /* FP64 pipe only: the integer-pipe arithmetic of cf_xd.h does not pay here (1M elements:
-     * 0.180 ms; integer comparisons 0.180 ms, comparisons and products 0.197 ms) */
-    V = element_update(M, U, st, s0, s1, s2, dt, nonfinite);
+    /* bit 4 of xd_mul_mask: the element's arithmetic on the integer pipes (cf_xd.h) */
+    if (a.xd_cmp && (a.xd_mul_mask & XD_CELLS)) V = element_update<XD<true>>(M, U, st, s0, s1, s2, dt, nonfinite);
+    else V = element_update(M, U, st, s0, s1, s2, dt, nonfinite);
     if (nonfinite) atomicOr(&S->status, CF_STATUS_NONFINITE);
     double4* o = a.Uout + c;
     reinterpret_cast<double2*>(o)[0] = make_double2(V.x, V.y);
@@ -368,9 +368,100 @@ __global__ void __launch_bounds__(256) k_probe_fp64(double* out, long long iters
   out[blockIdx.x * (size_t)blockDim.x + threadIdx.x] = sum;
 }
 
+/* Self-test of the integer-pipe arithmetic of cf_xd.h against the FP64 unit.  Pair i comes from
+ * a splitmix64 sequence: exponents over the whole range or near the step's values, all-ones and
+ * near-all-ones significands, signed zeros, subnormals, infinities, NaN, and quotients and roots
+ * within a few units of a rounding midpoint.  Counts the results of em_mul, em_div,
+ * em_sqrt, the exponent-change scalings, negation and the integer comparisons whose bits differ
+ * from the hardware's (two NaNs count as equal). */
+__device__ unsigned long long st_next(unsigned long long& s) {
+  s += 0x9e3779b97f4a7c15ull;
+  unsigned long long z = s;
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+  return z ^ (z >> 31);
+}
+__device__ double st_operand(unsigned long long& s, int emin, int emax) {
+  unsigned long long m = st_next(s) & ((1ull << 52) - 1);
+  const unsigned long long r = st_next(s);
+  const int mode = (int)(r & 7u);
+  if (mode == 0) m = (1ull << 52) - 1;
+  if (mode == 1) m = 0;
+  if (mode == 2) m = (r >> 8) & 15u;
+  if (mode == 3) m = ((1ull << 52) - 1) ^ ((r >> 8) & 15u);
+  const unsigned long long e = (unsigned long long)emin + (r >> 16) % (unsigned long long)(emax - emin + 1);
+  return xdbl(((r >> 63) << 63) | (e << 52) | m);
+}
+__device__ bool st_same(double x, double y) { return xbits(x) == xbits(y) || (x != x && y != y); }
+
+__global__ void __launch_bounds__(256) k_selftest_xd(long long n, unsigned long long seed,
+                                                     unsigned long long* bad) {
+  unsigned long long nbad = 0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    unsigned long long s = seed ^ ((unsigned long long)i * 0xd1342543de82ef95ull);
+    const int mode = (int)(st_next(s) % 8u);
+    double a, b;
+    if (mode == 0) { a = st_operand(s, 1, 2046); b = st_operand(s, 1, 2046); }
+    else if (mode == 1) { a = st_operand(s, 0, 2047); b = st_operand(s, 0, 2047); }
+    else if (mode == 2) { a = st_operand(s, 1000, 1050); b = st_operand(s, 1000, 1050); }
+    else if (mode == 3) { a = st_operand(s, 1, 30); b = st_operand(s, 990, 1030); }
+    else if (mode == 4) { a = st_operand(s, 2000, 2046); b = st_operand(s, 1000, 1100); }
+    else if (mode == 5) { a = (st_next(s) & 1) ? -0.0 : 0.0; b = st_operand(s, 0, 2047); }
+    else if (mode == 6) { a = st_operand(s, 0, 2047); b = (st_next(s) & 1) ? -0.0 : 0.0; }
+    else {
+      /* a / b close to a rounding midpoint: A = RN((2N+1) B / 2^sh), moved by up to two units */
+      const unsigned long long N = (1ull << 52) | (st_next(s) & ((1ull << 52) - 1));
+      const unsigned long long B = (1ull << 52) | (st_next(s) & ((1ull << 52) - 1));
+      const unsigned long long u = 2 * N + 1;
+      const unsigned long long lo = u * B, hi = __umul64hi(u, B);  /* (2N+1) B = hi 2^64 + lo */
+      const int sh = ((hi >> 42) != 0 || (st_next(s) & 1)) ? 54 : 53;
+      const unsigned long long half = 1ull << (sh - 1);
+      const unsigned long long lo2 = lo + half, hi2 = hi + (lo2 < lo ? 1u : 0u);
+      unsigned long long A = (hi2 << (64 - sh)) | (lo2 >> sh);
+      A += st_next(s) % 5u;
+      A -= 2;
+      if (A >= (1ull << 53)) A = (1ull << 53) - 1;
+      if (A < (1ull << 52)) A = 1ull << 52;
+      const unsigned long long r = st_next(s);
+      a = xdbl(((r >> 63) << 63) | ((1000ull + (r >> 8) % 40u) << 52) | (A & ((1ull << 52) - 1)));
+      b = xdbl((((r >> 62) & 1) << 63) | ((1000ull + (r >> 20) % 40u) << 52) | (B & ((1ull << 52) - 1)));
+    }
+    if (mode == 4 && (st_next(s) & 1)) {
+      /* sqrt(a) close to a rounding midpoint: the significand of RN((N + 1/2)^2 / 2^(52 + p)),
+       * moved by up to two units, with an exponent of parity p */
+      const unsigned long long N = (1ull << 52) | (st_next(s) & ((1ull << 52) - 1));
+      const unsigned long long u = 2 * N + 1;
+      const unsigned long long lo = u * u, hi = __umul64hi(u, u);  /* (2N+1)^2 = hi 2^64 + lo */
+      const int sh = (hi >> 43) ? 55 : 54;
+      const unsigned long long half = 1ull << (sh - 1);
+      const unsigned long long lo2 = lo + half, hi2 = hi + (lo2 < lo ? 1u : 0u);
+      unsigned long long A = (hi2 << (64 - sh)) | (lo2 >> sh);
+      A += st_next(s) % 5u;
+      A -= 2;
+      if (A >= (1ull << 53)) A = (1ull << 53) - 1;
+      if (A < (1ull << 52)) A = 1ull << 52;
+      const unsigned long long ex = 1001ull + 2 * (st_next(s) % 20u) - (sh == 55 ? 1u : 0u);
+      a = xdbl((ex << 52) | (A & ((1ull << 52) - 1)));
+    }
+    nbad += !st_same(em_sqrt(a), sqrt(a));
+    if (st_next(s) & 1) { const double t = a; a = b; b = t; }
+    nbad += !st_same(em_mul(a, b), a * b);
+    nbad += !st_same(em_div(a, b), a / b);
+    nbad += !st_same(xscale<-2>(a), a * 0.25) + !st_same(xscale<-1>(a), a * 0.5) + !st_same(xscale<1>(a), a * 2.0);
+    nbad += !st_same(val(-XD<true>(a)), -a);
+    nbad += (xlt(a, b) != (a < b)) + (xle(a, b) != (a <= b)) + (xeq(a, b) != (a == b));
+  }
+  if (nbad) atomicAdd(bad, nbad);
+}
+
 int check(cudaError_t e) { return e == cudaSuccess ? CF_OK : CF_ECUDA; }
 
 }  // namespace
+
+int launch_selftest_xd(int64_t n, uint64_t seed, unsigned long long* bad, int32_t nblocks, stream_t s) {
+  k_selftest_xd<<<nblocks, 256, 0, reinterpret_cast<cudaStream_t>(s)>>>((long long)n, (unsigned long long)seed, bad);
+  return check(cudaGetLastError());
+}
 
 int launch_probe_fp64(double* out, int32_t nblocks, int64_t iters, stream_t s) {
   k_probe_fp64<<<nblocks, 256, 0, reinterpret_cast<cudaStream_t>(s)>>>(out, (long long)iters);

@@ -80,6 +80,153 @@ XD_NOINLINE double em_mul(double a, double b) {
   return xdbl((((uint64_t)(e - 1) << 52) + mant) | ((ua ^ ub) & (1ull << 63)));
 }
 
+/* the FP64 quotient, for the operands and results the integer path does not cover */
+XD_NOINLINE double xdiv_slow(double a, double b) { return a / b; }
+
+/* bits of an approximation to 1/f, f in [1, 2): on the device the single-precision reciprocal
+ * (rcp.approx.ftz.f32, error at most one unit in the last place); on the host the IEEE float
+ * quotient moved by -1, 0 or +1 unit, so host runs exercise the device's error bound */
+XD_HD uint32_t xrcp_seed(float f, uint64_t salt) {
+#ifdef __CUDA_ARCH__
+  (void)salt;
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(f));
+  return __float_as_uint(r);
+#else
+  const float r = 1.0f / f;
+  uint32_t rb;
+  memcpy(&rb, &r, sizeof(rb));
+  return rb + (uint32_t)(salt % 3u) - 1u;
+#endif
+}
+
+/* a / b rounded to nearest even, in integer arithmetic (normal operands, normal result; zero
+ * numerators too).  With A, B the significands (2^52 <= A, B < 2^53) and t = (A < B), the
+ * result's significand is N = RN(X / B), X = A 2^(52 + t), in [2^52, 2^53]:
+ *  1. R0 ~ 2^84 / B from a float reciprocal of B's leading 24 bits (relative error < 2^-22;
+ *     the reciprocal is clamped to the interval the exact one lies in);
+ *  2. R ~ 2^115 / B = R0 2^31 (1 + e + e^2), e = 1 - B R0 / 2^84 (error e^3 plus truncations,
+ *     below 2^-60), all in 64-bit fixed point;
+ *  3. Q = floor(X R / 2^115), within one of floor(X / B); the remainder X - Q B is formed
+ *     exactly (its magnitude is below 2^55, so 64-bit wrap-around arithmetic holds it) and
+ *     brings Q to floor(X / B) with 0 <= remainder < B, which is checked: any other outcome takes
+ *     the FP64 quotient;
+ *  4. N = Q + 1 when twice the remainder exceeds B (or equals it, Q odd: a tie, which a quotient
+ *     of two 53-bit numbers cannot produce).
+ * Every result is the IEEE quotient's bits; the approximations of steps 1-2 only decide how
+ * often the correction of step 3 is needed. */
+XD_NOINLINE double em_div(double a, double b) {
+  const uint64_t ua = xbits(a), ub = xbits(b);
+  const uint32_t ea = (uint32_t)(ua >> 52) & 0x7ffu, eb = (uint32_t)(ub >> 52) & 0x7ffu;
+  const uint64_t S = (ua ^ ub) & 0x8000000000000000ull;
+  if (eb - 1u >= 2046u) return xdiv_slow(a, b);
+  if ((ua << 1) == 0) return xdbl(S);  /* +-0 / normal */
+  if (ea - 1u >= 2046u) return xdiv_slow(a, b);
+  const uint64_t M = (1ull << 52) - 1;
+  const uint64_t A = (ua & M) | (1ull << 52), B = (ub & M) | (1ull << 52);
+  const uint32_t t = (A < B) ? 1u : 0u;
+  const int e = (int)ea - (int)eb + 1023 - (int)t;  /* the result's exponent field */
+  if ((uint32_t)(e - 1) >= 2045u) return xdiv_slow(a, b);
+  /* 1. */
+  const uint32_t fb = 0x3f800000u | ((uint32_t)(B >> 29) & 0x7fffffu);
+  float f;
+  memcpy(&f, &fb, sizeof(f));
+  const uint32_t rb = xrcp_seed(f, B);
+  /* R0 = 2^32 r with r clamped to [1/2, 1 - 2^-32] (1/f lies in (1/2, 1]) */
+  const uint64_t R0 = (rb >= 0x3f800000u) ? 0xffffffffull
+                      : (rb < 0x3f000000u) ? 0x80000000ull : ((uint64_t)((rb & 0x7fffffu) | 0x800000u) << 8);
+  /* 2. E0 = 2^84 e (|E0| < 2^63); T = 2^84 (e + e^2), the square from E0's leading bits */
+  const int64_t E0 = (int64_t)(0ull - B * R0);
+  const int64_t Eh = E0 >> 32;
+  const int64_t T = E0 + ((Eh * Eh) >> 20);
+  const int64_t Ph = (int64_t)R0 * (T >> 32);
+  const uint64_t Pl = R0 * (uint64_t)(uint32_t)T;
+  const int64_t P = Ph + (int64_t)(Pl >> 32);  /* floor(R0 T / 2^32) */
+  const uint64_t R = (R0 << 31) + (uint64_t)(P >> 21);
+  /* 3. */
+  uint64_t Q = xmulhi(A << 11, R) >> (10 - t);
+  int64_t rem = (int64_t)((A << (52 + t)) - Q * B);
+  if (rem < 0) { Q -= 1; rem += (int64_t)B; }
+  else if (rem >= (int64_t)B) { Q += 1; rem -= (int64_t)B; }
+  if ((uint64_t)rem >= B) return xdiv_slow(a, b);
+  /* 4. */
+  const uint64_t r2 = (uint64_t)rem << 1;
+  Q += (r2 > B || (r2 == B && (Q & 1u))) ? 1u : 0u;
+  return xdbl((((uint64_t)(e - 1) << 52) + Q) | S);
+}
+
+XD_HD int64_t xmulhi_s(int64_t a, int64_t b) {
+#ifdef __CUDA_ARCH__
+  return __mul64hi(a, b);
+#else
+  return (int64_t)(((__int128)a * b) >> 64);
+#endif
+}
+
+/* the FP64 square root, for the operands the integer path does not cover */
+XD_NOINLINE double xsqrt_slow(double x) { return ::sqrt(x); }
+
+/* bits of an approximation to 1/sqrt(f), f in [1, 4): rsqrt.approx.ftz.f32 on the device; on the
+ * host the quotient of 1 and the float root moved by -1, 0 or +1 unit */
+XD_HD uint32_t xrsqrt_seed(float f, uint64_t salt) {
+#ifdef __CUDA_ARCH__
+  (void)salt;
+  float r;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(f));
+  return __float_as_uint(r);
+#else
+  const float r = 1.0f / std::sqrt(f);
+  uint32_t rb;
+  memcpy(&rb, &r, sizeof(rb));
+  return rb + (uint32_t)(salt % 3u) - 1u;
+#endif
+}
+
+/* sqrt(x) rounded to nearest even, in integer arithmetic (positive normal x; zeros too).  With X
+ * the significand and p the parity of the unbiased exponent, the result's significand is
+ * N = RN(sqrt(Y)), Y = X 2^(52 + p) in [2^104, 2^106):
+ *  1. G0 ~ 2^32 / sqrt(X 2^(p - 52)) from the float reciprocal square root of X's leading 24
+ *     bits (clamped to the interval (1/2, 1] the exact one lies in);
+ *  2. e = 1 - Y G0^2 / 2^168 and S = X G0 2^(p - 32) (1 + e/2 + 3 e^2 / 8) (error 5 e^3 / 16 plus
+ *     truncations), plus one, which puts S within one of floor(sqrt(Y));
+ *  3. the remainder Y - S^2, exact in 64-bit wrap-around arithmetic (its magnitude is below
+ *     2^57), brings S to floor(sqrt(Y)) with 0 <= remainder <= 2 S, which is checked: any other
+ *     outcome takes the FP64 root;
+ *  4. N = S + 1 when the remainder exceeds S (sqrt(Y) above S + 1/2; never equal to it).
+ * Every result is the IEEE root's bits. */
+XD_NOINLINE double em_sqrt(double x) {
+  const uint64_t ux = xbits(x);
+  if ((ux << 1) == 0) return x;
+  const uint32_t ex = (uint32_t)(ux >> 52);  /* sign bit included: negative x fails the test */
+  if (ex - 1u >= 2046u) return xsqrt_slow(x);
+  const uint64_t X = (ux & ((1ull << 52) - 1)) | (1ull << 52);
+  const uint32_t p = (ex & 1u) ^ 1u;
+  const int er = (((int)ex - 1023 - (int)p) >> 1) + 1023;  /* the result's exponent field */
+  /* 1. */
+  const uint32_t fb = ((127u + p) << 23) | ((uint32_t)(X >> 29) & 0x7fffffu);
+  float f;
+  memcpy(&f, &fb, sizeof(f));
+  const uint32_t gb = xrsqrt_seed(f, X);
+  const uint64_t G0 = (gb >= 0x3f800000u) ? 0xffffffffull
+                      : (gb < 0x3f000000u) ? 0x80000000ull : ((uint64_t)((gb & 0x7fffffu) | 0x800000u) << 8);
+  /* 2. Ee = 2^63 e, C = 2^64 (e/2 + 3 e^2 / 8) */
+  const uint64_t hi = xmulhi(X << 11, G0 * G0);  /* floor(X G0^2 / 2^53) ~ 2^(63 - p) (1 - e) */
+  const int64_t Ee = (int64_t)((1ull << (63 - p)) - hi) << p;
+  const int64_t Eh = Ee >> 20;
+  const int64_t Cc = Ee + ((3 * Eh * Eh) >> 25);
+  const uint64_t lo = X * G0, xh = xmulhi(X, G0);
+  const int64_t Sb = (int64_t)((xh << (32 + p)) | (lo >> (32 - p)));  /* floor(X G0 2^(p - 32)) */
+  uint64_t S = (uint64_t)(Sb + xmulhi_s(Sb, Cc)) + 1u;
+  /* 3. */
+  int64_t rem = (int64_t)((X << (52 + p)) - S * S);
+  if (rem < 0) { rem += (int64_t)(2 * S - 1); S -= 1; }
+  else if (rem > (int64_t)(2 * S)) { rem -= (int64_t)(2 * S + 1); S += 1; }
+  if (rem < 0 || rem > (int64_t)(2 * S)) return xsqrt_slow(x);
+  /* 4. */
+  S += (rem > (int64_t)S) ? 1u : 0u;
+  return xdbl(((uint64_t)(er - 1) << 52) + S);
+}
+
 /* ordered integer key of a non-NaN double: order of the values, -0 and +0 equal */
 XD_HD long long xkey(uint64_t b) {
   const long long s = (long long)b >> 63;
@@ -114,6 +261,11 @@ XD_HD double xd_mul(double a, double b) {
   if (MUL) return em_mul(a, b);
   return a * b;
 }
+template <bool MUL>
+XD_HD double xd_div(double a, double b) {
+  if (MUL) return em_div(a, b);
+  return a / b;
+}
 
 #define CF_XD_BIN(op, expr)                                                                               \
   template <bool MUL> XD_HD XD<MUL> operator op(const XD<MUL>& a, const XD<MUL>& b) { double x = a.v, y = b.v; return XD<MUL>(expr); } \
@@ -122,10 +274,12 @@ XD_HD double xd_mul(double a, double b) {
 CF_XD_BIN(+, x + y)
 CF_XD_BIN(-, x - y)
 CF_XD_BIN(*, xd_mul<MUL>(x, y))
-CF_XD_BIN(/, x / y)
+CF_XD_BIN(/, xd_div<MUL>(x, y))
 #undef CF_XD_BIN
 
-template <bool MUL> XD_HD XD<MUL> operator-(const XD<MUL>& a) { return XD<MUL>(-a.v); }
+/* negation as a sign-bit flip: an FP64 negation that is not folded into its consumer is an FP64
+ * instruction, and most consumers here are integer code (products, comparisons) */
+template <bool MUL> XD_HD XD<MUL> operator-(const XD<MUL>& a) { return XD<MUL>(xdbl(xbits(a.v) ^ 0x8000000000000000ull)); }
 
 #define CF_XD_CMP(op, expr)                                                                               \
   template <bool MUL> XD_HD bool operator op(const XD<MUL>& a, const XD<MUL>& b) { double x = a.v, y = b.v; return expr; } \
@@ -139,17 +293,36 @@ CF_XD_CMP(==, xeq(x, y))
 CF_XD_CMP(!=, !xeq(x, y))
 #undef CF_XD_CMP
 
-template <bool MUL> XD_HD XD<MUL> sqrt(const XD<MUL>& a) { return XD<MUL>(::sqrt(a.v)); }
+template <bool MUL> XD_HD XD<MUL> sqrt(const XD<MUL>& a) { return XD<MUL>(MUL ? em_sqrt(a.v) : ::sqrt(a.v)); }
 template <bool MUL> XD_HD XD<MUL> rcbrt(const XD<MUL>& a) { return XD<MUL>(rcbrt(a.v)); }
 template <bool MUL> XD_HD XD<MUL> fabs(const XD<MUL>& a) { return XD<MUL>(xdbl(xbits(a.v) & 0x7fffffffffffffffull)); }
 template <bool MUL> XD_HD XD<MUL> sgnmul(const XD<MUL>& x, const XD<MUL>& y) {
   return XD<MUL>(xdbl(xbits(y.v) ^ (xbits(x.v) & 0x8000000000000000ull)));
 }
 
-/* Markstein's quotient (div_rn in cf_flux.h) with the product on the chosen path */
+/* x * 2^K (K = -2, -1, 1) by a change of the exponent field, for a normal x whose result is
+ * normal: the exact scaling, the bits of the FP64 product.  Zeros keep their bits; subnormal,
+ * infinite and NaN operands and results out of the normal range take the FP64 product. */
+template <int K>
+XD_HD double xscale(double x) {
+  const uint64_t b = xbits(x);
+  const uint32_t e = (uint32_t)(b >> 52) & 0x7ffu;
+  const uint32_t lo = (K < 0) ? (uint32_t)(1 - K) : 1u;          /* lowest exponent field handled */
+  const uint32_t n = (K < 0) ? (uint32_t)(2046 + K) : (uint32_t)(2046 - K);  /* fields handled */
+  if (e - lo < n) return xdbl(b + ((uint64_t)(int64_t)K << 52));
+  if ((b << 1) == 0) return x;
+  return xmul_slow(x, (K == -2) ? 0.25 : ((K == -1) ? 0.5 : 2.0));
+}
+template <bool MUL> XD_HD XD<MUL> halve(const XD<MUL>& x) { return XD<MUL>(MUL ? xscale<-1>(x.v) : x.v * 0.5); }
+template <bool MUL> XD_HD XD<MUL> quarter(const XD<MUL>& x) { return XD<MUL>(MUL ? xscale<-2>(x.v) : x.v * 0.25); }
+template <bool MUL> XD_HD XD<MUL> twice(const XD<MUL>& x) { return XD<MUL>(MUL ? xscale<1>(x.v) : x.v * 2.0); }
+
+/* The quotient a / d that div_rn in cf_flux.h forms from y = RN(1/d) by Markstein's step: on the
+ * integer path the division itself (the same bits, y unused), otherwise Markstein's step. */
 template <bool MUL>
 XD_HD XD<MUL> div_rn(const XD<MUL>& a, double d, double y) {
-  const double q = xd_mul<MUL>(a.v, y);
+  if (MUL) return XD<MUL>(em_div(a.v, d));
+  const double q = a.v * y;
   const double r = fma(-d, q, a.v);
   const double q1 = fma(r, y, q);
   return XD<MUL>(((xbits(a.v) << 1) == 0) ? q : q1);

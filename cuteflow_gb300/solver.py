@@ -57,6 +57,7 @@ def load(build_if_missing: bool = True):
     L.cf_run.argtypes = [vp, C.c_double, C.c_int64, C.POINTER(_abi.CfStepInfo)]
     L.cf_set_tuning.argtypes = [vp, C.c_int32, C.c_int32]
     L.cf_probe_fp64.argtypes = [vp, dp]
+    L.cf_selftest_xd.argtypes = [vp, C.c_int64, C.c_uint64, C.POINTER(C.c_int64)]
     L.cf_advance.argtypes = [vp, dp, C.c_double, C.c_int32, dp, C.POINTER(_abi.CfStepInfo)]
     L.cf_get_elements.argtypes = [vp, C.c_int32, C.POINTER(C.c_int32), C.c_int32, dp]
     L.cf_set_elements.argtypes = [vp, C.c_int32, C.POINTER(C.c_int32), C.c_int32, dp]
@@ -116,7 +117,7 @@ def load(build_if_missing: bool = True):
                  "cf_set_initial_condition", "cf_step", "cf_step_noalloc", "cf_run", "cf_set_tuning",
                  "cf_get_tuning", "cf_autotune", "cf_get_elements", "cf_set_elements", "cf_set_dt", "cf_get_state", "cf_get_state_device",
                  "cf_get_info", "cf_get_mesh_tables", "cf_mesh_tables", "cf_get_sizes", "cf_set_timing", "cf_get_timing",
-                 "cf_probe_fp64", "cf_advance"):
+                 "cf_probe_fp64", "cf_selftest_xd", "cf_advance"):
         getattr(L, name).restype = C.c_int
     _lib = L
     return L
@@ -274,6 +275,13 @@ class Solver:
         r = C.c_double()
         self._check(self._L.cf_probe_fp64(self._ctx, C.byref(r)))
         return r.value
+
+    def selftest_xd(self, n: int, seed: int = 1) -> int:
+        """cf_selftest_xd: mismatches of the integer-pipe arithmetic against the FP64 unit on n
+        adversarial operand pairs (0 expected)."""
+        r = C.c_int64()
+        self._check(self._L.cf_selftest_xd(self._ctx, int(n), int(seed), C.byref(r)))
+        return int(r.value)
 
     def run(self, ts: float, max_steps: int = 1 << 40, check: bool = True) -> StepInfo:
         """The reference's time loop up to time ts (cf_run): stops with CF_STATUS_END, or at a

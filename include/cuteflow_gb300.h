@@ -266,12 +266,13 @@ int cf_get_elements(cf_ctx* ctx, int32_t member, const int32_t* ids, int32_t n, 
 int cf_set_elements(cf_ctx* ctx, int32_t member, const int32_t* ids, int32_t n, const double* hu3);
 int cf_set_dt(cf_ctx* ctx, int32_t member, double dt);
 
-/* How the edge kernel shares its FP64 work between GB300's FP64 pipe and its integer pipes
- * (results are identical bit for bit in every setting): int_compare 1 evaluates comparisons
- * on integer keys of the bit patterns; int_mul_warps is a mask over the 4 warps of an edge
- * block, and the warps whose bit is set form products by exact integer multiplication of the
- * significands.  Default (0, 0): every operation on the FP64 pipe.  cf_autotune picks a
- * setting by timing. */
+/* How the step shares its FP64 work between GB300's FP64 pipe and its integer pipes (results
+ * are identical bit for bit in every setting): int_compare 1 evaluates the edge kernel's
+ * comparisons on integer keys of the bit patterns; bits 0-3 of int_mul_warps are a mask over
+ * the 4 warps of an edge block, and the warps whose bit is set form products, quotients, square
+ * roots and scalings by 2^k in exact integer arithmetic on the significands (correctly rounded,
+ * the IEEE results); bit 4 does the same for the element kernel.  Default (0, 0): every
+ * operation on the FP64 pipe.  cf_autotune picks a setting by timing. */
 int cf_set_tuning(cf_ctx* ctx, int32_t int_compare, int32_t int_mul_warps);
 int cf_get_tuning(cf_ctx* ctx, int32_t* int_compare, int32_t* int_mul_warps);
 /* Autotuner: times steps_per_trial steps of every setting on the context's own state and keeps
@@ -285,6 +286,13 @@ int cf_autotune(cf_ctx* ctx, int32_t steps_per_trial, int32_t* int_compare, int3
  * roofline: the step is bound by FP64 instruction issue, not by HBM.  Allocates and frees a
  * scratch buffer of 2 KB per block. */
 int cf_probe_fp64(cf_ctx* ctx, double* instr_per_s);
+
+/* Diagnostic: checks the integer-pipe arithmetic the tuned step uses (products, quotients,
+ * scalings by 2^k, negation and comparisons of doubles in integer instructions) against the
+ * device's FP64 unit on n adversarial operand pairs generated on the device from seed, and
+ * stores in *mismatches how many results differ in any bit (0 expected).  Allocates and frees
+ * 8 bytes of device memory. */
+int cf_selftest_xd(cf_ctx* ctx, int64_t n, uint64_t seed, int64_t* mismatches);
 
 /* Kernel timing of the last cf_step call: total device milliseconds of the edge-flux and
  * cell-update kernels measured with CUDA events when timing is enabled. */

@@ -7,6 +7,7 @@
 #include "../cuteflow_gb300/csrc/cf_flux.h"
 #include "../cuteflow_gb300/csrc/cf_xd.h"
 
+#include <cmath>
 #include <vector>
 
 using namespace cf;
@@ -241,7 +242,7 @@ extern "C" void harness_rcbrt(const double* x, double* y, long long n) {
   for (long long i = 0; i < n; ++i) y[i] = cf::rcbrt(x[i]);
 }
 
-/* em_mul and the integer comparisons of cf_xd.h against the hardware on n adversarial operand
+/* em_mul, em_div, em_sqrt, the exponent-change scalings and the integer comparisons of cf_xd.h against the hardware on n adversarial operand
  * pairs: exponents over the whole range (subnormals, near overflow and underflow), all-ones and
  * near-all-ones significands, signed zeros, infinities and NaN.  Returns the mismatches. */
 extern "C" long long harness_xd_check(long long n, unsigned long long seed) {
@@ -271,10 +272,46 @@ extern "C" long long harness_xd_check(long long n, unsigned long long seed) {
     else if (mode == 4) { a = mk(2000, 2046); b = mk(1000, 1100); }   /* overflow edge */
     else { a = (rnd() & 1) ? -0.0 : 0.0; b = mk(0, 2047); }           /* signed zero times anything */
     if (mode == 6) std::swap(a, b);
+    if (mode == 5 && (rnd() & 1)) {
+      /* a / b close to a rounding midpoint: A = RN((2N+1) B / 2^sh) moved by up to two units */
+      const unsigned long long N = (1ull << 52) | (rnd() & ((1ull << 52) - 1));
+      const unsigned long long B = (1ull << 52) | (rnd() & ((1ull << 52) - 1));
+      const unsigned __int128 num = (unsigned __int128)(2 * N + 1) * B;
+      const int sh = ((num >> 106) != 0 || (rnd() & 1)) ? 54 : 53;  /* A / B below or above 1 */
+      unsigned long long A = (unsigned long long)((num + ((unsigned __int128)1 << (sh - 1))) >> sh);
+      A += (rnd() % 5) - 2;
+      if (A >= (1ull << 53)) A = (1ull << 53) - 1;
+      if (A < (1ull << 52)) A = 1ull << 52;
+      const unsigned long long ba = ((rnd() & 1) << 63) | ((unsigned long long)(1000 + rnd() % 40) << 52) | (A & ((1ull << 52) - 1));
+      const unsigned long long bb = ((rnd() & 1) << 63) | ((unsigned long long)(1000 + rnd() % 40) << 52) | (B & ((1ull << 52) - 1));
+      memcpy(&a, &ba, 8);
+      memcpy(&b, &bb, 8);
+    }
+    if (mode == 4 && (rnd() & 1)) {
+      /* sqrt(a) close to a rounding midpoint: significand of RN((N + 1/2)^2 / 2^(52 + p)), moved
+       * by up to two units */
+      const unsigned long long N = (1ull << 52) | (rnd() & ((1ull << 52) - 1));
+      const unsigned __int128 sq = (unsigned __int128)(2 * N + 1) * (2 * N + 1);  /* 4 (N + 1/2)^2 */
+      const int sh = (sq >> 107) ? 55 : 54;
+      unsigned long long A = (unsigned long long)((sq + ((unsigned __int128)1 << (sh - 1))) >> sh);
+      A += (rnd() % 5) - 2;
+      if (A >= (1ull << 53)) A = (1ull << 53) - 1;
+      if (A < (1ull << 52)) A = 1ull << 52;
+      const unsigned long long ex = (unsigned long long)(1001 + 2 * (rnd() % 20) - (sh == 55 ? 1 : 0));  /* parity p = sh - 54 */
+      const unsigned long long ba = (ex << 52) | (A & ((1ull << 52) - 1));
+      memcpy(&a, &ba, 8);
+    }
+    const double r1 = em_sqrt(a), r2 = std::sqrt(a);
+    if (memcmp(&r1, &r2, 8) != 0 && !(r1 != r1 && r2 != r2)) ++bad;
+    const double q1 = em_div(a, b), q2 = a / b;
+    if (memcmp(&q1, &q2, 8) != 0 && !(q1 != q1 && q2 != q2)) ++bad;
     const double p1 = em_mul(a, b), p2 = a * b;
     const double n1 = val(-XD<true>(a)), n2 = -a;
     if (memcmp(&n1, &n2, 8) != 0) ++bad;
     if (memcmp(&p1, &p2, 8) != 0 && !(p1 != p1 && p2 != p2)) ++bad;
+    const double s1[3] = {xscale<-2>(a), xscale<-1>(a), xscale<1>(a)}, s2[3] = {a * 0.25, a * 0.5, a * 2.0};
+    for (int k = 0; k < 3; ++k)
+      if (memcmp(&s1[k], &s2[k], 8) != 0 && !(s1[k] != s1[k] && s2[k] != s2[k])) ++bad;
     if (xlt(a, b) != (a < b) || xle(a, b) != (a <= b) || xeq(a, b) != (a == b)) ++bad;
     const double z = (rnd() & 1) ? -0.0 : 0.0;
     if (xlt(a, z) != (a < z) || xlt(z, a) != (z < a) || xle(a, z) != (a <= z) || xeq(a, z) != (a == z)) ++bad;

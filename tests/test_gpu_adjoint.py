@@ -157,14 +157,14 @@ def test_gradient_independent_of_checkpoint_interval(gpu_lib):
 
 @pytest.mark.parametrize("case", ["waf_flood", "hllc_dam"])
 def test_gradient_independent_of_integer_pipe_setting(gpu_lib, case):
-    """The recording forward and the segment replays run the step's edge kernel in the context's
+    """The recording forward and the segment replays run the step's kernels in the context's
     integer-pipe setting; every setting rounds identically, so the gradient is the same bit for bit."""
     from cuteflow_gb300.adjoint import Adjoint
     c, extra, s, adj, w_eta, w_state = _setup(case, nsteps=23)
     out = []
     with s:
         adj.close()
-        for tuning in ((0, 0), (1, 0), (1, 0xF), (1, 0x5)):
+        for tuning in ((0, 0), (1, 0), (1, 0xF), (1, 0x5), (1, 0x1F)):
             s.set_tuning(*tuning)
             with Adjoint(s, 23, adj.gauges, 4) as a:
                 s.set_state(c.U0)

@@ -195,14 +195,15 @@ def test_config1_circular_dam_break_full(gpu_lib, oracle):
 
 def test_config2_flooding_1M_5000_steps(gpu_lib, oracle):
     """The benchmark workload at full size and length: 1,000,000 triangles, WAF, inflow ramp and
-    fixed-level outflow, 5000 steps from the initial state, with the edge kernel's integer-pipe
-    setting the bench runs (int_compare 1, all warps multiplying on the integer pipes).  Bit for
-    bit the oracle's state, time and next dt (the tolerance of the target is 1e-9 m)."""
+    fixed-level outflow, 5000 steps from the initial state, with the integer-pipe setting the
+    bench's autotuner picks (int_compare 1, integer products, quotients and roots in every edge
+    warp and in the element kernel).  Bit for bit the oracle's state, time and next dt (the
+    tolerance of the target is 1e-9 m)."""
     from cuteflow_gb300 import Solver
     c = cases.flooding(1000, 500, seed=2, iflux=3)
     ref = oracle.run(c, 5000, check=False)
     with Solver(c) as s:
-        s.set_tuning(1, 0xF)
+        s.set_tuning(1, 0x1F)
         s.set_state(c.U0)
         info = s.step(5000)
         U = s.get_state()
@@ -295,15 +296,16 @@ def test_case_directory_runs_to_ts(gpu_lib, oracle, tmp_path):
     assert np.array_equal(U, oracle.run(c, k)["U"])
 
 
-@pytest.mark.parametrize("iflux", [1, 2, 3])
+@pytest.mark.parametrize("iflux", [1, 2, 3, 4])
 def test_integer_pipe_settings_are_bit_identical(gpu_lib, oracle, iflux):
-    """Every setting of cf_set_tuning (comparisons and products on the integer pipes, in some or
-    all warps) gives the oracle's run bit for bit."""
+    """Every setting of cf_set_tuning (comparisons, and products, quotients and roots on the
+    integer pipes in some or all edge warps and in the element kernel) gives the oracle's run bit
+    for bit."""
     from cuteflow_gb300 import Solver
     c = cases.flooding(60, 30, seed=4, iflux=iflux)
     ref = oracle.run(c, 120)
     with Solver(c) as s:
-        for cmp_, mask in ((1, 0), (1, 0xF), (1, 0x5), (1, 0x2), (0, 0)):
+        for cmp_, mask in ((1, 0), (1, 0xF), (1, 0x5), (1, 0x2), (1, 0x10), (1, 0x1F), (0, 0)):
             s.set_tuning(cmp_, mask)
             assert s.tuning() == (cmp_, mask)
             s.set_state(c.U0)
@@ -312,6 +314,8 @@ def test_integer_pipe_settings_are_bit_identical(gpu_lib, oracle, iflux):
             assert info.t == ref["t"]
         with pytest.raises(Exception):
             s.set_tuning(0, 0xF)
+        with pytest.raises(Exception):
+            s.set_tuning(1, 0x20)
 
 
 def test_autotune_leaves_the_run_unchanged(gpu_lib, oracle):
@@ -360,6 +364,20 @@ def test_fp64_probe_reports_a_plausible_rate(gpu_lib):
     with Solver(c) as s:
         r = s.probe_fp64()
         assert 1e11 < r < 5e12, r
+        s.set_state(c.U0)
+        assert s.step(3).status == 0
+
+
+def test_integer_pipe_arithmetic_matches_the_fp64_unit(gpu_lib):
+    """cf_selftest_xd: the device's integer products, quotients (float-seeded reciprocal,
+    fixed-point refinement, exact remainder), scalings by 2^k, negation and comparisons give the
+    FP64 unit's bits on 2^26 adversarial operand pairs per seed: whole exponent range, subnormals,
+    zeros, infinities, NaN, all-ones significands and quotients next to rounding midpoints."""
+    from cuteflow_gb300 import Solver
+    c = cases.flooding(20, 10, seed=1, iflux=1)
+    with Solver(c) as s:
+        for seed in (1, 2, 3):
+            assert s.selftest_xd(1 << 26, seed) == 0
         s.set_state(c.U0)
         assert s.step(3).status == 0
 
