@@ -39,14 +39,15 @@ UNIT = "tri-updates/s"
 ALG_BYTES_WAF = 144.0
 ALG_BYTES_HLLC = 128.0
 # DRAM bytes (read + write) of one 1M-triangle WAF step from one ncu capture of this workload's
-# kernels with the tuned setting (k_edges<3> 421.8 MB + k_cells 246.0 MB), and the FP64-pipe
-# activity the same capture reports; used for the default workload only.
-NCU_TRAFFIC_FLOODING_1M = 667.8e6
-NCU_FP64_PIPE_FLOODING_1M = {"k_edges": 0.786, "k_cells": 0.813}
-# FP64-pipe instructions (DADD + DMUL + DFMA + DSETP, thread-level, ncu sass__inst_executed_per_opcode)
-# of the same step: per edge in k_edges<3> by tuning setting (int_compare, int_mul_warps), per element
-# in k_cells.
-NCU_FP64_INSTR_FLOODING_1M = {"per_edge": {(1, 15): 176.4, (0, 0): 238.2}, "per_element": 73.7}
+# kernels with the tuned setting (k_edges<3> 422.4 MB + k_cells 245.7 MB), and the FP64-pipe and
+# issue activity the same capture reports; used for the default workload only.
+NCU_TRAFFIC_FLOODING_1M = 668.1e6
+NCU_FP64_PIPE_FLOODING_1M = {"k_edges": 0.661, "k_cells": 0.712}
+NCU_ISSUE_FLOODING_1M = {"k_edges": 0.411, "k_cells": 0.318}
+# FP64-pipe instructions (DADD + DMUL + DFMA + DSETP + F2F, thread-level, ncu
+# sass__inst_executed_per_opcode) of the same step by tuning setting (int_compare, int_mul_warps):
+# (per edge in k_edges<3>, per element in k_cells).
+NCU_FP64_INSTR_FLOODING_1M = {(1, 31): (123.2, 53.1), (0, 0): (238.2, 73.7)}
 
 
 def peaks():
@@ -505,9 +506,9 @@ def run_ours(args):
     achieved = alg_bytes * n / (step_kernel_ms * 1e-3) / 1e9
     fp64_rate = s.probe_fp64()
     fp64_instr = None
-    if args.config == "flooding" and (tune[0], tune[1]) in NCU_FP64_INSTR_FLOODING_1M["per_edge"]:
-        fp64_instr = (NCU_FP64_INSTR_FLOODING_1M["per_edge"][(tune[0], tune[1])] * s.nedge
-                      + NCU_FP64_INSTR_FLOODING_1M["per_element"] * n)
+    if args.config == "flooding" and (tune[0], tune[1]) in NCU_FP64_INSTR_FLOODING_1M:
+        per_edge, per_element = NCU_FP64_INSTR_FLOODING_1M[(tune[0], tune[1])]
+        fp64_instr = per_edge * s.nedge + per_element * n
     fp64_achieved = fp64_instr / (step_kernel_ms * 1e-3) if fp64_instr else None
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -527,14 +528,17 @@ def run_ours(args):
                      "traffic_note": "ncu dram__bytes_read.sum + dram__bytes_write.sum per step "
                                      "(k_edges + k_cells) of the 1M WAF step",
                      "k_edges_ms": k_edges_ms, "k_cells_ms": k_cells_ms},
-        "fp64": {"bound": "fp64 pipe (the step's limit; HBM runs at 10-21 % of peak)",
+        "fp64": {"bound": "FP64 pipe and dependent integer-pipe chains at 24 / 36 % warp occupancy (ncu: FP64 "
+                          "pipe 66 / 71 % and issue slots 41 / 32 % busy in k_edges / k_cells; HBM at 12-25 % "
+                          "of peak)",
                  "peak_instr_per_s": fp64_rate,
                  "peak_source": "cf_probe_fp64, measured live: independent FMA chains on every SM",
                  "instr_per_step": fp64_instr,
-                 "instr_source": "ncu sass__inst_executed_per_opcode of the same step (DADD+DMUL+DFMA+DSETP)",
+                 "instr_source": "ncu sass__inst_executed_per_opcode of the same step (DADD+DMUL+DFMA+DSETP+F2F)",
                  "achieved_instr_per_s": fp64_achieved,
                  "frac": fp64_achieved / fp64_rate if fp64_achieved else None,
-                 "pipe_active_ncu": NCU_FP64_PIPE_FLOODING_1M if args.config == "flooding" else None},
+                 "pipe_active_ncu": NCU_FP64_PIPE_FLOODING_1M if args.config == "flooding" else None,
+                 "issue_active_ncu": NCU_ISSUE_FLOODING_1M if args.config == "flooding" else None},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 24 * n, "d2h_bytes_per_step": 24 * n,
                 "steps": e2e_steps, "ms_per_step": e2e_ms / e2e_steps,
                 "link_h2d_gbs": 24 * n / (h2d_ms * 1e-3) / 1e9, "link_d2h_gbs": 24 * n / (d2h_ms * 1e-3) / 1e9,

@@ -12,6 +12,7 @@
 #define CF_DUAL_H
 
 #include "cf_flux.h"
+#include "cf_xd.h"
 
 #ifdef __CUDACC__
 #define CFD_HD __host__ __device__ __forceinline__
@@ -81,15 +82,13 @@ CFD_HD Dual<N> operator*(const Dual<N>& a, const Dual<N>& b) {
   for (int i = 0; i < N; ++i) r.d[i] = fma(a.d[i], b.v, a.v * b.d[i]);
   return r;
 }
-/* a / b: one reciprocal serves the value lane (Markstein's correction, the IEEE quotient) and
- * the derivative lanes; a zero, infinite or subnormal b divides directly. */
+/* a / b: the value lane is the IEEE quotient and the derivative lanes use the reciprocal, both
+ * from the integer-pipe division of cf_xd.h (the FP64 pipe keeps the lanes' FMAs) */
 template <int N>
 CFD_HD Dual<N> operator/(const Dual<N>& a, const Dual<N>& b) {
   Dual<N> r;
-  const double y = 1.0 / b.v;
-  long long yb;
-  memcpy(&yb, &y, sizeof(yb));
-  r.v = ((yb << 1) != 0 && finite_bits(y)) ? div_rn(a.v, b.v, y) : a.v / b.v;
+  const double y = em_div(1.0, b.v);
+  r.v = em_div(a.v, b.v);
 #pragma unroll
   for (int i = 0; i < N; ++i) r.d[i] = fma(-r.v, b.d[i], a.d[i]) * y;
   return r;
@@ -134,8 +133,8 @@ CFD_HD Dual<N> operator/(const Dual<N>& a, double b) {
 template <int N>
 CFD_HD Dual<N> operator/(double a, const Dual<N>& b) {
   Dual<N> r;
-  r.v = a / b.v;
-  const double y = 1.0 / b.v;
+  r.v = em_div(a, b.v);
+  const double y = em_div(1.0, b.v);
 #pragma unroll
   for (int i = 0; i < N; ++i) r.d[i] = -r.v * b.d[i] * y;
   return r;
@@ -157,8 +156,8 @@ template <int N> CFD_HD bool operator!=(const Dual<N>& a, const Dual<N>& b) { re
 template <int N>
 CFD_HD Dual<N> sqrt(const Dual<N>& a) {
   Dual<N> r;
-  r.v = ::sqrt(a.v);
-  const double y = r.v > 0.0 ? 0.5 / r.v : 0.0; /* sqrt(0) only where the depth is exactly zero */
+  r.v = em_sqrt(a.v);
+  const double y = r.v > 0.0 ? em_div(0.5, r.v) : 0.0; /* sqrt(0) only where the depth is exactly zero */
 #pragma unroll
   for (int i = 0; i < N; ++i) r.d[i] = a.d[i] * y;
   return r;
@@ -177,7 +176,7 @@ CFD_HD Dual<N> recip_h(const Dual<N>& h, double) { return 1.0 / h; }
 template <int N>
 CFD_HD Dual<N> div_rn(const Dual<N>& a, const Dual<N>& d, const Dual<N>& y) {
   Dual<N> r;
-  r.v = div_rn(a.v, d.v, y.v);
+  r.v = em_div(a.v, d.v);  /* the IEEE quotient, as div_rn's */
 #pragma unroll
   for (int i = 0; i < N; ++i) r.d[i] = fma(-r.v, d.d[i], a.d[i]) * y.v;
   return r;
@@ -185,7 +184,7 @@ CFD_HD Dual<N> div_rn(const Dual<N>& a, const Dual<N>& d, const Dual<N>& y) {
 template <int N>
 CFD_HD Dual<N> div_rn(const Dual<N>& a, double d, double y) {
   Dual<N> r;
-  r.v = div_rn(a.v, d, y);
+  r.v = em_div(a.v, d);
 #pragma unroll
   for (int i = 0; i < N; ++i) r.d[i] = a.d[i] * y;
   return r;
@@ -196,7 +195,7 @@ template <int N>
 CFD_HD Dual<N> rcbrt(const Dual<N>& x) {
   Dual<N> r;
   r.v = rcbrt(x.v);
-  const double k = -(r.v / (3.0 * x.v));
+  const double k = -em_div(r.v, 3.0 * x.v);
 #pragma unroll
   for (int i = 0; i < N; ++i) r.d[i] = x.d[i] * k;
   return r;
