@@ -39,15 +39,15 @@ UNIT = "tri-updates/s"
 ALG_BYTES_WAF = 144.0
 ALG_BYTES_HLLC = 128.0
 # DRAM bytes (read + write) of one 1M-triangle WAF step from one ncu capture of this workload's
-# kernels with the tuned setting (k_edges<3> 422.4 MB + k_cells 245.7 MB), and the FP64-pipe and
+# kernels with the tuned setting (k_edges<3> 457.5 MB + k_cells 245.9 MB), and the FP64-pipe and
 # issue activity the same capture reports; used for the default workload only.
-NCU_TRAFFIC_FLOODING_1M = 668.1e6
-NCU_FP64_PIPE_FLOODING_1M = {"k_edges": 0.661, "k_cells": 0.712}
-NCU_ISSUE_FLOODING_1M = {"k_edges": 0.411, "k_cells": 0.318}
+NCU_TRAFFIC_FLOODING_1M = 703.4e6
+NCU_FP64_PIPE_FLOODING_1M = {"k_edges": 0.751, "k_cells": 0.712}
+NCU_ISSUE_FLOODING_1M = {"k_edges": 0.486, "k_cells": 0.320}
 # FP64-pipe instructions (DADD + DMUL + DFMA + DSETP + F2F, thread-level, ncu
 # sass__inst_executed_per_opcode) of the same step by tuning setting (int_compare, int_mul_warps):
 # (per edge in k_edges<3>, per element in k_cells).
-NCU_FP64_INSTR_FLOODING_1M = {(1, 31): (123.2, 53.1), (0, 0): (238.2, 73.7)}
+NCU_FP64_INSTR_FLOODING_1M = {(1, 31): (124.0, 53.1), (0, 0): (238.2, 73.7)}
 
 
 def peaks():
@@ -528,8 +528,8 @@ def run_ours(args):
                      "traffic_note": "ncu dram__bytes_read.sum + dram__bytes_write.sum per step "
                                      "(k_edges + k_cells) of the 1M WAF step",
                      "k_edges_ms": k_edges_ms, "k_cells_ms": k_cells_ms},
-        "fp64": {"bound": "FP64 pipe and dependent integer-pipe chains at 24 / 36 % warp occupancy (ncu: FP64 "
-                          "pipe 66 / 71 % and issue slots 41 / 32 % busy in k_edges / k_cells; HBM at 12-25 % "
+        "fp64": {"bound": "FP64 pipe and dependent integer-pipe chains at 47 / 36 % warp occupancy (ncu: FP64 "
+                          "pipe 75 / 71 % and issue slots 49 / 32 % busy in k_edges / k_cells; HBM at 14-25 % "
                           "of peak)",
                  "peak_instr_per_s": fp64_rate,
                  "peak_source": "cf_probe_fp64, measured live: independent FMA chains on every SM",
