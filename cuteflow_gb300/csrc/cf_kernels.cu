@@ -38,8 +38,10 @@ template <int IFLUX>
 /* eight blocks per SM (at most 64 registers, with spills to L1): the tuned edge is chains of
  * dependent integer-pipe products and quotients between its FP64 sums, and the extra warps hide
  * their latency (1M WAF, tuned: 0.462 ms at four blocks, 0.434 at five, 0.421 at six, 0.408 at
- * eight) */
-__global__ void __launch_bounds__(TILE_E, 8) k_edges(StepArgs a) {
+ * eight; HLLC 0.266 -> 0.215 ms).  MUSCL-Hancock runs four (128 registers): at eight its spills
+ * cost more than the warps gain (1.39 ms), at three (138 registers) it takes 1.32 ms, at four
+ * 1.21 ms. */
+__global__ void __launch_bounds__(TILE_E, (IFLUX == 4) ? 4 : 8) k_edges(StepArgs a) {
   const int tile = blockIdx.x;
   const int m = __ldg(a.etile_mem + tile);
   const MemberDev& M = a.mdev[m];
