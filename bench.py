@@ -38,16 +38,13 @@ UNIT = "tri-updates/s"
 # statics 32, neighbour ids 12, per-edge geometry 24 x E/N = 36 (E/N = 1.5), centroids 16.
 ALG_BYTES_WAF = 144.0
 ALG_BYTES_HLLC = 128.0
-# DRAM bytes (read + write) of one 1M-triangle WAF step from one ncu capture of this workload's
-# kernels with the tuned setting (k_edges<3> 457.5 MB + k_cells 245.9 MB), and the FP64-pipe and
-# issue activity the same capture reports; used for the default workload only.
-NCU_TRAFFIC_FLOODING_1M = 703.4e6
-NCU_FP64_PIPE_FLOODING_1M = {"k_edges": 0.751, "k_cells": 0.712}
-NCU_ISSUE_FLOODING_1M = {"k_edges": 0.486, "k_cells": 0.320}
-# FP64-pipe instructions (DADD + DMUL + DFMA + DSETP + F2F, thread-level, ncu
-# sass__inst_executed_per_opcode) of the same step by tuning setting (int_compare, int_mul_warps):
-# (per edge in k_edges<3>, per element in k_cells).
-NCU_FP64_INSTR_FLOODING_1M = {(1, 31): (124.0, 53.1), (0, 0): (238.2, 73.7)}
+# Figures of one ncu capture of this workload's step kernels, keyed by (workload, tuning setting
+# (int_compare, int_mul_warps)): DRAM bytes read + written per step (k_edges + k_cells), FP64-pipe
+# instructions per edge and per element (DADD + DMUL + DFMA + DSETP + F2F, thread-level, from
+# sass__inst_executed_per_opcode), and the FP64-pipe and issue activity ncu reports.  They are
+# profile figures, not measured by this run: the bench line carries them under "from_profile" with
+# the summary they come from, and only for a (workload, setting) the capture covers.
+NCU_PROFILE = {}
 
 
 def peaks():
@@ -424,6 +421,10 @@ def run_ours(args):
         e1.record(stream)
         barrier()
     ms = e0.elapsed_time(e1)
+    # the dry parts of the mesh take the kernels' dry-region shortcuts, so the step's cost depends on
+    # how much of the mesh is wet: reported at the start and at the end of the timed steps
+    wet_end = float(np.mean(s.get_state()[:, 0] > 0.0))
+    wet_start = float(np.mean(case.U0[:, 0] > 0.0))
     if pg is not None:
         t = torch.tensor([ms], device="cuda", dtype=torch.float64)
         pg.all_reduce(t, op=pg.ReduceOp.MAX)
@@ -467,21 +468,30 @@ def run_ours(args):
     barrier()
     three_ms = f0.elapsed_time(f1)
     # the same per step through cf_advance: state in, one step, state out, one wait
-    lib.cf_advance(s._ctx, pin_in, 0.0, 1, pin_out, ctypes.byref(stepinfo))
-    barrier()
-    f0.record(stream)
-    for _ in range(e2e_steps):
-        if lib.cf_advance(s._ctx, pin_in, 0.0, 1, pin_out, ctypes.byref(stepinfo)):
-            raise SystemExit("C ABI call failed during the e2e loop")
-    f1.record(stream)
-    barrier()
-    e2e_ms = f0.elapsed_time(f1)
+    def advance_ms():
+        lib.cf_advance(s._ctx, pin_in, 0.0, 1, pin_out, ctypes.byref(stepinfo))
+        barrier()
+        f0.record(stream)
+        for _ in range(e2e_steps):
+            if lib.cf_advance(s._ctx, pin_in, 0.0, 1, pin_out, ctypes.byref(stepinfo)):
+                raise SystemExit("C ABI call failed during the e2e loop")
+        f1.record(stream)
+        barrier()
+        return f0.elapsed_time(f1)
+
+    # the same calls with every state buffer staged through the device copy (cf_set_direct_io 0),
+    # then the default: the state kernels read and write the pinned buffers over the CPU link
+    s.set_direct_io(False)
+    staged_ms = advance_ms()
+    s.set_direct_io(True)
+    e2e_ms = advance_ms()
     if pg is not None:
-        t = torch.tensor([e2e_ms, three_ms], device="cuda", dtype=torch.float64)
+        t = torch.tensor([e2e_ms, three_ms, staged_ms], device="cuda", dtype=torch.float64)
         pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        e2e_ms, three_ms = float(t[0].item()), float(t[1].item())
+        e2e_ms, three_ms, staged_ms = float(t[0].item()), float(t[1].item()), float(t[2].item())
     e2e_value = world * n * e2e_steps / (e2e_ms * 1e-3)
     three_value = world * n * e2e_steps / (three_ms * 1e-3)
+    staged_value = world * n * e2e_steps / (staged_ms * 1e-3)
     # the host link's own rate for the same bytes (plain pinned copies, no kernels): the floor of
     # the end-to-end step's copy time
     dbuf = torch.empty(hin.numel(), dtype=torch.float64, device="cuda")
@@ -505,10 +515,10 @@ def run_ours(args):
     hbm, hbm_src = peaks()
     achieved = alg_bytes * n / (step_kernel_ms * 1e-3) / 1e9
     fp64_rate = s.probe_fp64()
+    prof = NCU_PROFILE.get((args.config, (tune[0], tune[1])))
     fp64_instr = None
-    if args.config == "flooding" and (tune[0], tune[1]) in NCU_FP64_INSTR_FLOODING_1M:
-        per_edge, per_element = NCU_FP64_INSTR_FLOODING_1M[(tune[0], tune[1])]
-        fp64_instr = per_edge * s.nedge + per_element * n
+    if prof:
+        fp64_instr = prof["fp64_per_edge"] * s.nedge + prof["fp64_per_element"] * n
     fp64_achieved = fp64_instr / (step_kernel_ms * 1e-3) if fp64_instr else None
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -519,33 +529,38 @@ def run_ours(args):
                    "scheme": {1: "HLLC", 2: "HLLC-Ata", 3: "WAF", 4: "MUSCL-Hancock"}[case.params["iflux"]],
                    "l2": "working set > L2 (no flush needed)", "parallelism": f"replicas x{world}",
                    "time_steps_ran": info.steps,
+                   "wet_fraction": {"start": wet_start, "end_of_timed_steps": wet_end},
                    "tuning": {"int_compare": tune[0], "int_mul_warps": tune[1], "trial_ms_per_step": tune[2]}},
         "roofline": {"bound": "hbm", "kernel": "one time step (k_edges + k_cells)",
                      "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "peak_source": f"MEASURED_PEAKS.json hbm_gbs ({hbm_src})",
                      "alg_bytes_per_tri": alg_bytes,
-                     "traffic": NCU_TRAFFIC_FLOODING_1M if args.config == "flooding" else None,
-                     "traffic_note": "ncu dram__bytes_read.sum + dram__bytes_write.sum per step "
-                                     "(k_edges + k_cells) of the 1M WAF step",
+                     "traffic": prof["traffic"] if prof else None,
+                     "traffic_note": ("from_profile: ncu dram__bytes_read.sum + dram__bytes_write.sum per step "
+                                      "(k_edges + k_cells) of this workload and setting, " + prof["source"])
+                                     if prof else "no ncu capture of this workload and setting",
                      "k_edges_ms": k_edges_ms, "k_cells_ms": k_cells_ms},
-        "fp64": {"bound": "FP64 pipe and dependent integer-pipe chains at 47 / 36 % warp occupancy (ncu: FP64 "
-                          "pipe 75 / 71 % and issue slots 49 / 32 % busy in k_edges / k_cells; HBM at 14-25 % "
-                          "of peak)",
-                 "peak_instr_per_s": fp64_rate,
+        "fp64": {"peak_instr_per_s": fp64_rate,
                  "peak_source": "cf_probe_fp64, measured live: independent FMA chains on every SM",
                  "instr_per_step": fp64_instr,
-                 "instr_source": "ncu sass__inst_executed_per_opcode of the same step (DADD+DMUL+DFMA+DSETP+F2F)",
                  "achieved_instr_per_s": fp64_achieved,
                  "frac": fp64_achieved / fp64_rate if fp64_achieved else None,
-                 "pipe_active_ncu": NCU_FP64_PIPE_FLOODING_1M if args.config == "flooding" else None,
-                 "issue_active_ncu": NCU_ISSUE_FLOODING_1M if args.config == "flooding" else None},
+                 "from_profile": ({"source": prof["source"], "fp64_per_edge": prof["fp64_per_edge"],
+                                   "fp64_per_element": prof["fp64_per_element"],
+                                   "fp64_pipe_active": prof["fp64_pipe"], "issue_active": prof["issue"]}
+                                  if prof else None),
+                 "note": "instr_per_step is the profile's FP64-pipe instruction count of this workload and "
+                         "setting; achieved divides it by the live kernel time"},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 24 * n, "d2h_bytes_per_step": 24 * n,
                 "steps": e2e_steps, "ms_per_step": e2e_ms / e2e_steps,
                 "link_h2d_gbs": 24 * n / (h2d_ms * 1e-3) / 1e9, "link_d2h_gbs": 24 * n / (d2h_ms * 1e-3) / 1e9,
                 "three_calls_value": three_value, "three_calls_ms_per_step": three_ms / e2e_steps,
+                "staged_value": staged_value, "staged_ms_per_step": staged_ms / e2e_steps,
                 "note": "per step: cf_advance (the state from pinned host memory, one step, the state back "
-                        "into pinned host memory, one wait); three_calls: the same as cf_set_state + "
-                        "cf_step + cf_get_state; link_*: plain pinned copies of the same bytes"},
+                        "into pinned host memory, one wait), the state kernels reading and writing the pinned "
+                        "buffers over the CPU link; staged: the same with cudaMemcpyAsync copies through a "
+                        "device staging buffer (cf_set_direct_io 0); three_calls: cf_set_state + cf_step + "
+                        "cf_get_state; link_*: plain pinned copies of the same bytes"},
         "gpu_launches": 2 * args.steps + 1,
         "clocks": clk.summary(),
     }

@@ -363,9 +363,28 @@ int member_ok(cf_ctx* c, int32_t m) {
   return CF_OK;
 }
 
-/* Set the state of member m from c->staging (reference order), resetting its time and steps. */
-/* the device work of setting member m's state from the staging buffer (stream-ordered, no wait) */
-int enqueue_set_state(cf_ctx* c, int32_t m, double t0) {
+/* The address through which the kernels on c's device reach the caller's buffer p: p itself for
+ * device or managed memory of that device, the mapped address for pinned host memory (GB300 reads
+ * and writes it over the coherent CPU link), NULL for anything else (pageable host memory, another
+ * device's memory, a pointer not aligned to 8 bytes, or direct access switched off): such buffers
+ * go through the staging buffer with a copy. */
+void* device_view(cf_ctx* c, const void* p) {
+  if (!c->direct_io || !p || ((uintptr_t)p & 7u)) return nullptr;
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  if (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged)
+    return a.device == c->device ? const_cast<void*>(p) : nullptr;
+  if (a.type == cudaMemoryTypeHost) return a.devicePointer;
+  return nullptr;
+}
+
+/* Set the state of member m, resetting its time and steps: from src (reference order, an address
+ * the device reaches, see device_view) or, with src NULL, from c->staging.  Stream-ordered, no
+ * wait; c->ev[3] completes once the caller's inputs have been read. */
+int enqueue_set_state(cf_ctx* c, int32_t m, double t0, const double* src = nullptr) {
   const Member& M = c->mem[m];
   const int p0 = (int)(c->launched & 1);
   MemberState s;
@@ -377,18 +396,25 @@ int enqueue_set_state(cf_ctx* c, int32_t m, double t0) {
   s.base = p0;
   c->host_state[m] = s;
   CF_CUDA(c, cudaMemcpyAsync(c->mst + m, c->host_state + m, sizeof(MemberState), cudaMemcpyHostToDevice, c->stream));
-  CF_CUDA(c, cudaEventRecord(c->ev[3], c->stream));   /* the host inputs (caller's state, member record) read */
-  int rc = launch_scatter_state(c->staging, c->perm + M.cell_off, c->zcell + M.cell_off, c->U[p0] + M.cell_off, M.n,
-                                reinterpret_cast<stream_t>(c->stream));
-  if (rc != CF_OK) return fail(c, rc, "state scatter launch failed");
+  int rc;
+  if (src) {
+    rc = launch_load_ref(src, c->iperm + M.cell_off, c->U[p0] + M.cell_off, M.n, reinterpret_cast<stream_t>(c->stream));
+    if (rc != CF_OK) return fail(c, rc, "state load launch failed");
+    CF_CUDA(c, cudaEventRecord(c->ev[3], c->stream));   /* the host inputs (caller's state, member record) read */
+  } else {
+    CF_CUDA(c, cudaEventRecord(c->ev[3], c->stream));   /* the host inputs (caller's state, member record) read */
+    rc = launch_scatter_state(c->staging, c->perm + M.cell_off, c->zcell + M.cell_off, c->U[p0] + M.cell_off, M.n,
+                              reinterpret_cast<stream_t>(c->stream));
+    if (rc != CF_OK) return fail(c, rc, "state scatter launch failed");
+  }
   rc = launch_cfl(c->U[p0], c->cstat, c->ctile_mem, M.ctile_begin, M.ctile_end - M.ctile_begin, c->mdev, c->mst, p0,
                   reinterpret_cast<stream_t>(c->stream));
   if (rc != CF_OK) return fail(c, rc, "cfl launch failed");
   return CF_OK;
 }
 
-int set_state_member(cf_ctx* c, int32_t m, double t0) {
-  const int rc = enqueue_set_state(c, m, t0);
+int set_state_member(cf_ctx* c, int32_t m, double t0, const double* src = nullptr) {
+  const int rc = enqueue_set_state(c, m, t0, src);
   if (rc != CF_OK) return rc;
   /* return once the host buffers are consumed; the scatter and the initial dt run on the stream
    * ahead of the next call's work (which every later call orders after) */
@@ -401,6 +427,7 @@ int set_state_host(cf_ctx* c, int32_t m, const double* hu3, double t0, cudaMemcp
   if (rc) return rc;
   if (!hu3) return fail(c, CF_EINVAL, "null state");
   CF_CUDA(c, cudaSetDevice(c->device));
+  if (const void* v = device_view(c, hu3)) return set_state_member(c, m, t0, static_cast<const double*>(v));
   CF_CUDA(c, cudaMemcpyAsync(c->staging, hu3, 3 * (size_t)c->mem[m].n * sizeof(double), kind, c->stream));
   return set_state_member(c, m, t0);
 }
@@ -454,6 +481,13 @@ int get_state_member(cf_ctx* c, int32_t m, double* dst, cudaMemcpyKind kind) {
   if (s.status & STATUS_NO_STATE) return fail(c, CF_ESTATE, "no state set");
   const Member& M = c->mem[m];
   const int buf = (int)((s.base + s.nstep) & 1);
+  if (void* v = device_view(c, dst)) {
+    rc = launch_store_ref(c->U[buf] + M.cell_off, nullptr, nullptr, 0, c->iperm + M.cell_off, static_cast<double*>(v),
+                          M.n, reinterpret_cast<stream_t>(c->stream));
+    if (rc != CF_OK) return fail(c, rc, "state store launch failed");
+    CF_CUDA(c, cudaStreamSynchronize(c->stream));
+    return CF_OK;
+  }
   rc = launch_gather_state(c->U[buf] + M.cell_off, c->iperm + M.cell_off, c->staging, M.n,
                            reinterpret_cast<stream_t>(c->stream));
   if (rc != CF_OK) return fail(c, rc, "gather launch failed");
@@ -924,20 +958,25 @@ int cf_advance(cf_ctx* c, const double* hu3_in, double t0, int32_t nsteps, doubl
   const stream_t st = reinterpret_cast<stream_t>(c->stream);
   /* one stream-ordered sequence, one wait: state in, initial dt, the steps, the current state out
    * (its buffer chosen on the device, so a member that stopped early returns where it stopped) */
-  CF_CUDA(c, cudaMemcpyAsync(c->staging, hu3_in, bytes, cudaMemcpyDefault, c->stream));
-  int rc = enqueue_set_state(c, 0, t0);
+  const double* vin = static_cast<const double*>(device_view(c, hu3_in));
+  double* vout = static_cast<double*>(device_view(c, hu3_out));
+  if (!vin) CF_CUDA(c, cudaMemcpyAsync(c->staging, hu3_in, bytes, cudaMemcpyDefault, c->stream));
+  int rc = enqueue_set_state(c, 0, t0, vin);
   if (rc == CF_OK) rc = enqueue_steps(c, nsteps);
   if (rc != CF_OK) {
     cudaStreamSynchronize(c->stream);
     return rc;
   }
-  rc = launch_gather_current(c->U[0] + M.cell_off, c->U[1] + M.cell_off, c->mst, 0, c->iperm + M.cell_off, c->staging,
-                             M.n, st);
+  if (vout)
+    rc = launch_store_ref(c->U[0] + M.cell_off, c->U[1] + M.cell_off, c->mst, 0, c->iperm + M.cell_off, vout, M.n, st);
+  else
+    rc = launch_gather_current(c->U[0] + M.cell_off, c->U[1] + M.cell_off, c->mst, 0, c->iperm + M.cell_off,
+                               c->staging, M.n, st);
   if (rc != CF_OK) {
     cudaStreamSynchronize(c->stream);
     return fail(c, rc, "gather launch failed");
   }
-  CF_CUDA(c, cudaMemcpyAsync(hu3_out, c->staging, bytes, cudaMemcpyDefault, c->stream));
+  if (!vout) CF_CUDA(c, cudaMemcpyAsync(hu3_out, c->staging, bytes, cudaMemcpyDefault, c->stream));
   return finish_steps(c, info);
 }
 
@@ -1014,6 +1053,12 @@ int cf_get_sizes(cf_ctx* c, int64_t* nelt, int64_t* nedge) {
 void* cf_get_stream(cf_ctx* c) { return c ? (void*)c->stream : nullptr; }
 
 const char* cf_last_error(const cf_ctx* c) { return c ? c->err.c_str() : g_create_error.c_str(); }
+
+int cf_set_direct_io(cf_ctx* c, int32_t enable) {
+  if (!c) return CF_EINVAL;
+  c->direct_io = enable != 0;
+  return CF_OK;
+}
 
 int cf_set_timing(cf_ctx* c, int32_t enable) {
   if (!c) return CF_EINVAL;

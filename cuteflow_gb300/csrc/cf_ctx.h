@@ -67,6 +67,7 @@ struct cf_ctx {
   int32_t xd_cmp = 0;                  /* edge kernel: integer comparisons (cf_set_tuning) */
   int32_t xd_mul_mask = 0;             /* edge kernel: warps multiplying on the integer pipes */
   cf::MemberState* host_state = nullptr;   /* pinned, one record per member */
+  bool direct_io = true;               /* kernels read / write callers' pinned host states directly */
   /* stepping */
   int64_t launched = 0;                /* steps launched since creation (buffer parity) */
   cudaGraphExec_t graph2 = nullptr;    /* two steps: parity 0 then 1 */

@@ -889,6 +889,57 @@ CF_HD CF_INLINE void write_slots(Slot* sa, const double o[10]) {
   sb->q = 0.0;
 }
 
+/* ---- dry regions ------------------------------------------------------------------------ */
+
+CF_HD CF_INLINE uint64_t dbits_hd(double x) {
+  uint64_t b;
+  memcpy(&b, &x, sizeof(b));
+  return b;
+}
+CF_HD CF_INLINE double dbl_hd(uint64_t b) {
+  double x;
+  memcpy(&x, &b, sizeof(x));
+  return x;
+}
+CF_HD CF_INLINE bool finite_u(uint64_t b) { return (b & 0x7ff0000000000000ull) != 0x7ff0000000000000ull; }
+
+/* The two slots of an interior edge whose elements both hold the depth +0 (bit pattern 0), for the
+ * first-order and WAF schemes (IFLUX 1-3), written without evaluating the edge.  The general
+ * evaluation gives, for any bed elevations and any upwind states:
+ *   - masked depths 0, hydrostatic depths max(0, (+0 + z) - max(z, z')) = +0 (the difference is
+ *     <= 0 or NaN, and max(0, .) returns the +0 operand), so the wave-speed routine sees both
+ *     depths below eps and the flux vector of side A is +0 in every component (side B's too, or
+ *     its negation -0 with flux_mode 1; the second first-order evaluation is skipped because the
+ *     masked and raw depths agree);
+ *   - the bed source (g/2 (ha^2 - h^2)) len with ha = h = +0: (g/2 * +0) * len, a zero with the
+ *     sign of g times the sign of len, then times nx, ny (side B negated).
+ * Every product of a zero and a finite number is the zero with the product of the signs, so the
+ * slots are these signed zeros whenever g, len, nx and ny are finite; otherwise (returns false)
+ * the caller evaluates the edge. */
+CF_HD CF_INLINE bool dry_edge_slots(double g, int flux_mode, const double4& geo, Slot* sa) {
+  const uint64_t S = 0x8000000000000000ull;
+  const uint64_t bg = dbits_hd(g), bnx = dbits_hd(geo.x), bny = dbits_hd(geo.y), bl = dbits_hd(geo.z);
+  if (!(finite_u(bg) & finite_u(bnx) & finite_u(bny) & finite_u(bl))) return false;
+  const uint64_t sl = bl & S;                              /* F.a * len */
+  const uint64_t sb = (flux_mode == 1) ? (sl ^ S) : sl;    /* F.b * len */
+  const uint64_t st = (bg & S) ^ sl;                       /* ta = tb = (g/2 * +0) * len */
+  Slot* sbp = sa + 1;
+  const double fa = dbl_hd(sl), fb = dbl_hd(sb);
+  sa->f1 = fa;
+  sa->f2 = fa;
+  sa->f3 = fa;
+  sa->bx = dbl_hd(st ^ (bnx & S));
+  sa->by = dbl_hd(st ^ (bny & S));
+  sa->q = 0.0;
+  sbp->f1 = fb;
+  sbp->f2 = fb;
+  sbp->f3 = fb;
+  sbp->bx = dbl_hd(st ^ (bnx & S) ^ S);
+  sbp->by = dbl_hd(st ^ (bny & S) ^ S);
+  sbp->q = 0.0;
+  return true;
+}
+
 /* Fluxes (times the edge length) and bed sources of edge e into its two slots, from the
  * state U of step n: the body of the edge kernel. */
 template <int IFLUX, class S = double>
@@ -896,8 +947,15 @@ CF_HD CF_INLINE void edge_body(const StepArgs& a, const MemberDev& M, int e, dou
                                const double* surf = nullptr) {
   const int2 ab = ldro(a.ecell + e);
   const double4 UA = ld4(a.Uin + ab.x);   /* {h, hu, hv, RN(1/h)} */
-  const double4 ez = ld4(a.ez + e);       /* bed of A, of B, of A's and B's upwind reconstructions */
   Slot* sa = a.slots + 2 * (size_t)e;
+
+  if (IFLUX <= 3 && ab.y >= 0) {
+    /* an edge between two dry elements (most of a flood plain that the water has not reached)
+     * needs neither its geometry beyond the normal nor its upwind states */
+    const double hB = ldro(reinterpret_cast<const double*>(a.Uin + ab.y));
+    if ((dbits_hd(UA.x) | dbits_hd(hB)) == 0 && dry_edge_slots(M.gp, a.flux_mode, ld4(a.egeo + e), sa)) return;
+  }
+  const double4 ez = ld4(a.ez + e);       /* bed of A, of B, of A's and B's upwind reconstructions */
 
   if (ab.y < 0) {
     const double4 geo = ld4(a.egeo + e);
@@ -1050,11 +1108,29 @@ CF_HD CF_INLINE void element_core(const MemberDev& M, double area, double yarea,
   }
 }
 
-/* The element kernel's body: st = {area, manning n, cfl*L_cfl, 1/area}.  Returns the new
- * state; sets *nonfinite when it is not finite. */
+/* True when the general update of an element provably returns the state (+0, +0, +0, +0) without
+ * flagging it non-finite: its depth is +-0, its discharges are finite, every flux and bed-source
+ * component of its three slots is +-0, its area is a positive normal number, dt is finite and
+ * tolisec >= 0.  Then every residual (0 + 0 - rc) / area and (sb + sf - rc) / area is +0 (the
+ * friction source of a dry element is +0), each new component is the old one plus +-0 (finite),
+ * and the new depth +-0 <= tolisec clamps the state to +0. */
+CF_HD CF_INLINE bool dry_element(const MemberDev& M, const double4& U, const double4& st, const Slot& s0,
+                                 const Slot& s1, const Slot& s2, double dt) {
+  const uint64_t z = (dbits_hd(s0.f1) | dbits_hd(s0.f2) | dbits_hd(s0.f3) | dbits_hd(s0.bx) | dbits_hd(s0.by) |
+                      dbits_hd(s1.f1) | dbits_hd(s1.f2) | dbits_hd(s1.f3) | dbits_hd(s1.bx) | dbits_hd(s1.by) |
+                      dbits_hd(s2.f1) | dbits_hd(s2.f2) | dbits_hd(s2.f3) | dbits_hd(s2.bx) | dbits_hd(s2.by) |
+                      dbits_hd(U.x)) << 1;
+  const uint64_t ba = dbits_hd(st.x);
+  const bool area_ok = (ba >> 52) - 1u < 2046u;   /* positive normal (the sign bit fails the test) */
+  const uint64_t btol = dbits_hd(M.tolisec);
+  const bool tol_ok = (btol >> 63) == 0 && (btol & 0x7fffffffffffffffull) <= 0x7ff0000000000000ull;  /* +0..+inf */
+  return z == 0 && area_ok && tol_ok && finite_u(dbits_hd(U.y)) && finite_u(dbits_hd(U.z)) && finite_u(dbits_hd(dt));
+}
+
+/* The element kernel's general body (element_update without its dry-region shortcut). */
 template <class S = double>
-CF_HD CF_INLINE double4 element_update(const MemberDev& M, const double4 U, const double4 st, const Slot& s0,
-                                       const Slot& s1, const Slot& s2, double dt, bool& nonfinite) {
+CF_HD CF_INLINE double4 element_update_full(const MemberDev& M, const double4 U, const double4 st, const Slot& s0,
+                                            const Slot& s1, const Slot& s2, double dt, bool& nonfinite) {
   /* fixed-order sums over the three edges (flux_riemann.cuf:411-426, source_terms.cuf:54-100) */
   const double rc1 = s0.f1 + s1.f1 + s2.f1;
   const double rc2 = s0.f2 + s1.f2 + s2.f2;
@@ -1067,6 +1143,19 @@ CF_HD CF_INLINE double4 element_update(const MemberDev& M, const double4 U, cons
   /* the new state carries RN(1/h) for the next step's quotients by h */
   const double hn = val(h);
   return make_double4(hn, val(hu), val(hv), hn > 0.0 ? val(S(1.0) / h) : 0.0);
+}
+
+/* The element kernel's body: st = {area, manning n, cfl*L_cfl, 1/area}.  Returns the new
+ * state; sets *nonfinite when it is not finite. */
+template <class S = double>
+CF_HD CF_INLINE double4 element_update(const MemberDev& M, const double4 U, const double4 st, const Slot& s0,
+                                       const Slot& s1, const Slot& s2, double dt, bool& nonfinite) {
+  if (dry_element(M, U, st, s0, s1, s2, dt)) {
+    /* a dry element that no water reaches this step (its edges carry no flux) */
+    nonfinite = false;
+    return make_double4(0.0, 0.0, 0.0, 0.0);
+  }
+  return element_update_full<S>(M, U, st, s0, s1, s2, dt, nonfinite);
 }
 
 }  // namespace cf

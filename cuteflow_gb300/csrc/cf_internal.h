@@ -193,6 +193,12 @@ int launch_gather_state(const double4* U, const int32_t* iperm_old2new, double* 
 /* launch_gather_state out of member m's current buffer, chosen on the device from mst[m] */
 int launch_gather_current(const double4* U0, const double4* U1, const MemberState* mst, int32_t m,
                           const int32_t* iperm, double* hu3, int32_t n, stream_t s);
+/* The same directly between a buffer the GPU can address (device memory, or pinned host memory over
+ * the CPU link) and U, coalesced on the buffer's side: load writes U[iperm[o]] from hu3[3 o ..];
+ * store reads U0 (or, with mst, member m's current buffer of U0 / U1) into hu3. */
+int launch_load_ref(const double* hu3, const int32_t* iperm_old2new, double4* U, int32_t n, stream_t s);
+int launch_store_ref(const double4* U0, const double4* U1, const MemberState* mst, int32_t m,
+                     const int32_t* iperm_old2new, double* hu3, int32_t n, stream_t s);
 /* (h, hu, hv) of listed elements (member-local reference ids, iperm member-local) */
 int launch_gather_ids(const double4* U, const int32_t* iperm, const int32_t* ids, double* out, int32_t n, stream_t s);
 int launch_scatter_ids(double4* U, const int32_t* iperm, const int32_t* ids, const double* in, int32_t n, stream_t s);

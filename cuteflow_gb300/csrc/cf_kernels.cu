@@ -341,6 +341,62 @@ __global__ void k_gather_current(const double4* U0, const double4* U1, const Mem
   hu3[3 * (size_t)o + 2] = u.z;
 }
 
+/* The state of one member between a caller's buffer in reference order, hu3[3 n], and U (new
+ * order), where hu3 is any address the GPU can reach: device memory or pinned host memory, which
+ * GB300 reads and writes over its coherent CPU link, so that no separate copy pass is needed.  A
+ * block moves 256 elements = 768 consecutive doubles of hu3 with fully coalesced loads or stores
+ * (one double per thread and instruction, three instructions) through shared memory; the element
+ * side is U[iperm[o]].  The store form takes its buffer from member m's record when mst is given
+ * (U[(base + nstep) & 1], as k_gather_current). */
+constexpr int REF_BLOCK = 256;
+
+__global__ void __launch_bounds__(REF_BLOCK) k_load_ref(const double* __restrict__ hu3, const int32_t* iperm,
+                                                        double4* U, int n) {
+  __shared__ double s[3 * REF_BLOCK];
+  const long long base = (long long)blockIdx.x * REF_BLOCK;
+  const long long nd = 3 * (long long)min(REF_BLOCK, (int)(n - base));
+  const double* src = hu3 + 3 * base;
+  #pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const int j = threadIdx.x + k * REF_BLOCK;
+    if (j < nd) s[j] = src[j];
+  }
+  __syncthreads();
+  const long long o = base + threadIdx.x;
+  if (o >= n) return;
+  const double h = s[3 * threadIdx.x], hu = s[3 * threadIdx.x + 1], hv = s[3 * threadIdx.x + 2];
+  double4* u = U + iperm[o];
+  reinterpret_cast<double2*>(u)[0] = make_double2(h, hu);
+  reinterpret_cast<double2*>(u)[1] = make_double2(hv, h > 0.0 ? 1.0 / h : 0.0);
+}
+
+__global__ void __launch_bounds__(REF_BLOCK) k_store_ref(const double4* U0, const double4* U1, const MemberState* mst,
+                                                         int m, const int32_t* iperm, double* __restrict__ hu3, int n) {
+  __shared__ double s[3 * REF_BLOCK];
+  const double4* U = U0;
+  if (mst) {
+    const MemberState& st = mst[m];
+    U = ((st.base + st.nstep) & 1) ? U1 : U0;
+  }
+  const long long base = (long long)blockIdx.x * REF_BLOCK;
+  const long long o = base + threadIdx.x;
+  if (o < n) {
+    const double2 a = __ldg(reinterpret_cast<const double2*>(U + iperm[o]));
+    const double b = __ldg(reinterpret_cast<const double*>(U + iperm[o]) + 2);
+    s[3 * threadIdx.x] = a.x;
+    s[3 * threadIdx.x + 1] = a.y;
+    s[3 * threadIdx.x + 2] = b;
+  }
+  __syncthreads();
+  const long long nd = 3 * (long long)min(REF_BLOCK, (int)(n - base));
+  double* dst = hu3 + 3 * base;
+  #pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const int j = threadIdx.x + k * REF_BLOCK;
+    if (j < nd) dst[j] = s[j];
+  }
+}
+
 /* (h, hu, hv) of the listed elements (member-local reference ids) out of / into U */
 __global__ void k_gather_ids(const double4* U, const int32_t* iperm, const int32_t* ids, double* out, int n) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -527,6 +583,20 @@ int launch_scatter_ids(double4* U, const int32_t* iperm, const int32_t* ids, con
 int launch_gather_current(const double4* U0, const double4* U1, const MemberState* mst, int32_t m,
                           const int32_t* iperm, double* hu3, int32_t n, stream_t s) {
   k_gather_current<<<(n + 255) / 256, 256, 0, reinterpret_cast<cudaStream_t>(s)>>>(U0, U1, mst, m, iperm, hu3, n);
+  return check(cudaGetLastError());
+}
+
+int launch_load_ref(const double* hu3, const int32_t* iperm, double4* U, int32_t n, stream_t s) {
+  if (n <= 0) return CF_OK;
+  k_load_ref<<<(n + REF_BLOCK - 1) / REF_BLOCK, REF_BLOCK, 0, reinterpret_cast<cudaStream_t>(s)>>>(hu3, iperm, U, n);
+  return check(cudaGetLastError());
+}
+
+int launch_store_ref(const double4* U0, const double4* U1, const MemberState* mst, int32_t m, const int32_t* iperm,
+                     double* hu3, int32_t n, stream_t s) {
+  if (n <= 0) return CF_OK;
+  k_store_ref<<<(n + REF_BLOCK - 1) / REF_BLOCK, REF_BLOCK, 0, reinterpret_cast<cudaStream_t>(s)>>>(U0, U1, mst, m,
+                                                                                                   iperm, hu3, n);
   return check(cudaGetLastError());
 }
 

@@ -7,14 +7,16 @@
  * The scratch is the array of 48-byte slots through which the edge kernel passes each edge
  * side's flux and bed source to the element kernel.  Here it is one file-scope array of
  * CF_NOALLOC_SCRATCH_SLOTS slots (16 MiB), present on every GPU that loads the library until
- * the process exits.  Its name is a host-side stand-in, not a device address: the address is
- * taken with cudaGetSymbolAddress once per device, on the first call with that device
- * current, and handed to the kernels as their slot pointer.  Calls share the array and race
- * if their work overlaps on the GPU.
+ * the process exits.  Its name is a host-side stand-in, not a device address: every call takes
+ * the address in the current device's context with cudaGetSymbolAddress (which allocates nothing;
+ * on a device's first call it can load the library's device code there) and hands it to the
+ * kernels as their slot pointer.  Looking it up on every call, rather than caching it per
+ * device, keeps it valid after cudaDeviceReset or under a context other than the primary one,
+ * where the module and its array are loaded again at another address.  Calls share the array
+ * and race if their work overlaps on the GPU.
  */
 #include <cuda_runtime.h>
 
-#include <mutex>
 #include <string>
 
 #include "cf_internal.h"
@@ -23,26 +25,14 @@ static __device__ __align__(256) cf::Slot g_noalloc_slots[CF_NOALLOC_SCRATCH_SLO
 
 namespace {
 
-constexpr int kMaxDevices = 64;
-std::mutex g_mu;
-cf::Slot* g_addr[kMaxDevices] = {};
-
-/* The device address of the array on the current device (looked up on first use). */
+/* The device address of the array in the current context. */
 int scratch_address(cf_ctx* c, cf::Slot** out) {
-  int dev = -1;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) return cf::ctx_error(c, CF_ECUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
-  if (dev < 0 || dev >= kMaxDevices) return cf::ctx_error(c, CF_ENOTSUP, "device index beyond 63");
-  std::lock_guard<std::mutex> lock(g_mu);
-  if (!g_addr[dev]) {
-    void* p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_noalloc_slots);
-    if (e != cudaSuccess || !p)
-      return cf::ctx_error(c, CF_ECUDA, std::string("cudaGetSymbolAddress of the static scratch: ") +
-                                            cudaGetErrorString(e));
-    g_addr[dev] = static_cast<cf::Slot*>(p);
-  }
-  *out = g_addr[dev];
+  void* p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_slots);
+  if (e != cudaSuccess || !p)
+    return cf::ctx_error(c, CF_ECUDA, std::string("cudaGetSymbolAddress of the static scratch: ") +
+                                          cudaGetErrorString(e));
+  *out = static_cast<cf::Slot*>(p);
   return CF_OK;
 }
 

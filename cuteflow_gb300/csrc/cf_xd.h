@@ -2,21 +2,27 @@
  * cf_xd.h -- binary64 arithmetic that keeps GB300's FP64 pipe for the operations only it can do.
  *
  * GB300 issues two FP64 operations per clock per SM; its integer pipes issue ~30x more 32-bit
- * operations, run beside the FP64 pipe, and sit idle in the step kernels (ncu: FP64 pipe 85 %
- * busy, ALU 1.4 %).  Two exact substitutions move FP64-pipe work onto them:
+ * operations, run beside the FP64 pipe, and sit idle in an all-FP64 step (ncu: FP64 pipe 85 %
+ * busy, ALU 1.4 %).  Exact substitutions move FP64-pipe work onto them:
  *
  *   comparisons  x < y etc. on ordered integer keys of the bit patterns (negative values
  *                mirrored, -0 and +0 one key, NaN compares false): the IEEE result, on the ALU;
  *   products     x * y by integer multiplication of the significands with round to nearest
- *                even (em_mul): the IEEE product for normal operands with a normal result; any
- *                other operand (zero, subnormal, infinite, NaN) or result (overflow,
- *                underflow) takes the FP64 instruction, in an out-of-line function so that the
- *                compiler does not evaluate it speculatively on the fast path.
+ *                even (em_mul);
+ *   quotients    a / b from a float reciprocal seed, a fixed-point refinement and the exact
+ *                remainder, which decides the rounding (em_div);
+ *   roots        sqrt(x) the same way from a float reciprocal-root seed (em_sqrt);
+ *   scalings     x / 2, x / 4, 2 x and negation as exponent-field and sign-bit operations.
+ * Each takes the FP64 instruction (out of line, so that the compiler does not evaluate it
+ * speculatively on the fast path) wherever the integer path does not cover the case: a zero,
+ * subnormal, infinite or NaN operand (a zero numerator of em_div is covered), a result outside
+ * the normal range, and, for em_div and em_sqrt, a remainder check that fails.
  *
- * XD<MUL> is a double that compares on integer keys and, with MUL, multiplies with em_mul;
- * sums, quotients and square roots stay FP64 instructions.  Every result is the IEEE binary64
- * result of the same operation, so code instantiated on XD<...> rounds exactly like the same
- * code on double; which warps use the integer multiply is a tuning choice, not a numerical one.
+ * XD<MUL> is a double that compares on integer keys and, with MUL, multiplies, divides (div_rn
+ * included) and takes square roots with em_mul, em_div and em_sqrt; sums stay FP64
+ * instructions.  Every result is the IEEE binary64 result of the same operation, so code
+ * instantiated on XD<...> rounds exactly like the same code on double; which warps use the
+ * integer arithmetic is a tuning choice, not a numerical one.
  */
 #ifndef CF_XD_H
 #define CF_XD_H

@@ -75,6 +75,7 @@ def load(build_if_missing: bool = True):
     L.cf_last_error.argtypes = [vp]
     L.cf_last_error.restype = C.c_char_p
     L.cf_set_timing.argtypes = [vp, C.c_int32]
+    L.cf_set_direct_io.argtypes = [vp, C.c_int32]
     L.cf_get_timing.argtypes = [vp, dp, dp, C.POINTER(C.c_int64)]
     ip = C.POINTER(C.c_int32)
     L.cf_create_batch.argtypes = [C.POINTER(_abi.CfMesh), C.POINTER(_abi.CfParams), C.c_int32, C.POINTER(vp)]
@@ -117,7 +118,7 @@ def load(build_if_missing: bool = True):
                  "cf_set_initial_condition", "cf_step", "cf_step_noalloc", "cf_run", "cf_set_tuning",
                  "cf_get_tuning", "cf_autotune", "cf_get_elements", "cf_set_elements", "cf_set_dt", "cf_get_state", "cf_get_state_device",
                  "cf_get_info", "cf_get_mesh_tables", "cf_mesh_tables", "cf_get_sizes", "cf_set_timing", "cf_get_timing",
-                 "cf_probe_fp64", "cf_selftest_xd", "cf_advance"):
+                 "cf_set_direct_io", "cf_probe_fp64", "cf_selftest_xd", "cf_advance"):
         getattr(L, name).restype = C.c_int
     _lib = L
     return L
@@ -318,6 +319,11 @@ class Solver:
 
     def set_timing(self, on: bool):
         self._check(self._L.cf_set_timing(self._ctx, 1 if on else 0))
+
+    def set_direct_io(self, on: bool):
+        """Kernels read and write pinned or device state buffers directly (default) or through
+        the staging copy (results identical)."""
+        self._check(self._L.cf_set_direct_io(self._ctx, 1 if on else 0))
 
     def timing(self):
         f, u, n = C.c_double(), C.c_double(), C.c_int64()

@@ -294,6 +294,15 @@ int cf_probe_fp64(cf_ctx* ctx, double* instr_per_s);
  * 8 bytes of device memory. */
 int cf_selftest_xd(cf_ctx* ctx, int64_t n, uint64_t seed, int64_t* mismatches);
 
+/* How cf_set_state, cf_get_state and cf_advance move a caller's state (no counterpart in the
+ * reference, which keeps the state on the device).  enable = 1 (the default): a state buffer
+ * the device can address (device memory, or pinned host memory, which GB300 reaches over its
+ * coherent CPU link) is read and written by the state kernels themselves, coalesced in the
+ * caller's element order, with no staging copy; pageable host memory is still copied through a
+ * device staging buffer.  enable = 0: every buffer goes through the staging copy.  The results
+ * are the same bytes either way. */
+int cf_set_direct_io(cf_ctx* ctx, int32_t enable);
+
 /* Kernel timing of the last cf_step call: total device milliseconds of the edge-flux and
  * cell-update kernels measured with CUDA events when timing is enabled. */
 int cf_set_timing(cf_ctx* ctx, int32_t enable);
@@ -390,8 +399,9 @@ int cf_zones_descend(cf_zones* z, double lr, double lo, double hi);
  *     each member's edges rounded up to a multiple of 128): about 116,000 triangles in one
  *     member.  A larger context is rejected with CF_EINVAL, the sizes in cf_last_error, and
  *     nothing is launched.
- *   - The first call on a device sets up that device's address of the array (which can load
- *     the library's device code there); make that first call before any stream capture.
+ *   - Every call looks up the array's address in the current device context (a lookup that
+ *     allocates nothing); the first call on a device can load the library's device code there,
+ *     so make that first call before any stream capture.
  *   - Every call on a device shares the one array, which keeps the last call's contents; a
  *     call clears the part it uses before its first step.  Calls whose work overlaps on the
  *     GPU (contexts stepped at the same time from several host threads) race on the array:

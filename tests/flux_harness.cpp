@@ -421,3 +421,102 @@ extern "C" int harness_tangent(const cf_mesh* m, const cf_params* p, const doubl
   }
   return 0;
 }
+
+/* The dry-region shortcuts of the step against the general evaluation they skip, on n random
+ * adversarial cases each: dry_edge_slots against interior_edge (IFLUX 1-3, every limiter, both
+ * flux modes, the three arithmetic types) for two elements of depth +0 with random beds (signed
+ * zeros, ties, infinities, NaN), random upwind states (wet ones too), random signs of g, nx, ny
+ * and len (zeros included); dry_element against element_update_full with random friction
+ * options, thresholds, areas, time steps and signed-zero slots.  Counts the cases a shortcut
+ * takes whose bits differ from the general result; *taken returns how many it took. */
+extern "C" long long harness_dry_check(long long n, unsigned long long seed, long long* taken) {
+  unsigned long long s = seed | 1;
+  auto rnd = [&]() { s ^= s << 13; s ^= s >> 7; s ^= s << 17; return s; };
+  auto unif = [&]() { return (double)(rnd() >> 11) * (1.0 / 9007199254740992.0); };
+  auto sgn = [&](double x) { return (rnd() & 1) ? -x : x; };
+  auto special = [&](double x) {
+    const unsigned k = (unsigned)(rnd() % 16);
+    if (k == 0) return 0.0;
+    if (k == 1) return -0.0;
+    if (k == 2) return (double)INFINITY;
+    if (k == 3) return -(double)INFINITY;
+    if (k == 4) return (double)NAN;
+    return x;
+  };
+  auto same = [](double a, double b) { return memcmp(&a, &b, 8) == 0; };
+  long long bad = 0, took = 0;
+  for (long long i = 0; i < n; ++i) {
+    /* ---- one edge ---- */
+    MemberDev M;
+    std::memset(&M, 0, sizeof(M));
+    M.gp = (rnd() % 8 == 0) ? special(sgn(9.81)) : sgn(0.5 + 20.0 * unif());
+    M.tolisec = (rnd() % 4 == 0) ? 0.0 : 1e-4 * unif();
+    EdgeGeo G;
+    G.nx = (rnd() % 6 == 0) ? sgn(0.0) : (rnd() % 20 == 0 ? special(1.0) : sgn(unif()));
+    G.ny = (rnd() % 6 == 0) ? sgn(0.0) : (rnd() % 20 == 0 ? special(1.0) : sgn(unif()));
+    G.len = (rnd() % 8 == 0) ? special(0.3) : 0.01 + 5.0 * unif();
+    G.d_mrl = 0.1 + unif(); G.y_mrl = 1.0 / G.d_mrl;
+    G.d_mkvol = 0.1 + unif(); G.y_mkvol = 1.0 / G.d_mkvol;
+    G.d_mkvoisin = 0.1 + unif(); G.y_mkvoisin = 1.0 / G.d_mkvoisin;
+    G.ysum_a = G.ysum_b = 0.5;
+    const double zl = (rnd() % 3 == 0) ? special(3.0 * unif()) : 3.0 * unif();
+    const double zr = (rnd() % 3 == 0) ? zl : ((rnd() % 3 == 0) ? special(3.0 * unif()) : 3.0 * unif());
+    const double up[4] = {(rnd() & 1) ? 2.0 * unif() : 0.0, sgn(unif()), (rnd() & 1) ? 2.0 * unif() : 0.0, sgn(unif())};
+    const double zu[2] = {3.0 * unif(), 3.0 * unif()};
+    const double dt = 1e-3 + unif();
+    const int iflux = 1 + (int)(rnd() % 3), ilim = (int)(rnd() % 5), fm = (int)(rnd() % 2), xd = (int)(rnd() % 3);
+    const double huA = sgn(unif()), hvA = sgn(unif()), huB = sgn(unif()), hvB = sgn(unif());
+    double o[10];
+    auto general = [&](auto tag) {
+      using T = decltype(tag);
+      T ot[10];
+      if (iflux == 1)
+        interior_edge<1, T>(M, ilim, fm, G, dt, T(0.0), T(huA), T(hvA), zl, 0.0, T(0.0), T(huB), T(hvB), zr, 0.0,
+                            T(up[0]), T(up[1]), zu[0], T(up[2]), T(up[3]), zu[1], ot);
+      else if (iflux == 2)
+        interior_edge<2, T>(M, ilim, fm, G, dt, T(0.0), T(huA), T(hvA), zl, 0.0, T(0.0), T(huB), T(hvB), zr, 0.0,
+                            T(up[0]), T(up[1]), zu[0], T(up[2]), T(up[3]), zu[1], ot);
+      else
+        interior_edge<3, T>(M, ilim, fm, G, dt, T(0.0), T(huA), T(hvA), zl, 0.0, T(0.0), T(huB), T(hvB), zr, 0.0,
+                            T(up[0]), T(up[1]), zu[0], T(up[2]), T(up[3]), zu[1], ot);
+      for (int k = 0; k < 10; ++k) o[k] = val(ot[k]);
+    };
+    if (xd == 0) general(0.0);
+    else if (xd == 1) general(XD<false>(0.0));
+    else general(XD<true>(0.0));
+    Slot sl[2];
+    if (dry_edge_slots(M.gp, fm, make_double4(G.nx, G.ny, G.len, G.d_mrl), sl)) {
+      ++took;
+      const double w[10] = {sl[0].f1, sl[0].f2, sl[0].f3, sl[0].bx, sl[0].by, sl[1].f1, sl[1].f2, sl[1].f3, sl[1].bx, sl[1].by};
+      bool ok = same(sl[0].q, 0.0) && same(sl[1].q, 0.0);
+      for (int k = 0; k < 10; ++k) ok = ok && same(w[k], o[k]);
+      if (!ok) ++bad;
+    }
+    /* ---- one element ---- */
+    M.friction = (int)(rnd() % 2);
+    M.fricimplic = (int)(rnd() % 3);
+    M.tol = 1e-6;
+    M.tolisec = (rnd() % 8 == 0) ? special(1e-4) : ((rnd() % 4 == 0) ? 0.0 : 1e-3 * unif());
+    const double area = (rnd() % 8 == 0) ? special(sgn(2.0)) : 0.1 + 4.0 * unif();
+    const double4 st = make_double4(area, 0.01 + 0.05 * unif(), 0.5 * unif(), 1.0 / area);
+    const double4 U = make_double4((rnd() % 8 == 0) ? 1e-5 * unif() : sgn(0.0), (rnd() % 10 == 0) ? special(0.5) : sgn(unif()),
+                                   (rnd() % 10 == 0) ? special(0.5) : sgn(unif()), 0.0);
+    Slot c[3];
+    for (int k = 0; k < 3; ++k) {
+      double* f = &c[k].f1;
+      for (int j = 0; j < 6; ++j) f[j] = sgn(0.0);
+      if (rnd() % 10 == 0) f[rnd() % 5] = sgn(1e-3 * unif());
+    }
+    const double dte = (rnd() % 10 == 0) ? special(0.05) : sgn(0.05 * unif());
+    if (dry_element(M, U, st, c[0], c[1], c[2], dte)) {
+      ++took;
+      bool nf = true;
+      const double4 V = xd == 0 ? element_update_full(M, U, st, c[0], c[1], c[2], dte, nf)
+                      : xd == 1 ? element_update_full<XD<false>>(M, U, st, c[0], c[1], c[2], dte, nf)
+                                : element_update_full<XD<true>>(M, U, st, c[0], c[1], c[2], dte, nf);
+      if (nf || !same(V.x, 0.0) || !same(V.y, 0.0) || !same(V.z, 0.0) || !same(V.w, 0.0)) ++bad;
+    }
+  }
+  if (taken) *taken = took;
+  return bad;
+}

@@ -15,7 +15,7 @@ The Divergent_Canal logs differ from the donnees.f next to them only in the prin
 (debitglob 0.5, H_sortie 0.02); the Manning override of each run is not printed.  The values used
 here (0.01 and 0.05) are the ones that reproduce the logged discharge to every printed digit.
 
-    python tests/golden/make_golden.py [/path/to/reference]
+    python tests/golden/make_golden.py /path/to/reference   (or CUTEFLOW_REFERENCE=/path/to/reference)
 """
 from __future__ import annotations
 
@@ -61,9 +61,11 @@ def read_table(path):
     return np.stack([a[:, 0:3], a[:, 3:6]], axis=2).astype(np.int32)  # boundary(k, j, 1:2), before walls
 
 
-# where the reference checkout is read from when no path is given (tests that read its case
-# directories directly, on a machine that has it, use the same default)
-DEFAULT_REFERENCE = "/root/reference"
+# where the reference checkout is read from when no path is given: the CUTEFLOW_REFERENCE
+# environment variable (tests that read its case directories directly use the same variable and
+# are skipped when it is unset)
+def reference_root():
+    return os.environ.get("CUTEFLOW_REFERENCE") or None
 
 
 def main(ref):
@@ -92,4 +94,7 @@ def main(ref):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else DEFAULT_REFERENCE)
+    root = sys.argv[1] if len(sys.argv) > 1 else reference_root()
+    if not root:
+        sys.exit("usage: make_golden.py /path/to/reference  (or set CUTEFLOW_REFERENCE)")
+    main(root)

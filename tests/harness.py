@@ -130,3 +130,14 @@ def tangent(case, params, U0, dU0, manning, dn, dt, t, gauges, freeze_r=False):
                            _abi.dptr(eta), _abi.dptr(deta), _abi.dptr(U), _abi.dptr(dU), int(bool(freeze_r)))
     assert rc == 0
     return eta, deta, U, dU
+
+
+def dry_check(n, seed=12345):
+    """(mismatches, shortcuts taken) of harness_dry_check: the dry-region shortcuts of the step
+    against the general evaluation on n adversarial edges and n adversarial elements."""
+    L = lib()
+    L.harness_dry_check.argtypes = [C.c_longlong, C.c_ulonglong, C.POINTER(C.c_longlong)]
+    L.harness_dry_check.restype = C.c_longlong
+    took = C.c_longlong(0)
+    bad = int(L.harness_dry_check(int(n), int(seed), C.byref(took)))
+    return bad, int(took.value)

@@ -163,14 +163,24 @@ def test_restart_file_layout(tmp_path):
     assert np.abs(r.U0 - U).max() <= 5e-7
 
 
-def _reference_case_dir(sub):
-    """A case directory of the reference checkout, where this machine has one (the path the golden
-    fixtures were made from); None elsewhere."""
+def _reference_root():
+    """The reference checkout named by CUTEFLOW_REFERENCE (the tree the golden fixtures were made
+    from), or None when the variable is unset."""
     import os
     import sys
     sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden"))
     import make_golden
-    d = os.path.join(make_golden.DEFAULT_REFERENCE, "Calibration_manning", "docs_calibration", sub)
+    return make_golden.reference_root()
+
+
+def _reference_case_dir(sub):
+    """A case directory of the reference checkout named by CUTEFLOW_REFERENCE; None when the
+    variable is unset or the directory is absent."""
+    import os
+    root = _reference_root()
+    if not root:
+        return None
+    d = os.path.join(root, "Calibration_manning", "docs_calibration", sub)
     return d if os.path.isfile(os.path.join(d, "donnees.f")) else None
 
 
@@ -183,7 +193,7 @@ def test_cgns_case_directories_of_the_reference(tmp_path, name, sub):
     with is_override_manning = 0 the per-element Manning n comes from the mesh's user data."""
     d = _reference_case_dir(sub)
     if d is None:
-        pytest.skip("the reference checkout is not on this machine")
+        pytest.skip("CUTEFLOW_REFERENCE does not name a reference checkout")
     import os
     import golden_cases as G
     g = G.load(name)
@@ -214,10 +224,9 @@ def test_cgns_mesh_without_boundary_lists(tmp_path):
     import os
     d = _reference_case_dir("River_piers/Froude")
     if d is None:
-        pytest.skip("the reference checkout is not on this machine")
-    import make_golden
+        pytest.skip("CUTEFLOW_REFERENCE does not name a reference checkout")
     from hdf5_min import H5
-    mesh = os.path.join(make_golden.DEFAULT_REFERENCE, "Calibration_manning", "Exemple2", "base_files", "mesh_6072.cgns")
+    mesh = os.path.join(_reference_root(), "Calibration_manning", "Exemple2", "base_files", "mesh_6072.cgns")
     (tmp_path / "donnees.f").write_text(
         f"&donnees_namelist\n is_cgns=1, meshfile_path='{os.path.dirname(mesh)}/', meshfile='mesh_6072.cgns',\n"
         " is_override_manning=1, override_manning=0.03,\n/\n")

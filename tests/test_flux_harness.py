@@ -149,3 +149,14 @@ def test_integer_product_is_the_ieee_product():
     """em_mul (cf_xd.h) against the hardware product on adversarial operands: normal and
     near-overflow/underflow exponents, all-ones and near-all-ones significands, ties."""
     assert H.mul_check(2_000_000, seed=3) == 0
+
+
+def test_dry_region_shortcuts_are_the_general_result():
+    """The edge kernel's shortcut for two elements of depth +0 and the element kernel's shortcut
+    for a dry element with zero slots return, bit for bit, what the general evaluation returns
+    (signed zeros included) on adversarial inputs: random signs of g, nx, ny, len, beds with
+    signed zeros, ties, infinities and NaN, wet upwind states, every scheme, limiter, flux mode,
+    friction option and arithmetic type."""
+    bad, took = H.dry_check(400_000, seed=7)
+    assert took > 200_000
+    assert bad == 0

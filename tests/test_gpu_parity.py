@@ -355,6 +355,48 @@ def test_set_state_consumes_a_pinned_buffer_before_returning(gpu_lib, oracle):
         assert np.array_equal(s.get_state(), ref["U"]) and info.t == ref["t"]
 
 
+@pytest.mark.parametrize("direct", [1, 0])
+def test_state_buffers_of_every_kind_move_the_same_bytes(gpu_lib, oracle, direct):
+    """cf_set_state / cf_get_state / cf_advance with pageable host memory, pinned host memory
+    (read and written by the state kernels over the CPU link when direct access is on) and device
+    memory, and cf_advance with one pinned buffer for input and output: every combination runs the
+    oracle's trajectory bit for bit."""
+    import ctypes
+    torch = pytest.importorskip("torch")
+    from cuteflow_gb300 import Solver
+    c = cases.flooding(70, 40, seed=5, iflux=3)
+    ref = oracle.run(c, 30)
+    U0 = np.ascontiguousarray(c.U0, dtype=np.float64)
+    dp = ctypes.POINTER(ctypes.c_double)
+    with Solver(c) as s:
+        s.set_direct_io(bool(direct))
+        pinned = torch.from_numpy(U0.copy()).pin_memory()
+        device = torch.from_numpy(U0.copy()).cuda()
+        for kind in ("pageable", "pinned", "device"):
+            if kind == "pageable":
+                s.set_state(U0)
+            elif kind == "pinned":
+                assert s._L.cf_set_state(s._ctx, ctypes.cast(pinned.data_ptr(), dp), 0.0) == 0
+            else:
+                s.set_state_device(device.data_ptr())
+            info = s.step(30)
+            assert info.t == ref["t"]
+            out_p = torch.zeros_like(pinned).pin_memory()
+            out_d = torch.zeros_like(device)
+            assert s._L.cf_get_state(s._ctx, ctypes.cast(out_p.data_ptr(), dp)) == 0
+            s.get_state_device(out_d.data_ptr())
+            torch.cuda.synchronize()
+            assert np.array_equal(out_p.numpy(), ref["U"]), kind
+            assert np.array_equal(out_d.cpu().numpy(), ref["U"]), kind
+            assert np.array_equal(s.get_state(), ref["U"]), kind
+        # cf_advance in place on one pinned buffer
+        buf = torch.from_numpy(U0.copy()).pin_memory()
+        info = _abi.CfStepInfo()
+        ptr = ctypes.cast(buf.data_ptr(), dp)
+        assert s._L.cf_advance(s._ctx, ptr, 0.0, 30, ptr, ctypes.byref(info)) == 0
+        assert np.array_equal(buf.numpy(), ref["U"]) and info.t == ref["t"]
+
+
 def test_fp64_probe_reports_a_plausible_rate(gpu_lib):
     """cf_probe_fp64 (the step's roofline denominator): GB300 issues ~2 FP64 instructions per
     clock per SM, ~6e11/s over 152 SMs at 2 GHz; the probe must land in that range and leave the

@@ -69,6 +69,26 @@ def test_noalloc_batch_and_shared_scratch(gpu_lib):
             assert np.array_equal(sa.get_state(), sb.get_state())
 
 
+def test_noalloc_allocates_no_device_memory(gpu_lib):
+    """The property the entry point exists for: once a first call has loaded the library's device
+    code and its static array on the device, further calls leave the device's free memory
+    (cudaMemGetInfo) exactly where it was."""
+    torch = pytest.importorskip("torch")
+    from cuteflow_gb300 import Solver
+    c = cases.flooding(60, 30, seed=12, iflux=3)
+    with Solver(c) as s:
+        s.set_state(c.U0)
+        _noalloc(gpu_lib, s, 3)
+        torch.cuda.synchronize()
+        free0, _ = torch.cuda.mem_get_info()
+        for n in (5, 8, 13):
+            _noalloc(gpu_lib, s, n)
+        torch.cuda.synchronize()
+        free1, _ = torch.cuda.mem_get_info()
+        assert free1 == free0
+        assert s.info().steps == 29
+
+
 def test_noalloc_rejects_a_context_beyond_the_scratch(gpu_lib):
     from cuteflow_gb300 import Solver
     c = cases.circular_dam_break(260, 260, iflux=1)     # 135,200 triangles: about 406,000 slots
