@@ -44,7 +44,12 @@ ALG_BYTES_HLLC = 128.0
 # sass__inst_executed_per_opcode), and the FP64-pipe and issue activity ncu reports.  They are
 # profile figures, not measured by this run: the bench line carries them under "from_profile" with
 # the summary they come from, and only for a (workload, setting) the capture covers.
-NCU_PROFILE = {}
+NCU_PROFILE = {
+    ("flooding", (1, 31)): {"traffic": 538.8e6, "fp64_per_edge": 66.0, "fp64_per_element": 23.7,
+                            "fp64_pipe": {"k_edges": 0.563, "k_cells": 0.477},
+                            "issue": {"k_edges": 0.550, "k_cells": 0.338},
+                            "source": "profiles/step_kernels_flooding_1M_WAF.md"},
+}
 
 
 def peaks():

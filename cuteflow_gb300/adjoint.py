@@ -36,16 +36,27 @@ class Adjoint:
     """Adjoint of ``nsteps`` steps of ``solver`` with gauge elements ``gauges`` (0-based,
     reference order).  ``solver`` is a Solver, or a Batch with ``gauge_member`` giving each
     gauge's member; states and gradients of a batch are concatenated in member order.
-    ``checkpoint_interval`` 0 keeps ceil(sqrt(N))."""
+    ``checkpoint_interval`` 0 keeps ceil(sqrt(N)).  ``budget_bytes`` > 0 chooses the memory
+    schedule that fits that much device memory (cf_adjoint_create_budget): the recording forward
+    keeps the step records of as many of the last steps as fit, so the backward pass replays only
+    the steps before them (none when the whole run fits); the gradient is the same bits."""
 
-    def __init__(self, solver, nsteps: int, gauges, checkpoint_interval: int = 0, gauge_member=None):
+    def __init__(self, solver, nsteps: int, gauges, checkpoint_interval: int = 0, gauge_member=None,
+                 budget_bytes: int = 0):
         self._L = load()
         self.solver = solver
         self.nsteps = int(nsteps)
         self.gauges = np.ascontiguousarray(gauges, dtype=np.int32).ravel()
         self._h = C.c_void_p()
         ip = C.POINTER(C.c_int32)
-        if gauge_member is None:
+        if budget_bytes > 0:
+            gm = None if gauge_member is None else np.ascontiguousarray(gauge_member, dtype=np.int32).ravel()
+            rc = self._L.cf_adjoint_create_budget(solver._ctx, self.nsteps, int(checkpoint_interval),
+                                                  None if gm is None else gm.ctypes.data_as(ip),
+                                                  self.gauges.ctypes.data_as(ip), int(self.gauges.size),
+                                                  int(budget_bytes), C.byref(self._h))
+            self.gauge_member = np.zeros_like(self.gauges) if gm is None else gm
+        elif gauge_member is None:
             rc = self._L.cf_adjoint_create(solver._ctx, self.nsteps, int(checkpoint_interval),
                                            self.gauges.ctypes.data_as(ip), int(self.gauges.size), C.byref(self._h))
             self.gauge_member = np.zeros_like(self.gauges)
@@ -64,6 +75,11 @@ class Adjoint:
         self._L.cf_adjoint_sizes(self._h, None, C.byref(k), C.byref(g), C.byref(b))
         self.checkpoint_interval = int(k.value)
         self.device_bytes = int(b.value)
+        st, ki, nc, nr = C.c_int32(), C.c_int32(), C.c_int32(), C.c_int32()
+        self._L.cf_adjoint_schedule(self._h, C.byref(st), C.byref(ki), C.byref(nc), C.byref(nr), None)
+        # steps whose records the recording forward keeps, checkpoints of the others, record pool
+        self.schedule = {"stored_steps": int(st.value), "checkpoint_interval": int(ki.value),
+                         "checkpoints": int(nc.value), "records": int(nr.value), "device_bytes": int(b.value)}
         self.generation = 0
 
     def set_linearization(self, freeze_limiter_ratios: bool):

@@ -340,35 +340,34 @@ def ensemble_member(index: int, seed: int = 3, n_min: int = 20000, n_max: int = 
 
 def calibration(nx: int = 500, ny: int = 200, seed: int = 4, nzones: int = 12, ngauges: int = 40,
                 iflux: int = 1):
-    """Manning calibration case: the flooding bathymetry and boundaries on an nx x ny quad grid
-    at the flooding case's 2 m spacing (500x200 -> 200,000 triangles), a true Manning field
-    piecewise constant over ``nzones`` Voronoi zones of seeded sites with n ~ U(0.02, 0.06),
-    and ``ngauges`` seeded gauge elements among the initially wet ones.
+    """Manning calibration case: the circular dam break's bed and boundaries (flat bed z = 0,
+    reflective walls) on an nx x ny quad grid at 2 m spacing (500x200 -> 200,000 triangles over
+    1000 m x 400 m), h = 10 m inside a circle of radius a quarter of the shorter side centred in
+    the domain and 1 m outside, u = v = 0; a true Manning field piecewise constant over
+    ``nzones`` Voronoi zones of seeded sites with n ~ U(0.02, 0.06), and ``ngauges`` seeded gauge
+    elements drawn uniformly over the mesh.  The dam-break wave crosses the whole domain within
+    the calibration run, so the flow, and with it the friction of every zone, reaches the gauges.
 
     First-order HLLC by default: over thousands of steps the gauge misfit of the WAF scheme is
     not a differentiable function of n (its limiters jump when the local depth difference
-    changes sign, superbee also at r = 0.5, 1, 2), while the first-order one is, wet/dry front
-    included, so gradients and finite differences agree.
+    changes sign, superbee also at r = 0.5, 1, 2), while the first-order one is, so gradients
+    and finite differences agree.
 
     Returns (case with the true field, zones [nelt] zone id of every element, true zone values
     [nzones], gauges [ngauges] element ids)."""
     lx, ly = 2.0 * nx, 2.0 * ny
-    # 8 bumps on the 1000 m x 400 m case, proportionally fewer on smaller domains (bumps 30-150 m
-    # wide would otherwise cover a small domain and leave it dry)
-    nbumps = int(round(8 * (lx * ly) / (1000.0 * 400.0)))
-    c = flooding(nx, ny, seed=seed, lx=lx, ly=ly, iflux=iflux, nbumps=nbumps)
+    c = circular_dam_break(nx, ny, seed=seed, lx=lx, ly=ly, iflux=iflux)
     xc, yc = cell_centroids(c.x, c.y, c.tri)
     sx = uniform(seed, 30, nzones, 0.0, lx)
     sy = uniform(seed, 31, nzones, 0.0, ly)
     zones = np.argmin((xc[:, None] - sx[None, :]) ** 2 + (yc[:, None] - sy[None, :]) ** 2, axis=1).astype(np.int32)
     nz = uniform(seed, 32, nzones, 0.02, 0.06)
     c.manning = nz[zones]
-    wet = np.flatnonzero(c.U0[:, 0] > 0.05)
-    pick = np.floor(uniform(seed, 33, ngauges, 0.0, 1.0) * wet.size).astype(np.int64)
-    gauges = np.unique(wet[pick])
+    pick = np.floor(uniform(seed, 33, ngauges, 0.0, 1.0) * c.nelt).astype(np.int64)
+    gauges = np.unique(pick)
     k = 34
     while gauges.size < ngauges:      # draw again on collisions
-        extra = wet[np.floor(uniform(seed, k, ngauges, 0.0, 1.0) * wet.size).astype(np.int64)]
+        extra = np.floor(uniform(seed, k, ngauges, 0.0, 1.0) * c.nelt).astype(np.int64)
         gauges = np.unique(np.concatenate([gauges, extra]))[:ngauges]
         k += 1
     c.name = f"calibration_{nx}x{ny}"

@@ -9,12 +9,19 @@
  * at its recorded value (the time step is not differentiated).  A caller with a non-linear
  * misfit passes its derivative with respect to eta and U^N as the weights (chain rule).
  *
- * Checkpointing.  The recording forward keeps the state every K steps (K ~ sqrt(N) by default).
- * The backward sweep walks the segments from the last: it recomputes the segment's states from
- * its checkpoint with the recorded dt sequence (bit-identical to the recorded run), keeping
- * every step's per-element flux and bed sums, and then runs the reverse steps through them.
- * Memory: ceil(N/K) + max(K, 2) states and max(K, 2) sum records (48 B per element each);
- * cost: one extra forward pass besides the reverse steps.
+ * Schedule.  A reverse step k needs the state U^k and every element's flux and bed sums at U^k
+ * (a step record: 32 + 48 bytes per element).  The recording forward keeps the records of the
+ * last T steps itself and a checkpoint state every K steps of the first M = N - T; the backward
+ * sweep runs the reverse steps of the stored tail directly, then walks the checkpointed
+ * segments from the last: it recomputes a segment's records from its checkpoint with the
+ * recorded dt sequence (bit-identical to the recorded run) into the same record pool and runs
+ * their reverse steps.  Cost: the reverse steps plus M replayed forward steps; memory: R = max(T,
+ * K, 2) records, ceil(M / K) checkpoints and two run states.  With no budget T = 0 and
+ * K = ceil(sqrt(N)) (or the caller's interval).  With a device-memory budget the schedule keeps
+ * the largest record pool that fits it: T = min(N, R) and K = R (or the caller's interval),
+ * every replay is saved when the whole run fits.  The gradient does not depend on the schedule:
+ * a record written by the recording forward and the same record written by a replay are the
+ * same bits.
  *
  * Batches.  On a context of several members the run, the checkpoints, the replay and the reverse
  * steps cover every member in the same launches, each with its own recorded dt (histories are
@@ -36,7 +43,11 @@ using namespace cf;
 
 struct cf_adjoint {
   cf_ctx* ctx = nullptr;
-  int32_t N = 0, K = 1, G = 0, nseg = 0, nseg_states = 2;
+  int32_t N = 0, K = 1, G = 0, nseg = 0, nseg_states = 2;   /* nseg_states: R, the record pool */
+  int32_t T = 0;             /* stored tail steps N - T .. N - 1 (records of the recording forward) */
+  int32_t Mc = 0;            /* checkpointed steps 0 .. Mc - 1 (Mc = N - T) */
+  int64_t bytes = 0;         /* device bytes of the adjoint */
+  double4* pp = nullptr;     /* two run states of the forward */
   int32_t nm = 1;            /* members */
   int64_t n_all = 0;         /* elements of all members */
   int32_t n_pad = 0;
@@ -79,7 +90,7 @@ struct cf_zones {
 namespace {
 
 void adj_free(cf_adjoint* a) {
-  void* ptrs[] = {a->ckpt, a->seg, a->mst, a->dt_hist, a->t_hist, a->eta, a->wbuf, a->gcell, a->goff, a->gidx,
+  void* ptrs[] = {a->pp, a->ckpt, a->seg, a->mst, a->dt_hist, a->t_hist, a->eta, a->wbuf, a->gcell, a->goff, a->gidx,
                   a->lam[0], a->lam[1], a->sums, a->cadj, a->eadj, a->uadj, a->uoff, a->uidx, a->gman, a->flag};
   for (void* p : ptrs)
     if (p) cudaFree(p);
@@ -103,7 +114,7 @@ void build_csr(int32_t n, const std::vector<int32_t>& elem, const std::vector<in
 }
 
 int create_impl(cf_ctx* c, int32_t nsteps, int32_t interval, const int32_t* gauge_member, const int32_t* gauges,
-                int32_t ngauges, cf_adjoint** out) {
+                int32_t ngauges, int64_t budget, cf_adjoint** out) {
   if (!out) return fail(c, CF_EINVAL, "out is NULL");
   *out = nullptr;
   if (c->iflux > 3) return fail(c, CF_ENOTSUP, "the adjoint covers iflux 1..3");
@@ -130,17 +141,55 @@ int create_impl(cf_ctx* c, int32_t nsteps, int32_t interval, const int32_t* gaug
   };
   a->ctx = c;
   a->N = nsteps;
-  a->K = interval > 0 ? std::min(interval, nsteps) : std::max(1, (int32_t)std::ceil(std::sqrt((double)nsteps)));
   a->G = ngauges;
-  a->nseg = (nsteps + a->K - 1) / a->K;
-  a->nseg_states = std::max(a->K, 2);
   a->nm = nm;
   for (const Member& M : c->mem) a->n_all += M.n;
   a->n_pad = c->n_pad;
   const size_t np = (size_t)c->n_pad, nep = (size_t)c->ne_pad;
   const bool second = c->iflux >= 3;
+  /* device bytes besides the record pool and the checkpoints (upper bound for the upwind lists) */
+  const int64_t st4 = (int64_t)np * (int64_t)sizeof(double4), rec = st4 + (int64_t)np * (int64_t)sizeof(Slot);
+  const int64_t fixed = 4 * st4 + (int64_t)np * (int64_t)sizeof(Slot) + 2 * (int64_t)nep * (int64_t)sizeof(double4) +
+                        (int64_t)np * 8 + (int64_t)nsteps * (16 * (int64_t)nm + 16 * (int64_t)ngauges) +
+                        (int64_t)(np + 1) * 4 + 8 * (int64_t)ngauges + (int64_t)nm * (int64_t)sizeof(MemberState) +
+                        (second ? 4 * (int64_t)nep * (int64_t)sizeof(double4) + (int64_t)(np + 1) * 4 +
+                                      4 * (int64_t)nep * 4
+                                : 0);
+  if (budget <= 0) {
+    a->T = 0;
+    a->K = interval > 0 ? std::min(interval, nsteps) : std::max(1, (int32_t)std::ceil(std::sqrt((double)nsteps)));
+    a->nseg_states = std::max(a->K, 2);
+  } else {
+    /* the largest record pool R whose schedule fits the budget: T = min(N, R) stored steps, the
+     * other M = N - T in checkpointed segments of K = R steps (or the caller's interval) */
+    int32_t best = 0;
+    for (int32_t R = nsteps; R >= 2; --R) {
+      const int32_t T = std::min(nsteps, R), M = nsteps - T;
+      const int32_t K = M > 0 ? (interval > 0 ? std::min(interval, R) : R) : 1;
+      const int64_t need = fixed + (int64_t)R * rec + (int64_t)((M + K - 1) / K) * st4;
+      if (need <= budget) {
+        best = R;
+        break;
+      }
+    }
+    if (best == 0) {
+      a->bytes = fixed + 2 * rec + (int64_t)((nsteps + 1) / 2) * st4;
+      adj_free(a);
+      delete a;
+      return fail(c, CF_ENOMEM, "adjoint memory budget of " + std::to_string(budget) +
+                                    " bytes is below this run's smallest schedule");
+    }
+    a->nseg_states = std::max(best, 2);
+    a->T = std::min(nsteps, best);
+    const int32_t M = nsteps - a->T;
+    a->K = M > 0 ? (interval > 0 ? std::min(interval, best) : best) : std::max(1, std::min(nsteps, best));
+  }
+  a->Mc = nsteps - a->T;
+  a->nseg = a->Mc > 0 ? (a->Mc + a->K - 1) / a->K : 0;
+  a->bytes = fixed + (int64_t)a->nseg_states * rec + (int64_t)a->nseg * st4;
   int rc;
-  if ((rc = dalloc(c, &a->ckpt, (size_t)a->nseg * np)) || (rc = dalloc(c, &a->seg, (size_t)a->nseg_states * np)) ||
+  if ((rc = dalloc(c, &a->pp, 2 * np)) || (rc = dalloc(c, &a->ckpt, (size_t)std::max(a->nseg, 1) * np)) ||
+      (rc = dalloc(c, &a->seg, (size_t)a->nseg_states * np)) ||
       (rc = dalloc(c, &a->mst, (size_t)nm)) || (rc = dalloc(c, &a->dt_hist, (size_t)nsteps * nm)) ||
       (rc = dalloc(c, &a->t_hist, (size_t)nsteps * nm)) || (rc = dalloc(c, &a->eta, (size_t)nsteps * ngauges)) ||
       (rc = dalloc(c, &a->wbuf, (size_t)nsteps * ngauges)) || (rc = dalloc(c, &a->gcell, (size_t)ngauges)) ||
@@ -238,7 +287,9 @@ int forward_impl(cf_adjoint* a, int32_t replay, double* eta_out, double* state_o
     }
     const Member& M = c->mem[i];
     const int cur = (int)((s.base + s.nstep) & 1);
-    CF_CUDA(c, cudaMemcpyAsync(a->seg + M.cell_off, c->U[cur] + M.cell_off, (size_t)M.n * sizeof(double4),
+    /* the run starts in a run state, or in the first record when every step is stored */
+    double4* X0 = a->Mc > 0 ? a->pp : a->seg;
+    CF_CUDA(c, cudaMemcpyAsync(X0 + M.cell_off, c->U[cur] + M.cell_off, (size_t)M.n * sizeof(double4),
                                cudaMemcpyDeviceToDevice, c->stream));
     if (cur != p0) {
       std::swap(s.dt[0], s.dt[1]);
@@ -250,13 +301,16 @@ int forward_impl(cf_adjoint* a, int32_t replay, double* eta_out, double* state_o
   if (!replay) CF_CUDA(c, cudaMemcpyAsync(a->mst, ms.data(), ms.size() * sizeof(MemberState), cudaMemcpyHostToDevice,
                                           c->stream));
   CF_CUDA(c, cudaMemsetAsync(a->flag, 0, sizeof(uint32_t), c->stream));
-  double4* X = a->seg;
-  double4* Y = a->seg + np;
+  const int32_t Mc = a->Mc;
+  double4* X = Mc > 0 ? a->pp : a->seg;
   int p = p0;
   for (int32_t k = 0; k < a->N; ++k) {
-    if (k % a->K == 0)
+    if (k < Mc && k % a->K == 0)
       CF_CUDA(c, cudaMemcpyAsync(a->ckpt + (size_t)(k / a->K) * np, X, np * sizeof(double4), cudaMemcpyDeviceToDevice,
                                  c->stream));
+    /* U^{k+1} into its record when that step is stored, else into the other run state */
+    double4* Y = (k + 1 >= Mc && k + 1 < a->N) ? a->seg + (size_t)(k + 1 - Mc) * np : (X == a->pp ? a->pp + np : a->pp);
+    Slot* sums = k >= Mc ? a->sums + (size_t)(k - Mc) * np : nullptr;
     StepArgs sa = step_args(c, p);
     sa.Uin = X;
     sa.Uout = Y;
@@ -264,14 +318,15 @@ int forward_impl(cf_adjoint* a, int32_t replay, double* eta_out, double* state_o
     if (!replay) {
       sa.mst = a->mst;
       if ((rc = launch_step(sa, st, nullptr, nullptr))) return fail(c, rc, "step launch failed");
+      if (sums && (rc = launch_slot_sums(sa, sums, st))) return fail(c, rc, "sums launch failed");
       rc = launch_record(Y, c->zcell, a->mst, a->nm, p, k, a->dt_hist, a->t_hist, a->gcell, a->G, a->eta, st);
     } else {
-      if ((rc = launch_replay_step(sa, a->dt_hist, a->t_hist, k, a->flag, nullptr, st)))
+      if ((rc = launch_replay_step(sa, a->dt_hist, a->t_hist, k, a->flag, sums, st)))
         return fail(c, rc, "replay launch failed");
       rc = launch_record(Y, c->zcell, nullptr, a->nm, 0, k, a->dt_hist, a->t_hist, a->gcell, a->G, a->eta, st);
     }
     if (rc) return fail(c, rc, "record launch failed");
-    std::swap(X, Y);
+    X = Y;
     p ^= 1;
   }
   if (state_out && (rc = gather_members(a, X, state_out, 3))) return rc;
@@ -322,28 +377,18 @@ int backward_impl(cf_adjoint* a, const double* w_eta, const double* w_state, dou
    * step (the edge contributions are gathered by the next reverse step, or the final pass). */
   bool first = true;
   AdjArgs A{};
-  for (int32_t j = a->nseg - 1; j >= 0; --j) {
-    const int32_t s0 = j * a->K, s1 = std::min(a->N, s0 + a->K);
-    CF_CUDA(c, cudaMemcpyAsync(a->seg, a->ckpt + (size_t)j * np, np * sizeof(double4), cudaMemcpyDeviceToDevice,
-                               c->stream));
-    /* replay the segment: its states and, for every step, the flux and bed sums at U^k */
-    for (int32_t i = 0; i < s1 - s0; ++i) {
-      StepArgs sa = step_args(c, 0);
-      sa.Uin = a->seg + (size_t)i * np;
-      sa.Uout = (i + 1 < s1 - s0) ? a->seg + (size_t)(i + 1) * np : nullptr;
-      if ((rc = launch_replay_step(sa, a->dt_hist, a->t_hist, s0 + i, a->flag, a->sums + (size_t)i * np, st)))
-        return fail(c, rc, "replay launch failed");
-    }
-    for (int32_t k = s1 - 1; k >= s0; --k) {
+  /* the reverse steps k = k1 - 1 .. k0 whose records r = k - k0 are in the pool */
+  auto reverse = [&](int32_t k0, int32_t k1) -> int {
+    for (int32_t k = k1 - 1; k >= k0; --k) {
       A = AdjArgs{};
       A.s = step_args(c, 0);
-      A.s.Uin = a->seg + (size_t)(k - s0) * np;
+      A.s.Uin = a->seg + (size_t)(k - k0) * np;
       A.s.Uout = nullptr;
       A.dt_hist = a->dt_hist;
       A.t_hist = a->t_hist;
       A.n = k;
       A.gather = first ? 0 : 1;
-      A.sums = a->sums + (size_t)(k - s0) * np;
+      A.sums = a->sums + (size_t)(k - k0) * np;
       A.lam_init = a->lam[0];
       A.lam_own = a->lam[1];
       A.cadj = a->cadj;
@@ -357,9 +402,27 @@ int backward_impl(cf_adjoint* a, const double* w_eta, const double* w_state, dou
       A.gw = (weights && k + 1 < a->N) ? a->wbuf + (size_t)k * a->G : nullptr;
       A.gman = a->gman;
       A.freeze_r = a->freeze_r;
-      if ((rc = launch_adjoint_step(A, st))) return fail(c, rc, "adjoint launch failed");
+      const int r = launch_adjoint_step(A, st);
+      if (r) return fail(c, r, "adjoint launch failed");
       first = false;
     }
+    return CF_OK;
+  };
+  /* the tail the recording forward stored: no replay */
+  if (a->T > 0 && (rc = reverse(a->Mc, a->N))) return rc;
+  for (int32_t j = a->nseg - 1; j >= 0; --j) {
+    const int32_t s0 = j * a->K, s1 = std::min(a->Mc, s0 + a->K);
+    CF_CUDA(c, cudaMemcpyAsync(a->seg, a->ckpt + (size_t)j * np, np * sizeof(double4), cudaMemcpyDeviceToDevice,
+                               c->stream));
+    /* replay the segment: its states and, for every step, the flux and bed sums at U^k */
+    for (int32_t i = 0; i < s1 - s0; ++i) {
+      StepArgs sa = step_args(c, 0);
+      sa.Uin = a->seg + (size_t)i * np;
+      sa.Uout = (i + 1 < s1 - s0) ? a->seg + (size_t)(i + 1) * np : nullptr;
+      if ((rc = launch_replay_step(sa, a->dt_hist, a->t_hist, s0 + i, a->flag, a->sums + (size_t)i * np, st)))
+        return fail(c, rc, "replay launch failed");
+    }
+    if ((rc = reverse(s0, s1))) return rc;
   }
   if ((rc = launch_adjoint_final(A, st))) return fail(c, rc, "adjoint launch failed");
   double4* Lin = a->lam[1];
@@ -396,14 +459,37 @@ int cf_set_manning(cf_ctx* c, const double* n_elt) {
 int cf_adjoint_create(cf_ctx* ctx, int32_t nsteps, int32_t checkpoint_interval, const int32_t* gauges,
                       int32_t ngauges, cf_adjoint** out) {
   if (!ctx) return CF_EINVAL;
-  return abi_guard(ctx, [&] { return create_impl(ctx, nsteps, checkpoint_interval, nullptr, gauges, ngauges, out); });
+  return abi_guard(ctx, [&] { return create_impl(ctx, nsteps, checkpoint_interval, nullptr, gauges, ngauges, 0, out); });
 }
 
 int cf_adjoint_create_batch(cf_ctx* ctx, int32_t nsteps, int32_t checkpoint_interval, const int32_t* gauge_member,
                             const int32_t* gauges, int32_t ngauges, cf_adjoint** out) {
   if (!ctx) return CF_EINVAL;
   if (ngauges > 0 && !gauge_member) return fail(ctx, CF_EINVAL, "gauge_member is NULL");
-  return abi_guard(ctx, [&] { return create_impl(ctx, nsteps, checkpoint_interval, gauge_member, gauges, ngauges, out); });
+  return abi_guard(ctx, [&] {
+    return create_impl(ctx, nsteps, checkpoint_interval, gauge_member, gauges, ngauges, 0, out);
+  });
+}
+
+int cf_adjoint_create_budget(cf_ctx* ctx, int32_t nsteps, int32_t checkpoint_interval, const int32_t* gauge_member,
+                             const int32_t* gauges, int32_t ngauges, int64_t budget_bytes, cf_adjoint** out) {
+  if (!ctx) return CF_EINVAL;
+  if (budget_bytes <= 0) return fail(ctx, CF_EINVAL, "budget_bytes <= 0");
+  if (ngauges > 0 && !gauge_member && ctx->mem.size() > 1) return fail(ctx, CF_EINVAL, "gauge_member is NULL");
+  return abi_guard(ctx, [&] {
+    return create_impl(ctx, nsteps, checkpoint_interval, gauge_member, gauges, ngauges, budget_bytes, out);
+  });
+}
+
+int cf_adjoint_schedule(cf_adjoint* a, int32_t* stored_steps, int32_t* checkpoint_interval, int32_t* checkpoints,
+                        int32_t* records, int64_t* device_bytes) {
+  if (!a) return CF_EINVAL;
+  if (stored_steps) *stored_steps = a->T;
+  if (checkpoint_interval) *checkpoint_interval = a->K;
+  if (checkpoints) *checkpoints = a->nseg;
+  if (records) *records = a->nseg_states;
+  if (device_bytes) *device_bytes = a->bytes;
+  return CF_OK;
 }
 
 void cf_adjoint_destroy(cf_adjoint* a) {
@@ -462,14 +548,7 @@ int cf_adjoint_sizes(cf_adjoint* a, int32_t* nsteps, int32_t* interval, int32_t*
   if (nsteps) *nsteps = a->N;
   if (interval) *interval = a->K;
   if (ngauges) *ngauges = a->G;
-  if (device_bytes) {
-    const int64_t np = a->n_pad, nep = a->ctx->ne_pad;
-    int64_t b = (int64_t)(a->nseg + a->nseg_states + 2) * np * (int64_t)sizeof(double4) +
-                (int64_t)(a->nseg_states + 1) * np * (int64_t)sizeof(Slot) +
-                2 * nep * (int64_t)sizeof(double4) + np * 8 + (int64_t)a->N * (16 * (int64_t)a->nm + 16 * (int64_t)a->G);
-    if (a->uadj) b += 4 * nep * (int64_t)sizeof(double4);
-    *device_bytes = b;
-  }
+  if (device_bytes) *device_bytes = a->bytes;
   return CF_OK;
 }
 

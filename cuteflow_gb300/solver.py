@@ -96,6 +96,8 @@ def load(build_if_missing: bool = True):
     L.cf_adjoint_set_dt.argtypes = [vp, vp, vp]
     L.cf_adjoint_sizes.argtypes = [vp, ip, ip, ip, C.POINTER(C.c_int64)]
     L.cf_adjoint_set_linearization.argtypes = [vp, C.c_int32]
+    L.cf_adjoint_create_budget.argtypes = [vp, C.c_int32, C.c_int32, ip, ip, C.c_int32, C.c_int64, vpp]
+    L.cf_adjoint_schedule.argtypes = [vp, ip, ip, ip, ip, C.POINTER(C.c_int64)]
     L.cf_adjoint_create_batch.argtypes = [vp, C.c_int32, C.c_int32, ip, ip, C.c_int32, vpp]
     L.cf_member_set_manning.argtypes = [vp, C.c_int32, vp]
     L.cf_zones_create.argtypes = [vp, ip, C.c_int32, vpp]
@@ -105,7 +107,7 @@ def load(build_if_missing: bool = True):
     L.cf_zones_get.argtypes = [vp, vp, vp]
     L.cf_zones_gradient.argtypes = [vp, vp, vp]
     L.cf_zones_descend.argtypes = [vp, C.c_double, C.c_double, C.c_double]
-    for name in ("cf_adjoint_create_batch", "cf_member_set_manning", "cf_zones_create", "cf_zones_set",
+    for name in ("cf_adjoint_create_budget", "cf_adjoint_schedule", "cf_adjoint_create_batch", "cf_member_set_manning", "cf_zones_create", "cf_zones_set",
                  "cf_zones_get", "cf_zones_gradient", "cf_zones_descend"):
         getattr(L, name).restype = C.c_int
     for name in ("cf_set_manning", "cf_adjoint_create", "cf_adjoint_forward", "cf_adjoint_backward",

@@ -337,6 +337,20 @@ int cf_adjoint_create(cf_ctx* ctx, int32_t nsteps, int32_t checkpoint_interval, 
  * ([sum of nelt] elements); the dt / time histories are [N][members]. */
 int cf_adjoint_create_batch(cf_ctx* ctx, int32_t nsteps, int32_t checkpoint_interval, const int32_t* gauge_member,
                             const int32_t* gauges, int32_t ngauges, cf_adjoint** out);
+/* The adjoint (one member: gauge_member may be NULL; a batch: as cf_adjoint_create_batch) with
+ * its memory schedule chosen to fit budget_bytes of device memory (no counterpart in the
+ * reference).  A reverse step needs the state and every element's flux and bed sums of its
+ * forward step (a record, 80 bytes per element); the recording forward keeps the records of the
+ * last steps itself, as many as fit, so that the backward pass replays only the steps before
+ * them, from checkpoints every checkpoint_interval steps (0: as long as the record pool).  When
+ * the whole run fits nothing is replayed.  CF_ENOMEM when no schedule fits.  The gradient is the
+ * same, bit for bit, under every schedule. */
+int cf_adjoint_create_budget(cf_ctx* ctx, int32_t nsteps, int32_t checkpoint_interval, const int32_t* gauge_member,
+                             const int32_t* gauges, int32_t ngauges, int64_t budget_bytes, cf_adjoint** out);
+/* The schedule: steps whose records the recording forward keeps (the last stored_steps), the
+ * checkpoint interval and count of the steps before them, the record pool, device bytes. */
+int cf_adjoint_schedule(cf_adjoint* adj, int32_t* stored_steps, int32_t* checkpoint_interval, int32_t* checkpoints,
+                        int32_t* records, int64_t* device_bytes);
 void cf_adjoint_destroy(cf_adjoint* adj);
 
 /* N steps from the context's current state (which is left unchanged).  replay 0: the dt of

@@ -156,6 +156,51 @@ def test_gradient_independent_of_checkpoint_interval(gpu_lib):
 
 
 @pytest.mark.parametrize("case", ["waf_flood", "hllc_dam"])
+def test_gradient_independent_of_memory_budget(gpu_lib, case):
+    """cf_adjoint_create_budget: the recording forward keeps the step records of the last steps
+    that fit the budget (all of them, some, or none beyond the minimum), the backward replays only
+    the rest; every schedule, with or without a checkpoint interval, gives the gradient of the
+    plain sqrt(N) schedule bit for bit, and a budget below every schedule is CF_ENOMEM."""
+    from cuteflow_gb300.adjoint import Adjoint
+    from cuteflow_gb300.solver import CFError
+    c, extra, s, adj, w_eta, w_state = _setup(case, nsteps=23)
+    with s:
+        adj.close()
+        with Adjoint(s, 23, adj.gauges, 0) as a:
+            s.set_state(c.U0)
+            eta_ref, U_ref = a.forward()
+            ref = a.backward(w_eta, w_state)
+        with Adjoint(s, 23, adj.gauges, 0, budget_bytes=1 << 40) as a:
+            full = a.device_bytes
+            assert a.schedule["stored_steps"] == 23 and a.schedule["checkpoints"] == 0
+        stored = set()
+        for frac, k in ((1.0, 0), (0.8, 0), (0.6, 0), (0.45, 0), (0.6, 4), (0.3, 0)):
+            try:
+                a = Adjoint(s, 23, adj.gauges, k, budget_bytes=int(full * frac))
+            except CFError as e:
+                assert e.code == -3
+                continue
+            with a:
+                assert a.device_bytes <= int(full * frac)
+                sc = a.schedule
+                rest = 23 - sc["stored_steps"]
+                assert sc["checkpoints"] == (0 if rest == 0 else -(-rest // sc["checkpoint_interval"]))
+                stored.add(sc["stored_steps"])
+                s.set_state(c.U0)
+                eta, U = a.forward()
+                assert np.array_equal(eta, eta_ref) and np.array_equal(U, U_ref)
+                gU, gn = a.backward(w_eta, w_state)
+                assert np.array_equal(gU, ref[0]) and np.array_equal(gn, ref[1]), (frac, k, sc)
+                # a second backward of the same forward (the records are still there)
+                gU2, gn2 = a.backward(w_eta, w_state)
+                assert np.array_equal(gU2, ref[0]) and np.array_equal(gn2, ref[1])
+        assert 23 in stored and any(0 < t < 23 for t in stored)
+        with pytest.raises(CFError) as e:
+            Adjoint(s, 23, adj.gauges, 0, budget_bytes=1024)
+        assert e.value.code == -3
+
+
+@pytest.mark.parametrize("case", ["waf_flood", "hllc_dam"])
 def test_gradient_independent_of_integer_pipe_setting(gpu_lib, case):
     """The recording forward and the segment replays run the step's kernels in the context's
     integer-pipe setting; every setting rounds identically, so the gradient is the same bit for bit."""
