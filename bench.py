@@ -222,18 +222,21 @@ def ensemble(nmembers: int, steps: int, warmup: int, seed: int = 3):
             "tuning": {"int_compare": tune[0], "int_mul_warps": tune[1]}}
 
 
-def adjoint_leg(steps: int, warmup: int, obs_every: float = 10.0):
+def adjoint_leg(steps: int, warmup: int, obs_every: float = 10.0, budget_gb: float = 64.0):
     """Adjoint Manning calibration: cost of one gradient against one forward.
 
-    Case: 500x200 quads (200,000 triangles) over the flooding bathymetry and boundaries,
+    Case: 500x200 quads (200,000 triangles) with the circular dam break's flat bed and walls,
     first-order HLLC, true Manning field piecewise constant on 12 seeded Voronoi zones, 40
     seeded gauges observed every 10 s of simulated time.  The gradient is taken at the
     calibration's initial guess n = 0.035 with the objective sum (eta - eta_obs)^2 over the
-    observations; ~sqrt(N) checkpoints.  Timed with CUDA events on the solver's stream:
+    observations, with the memory schedule that fits budget_gb of device memory (the recording
+    forward keeps the step records of as many of the last steps as fit; the backward replays
+    only the others).  Timed with CUDA events on the solver's stream:
       forward   : N plain steps (cf_step),
-      record    : the recording forward (cf_adjoint_forward: steps + gauges + checkpoints),
-      backward  : cf_adjoint_backward (segment replays + reverse steps).
-    ratio = (record + backward) / forward, the cost of a gradient in forward runs."""
+      record    : the recording forward (cf_adjoint_forward: steps + gauges + records/checkpoints),
+      backward  : cf_adjoint_backward (replays of the checkpointed steps + reverse steps).
+    ratio = (record + backward) / forward, the cost of a gradient in forward runs.  The same
+    gradient with the sqrt(N) checkpoint schedule (no budget) is timed beside it."""
     import torch
     from cuteflow_gb300 import Solver, cases
     from cuteflow_gb300.adjoint import Adjoint, zone_gradient
@@ -243,7 +246,7 @@ def adjoint_leg(steps: int, warmup: int, obs_every: float = 10.0):
     s.set_state(c.U0)
     tune = s.autotune(20)   # the forward, the recording forward and the replays all run this setting
     stream = torch.cuda.ExternalStream(s.stream())
-    adj = Adjoint(s, steps, gauges, 0)
+    adj = Adjoint(s, steps, gauges, 0, budget_bytes=int(budget_gb * (1 << 30)))
 
     def timed(fn):
         torch.cuda.synchronize()
@@ -277,28 +280,43 @@ def adjoint_leg(steps: int, warmup: int, obs_every: float = 10.0):
     (gU, gn), bwd_ms = timed(lambda: adj.backward(w))
     gz = zone_gradient(gn, zones, nz_true.size)
     ok = bool(np.isfinite(gn).all() and np.isfinite(gU).all())
+    sched = dict(adj.schedule)
+    adj.close()
+    # the sqrt(N) checkpoint schedule: same gradient, one replay of every step in the backward
+    with Adjoint(s, steps, gauges, 0) as a2:
+        s.set_state(c.U0)
+        (_, _), rec2_ms = timed(lambda: a2.forward())
+        (gU2, gn2), bwd2_ms = timed(lambda: a2.backward(w))
+        same = bool(np.array_equal(gn2, gn) and np.array_equal(gU2, gU))
+        sched2 = dict(a2.schedule)
     out = {"workload": c.name, "triangles": c.nelt, "scheme": "HLLC", "steps": steps,
-           "checkpoint_interval": adj.checkpoint_interval, "gauges": int(gauges.size),
-           "observations": int(obs.size), "device_bytes": adj.device_bytes,
+           "schedule": sched, "budget_gb": budget_gb, "gauges": int(gauges.size),
+           "observations": int(obs.size), "device_bytes": sched["device_bytes"],
            "forward_ms": fwd_ms, "record_ms": rec_ms, "backward_ms": bwd_ms,
            "ratio": (rec_ms + bwd_ms) / fwd_ms, "ratio_target": 5.0,
            "forward_value": c.nelt * steps / (fwd_ms * 1e-3),
            "gradient_value": c.nelt * steps / ((rec_ms + bwd_ms) * 1e-3), "unit": UNIT,
-           "misfit": misfit, "zone_gradient": [float(x) for x in gz], "finite": ok,
+           "misfit": misfit, "zone_gradient": [float(x) for x in gz],
+           "zones_with_zero_gradient": int(np.sum(gz == 0.0)), "finite": ok,
+           "sqrt_schedule": {"schedule": sched2, "record_ms": rec2_ms, "backward_ms": bwd2_ms,
+                             "ratio": (rec2_ms + bwd2_ms) / fwd_ms, "gradient_bit_identical": same},
            "tuning": {"int_compare": tune[0], "int_mul_warps": tune[1]}}
-    adj.close()
     s.close()
     return out
 
 
-def calibration_batch_leg(ninst: int, steps: int, iters: int, obs_every: float = 10.0, full: bool = False):
+def calibration_batch_leg(ninst: int, steps: int, iters: int, obs_every: float = 10.0, full: bool = False,
+                          budget_gb: float = 120.0):
     """Batched adjoint calibration (a sample of the 64-instance workload): ninst instances of the
     calibration case with seeded sizes, zone fields and gauges, in one batch context; every
     gradient-descent iteration runs one recording forward and one backward for all instances in
     the same launches, sums dJ/dn per zone and steps the zone values on the device.  Timed
     against the same instances' one-member adjoints run one after another (forward, backward,
     zone gradient and step each).  Misfit: sum of squared gauge misfits every obs_every s.
-    Instance meshes: 8k-39k triangles for the sample, 50k-273k with full (the workload's sizes)."""
+    Instance meshes: 8k-39k triangles for the sample, 50k-273k with full (the workload's sizes).
+    The batch's adjoint keeps to budget_gb of device memory (its schedule stores the step records
+    of as many of the last steps as fit and replays the rest); each instance run alone gets the
+    same cap."""
     import torch
     from cuteflow_gb300 import Batch, Solver, cases
     from cuteflow_gb300.adjoint import Adjoint, Zones
@@ -316,8 +334,10 @@ def calibration_batch_leg(ninst: int, steps: int, iters: int, obs_every: float =
     true_vals = np.concatenate([nz for _, _, nz, _ in inst])
     gm = np.concatenate([np.full(len(g), i, np.int32) for i, (_, _, _, g) in enumerate(inst)])
     gg = np.concatenate([g for *_, g in inst]).astype(np.int32)
+    budget = int(budget_gb * (1 << 30))
     b = Batch([c for c, *_ in inst])
-    adj = Adjoint(b, steps, gg, 0, gauge_member=gm)
+    adj = Adjoint(b, steps, gg, 0, gauge_member=gm, budget_bytes=budget)
+    sched = dict(adj.schedule)
     zs = Zones(b, zone_all, int(zoff[-1]))
 
     def start():
@@ -360,7 +380,7 @@ def calibration_batch_leg(ninst: int, steps: int, iters: int, obs_every: float =
     t_seq = 0.0
     for i, (c, zones, nz, gauges) in enumerate(inst):
         s = Solver(c)
-        a1 = Adjoint(s, steps, gauges, 0)
+        a1 = Adjoint(s, steps, gauges, 0, budget_bytes=budget)
         z1 = Zones(s, zones, len(nz))
         z1.set(vals0[zoff[i]:zoff[i + 1]])
         obs_i, mask_i = eta_obs[:, col[i]:col[i + 1]], mask[:, col[i]:col[i + 1]]
@@ -376,6 +396,7 @@ def calibration_batch_leg(ninst: int, steps: int, iters: int, obs_every: float =
         t_seq += (time.perf_counter() - t1) / iters
         z1.close(); a1.close(); s.close()
     return {"instances": ninst, "triangles_total": tri, "steps": steps, "iterations": iters,
+            "budget_gb": budget_gb, "schedule": sched,
             "zones_total": int(zoff[-1]), "gauges_total": int(gg.size),
             "batched_s_per_iteration": t_batch, "sequential_s_per_iteration": t_seq,
             "speedup_vs_sequential": t_seq / t_batch, "misfit_per_iteration": misfits,
@@ -574,10 +595,10 @@ def run_ours(args):
         line["batched"]["note"] = ("sample of the 256-member, 2000-step ensemble workload; run "
                                    "`bench.py --config ensemble` for the full size")
     if rank == 0 and args.adjoint_steps > 0:
-        line["adjoint"] = adjoint_leg(args.adjoint_steps, 10)
+        line["adjoint"] = adjoint_leg(args.adjoint_steps, 10, budget_gb=args.adjoint_budget_gb)
     if rank == 0 and args.calib_instances > 0:
         line["batched_adjoint"] = calibration_batch_leg(args.calib_instances, args.calib_steps, args.calib_iters,
-                                                        full=args.calib_full)
+                                                        full=args.calib_full, budget_gb=args.calib_budget_gb)
         line["batched_adjoint"]["note"] = (
             "the 64-instance calibration workload's instance sizes (50k-273k triangles)" if args.calib_full else
             "sample of the 64-instance calibration workload (50k-300k triangles, 3000 steps, 10 iterations); "
@@ -608,6 +629,8 @@ def main():
     ap.add_argument("--calib-steps", type=int, default=400)
     ap.add_argument("--calib-iters", type=int, default=3)
     ap.add_argument("--calib-full", action="store_true", help="calibration instances at the workload's sizes")
+    ap.add_argument("--calib-budget-gb", type=float, default=120.0, help="device memory cap of the batch's adjoint")
+    ap.add_argument("--adjoint-budget-gb", type=float, default=64.0, help="device memory cap of the adjoint leg")
     ap.add_argument("--adjoint-steps", type=int, default=3000,
                     help="adjoint calibration leg beside the plain line (0: skip)")
     args = ap.parse_args()
