@@ -313,13 +313,16 @@ def calibration_batch_leg(ninst: int, steps: int, iters: int, obs_every: float =
     the same launches, sums dJ/dn per zone and steps the zone values on the device.  Timed
     against the same instances' one-member adjoints run one after another (forward, backward,
     zone gradient and step each).  Misfit: sum of squared gauge misfits every obs_every s.
-    Instance meshes: 8k-39k triangles for the sample, 50k-273k with full (the workload's sizes).
+    Instance meshes: 8k-39k triangles for the sample, 50k-273k with full (the workload's sizes);
+    observations every 10 s with full, every 1 s for the sample (its 400 steps cover a few seconds).
     The batch's adjoint keeps to budget_gb of device memory (its schedule stores the step records
     of as many of the last steps as fit and replays the rest); each instance run alone gets the
     same cap."""
     import torch
     from cuteflow_gb300 import Batch, Solver, cases
     from cuteflow_gb300.adjoint import Adjoint, Zones
+    if not full:
+        obs_every = min(obs_every, 1.0)
     inst = []
     for i in range(ninst):
         if full:
@@ -396,7 +399,7 @@ def calibration_batch_leg(ninst: int, steps: int, iters: int, obs_every: float =
         t_seq += (time.perf_counter() - t1) / iters
         z1.close(); a1.close(); s.close()
     return {"instances": ninst, "triangles_total": tri, "steps": steps, "iterations": iters,
-            "budget_gb": budget_gb, "schedule": sched,
+            "budget_gb": budget_gb, "schedule": sched, "observation_every_s": obs_every,
             "zones_total": int(zoff[-1]), "gauges_total": int(gg.size),
             "batched_s_per_iteration": t_batch, "sequential_s_per_iteration": t_seq,
             "speedup_vs_sequential": t_seq / t_batch, "misfit_per_iteration": misfits,

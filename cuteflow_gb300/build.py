@@ -21,9 +21,10 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA_HOME, "bin", "nvcc") if os.path.exists(os.path.join(CUDA_HOME, "bin", "nvcc")) else "nvcc"
 
-CU_SOURCES = ["cf_kernels.cu", "cf_noalloc.cu", "cf_adjoint.cu"]
+CU_SOURCES = ["cf_kernels.cu", "cf_edges_1.cu", "cf_edges_2.cu", "cf_edges_3.cu", "cf_edges_4.cu", "cf_noalloc.cu",
+              "cf_adjoint.cu"]
 CPP_SOURCES = ["cf_mesh.cpp", "cf_api.cpp", "cf_adjoint_api.cpp", "cf_io.cpp", "cf_cgns.cpp"]
-HEADERS = ["cf_internal.h", "cf_flux.h", "cf_dual.h", "cf_ctx.h", "cf_xd.h"]
+HEADERS = ["cf_internal.h", "cf_flux.h", "cf_dual.h", "cf_ctx.h", "cf_xd.h", "cf_edge_kernel.cuh"]
 
 
 def _sources():

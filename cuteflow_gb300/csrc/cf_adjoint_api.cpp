@@ -48,6 +48,8 @@ struct cf_adjoint {
   int32_t Mc = 0;            /* checkpointed steps 0 .. Mc - 1 (Mc = N - T) */
   int64_t bytes = 0;         /* device bytes of the adjoint */
   double4* pp = nullptr;     /* two run states of the forward */
+  bool tail_valid = false;   /* the pool holds the stored tail's records (a backward that replays
+                                checkpointed segments reuses the pool and clears this) */
   int32_t nm = 1;            /* members */
   int64_t n_all = 0;         /* elements of all members */
   int32_t n_pad = 0;
@@ -166,7 +168,8 @@ int create_impl(cf_ctx* c, int32_t nsteps, int32_t interval, const int32_t* gaug
     for (int32_t R = nsteps; R >= 2; --R) {
       const int32_t T = std::min(nsteps, R), M = nsteps - T;
       const int32_t K = M > 0 ? (interval > 0 ? std::min(interval, R) : R) : 1;
-      const int64_t need = fixed + (int64_t)R * rec + (int64_t)((M + K - 1) / K) * st4;
+      /* checkpoints of the replayed steps, and one of the tail's first state when both exist */
+      const int64_t need = fixed + (int64_t)R * rec + (int64_t)((M + K - 1) / K + (M > 0 ? 1 : 0)) * st4;
       if (need <= budget) {
         best = R;
         break;
@@ -186,9 +189,11 @@ int create_impl(cf_ctx* c, int32_t nsteps, int32_t interval, const int32_t* gaug
   }
   a->Mc = nsteps - a->T;
   a->nseg = a->Mc > 0 ? (a->Mc + a->K - 1) / a->K : 0;
-  a->bytes = fixed + (int64_t)a->nseg_states * rec + (int64_t)a->nseg * st4;
+  /* checkpoint nseg (when the run has both parts) keeps U^Mc, the tail's first state */
+  const int32_t nck = a->nseg + ((a->T > 0 && a->Mc > 0) ? 1 : 0);
+  a->bytes = fixed + (int64_t)a->nseg_states * rec + (int64_t)nck * st4;
   int rc;
-  if ((rc = dalloc(c, &a->pp, 2 * np)) || (rc = dalloc(c, &a->ckpt, (size_t)std::max(a->nseg, 1) * np)) ||
+  if ((rc = dalloc(c, &a->pp, 2 * np)) || (rc = dalloc(c, &a->ckpt, (size_t)std::max(nck, 1) * np)) ||
       (rc = dalloc(c, &a->seg, (size_t)a->nseg_states * np)) ||
       (rc = dalloc(c, &a->mst, (size_t)nm)) || (rc = dalloc(c, &a->dt_hist, (size_t)nsteps * nm)) ||
       (rc = dalloc(c, &a->t_hist, (size_t)nsteps * nm)) || (rc = dalloc(c, &a->eta, (size_t)nsteps * ngauges)) ||
@@ -305,9 +310,9 @@ int forward_impl(cf_adjoint* a, int32_t replay, double* eta_out, double* state_o
   double4* X = Mc > 0 ? a->pp : a->seg;
   int p = p0;
   for (int32_t k = 0; k < a->N; ++k) {
-    if (k < Mc && k % a->K == 0)
-      CF_CUDA(c, cudaMemcpyAsync(a->ckpt + (size_t)(k / a->K) * np, X, np * sizeof(double4), cudaMemcpyDeviceToDevice,
-                                 c->stream));
+    if ((k < Mc && k % a->K == 0) || (k == Mc && k > 0))
+      CF_CUDA(c, cudaMemcpyAsync(a->ckpt + (size_t)(k < Mc ? k / a->K : a->nseg) * np, X, np * sizeof(double4),
+                                 cudaMemcpyDeviceToDevice, c->stream));
     /* U^{k+1} into its record when that step is stored, else into the other run state */
     double4* Y = (k + 1 >= Mc && k + 1 < a->N) ? a->seg + (size_t)(k + 1 - Mc) * np : (X == a->pp ? a->pp + np : a->pp);
     Slot* sums = k >= Mc ? a->sums + (size_t)(k - Mc) * np : nullptr;
@@ -344,6 +349,7 @@ int forward_impl(cf_adjoint* a, int32_t replay, double* eta_out, double* state_o
   }
   if (!replay) a->recorded = true;
   a->have_traj = true;
+  a->tail_valid = true;
   return CF_OK;
 }
 
@@ -408,8 +414,24 @@ int backward_impl(cf_adjoint* a, const double* w_eta, const double* w_state, dou
     }
     return CF_OK;
   };
-  /* the tail the recording forward stored: no replay */
-  if (a->T > 0 && (rc = reverse(a->Mc, a->N))) return rc;
+  /* the tail the recording forward stored: no replay (after a backward that replayed segments
+   * into the pool, the tail's records are rebuilt from its checkpoint first) */
+  if (a->T > 0) {
+    if (!a->tail_valid) {
+      CF_CUDA(c, cudaMemcpyAsync(a->seg, a->ckpt + (size_t)a->nseg * np, np * sizeof(double4),
+                                 cudaMemcpyDeviceToDevice, c->stream));
+      for (int32_t i = 0; i < a->T; ++i) {
+        StepArgs sa = step_args(c, 0);
+        sa.Uin = a->seg + (size_t)i * np;
+        sa.Uout = (i + 1 < a->T) ? a->seg + (size_t)(i + 1) * np : nullptr;
+        if ((rc = launch_replay_step(sa, a->dt_hist, a->t_hist, a->Mc + i, a->flag, a->sums + (size_t)i * np, st)))
+          return fail(c, rc, "replay launch failed");
+      }
+      a->tail_valid = true;
+    }
+    if ((rc = reverse(a->Mc, a->N))) return rc;
+  }
+  if (a->nseg > 0) a->tail_valid = false;   /* the segment replays below reuse the pool */
   for (int32_t j = a->nseg - 1; j >= 0; --j) {
     const int32_t s0 = j * a->K, s1 = std::min(a->Mc, s0 + a->K);
     CF_CUDA(c, cudaMemcpyAsync(a->seg, a->ckpt + (size_t)j * np, np * sizeof(double4), cudaMemcpyDeviceToDevice,

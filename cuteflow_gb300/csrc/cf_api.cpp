@@ -76,6 +76,9 @@ StepArgs step_args(const cf_ctx* c, int parity) {
   a.steady = c->any_steady ? 1 : 0;
   a.xd_cmp = c->xd_cmp;
   a.xd_mul_mask = c->xd_mul_mask;
+  a.eblock = c->eblock;
+  a.ept = c->ept;
+  a.cblock = c->cblock;
   return a;
 }
 
@@ -152,6 +155,7 @@ int check_params(const cf_params* p, std::string& why) {
   if (!(p->gp > 0.0) || !(p->cfl > 0.0) || !(p->tolisec >= 0.0)) { why = "gp and cfl must be positive, tolisec non-negative"; return CF_EINVAL; }
   if (p->ramp_time < 0.0) { why = "ramp_time must be non-negative"; return CF_EINVAL; }
   if (!(p->tol_reg_perm >= 0.0)) { why = "tol_reg_perm must be non-negative"; return CF_EINVAL; }
+  if (p->reorder < 0 || p->reorder > 2) { why = "reorder must be 0 (the caller's order), 1 (Hilbert) or 2 (Morton)"; return CF_EINVAL; }
   return CF_OK;
 }
 
@@ -741,6 +745,32 @@ int cf_get_tuning(cf_ctx* ctx, int32_t* int_compare, int32_t* int_mul_warps) {
   return CF_OK;
 }
 
+int cf_set_launch_shape(cf_ctx* ctx, int32_t edge_block, int32_t edges_per_thread, int32_t cell_block) {
+  if (!ctx) return CF_EINVAL;
+  if ((edge_block != 64 && edge_block != 128 && edge_block != 256) || (edges_per_thread != 1 && edges_per_thread != 2) ||
+      (cell_block != 128 && cell_block != 256))
+    return fail(ctx, CF_EINVAL, "launch shape: edge_block 64, 128 or 256, edges_per_thread 1 or 2, cell_block 128 or 256");
+  if (ctx->eblock != edge_block || ctx->ept != edges_per_thread || ctx->cblock != cell_block) {
+    ctx->eblock = edge_block;
+    ctx->ept = edges_per_thread;
+    ctx->cblock = cell_block;
+    if (ctx->graph2) {   /* the captured steps hold the old launch configuration */
+      CF_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+      cudaGraphExecDestroy(ctx->graph2);
+      ctx->graph2 = nullptr;
+    }
+  }
+  return CF_OK;
+}
+
+int cf_get_launch_shape(cf_ctx* ctx, int32_t* edge_block, int32_t* edges_per_thread, int32_t* cell_block) {
+  if (!ctx) return CF_EINVAL;
+  if (edge_block) *edge_block = ctx->eblock;
+  if (edges_per_thread) *edges_per_thread = ctx->ept;
+  if (cell_block) *cell_block = ctx->cblock;
+  return CF_OK;
+}
+
 int cf_autotune(cf_ctx* ctx, int32_t steps_per_trial, int32_t* int_compare, int32_t* int_mul_warps, double* ms_per_step) {
   if (!ctx) return CF_EINVAL;
   cf_ctx* c = ctx;
@@ -757,7 +787,7 @@ int cf_autotune(cf_ctx* ctx, int32_t steps_per_trial, int32_t* int_compare, int3
   CF_CUDA(c, cudaMalloc((void**)&saved, 2 * np * sizeof(double4)));
   std::vector<MemberState> ms(c->host_state, c->host_state + nm);
   const int64_t launched0 = c->launched;
-  const int32_t cmp0 = c->xd_cmp, mul0 = c->xd_mul_mask;
+  const int32_t cmp0 = c->xd_cmp, mul0 = c->xd_mul_mask, eb0 = c->eblock, ept0 = c->ept, cb0 = c->cblock;
   auto restore = [&]() -> int {
     CF_CUDA(c, cudaMemcpyAsync(c->U[0], saved, np * sizeof(double4), cudaMemcpyDeviceToDevice, c->stream));
     CF_CUDA(c, cudaMemcpyAsync(c->U[1], saved + np, np * sizeof(double4), cudaMemcpyDeviceToDevice, c->stream));
@@ -772,38 +802,99 @@ int cf_autotune(cf_ctx* ctx, int32_t steps_per_trial, int32_t* int_compare, int3
     cudaFree(saved);
     return cuda_fail(c, e, "cudaMemcpyAsync");
   }
-  /* candidates: all on the FP64 pipe; comparisons on the integer pipes; comparisons and the
-   * arithmetic of all edge warps, of half of them, and of all edge warps and the elements */
-  const int32_t cand[5][2] = {{0, 0}, {1, 0}, {1, 0xf}, {1, 0x5}, {1, 0x1f}};
-  double best = 1e300;
-  int32_t bc = 0, bm = 0;
-  rc = CF_OK;
-  for (const auto& k : cand) {
-    if ((rc = cf_set_tuning(c, k[0], k[1]))) break;
-    if ((rc = step_impl(c, 2, nullptr))) break;  /* warm-up (and graph build) */
+  /* one trial: warm-up (and graph build), steps_per_trial timed steps, the state restored */
+  auto trial = [&](double& per) -> int {
+    int r;
+    if ((r = step_impl(c, 2, nullptr))) return r;
     CF_CUDA(c, cudaEventRecord(c->ev[0], c->stream));
-    if ((rc = step_impl(c, steps_per_trial, nullptr))) break;
+    if ((r = step_impl(c, steps_per_trial, nullptr))) return r;
     CF_CUDA(c, cudaEventRecord(c->ev[1], c->stream));
     CF_CUDA(c, cudaEventSynchronize(c->ev[1]));
     float t = 0.f;
     cudaEventElapsedTime(&t, c->ev[0], c->ev[1]);
-    if ((rc = restore())) break;
-    const double per = t / steps_per_trial;
+    if ((r = restore())) return r;
+    per = t / steps_per_trial;
+    return CF_OK;
+  };
+  /* 1. how the FP64 work is shared with the integer pipes, at the current launch shape:
+   * all on the FP64 pipe; comparisons on the integer pipes; comparisons and the arithmetic of
+   * all edge warps, of half of them, and of all edge warps and the elements */
+  const int32_t cand[5][2] = {{0, 0}, {1, 0}, {1, 0xf}, {1, 0x5}, {1, 0x1f}};
+  double best = 1e300;
+  int32_t bc = cmp0, bm = mul0, beb = eb0, bept = ept0, bcb = cb0;
+  rc = CF_OK;
+  for (const auto& k : cand) {
+    double per = 0.0;
+    if ((rc = cf_set_tuning(c, k[0], k[1])) || (rc = trial(per))) break;
     if (per < best) {
       best = per;
       bc = k[0];
       bm = k[1];
     }
   }
+  /* 2. the edge kernel's launch shape (threads per block, edges per thread), then 3. the element
+   * kernel's block, with the setting of 1 */
+  if (rc == CF_OK) rc = cf_set_tuning(c, bc, bm);
+  const int32_t eshape[6][2] = {{128, 1}, {64, 1}, {256, 1}, {128, 2}, {64, 2}, {256, 2}};
+  for (int i = 0; rc == CF_OK && i < 6; ++i) {
+    double per = 0.0;
+    if ((rc = cf_set_launch_shape(c, eshape[i][0], eshape[i][1], bcb)) || (rc = trial(per))) break;
+    if (per < best) {
+      best = per;
+      beb = eshape[i][0];
+      bept = eshape[i][1];
+    }
+  }
+  for (int cb : {256, 128}) {
+    if (rc != CF_OK) break;
+    double per = 0.0;
+    if ((rc = cf_set_launch_shape(c, beb, bept, cb)) || (rc = trial(per))) break;
+    if (per < best) {
+      best = per;
+      bcb = cb;
+    }
+  }
   cudaFree(saved);
   if (rc != CF_OK) {
     cf_set_tuning(c, cmp0, mul0);
+    cf_set_launch_shape(c, eb0, ept0, cb0);
     restore();
     return rc;
   }
-  if ((rc = cf_set_tuning(c, bc, bm))) return rc;
+  if ((rc = cf_set_tuning(c, bc, bm)) || (rc = cf_set_launch_shape(c, beb, bept, bcb))) return rc;
   if (int_compare) *int_compare = bc;
   if (int_mul_warps) *int_mul_warps = bm;
+  if (ms_per_step) *ms_per_step = best;
+  return CF_OK;
+}
+
+int cf_autotune_order(const cf_mesh* mesh, const cf_params* params, const double* hu3, int32_t steps_per_trial,
+                      int32_t* reorder, double* ms_per_step) {
+  if (!mesh || !params || !hu3) return CF_EINVAL;
+  /* the element orders a context can be created with: Hilbert, Morton, the caller's; each timed
+   * with the rest of its tuning (cf_autotune) on the caller's state */
+  double best = 1e300;
+  int32_t br = -1;
+  for (int32_t r : {1, 2, 0}) {
+    cf_params q = *params;
+    q.reorder = r;
+    cf_ctx* c = nullptr;
+    int rc = cf_create(mesh, &q, &c);
+    if (rc == CF_OK) rc = cf_set_state(c, hu3, 0.0);
+    double per = 0.0;
+    if (rc == CF_OK) rc = cf_autotune(c, steps_per_trial, nullptr, nullptr, &per);
+    if (rc != CF_OK) {
+      if (c) g_create_error = c->err;
+      cf_destroy(c);
+      return rc;
+    }
+    cf_destroy(c);
+    if (per < best) {
+      best = per;
+      br = r;
+    }
+  }
+  if (reorder) *reorder = br;
   if (ms_per_step) *ms_per_step = best;
   return CF_OK;
 }

@@ -66,6 +66,8 @@ struct cf_ctx {
   int32_t* ids = nullptr;              /* max_n element ids (cf_get_elements / cf_set_elements) */
   int32_t xd_cmp = 0;                  /* edge kernel: integer comparisons (cf_set_tuning) */
   int32_t xd_mul_mask = 0;             /* edge kernel: warps multiplying on the integer pipes */
+  int32_t eblock = 128, ept = 1;       /* launch shape of the edge kernel (cf_set_launch_shape) */
+  int32_t cblock = 256;                /* threads per block of the element kernel */
   cf::MemberState* host_state = nullptr;   /* pinned, one record per member */
   bool direct_io = true;               /* kernels read / write callers' pinned host states directly */
   /* stepping */

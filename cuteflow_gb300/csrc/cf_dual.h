@@ -139,19 +139,20 @@ CFD_HD Dual<N> operator/(double a, const Dual<N>& b) {
   for (int i = 0; i < N; ++i) r.d[i] = -r.v * b.d[i] * y;
   return r;
 }
-/* comparisons act on values */
-template <int N> CFD_HD bool operator<(const Dual<N>& a, const Dual<N>& b) { return a.v < b.v; }
-template <int N> CFD_HD bool operator>(const Dual<N>& a, const Dual<N>& b) { return a.v > b.v; }
-template <int N> CFD_HD bool operator<=(const Dual<N>& a, const Dual<N>& b) { return a.v <= b.v; }
-template <int N> CFD_HD bool operator>=(const Dual<N>& a, const Dual<N>& b) { return a.v >= b.v; }
-template <int N> CFD_HD bool operator<(const Dual<N>& a, double b) { return a.v < b; }
-template <int N> CFD_HD bool operator>(const Dual<N>& a, double b) { return a.v > b; }
-template <int N> CFD_HD bool operator<=(const Dual<N>& a, double b) { return a.v <= b; }
-template <int N> CFD_HD bool operator>=(const Dual<N>& a, double b) { return a.v >= b; }
-template <int N> CFD_HD bool operator<(double a, const Dual<N>& b) { return a < b.v; }
-template <int N> CFD_HD bool operator>(double a, const Dual<N>& b) { return a > b.v; }
-template <int N> CFD_HD bool operator==(const Dual<N>& a, const Dual<N>& b) { return a.v == b.v; }
-template <int N> CFD_HD bool operator!=(const Dual<N>& a, const Dual<N>& b) { return a.v != b.v; }
+/* comparisons act on values, on the ordered integer keys of cf_xd.h (the IEEE results: NaN
+ * compares false, -0 equals +0), which keeps them off the FP64 pipe the derivative lanes use */
+template <int N> CFD_HD bool operator<(const Dual<N>& a, const Dual<N>& b) { return xlt(a.v, b.v); }
+template <int N> CFD_HD bool operator>(const Dual<N>& a, const Dual<N>& b) { return xlt(b.v, a.v); }
+template <int N> CFD_HD bool operator<=(const Dual<N>& a, const Dual<N>& b) { return xle(a.v, b.v); }
+template <int N> CFD_HD bool operator>=(const Dual<N>& a, const Dual<N>& b) { return xle(b.v, a.v); }
+template <int N> CFD_HD bool operator<(const Dual<N>& a, double b) { return xlt(a.v, b); }
+template <int N> CFD_HD bool operator>(const Dual<N>& a, double b) { return xlt(b, a.v); }
+template <int N> CFD_HD bool operator<=(const Dual<N>& a, double b) { return xle(a.v, b); }
+template <int N> CFD_HD bool operator>=(const Dual<N>& a, double b) { return xle(b, a.v); }
+template <int N> CFD_HD bool operator<(double a, const Dual<N>& b) { return xlt(a, b.v); }
+template <int N> CFD_HD bool operator>(double a, const Dual<N>& b) { return xlt(b.v, a); }
+template <int N> CFD_HD bool operator==(const Dual<N>& a, const Dual<N>& b) { return xeq(a.v, b.v); }
+template <int N> CFD_HD bool operator!=(const Dual<N>& a, const Dual<N>& b) { return !xeq(a.v, b.v); }
 
 template <int N>
 CFD_HD Dual<N> sqrt(const Dual<N>& a) {

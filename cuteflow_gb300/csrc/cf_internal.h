@@ -121,9 +121,12 @@ struct StepArgs {
   int32_t phys_inflow;       /* some member uses inlet 3: k_surf runs before the edges */
   int32_t steady;            /* some member tests for steady state: k_steady runs after the cells */
   int32_t xd_cmp;            /* edge kernel: 1 = comparisons on integer keys (cf_xd.h) */
-  int32_t xd_mul_mask;       /* with xd_cmp: warps w (0-3) of an edge block with bit w set, and with
-                                bit 4 (XD_CELLS) the element kernel, form products, quotients and
-                                roots on the integer pipes */
+  int32_t xd_mul_mask;       /* with xd_cmp: the edges of warp w (0-3) of an edge tile with bit w set,
+                                and with bit 4 (XD_CELLS) the element kernel, form products,
+                                quotients and roots on the integer pipes */
+  int32_t eblock, ept;       /* launch shape of the edge kernel: threads per block (64, 128, 256) and
+                                edges per thread (1, 2) */
+  int32_t cblock;            /* threads per block of the element kernel (128, 256) */
 };
 
 /* ---- host preprocessing (cf_mesh.cpp) ---------------------------------------------- */
@@ -176,6 +179,11 @@ int prepare_mesh(const cf_mesh* m, const cf_params* p, Prep& out, std::string& e
 typedef struct CUstream_st* stream_t;
 
 int launch_step(const StepArgs& a, stream_t s, void* ev_mid, void* ev_end);
+/* the edge kernel of one scheme in the shape a.eblock x a.ept (cf_edges_<IFLUX>.cu) */
+int launch_edges_1(const StepArgs& a, stream_t s);
+int launch_edges_2(const StepArgs& a, stream_t s);
+int launch_edges_3(const StepArgs& a, stream_t s);
+int launch_edges_4(const StepArgs& a, stream_t s);
 int launch_probe_fp64(double* out, int32_t nblocks, int64_t iters, stream_t s);  /* nblocks x 256 outputs */
 int launch_selftest_xd(int64_t n, uint64_t seed, unsigned long long* bad, int32_t nblocks, stream_t s);
 int launch_cfl(const double4* U, const double4* cstat, const int32_t* ctile_mem, int32_t tile_begin,

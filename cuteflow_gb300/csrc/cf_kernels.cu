@@ -3,7 +3,7 @@
  *
  * One step is two kernels on the context's stream:
  *
- *   k_edges : one thread per edge.  Loads both elements' {h, hu, hv, z}, solves the Riemann
+ *   k_edges : one thread per edge (cf_edge_kernel.cuh, in every launch shape).  Loads both elements' {h, hu, hv, z}, solves the Riemann
  *             problem once (wave speeds, physical and HLL fluxes), and writes into the edge's
  *             two slots the flux each side computes for itself in the reference
  *             (flux_riemann.cuf:33-426 evaluates every interior edge from both elements).
@@ -33,54 +33,6 @@
 
 namespace cf {
 namespace {
-
-template <int IFLUX>
-/* eight blocks per SM (at most 64 registers, with spills to L1): the tuned edge is chains of
- * dependent integer-pipe products and quotients between its FP64 sums, and the extra warps hide
- * their latency (1M WAF, tuned: 0.462 ms at four blocks, 0.434 at five, 0.421 at six, 0.408 at
- * eight; HLLC 0.266 -> 0.215 ms).  MUSCL-Hancock runs four (128 registers): at eight its spills
- * cost more than the warps gain (1.39 ms), at three (138 registers) it takes 1.32 ms, at four
- * 1.21 ms. */
-__global__ void __launch_bounds__(TILE_E, (IFLUX == 4) ? 4 : 8) k_edges(StepArgs a) {
-  const int tile = blockIdx.x;
-  const int m = __ldg(a.etile_mem + tile);
-  const MemberDev& M = a.mdev[m];
-  MemberState* S = a.mst + m;
-  const int p = a.parity;
-  if (S->status) return;
-  const double dt = S->dt[p];
-  const double t = S->t[p];
-  const int e = tile * TILE_E + threadIdx.x;
-  if (e == M.edge_begin) {
-    /* Start of the member's step: the dt sanity test of cfl_condition.cuf:129-132 (a failing
-     * dt ends the run with the current state), the next time, and the start value of the
-     * next dt minimum (cflcond sets dt_d = 1e6 and the block reduction pads a partial last
-     * block with 1e5, cfl_condition.cuf:21,86). */
-    if (S->nstep > 0 && (dt > 9999.0 || dt < DT_LOW)) {   /* the initial dt is not tested (:113-116) */
-      atomicOr(&S->status, CF_STATUS_DT_RANGE);
-    } else if (S->nstep > 0 && !((S->tc + dt) - S->ts + 2.0 * TOL_LOOP < TOL_LOOP)) {
-      /* the time loop's test (finite_volumes_method.cuf:123) on tc = tc + dt (:232); tc keeps
-       * its value, so that a later cf_run adds this dt once and tests again */
-      atomicOr(&S->status, CF_STATUS_END);
-    } else if (S->nstep == 0 && !(S->tc - S->ts + 2.0 * TOL_LOOP < TOL_LOOP)) {
-      atomicOr(&S->status, CF_STATUS_END);
-    } else {
-      if (S->nstep > 0) S->tc = S->tc + dt;
-      S->t[1 - p] = t + dt;
-      S->dt[1 - p] = M.dt_reset;
-      S->nstep += 1;
-    }
-  }
-  if (e >= M.edge_end) return;
-  if (a.xd_cmp) {
-    /* the same arithmetic with exact integer comparisons and, in the warps of xd_mul_mask,
-     * exact integer products: the FP64 pipe and the integer pipes share the work */
-    if ((a.xd_mul_mask >> (threadIdx.x >> 5)) & 1) edge_body<IFLUX, XD<true>>(a, M, e, dt, t, S->surf);
-    else edge_body<IFLUX, XD<false>>(a, M, e, dt, t, S->surf);
-  } else {
-    edge_body<IFLUX>(a, M, e, dt, t, S->surf);
-  }
-}
 
 /* phys_inflow: per member (one warp) and inlet, calcul_surf_entree (maillage.cuf:1368-1421)
  * on the state at the step's start: the entries' length * depth in blocks of 32 in list
@@ -124,8 +76,9 @@ __device__ __forceinline__ Slot load_slot(const Slot* p) {
 /* Minimum over the block, folded into *target with one atomic.  The values are positive (or
  * NaN, which the minimum ignores as fmin would), so they order like their bit patterns: the
  * reduction is integer work. */
+template <int BC>
 __device__ __forceinline__ void block_min_atomic(double v, double* target) {
-  __shared__ unsigned long long red[TILE_C / 32];
+  __shared__ unsigned long long red[BC / 32];
   unsigned long long b = dbits(v);
   #pragma unroll
   for (int o = 16; o > 0; o >>= 1) b = min(b, __shfl_xor_sync(0xffffffffu, b, o));
@@ -133,7 +86,7 @@ __device__ __forceinline__ void block_min_atomic(double v, double* target) {
   if (lane == 0) red[wid] = b;
   __syncthreads();
   if (wid == 0) {
-    b = (lane < TILE_C / 32) ? red[lane] : dbits(1.0e300);
+    b = (lane < BC / 32) ? red[lane] : dbits(1.0e300);
     #pragma unroll
     for (int o = 16; o > 0; o >>= 1) b = min(b, __shfl_xor_sync(0xffffffffu, b, o));
     if (lane == 0) atomicMin(reinterpret_cast<unsigned long long*>(target), b);
@@ -141,8 +94,9 @@ __device__ __forceinline__ void block_min_atomic(double v, double* target) {
 }
 
 /* Minimum over the block of a float, returned to every thread. */
+template <int BC>
 __device__ __forceinline__ float block_min_f32(float v) {
-  __shared__ float red[TILE_C / 32];
+  __shared__ float red[BC / 32];
   #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v = fminf(v, __shfl_xor_sync(0xffffffffu, v, o));
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -150,7 +104,7 @@ __device__ __forceinline__ float block_min_f32(float v) {
   __syncthreads();
   v = red[0];
   #pragma unroll
-  for (int w = 1; w < TILE_C / 32; ++w) v = fminf(v, red[w]);
+  for (int w = 1; w < BC / 32; ++w) v = fminf(v, red[w]);
   return v;
 }
 
@@ -196,6 +150,7 @@ __device__ __forceinline__ bool cfl_dt_f32(const MemberDev& M, double cflL, doub
  * single-precision minimum: m_f >= (1 - 7e-7) d_min and d_f(argmin) <= (1 + 7e-7) d_min, so the
  * element of the minimum passes d_f <= 1.000004 m_f.  Elements without a single-precision value
  * (dry ones, constant dt, out-of-range inputs) take their FP64 value directly. */
+template <int BC>
 __device__ __forceinline__ void block_cfl_min(const MemberDev& M, bool active, double cflL, const double4& V,
                                               double* target) {
   double dti = 1.0e300;
@@ -206,16 +161,19 @@ __device__ __forceinline__ void block_cfl_min(const MemberDev& M, bool active, d
     else if (cfl_dt_f32(M, cflL, V.x, V.y, V.z, df)) pending = true;
     else dti = cfl_dt_elem(M, cflL, V.x, V.y, V.z, V.w);
   }
-  const float mf = block_min_f32(df);
+  const float mf = block_min_f32<BC>(df);
   if (pending && df <= mf * 1.000004f) dti = cfl_dt_elem(M, cflL, V.x, V.y, V.z, V.w);
-  block_min_atomic(dti, target);
+  block_min_atomic<BC>(dti, target);
 }
 
-/* three blocks per SM (at most 85 registers; 80 used, no spills): the element update is a chain
+/* 768 threads per SM (at most 85 registers; 80 used, no spills): the element update is a chain
  * of dependent integer-pipe quotients and products, and the extra warps hide its latency
- * (1M elements, tuned: 0.152 -> 0.130 ms) */
-__global__ void __launch_bounds__(TILE_C, 3) k_cells(StepArgs a) {
-  const int tile = blockIdx.x;
+ * (1M elements, tuned, 256-thread blocks: 0.152 -> 0.130 ms).  A block of BC threads (128 or 256,
+ * the launch shape) lies within one tile of TILE_C elements, so within one member; each block
+ * folds its dt minimum into the member's with one atomic. */
+template <int BC>
+__global__ void __launch_bounds__(BC, 768 / BC) k_cells(StepArgs a) {
+  const int tile = (int)(((long long)blockIdx.x * BC) / TILE_C);
   const int m = __ldg(a.ctile_mem + tile);
   const MemberDev& M = a.mdev[m];
   MemberState* S = a.mst + m;
@@ -226,7 +184,7 @@ __global__ void __launch_bounds__(TILE_C, 3) k_cells(StepArgs a) {
   __syncthreads();
   if (s_stop) return;
   const double dt = S->dt[p];
-  const int c = tile * TILE_C + threadIdx.x;
+  const int c = blockIdx.x * BC + threadIdx.x;
   double4 V = make_double4(0.0, 0.0, 0.0, 0.0);
   double cflL = 0.0;
   if (c < M.cell_end) {
@@ -246,7 +204,7 @@ __global__ void __launch_bounds__(TILE_C, 3) k_cells(StepArgs a) {
     reinterpret_cast<double2*>(o)[1] = make_double2(V.z, V.w);
     cflL = st.z;
   }
-  block_cfl_min(M, c < M.cell_end, cflL, V, &S->dt[1 - p]);
+  block_cfl_min<BC>(M, c < M.cell_end, cflL, V, &S->dt[1 - p]);
 }
 
 /* CFL of a state into mst[m].dt[slot] (the initial dt, finite_volumes_method.cuf:113-116). */
@@ -262,7 +220,7 @@ __global__ void __launch_bounds__(TILE_C) k_cfl(const double4* U, const double4*
     u = ld4(U + c);
     cflL = ld4(cstat + c).z;
   }
-  block_cfl_min(M, c < M.cell_end, cflL, u, &mst[m].dt[slot]);
+  block_cfl_min<TILE_C>(M, c < M.cell_end, cflL, u, &mst[m].dt[slot]);
 }
 
 /* Discharge diagnostics of the last step (debit_entree_sum, debit_sortie,
@@ -536,15 +494,18 @@ int launch_probe_fp64(double* out, int32_t nblocks, int64_t iters, stream_t s) {
 int launch_step(const StepArgs& a, stream_t s, void* ev_mid, void* ev_end) {
   cudaStream_t st = reinterpret_cast<cudaStream_t>(s);
   if (a.phys_inflow) k_surf<<<a.nmembers, 32, 0, st>>>(a);
+  int rc;
   switch (a.iflux) {
-    case 1: k_edges<1><<<a.n_etiles, TILE_E, 0, st>>>(a); break;
-    case 2: k_edges<2><<<a.n_etiles, TILE_E, 0, st>>>(a); break;
-    case 3: k_edges<3><<<a.n_etiles, TILE_E, 0, st>>>(a); break;
-    case 4: k_edges<4><<<a.n_etiles, TILE_E, 0, st>>>(a); break;
+    case 1: rc = launch_edges_1(a, s); break;
+    case 2: rc = launch_edges_2(a, s); break;
+    case 3: rc = launch_edges_3(a, s); break;
+    case 4: rc = launch_edges_4(a, s); break;
     default: return CF_ENOTSUP;
   }
+  if (rc != CF_OK) return rc;
   if (ev_mid) cudaEventRecord(reinterpret_cast<cudaEvent_t>(ev_mid), st);
-  k_cells<<<a.n_ctiles, TILE_C, 0, st>>>(a);
+  if (a.cblock == 128) k_cells<128><<<a.n_ctiles * (TILE_C / 128), 128, 0, st>>>(a);
+  else k_cells<TILE_C><<<a.n_ctiles, TILE_C, 0, st>>>(a);
   if (a.steady) k_discharge<<<a.nmembers, 256, 0, st>>>(a.slots, a.ecell, a.mdev, a.mst, 1);
   if (ev_end) cudaEventRecord(reinterpret_cast<cudaEvent_t>(ev_end), st);
   return check(cudaGetLastError());

@@ -43,6 +43,20 @@ uint64_t hilbert_index(uint32_t x, uint32_t y, int order) {
   return d;
 }
 
+/* Morton (Z-order) index of (x, y): the bits of x and y interleaved, x in the even bits. */
+uint64_t morton_index(uint32_t x, uint32_t y) {
+  auto spread = [](uint64_t v) {
+    v &= 0xffffffffull;
+    v = (v | (v << 16)) & 0x0000ffff0000ffffull;
+    v = (v | (v << 8)) & 0x00ff00ff00ff00ffull;
+    v = (v | (v << 4)) & 0x0f0f0f0f0f0f0f0full;
+    v = (v | (v << 2)) & 0x3333333333333333ull;
+    v = (v | (v << 1)) & 0x5555555555555555ull;
+    return v;
+  };
+  return spread(x) | (spread(y) << 1);
+}
+
 inline int nd(const cf_mesh* m, int e, int k) { return m->tri[3 * e + k] - 1; }
 
 /* Unit normal and length of local edge k of element e, oriented out of the element by the
@@ -185,11 +199,12 @@ int prepare_mesh(const cf_mesh* m, const cf_params* p, Prep& P, std::string& err
           return CF_EINVAL;
         }
 
-  /* -- renumbering along a Hilbert curve of the centroids ------------------------------- */
+  /* -- renumbering along a space-filling curve of the centroids: reorder 1 Hilbert, 2 Morton,
+   * 0 the caller's order ------------------------------------------------------------------ */
   P.perm.resize(n);
   P.iperm.resize(n);
   std::iota(P.perm.begin(), P.perm.end(), 0);
-  if (p->reorder) {
+  if (p->reorder == 1 || p->reorder == 2) {
     double xmin = P.xc[0], xmax = P.xc[0], ymin = P.yc[0], ymax = P.yc[0];
     for (int e = 1; e < n; ++e) {
       xmin = std::min(xmin, P.xc[e]); xmax = std::max(xmax, P.xc[e]);
@@ -201,7 +216,7 @@ int prepare_mesh(const cf_mesh* m, const cf_params* p, Prep& P, std::string& err
     std::vector<uint64_t> h(n);
     for (int e = 0; e < n; ++e) {
       uint32_t ix = (uint32_t)((P.xc[e] - xmin) * scale), iy = (uint32_t)((P.yc[e] - ymin) * scale);
-      h[e] = hilbert_index(ix, iy, order_bits);
+      h[e] = p->reorder == 1 ? hilbert_index(ix, iy, order_bits) : morton_index(ix, iy);
     }
     std::stable_sort(P.perm.begin(), P.perm.end(), [&](int32_t i, int32_t j) { return h[i] < h[j]; });
   }

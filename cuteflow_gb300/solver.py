@@ -76,6 +76,10 @@ def load(build_if_missing: bool = True):
     L.cf_last_error.restype = C.c_char_p
     L.cf_set_timing.argtypes = [vp, C.c_int32]
     L.cf_set_direct_io.argtypes = [vp, C.c_int32]
+    L.cf_set_launch_shape.argtypes = [vp, C.c_int32, C.c_int32, C.c_int32]
+    L.cf_get_launch_shape.argtypes = [vp, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
+    L.cf_autotune_order.argtypes = [C.POINTER(_abi.CfMesh), C.POINTER(_abi.CfParams), dp, C.c_int32,
+                                    C.POINTER(C.c_int32), dp]
     L.cf_get_timing.argtypes = [vp, dp, dp, C.POINTER(C.c_int64)]
     ip = C.POINTER(C.c_int32)
     L.cf_create_batch.argtypes = [C.POINTER(_abi.CfMesh), C.POINTER(_abi.CfParams), C.c_int32, C.POINTER(vp)]
@@ -120,7 +124,8 @@ def load(build_if_missing: bool = True):
                  "cf_set_initial_condition", "cf_step", "cf_step_noalloc", "cf_run", "cf_set_tuning",
                  "cf_get_tuning", "cf_autotune", "cf_get_elements", "cf_set_elements", "cf_set_dt", "cf_get_state", "cf_get_state_device",
                  "cf_get_info", "cf_get_mesh_tables", "cf_mesh_tables", "cf_get_sizes", "cf_set_timing", "cf_get_timing",
-                 "cf_set_direct_io", "cf_probe_fp64", "cf_selftest_xd", "cf_advance"):
+                 "cf_set_direct_io", "cf_set_launch_shape", "cf_get_launch_shape", "cf_autotune_order",
+                 "cf_probe_fp64", "cf_selftest_xd", "cf_advance"):
         getattr(L, name).restype = C.c_int
     _lib = L
     return L
@@ -254,11 +259,22 @@ class Solver:
         return a.value, b.value
 
     def autotune(self, steps_per_trial: int = 50):
-        """cf_autotune: time each setting on the current state (restored afterwards) and keep
-        the fastest; returns (int_compare, int_mul_warps, ms_per_step)."""
+        """cf_autotune: time each integer-pipe setting and launch shape on the current state
+        (restored afterwards) and keep the fastest; returns (int_compare, int_mul_warps,
+        ms_per_step); launch_shape() gives the shape."""
         a, b, t = C.c_int32(), C.c_int32(), C.c_double()
         self._check(self._L.cf_autotune(self._ctx, int(steps_per_trial), C.byref(a), C.byref(b), C.byref(t)))
         return a.value, b.value, t.value
+
+    def set_launch_shape(self, edge_block: int, edges_per_thread: int, cell_block: int):
+        """cf_set_launch_shape (results identical in every shape)."""
+        self._check(self._L.cf_set_launch_shape(self._ctx, int(edge_block), int(edges_per_thread), int(cell_block)))
+
+    def launch_shape(self):
+        """(edge_block, edges_per_thread, cell_block) of cf_get_launch_shape."""
+        a, b, c = C.c_int32(), C.c_int32(), C.c_int32()
+        self._check(self._L.cf_get_launch_shape(self._ctx, C.byref(a), C.byref(b), C.byref(c)))
+        return a.value, b.value, c.value
 
     def advance(self, U: np.ndarray, t0: float, nsteps: int, check: bool = True):
         """cf_advance: the host state U (reference order, [nelt, 3]) at time t0 advanced by nsteps
@@ -391,6 +407,17 @@ class Batch:
             self._check(rc)
         return [_info(i) for i in infos]
 
+    def set_tuning(self, int_compare: int, int_mul_warps: int):
+        self._check(self._L.cf_set_tuning(self._ctx, int(int_compare), int(int_mul_warps)))
+
+    def set_launch_shape(self, edge_block: int, edges_per_thread: int, cell_block: int):
+        self._check(self._L.cf_set_launch_shape(self._ctx, int(edge_block), int(edges_per_thread), int(cell_block)))
+
+    def launch_shape(self):
+        a, b, c = C.c_int32(), C.c_int32(), C.c_int32()
+        self._check(self._L.cf_get_launch_shape(self._ctx, C.byref(a), C.byref(b), C.byref(c)))
+        return a.value, b.value, c.value
+
     def autotune(self, steps_per_trial: int = 50):
         """cf_autotune on the batch (every member set and running); the state is restored."""
         a, b, t = C.c_int32(), C.c_int32(), C.c_double()
@@ -434,3 +461,19 @@ class Batch:
         f, u, n = C.c_double(), C.c_double(), C.c_int64()
         self._check(self._L.cf_get_timing(self._ctx, C.byref(f), C.byref(u), C.byref(n)))
         return f.value, u.value, int(n.value)
+
+
+def autotune_order(case, params: Optional[dict] = None, U: Optional[np.ndarray] = None, steps_per_trial: int = 20):
+    """cf_autotune_order: the element order (reorder 1 Hilbert, 2 Morton, 0 the case's own) with
+    which a context of this case steps fastest from the state U (default case.U0), each order
+    timed with the rest of its tuning; returns (reorder, ms_per_step)."""
+    L = load()
+    ma = _abi.MeshArrays(case)
+    p = _abi.make_params({**case.params, **(params or {})})
+    src = np.ascontiguousarray(case.U0 if U is None else U, dtype=np.float64)
+    r, t = C.c_int32(), C.c_double()
+    rc = L.cf_autotune_order(C.byref(ma.mesh), C.byref(p), src.ctypes.data_as(C.POINTER(C.c_double)),
+                             int(steps_per_trial), C.byref(r), C.byref(t))
+    if rc != 0:
+        raise CFError(rc, L.cf_last_error(None).decode(errors="replace"))
+    return r.value, t.value

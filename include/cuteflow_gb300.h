@@ -96,7 +96,9 @@ typedef struct cf_params {
                                       every (element, edge) as that element evaluates it
                                       (flux_riemann.cuf:33-426); 1 = conservative, one evaluation
                                       per edge with the opposite sign for the neighbour */
-  int32_t reorder;                 /* extension: 1 = space-filling-curve renumbering (default) */
+  int32_t reorder;                 /* extension: element order on the device: 1 = along a Hilbert curve of the
+                                      centroids (default), 2 = along a Morton curve, 0 = the caller's
+                                      order (results are identical; cf_autotune_order picks one) */
   int32_t pad_;
   double tol_reg_perm;             /* steady-state stop (tol_reg_perm): after a step whose inflow
                                       Q_in > 1e-8 and |Q_in - Q_out| / Q_in < tol_reg_perm for
@@ -275,11 +277,26 @@ int cf_set_dt(cf_ctx* ctx, int32_t member, double dt);
  * operation on the FP64 pipe.  cf_autotune picks a setting by timing. */
 int cf_set_tuning(cf_ctx* ctx, int32_t int_compare, int32_t int_mul_warps);
 int cf_get_tuning(cf_ctx* ctx, int32_t* int_compare, int32_t* int_mul_warps);
-/* Autotuner: times steps_per_trial steps of every setting on the context's own state and keeps
- * the fastest (the state, time and step count are restored after each trial, so the simulation
- * is unchanged).  Every member must have a state and be running.  Outputs may be NULL. */
+/* Launch shape of the step (no counterpart in the reference, whose launch shapes are fixed,
+ * finite_volumes_method.cuf:85-109): threads per block of the edge kernel (64, 128 or 256), edges
+ * each of its threads evaluates (1 or 2), threads per block of the element kernel (128 or 256).
+ * Default (128, 1, 256).  Results are identical bit for bit in every shape. */
+int cf_set_launch_shape(cf_ctx* ctx, int32_t edge_block, int32_t edges_per_thread, int32_t cell_block);
+int cf_get_launch_shape(cf_ctx* ctx, int32_t* edge_block, int32_t* edges_per_thread, int32_t* cell_block);
+/* Autotuner: times steps_per_trial steps on the context's own state and keeps the fastest
+ * setting (the state, time and step count are restored after each trial, so the simulation is
+ * unchanged): first the integer-pipe setting (5 candidates), then the edge kernel's launch shape
+ * (6) and the element kernel's block (2).  Returns the integer-pipe setting and the best time per
+ * step; cf_get_launch_shape reports the shape.  Every member must have a state and be running.
+ * Outputs may be NULL. */
 int cf_autotune(cf_ctx* ctx, int32_t steps_per_trial, int32_t* int_compare, int32_t* int_mul_warps,
                 double* ms_per_step);
+/* The element order (params->reorder 1 Hilbert, 2 Morton, 0 the caller's) with which a context of
+ * this mesh steps fastest: creates a context per order, sets the state hu3, runs cf_autotune on
+ * it, and destroys it.  The caller then creates its context with that order.  Outputs may be
+ * NULL. */
+int cf_autotune_order(const cf_mesh* mesh, const cf_params* params, const double* hu3, int32_t steps_per_trial,
+                      int32_t* reorder, double* ms_per_step);
 
 /* Diagnostic: the FP64 pipe's throughput on the context's device in FP64 instructions per second
  * (independent FMA chains on every SM, timed with CUDA events), the denominator of the step's

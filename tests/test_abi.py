@@ -93,6 +93,17 @@ def test_mesh_tables_match_oracle(lib, oracle, make):
     assert np.array_equal(a1, a2) and np.array_equal(z1, z2) and np.array_equal(m1, m2)
 
 
+@pytest.mark.parametrize("reorder", [0, 2])
+def test_mesh_tables_do_not_depend_on_the_element_order(lib, reorder):
+    """The device element order (Hilbert by default, Morton, or the caller's) is undone at the
+    boundary: the reference-order tables are the same."""
+    c = cases.flooding(40, 20, seed=3)
+    a = solver.mesh_tables(c)
+    b = solver.mesh_tables(c, dict(reorder=reorder))
+    for x, y in zip(a, b):
+        assert np.array_equal(x, y)
+
+
 def test_boundary_kinds(lib):
     c = cases.flooding(20, 10, seed=3)
     b, _, _, _ = solver.mesh_tables(c)

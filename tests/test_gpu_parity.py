@@ -336,6 +336,33 @@ def test_autotune_leaves_the_run_unchanged(gpu_lib, oracle):
         assert info1.steps == info0.steps and info1.t == info0.t and info1.dt_next == info0.dt_next
         info = s.step(50)
         assert np.array_equal(s.get_state(), ref["U"]) and info.t == ref["t"] and info.steps == 90
+        eb, ept, cb = s.launch_shape()
+        assert eb in (64, 128, 256) and ept in (1, 2) and cb in (128, 256)
+
+
+@pytest.mark.parametrize("iflux", [1, 3, 4])
+def test_every_launch_shape_and_element_order_is_bit_identical(gpu_lib, oracle, iflux):
+    """The autotuner's search space: every edge-kernel shape (64, 128 or 256 threads per block, 1
+    or 2 edges per thread), both element-kernel blocks (128, 256) and the three element orders
+    (Hilbert, Morton, the caller's), with the integer-pipe arithmetic on and off, each run equal
+    to the oracle bit for bit; cf_autotune_order picks one of the orders."""
+    from cuteflow_gb300 import Solver, solver
+    c = cases.flooding(50, 30, seed=21, iflux=iflux)
+    ref = oracle.run(c, 40)
+    shapes = [(eb, ept, cb) for eb in (64, 128, 256) for ept in (1, 2) for cb in (256, 128)]
+    for reorder in (1, 2, 0):
+        with Solver(c, dict(reorder=reorder)) as s:
+            for k, shape in enumerate(shapes):
+                if reorder != 1 and k % 3:
+                    continue
+                s.set_launch_shape(*shape)
+                s.set_tuning(*((1, 0x1F) if k % 2 else (0, 0)))
+                s.set_state(c.U0)
+                info = s.step(40)
+                assert s.launch_shape() == shape
+                assert np.array_equal(s.get_state(), ref["U"]) and info.t == ref["t"], (reorder, shape)
+    r, ms = solver.autotune_order(c, steps_per_trial=5)
+    assert r in (0, 1, 2) and ms > 0
 
 
 def test_set_state_consumes_a_pinned_buffer_before_returning(gpu_lib, oracle):
