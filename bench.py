@@ -222,6 +222,51 @@ def ensemble(nmembers: int, steps: int, warmup: int, seed: int = 3):
             "tuning": {"int_compare": tune[0], "int_mul_warps": tune[1]}}
 
 
+def ensemble_sizes(steps: int = 200, warmup: int = 10, sizes=(20000, 50000, 100000, 200000, 500000)):
+    """Throughput of ensemble-type members by size: one member alone (two members timed, the
+    faster kept) against a batch of eight members of that size, both with the tuned setting
+    (1, 31).  Members: the flooding generator at the benchmark's 2 m spacing on square domains,
+    seeds 500..507.  Shows whether a member run alone is launch- or tail-bound (batching then
+    pays) or already fills the GPU."""
+    import torch
+    from cuteflow_gb300 import Batch, Solver, cases
+    rows = []
+    for target in sizes:
+        ny = int(round(np.sqrt(target / 2.0)))
+        nx = int(round(target / 2.0 / ny))
+        area = 4.0 * nx * ny
+        mem = [cases.flooding(nx, ny, seed=500 + i, lx=2.0 * nx, ly=2.0 * ny, iflux=3,
+                              nbumps=max(1, int(round(8.0 * area / 2.0e6))),
+                              bump_scale=min(1.0, float(np.sqrt(area / 2.0e6)))) for i in range(8)]
+        t_alone = []
+        for c in mem[:2]:
+            with Solver(c) as s:
+                s.set_state(c.U0)
+                s.set_tuning(1, 31)
+                s.step(warmup)
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                s.step(steps)
+                torch.cuda.synchronize()
+                t_alone.append(time.perf_counter() - t0)
+        n = mem[0].nelt
+        with Batch(mem) as b:
+            for i, c in enumerate(mem):
+                b.set_state(i, c.U0)
+            b.set_tuning(1, 31)
+            b.step(warmup, check=False)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            b.step(steps, check=False)
+            torch.cuda.synchronize()
+            tb = time.perf_counter() - t0
+        rows.append({"triangles": n, "wet_fraction": float(np.mean(mem[0].U0[:, 0] > 0)),
+                     "alone_ms_per_step": 1e3 * min(t_alone) / steps, "alone_value": n * steps / min(t_alone),
+                     "batch8_ms_per_step": 1e3 * tb / steps, "batch8_value": 8 * n * steps / tb,
+                     "batched_over_alone": (8 * n * steps / tb) / (n * steps / min(t_alone))})
+    return rows
+
+
 def adjoint_leg(steps: int, warmup: int, obs_every: float = 10.0, budget_gb: float = 64.0):
     """Adjoint Manning calibration: cost of one gradient against one forward.
 
@@ -621,7 +666,7 @@ def main():
     ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="flooding", choices=["flooding", "flooding_muscl", "dam_break", "ensemble"])
+    ap.add_argument("--config", default="flooding", choices=["flooding", "flooding_muscl", "dam_break", "ensemble", "ensemble_sizes"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (every operation on the FP64 pipe)")
     ap.add_argument("--tuning", default=None, metavar="CMP,MASK",
@@ -639,6 +684,15 @@ def main():
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    if args.config == "ensemble_sizes":
+        import torch
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        from cuteflow_gb300 import build
+        build.build()
+        rows = ensemble_sizes()
+        print(json.dumps({"metric": "ensemble member throughput by size: " + METRIC, "unit": UNIT, "n_gpus": 1,
+                          "dtype": "f64", "data": "synthetic", "rows": rows}), flush=True)
+        return
     if args.config == "ensemble":
         import torch
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))

@@ -31,6 +31,8 @@
  */
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "cf_dual.h"
 #include "cf_xd.h"
 
@@ -260,35 +262,35 @@ __device__ __forceinline__ void upwind_chain(const double4* U, int i1, int i2, d
   *o2 = make_double4(wh * hu_.d[3] + wv * vu_.d[3], wh * hu_.d[4] + wv * vu_.d[4], wh * hu_.d[5] + wv * vu_.d[5], 0.0);
 }
 
-template <int IFLUX, int D>
-__global__ void __launch_bounds__(TILE_E) k_adj_edges(AdjArgs A) {
+/* The transposed edge stage of boundary edge e (side A only): its flux differentiated in three
+ * Dual lanes, contracted with the side's slot adjoint. */
+template <int IFLUX>
+__device__ __forceinline__ void adj_boundary_edge(const AdjArgs& A, const MemberDev& M, int e, int2 ab, double t) {
   const StepArgs& a = A.s;
-  const int tile = blockIdx.x;
-  const int m = __ldg(a.etile_mem + tile);
-  const MemberDev& M = a.mdev[m];
-  const int e = tile * TILE_E + threadIdx.x;
-  if (e >= M.edge_end) return;
-  const size_t h = hidx(A.n, m, a.nmembers);
-  const double dt = __ldg(A.dt_hist + h), t = __ldg(A.t_hist + h);
-  const int2 ab = ldro(a.ecell + e);
   const double4 UA = ld4(a.Uin + ab.x);
   const double4 ez = ld4(a.ez + e);
   const Slot wa = A.cadj[ab.x];
-
-  if (ab.y < 0) {
-    const double4 geo = ld4(a.egeo + e);
-    const int id = ldro(a.ebid + e);
-    Dual<3> f1, f2, f3, q;
-    boundary_flux(IFLUX, M, ab.y, id, t, geo.x, geo.y, Dual<3>::var(UA.x, 0), Dual<3>::var(UA.y, 1),
-                  Dual<3>::var(UA.z, 2), UA.w, ez.x, f1, f2, f3, q);
-    const double len = geo.z;
-    double o[3];
+  const double4 geo = ld4(a.egeo + e);
+  const int id = ldro(a.ebid + e);
+  Dual<3> f1, f2, f3, q;
+  boundary_flux(IFLUX, M, ab.y, id, t, geo.x, geo.y, Dual<3>::var(UA.x, 0), Dual<3>::var(UA.y, 1),
+                Dual<3>::var(UA.z, 2), UA.w, ez.x, f1, f2, f3, q);
+  const double len = geo.z;
+  double o[3];
 #pragma unroll
-    for (int i = 0; i < 3; ++i) o[i] = (wa.f1 * f1.d[i] + wa.f2 * f2.d[i] + wa.f3 * f3.d[i]) * len;
-    A.eadj[2 * (size_t)e] = make_double4(o[0], o[1], o[2], 0.0);
-    return;
-  }
+  for (int i = 0; i < 3; ++i) o[i] = (wa.f1 * f1.d[i] + wa.f2 * f2.d[i] + wa.f3 * f3.d[i]) * len;
+  A.eadj[2 * (size_t)e] = make_double4(o[0], o[1], o[2], 0.0);
+}
 
+/* The transposed edge stage of interior edge e: the edge's slot values differentiated in Dual<D>
+ * chunks over its 6 (first order) or 10 (WAF: + the upwind reconstructions) inputs, contracted
+ * with the slot adjoints of its two elements. */
+template <int IFLUX, int D>
+__device__ __forceinline__ void adj_interior_edge(const AdjArgs& A, const MemberDev& M, int e, int2 ab, double dt) {
+  const StepArgs& a = A.s;
+  const double4 UA = ld4(a.Uin + ab.x);
+  const double4 ez = ld4(a.ez + e);
+  const Slot wa = A.cadj[ab.x];
   const double4 UB = ld4(a.Uin + ab.y);
   const Slot wb = A.cadj[ab.y];
   const EdgeGeo G = edge_geo(a, e, IFLUX >= 3);
@@ -332,6 +334,65 @@ __global__ void __launch_bounds__(TILE_E) k_adj_edges(AdjArgs A) {
     u[1] = c1;
     u[2] = c2;
     u[3] = c3;
+  }
+}
+
+template <int IFLUX, int D>
+__global__ void __launch_bounds__(TILE_E) k_adj_edges(AdjArgs A) {
+  const StepArgs& a = A.s;
+  const int tile = blockIdx.x;
+  const int m = __ldg(a.etile_mem + tile);
+  const MemberDev& M = a.mdev[m];
+  const int e = tile * TILE_E + threadIdx.x;
+  if (e >= M.edge_end) return;
+  const size_t h = hidx(A.n, m, a.nmembers);
+  const double dt = __ldg(A.dt_hist + h), t = __ldg(A.t_hist + h);
+  const int2 ab = ldro(a.ecell + e);
+  if (ab.y < 0) adj_boundary_edge<IFLUX>(A, M, e, ab, t);
+  else adj_interior_edge<IFLUX, D>(A, M, e, ab, dt);
+}
+
+/* First-order HLLC (flux_mode 0): the closed-form reverse edge (adj_edge_hllc: frame change,
+ * reconstruction, tangential velocities and bed sources by hand around a Dual<4> flux core) for
+ * every interior edge it covers, at three blocks per SM; the edges it leaves (a nearly dry side
+ * whose raw and masked depths differ) are queued for k_adj_edges_rest. */
+__global__ void __launch_bounds__(TILE_E, 3) k_adj_edges_hllc(AdjArgs A) {
+  const StepArgs& a = A.s;
+  const int tile = blockIdx.x;
+  const int m = __ldg(a.etile_mem + tile);
+  const MemberDev& M = a.mdev[m];
+  const int e = tile * TILE_E + threadIdx.x;
+  if (e >= M.edge_end) return;
+  const int2 ab = ldro(a.ecell + e);
+  if (ab.y < 0) {
+    adj_boundary_edge<1>(A, M, e, ab, __ldg(A.t_hist + hidx(A.n, m, a.nmembers)));
+    return;
+  }
+  const double4 UA = ld4(a.Uin + ab.x), UB = ld4(a.Uin + ab.y);
+  const double4 ez = ld4(a.ez + e);
+  const Slot wa = A.cadj[ab.x], wb = A.cadj[ab.y];
+  const EdgeGeo G = edge_geo(a, e, false);
+  const double w[10] = {wa.f1, wa.f2, wa.f3, wa.bx, wa.by, wb.f1, wb.f2, wb.f3, wb.bx, wb.by};
+  double la[3], lb[3];
+  if (adj_edge_hllc(M, G, UA, UB, ez.x, ez.y, w, la, lb)) {
+    A.eadj[2 * (size_t)e] = make_double4(la[0], la[1], la[2], 0.0);
+    A.eadj[2 * (size_t)e + 1] = make_double4(lb[0], lb[1], lb[2], 0.0);
+  } else {
+    A.pend[atomicAdd(A.npend, 1)] = e;
+  }
+}
+
+/* The queued interior edges of k_adj_edges_hllc, differentiated in six Dual lanes (grid-stride
+ * over the queue; the queue's order does not matter, every edge writes only its own entries). */
+__global__ void __launch_bounds__(TILE_E) k_adj_edges_rest(AdjArgs A) {
+  const StepArgs& a = A.s;
+  const int n = *A.npend;
+  for (int i = blockIdx.x * TILE_E + threadIdx.x; i < n; i += gridDim.x * TILE_E) {
+    const int e = A.pend[i];
+    const int m = __ldg(a.etile_mem + e / TILE_E);
+    const MemberDev& M = a.mdev[m];
+    const double dt = __ldg(A.dt_hist + hidx(A.n, m, a.nmembers));
+    adj_interior_edge<1, 6>(A, M, e, ldro(a.ecell + e), dt);
   }
 }
 
@@ -427,7 +488,15 @@ int launch_adjoint_step(const AdjArgs& A, stream_t s) {
   const StepArgs& a = A.s;
   k_adj_cells<<<a.n_ctiles, TILE_C, 0, st>>>(A);
   switch (a.iflux) {
-    case 1: k_adj_edges<1, 6><<<a.n_etiles, TILE_E, 0, st>>>(A); break;
+    case 1:
+      if (a.flux_mode == 0 && A.pend && A.npend) {
+        cudaMemsetAsync(A.npend, 0, sizeof(int32_t), st);
+        k_adj_edges_hllc<<<a.n_etiles, TILE_E, 0, st>>>(A);
+        k_adj_edges_rest<<<std::min(a.n_etiles, 304), TILE_E, 0, st>>>(A);
+      } else {
+        k_adj_edges<1, 6><<<a.n_etiles, TILE_E, 0, st>>>(A);
+      }
+      break;
     case 2: k_adj_edges<2, 3><<<a.n_etiles, TILE_E, 0, st>>>(A); break;
     case 3: k_adj_edges<3, 2><<<a.n_etiles, TILE_E, 0, st>>>(A); break;
     default: return CF_ENOTSUP;

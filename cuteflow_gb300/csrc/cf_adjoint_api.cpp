@@ -72,6 +72,8 @@ struct cf_adjoint {
   int32_t* uidx = nullptr;
   double* gman = nullptr;
   uint32_t* flag = nullptr;
+  int32_t* pend = nullptr;   /* the reverse edge kernel's queue of edges for its six-lane path */
+  int32_t* npend = nullptr;
   int32_t freeze_r = 0;      /* linearization of the WAF limiter ratios: 0 exact, 1 held */
   bool recorded = false;     /* a recording forward has filled dt_hist / t_hist */
   bool have_traj = false;    /* the checkpoints hold the last forward's trajectory */
@@ -92,7 +94,7 @@ struct cf_zones {
 namespace {
 
 void adj_free(cf_adjoint* a) {
-  void* ptrs[] = {a->pp, a->ckpt, a->seg, a->mst, a->dt_hist, a->t_hist, a->eta, a->wbuf, a->gcell, a->goff, a->gidx,
+  void* ptrs[] = {a->pend, a->npend, a->pp, a->ckpt, a->seg, a->mst, a->dt_hist, a->t_hist, a->eta, a->wbuf, a->gcell, a->goff, a->gidx,
                   a->lam[0], a->lam[1], a->sums, a->cadj, a->eadj, a->uadj, a->uoff, a->uidx, a->gman, a->flag};
   for (void* p : ptrs)
     if (p) cudaFree(p);
@@ -152,6 +154,7 @@ int create_impl(cf_ctx* c, int32_t nsteps, int32_t interval, const int32_t* gaug
   /* device bytes besides the record pool and the checkpoints (upper bound for the upwind lists) */
   const int64_t st4 = (int64_t)np * (int64_t)sizeof(double4), rec = st4 + (int64_t)np * (int64_t)sizeof(Slot);
   const int64_t fixed = 4 * st4 + (int64_t)np * (int64_t)sizeof(Slot) + 2 * (int64_t)nep * (int64_t)sizeof(double4) +
+                        4 * (int64_t)nep + 4 +
                         (int64_t)np * 8 + (int64_t)nsteps * (16 * (int64_t)nm + 16 * (int64_t)ngauges) +
                         (int64_t)(np + 1) * 4 + 8 * (int64_t)ngauges + (int64_t)nm * (int64_t)sizeof(MemberState) +
                         (second ? 4 * (int64_t)nep * (int64_t)sizeof(double4) + (int64_t)(np + 1) * 4 +
@@ -201,7 +204,8 @@ int create_impl(cf_ctx* c, int32_t nsteps, int32_t interval, const int32_t* gaug
       (rc = dalloc(c, &a->goff, np + 1)) || (rc = dalloc(c, &a->gidx, (size_t)ngauges)) ||
       (rc = dalloc(c, &a->lam[0], np)) || (rc = dalloc(c, &a->lam[1], np)) || (rc = dalloc(c, &a->cadj, np)) ||
       (rc = dalloc(c, &a->sums, (size_t)a->nseg_states * np)) ||
-      (rc = dalloc(c, &a->eadj, 2 * nep)) || (rc = dalloc(c, &a->gman, np)) || (rc = dalloc(c, &a->flag, 1)))
+      (rc = dalloc(c, &a->eadj, 2 * nep)) || (rc = dalloc(c, &a->gman, np)) || (rc = dalloc(c, &a->flag, 1)) ||
+      (rc = dalloc(c, &a->pend, nep)) || (rc = dalloc(c, &a->npend, 1)))
     return done(rc);
   /* gauges: new order, and their CSR over the elements */
   {
@@ -408,6 +412,8 @@ int backward_impl(cf_adjoint* a, const double* w_eta, const double* w_state, dou
       A.gw = (weights && k + 1 < a->N) ? a->wbuf + (size_t)k * a->G : nullptr;
       A.gman = a->gman;
       A.freeze_r = a->freeze_r;
+      A.pend = a->pend;
+      A.npend = a->npend;
       const int r = launch_adjoint_step(A, st);
       if (r) return fail(c, r, "adjoint launch failed");
       first = false;

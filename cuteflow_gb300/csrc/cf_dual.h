@@ -202,6 +202,94 @@ CFD_HD Dual<N> rcbrt(const Dual<N>& x) {
   return r;
 }
 
+/* The transposed edge stage of an interior first-order HLLC edge (IFLUX 1, flux_mode 0): given the
+ * adjoint weights w[10] of its two slots (side A: flux 1-3, bed x, y; then side B), the
+ * contributions lamA, lamB to the adjoints of (h, hu, hv) of its two elements, i.e. J^T w for the
+ * edge's Jacobian J, at a fraction of the cost of differentiating the whole edge in six lanes:
+ *   - the change to the edge frame and the hydrostatic reconstruction have closed-form
+ *     derivatives (u_n = (hu nx + hv ny) / h, u_t = (hv nx - hu ny) / h; reconstructed depths pass
+ *     or are clamped to 0);
+ *   - the flux core depends on (hl, ul, hr, ur) and on the tangential velocities only through its
+ *     tangential components, which are x1 vl or x1 vr (side A) and y1 vl or y1 vr (side B) with
+ *     the region telling which (first_order_flux reports it): the core runs on Dual<4> numbers over
+ *     (hl, ul, hr, ur), and the tangential derivatives are x1, y1;
+ *   - the bed sources g/2 (ha^2 - h^2) len have closed-form derivatives.
+ * The value lanes repeat the step's IEEE operations, so every branch is the forward's.  Returns
+ * false, and the caller differentiates the edge in full, where a side's raw and masked depths
+ * differ (0 < h <= tolisec; the reference then evaluates the two sides differently). */
+CFD_HD bool adj_edge_hllc(const MemberDev& M, const EdgeGeo& G, const double4& UA, const double4& UB, double zml,
+                          double zmr, const double w[10], double lamA[3], double lamB[3]) {
+  const double g = M.gp, tolisec = M.tolisec, nx = G.nx, ny = G.ny, len = G.len;
+  const double zij = dmax(zml, zmr);
+  double hautl, vitul, vitvl, hautr, vitur, vitvr;
+  to_frame(UA.x, UA.y, UA.z, UA.w, nx, ny, tolisec, hautl, vitul, vitvl);
+  to_frame(UB.x, UB.y, UB.z, UB.w, nx, ny, tolisec, hautr, vitur, vitvr);
+  if (hautl != UA.x || hautr != UB.x) return false;
+  /* hydrostatic reconstruction (flux_riemann.cuf:176-181, :200-210); which variables carry a
+   * derivative (a clamped or masked one is a constant of the inputs) */
+  const double el = hautl + zml - zij, er = UB.x + zmr - zij;
+  double hl = dmax(0.0, el), hr = dmax(0.0, er);
+  double ul = vitul, vl = vitvl, ur = vitur, vr = vitvr;
+  const bool pl = !(hl < tolisec), pr = !(hr < tolisec);
+  if (!pl) { hl = 0.; ul = 0.; vl = 0.; }
+  if (!pr) { hr = 0.; ur = 0.; vr = 0.; }
+  const bool wa = UA.x > tolisec, wb = UB.x > tolisec;   /* frame velocities differentiable */
+  const bool s_hl = pl && 0.0 < el, s_ul = pl && wa, s_hr = pr && 0.0 < er, s_ur = pr && wb;
+  const Dual<4> Hl = s_hl ? Dual<4>::var(hl, 0) : Dual<4>(hl), Ul = s_ul ? Dual<4>::var(ul, 1) : Dual<4>(ul);
+  const Dual<4> Hr = s_hr ? Dual<4>::var(hr, 2) : Dual<4>(hr), Ur = s_ur ? Dual<4>::var(ur, 3) : Dual<4>(ur);
+  TwoFluxT<Dual<4>> F;
+  HllcRegions rg;
+  first_order_flux<1>(g, nx, ny, Hl, Ul, Dual<4>(vl), Hr, Ur, Dual<4>(vr), F, &rg);
+  /* w^T d(slot fluxes)/d(hl, ul, hr, ur): the slots hold F * len */
+  double gc[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+    gc[i] = len * (w[0] * F.a1.d[i] + w[1] * F.a2.d[i] + w[2] * F.a3.d[i] + w[5] * F.b1.d[i] + w[6] * F.b2.d[i] +
+                   w[7] * F.b3.d[i]);
+  /* tangential velocities: a2 = nx x2 - ny x3, a3 = ny x2 + nx x3 with x3 = x1 v (x1 = a1);
+   * b2 = -(nx y2 - ny y3), b3 = -(ny y2 + nx y3) with y3 = y1 v (y1 = -b1) */
+  double gvl = 0.0, gvr = 0.0;
+  if (rg.valid) {
+    const double ga = len * (w[2] * nx - w[1] * ny) * F.a1.v;
+    const double gb = len * (w[7] * nx - w[6] * ny) * F.b1.v;   /* (ny w6 - nx w7) y1 with y1 = -b1 */
+    if (rg.a_vr) gvr += ga; else gvl += ga;
+    if (rg.b_vr) gvr += gb; else gvl += gb;
+  }
+  /* to the conserved variables: d(h_m, u_n, u_t)/d(h, hu, hv) with y = RN(1/h) */
+  lamA[0] = lamA[1] = lamA[2] = 0.0;
+  lamB[0] = lamB[1] = lamB[2] = 0.0;
+  {
+    const double gh = s_hl ? gc[0] : 0.0, gu = s_ul ? gc[1] : 0.0, gv = s_ul ? gvl : 0.0;
+    if (wa) {
+      const double y = UA.w;
+      lamA[0] = gh - (gu * vitul + gv * vitvl) * y;
+      lamA[1] = (gu * nx - gv * ny) * y;
+      lamA[2] = (gu * ny + gv * nx) * y;
+    }
+  }
+  {
+    const double gh = s_hr ? gc[2] : 0.0, gu = s_ur ? gc[3] : 0.0, gv = s_ur ? gvr : 0.0;
+    lamB[0] = gh;   /* the B side reconstructs from the raw depth */
+    if (wb) {
+      const double y = UB.w;
+      lamB[0] -= (gu * vitur + gv * vitvr) * y;
+      lamB[1] = (gu * nx - gv * ny) * y;
+      lamB[2] = (gu * ny + gv * nx) * y;
+    }
+  }
+  /* bed sources (source_terms.cuf:90-97): ta = g/2 (ha^2 - hA^2) len into (ta nx, ta ny) of
+   * side A, tb likewise into -(tb nx, tb ny) of side B */
+  {
+    const double ea = UA.x + zml - zij, eb = UB.x + zmr - zij;
+    const double ha = dmax(0.0, ea), hb = dmax(0.0, eb);
+    const double dta = g / 2.0 * (2.0 * (0.0 < ea ? ha : 0.0) - 2.0 * UA.x) * len;
+    const double dtb = g / 2.0 * (2.0 * (0.0 < eb ? hb : 0.0) - 2.0 * UB.x) * len;
+    lamA[0] += (w[3] * nx + w[4] * ny) * dta;
+    lamB[0] -= (w[8] * nx + w[9] * ny) * dtb;
+  }
+  return true;
+}
+
 }  // namespace cf
 
 #endif

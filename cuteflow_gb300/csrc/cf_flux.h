@@ -274,11 +274,21 @@ CF_HD CF_INLINE void reproject_both(double nx, double ny, T x1, T x2, T x3, T y1
  * al. (IFLUX 2, :1029-1182), for both sides.  Side B's evaluation is the mirror image
  * (h -> h, u_n -> -u_n, u_t -> -u_t, s_L -> -s_R, s_R -> -s_L, s_* -> -s_*): it selects a
  * region with its own tests and its vector is the mirror of an A-frame vector. */
+/* Which tangential velocity the HLLC (IFLUX 1) tangential fluxes of the two sides carry, for the
+ * adjoint: the tangential component of side A's frame flux is x1 * (vl or vr) and side B's is
+ * y1 * (vl or vr) in every region (FL: hl ul vl = fl1 vl, FR: fr1 vr, HLL: h1 times the velocity of
+ * the upwind side of s*).  a_vr / b_vr: 1 when the side's velocity is vr; valid 0 when both sides
+ * are dry (zero flux). */
+struct HllcRegions {
+  int valid, a_vr, b_vr;
+};
+
 template <int IFLUX, class T>
 CF_HD CF_INLINE void first_order_flux(double g, double nx, double ny, T hl, T ul, T vl, T hr, T ur, T vr,
-                                      TwoFluxT<T>& F) {
+                                      TwoFluxT<T>& F, HllcRegions* regions = nullptr) {
   const double eps = (IFLUX == 1) ? EPS_HLLC : EPS_RIADH;
   T sl, sr, set;
+  if (regions) regions->valid = 0;
   if (!wave_speeds(g, eps, hl, ul, hr, ur, sl, sr, set)) {
     F.a1 = F.a2 = F.a3 = F.b1 = F.b2 = F.b3 = T(0.0);
     return;
@@ -303,6 +313,11 @@ CF_HD CF_INLINE void first_order_flux(double g, double nx, double ny, T hl, T ul
     if (rb == 0) { y1 = fl1; y2 = fl2; y3 = fl3; }
     else if (rb == 1) { y1 = fr1; y2 = fr2; y3 = fr3; }
     else { y1 = h1; y2 = h2; y3 = (-set > 0.) ? h1 * vr : h1 * vl; }
+    if (regions) {
+      regions->valid = 1;
+      regions->a_vr = (ra == 1 || (ra == 2 && !(set > 0.))) ? 1 : 0;
+      regions->b_vr = (rb == 1 || (rb == 2 && (-set > 0.))) ? 1 : 0;
+    }
   } else {
     const T pl = (fabs(sl - set) > eps) ? hl * (sl - ul) / (sl - set) : T(0.0);
     const T pr = (fabs(sr - set) > eps) ? hr * (sr - ur) / (sr - set) : T(0.0);

@@ -233,6 +233,8 @@ struct AdjArgs {
   const double* gw;        /* objective weights of the gauge elevations after step n+1, or NULL */
   double* gman;            /* dJ/dn, accumulated */
   int32_t freeze_r;        /* 1: WAF limiter ratios held constant in the linearization */
+  int32_t* pend;           /* first-order HLLC: interior edges left to the six-lane kernel */
+  int32_t* npend;          /* their count (zeroed before each reverse step) */
 };
 
 /* Step n with the recorded dt / time: edge stage, then element stage writing a.Uout (if not

@@ -520,3 +520,71 @@ extern "C" long long harness_dry_check(long long n, unsigned long long seed, lon
   if (taken) *taken = took;
   return bad;
 }
+
+/* adj_edge_hllc (the reverse edge kernel's closed-form first-order HLLC path) against the generic
+ * path it replaces (the edge differentiated in six Dual lanes and contracted with the weights) on n
+ * random interior edges: wet, dry and nearly dry sides (clamped reconstructions, masked frames),
+ * equal and unequal beds, random normals, velocities and weights.  Returns the largest difference
+ * relative to the largest contribution of the edge; *taken counts the edges the path handled. */
+#include "../cuteflow_gb300/csrc/cf_dual.h"
+extern "C" double harness_adj_hllc_check(long long n, unsigned long long seed, long long* taken) {
+  unsigned long long s = seed | 1;
+  auto rnd = [&]() { s ^= s << 13; s ^= s >> 7; s ^= s << 17; return s; };
+  auto unif = [&]() { return (double)(rnd() >> 11) * (1.0 / 9007199254740992.0); };
+  double worst = 0.0;
+  long long took = 0;
+  for (long long i = 0; i < n; ++i) {
+    MemberDev M;
+    std::memset(&M, 0, sizeof(M));
+    M.gp = 9.81;
+    M.tolisec = (rnd() & 1) ? 1e-4 : 1e-5;
+    auto depth = [&]() {
+      const unsigned k = (unsigned)(rnd() % 8);
+      if (k == 0) return 0.0;
+      if (k == 1) return 0.5 * M.tolisec * unif();
+      if (k == 2) return 1e-3 * unif();
+      return 0.01 + 5.0 * unif();
+    };
+    const double hA = depth(), hB = depth();
+    auto state = [&](double h) {
+      const double u = 3.0 * (unif() - 0.5), v = 3.0 * (unif() - 0.5);
+      return make_double4(h, h * u, h * v, h > 0.0 ? 1.0 / h : 0.0);
+    };
+    const double4 UA = state(hA), UB = state(hB);
+    const double ang = 6.283185307179586 * unif();
+    EdgeGeo G;
+    std::memset(&G, 0, sizeof(G));
+    G.nx = std::cos(ang);
+    G.ny = std::sin(ang);
+    G.len = 0.2 + 2.0 * unif();
+    G.d_mrl = 1.0;
+    const double zml = (rnd() % 4 == 0) ? 0.0 : 2.0 * unif();
+    const double zmr = (rnd() % 4 == 0) ? zml : 2.0 * unif();
+    double w[10];
+    for (int k = 0; k < 10; ++k) w[k] = unif() - 0.5;
+    double la[3], lb[3];
+    if (!adj_edge_hllc(M, G, UA, UB, zml, zmr, w, la, lb)) continue;
+    ++took;
+    Dual<6> o[10];
+    auto sd = [](double v, int k) { Dual<6> r(v); r.d[k] = 1.0; return r; };
+    interior_edge<1>(M, 1, 0, G, 0.01, sd(UA.x, 0), sd(UA.y, 1), sd(UA.z, 2), zml, UA.w, sd(UB.x, 3), sd(UB.y, 4),
+                     sd(UB.z, 5), zmr, UB.w, Dual<6>(0.0), Dual<6>(0.0), 0.0, Dual<6>(0.0), Dual<6>(0.0), 0.0, o);
+    double acc[6], scale = 1e-300;
+    for (int j = 0; j < 6; ++j) {
+      double v = 0.0;
+      for (int k = 0; k < 10; ++k) {
+        v = std::fma(w[k], o[k].d[j], v);
+        scale = std::max(scale, std::fabs(w[k] * o[k].d[j]));
+      }
+      acc[j] = v;
+    }
+    const double got[6] = {la[0], la[1], la[2], lb[0], lb[1], lb[2]};
+    for (int j = 0; j < 6; ++j) {
+      const double d = std::fabs(got[j] - acc[j]);
+      if (!(d <= 1e300)) return 1e300;   /* a NaN or an infinity on either side */
+      worst = std::max(worst, d / scale);
+    }
+  }
+  if (taken) *taken = took;
+  return worst;
+}

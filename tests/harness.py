@@ -141,3 +141,14 @@ def dry_check(n, seed=12345):
     took = C.c_longlong(0)
     bad = int(L.harness_dry_check(int(n), int(seed), C.byref(took)))
     return bad, int(took.value)
+
+
+def adj_hllc_check(n, seed=12345):
+    """(largest relative difference, edges handled) of harness_adj_hllc_check: the closed-form
+    first-order HLLC reverse edge against the six-lane Dual differentiation of the edge."""
+    L = lib()
+    L.harness_adj_hllc_check.argtypes = [C.c_longlong, C.c_ulonglong, C.POINTER(C.c_longlong)]
+    L.harness_adj_hllc_check.restype = C.c_double
+    took = C.c_longlong(0)
+    worst = float(L.harness_adj_hllc_check(int(n), int(seed), C.byref(took)))
+    return worst, int(took.value)

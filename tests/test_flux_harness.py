@@ -160,3 +160,13 @@ def test_dry_region_shortcuts_are_the_general_result():
     bad, took = H.dry_check(400_000, seed=7)
     assert took > 200_000
     assert bad == 0
+
+
+def test_closed_form_hllc_reverse_edge_is_the_dual_derivative():
+    """The reverse edge kernel's closed-form path for first-order HLLC (frame change, hydrostatic
+    reconstruction, tangential velocities and bed sources by hand around a Dual<4> flux core)
+    equals the edge differentiated in six Dual lanes, to round-off, on random wet, dry and nearly
+    dry edges; nearly dry sides (raw and masked depths differ) are left to the six-lane path."""
+    worst, took = H.adj_hllc_check(200_000, seed=11)
+    assert took > 100_000
+    assert worst < 1e-12, worst
