@@ -15,6 +15,8 @@
  */
 #include <cuda_runtime.h>
 
+#include <cstddef>
+
 #include <algorithm>
 #include <atomic>
 #include <cmath>
@@ -79,6 +81,9 @@ StepArgs step_args(const cf_ctx* c, int parity) {
   a.eblock = c->eblock;
   a.ept = c->ept;
   a.cblock = c->cblock;
+  a.c_lo = 0;
+  a.c_hi = 0x7fffffff;
+  a.bq = c->bq;
   return a;
 }
 
@@ -86,12 +91,14 @@ void free_all(cf_ctx* c) {
   if (c->graph2) cudaGraphExecDestroy(c->graph2);
   void* ptrs[] = {c->U[0], c->U[1], c->cslot, c->cstat, c->zcell, c->perm, c->iperm, c->ecell, c->egeo, c->ez,
                   c->ebid, c->eupw, c->ewts, c->edk, c->einv, c->slots, c->etile_mem, c->ctile_mem, c->mdev,
-                  c->mst, c->staging, c->inl_cell, c->inl_len, c->ids};
+                  c->mst, c->staging, c->inl_cell, c->inl_len, c->ids, c->bq, c->elist1, c->elist2,
+                  c->xsend, c->xrecv, c->terms};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (c->host_state) cudaFreeHost(c->host_state);
   for (auto& e : c->ev)
     if (e) cudaEventDestroy(e);
+  if (c->ev_pack) cudaEventDestroy(c->ev_pack);
   if (c->stream) cudaStreamDestroy(c->stream);
 }
 
@@ -195,7 +202,8 @@ MemberDev member_dev(const Member& M) {
 }
 
 /* Build a context of nm members (the meshes are preprocessed in parallel on the host). */
-int create_impl(const cf_mesh* meshes, const cf_params* params, int32_t nm, cf_ctx** out) {
+int create_impl(const cf_mesh* meshes, const cf_params* params, int32_t nm, cf_ctx** out,
+                const int32_t* elem_class = nullptr) {
   if (!out) return fail(nullptr, CF_EINVAL, "out is NULL");
   *out = nullptr;
   if (!meshes || !params || nm < 1) return fail(nullptr, CF_EINVAL, "meshes/params NULL or no member");
@@ -222,7 +230,8 @@ int create_impl(const cf_mesh* meshes, const cf_params* params, int32_t nm, cf_c
     unsigned hw = std::max(1u, std::thread::hardware_concurrency());
     int nth = (int)std::min<unsigned>(hw, (unsigned)nm);
     auto work = [&]() {
-      for (int i = next++; i < nm; i = next++) rcs[i] = prepare_mesh(&meshes[i], &params[i], c->mem[i].prep, errs[i]);
+      for (int i = next++; i < nm; i = next++)
+        rcs[i] = prepare_mesh(&meshes[i], &params[i], c->mem[i].prep, errs[i], elem_class);
     };
     std::vector<std::thread> th;
     for (int t = 1; t < nth; ++t) th.emplace_back(work);
@@ -347,6 +356,34 @@ int create_impl(const cf_mesh* meshes, const cf_params* params, int32_t nm, cf_c
     std::vector<double4>().swap(P.ez);
     std::vector<int32_t>().swap(P.ebid);
     std::vector<HostEdge>().swap(P.edges);
+  }
+  /* boundary edges in reference order (flat, edge offsets applied) */
+  {
+    std::vector<int32_t> bq;
+    for (int i = 0; i < nm; ++i) {
+      Member& M = c->mem[i];
+      mdev[i].bq_begin = M.dev.bq_begin = (int32_t)bq.size();
+      mdev[i].bq_count = M.dev.bq_count = (int32_t)M.prep.bq_ref.size();
+      for (int32_t e : M.prep.bq_ref) bq.push_back(e + M.edge_off);
+    }
+    if ((rc = dalloc(c, &c->bq, bq.size())) || (rc = put(c, c->bq, bq.data(), bq.size()))) return done(rc);
+  }
+  /* a part of a decomposed mesh: its phase edge lists */
+  if (elem_class) {
+    const Prep& P = c->mem[0].prep;
+    c->is_part = true;
+    c->n_send = P.n_send;
+    c->n_own = P.n_own;
+    c->nel1 = (int32_t)P.elist1.size();
+    c->nel2 = (int32_t)P.elist2.size();
+    if ((rc = dalloc(c, &c->elist1, P.elist1.size())) || (rc = dalloc(c, &c->elist2, P.elist2.size())) ||
+        (rc = put(c, c->elist1, P.elist1.data(), P.elist1.size())) ||
+        (rc = put(c, c->elist2, P.elist2.data(), P.elist2.size())))
+      return done(rc);
+    e = cudaEventCreateWithFlags(&c->ev_pack, cudaEventDisableTiming);
+    if (e != cudaSuccess) return done(cuda_fail(c, e, "cudaEventCreate"));
+    const size_t nt = std::max(P.inl_cell.size() * (size_t)std::max(P.nin, 1), P.bq_ref.size());
+    if ((rc = dalloc(c, &c->terms, std::max<size_t>(nt, 1)))) return done(rc);
   }
   if ((rc = put(c, c->etile_mem, etm.data(), etm.size())) || (rc = put(c, c->ctile_mem, ctm.data(), ctm.size())) ||
       (rc = put(c, c->mdev, mdev.data(), mdev.size())))
@@ -537,7 +574,8 @@ int enqueue_steps(cf_ctx* c, int32_t nsteps) {
     c->launches = 2 * (int64_t)nsteps;
   }
   c->launched += nsteps;
-  rc = launch_discharge(c->slots, c->ecell, c->mdev, c->mst, (int32_t)c->mem.size(), reinterpret_cast<stream_t>(c->stream));
+  rc = launch_discharge(c->slots, c->ecell, c->bq, c->mdev, c->mst, (int32_t)c->mem.size(),
+                        reinterpret_cast<stream_t>(c->stream));
   if (rc != CF_OK) return fail(c, rc, "discharge launch failed");
   return CF_OK;
 }
@@ -645,7 +683,7 @@ int cf::step_with_slots(cf_ctx* c, int32_t nsteps, cf_step_info* infos, Slot* sl
       if ((rc = launch_step(a, s, nullptr, nullptr))) return fail(c, rc, "step launch failed");
     }
     c->launched += nsteps;
-    rc = launch_discharge(slots, c->ecell, c->mdev, c->mst, (int32_t)c->mem.size(), s);
+    rc = launch_discharge(slots, c->ecell, c->bq, c->mdev, c->mst, (int32_t)c->mem.size(), s);
     if (rc != CF_OK) return fail(c, rc, "discharge launch failed");
   }
   c->flux_ms = c->update_ms = 0.0;
@@ -1144,6 +1182,157 @@ int cf_get_sizes(cf_ctx* c, int64_t* nelt, int64_t* nedge) {
 void* cf_get_stream(cf_ctx* c) { return c ? (void*)c->stream : nullptr; }
 
 const char* cf_last_error(const cf_ctx* c) { return c ? c->err.c_str() : g_create_error.c_str(); }
+
+/* ---- a part of a decomposed mesh ----------------------------------------------------------- */
+
+namespace {
+
+int part_ok(cf_ctx* c) {
+  if (!c) return CF_EINVAL;
+  if (!c->is_part) return fail(c, CF_EINVAL, "not a part context (cf_create_part)");
+  return CF_OK;
+}
+
+/* terms (device) -> dst (host or device), count doubles, waiting for them */
+int part_terms_out(cf_ctx* c, double* dst, size_t count) {
+  if (count) CF_CUDA(c, cudaMemcpyAsync(dst, c->terms, count * sizeof(double), cudaMemcpyDefault, c->stream));
+  CF_CUDA(c, cudaStreamSynchronize(c->stream));
+  return CF_OK;
+}
+
+}  // namespace
+
+int cf_create_part(const cf_mesh* mesh, const cf_params* params, const int32_t* elem_class, cf_ctx** out) {
+  if (!elem_class) return fail(nullptr, CF_EINVAL, "elem_class is NULL");
+  return abi_guard(nullptr, [&] { return create_impl(mesh, params, 1, out, elem_class); });
+}
+
+int cf_part_sizes(cf_ctx* c, int32_t* n_send, int32_t* n_own, int32_t* inlet_entries, int32_t* boundary_edges) {
+  int rc = part_ok(c);
+  if (rc) return rc;
+  const Member& M = c->mem[0];
+  if (n_send) *n_send = c->n_send;
+  if (n_own) *n_own = c->n_own;
+  if (inlet_entries) *inlet_entries = M.dev.inl_count;
+  if (boundary_edges) *boundary_edges = M.dev.bq_count;
+  return CF_OK;
+}
+
+int cf_part_set_exchange(cf_ctx* c, const int32_t* send_ids, int32_t nsend, const int32_t* recv_ids, int32_t nrecv) {
+  int rc = part_ok(c);
+  if (rc) return rc;
+  if (nsend < 0 || nrecv < 0 || (nsend && !send_ids) || (nrecv && !recv_ids))
+    return fail(c, CF_EINVAL, "exchange lists NULL or negative counts");
+  const Prep& P = c->mem[0].prep;
+  std::vector<int32_t> s(nsend), r(nrecv);
+  for (int32_t i = 0; i < nsend; ++i) {
+    if (send_ids[i] < 0 || send_ids[i] >= P.nelt || P.iperm[send_ids[i]] >= c->n_send)
+      return fail(c, CF_EINVAL, "send element " + std::to_string(send_ids[i]) + " is not a send element of the part");
+    s[i] = P.iperm[send_ids[i]];
+  }
+  for (int32_t i = 0; i < nrecv; ++i) {
+    if (recv_ids[i] < 0 || recv_ids[i] >= P.nelt || P.iperm[recv_ids[i]] < c->n_own)
+      return fail(c, CF_EINVAL, "receive element " + std::to_string(recv_ids[i]) + " is not a halo element of the part");
+    r[i] = P.iperm[recv_ids[i]];
+  }
+  CF_CUDA(c, cudaSetDevice(c->device));
+  CF_CUDA(c, cudaStreamSynchronize(c->stream));
+  if (c->xsend) cudaFree(c->xsend);
+  if (c->xrecv) cudaFree(c->xrecv);
+  c->xsend = c->xrecv = nullptr;
+  c->nxsend = c->nxrecv = 0;
+  if ((rc = dalloc(c, &c->xsend, s.size())) || (rc = dalloc(c, &c->xrecv, r.size())) ||
+      (rc = put(c, c->xsend, s.data(), s.size())) || (rc = put(c, c->xrecv, r.data(), r.size())))
+    return rc;
+  c->nxsend = nsend;
+  c->nxrecv = nrecv;
+  return CF_OK;
+}
+
+int cf_part_step_begin(cf_ctx* c, double* send_buf) {
+  int rc = part_ok(c);
+  if (rc) return rc;
+  CF_CUDA(c, cudaSetDevice(c->device));
+  double* v = static_cast<double*>(device_view(c, send_buf));
+  if (c->nxsend && !v) return fail(c, CF_EINVAL, "the send buffer must be device memory or pinned host memory");
+  if (c->any_phys_inflow && !c->external_sums)
+    return fail(c, CF_ESTATE, "a phys_inflow part needs the whole mesh's inlet sums (cf_part_set_inlet_sums)");
+  const stream_t st = reinterpret_cast<stream_t>(c->stream);
+  StepArgs a = step_args(c, (int)(c->launched & 1));
+  a.steady = 0;        /* the steady-state test runs on the whole mesh's discharges (cf_part_apply_discharges) */
+  a.phys_inflow = 0;   /* the inlet sums are the whole mesh's (cf_part_set_inlet_sums) */
+  /* the send elements first, their states out to the other parts, then the interior elements */
+  if ((rc = launch_part_phase(a, 1, c->elist1, c->nel1, 0, c->n_send, st))) return fail(c, rc, "step launch failed");
+  if ((rc = launch_pack(a.Uout, c->xsend, c->nxsend, v, st))) return fail(c, rc, "pack launch failed");
+  CF_CUDA(c, cudaEventRecord(c->ev_pack, c->stream));
+  if ((rc = launch_part_phase(a, 2, c->elist2, c->nel2, c->n_send, c->n_own, st))) return fail(c, rc, "step launch failed");
+  c->launched += 1;
+  return CF_OK;
+}
+
+int cf_part_wait_send(cf_ctx* c) {
+  int rc = part_ok(c);
+  if (rc) return rc;
+  CF_CUDA(c, cudaEventSynchronize(c->ev_pack));
+  return CF_OK;
+}
+
+int cf_part_step_end(cf_ctx* c, const double* recv_buf, cf_step_info* info) {
+  int rc = part_ok(c);
+  if (rc) return rc;
+  CF_CUDA(c, cudaSetDevice(c->device));
+  const double* v = static_cast<const double*>(device_view(c, recv_buf));
+  if (c->nxrecv && !v) return fail(c, CF_EINVAL, "the receive buffer must be device memory or pinned host memory");
+  if ((rc = launch_unpack(c->U[c->launched & 1], c->xrecv, c->nxrecv, v, reinterpret_cast<stream_t>(c->stream))))
+    return fail(c, rc, "unpack launch failed");
+  return finish_steps(c, info);
+}
+
+int cf_part_inlet_terms(cf_ctx* c, double* out) {
+  int rc = part_ok(c);
+  if (rc) return rc;
+  if (!out) return fail(c, CF_EINVAL, "out is NULL");
+  CF_CUDA(c, cudaSetDevice(c->device));
+  const MemberDev& D = c->mem[0].dev;
+  if (!c->any_phys_inflow) return CF_OK;
+  if ((rc = launch_inlet_terms(step_args(c, 0), c->U[c->launched & 1], D.inl_count, c->terms,
+                               reinterpret_cast<stream_t>(c->stream))))
+    return fail(c, rc, "terms launch failed");
+  return part_terms_out(c, out, (size_t)D.inl_count * D.nin);
+}
+
+int cf_part_set_inlet_sums(cf_ctx* c, const double* surf) {
+  int rc = part_ok(c);
+  if (rc) return rc;
+  if (!surf) return fail(c, CF_EINVAL, "surf is NULL");
+  CF_CUDA(c, cudaSetDevice(c->device));
+  const int32_t nin = c->mem[0].dev.nin;
+  CF_CUDA(c, cudaStreamSynchronize(c->stream));
+  char* dst = reinterpret_cast<char*>(c->mst) + offsetof(MemberState, surf);
+  if (nin > 0) CF_CUDA(c, cudaMemcpy(dst, surf, (size_t)nin * sizeof(double), cudaMemcpyDefault));
+  c->external_sums = true;
+  return CF_OK;
+}
+
+int cf_part_discharge_terms(cf_ctx* c, double* out) {
+  int rc = part_ok(c);
+  if (rc) return rc;
+  if (!out) return fail(c, CF_EINVAL, "out is NULL");
+  CF_CUDA(c, cudaSetDevice(c->device));
+  const MemberDev& D = c->mem[0].dev;
+  if ((rc = launch_bq_terms(c->slots, c->bq, c->mdev, D.bq_count, c->terms, reinterpret_cast<stream_t>(c->stream))))
+    return fail(c, rc, "terms launch failed");
+  return part_terms_out(c, out, (size_t)D.bq_count);
+}
+
+int cf_part_apply_discharges(cf_ctx* c, double q_in, double q_out) {
+  int rc = part_ok(c);
+  if (rc) return rc;
+  CF_CUDA(c, cudaSetDevice(c->device));
+  if ((rc = launch_steady_apply(c->mdev, c->mst, q_in, q_out, reinterpret_cast<stream_t>(c->stream))))
+    return fail(c, rc, "steady launch failed");
+  return finish_steps(c, nullptr);
+}
 
 int cf_set_direct_io(cf_ctx* c, int32_t enable) {
   if (!c) return CF_EINVAL;

@@ -70,6 +70,19 @@ struct cf_ctx {
   int32_t cblock = 256;                /* threads per block of the element kernel */
   cf::MemberState* host_state = nullptr;   /* pinned, one record per member */
   bool direct_io = true;               /* kernels read / write callers' pinned host states directly */
+  int32_t* bq = nullptr;               /* boundary edges of every member in reference order */
+  /* a part of a decomposed mesh (cf_create_part): elements ordered send, interior, halo */
+  bool is_part = false;
+  int32_t n_send = 0, n_own = 0;
+  int32_t* elist1 = nullptr;           /* edges of the send elements */
+  int32_t* elist2 = nullptr;           /* the other edges of the interior elements */
+  int32_t nel1 = 0, nel2 = 0;
+  int32_t* xsend = nullptr;            /* exchange plan: element ids (device order) packed, unpacked */
+  int32_t* xrecv = nullptr;
+  int32_t nxsend = 0, nxrecv = 0;
+  bool external_sums = false;          /* phys_inflow sums set by the caller (cf_part_set_inlet_sums) */
+  double* terms = nullptr;             /* a part's inlet or discharge terms, for the caller's sums */
+  cudaEvent_t ev_pack = nullptr;       /* the send buffer of the last cf_part_step_begin is complete */
   /* stepping */
   int64_t launched = 0;                /* steps launched since creation (buffer parity) */
   cudaGraphExec_t graph2 = nullptr;    /* two steps: parity 0 then 1 */

@@ -3,4 +3,7 @@
 
 namespace cf {
 int launch_edges_2(const StepArgs& a, stream_t s) { return launch_edges_iflux<2>(a, reinterpret_cast<cudaStream_t>(s)); }
+int launch_edges_list_2(const StepArgs& a, const int32_t* list, int32_t n, stream_t s) {
+  return launch_edges_list_iflux<2>(a, list, n, reinterpret_cast<cudaStream_t>(s));
+}
 }  // namespace cf

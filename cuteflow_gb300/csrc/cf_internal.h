@@ -70,6 +70,8 @@ struct MemberDev {
   int32_t inl_len_off;            /* first entry length: inl_len[inl_len_off + entry * nin + id - 1] */
   int32_t nin;                    /* inlets (nombre_entrees) of the entry table */
   int32_t steady_count;           /* steady-state stop after more than this many qualifying steps */
+  int32_t bq_begin;               /* boundary edges in reference order: bq[bq_begin, + bq_count) */
+  int32_t bq_count;
   int32_t pad2_;
   double tol_reg_perm;            /* steady-state tolerance; 0: no test */
 };
@@ -127,6 +129,8 @@ struct StepArgs {
   int32_t eblock, ept;       /* launch shape of the edge kernel: threads per block (64, 128, 256) and
                                 edges per thread (1, 2) */
   int32_t cblock;            /* threads per block of the element kernel (128, 256) */
+  int32_t c_lo, c_hi;        /* elements the element kernel updates: [c_lo, c_hi) of the flat space */
+  const int32_t* bq;         /* boundary edges of every member in reference order (MemberDev.bq_*) */
 };
 
 /* ---- host preprocessing (cf_mesh.cpp) ---------------------------------------------- */
@@ -168,11 +172,21 @@ struct Prep {
   std::vector<int32_t> inl_cell;
   std::vector<double> inl_len;    /* [entries * nin] */
   int32_t nin = 0;
+  /* boundary edges (device edge index) in reference order: element, then local edge; the
+   * discharge sums run over this list (so that a decomposed mesh can reproduce them) */
+  std::vector<int32_t> bq_ref;
+  /* a part of a decomposed mesh (element classes given): the elements are ordered send, interior,
+   * halo; elist1 holds the edges of the send elements, elist2 those of the interior ones that
+   * are not in elist1 (the halo's other edges are not evaluated) */
+  int32_t n_send = 0, n_own = 0;
+  std::vector<int32_t> elist1, elist2;
 };
 
-/* Build every host table from the reference mesh inputs.  Returns CF_OK or CF_EINVAL with a
- * message in err. */
-int prepare_mesh(const cf_mesh* m, const cf_params* p, Prep& out, std::string& err);
+/* Build every host table from the reference mesh inputs.  elem_class (NULL: a whole mesh) gives,
+ * for a part of a decomposed mesh, each element's class: 0 owned interior, 1 owned and read by
+ * another part (send), 2 halo.  Returns CF_OK or CF_EINVAL with a message in err. */
+int prepare_mesh(const cf_mesh* m, const cf_params* p, Prep& out, std::string& err,
+                 const int32_t* elem_class = nullptr);
 
 /* ---- kernel launchers (cf_kernels.cu) ---------------------------------------------- */
 
@@ -188,8 +202,24 @@ int launch_probe_fp64(double* out, int32_t nblocks, int64_t iters, stream_t s); 
 int launch_selftest_xd(int64_t n, uint64_t seed, unsigned long long* bad, int32_t nblocks, stream_t s);
 int launch_cfl(const double4* U, const double4* cstat, const int32_t* ctile_mem, int32_t tile_begin,
                int32_t n_tiles, const MemberDev* mdev, MemberState* mst, int32_t slot, stream_t s);
-int launch_discharge(const Slot* slots, const int2* ecell, const MemberDev* mdev, MemberState* mst,
+int launch_discharge(const Slot* slots, const int2* ecell, const int32_t* bq, const MemberDev* mdev, MemberState* mst,
                      int32_t nmembers, stream_t s);
+/* A part of a decomposed mesh.  One phase of its step: phase 1 first makes every member's step
+ * start (k_begin_step); then the edges of elist and the element update of [c_lo, c_hi). */
+int launch_part_phase(const StepArgs& a, int phase, const int32_t* elist, int32_t nel, int32_t c_lo, int32_t c_hi,
+                      stream_t s);
+int launch_edges_list_1(const StepArgs& a, const int32_t* list, int32_t n, stream_t s);
+int launch_edges_list_2(const StepArgs& a, const int32_t* list, int32_t n, stream_t s);
+int launch_edges_list_3(const StepArgs& a, const int32_t* list, int32_t n, stream_t s);
+int launch_edges_list_4(const StepArgs& a, const int32_t* list, int32_t n, stream_t s);
+/* (h, hu, hv) of the listed elements (device order) into / out of buf (device or pinned host) */
+int launch_pack(const double4* U, const int32_t* ids, int32_t n, double* buf, stream_t s);
+int launch_unpack(double4* U, const int32_t* ids, int32_t n, const double* buf, stream_t s);
+/* member 0's phys_inflow terms of U (entries x inlets) and boundary discharges (reference order) */
+int launch_inlet_terms(const StepArgs& a, const double4* U, int32_t count, double* out, stream_t s);
+int launch_bq_terms(const Slot* slots, const int32_t* bq, const MemberDev* mdev, int32_t count, double* out, stream_t s);
+/* member 0's discharges and steady-state test with given (whole-mesh) discharges */
+int launch_steady_apply(const MemberDev* mdev, MemberState* mst, double qi, double qo, stream_t s);
 /* phys_inflow inlet sums of the state U into mst[m].surf (every member with inlet 3) */
 int launch_surf(const StepArgs& a, const double4* U, stream_t s);
 /* hu3 (reference order, one member) <-> U (new order); perm/iperm/zcell/U point at the member's

@@ -28,6 +28,7 @@
 
 #include <cstdio>
 
+#include "cf_edge_kernel.cuh"
 #include "cf_flux.h"
 #include "cf_xd.h"
 
@@ -173,7 +174,8 @@ __device__ __forceinline__ void block_cfl_min(const MemberDev& M, bool active, d
  * folds its dt minimum into the member's with one atomic. */
 template <int BC>
 __global__ void __launch_bounds__(BC, 768 / BC) k_cells(StepArgs a) {
-  const int tile = (int)(((long long)blockIdx.x * BC) / TILE_C);
+  const int c0 = a.c_lo + blockIdx.x * BC;   /* the block's first element (c_lo: a part's phase) */
+  const int tile = c0 / TILE_C;
   const int m = __ldg(a.ctile_mem + tile);
   const MemberDev& M = a.mdev[m];
   MemberState* S = a.mst + m;
@@ -184,10 +186,11 @@ __global__ void __launch_bounds__(BC, 768 / BC) k_cells(StepArgs a) {
   __syncthreads();
   if (s_stop) return;
   const double dt = S->dt[p];
-  const int c = blockIdx.x * BC + threadIdx.x;
+  const int c = c0 + threadIdx.x;
+  const int cend = min(M.cell_end, a.c_hi);
   double4 V = make_double4(0.0, 0.0, 0.0, 0.0);
   double cflL = 0.0;
-  if (c < M.cell_end) {
+  if (c < cend) {
     const double4 U = ld4(a.Uin + c);
     const double4 st = ld4(a.cstat + c);   /* area, manning n, cfl L, - */
     const int4 sl = __ldg(a.cslot + c);
@@ -204,7 +207,7 @@ __global__ void __launch_bounds__(BC, 768 / BC) k_cells(StepArgs a) {
     reinterpret_cast<double2*>(o)[1] = make_double2(V.z, V.w);
     cflL = st.z;
   }
-  block_cfl_min<BC>(M, c < M.cell_end, cflL, V, &S->dt[1 - p]);
+  block_cfl_min<BC>(M, c < cend, cflL, V, &S->dt[1 - p]);
 }
 
 /* CFL of a state into mst[m].dt[slot] (the initial dt, finite_volumes_method.cuf:113-116). */
@@ -225,18 +228,21 @@ __global__ void __launch_bounds__(TILE_C) k_cfl(const double4* U, const double4*
 
 /* Discharge diagnostics of the last step (debit_entree_sum, debit_sortie,
  * finite_volumes_method.cuf:197-214): per member, fixed-order sums over its boundary edges
- * (deterministic: each thread sums a fixed stride, then a fixed tree).  With steady set (the
+ * (deterministic: each thread sums a fixed stride of the reference-order list, then a fixed tree).  With steady set (the
  * launch at the end of every step of a context that tests for steady state) it also applies
  * check_steady_state (finite_volumes_method.cuf:370-393) to the members that stepped:
  * Q_in > 1e-8 (single precision) and |Q_in - Q_out| / Q_in < tol_reg_perm counts a step, any
  * other step resets the count, and more than steady_count stops the member. */
-__global__ void __launch_bounds__(256) k_discharge(const Slot* slots, const int2* ecell, const MemberDev* mdev,
-                                                    MemberState* mst, int steady) {
+__global__ void __launch_bounds__(256) k_discharge(const Slot* slots, const int2* ecell, const int32_t* bq,
+                                                    const MemberDev* mdev, MemberState* mst, int steady) {
   __shared__ double si[256], so[256];
   const int m = blockIdx.x;
   const MemberDev& M = mdev[m];
   double qi = 0.0, qo = 0.0;
-  for (int e = M.bedge_begin + threadIdx.x; e < M.bedge_end; e += 256) {
+  /* the boundary edges in reference order (element, local edge): thread t sums entries t, t + 256,
+   * ..., then a fixed tree, an order a decomposed mesh reproduces from its parts' entries */
+  for (int j = threadIdx.x; j < M.bq_count; j += 256) {
+    const int e = bq[M.bq_begin + j];
     const int kind = ecell[e].y;
     const double q = slots[2 * (size_t)e].q;
     if (kind == -1) qi += q;
@@ -391,6 +397,73 @@ __global__ void __launch_bounds__(256) k_probe_fp64(double* out, long long iters
   out[blockIdx.x * (size_t)blockDim.x + threadIdx.x] = sum;
 }
 
+/* ---- a part of a decomposed mesh ------------------------------------------------------- */
+
+/* The start of every member's step (step_start), made once before a part's phased step. */
+__global__ void k_begin_step(StepArgs a) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= a.nmembers) return;
+  MemberState* S = a.mst + m;
+  if (S->status) return;
+  step_start(a.mdev[m], S, a.parity);
+}
+
+/* (h, hu, hv) of the listed elements (device order) into buf[3 i ..], and back (with RN(1/h));
+ * buf may be pinned host memory (read and written over the CPU link). */
+__global__ void k_pack(const double4* U, const int32_t* ids, int n, double* buf) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double4 u = U[ids[i]];
+  buf[3 * (size_t)i] = u.x;
+  buf[3 * (size_t)i + 1] = u.y;
+  buf[3 * (size_t)i + 2] = u.z;
+}
+
+__global__ void k_unpack(double4* U, const int32_t* ids, int n, const double* buf) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double h = buf[3 * (size_t)i];
+  double4* u = U + ids[i];
+  reinterpret_cast<double2*>(u)[0] = make_double2(h, buf[3 * (size_t)i + 1]);
+  reinterpret_cast<double2*>(u)[1] = make_double2(buf[3 * (size_t)i + 2], h > 0.0 ? 1.0 / h : 0.0);
+}
+
+/* Member 0's phys_inflow terms of the state U: for every entry j of its inlet list (reference
+ * order) and inlet id, the length * depth that calcul_surf_entree sums, out[j * nin + id]. */
+__global__ void k_inlet_terms(StepArgs a, const double4* U, double* out) {
+  const MemberDev& M = a.mdev[0];
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= M.inl_count) return;
+  const double h = U[a.inl_cell[M.inl_begin + j]].x;
+  for (int id = 0; id < M.nin; ++id)
+    out[(size_t)j * M.nin + id] = a.inl_len[M.inl_len_off + (size_t)j * M.nin + id] * h;
+}
+
+/* Member 0's boundary discharges of the last step, in the reference order of its boundary edges. */
+__global__ void k_bq_terms(const Slot* slots, const int32_t* bq, const MemberDev* mdev, double* out) {
+  const MemberDev& M = mdev[0];
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= M.bq_count) return;
+  out[j] = slots[2 * (size_t)bq[M.bq_begin + j]].q;
+}
+
+/* The discharge diagnostics and the steady-state test (check_steady_state,
+ * finite_volumes_method.cuf:370-393) of member 0 with the whole mesh's discharges. */
+__global__ void k_steady_apply(const MemberDev* mdev, MemberState* mst, double qi, double qo) {
+  const MemberDev& M = mdev[0];
+  MemberState* S = mst;
+  S->q_in = qi;
+  S->q_out = qo;
+  if (M.tol_reg_perm > 0.0 && S->status == 0) {
+    if (qi > (double)1e-8f && fabs(qi - qo) / qi < M.tol_reg_perm) {
+      S->steady_iter += 1;
+      if (S->steady_iter > M.steady_count) S->status |= CF_STATUS_STEADY;
+    } else {
+      S->steady_iter = 0;
+    }
+  }
+}
+
 /* Self-test of the integer-pipe arithmetic of cf_xd.h against the FP64 unit.  Pair i comes from
  * a splitmix64 sequence: exponents over the whole range or near the step's values, all-ones and
  * near-all-ones significands, signed zeros, subnormals, infinities, NaN, and quotients and roots
@@ -506,7 +579,7 @@ int launch_step(const StepArgs& a, stream_t s, void* ev_mid, void* ev_end) {
   if (ev_mid) cudaEventRecord(reinterpret_cast<cudaEvent_t>(ev_mid), st);
   if (a.cblock == 128) k_cells<128><<<a.n_ctiles * (TILE_C / 128), 128, 0, st>>>(a);
   else k_cells<TILE_C><<<a.n_ctiles, TILE_C, 0, st>>>(a);
-  if (a.steady) k_discharge<<<a.nmembers, 256, 0, st>>>(a.slots, a.ecell, a.mdev, a.mst, 1);
+  if (a.steady) k_discharge<<<a.nmembers, 256, 0, st>>>(a.slots, a.ecell, a.bq, a.mdev, a.mst, 1);
   if (ev_end) cudaEventRecord(reinterpret_cast<cudaEvent_t>(ev_end), st);
   return check(cudaGetLastError());
 }
@@ -518,9 +591,9 @@ int launch_cfl(const double4* U, const double4* cstat, const int32_t* ctile_mem,
   return check(cudaGetLastError());
 }
 
-int launch_discharge(const Slot* slots, const int2* ecell, const MemberDev* mdev, MemberState* mst, int32_t nmembers,
-                     stream_t s) {
-  k_discharge<<<nmembers, 256, 0, reinterpret_cast<cudaStream_t>(s)>>>(slots, ecell, mdev, mst, 0);
+int launch_discharge(const Slot* slots, const int2* ecell, const int32_t* bq, const MemberDev* mdev, MemberState* mst,
+                     int32_t nmembers, stream_t s) {
+  k_discharge<<<nmembers, 256, 0, reinterpret_cast<cudaStream_t>(s)>>>(slots, ecell, bq, mdev, mst, 0);
   return check(cudaGetLastError());
 }
 
@@ -544,6 +617,57 @@ int launch_scatter_ids(double4* U, const int32_t* iperm, const int32_t* ids, con
 int launch_gather_current(const double4* U0, const double4* U1, const MemberState* mst, int32_t m,
                           const int32_t* iperm, double* hu3, int32_t n, stream_t s) {
   k_gather_current<<<(n + 255) / 256, 256, 0, reinterpret_cast<cudaStream_t>(s)>>>(U0, U1, mst, m, iperm, hu3, n);
+  return check(cudaGetLastError());
+}
+
+int launch_part_phase(const StepArgs& a, int phase, const int32_t* elist, int32_t nel, int32_t c_lo, int32_t c_hi,
+                      stream_t s) {
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(s);
+  if (phase == 1) k_begin_step<<<(a.nmembers + 31) / 32, 32, 0, st>>>(a);
+  int rc = CF_OK;
+  switch (a.iflux) {
+    case 1: rc = launch_edges_list_1(a, elist, nel, s); break;
+    case 2: rc = launch_edges_list_2(a, elist, nel, s); break;
+    case 3: rc = launch_edges_list_3(a, elist, nel, s); break;
+    case 4: rc = launch_edges_list_4(a, elist, nel, s); break;
+    default: return CF_ENOTSUP;
+  }
+  if (rc != CF_OK) return rc;
+  if (c_hi > c_lo) {
+    StepArgs b = a;
+    b.c_lo = c_lo;
+    b.c_hi = c_hi;
+    k_cells<TILE_C><<<(c_hi - c_lo + TILE_C - 1) / TILE_C, TILE_C, 0, st>>>(b);
+  }
+  return check(cudaGetLastError());
+}
+
+int launch_pack(const double4* U, const int32_t* ids, int32_t n, double* buf, stream_t s) {
+  if (n <= 0) return CF_OK;
+  k_pack<<<(n + 255) / 256, 256, 0, reinterpret_cast<cudaStream_t>(s)>>>(U, ids, n, buf);
+  return check(cudaGetLastError());
+}
+
+int launch_unpack(double4* U, const int32_t* ids, int32_t n, const double* buf, stream_t s) {
+  if (n <= 0) return CF_OK;
+  k_unpack<<<(n + 255) / 256, 256, 0, reinterpret_cast<cudaStream_t>(s)>>>(U, ids, n, buf);
+  return check(cudaGetLastError());
+}
+
+int launch_inlet_terms(const StepArgs& a, const double4* U, int32_t count, double* out, stream_t s) {
+  if (count <= 0) return CF_OK;
+  k_inlet_terms<<<(count + 255) / 256, 256, 0, reinterpret_cast<cudaStream_t>(s)>>>(a, U, out);
+  return check(cudaGetLastError());
+}
+
+int launch_bq_terms(const Slot* slots, const int32_t* bq, const MemberDev* mdev, int32_t count, double* out, stream_t s) {
+  if (count <= 0) return CF_OK;
+  k_bq_terms<<<(count + 255) / 256, 256, 0, reinterpret_cast<cudaStream_t>(s)>>>(slots, bq, mdev, out);
+  return check(cudaGetLastError());
+}
+
+int launch_steady_apply(const MemberDev* mdev, MemberState* mst, double qi, double qo, stream_t s) {
+  k_steady_apply<<<1, 1, 0, reinterpret_cast<cudaStream_t>(s)>>>(mdev, mst, qi, qo);
   return check(cudaGetLastError());
 }
 

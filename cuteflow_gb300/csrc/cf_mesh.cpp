@@ -76,7 +76,7 @@ void edge_normal(const cf_mesh* m, int e, int k, double& n1, double& n2, double&
 
 }  // namespace
 
-int prepare_mesh(const cf_mesh* m, const cf_params* p, Prep& P, std::string& err) {
+int prepare_mesh(const cf_mesh* m, const cf_params* p, Prep& P, std::string& err, const int32_t* elem_class) {
   if (!m || !p) { err = "null mesh or params"; return CF_EINVAL; }
   const int n = m->nelt, nnt = m->nnt;
   if (n <= 0 || nnt <= 0 || !m->x || !m->y || !m->z || !m->tri) { err = "empty mesh"; return CF_EINVAL; }
@@ -204,6 +204,12 @@ int prepare_mesh(const cf_mesh* m, const cf_params* p, Prep& P, std::string& err
   P.perm.resize(n);
   P.iperm.resize(n);
   std::iota(P.perm.begin(), P.perm.end(), 0);
+  if (elem_class)
+    for (int e = 0; e < n; ++e)
+      if (elem_class[e] < 0 || elem_class[e] > 2) {
+        err = "element class outside 0..2";
+        return CF_EINVAL;
+      }
   if (p->reorder == 1 || p->reorder == 2) {
     double xmin = P.xc[0], xmax = P.xc[0], ymin = P.yc[0], ymax = P.yc[0];
     for (int e = 1; e < n; ++e) {
@@ -219,6 +225,17 @@ int prepare_mesh(const cf_mesh* m, const cf_params* p, Prep& P, std::string& err
       h[e] = p->reorder == 1 ? hilbert_index(ix, iy, order_bits) : morton_index(ix, iy);
     }
     std::stable_sort(P.perm.begin(), P.perm.end(), [&](int32_t i, int32_t j) { return h[i] < h[j]; });
+  }
+  P.n_send = P.n_own = 0;
+  if (elem_class) {
+    /* a part: send elements first, then the other owned ones, then the halo (each group in the
+     * curve's order) */
+    auto rank = [&](int32_t e) { return elem_class[e] == 1 ? 0 : (elem_class[e] == 0 ? 1 : 2); };
+    std::stable_sort(P.perm.begin(), P.perm.end(), [&](int32_t i, int32_t j) { return rank(i) < rank(j); });
+    for (int e = 0; e < n; ++e) {
+      P.n_send += elem_class[e] == 1;
+      P.n_own += elem_class[e] != 2;
+    }
   }
   for (int i = 0; i < n; ++i) P.iperm[P.perm[i]] = i;
 
@@ -282,6 +299,27 @@ int prepare_mesh(const cf_mesh* m, const cf_params* p, Prep& P, std::string& err
     }
   }
   const size_t ne = P.edges.size();
+  /* boundary edges in reference order (element, local edge) */
+  {
+    std::vector<int32_t> bslot(3 * (size_t)n, -1);
+    for (size_t e = (size_t)P.n_interior; e < ne; ++e) bslot[3 * (size_t)P.perm[P.edges[e].a] + P.edges[e].ka] = (int32_t)e;
+    P.bq_ref.clear();
+    for (size_t i = 0; i < bslot.size(); ++i)
+      if (bslot[i] >= 0) P.bq_ref.push_back(bslot[i]);
+  }
+  /* a part: the edges of the send elements (first phase of its step), then those of the interior */
+  P.elist1.clear();
+  P.elist2.clear();
+  if (elem_class) {
+    const int32_t ns = P.n_send, no = P.n_own;
+    for (size_t e = 0; e < ne; ++e) {
+      const HostEdge& E = P.edges[e];
+      const bool s1 = E.a < ns || (E.b >= 0 && E.b < ns);
+      const bool s2 = (E.a >= ns && E.a < no) || (E.b >= ns && E.b < no);
+      if (s1) P.elist1.push_back((int32_t)e);
+      else if (s2) P.elist2.push_back((int32_t)e);
+    }
+  }
 
   /* -- per-element tables (new order) --------------------------------------------------- */
   P.cslot.assign(n, make_int4(-1, -1, -1, 0));

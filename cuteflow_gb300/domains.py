@@ -194,3 +194,205 @@ class Decomposed:
         for s, p in zip(self.solvers, self.parts):
             U[p.owned] = s.get_state()[: p.n_owned]
         return U
+
+
+# ---- the decomposed run as a data plane: one process per part ------------------------------------
+
+def inlet_entries(bnd: np.ndarray) -> List[tuple]:
+    """The phys_inflow entry list of a mesh (compute_input_elems, maillage.cuf:1333-1363): one entry
+    per (element, inflow edge) in element then local-edge order."""
+    e, k = np.nonzero(bnd[:, :, 0] == -1)
+    return list(zip(e.tolist(), k.tolist()))
+
+
+def boundary_entries(bnd: np.ndarray) -> List[tuple]:
+    """The boundary edges of a mesh in element then local-edge order, with their kinds."""
+    e, k = np.nonzero(bnd[:, :, 0] < 0)
+    return list(zip(e.tolist(), k.tolist(), bnd[e, k, 0].tolist()))
+
+
+def inlet_sum(values: np.ndarray) -> float:
+    """calcul_surf_entree's sum as the step forms it (k_surf): blocks of 32 entries in list order,
+    each summed by the tree s[l] += s[l + i] (i = 16 .. 1), the block sums added in order."""
+    total = 0.0
+    n = len(values)
+    for b in range(0, n, 32):
+        s = [float(values[b + l]) if b + l < n else 0.0 for l in range(32)]
+        i = 16
+        while i > 0:
+            for l in range(i):
+                s[l] = s[l] + s[l + i]
+            i >>= 1
+        total = total + s[0]
+    return total
+
+
+def discharge_sum(q: np.ndarray, kinds: np.ndarray, kind: int) -> float:
+    """The discharge sums as the step forms them (k_discharge): over the boundary edges in
+    reference order, 256 strided partial sums of the edges of one kind, then a fixed tree."""
+    part = [0.0] * 256
+    for j in range(len(q)):
+        if kinds[j] == kind:
+            t = j % 256
+            part[t] = part[t] + float(q[j])
+    w = 128
+    while w > 0:
+        for t in range(w):
+            part[t] = part[t] + part[t + w]
+        w >>= 1
+    return part[0]
+
+
+class PartRunner:
+    """Part `rank` of a decomposed mesh stepped by this process (one rank per part) on its GPU,
+    the reference's send-cells-first scheme (finite_volumes_method.cuf:141-171,
+    memory_exchange_functions.cuf:129-172) as a data plane:
+
+      - the part's context (cf_create_part) orders its elements send, interior, halo;
+      - each step (cf_part_step_begin) updates the send elements first and packs their states
+        straight into a pinned host buffer (the kernel writes it over the CPU link), then updates
+        the interior elements while this process exchanges the halo with its neighbour ranks over
+        `comm` (torch.distributed point-to-point); cf_part_step_end unpacks the received halo;
+      - the next dt is the MIN over the ranks (MPI_ALLREDUCE MIN, cfl_condition.cuf:117-126);
+      - phys_inflow's inlet sums and the discharges of the steady-state test are the whole
+        mesh's: every rank places its own elements' terms at their positions in the whole mesh's
+        lists, a SUM all-reduce assembles the lists (each position has one contributor, so the
+        sum is exact), and every rank sums them in the undivided step's order.
+    Every element evolves bit for bit as in the undivided mesh."""
+
+    def __init__(self, case, nparts: int, rank: int, comm, params: Optional[dict] = None):
+        import torch
+        self.comm = comm
+        self.rank = rank
+        self.parts = partition(case, nparts, params)
+        p = self.parts[rank]
+        self.part = p
+        # element classes: owned elements another part reads are sent
+        cls = np.zeros(p.n_owned + p.halo.size, dtype=np.int32)
+        cls[p.n_owned:] = 2
+        self.send_to = {}
+        for r, q in enumerate(self.parts):
+            if r != rank and rank in q.recv:
+                ids = q.recv[rank][1]
+                self.send_to[r] = ids
+                cls[ids] = 1
+        self.recv_from = {r: here for r, (here, _) in sorted(p.recv.items())}
+        self.solver = Solver(p.case, p.params, elem_class=cls)
+        L, ctx = self.solver._L, self.solver._ctx
+        send = np.concatenate([self.send_to[r] for r in sorted(self.send_to)]).astype(np.int32) \
+            if self.send_to else np.zeros(0, np.int32)
+        recv = np.concatenate([self.recv_from[r] for r in sorted(self.recv_from)]).astype(np.int32) \
+            if self.recv_from else np.zeros(0, np.int32)
+        ip = __import__("ctypes").POINTER(__import__("ctypes").c_int32)
+        self.solver._check(L.cf_part_set_exchange(ctx, send.ctypes.data_as(ip), int(send.size),
+                                                  recv.ctypes.data_as(ip), int(recv.size)))
+        self.sendbuf = torch.zeros(max(3 * send.size, 1), dtype=torch.float64).pin_memory()
+        self.recvbuf = torch.zeros(max(3 * recv.size, 1), dtype=torch.float64).pin_memory()
+        self._send_slices, off = {}, 0
+        for r in sorted(self.send_to):
+            n = 3 * self.send_to[r].size
+            self._send_slices[r] = (off, off + n)
+            off += n
+        self._recv_slices, off = {}, 0
+        for r in sorted(self.recv_from):
+            n = 3 * self.recv_from[r].size
+            self._recv_slices[r] = (off, off + n)
+            off += n
+        # the whole mesh's inlet and boundary lists, and this part's entries in them
+        prm = {**getattr(case, "params", {}), **(params or {})}
+        gb = mesh_tables(case, params)[0]
+        lb = mesh_tables(p.case, p.params)[0]
+        self.phys_inflow = int(prm.get("inlet", 2)) == 3
+        self.steady = float(prm.get("tol_reg_perm", 0.0)) > 0.0
+        self.nin = int(case.nombre_entrees)
+        gi = {ek: j for j, ek in enumerate(inlet_entries(gb))}
+        self.n_inlet = len(gi)
+        li = inlet_entries(lb)
+        self.inlet_map = [(j, gi[(int(p.owned[e]), k)]) for j, (e, k) in enumerate(li) if e < p.n_owned]
+        gq = boundary_entries(gb)
+        self.q_kinds = np.array([kd for _, _, kd in gq], dtype=np.int64)
+        gpos = {(e, k): j for j, (e, k, _) in enumerate(gq)}
+        lq = boundary_entries(lb)
+        self.n_local_q = len(lq)
+        self.q_map = [(j, gpos[(int(p.owned[e]), k)]) for j, (e, k, _) in enumerate(lq) if e < p.n_owned]
+
+    # -- collectives over the ranks --
+    def _allreduce(self, t, op):
+        self.comm.all_reduce(t, op=op)
+        return t
+
+    def _global_dt(self, dt_part: float) -> float:
+        import torch
+        t = torch.tensor([dt_part], dtype=torch.float64)
+        return float(self._allreduce(t, self.comm.ReduceOp.MIN).item())
+
+    def set_state(self, U: np.ndarray, t0: float = 0.0):
+        p = self.part
+        self.solver.set_state(U[np.concatenate([p.owned, p.halo])], t0)
+        self.solver.set_dt(self._global_dt(self.solver.info().dt_next))
+
+    def _inlet_sums(self):
+        import torch
+        L, ctx = self.solver._L, self.solver._ctx
+        n_local = len(inlet_entries(mesh_tables(self.part.case, self.part.params)[0])) if not hasattr(self, "_n_li") \
+            else self._n_li
+        self._n_li = n_local
+        terms = np.zeros(max(n_local * self.nin, 1))
+        dp = __import__("ctypes").POINTER(__import__("ctypes").c_double)
+        self.solver._check(L.cf_part_inlet_terms(ctx, terms.ctypes.data_as(dp)))
+        G = torch.zeros((max(self.n_inlet, 1), self.nin), dtype=torch.float64)
+        tv = terms[: n_local * self.nin].reshape(n_local, self.nin) if n_local else np.zeros((0, self.nin))
+        for j, g in self.inlet_map:
+            G[g] = torch.from_numpy(tv[j].copy())
+        self._allreduce(G, self.comm.ReduceOp.SUM)
+        Gn = G.numpy()
+        surf = np.array([inlet_sum(Gn[: self.n_inlet, i]) for i in range(self.nin)] + [0.0] * (20 - self.nin))
+        self.solver._check(L.cf_part_set_inlet_sums(ctx, surf.ctypes.data_as(dp)))
+
+    def _discharges(self):
+        import torch
+        L, ctx = self.solver._L, self.solver._ctx
+        dp = __import__("ctypes").POINTER(__import__("ctypes").c_double)
+        terms = np.zeros(max(self.n_local_q, 1))
+        self.solver._check(L.cf_part_discharge_terms(ctx, terms.ctypes.data_as(dp)))
+        G = torch.zeros(max(self.q_kinds.size, 1), dtype=torch.float64)
+        for j, g in self.q_map:
+            G[g] = float(terms[j])
+        self._allreduce(G, self.comm.ReduceOp.SUM)
+        q = G.numpy()[: self.q_kinds.size]
+        qi, qo = discharge_sum(q, self.q_kinds, -1), discharge_sum(q, self.q_kinds, -2)
+        self.solver._check(L.cf_part_apply_discharges(ctx, qi, qo))
+
+    def _exchange(self):
+        reqs = []
+        for r, (a, b) in self._recv_slices.items():
+            reqs.append(self.comm.irecv(self.recvbuf[a:b], src=r))
+        for r, (a, b) in self._send_slices.items():
+            reqs.append(self.comm.isend(self.sendbuf[a:b], dst=r))
+        for q in reqs:
+            q.wait()
+
+    def step(self, nsteps: int = 1):
+        import ctypes
+        from . import _abi
+        L, ctx = self.solver._L, self.solver._ctx
+        info = _abi.CfStepInfo()
+        for _ in range(nsteps):
+            if self.phys_inflow:
+                self._inlet_sums()
+            self.solver._check(L.cf_part_step_begin(ctx, ctypes.c_void_p(self.sendbuf.data_ptr())))
+            self.solver._check(L.cf_part_wait_send(ctx))
+            self._exchange()   # while the GPU updates the interior elements
+            rc = L.cf_part_step_end(ctx, ctypes.c_void_p(self.recvbuf.data_ptr()), ctypes.byref(info))
+            if rc not in (0, -4, -5):
+                self.solver._check(rc)
+            if self.steady:
+                self._discharges()
+            self.solver.set_dt(self._global_dt(self.solver.info().dt_next))
+        return self.solver.info()
+
+    def get_owned_state(self) -> np.ndarray:
+        return self.solver.get_state()[: self.part.n_owned]
+
+    def close(self):
+        self.solver.close()

@@ -77,6 +77,17 @@ def load(build_if_missing: bool = True):
     L.cf_set_timing.argtypes = [vp, C.c_int32]
     L.cf_set_direct_io.argtypes = [vp, C.c_int32]
     L.cf_set_launch_shape.argtypes = [vp, C.c_int32, C.c_int32, C.c_int32]
+    ipp = C.POINTER(C.c_int32)
+    L.cf_create_part.argtypes = [C.POINTER(_abi.CfMesh), C.POINTER(_abi.CfParams), ipp, C.POINTER(vp)]
+    L.cf_part_sizes.argtypes = [vp, ipp, ipp, ipp, ipp]
+    L.cf_part_set_exchange.argtypes = [vp, ipp, C.c_int32, ipp, C.c_int32]
+    L.cf_part_step_begin.argtypes = [vp, vp]
+    L.cf_part_wait_send.argtypes = [vp]
+    L.cf_part_step_end.argtypes = [vp, vp, C.POINTER(_abi.CfStepInfo)]
+    L.cf_part_inlet_terms.argtypes = [vp, dp]
+    L.cf_part_set_inlet_sums.argtypes = [vp, dp]
+    L.cf_part_discharge_terms.argtypes = [vp, dp]
+    L.cf_part_apply_discharges.argtypes = [vp, C.c_double, C.c_double]
     L.cf_get_launch_shape.argtypes = [vp, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
     L.cf_autotune_order.argtypes = [C.POINTER(_abi.CfMesh), C.POINTER(_abi.CfParams), dp, C.c_int32,
                                     C.POINTER(C.c_int32), dp]
@@ -125,6 +136,9 @@ def load(build_if_missing: bool = True):
                  "cf_get_tuning", "cf_autotune", "cf_get_elements", "cf_set_elements", "cf_set_dt", "cf_get_state", "cf_get_state_device",
                  "cf_get_info", "cf_get_mesh_tables", "cf_mesh_tables", "cf_get_sizes", "cf_set_timing", "cf_get_timing",
                  "cf_set_direct_io", "cf_set_launch_shape", "cf_get_launch_shape", "cf_autotune_order",
+                 "cf_create_part", "cf_part_sizes", "cf_part_set_exchange", "cf_part_step_begin", "cf_part_wait_send",
+                 "cf_part_step_end", "cf_part_inlet_terms", "cf_part_set_inlet_sums", "cf_part_discharge_terms",
+                 "cf_part_apply_discharges",
                  "cf_probe_fp64", "cf_selftest_xd", "cf_advance"):
         getattr(L, name).restype = C.c_int
     _lib = L
@@ -163,12 +177,19 @@ def _info(s: _abi.CfStepInfo) -> StepInfo:
 class Solver:
     """One simulation on the current CUDA device."""
 
-    def __init__(self, case, params: Optional[dict] = None):
+    def __init__(self, case, params: Optional[dict] = None, elem_class: Optional[np.ndarray] = None):
+        """elem_class (a part of a decomposed mesh, cf_create_part): per element 0 owned interior,
+        1 owned and read by another part, 2 halo."""
         self._L = load()
         self._ctx = C.c_void_p()
         self._mesh = _abi.MeshArrays(case)
         self.params = _abi.make_params({**getattr(case, "params", {}), **(params or {})})
-        rc = self._L.cf_create(C.byref(self._mesh.mesh), C.byref(self.params), C.byref(self._ctx))
+        if elem_class is not None:
+            self._elem_class = np.ascontiguousarray(elem_class, dtype=np.int32)
+            rc = self._L.cf_create_part(C.byref(self._mesh.mesh), C.byref(self.params),
+                                        self._elem_class.ctypes.data_as(C.POINTER(C.c_int32)), C.byref(self._ctx))
+        else:
+            rc = self._L.cf_create(C.byref(self._mesh.mesh), C.byref(self.params), C.byref(self._ctx))
         if rc != 0:
             raise CFError(rc, self._L.cf_last_error(None).decode())
         self.nelt = int(self._mesh.mesh.nelt)
