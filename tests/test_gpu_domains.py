@@ -75,7 +75,7 @@ def test_decomposed_processes_equal_the_undivided_run(gpu_lib, kind, world, nste
     ctx = mp.get_context("spawn")
     out = ctx.Queue()
     port = _free_port()
-    procs = [ctx.Process(target=_rank, args=(r, world, kind, nsteps, port, out)) for r in range(world)]
+    procs = [ctx.Process(target=_rank, args=(r, world, kind, nsteps, port, out), daemon=True) for r in range(world)]
     for pr in procs:
         pr.start()
     got = [out.get(timeout=300) for _ in range(world)]
