@@ -351,7 +351,7 @@ def adjoint_leg(steps: int, warmup: int, obs_every: float = 10.0, budget_gb: flo
 
 
 def calibration_batch_leg(ninst: int, steps: int, iters: int, obs_every: float = 10.0, full: bool = False,
-                          budget_gb: float = 120.0):
+                          budget_gb: float = 120.0, seq_iters: int = 1, fd_zones: int = 0):
     """Batched adjoint calibration (a sample of the 64-instance workload): ninst instances of the
     calibration case with seeded sizes, zone fields and gauges, in one batch context; every
     gradient-descent iteration runs one recording forward and one backward for all instances in
@@ -362,7 +362,8 @@ def calibration_batch_leg(ninst: int, steps: int, iters: int, obs_every: float =
     observations every 10 s with full, every 1 s for the sample (its 400 steps cover a few seconds).
     The batch's adjoint keeps to budget_gb of device memory (its schedule stores the step records
     of as many of the last steps as fit and replays the rest); each instance run alone gets the
-    same cap."""
+    same cap.  The one-after-another form runs seq_iters iterations per instance (its time per
+    iteration does not depend on the iteration)."""
     import torch
     from cuteflow_gb300 import Batch, Solver, cases
     from cuteflow_gb300.adjoint import Adjoint, Zones
@@ -423,6 +424,27 @@ def calibration_batch_leg(ninst: int, steps: int, iters: int, obs_every: float =
     r = (eta - eta_obs) * mask
     misfits.append(float(np.sum(r * r)))
     vals, _ = zs.get()
+    # central differences (step 1e-6 relative, the recorded dt sequence replayed) of the zones with
+    # the largest gradients at the final values, against the batch's zone gradient
+    fd = []
+    if fd_zones > 0:
+        adj.backward(2.0 * r)
+        g = zs.gradient(adj)
+        for z in np.argsort(-np.abs(g))[:fd_zones]:
+            d = 1e-6 * vals[z]
+            Jz = []
+            for sign in (1.0, -1.0):
+                v = vals.copy()
+                v[z] += sign * d
+                zs.set(v)
+                start()
+                e_, _ = adj.forward(replay=True)
+                Jz.append(((e_ - eta_obs) * mask))
+            zs.set(vals)
+            dJ = float(np.sum((Jz[0] - Jz[1]) * (Jz[0] + Jz[1])))
+            fdz = dJ / (2.0 * d)
+            fd.append({"zone": int(z), "adjoint": float(g[z]), "central_difference": fdz,
+                       "relative_difference": abs(fdz - g[z]) / abs(g[z])})
     zs.close(); adj.close(); b.close()
     # the same iteration, instance by instance
     t_seq = 0.0
@@ -434,22 +456,23 @@ def calibration_batch_leg(ninst: int, steps: int, iters: int, obs_every: float =
         obs_i, mask_i = eta_obs[:, col[i]:col[i + 1]], mask[:, col[i]:col[i + 1]]
         torch.cuda.synchronize()
         t1 = time.perf_counter()
-        for it in range(iters):
+        for it in range(seq_iters):
             s.set_state(c.U0)
             eta_i, _ = a1.forward()
             a1.backward(2.0 * (eta_i - obs_i) * mask_i)
             z1.gradient(a1)
             z1.descend(lr, 0.01, 0.1)
         torch.cuda.synchronize()
-        t_seq += (time.perf_counter() - t1) / iters
+        t_seq += (time.perf_counter() - t1) / seq_iters
         z1.close(); a1.close(); s.close()
     return {"instances": ninst, "triangles_total": tri, "steps": steps, "iterations": iters,
             "budget_gb": budget_gb, "schedule": sched, "observation_every_s": obs_every,
             "zones_total": int(zoff[-1]), "gauges_total": int(gg.size),
             "batched_s_per_iteration": t_batch, "sequential_s_per_iteration": t_seq,
+            "sequential_iterations_timed": seq_iters,
             "speedup_vs_sequential": t_seq / t_batch, "misfit_per_iteration": misfits,
             "zone_error_start": float(np.abs(vals0 - true_vals).mean()),
-            "zone_error_end": float(np.abs(vals - true_vals).mean())}
+            "zone_error_end": float(np.abs(vals - true_vals).mean()), "fd_check": fd}
 
 
 def run_ours(args):
@@ -482,6 +505,25 @@ def run_ours(args):
         tune = (cmp_, mask, None)
     else:
         tune = s.autotune(30) if not args.no_tune else (0, 0, None)
+
+    # the launch shapes the autotuner chose among, each timed on the same state (20 steps), then the
+    # chosen one restored
+    shape = s.launch_shape()
+    shape_ms = {}
+    for eb in (64, 128, 256):
+        for ept in (1, 2):
+            for cb in (256, 128):
+                s.set_launch_shape(eb, ept, cb)
+                s.set_state(case.U0)
+                s.step(3)
+                torch.cuda.synchronize()
+                a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a0.record(stream)
+                s.step(20)
+                a1.record(stream)
+                torch.cuda.synchronize()
+                shape_ms[f"{eb}x{ept}/{cb}"] = a0.elapsed_time(a1) / 20
+    s.set_launch_shape(*shape)
 
     # ---- device-resident throughput (value) ----
     s.set_state(case.U0)
@@ -604,7 +646,10 @@ def run_ours(args):
                    "l2": "working set > L2 (no flush needed)", "parallelism": f"replicas x{world}",
                    "time_steps_ran": info.steps,
                    "wet_fraction": {"start": wet_start, "end_of_timed_steps": wet_end},
-                   "tuning": {"int_compare": tune[0], "int_mul_warps": tune[1], "trial_ms_per_step": tune[2]}},
+                   "tuning": {"int_compare": tune[0], "int_mul_warps": tune[1], "trial_ms_per_step": tune[2],
+                              "launch_shape": {"edge_block": shape[0], "edges_per_thread": shape[1],
+                                               "cell_block": shape[2]},
+                              "ms_per_step_by_shape": shape_ms}},
         "roofline": {"bound": "hbm", "kernel": "one time step (k_edges + k_cells)",
                      "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "peak_source": f"MEASURED_PEAKS.json hbm_gbs ({hbm_src})",
@@ -646,7 +691,8 @@ def run_ours(args):
         line["adjoint"] = adjoint_leg(args.adjoint_steps, 10, budget_gb=args.adjoint_budget_gb)
     if rank == 0 and args.calib_instances > 0:
         line["batched_adjoint"] = calibration_batch_leg(args.calib_instances, args.calib_steps, args.calib_iters,
-                                                        full=args.calib_full, budget_gb=args.calib_budget_gb)
+                                                        full=args.calib_full, budget_gb=args.calib_budget_gb,
+                                                        seq_iters=args.calib_seq_iters, fd_zones=args.calib_fd_zones)
         line["batched_adjoint"]["note"] = (
             "the 64-instance calibration workload's instance sizes (50k-273k triangles)" if args.calib_full else
             "sample of the 64-instance calibration workload (50k-300k triangles, 3000 steps, 10 iterations); "
@@ -678,6 +724,10 @@ def main():
     ap.add_argument("--calib-iters", type=int, default=3)
     ap.add_argument("--calib-full", action="store_true", help="calibration instances at the workload's sizes")
     ap.add_argument("--calib-budget-gb", type=float, default=120.0, help="device memory cap of the batch's adjoint")
+    ap.add_argument("--calib-fd-zones", type=int, default=2,
+                    help="central-difference check of the batch's zone gradient on this many zones")
+    ap.add_argument("--calib-seq-iters", type=int, default=1,
+                    help="iterations of the one-after-another comparison per instance")
     ap.add_argument("--adjoint-budget-gb", type=float, default=64.0, help="device memory cap of the adjoint leg")
     ap.add_argument("--adjoint-steps", type=int, default=3000,
                     help="adjoint calibration leg beside the plain line (0: skip)")
