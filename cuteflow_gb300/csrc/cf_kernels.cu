@@ -205,6 +205,12 @@ __global__ void __launch_bounds__(BC, 768 / BC) k_cells(StepArgs a) {
     double4* o = a.Uout + c;
     reinterpret_cast<double2*>(o)[0] = make_double2(V.x, V.y);
     reinterpret_cast<double2*>(o)[1] = make_double2(V.z, V.w);
+    if (a.host_out) {
+      double* h = a.host_out + 3 * (size_t)__ldg(a.perm + c);
+      h[0] = V.x;
+      h[1] = V.y;
+      h[2] = V.z;
+    }
     cflL = st.z;
   }
   block_cfl_min<BC>(M, c < cend, cflL, V, &S->dt[1 - p]);
@@ -335,11 +341,14 @@ __global__ void __launch_bounds__(REF_BLOCK) k_load_ref(const double* __restrict
 }
 
 __global__ void __launch_bounds__(REF_BLOCK) k_store_ref(const double4* U0, const double4* U1, const MemberState* mst,
-                                                         int m, const int32_t* iperm, double* __restrict__ hu3, int n) {
+                                                         int m, const int32_t* iperm, double* __restrict__ hu3, int n,
+                                                         int only_if_stopped) {
   __shared__ double s[3 * REF_BLOCK];
   const double4* U = U0;
   if (mst) {
     const MemberState& st = mst[m];
+    /* the last step's element kernel has written hu3 already unless the member stopped */
+    if (only_if_stopped && st.status == 0) return;
     U = ((st.base + st.nstep) & 1) ? U1 : U0;
   }
   const long long base = (long long)blockIdx.x * REF_BLOCK;
@@ -678,10 +687,10 @@ int launch_load_ref(const double* hu3, const int32_t* iperm, double4* U, int32_t
 }
 
 int launch_store_ref(const double4* U0, const double4* U1, const MemberState* mst, int32_t m, const int32_t* iperm,
-                     double* hu3, int32_t n, stream_t s) {
+                     double* hu3, int32_t n, stream_t s, bool only_if_stopped) {
   if (n <= 0) return CF_OK;
-  k_store_ref<<<(n + REF_BLOCK - 1) / REF_BLOCK, REF_BLOCK, 0, reinterpret_cast<cudaStream_t>(s)>>>(U0, U1, mst, m,
-                                                                                                   iperm, hu3, n);
+  k_store_ref<<<(n + REF_BLOCK - 1) / REF_BLOCK, REF_BLOCK, 0, reinterpret_cast<cudaStream_t>(s)>>>(
+      U0, U1, mst, m, iperm, hu3, n, only_if_stopped ? 1 : 0);
   return check(cudaGetLastError());
 }
 

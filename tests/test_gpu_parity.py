@@ -127,6 +127,28 @@ def test_advance_returns_a_stopped_state_like_the_three_calls(gpu_lib, oracle):
     assert np.array_equal(U, ref["U"]) and info.t == ref["t"]
 
 
+def test_advance_with_pinned_buffers_writes_the_last_step_or_the_stopped_state(gpu_lib, oracle):
+    """cf_advance into pinned host memory: the last step's element kernel writes the caller's buffer
+    itself; a member that stopped before it (the dt-range test) gets its stopped state from the
+    store kernel instead; a call of zero steps returns the state it was given.  Each is the
+    oracle's state bit for bit."""
+    import ctypes
+    torch = pytest.importorskip("torch")
+    from cuteflow_gb300 import Solver
+    dp = ctypes.POINTER(ctypes.c_double)
+    c = cases.flooding(40, 20, seed=8, iflux=1)
+    for prm, n in ((dict(fricimplic=0), 120), ({}, 35), ({}, 0)):
+        ref = oracle.run(c, n, params=prm, check=False)
+        with Solver(c, prm) as s:
+            src = torch.from_numpy(np.ascontiguousarray(c.U0, dtype=np.float64)).pin_memory()
+            dst = torch.full_like(src, float("nan")).pin_memory()
+            info = _abi.CfStepInfo()
+            rc = s._L.cf_advance(s._ctx, ctypes.cast(src.data_ptr(), dp), 0.0, n, ctypes.cast(dst.data_ptr(), dp),
+                                 ctypes.byref(info))
+            assert rc == (_abi.CF_EDT if prm else 0)
+            assert np.array_equal(dst.numpy(), ref["U"]) and info.t == ref["t"], (prm, n)
+
+
 @pytest.mark.parametrize("iflux", [3, 4])
 def test_lake_at_rest(gpu_lib, oracle, iflux):
     c = cases.lake_at_rest(40, 20, iflux=iflux)
