@@ -243,6 +243,24 @@ def discharge_sum(q: np.ndarray, kinds: np.ndarray, kind: int) -> float:
     return part[0]
 
 
+def part_plan(parts: List[Part], rank: int):
+    """The exchange plan of part `rank`: its element classes for cf_create_part (0 owned interior,
+    1 owned and held in another part's halo, 2 halo), the own elements it sends to each other part
+    (local ids, in that part's receive order) and the halo elements it receives from each (local
+    ids)."""
+    p = parts[rank]
+    cls = np.zeros(p.n_owned + p.halo.size, dtype=np.int32)
+    cls[p.n_owned:] = 2
+    send_to = {}
+    for r, q in enumerate(parts):
+        if r != rank and rank in q.recv:
+            ids = q.recv[rank][1]
+            send_to[r] = ids
+            cls[ids] = 1
+    recv_from = {r: here for r, (here, _) in sorted(p.recv.items())}
+    return cls, send_to, recv_from
+
+
 class PartRunner:
     """Part `rank` of a decomposed mesh stepped by this process (one rank per part) on its GPU,
     the reference's send-cells-first scheme (finite_volumes_method.cuf:141-171,
@@ -267,16 +285,7 @@ class PartRunner:
         self.parts = partition(case, nparts, params)
         p = self.parts[rank]
         self.part = p
-        # element classes: owned elements another part reads are sent
-        cls = np.zeros(p.n_owned + p.halo.size, dtype=np.int32)
-        cls[p.n_owned:] = 2
-        self.send_to = {}
-        for r, q in enumerate(self.parts):
-            if r != rank and rank in q.recv:
-                ids = q.recv[rank][1]
-                self.send_to[r] = ids
-                cls[ids] = 1
-        self.recv_from = {r: here for r, (here, _) in sorted(p.recv.items())}
+        cls, self.send_to, self.recv_from = part_plan(self.parts, rank)
         self.solver = Solver(p.case, p.params, elem_class=cls)
         L, ctx = self.solver._L, self.solver._ctx
         send = np.concatenate([self.send_to[r] for r in sorted(self.send_to)]).astype(np.int32) \

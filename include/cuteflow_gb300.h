@@ -268,6 +268,40 @@ int cf_get_elements(cf_ctx* ctx, int32_t member, const int32_t* ids, int32_t n, 
 int cf_set_elements(cf_ctx* ctx, int32_t member, const int32_t* ids, int32_t n, const double* hu3);
 int cf_set_dt(cf_ctx* ctx, int32_t member, double dt);
 
+/* A part as its own rank, with the reference's send-cells-first step (finite_volumes_method.cuf:141-171;
+ * update_send_cells and gpu_echange_cgns, memory_exchange_functions.cuf:129-172).
+ * cf_create_part: as cf_create for one mesh (a part: own elements and halo), with elem_class[k] the
+ *   class of element k: 0 owned interior, 1 owned and held in another part's halo (send), 2 halo.
+ * cf_part_set_exchange: the send elements (class 1) whose states go out, and the halo elements
+ *   (class 2) whose states come in, each in the order of the caller's buffers (0-based ids).
+ * cf_part_step_begin: enqueues one step: its start (dt test, next time), the send elements' edges
+ *   and update, their new states packed into send_buf (3 per element, in the exchange order; device
+ *   memory or pinned host memory, written by the kernel over the CPU link), then the interior
+ *   elements' edges and update; returns without waiting.
+ * cf_part_wait_send: waits until send_buf is complete (the interior may still be running).
+ * cf_part_step_end: unpacks recv_buf (the halo states, exchange order) into the new state, waits,
+ *   and reports the step (info.dt_next: the part's own elements' minimum; the caller applies the
+ *   minimum over the parts with cf_set_dt, the reference's MPI_ALLREDUCE MIN).
+ * The whole mesh's sums (MPI_ALLREDUCE SUM, finite_volumes_method.cuf:133-138, :218-219):
+ * cf_part_inlet_terms: before a phys_inflow step, the part's inlet terms (length * depth, entries x
+ *   inlets, its inlet entries in element then local-edge order); the caller sums the whole mesh's
+ *   entries in the step's order and passes the sums per inlet to cf_part_set_inlet_sums (required
+ *   before every step of a phys_inflow part).
+ * cf_part_discharge_terms: after a step, the part's boundary discharges (its boundary edges in element
+ *   then local-edge order); the caller sums the whole mesh's and passes them to
+ *   cf_part_apply_discharges, which sets info.q_in / q_out and applies the steady-state test.
+ * cf_part_sizes: send and own element counts, inlet entries and boundary edges of the part. */
+int cf_create_part(const cf_mesh* mesh, const cf_params* params, const int32_t* elem_class, cf_ctx** out);
+int cf_part_sizes(cf_ctx* ctx, int32_t* n_send, int32_t* n_own, int32_t* inlet_entries, int32_t* boundary_edges);
+int cf_part_set_exchange(cf_ctx* ctx, const int32_t* send_ids, int32_t nsend, const int32_t* recv_ids, int32_t nrecv);
+int cf_part_step_begin(cf_ctx* ctx, double* send_buf);
+int cf_part_wait_send(cf_ctx* ctx);
+int cf_part_step_end(cf_ctx* ctx, const double* recv_buf, cf_step_info* info);
+int cf_part_inlet_terms(cf_ctx* ctx, double* out);
+int cf_part_set_inlet_sums(cf_ctx* ctx, const double* surf);
+int cf_part_discharge_terms(cf_ctx* ctx, double* out);
+int cf_part_apply_discharges(cf_ctx* ctx, double q_in, double q_out);
+
 /* How the step shares its FP64 work between GB300's FP64 pipe and its integer pipes (results
  * are identical bit for bit in every setting): int_compare 1 evaluates the edge kernel's
  * comparisons on integer keys of the bit patterns; bits 0-3 of int_mul_warps are a mask over

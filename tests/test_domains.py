@@ -45,6 +45,66 @@ def test_partition_covers_the_mesh_with_exact_neighbourhoods(kind, nparts):
             assert np.array_equal(loc[here], parts[r].owned[there])
 
 
+@pytest.mark.parametrize("kind,nparts", [("flood_waf", 3), ("flood_hllc", 4)])
+def test_exchange_plan_sends_exactly_what_the_halos_hold(kind, nparts):
+    """The part contexts' plan: an owned element is a send element exactly when another part's halo
+    holds it, every part sends each neighbour the elements that neighbour receives, in its order,
+    and the halo is the receive side; the whole mesh's inlet and boundary lists partition over the
+    parts' own entries."""
+    c = _case(kind)
+    parts = domains.partition(c, nparts)
+    held = set()
+    for q in parts:
+        for r, (_, there) in q.recv.items():
+            held.update((r, int(i)) for i in there)
+    g = solver.mesh_tables(c)[0]
+    nb_global = len(domains.boundary_entries(g))
+    seen = []
+    for rank, p in enumerate(parts):
+        cls, send_to, recv_from = domains.part_plan(parts, rank)
+        assert np.array_equal(np.flatnonzero(cls == 2), p.n_owned + np.arange(p.halo.size))
+        for i in range(p.n_owned):
+            assert (cls[i] == 1) == ((rank, i) in held)
+        for r, ids in send_to.items():
+            assert np.array_equal(ids, parts[r].recv[rank][1])
+        for r, here in recv_from.items():
+            assert np.array_equal(here, p.recv[r][0])
+        lb = solver.mesh_tables(p.case, p.params)[0]
+        seen += [(int(p.owned[e]), k) for e, k, _ in domains.boundary_entries(lb) if e < p.n_owned]
+    assert sorted(seen) == [(e, k) for e, k, _ in domains.boundary_entries(g)] and len(seen) == nb_global
+
+
+def test_whole_mesh_sums_follow_the_steps_order():
+    """inlet_sum is calcul_surf_entree's sum as the step forms it (blocks of 32, tree per block,
+    blocks in order) and discharge_sum the discharge sums' (256 strided partial sums of one kind,
+    then a tree): exact on integers, and equal to the same orders written out."""
+    rng = np.random.default_rng(3)
+    v = rng.standard_normal(77)
+    blocks = []
+    for b in range(0, 77, 32):
+        s = list(v[b:b + 32]) + [0.0] * (32 - len(v[b:b + 32]))
+        for i in (16, 8, 4, 2, 1):
+            s = [s[l] + s[l + i] if l < i else s[l] for l in range(32)]
+        blocks.append(s[0])
+    total = 0.0
+    for x in blocks:
+        total = total + x
+    assert domains.inlet_sum(v) == total
+    assert domains.inlet_sum(np.arange(100.0)) == 4950.0
+    q = rng.standard_normal(600)
+    kinds = rng.choice([-1, -2, -3], 600)
+    part = [0.0] * 256
+    for j in range(600):
+        if kinds[j] == -2:
+            part[j % 256] += q[j]
+    w = 128
+    while w:
+        part = [part[t] + part[t + w] if t < w else part[t] for t in range(256)]
+        w //= 2
+    assert domains.discharge_sum(q, kinds, -2) == part[0]
+    assert domains.discharge_sum(np.ones(600), kinds, -1) == float(np.sum(kinds == -1))
+
+
 def _free_port():
     with socket.socket() as s:
         s.bind(("127.0.0.1", 0))
