@@ -109,23 +109,6 @@ __global__ void __launch_bounds__(TILE_C) k_rep_cells(StepArgs a, const double* 
   }
 }
 
-/* The flux and bed sums of every element from the slots the step's edge kernel has just written:
- * what k_rep_cells stores for a replayed step (the same expressions, the same values), for the
- * steps whose records the recording forward keeps. */
-__global__ void __launch_bounds__(TILE_C) k_slot_sums(StepArgs a, Slot* sums) {
-  const int tile = blockIdx.x;
-  const int m = __ldg(a.ctile_mem + tile);
-  const MemberDev& M = a.mdev[m];
-  const int c = tile * TILE_C + threadIdx.x;
-  if (c >= M.cell_end) return;
-  const int4 sl = __ldg(a.cslot + c);
-  const Slot s0 = load_slot_adj(a.slots + sl.x), s1 = load_slot_adj(a.slots + sl.y), s2 = load_slot_adj(a.slots + sl.z);
-  double2* q = reinterpret_cast<double2*>(sums + c);
-  q[0] = make_double2(s0.f1 + s1.f1 + s2.f1, s0.f2 + s1.f2 + s2.f2);
-  q[1] = make_double2(s0.f3 + s1.f3 + s2.f3, s0.bx + s1.bx + s2.bx);
-  q[2] = make_double2(s0.by + s1.by + s2.by, 0.0);
-}
-
 /* After step n: the gauge elevations h + z of the new state and, when recording, every
  * member's dt and start time of the step (read from its record of parity p). */
 __global__ void k_record(const double4* Unew, const double* zcell, const MemberState* S, int nm, int p, int n,
@@ -469,11 +452,6 @@ int launch_replay_step(const StepArgs& a, const double* dt_hist, const double* t
     default: return CF_ENOTSUP;
   }
   k_rep_cells<<<a.n_ctiles, TILE_C, 0, st>>>(a, dt_hist, n, flag, sums);
-  return chk(cudaGetLastError());
-}
-
-int launch_slot_sums(const StepArgs& a, Slot* sums, stream_t s) {
-  k_slot_sums<<<a.n_ctiles, TILE_C, 0, reinterpret_cast<cudaStream_t>(s)>>>(a, sums);
   return chk(cudaGetLastError());
 }
 

@@ -326,8 +326,8 @@ int forward_impl(cf_adjoint* a, int32_t replay, double* eta_out, double* state_o
     sa.steady = 0;   /* the adjoint's run has N steps: no steady-state stop */
     if (!replay) {
       sa.mst = a->mst;
+      sa.sums_out = sums;   /* the element kernel stores the step's sums for the stored records */
       if ((rc = launch_step(sa, st, nullptr, nullptr))) return fail(c, rc, "step launch failed");
-      if (sums && (rc = launch_slot_sums(sa, sums, st))) return fail(c, rc, "sums launch failed");
       rc = launch_record(Y, c->zcell, a->mst, a->nm, p, k, a->dt_hist, a->t_hist, a->gcell, a->G, a->eta, st);
     } else {
       if ((rc = launch_replay_step(sa, a->dt_hist, a->t_hist, k, a->flag, sums, st)))

@@ -86,6 +86,7 @@ StepArgs step_args(const cf_ctx* c, int parity) {
   a.bq = c->bq;
   a.host_out = nullptr;
   a.perm = c->perm;
+  a.sums_out = nullptr;
   return a;
 }
 

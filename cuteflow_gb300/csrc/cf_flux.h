@@ -918,37 +918,57 @@ CF_HD CF_INLINE double dbl_hd(uint64_t b) {
 }
 CF_HD CF_INLINE bool finite_u(uint64_t b) { return (b & 0x7ff0000000000000ull) != 0x7ff0000000000000ull; }
 
-/* The two slots of an interior edge whose elements both hold the depth +0 (bit pattern 0), for the
- * first-order and WAF schemes (IFLUX 1-3), written without evaluating the edge.  The general
- * evaluation gives, for any bed elevations and any upwind states:
+/* The two slots of an interior edge whose elements both hold the depth +0 (bit pattern 0), written
+ * without evaluating the edge.  The general evaluation gives, for any bed elevations and any upwind
+ * states:
  *   - masked depths 0, hydrostatic depths max(0, (+0 + z) - max(z, z')) = +0 (the difference is
- *     <= 0 or NaN, and max(0, .) returns the +0 operand), so the wave-speed routine sees both
- *     depths below eps and the flux vector of side A is +0 in every component (side B's too, or
- *     its negation -0 with flux_mode 1; the second first-order evaluation is skipped because the
- *     masked and raw depths agree);
+ *     <= 0 or NaN, and max(0, .) returns the +0 operand); the first-order and WAF schemes
+ *     (IFLUX 1-3) then see both depths below eps and assign +0 to every component of both sides'
+ *     flux vectors (the second first-order evaluation is skipped: masked and raw depths agree);
+ *   - MUSCL-Hancock (IFLUX 4): the local slopes are (+0 - +0) / d = +0, each limited slope is +0 (the
+ *     limiters return their +0 operand for a +0 local slope and an upwind slope of either sign; a
+ *     NaN slope of van Leer's 0 / 0 is removed by the max with 0), so the face depths, the clamped
+ *     face velocities and the predicted states are +0 and the wave-speed routine gives the frame
+ *     flux (+0, +0, +0); rotated back, a2 = nx 0 - ny 0, a3 = ny 0 + nx 0 (side B with -n), signed
+ *     zeros formed here by the same operations (the time step must be finite);
+ *   - with flux_mode 1 side B's fluxes are the negated side A's;
  *   - the bed source (g/2 (ha^2 - h^2)) len with ha = h = +0: (g/2 * +0) * len, a zero with the
  *     sign of g times the sign of len, then times nx, ny (side B negated).
  * Every product of a zero and a finite number is the zero with the product of the signs, so the
  * slots are these signed zeros whenever g, len, nx and ny are finite; otherwise (returns false)
  * the caller evaluates the edge. */
-CF_HD CF_INLINE bool dry_edge_slots(double g, int flux_mode, const double4& geo, Slot* sa) {
+template <int IFLUX>
+CF_HD CF_INLINE bool dry_edge_slots(double g, int flux_mode, const double4& geo, Slot* sa, double dt = 0.0) {
   const uint64_t S = 0x8000000000000000ull;
   const uint64_t bg = dbits_hd(g), bnx = dbits_hd(geo.x), bny = dbits_hd(geo.y), bl = dbits_hd(geo.z);
   if (!(finite_u(bg) & finite_u(bnx) & finite_u(bny) & finite_u(bl))) return false;
-  const uint64_t sl = bl & S;                              /* F.a * len */
-  const uint64_t sb = (flux_mode == 1) ? (sl ^ S) : sl;    /* F.b * len */
+  if (IFLUX == 4 && !finite_u(dbits_hd(dt))) return false;
+  const uint64_t sl = bl & S;                              /* the sign of len */
   const uint64_t st = (bg & S) ^ sl;                       /* ta = tb = (g/2 * +0) * len */
+  /* the flux vectors (before * len): side A's frame flux rotated by n, side B's by -n */
+  uint64_t a1 = 0, a2 = 0, a3 = 0, b1 = 0, b2 = 0, b3 = 0;
+  if (IFLUX == 4) {
+    const double x = geo.x * 0.0, y = geo.y * 0.0, mx = (-geo.x) * 0.0, my = (-geo.y) * 0.0;
+    a2 = dbits_hd(x - y);
+    a3 = dbits_hd(y + x);
+    b2 = dbits_hd(mx - my);
+    b3 = dbits_hd(my + mx);
+  }
+  if (flux_mode == 1) {
+    b1 = a1 ^ S;
+    b2 = a2 ^ S;
+    b3 = a3 ^ S;
+  }
   Slot* sbp = sa + 1;
-  const double fa = dbl_hd(sl), fb = dbl_hd(sb);
-  sa->f1 = fa;
-  sa->f2 = fa;
-  sa->f3 = fa;
+  sa->f1 = dbl_hd((a1 & S) ^ sl);
+  sa->f2 = dbl_hd((a2 & S) ^ sl);
+  sa->f3 = dbl_hd((a3 & S) ^ sl);
   sa->bx = dbl_hd(st ^ (bnx & S));
   sa->by = dbl_hd(st ^ (bny & S));
   sa->q = 0.0;
-  sbp->f1 = fb;
-  sbp->f2 = fb;
-  sbp->f3 = fb;
+  sbp->f1 = dbl_hd((b1 & S) ^ sl);
+  sbp->f2 = dbl_hd((b2 & S) ^ sl);
+  sbp->f3 = dbl_hd((b3 & S) ^ sl);
   sbp->bx = dbl_hd(st ^ (bnx & S) ^ S);
   sbp->by = dbl_hd(st ^ (bny & S) ^ S);
   sbp->q = 0.0;
@@ -964,11 +984,12 @@ CF_HD CF_INLINE void edge_body(const StepArgs& a, const MemberDev& M, int e, dou
   const double4 UA = ld4(a.Uin + ab.x);   /* {h, hu, hv, RN(1/h)} */
   Slot* sa = a.slots + 2 * (size_t)e;
 
-  if (IFLUX <= 3 && ab.y >= 0) {
+  if (ab.y >= 0) {
     /* an edge between two dry elements (most of a flood plain that the water has not reached)
      * needs neither its geometry beyond the normal nor its upwind states */
     const double hB = ldro(reinterpret_cast<const double*>(a.Uin + ab.y));
-    if ((dbits_hd(UA.x) | dbits_hd(hB)) == 0 && dry_edge_slots(M.gp, a.flux_mode, ld4(a.egeo + e), sa)) return;
+    if ((dbits_hd(UA.x) | dbits_hd(hB)) == 0 && dry_edge_slots<IFLUX>(M.gp, a.flux_mode, ld4(a.egeo + e), sa, dt))
+      return;
   }
   const double4 ez = ld4(a.ez + e);       /* bed of A, of B, of A's and B's upwind reconstructions */
 

@@ -134,6 +134,8 @@ struct StepArgs {
   double* host_out;          /* one member: the element kernel also writes (h, hu, hv) of element c to
                                 host_out[3 perm[c] ..] (the caller's order), or NULL */
   const int32_t* perm;       /* new -> reference element order (member-local) */
+  Slot* sums_out;            /* the adjoint's recording forward: every element's flux and bed sums of the
+                                step (the expressions k_rep_cells stores), or NULL */
 };
 
 /* ---- host preprocessing (cf_mesh.cpp) ---------------------------------------------- */
@@ -275,8 +277,6 @@ struct AdjArgs {
  * OR-ed into *flag. */
 int launch_replay_step(const StepArgs& a, const double* dt_hist, const double* t_hist, int n, uint32_t* flag,
                        Slot* sums, stream_t s);
-/* every element's flux and bed sums from the slots of the step just launched with a, into sums */
-int launch_slot_sums(const StepArgs& a, Slot* sums, stream_t s);
 /* gauge elevations h + z of Unew into eta row n; with S, also dt / t of parity p into the histories */
 int launch_record(const double4* Unew, const double* zcell, const MemberState* S, int nm, int p, int n, double* dt_hist,
                   double* t_hist, const int32_t* gcell, int G, double* eta, stream_t s);

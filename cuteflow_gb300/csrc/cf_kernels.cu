@@ -197,6 +197,13 @@ __global__ void __launch_bounds__(BC, 768 / BC) k_cells(StepArgs a) {
     const Slot s0 = load_slot(a.slots + sl.x);
     const Slot s1 = load_slot(a.slots + sl.y);
     const Slot s2 = load_slot(a.slots + sl.z);
+    if (a.sums_out) {
+      /* the sums element_update forms (same expressions, same values) */
+      double2* q = reinterpret_cast<double2*>(a.sums_out + c);
+      q[0] = make_double2(s0.f1 + s1.f1 + s2.f1, s0.f2 + s1.f2 + s2.f2);
+      q[1] = make_double2(s0.f3 + s1.f3 + s2.f3, s0.bx + s1.bx + s2.bx);
+      q[2] = make_double2(s0.by + s1.by + s2.by, 0.0);
+    }
     bool nonfinite = false;
     /* bit 4 of xd_mul_mask: the element's arithmetic on the integer pipes (cf_xd.h) */
     if (a.xd_cmp && (a.xd_mul_mask & XD_CELLS)) V = element_update<XD<true>>(M, U, st, s0, s1, s2, dt, nonfinite);

@@ -423,7 +423,8 @@ extern "C" int harness_tangent(const cf_mesh* m, const cf_params* p, const doubl
 }
 
 /* The dry-region shortcuts of the step against the general evaluation they skip, on n random
- * adversarial cases each: dry_edge_slots against interior_edge (IFLUX 1-3, every limiter, both
+ * adversarial cases each: dry_edge_slots against interior_edge (IFLUX 1-3) and
+ * interior_edge_muscl (IFLUX 4), every limiter, both
  * flux modes, the three arithmetic types) for two elements of depth +0 with random beds (signed
  * zeros, ties, infinities, NaN), random upwind states (wet ones too), random signs of g, nx, ny
  * and len (zeros included); dry_element against element_update_full with random friction
@@ -464,7 +465,7 @@ extern "C" long long harness_dry_check(long long n, unsigned long long seed, lon
     const double up[4] = {(rnd() & 1) ? 2.0 * unif() : 0.0, sgn(unif()), (rnd() & 1) ? 2.0 * unif() : 0.0, sgn(unif())};
     const double zu[2] = {3.0 * unif(), 3.0 * unif()};
     const double dt = 1e-3 + unif();
-    const int iflux = 1 + (int)(rnd() % 3), ilim = (int)(rnd() % 5), fm = (int)(rnd() % 2), xd = (int)(rnd() % 3);
+    const int iflux = 1 + (int)(rnd() % 4), ilim = (int)(rnd() % 5), fm = (int)(rnd() % 2), xd = (int)(rnd() % 3);
     const double huA = sgn(unif()), hvA = sgn(unif()), huB = sgn(unif()), hvB = sgn(unif());
     double o[10];
     auto general = [&](auto tag) {
@@ -476,16 +477,26 @@ extern "C" long long harness_dry_check(long long n, unsigned long long seed, lon
       else if (iflux == 2)
         interior_edge<2, T>(M, ilim, fm, G, dt, T(0.0), T(huA), T(hvA), zl, 0.0, T(0.0), T(huB), T(hvB), zr, 0.0,
                             T(up[0]), T(up[1]), zu[0], T(up[2]), T(up[3]), zu[1], ot);
-      else
+      else if (iflux == 3)
         interior_edge<3, T>(M, ilim, fm, G, dt, T(0.0), T(huA), T(hvA), zl, 0.0, T(0.0), T(huB), T(hvB), zr, 0.0,
                             T(up[0]), T(up[1]), zu[0], T(up[2]), T(up[3]), zu[1], ot);
+      else {
+        const T ua[3] = {T(up[0]), T(up[1]), T(-up[3])}, ub[3] = {T(up[2]), T(up[3]), T(up[1])};
+        interior_edge_muscl<T>(M, ilim, fm, G, dt, T(0.0), T(huA), T(hvA), zl, 0.0, T(0.0), T(huB), T(hvB), zr, 0.0, ua,
+                               zu[0], ub, zu[1], ot);
+      }
       for (int k = 0; k < 10; ++k) o[k] = val(ot[k]);
     };
     if (xd == 0) general(0.0);
     else if (xd == 1) general(XD<false>(0.0));
     else general(XD<true>(0.0));
     Slot sl[2];
-    if (dry_edge_slots(M.gp, fm, make_double4(G.nx, G.ny, G.len, G.d_mrl), sl)) {
+    const double4 geo = make_double4(G.nx, G.ny, G.len, G.d_mrl);
+    const bool took_edge = iflux == 1   ? dry_edge_slots<1>(M.gp, fm, geo, sl, dt)
+                           : iflux == 2 ? dry_edge_slots<2>(M.gp, fm, geo, sl, dt)
+                           : iflux == 3 ? dry_edge_slots<3>(M.gp, fm, geo, sl, dt)
+                                        : dry_edge_slots<4>(M.gp, fm, geo, sl, dt);
+    if (took_edge) {
       ++took;
       const double w[10] = {sl[0].f1, sl[0].f2, sl[0].f3, sl[0].bx, sl[0].by, sl[1].f1, sl[1].f2, sl[1].f3, sl[1].bx, sl[1].by};
       bool ok = same(sl[0].q, 0.0) && same(sl[1].q, 0.0);
