@@ -869,8 +869,9 @@ int cf_autotune(cf_ctx* ctx, int32_t steps_per_trial, int32_t* int_compare, int3
   };
   /* 1. how the FP64 work is shared with the integer pipes, at the current launch shape:
    * all on the FP64 pipe; comparisons on the integer pipes; comparisons and the arithmetic of
-   * all edge warps, of half of them, and of all edge warps and the elements */
-  const int32_t cand[5][2] = {{0, 0}, {1, 0}, {1, 0xf}, {1, 0x5}, {1, 0x1f}};
+   * all edge warps, of half of them, of three of four, each without and with the elements, and
+   * of the elements alone */
+  const int32_t cand[8][2] = {{0, 0}, {1, 0}, {1, 0xf}, {1, 0x5}, {1, 0x1f}, {1, 0x15}, {1, 0x17}, {1, 0x10}};
   double best = 1e300;
   int32_t bc = cmp0, bm = mul0, beb = eb0, bept = ept0, bcb = cb0;
   rc = CF_OK;

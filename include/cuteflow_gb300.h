@@ -319,7 +319,7 @@ int cf_set_launch_shape(cf_ctx* ctx, int32_t edge_block, int32_t edges_per_threa
 int cf_get_launch_shape(cf_ctx* ctx, int32_t* edge_block, int32_t* edges_per_thread, int32_t* cell_block);
 /* Autotuner: times steps_per_trial steps on the context's own state and keeps the fastest
  * setting (the state, time and step count are restored after each trial, so the simulation is
- * unchanged): first the integer-pipe setting (5 candidates), then the edge kernel's launch shape
+ * unchanged): first the integer-pipe setting (8 candidates), then the edge kernel's launch shape
  * (6) and the element kernel's block (2).  Returns the integer-pipe setting and the best time per
  * step; cf_get_launch_shape reports the shape.  Every member must have a state and be running.
  * Outputs may be NULL. */
