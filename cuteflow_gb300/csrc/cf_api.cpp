@@ -442,9 +442,12 @@ int enqueue_set_state(cf_ctx* c, int32_t m, double t0, const double* src = nullp
   CF_CUDA(c, cudaMemcpyAsync(c->mst + m, c->host_state + m, sizeof(MemberState), cudaMemcpyHostToDevice, c->stream));
   int rc;
   if (src) {
-    rc = launch_load_ref(src, c->iperm + M.cell_off, c->U[p0] + M.cell_off, M.n, reinterpret_cast<stream_t>(c->stream));
+    /* the state, and with it the first dt (the block minima of its CFL dt) */
+    rc = launch_load_ref(src, c->iperm + M.cell_off, c->U[p0] + M.cell_off, M.n, reinterpret_cast<stream_t>(c->stream),
+                         c->cstat + M.cell_off, c->mdev, c->mst, m, p0);
     if (rc != CF_OK) return fail(c, rc, "state load launch failed");
     CF_CUDA(c, cudaEventRecord(c->ev[3], c->stream));   /* the host inputs (caller's state, member record) read */
+    return CF_OK;
   } else {
     CF_CUDA(c, cudaEventRecord(c->ev[3], c->stream));   /* the host inputs (caller's state, member record) read */
     rc = launch_scatter_state(c->staging, c->perm + M.cell_off, c->zcell + M.cell_off, c->U[p0] + M.cell_off, M.n,

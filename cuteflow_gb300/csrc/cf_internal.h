@@ -239,7 +239,9 @@ int launch_gather_current(const double4* U0, const double4* U1, const MemberStat
 /* The same directly between a buffer the GPU can address (device memory, or pinned host memory over
  * the CPU link) and U, coalesced on the buffer's side: load writes U[iperm[o]] from hu3[3 o ..];
  * store reads U0 (or, with mst, member m's current buffer of U0 / U1) into hu3. */
-int launch_load_ref(const double* hu3, const int32_t* iperm_old2new, double4* U, int32_t n, stream_t s);
+int launch_load_ref(const double* hu3, const int32_t* iperm_old2new, double4* U, int32_t n, stream_t s,
+                    const double4* cstat = nullptr, const MemberDev* mdev = nullptr, MemberState* mst = nullptr,
+                    int32_t m = 0, int32_t slot = 0);   /* with mst: also the state's CFL dt into mst[m].dt[slot] */
 int launch_store_ref(const double4* U0, const double4* U1, const MemberState* mst, int32_t m,
                      const int32_t* iperm_old2new, double* hu3, int32_t n, stream_t s, bool only_if_stopped = false);
 /* (h, hu, hv) of listed elements (member-local reference ids, iperm member-local) */

@@ -328,7 +328,8 @@ __global__ void k_gather_current(const double4* U0, const double4* U1, const Mem
 constexpr int REF_BLOCK = 256;
 
 __global__ void __launch_bounds__(REF_BLOCK) k_load_ref(const double* __restrict__ hu3, const int32_t* iperm,
-                                                        double4* U, int n) {
+                                                        double4* U, int n, const double4* cstat,
+                                                        const MemberDev* mdev, MemberState* mst, int m, int slot) {
   __shared__ double s[3 * REF_BLOCK];
   const long long base = (long long)blockIdx.x * REF_BLOCK;
   const long long nd = 3 * (long long)min(REF_BLOCK, (int)(n - base));
@@ -340,11 +341,20 @@ __global__ void __launch_bounds__(REF_BLOCK) k_load_ref(const double* __restrict
   }
   __syncthreads();
   const long long o = base + threadIdx.x;
-  if (o >= n) return;
-  const double h = s[3 * threadIdx.x], hu = s[3 * threadIdx.x + 1], hv = s[3 * threadIdx.x + 2];
-  double4* u = U + iperm[o];
-  reinterpret_cast<double2*>(u)[0] = make_double2(h, hu);
-  reinterpret_cast<double2*>(u)[1] = make_double2(hv, h > 0.0 ? 1.0 / h : 0.0);
+  const bool active = o < n;
+  double4 V = make_double4(0.0, 0.0, 0.0, 0.0);
+  double cflL = 0.0;
+  if (active) {
+    const double h = s[3 * threadIdx.x], hu = s[3 * threadIdx.x + 1], hv = s[3 * threadIdx.x + 2];
+    const int c = iperm[o];
+    V = make_double4(h, hu, hv, h > 0.0 ? 1.0 / h : 0.0);
+    double4* u = U + c;
+    reinterpret_cast<double2*>(u)[0] = make_double2(V.x, V.y);
+    reinterpret_cast<double2*>(u)[1] = make_double2(V.z, V.w);
+    if (mst) cflL = ld4(cstat + c).z;
+  }
+  /* with mst: the initial dt of the state (k_cfl's minimum), folded into mst[m].dt[slot] */
+  if (mst) block_cfl_min<REF_BLOCK>(mdev[m], active, cflL, V, &mst[m].dt[slot]);
 }
 
 __global__ void __launch_bounds__(REF_BLOCK) k_store_ref(const double4* U0, const double4* U1, const MemberState* mst,
@@ -687,9 +697,11 @@ int launch_steady_apply(const MemberDev* mdev, MemberState* mst, double qi, doub
   return check(cudaGetLastError());
 }
 
-int launch_load_ref(const double* hu3, const int32_t* iperm, double4* U, int32_t n, stream_t s) {
+int launch_load_ref(const double* hu3, const int32_t* iperm, double4* U, int32_t n, stream_t s, const double4* cstat,
+                    const MemberDev* mdev, MemberState* mst, int32_t m, int32_t slot) {
   if (n <= 0) return CF_OK;
-  k_load_ref<<<(n + REF_BLOCK - 1) / REF_BLOCK, REF_BLOCK, 0, reinterpret_cast<cudaStream_t>(s)>>>(hu3, iperm, U, n);
+  k_load_ref<<<(n + REF_BLOCK - 1) / REF_BLOCK, REF_BLOCK, 0, reinterpret_cast<cudaStream_t>(s)>>>(
+      hu3, iperm, U, n, cstat, mdev, mst, m, slot);
   return check(cudaGetLastError());
 }
 
