@@ -510,7 +510,7 @@ def run_ours(args):
     # chosen one restored
     shape = s.launch_shape()
     shape_ms = {}
-    for eb in (64, 128, 256):
+    for eb in ((64, 128, 256) if not args.no_shape_sweep else ()):
         for ept in (1, 2):
             for cb in (256, 128):
                 s.set_launch_shape(eb, ept, cb)
@@ -715,6 +715,8 @@ def main():
     ap.add_argument("--config", default="flooding", choices=["flooding", "flooding_muscl", "dam_break", "ensemble", "ensemble_sizes"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (every operation on the FP64 pipe)")
+    ap.add_argument("--no-shape-sweep", action="store_true",
+                    help="do not time every launch shape beside the chosen one (the profiling commands use it)")
     ap.add_argument("--tuning", default=None, metavar="CMP,MASK",
                     help="fix the edge kernel's integer-pipe setting instead of autotuning (e.g. 1,15)")
     ap.add_argument("--batched-members", type=int, default=32, help="ensemble sample beside the plain line (0: skip)")
