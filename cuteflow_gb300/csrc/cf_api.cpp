@@ -84,8 +84,6 @@ StepArgs step_args(const cf_ctx* c, int parity) {
   a.c_lo = 0;
   a.c_hi = 0x7fffffff;
   a.bq = c->bq;
-  a.host_out = nullptr;
-  a.perm = c->perm;
   a.sums_out = nullptr;
   return a;
 }
@@ -544,16 +542,13 @@ int get_state_member(cf_ctx* c, int32_t m, double* dst, cudaMemcpyKind kind) {
 }
 
 /* the launches of nsteps steps and the discharge diagnostics (stream-ordered, no wait) */
-int enqueue_steps(cf_ctx* c, int32_t nsteps, double* host_out = nullptr) {
+int enqueue_steps(cf_ctx* c, int32_t nsteps) {
   if (nsteps < 0) return fail(c, CF_EINVAL, "nsteps < 0");
   CF_CUDA(c, cudaSetDevice(c->device));
   int rc;
   c->flux_ms = c->update_ms = 0.0;
   c->launches = 0;
-  /* host_out (one member): the last step's element kernel also writes the new state there, in the
-   * caller's element order (a pinned buffer the device reaches: the write overlaps the update) */
-  const bool fuse = host_out && nsteps >= 1 && !c->timing;
-  int32_t left = fuse ? nsteps - 1 : nsteps;
+  int32_t left = nsteps;
   if (c->timing) {
     for (int32_t i = 0; i < nsteps; ++i) {
       CF_CUDA(c, cudaEventRecord(c->ev[0], c->stream));
@@ -576,16 +571,9 @@ int enqueue_steps(cf_ctx* c, int32_t nsteps, double* host_out = nullptr) {
       if (!c->graph2 && (rc = build_graph(c))) return rc;
       for (; left >= 2; left -= 2) CF_CUDA(c, cudaGraphLaunch(c->graph2, c->stream));
     }
-    const int32_t run = fuse ? nsteps - 1 : nsteps;
     while (left > 0) {
-      if ((rc = enqueue_step(c, (int)((c->launched + run - left) & 1), false))) return rc;
+      if ((rc = enqueue_step(c, (int)((c->launched + nsteps - left) & 1), false))) return rc;
       --left;
-    }
-    if (fuse) {
-      StepArgs a = step_args(c, (int)((c->launched + nsteps - 1) & 1));
-      a.host_out = host_out;
-      if ((rc = launch_step(a, reinterpret_cast<stream_t>(c->stream), nullptr, nullptr)))
-        return fail(c, rc, "kernel launch failed");
     }
     c->launches = 2 * (int64_t)nsteps;
   }
@@ -1108,16 +1096,16 @@ int cf_advance(cf_ctx* c, const double* hu3_in, double t0, int32_t nsteps, doubl
   double* vout = static_cast<double*>(device_view(c, hu3_out));
   if (!vin) CF_CUDA(c, cudaMemcpyAsync(c->staging, hu3_in, bytes, cudaMemcpyDefault, c->stream));
   int rc = enqueue_set_state(c, 0, t0, vin);
-  if (rc == CF_OK) rc = enqueue_steps(c, nsteps, vout);
+  if (rc == CF_OK) rc = enqueue_steps(c, nsteps);
   if (rc != CF_OK) {
     cudaStreamSynchronize(c->stream);
     return rc;
   }
-  /* with vout the last step wrote it unless the member has stopped (then nothing ran, or a
-   * non-finite value stopped it): the store runs only for a stopped member, or without steps */
+  /* the store kernel writes the caller's buffer in its own order with coalesced stores (a step's
+   * element kernel writing it through the permutation took 0.33 instead of 0.24 ms per 1M step,
+   * its scattered 8-byte stores crossing the CPU link) */
   if (vout)
-    rc = launch_store_ref(c->U[0] + M.cell_off, c->U[1] + M.cell_off, c->mst, 0, c->iperm + M.cell_off, vout, M.n, st,
-                          nsteps >= 1 && !c->timing);
+    rc = launch_store_ref(c->U[0] + M.cell_off, c->U[1] + M.cell_off, c->mst, 0, c->iperm + M.cell_off, vout, M.n, st);
   else
     rc = launch_gather_current(c->U[0] + M.cell_off, c->U[1] + M.cell_off, c->mst, 0, c->iperm + M.cell_off,
                                c->staging, M.n, st);

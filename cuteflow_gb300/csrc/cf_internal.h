@@ -131,9 +131,6 @@ struct StepArgs {
   int32_t cblock;            /* threads per block of the element kernel (128, 256) */
   int32_t c_lo, c_hi;        /* elements the element kernel updates: [c_lo, c_hi) of the flat space */
   const int32_t* bq;         /* boundary edges of every member in reference order (MemberDev.bq_*) */
-  double* host_out;          /* one member: the element kernel also writes (h, hu, hv) of element c to
-                                host_out[3 perm[c] ..] (the caller's order), or NULL */
-  const int32_t* perm;       /* new -> reference element order (member-local) */
   Slot* sums_out;            /* the adjoint's recording forward: every element's flux and bed sums of the
                                 step (the expressions k_rep_cells stores), or NULL */
 };
@@ -243,7 +240,7 @@ int launch_load_ref(const double* hu3, const int32_t* iperm_old2new, double4* U,
                     const double4* cstat = nullptr, const MemberDev* mdev = nullptr, MemberState* mst = nullptr,
                     int32_t m = 0, int32_t slot = 0);   /* with mst: also the state's CFL dt into mst[m].dt[slot] */
 int launch_store_ref(const double4* U0, const double4* U1, const MemberState* mst, int32_t m,
-                     const int32_t* iperm_old2new, double* hu3, int32_t n, stream_t s, bool only_if_stopped = false);
+                     const int32_t* iperm_old2new, double* hu3, int32_t n, stream_t s);
 /* (h, hu, hv) of listed elements (member-local reference ids, iperm member-local) */
 int launch_gather_ids(const double4* U, const int32_t* iperm, const int32_t* ids, double* out, int32_t n, stream_t s);
 int launch_scatter_ids(double4* U, const int32_t* iperm, const int32_t* ids, const double* in, int32_t n, stream_t s);
