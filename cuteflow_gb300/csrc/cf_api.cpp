@@ -51,6 +51,7 @@ StepArgs step_args(const cf_ctx* c, int parity) {
   a.Uin = c->U[parity];
   a.Uout = c->U[1 - parity];
   a.cslot = c->cslot;
+  a.cnbr = c->cnbr;
   a.cstat = c->cstat;
   a.ecell = c->ecell;
   a.egeo = c->egeo;
@@ -90,7 +91,7 @@ StepArgs step_args(const cf_ctx* c, int parity) {
 
 void free_all(cf_ctx* c) {
   if (c->graph2) cudaGraphExecDestroy(c->graph2);
-  void* ptrs[] = {c->U[0], c->U[1], c->cslot, c->cstat, c->zcell, c->perm, c->iperm, c->ecell, c->egeo, c->ez,
+  void* ptrs[] = {c->U[0], c->U[1], c->cslot, c->cnbr, c->cstat, c->zcell, c->perm, c->iperm, c->ecell, c->egeo, c->ez,
                   c->ebid, c->eupw, c->ewts, c->edk, c->einv, c->slots, c->etile_mem, c->ctile_mem, c->mdev,
                   c->mst, c->staging, c->inl_cell, c->inl_len, c->ids, c->bq, c->elist1, c->elist2,
                   c->xsend, c->xrecv, c->terms};
@@ -289,7 +290,7 @@ int create_impl(const cf_mesh* meshes, const cf_params* params, int32_t nm, cf_c
   int rc;
   const bool second = c->iflux >= 3;
   if ((rc = dalloc(c, &c->U[0], c->n_pad)) || (rc = dalloc(c, &c->U[1], c->n_pad)) ||
-      (rc = dalloc(c, &c->cslot, c->n_pad)) || (rc = dalloc(c, &c->cstat, c->n_pad)) ||
+      (rc = dalloc(c, &c->cslot, c->n_pad)) || (rc = dalloc(c, &c->cnbr, c->n_pad)) || (rc = dalloc(c, &c->cstat, c->n_pad)) ||
       (rc = dalloc(c, &c->zcell, c->n_pad)) || (rc = dalloc(c, &c->perm, c->n_pad)) ||
       (rc = dalloc(c, &c->iperm, c->n_pad)) || (rc = dalloc(c, &c->ecell, c->ne_pad)) ||
       (rc = dalloc(c, &c->egeo, c->ne_pad)) || (rc = dalloc(c, &c->ebid, c->ne_pad)) ||
@@ -320,7 +321,13 @@ int create_impl(const cf_mesh* meshes, const cf_params* params, int32_t nm, cf_c
     for (auto& s : cslot) { s.x += 2 * eo; s.y += 2 * eo; s.z += 2 * eo; }
     std::vector<int2> ecell(P.ecell);
     for (auto& e2 : ecell) { e2.x += co; if (e2.y >= 0) e2.y += co; }
-    if ((rc = put(c, c->cslot + co, cslot.data(), cslot.size())) || (rc = put(c, c->cstat + co, P.cstat.data(), P.cstat.size())) ||
+    std::vector<int4> cnbr(P.cnbr);
+    for (auto& b : cnbr) {
+      if (b.x >= 0) b.x += co;
+      if (b.y >= 0) b.y += co;
+      if (b.z >= 0) b.z += co;
+    }
+    if ((rc = put(c, c->cslot + co, cslot.data(), cslot.size())) || (rc = put(c, c->cnbr + co, cnbr.data(), cnbr.size())) || (rc = put(c, c->cstat + co, P.cstat.data(), P.cstat.size())) ||
         (rc = put(c, c->zcell + co, P.zcell.data(), P.zcell.size())) || (rc = put(c, c->perm + co, P.perm.data(), P.perm.size())) ||
         (rc = put(c, c->iperm + co, P.iperm.data(), P.iperm.size())) || (rc = put(c, c->ecell + eo, ecell.data(), ecell.size())) ||
         (rc = put(c, c->egeo + eo, P.egeo.data(), P.egeo.size())) || (rc = put(c, c->ebid + eo, P.ebid.data(), P.ebid.size())) ||
@@ -351,6 +358,7 @@ int create_impl(const cf_mesh* meshes, const cf_params* params, int32_t nm, cf_c
     mdev[i] = M.dev;
     /* the device copies are authoritative; keep the reference-order tables and the permutation */
     std::vector<int4>().swap(P.cslot);
+    std::vector<int4>().swap(P.cnbr);
     std::vector<double4>().swap(P.cstat);
     std::vector<int2>().swap(P.ecell);
     std::vector<double4>().swap(P.egeo);

@@ -40,6 +40,7 @@ struct cf_ctx {
   /* device memory (flat over members) */
   double4* U[2] = {nullptr, nullptr};
   int4* cslot = nullptr;
+  int4* cnbr = nullptr;
   double4* cstat = nullptr;
   double* zcell = nullptr;
   int32_t* perm = nullptr;   /* new -> old, member-local */

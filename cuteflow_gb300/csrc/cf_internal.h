@@ -6,6 +6,8 @@
  *   cells  U[2]  : double4 {h, hu, hv, RN(1/h) (0 where h = 0)} per element, ping-pong (state n in
  *                  U[n & 1]); the bed elevations live in zcell and, per edge, in ez
  *          cslot : int4 {slot of local edge 0, 1, 2, -}   (local edges in the reference's order)
+ *          cnbr  : int4 {element across local edge 0, 1, 2 (-1: boundary), 1 when all three edges
+ *                  are interior with finite normals and lengths, else 0}
  *          cstat : double4 {area, Manning n, cfl*L_cfl, RN(1/area)}
  *   edges  ecell : int2 {A, B}; B >= 0 another element, B < 0 the boundary kind (-1/-2/-3)
  *          egeo  : double4 {nx, ny, len, d_AB}, normal pointing out of A, centroid distance
@@ -100,6 +102,7 @@ struct StepArgs {
   const double4* Uin;
   double4* Uout;
   const int4* cslot;
+  const int4* cnbr;
   const double4* cstat;
   const double4* ez;       /* per edge: bed of A, of B, of the upwind reconstructions of A and B */
   const int2* ecell;
@@ -157,6 +160,7 @@ struct Prep {
   std::vector<HostEdge> edges;    /* interior edges, then boundary edges */
   int32_t n_interior = 0;
   std::vector<int4> cslot;
+  std::vector<int4> cnbr;
   std::vector<double4> cstat;
   std::vector<double> zcell;      /* new order */
   std::vector<int2> ecell;

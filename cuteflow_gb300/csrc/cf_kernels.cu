@@ -167,7 +167,7 @@ __device__ __forceinline__ void block_cfl_min(const MemberDev& M, bool active, d
   block_min_atomic<BC>(dti, target);
 }
 
-/* 768 threads per SM (at most 85 registers; 80 used, 20 bytes spilled): the element update is a chain
+/* 768 threads per SM (at most 85 registers; 80 used, 8 bytes spilled): the element update is a chain
  * of dependent integer-pipe quotients and products, and the extra warps hide its latency
  * (1M elements, tuned, 256-thread blocks: 0.152 -> 0.130 ms).  A block of BC threads (128 or 256,
  * the launch shape) lies within one tile of TILE_C elements, so within one member; each block
@@ -197,21 +197,31 @@ __global__ void __launch_bounds__(BC, 768 / BC) k_cells(StepArgs a) {
     const double4 U = ld4(a.Uin + c);
     const double4 st = ld4(a.cstat + c);   /* area, manning n, cfl L, - */
     const int4 sl = __ldg(a.cslot + c);
-    const Slot s0 = load_slot(a.slots + sl.x);
-    const Slot s1 = load_slot(a.slots + sl.y);
-    const Slot s2 = load_slot(a.slots + sl.z);
-    if (SUMS) {
-      /* the sums element_update forms (same expressions, same values) */
-      double2* q = reinterpret_cast<double2*>(a.sums_out + c);
-      q[0] = make_double2(s0.f1 + s1.f1 + s2.f1, s0.f2 + s1.f2 + s2.f2);
-      q[1] = make_double2(s0.f3 + s1.f3 + s2.f3, s0.bx + s1.bx + s2.bx);
-      q[2] = make_double2(s0.by + s1.by + s2.by, 0.0);
+    /* a dry element amid dry ones (most of an unflooded plain): its slots are signed zeros and
+     * its update is +0, known from four depths instead of its three slots */
+    bool dry = false;
+    if (!SUMS) {
+      const int4 nb = __ldg(a.cnbr + c);
+      dry = dry_element_state(M, U, st, dt) &&
+            dry_neighbourhood(M, nb, U, [&](int k) { return ldro(reinterpret_cast<const double*>(a.Uin + k)); });
     }
-    bool nonfinite = false;
-    /* bit 4 of xd_mul_mask: the element's arithmetic on the integer pipes (cf_xd.h) */
-    if (a.xd_cmp && (a.xd_mul_mask & XD_CELLS)) V = element_update<XD<true>>(M, U, st, s0, s1, s2, dt, nonfinite);
-    else V = element_update(M, U, st, s0, s1, s2, dt, nonfinite);
-    if (nonfinite) atomicOr(&S->status, CF_STATUS_NONFINITE);
+    if (!dry) {
+      const Slot s0 = load_slot(a.slots + sl.x);
+      const Slot s1 = load_slot(a.slots + sl.y);
+      const Slot s2 = load_slot(a.slots + sl.z);
+      if (SUMS) {
+        /* the sums element_update forms (same expressions, same values) */
+        double2* q = reinterpret_cast<double2*>(a.sums_out + c);
+        q[0] = make_double2(s0.f1 + s1.f1 + s2.f1, s0.f2 + s1.f2 + s2.f2);
+        q[1] = make_double2(s0.f3 + s1.f3 + s2.f3, s0.bx + s1.bx + s2.bx);
+        q[2] = make_double2(s0.by + s1.by + s2.by, 0.0);
+      }
+      bool nonfinite = false;
+      /* bit 4 of xd_mul_mask: the element's arithmetic on the integer pipes (cf_xd.h) */
+      if (a.xd_cmp && (a.xd_mul_mask & XD_CELLS)) V = element_update<XD<true>>(M, U, st, s0, s1, s2, dt, nonfinite);
+      else V = element_update(M, U, st, s0, s1, s2, dt, nonfinite);
+      if (nonfinite) atomicOr(&S->status, CF_STATUS_NONFINITE);
+    }
     double4* o = a.Uout + c;
     reinterpret_cast<double2*>(o)[0] = make_double2(V.x, V.y);
     reinterpret_cast<double2*>(o)[1] = make_double2(V.z, V.w);

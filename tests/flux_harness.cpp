@@ -128,8 +128,17 @@ extern "C" int harness_edge_fluxes(const cf_mesh* m, const cf_params* p, const d
   return 0;
 }
 
-/* The whole GPU step algorithm on the CPU: edge pass, element pass, device dt rule, for
- * nsteps steps from U (reference order); U_out and dt_hist (nsteps+1) like the oracle. */
+/* Elements of the last harness_run that took the element kernel's dry-neighbourhood shortcut,
+ * and those among them whose slots were not all signed zeros (the shortcut would be wrong). */
+static long long g_nbhd_took = 0, g_nbhd_bad = 0;
+extern "C" void harness_nbhd_stats(long long* took, long long* bad) {
+  *took = g_nbhd_took;
+  *bad = g_nbhd_bad;
+}
+
+/* The whole GPU step algorithm on the CPU: edge pass, element pass (with the element kernel's
+ * dry-neighbourhood shortcut, checked against the slots it skips), device dt rule, for nsteps
+ * steps from U (reference order); U_out and dt_hist (nsteps+1) like the oracle. */
 extern "C" int harness_run(const cf_mesh* m, const cf_params* p, const double* U, int nsteps, double* U_out,
                            double* dt_hist, double* t_out, int* steps_out) {
   int done = 0, steady_iter = 0;
@@ -137,6 +146,7 @@ extern "C" int harness_run(const cf_mesh* m, const cf_params* p, const double* U
   std::string err;
   int rc = prepare_mesh(m, p, P, err);
   if (rc != CF_OK) return rc;
+  g_nbhd_took = g_nbhd_bad = 0;
   const int n = P.nelt;
   std::vector<double4> Ua(n), Ub(n);
   for (int c = 0; c < n; ++c) {
@@ -177,6 +187,12 @@ extern "C" int harness_run(const cf_mesh* m, const cf_params* p, const double* U
     for (int c = 0; c < n; ++c) {
       const int* sl = &P.cslot[c].x;
       bool nf = false;
+      if (dry_element_state(M, cur[c], P.cstat[c], dt) &&
+          dry_neighbourhood(M, P.cnbr[c], cur[c], [&](int k) { return cur[k].x; })) {
+        ++g_nbhd_took;
+        if (!dry_element(M, cur[c], P.cstat[c], slots[sl[0]], slots[sl[1]], slots[sl[2]], dt)) ++g_nbhd_bad;
+        nxt[c] = make_double4(0.0, 0.0, 0.0, 0.0);
+      } else
       nxt[c] = g_xd == 0 ? element_update(M, cur[c], P.cstat[c], slots[sl[0]], slots[sl[1]], slots[sl[2]], dt, nf)
                : g_xd == 1 ? element_update<XD<false>>(M, cur[c], P.cstat[c], slots[sl[0]], slots[sl[1]], slots[sl[2]], dt, nf)
                            : element_update<XD<true>>(M, cur[c], P.cstat[c], slots[sl[0]], slots[sl[1]], slots[sl[2]], dt, nf);

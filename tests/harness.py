@@ -58,6 +58,8 @@ def run(case, nsteps, params=None, U0=None):
         L.harness_run.argtypes = [C.POINTER(_abi.CfMesh), C.POINTER(_abi.CfParams), dp, C.c_int, dp, dp, dp,
                                   C.POINTER(C.c_int)]
         L.harness_run.restype = C.c_int
+        L.harness_nbhd_stats.argtypes = [C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]
+        L.harness_nbhd_stats.restype = None
         L._run_typed = True
     ma = _abi.MeshArrays(case)
     p = _abi.make_params({**case.params, **(params or {})})
@@ -68,7 +70,9 @@ def run(case, nsteps, params=None, U0=None):
     steps = C.c_int(0)
     rc = L.harness_run(C.byref(ma.mesh), C.byref(p), _abi.dptr(U0), int(nsteps), _abi.dptr(U), _abi.dptr(dth),
                        C.byref(t), C.byref(steps))
-    return dict(U=U, dt_hist=dth, t=t.value, rc=rc, steps=steps.value)
+    took, bad = C.c_longlong(0), C.c_longlong(0)
+    L.harness_nbhd_stats(C.byref(took), C.byref(bad))
+    return dict(U=U, dt_hist=dth, t=t.value, rc=rc, steps=steps.value, nbhd_took=took.value, nbhd_bad=bad.value)
 
 
 def set_xd(mode: int):

@@ -113,6 +113,7 @@ def test_full_run_bitwise(oracle, name, make, n, prm):
     c = make()
     r1 = oracle.run(c, n, params=prm, check=False)
     r2 = H.run(c, n, params=prm)
+    assert r2["nbhd_bad"] == 0
     assert r1["rc"] == r2["rc"]
     assert r1["steps"] == r2["steps"]
     assert np.array_equal(r1["dt_hist"], r2["dt_hist"])
@@ -139,10 +140,26 @@ def test_full_run_bitwise_integer_pipes(oracle, name, make, n, prm, mode):
         r2 = H.run(c, n, params=prm)
     finally:
         H.set_xd(0)
+    assert r2["nbhd_bad"] == 0
     assert r1["rc"] == r2["rc"] and r1["steps"] == r2["steps"]
     assert np.array_equal(r1["dt_hist"], r2["dt_hist"])
     assert np.array_equal(r1["U"], r2["U"])
     assert r1["t"] == r2["t"]
+
+
+@pytest.mark.parametrize("name", ["flood_waf", "flood_muscl", "flood_hllc", "dry_start_inflow", "lake_islands",
+                                  "phys_inflow_waf"])
+def test_dry_neighbourhood_shortcut_is_taken_and_exact(oracle, name):
+    """The element kernel's shortcut for a dry element amid dry ones (its depth and its three
+    neighbours' depths +0, three interior edges) skips reading its slots: on the wet/dry cases it
+    is taken, every element that takes it has signed-zero slots (the general test passes on them),
+    and the run is the oracle's bit for bit."""
+    _, make, n, prm = next(c for c in CASES if c[0] == name)
+    c = make()
+    r1 = oracle.run(c, n, params=prm, check=False)
+    r2 = H.run(c, n, params=prm)
+    assert r2["nbhd_took"] > 0 and r2["nbhd_bad"] == 0
+    assert np.array_equal(r1["U"], r2["U"]) and np.array_equal(r1["dt_hist"], r2["dt_hist"])
 
 
 def test_integer_product_is_the_ieee_product():
