@@ -350,20 +350,40 @@ def adjoint_leg(steps: int, warmup: int, obs_every: float = 10.0, budget_gb: flo
     return out
 
 
+def budget_groups(nelts, steps: int, budget: int):
+    """Consecutive instances packed into groups whose adjoint fits budget bytes with every step
+    record stored: 80 bytes per element and step (state and flux sums) plus ~400 bytes per element
+    of step buffers, slots, edge tables and checkpoints, with 2 % of slack.  An instance that does
+    not fit alone forms its own group (its adjoint then replays part of its steps)."""
+    per = lambda n: int(1.02 * n * (80 * steps + 400)) + (64 << 20)
+    groups, cur, used = [], [], 0
+    for i, n in enumerate(nelts):
+        if cur and used + per(n) > budget:
+            groups.append(cur)
+            cur, used = [], 0
+        cur.append(i)
+        used += per(n)
+    if cur:
+        groups.append(cur)
+    return groups
+
+
 def calibration_batch_leg(ninst: int, steps: int, iters: int, obs_every: float = 10.0, full: bool = False,
                           budget_gb: float = 120.0, seq_iters: int = 1, fd_zones: int = 0):
-    """Batched adjoint calibration (a sample of the 64-instance workload): ninst instances of the
-    calibration case with seeded sizes, zone fields and gauges, in one batch context; every
-    gradient-descent iteration runs one recording forward and one backward for all instances in
-    the same launches, sums dJ/dn per zone and steps the zone values on the device.  Timed
-    against the same instances' one-member adjoints run one after another (forward, backward,
-    zone gradient and step each).  Misfit: sum of squared gauge misfits every obs_every s.
-    Instance meshes: 8k-39k triangles for the sample, 50k-273k with full (the workload's sizes);
-    observations every 10 s with full, every 1 s for the sample (its 400 steps cover a few seconds).
-    The batch's adjoint keeps to budget_gb of device memory (its schedule stores the step records
-    of as many of the last steps as fit and replays the rest); each instance run alone gets the
-    same cap.  The one-after-another form runs seq_iters iterations per instance (its time per
-    iteration does not depend on the iteration)."""
+    """Batched adjoint calibration: ninst instances of the calibration case with seeded sizes, zone
+    fields and gauges.  Instances are packed, in order, into groups whose adjoint step records fit
+    budget_gb of device memory together (budget_groups), so that no group replays a step; each
+    group is one batch context, and every gradient-descent iteration runs one recording forward
+    and one backward for the group's instances in the same launches, sums dJ/dn per zone and
+    steps the zone values on the device (the instances are independent calibrations, so the
+    groups run one after another, each for all iterations, with the learning rate of its first
+    gradient).  Timed against the same instances' one-member adjoints run one after another
+    (forward, backward, zone gradient and step each, with the same cap).  Misfit: sum of squared
+    gauge misfits every obs_every s, summed over the instances.  Instance meshes: 8k-39k triangles
+    for the sample, 50k-273k with full (the workload's sizes); observations every 10 s with full,
+    every 1 s for the sample (its 400 steps cover a few seconds).  The one-after-another form runs
+    seq_iters iterations per instance (its time per iteration does not depend on the
+    iteration)."""
     import torch
     from cuteflow_gb300 import Batch, Solver, cases
     from cuteflow_gb300.adjoint import Adjoint, Zones
@@ -379,73 +399,85 @@ def calibration_batch_leg(ninst: int, steps: int, iters: int, obs_every: float =
         inst.append((c, zones, nz, gauges))
     tri = sum(c.nelt for c, *_ in inst)
     zoff = np.cumsum([0] + [len(nz) for _, _, nz, _ in inst])
-    zone_all = np.concatenate([z + zoff[i] for i, (_, z, _, _) in enumerate(inst)]).astype(np.int32)
     true_vals = np.concatenate([nz for _, _, nz, _ in inst])
-    gm = np.concatenate([np.full(len(g), i, np.int32) for i, (_, _, _, g) in enumerate(inst)])
     gg = np.concatenate([g for *_, g in inst]).astype(np.int32)
     budget = int(budget_gb * (1 << 30))
-    b = Batch([c for c, *_ in inst])
-    adj = Adjoint(b, steps, gg, 0, gauge_member=gm, budget_bytes=budget)
-    sched = dict(adj.schedule)
-    zs = Zones(b, zone_all, int(zoff[-1]))
-
-    def start():
-        for i, (c, *_) in enumerate(inst):
-            b.set_state(i, c.U0)
-
-    zs.set(true_vals)
-    start()
-    eta_obs, _ = adj.forward()
-    dt, t = adj.dt_history()
-    obs = [cases.observation_steps(t[:, i], dt[:, i], obs_every) for i in range(ninst)]
-    col = np.cumsum([0] + [len(g) for *_, g in inst])
-    mask = np.zeros_like(eta_obs)
-    for i in range(ninst):
-        mask[obs[i], col[i]:col[i + 1]] = 1.0
+    groups = budget_groups([c.nelt for c, *_ in inst], steps, budget)
     vals0 = np.full(int(zoff[-1]), 0.035)
-    zs.set(vals0)
-    misfits, lr = [], None
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for it in range(iters):
+    vals = vals0.copy()
+    eta_obs_i, mask_i, lr_i = [None] * ninst, [None] * ninst, [None] * ninst
+    misfits = np.zeros(iters + 1)
+    t_batch, scheds, fd = 0.0, [], []
+    for gi, grp in enumerate(groups):
+        # one batch context per group: its adjoint's step records fit the budget (nothing replayed)
+        zl = np.concatenate([inst[i][1] + (zoff[i] - zoff[grp[0]]) for i in grp])
+        gmg = np.concatenate([np.full(len(inst[i][3]), k, np.int32) for k, i in enumerate(grp)])
+        ggg = np.concatenate([inst[i][3] for i in grp]).astype(np.int32)
+        z_lo, z_hi = int(zoff[grp[0]]), int(zoff[grp[-1] + 1])
+        b = Batch([inst[i][0] for i in grp])
+        adj = Adjoint(b, steps, ggg, 0, gauge_member=gmg, budget_bytes=budget)
+        scheds.append({"instances": len(grp), "triangles": int(sum(inst[i][0].nelt for i in grp)), **adj.schedule})
+        zs = Zones(b, zl.astype(np.int32), z_hi - z_lo)
+
+        def start():
+            for k, i in enumerate(grp):
+                b.set_state(k, inst[i][0].U0)
+
+        zs.set(true_vals[z_lo:z_hi])
+        start()
+        eta_obs, _ = adj.forward()
+        dt, t = adj.dt_history()
+        dt, t = dt.reshape(steps, -1), t.reshape(steps, -1)
+        gcol = np.cumsum([0] + [len(inst[i][3]) for i in grp])
+        mask = np.zeros_like(eta_obs)
+        for k, i in enumerate(grp):
+            mask[cases.observation_steps(t[:, k], dt[:, k], obs_every), gcol[k]:gcol[k + 1]] = 1.0
+            eta_obs_i[i], mask_i[i] = eta_obs[:, gcol[k]:gcol[k + 1]], mask[:, gcol[k]:gcol[k + 1]]
+        zs.set(vals0[z_lo:z_hi])
+        lr = None
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for it in range(iters):
+            start()
+            eta, _ = adj.forward()
+            r = (eta - eta_obs) * mask
+            misfits[it] += float(np.sum(r * r))
+            adj.backward(2.0 * r)
+            g = zs.gradient(adj)
+            if lr is None:
+                lr = 0.004 / max(np.abs(g).max(), 1e-300)
+            zs.descend(lr, 0.01, 0.1)
+        torch.cuda.synchronize()
+        t_batch += (time.perf_counter() - t0) / iters
+        for i in grp:
+            lr_i[i] = lr
         start()
         eta, _ = adj.forward()
         r = (eta - eta_obs) * mask
-        misfits.append(float(np.sum(r * r)))
-        adj.backward(2.0 * r)
-        g = zs.gradient(adj)
-        if lr is None:
-            lr = 0.004 / max(np.abs(g).max(), 1e-300)
-        zs.descend(lr, 0.01, 0.1)
-    torch.cuda.synchronize()
-    t_batch = (time.perf_counter() - t0) / iters
-    start()
-    eta, _ = adj.forward()
-    r = (eta - eta_obs) * mask
-    misfits.append(float(np.sum(r * r)))
-    vals, _ = zs.get()
-    # central differences (step 1e-6 relative, the recorded dt sequence replayed) of the zones with
-    # the largest gradients at the final values, against the batch's zone gradient
-    fd = []
-    if fd_zones > 0:
-        adj.backward(2.0 * r)
-        g = zs.gradient(adj)
-        for z in np.argsort(-np.abs(g))[:fd_zones]:
-            d = 1e-6 * vals[z]
-            Jz = []
-            for sign in (1.0, -1.0):
-                v = vals.copy()
-                v[z] += sign * d
-                zs.set(v)
-                start()
-                e_, _ = adj.forward(replay=True)
-                Jz.append(((e_ - eta_obs) * mask))
-            zs.set(vals)
-            dJ = float(np.sum((Jz[0] - Jz[1]) * (Jz[0] + Jz[1])))
-            fdz = dJ / (2.0 * d)
-            fd.append({"zone": int(z), "adjoint": float(g[z]), "central_difference": fdz,
-                       "relative_difference": abs(fdz - g[z]) / abs(g[z])})
-    zs.close(); adj.close(); b.close()
+        misfits[iters] += float(np.sum(r * r))
+        vals[z_lo:z_hi] = zs.get()[0]
+        # central differences (step 1e-6 relative, the recorded dt sequence replayed) of the first
+        # group's zones with the largest gradients at the final values, against its zone gradient
+        if gi == 0 and fd_zones > 0:
+            adj.backward(2.0 * r)
+            g = zs.gradient(adj)
+            vg = vals[z_lo:z_hi]
+            for z in np.argsort(-np.abs(g))[:fd_zones]:
+                d = 1e-6 * vg[z]
+                Jz = []
+                for sign in (1.0, -1.0):
+                    v = vg.copy()
+                    v[z] += sign * d
+                    zs.set(v)
+                    start()
+                    e_, _ = adj.forward(replay=True)
+                    Jz.append(((e_ - eta_obs) * mask))
+                zs.set(vg)
+                dJ = float(np.sum((Jz[0] - Jz[1]) * (Jz[0] + Jz[1])))
+                fdz = dJ / (2.0 * d)
+                fd.append({"zone": int(z_lo + z), "adjoint": float(g[z]), "central_difference": fdz,
+                           "relative_difference": abs(fdz - g[z]) / abs(g[z])})
+        zs.close(); adj.close(); b.close()
     # the same iteration, instance by instance
     t_seq = 0.0
     for i, (c, zones, nz, gauges) in enumerate(inst):
@@ -453,24 +485,23 @@ def calibration_batch_leg(ninst: int, steps: int, iters: int, obs_every: float =
         a1 = Adjoint(s, steps, gauges, 0, budget_bytes=budget)
         z1 = Zones(s, zones, len(nz))
         z1.set(vals0[zoff[i]:zoff[i + 1]])
-        obs_i, mask_i = eta_obs[:, col[i]:col[i + 1]], mask[:, col[i]:col[i + 1]]
         torch.cuda.synchronize()
         t1 = time.perf_counter()
         for it in range(seq_iters):
             s.set_state(c.U0)
             eta_i, _ = a1.forward()
-            a1.backward(2.0 * (eta_i - obs_i) * mask_i)
+            a1.backward(2.0 * (eta_i - eta_obs_i[i]) * mask_i[i])
             z1.gradient(a1)
-            z1.descend(lr, 0.01, 0.1)
+            z1.descend(lr_i[i], 0.01, 0.1)
         torch.cuda.synchronize()
         t_seq += (time.perf_counter() - t1) / seq_iters
         z1.close(); a1.close(); s.close()
     return {"instances": ninst, "triangles_total": tri, "steps": steps, "iterations": iters,
-            "budget_gb": budget_gb, "schedule": sched, "observation_every_s": obs_every,
+            "budget_gb": budget_gb, "groups": scheds, "observation_every_s": obs_every,
             "zones_total": int(zoff[-1]), "gauges_total": int(gg.size),
             "batched_s_per_iteration": t_batch, "sequential_s_per_iteration": t_seq,
             "sequential_iterations_timed": seq_iters,
-            "speedup_vs_sequential": t_seq / t_batch, "misfit_per_iteration": misfits,
+            "speedup_vs_sequential": t_seq / t_batch, "misfit_per_iteration": [float(m) for m in misfits],
             "zone_error_start": float(np.abs(vals0 - true_vals).mean()),
             "zone_error_end": float(np.abs(vals - true_vals).mean()), "fd_check": fd}
 
