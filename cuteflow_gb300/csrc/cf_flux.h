@@ -865,8 +865,7 @@ CF_HD CF_INLINE void interior_edge_muscl(const MemberDev& M, int ilim, int flux_
 }
 
 /* Static data of edge e in the form interior_edge takes. */
-CF_HD CF_INLINE EdgeGeo edge_geo(const StepArgs& a, int e, bool second) {
-  const double4 geo = ld4(a.egeo + e);
+CF_HD CF_INLINE EdgeGeo edge_geo(const StepArgs& a, int e, bool second, const double4& geo) {
   EdgeGeo G;
   G.nx = geo.x;
   G.ny = geo.y;
@@ -886,22 +885,31 @@ CF_HD CF_INLINE EdgeGeo edge_geo(const StepArgs& a, int e, bool second) {
   }
   return G;
 }
+CF_HD CF_INLINE EdgeGeo edge_geo(const StepArgs& a, int e, bool second) { return edge_geo(a, e, second, ld4(a.egeo + e)); }
+
+/* One slot's six values.  On the device three 16-byte stores: every slot array starts on a
+ * 256-byte boundary (cudaMalloc, the no-allocation scratch) and a slot is 48 bytes, so every slot
+ * starts on a 16-byte boundary.  On the host (the CPU harness) plain stores. */
+CF_HD CF_INLINE void store_slot(Slot* p, double f1, double f2, double f3, double bx, double by, double q) {
+#ifdef __CUDA_ARCH__
+  double2* d = reinterpret_cast<double2*>(p);
+  d[0] = make_double2(f1, f2);
+  d[1] = make_double2(f3, bx);
+  d[2] = make_double2(by, q);
+#else
+  p->f1 = f1;
+  p->f2 = f2;
+  p->f3 = f3;
+  p->bx = bx;
+  p->by = by;
+  p->q = q;
+#endif
+}
 
 /* The two slots of an interior edge from interior_edge's out[10]. */
 CF_HD CF_INLINE void write_slots(Slot* sa, const double o[10]) {
-  Slot* sb = sa + 1;
-  sa->f1 = o[0];
-  sa->f2 = o[1];
-  sa->f3 = o[2];
-  sa->bx = o[3];
-  sa->by = o[4];
-  sa->q = 0.0;
-  sb->f1 = o[5];
-  sb->f2 = o[6];
-  sb->f3 = o[7];
-  sb->bx = o[8];
-  sb->by = o[9];
-  sb->q = 0.0;
+  store_slot(sa, o[0], o[1], o[2], o[3], o[4], 0.0);
+  store_slot(sa + 1, o[5], o[6], o[7], o[8], o[9], 0.0);
 }
 
 /* ---- dry regions ------------------------------------------------------------------------ */
@@ -959,19 +967,10 @@ CF_HD CF_INLINE bool dry_edge_slots(double g, int flux_mode, const double4& geo,
     b2 = a2 ^ S;
     b3 = a3 ^ S;
   }
-  Slot* sbp = sa + 1;
-  sa->f1 = dbl_hd((a1 & S) ^ sl);
-  sa->f2 = dbl_hd((a2 & S) ^ sl);
-  sa->f3 = dbl_hd((a3 & S) ^ sl);
-  sa->bx = dbl_hd(st ^ (bnx & S));
-  sa->by = dbl_hd(st ^ (bny & S));
-  sa->q = 0.0;
-  sbp->f1 = dbl_hd((b1 & S) ^ sl);
-  sbp->f2 = dbl_hd((b2 & S) ^ sl);
-  sbp->f3 = dbl_hd((b3 & S) ^ sl);
-  sbp->bx = dbl_hd(st ^ (bnx & S) ^ S);
-  sbp->by = dbl_hd(st ^ (bny & S) ^ S);
-  sbp->q = 0.0;
+  store_slot(sa, dbl_hd((a1 & S) ^ sl), dbl_hd((a2 & S) ^ sl), dbl_hd((a3 & S) ^ sl), dbl_hd(st ^ (bnx & S)),
+             dbl_hd(st ^ (bny & S)), 0.0);
+  store_slot(sa + 1, dbl_hd((b1 & S) ^ sl), dbl_hd((b2 & S) ^ sl), dbl_hd((b3 & S) ^ sl),
+             dbl_hd(st ^ (bnx & S) ^ S), dbl_hd(st ^ (bny & S) ^ S), 0.0);
   return true;
 }
 
@@ -981,6 +980,9 @@ template <int IFLUX, class S = double>
 CF_HD CF_INLINE void edge_body(const StepArgs& a, const MemberDev& M, int e, double dt, double t,
                                const double* surf = nullptr) {
   const int2 ab = ldro(a.ecell + e);
+  /* the normal and length, which every path needs, load beside the element states (a dry edge
+   * then waits for two memory round trips, not three) */
+  const double4 geo = ld4(a.egeo + e);
   const double4 UA = ld4(a.Uin + ab.x);   /* {h, hu, hv, RN(1/h)} */
   Slot* sa = a.slots + 2 * (size_t)e;
 
@@ -988,28 +990,21 @@ CF_HD CF_INLINE void edge_body(const StepArgs& a, const MemberDev& M, int e, dou
     /* an edge between two dry elements (most of a flood plain that the water has not reached)
      * needs neither its geometry beyond the normal nor its upwind states */
     const double hB = ldro(reinterpret_cast<const double*>(a.Uin + ab.y));
-    if ((dbits_hd(UA.x) | dbits_hd(hB)) == 0 && dry_edge_slots<IFLUX>(M.gp, a.flux_mode, ld4(a.egeo + e), sa, dt))
-      return;
+    if ((dbits_hd(UA.x) | dbits_hd(hB)) == 0 && dry_edge_slots<IFLUX>(M.gp, a.flux_mode, geo, sa, dt)) return;
   }
   const double4 ez = ld4(a.ez + e);       /* bed of A, of B, of A's and B's upwind reconstructions */
 
   if (ab.y < 0) {
-    const double4 geo = ld4(a.egeo + e);
     const double len = geo.z;
     const int id = ldro(a.ebid + e);
     const double sf = (surf && ab.y == -1 && M.inlet == 3 && id >= 1 && id <= M.nin) ? surf[id - 1] : 0.0;
     double f1, f2, f3, q;
     boundary_flux(IFLUX, M, ab.y, id, t, geo.x, geo.y, UA.x, UA.y, UA.z, UA.w, ez.x, f1, f2, f3, q, sf);
-    sa->f1 = f1 * len;
-    sa->f2 = f2 * len;
-    sa->f3 = f3 * len;
-    sa->bx = 0.0;
-    sa->by = 0.0;
-    sa->q = q * len;
+    store_slot(sa, f1 * len, f2 * len, f3 * len, 0.0, 0.0, q * len);
     return;
   }
 
-  const EdgeGeo G = edge_geo(a, e, IFLUX >= 3);
+  const EdgeGeo G = edge_geo(a, e, IFLUX >= 3, geo);
   const double4 UB = ld4(a.Uin + ab.y);
   double o[10];
   if (IFLUX == 4) {
