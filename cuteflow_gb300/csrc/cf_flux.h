@@ -974,6 +974,49 @@ CF_HD CF_INLINE bool dry_edge_slots(double g, int flux_mode, const double4& geo,
   return true;
 }
 
+/* An element area for which a dry element's update is exact zeros: a positive normal number (the
+ * sign bit fails the test). */
+CF_HD CF_INLINE bool area_ok(double area) { return (dbits_hd(area) >> 52) - 1u < 2046u; }
+
+/* The conditions on the element's state and the member under which a dry element's update is
+ * (+0, +0, +0, +0), besides area_ok: its depth is +-0, its discharges are finite, dt is finite and
+ * tolisec >= 0. */
+CF_HD CF_INLINE bool dry_state_ok(const MemberDev& M, const double4& U, double dt) {
+  const uint64_t btol = dbits_hd(M.tolisec);
+  const bool tol_ok = (btol >> 63) == 0 && (btol & 0x7fffffffffffffffull) <= 0x7ff0000000000000ull;  /* +0..+inf */
+  return (dbits_hd(U.x) << 1) == 0 && tol_ok && finite_u(dbits_hd(U.y)) && finite_u(dbits_hd(U.z)) &&
+         finite_u(dbits_hd(dt));
+}
+
+/* The conditions on the element itself under which a dry element's update is (+0, +0, +0, +0). */
+CF_HD CF_INLINE bool dry_element_state(const MemberDev& M, const double4& U, const double4& st, double dt) {
+  return area_ok(st.x) && dry_state_ok(M, U, dt);
+}
+
+/* True when the general update of an element provably returns the state (+0, +0, +0, +0) without
+ * flagging it non-finite: dry_element_state holds and every flux and bed-source component of its
+ * three slots is +-0.  Then every residual (0 + 0 - rc) / area and (sb + sf - rc) / area is +0 (the
+ * friction source of a dry element is +0), each new component is the old one plus +-0 (finite),
+ * and the new depth +-0 <= tolisec clamps the state to +0. */
+CF_HD CF_INLINE bool dry_element(const MemberDev& M, const double4& U, const double4& st, const Slot& s0,
+                                 const Slot& s1, const Slot& s2, double dt) {
+  const uint64_t z = (dbits_hd(s0.f1) | dbits_hd(s0.f2) | dbits_hd(s0.f3) | dbits_hd(s0.bx) | dbits_hd(s0.by) |
+                      dbits_hd(s1.f1) | dbits_hd(s1.f2) | dbits_hd(s1.f3) | dbits_hd(s1.bx) | dbits_hd(s1.by) |
+                      dbits_hd(s2.f1) | dbits_hd(s2.f2) | dbits_hd(s2.f3) | dbits_hd(s2.bx) | dbits_hd(s2.by)) << 1;
+  return z == 0 && dry_element_state(M, U, st, dt);
+}
+
+/* True when an element's three slots are signed zeros without reading them: nb (cnbr) flags three
+ * interior edges with finite normals and lengths (and an area for which area_ok holds), the
+ * member's g is finite, and the element and its three neighbours have depth +0 (bits 0), so that
+ * every one of its edges took the edge kernel's dry shortcut (edge_body, dry_edge_slots; the
+ * element kernel reads the same state and dt).  With dry_state_ok it gives dry_element's answer. */
+template <class Ld>
+CF_HD CF_INLINE bool dry_neighbourhood(const MemberDev& M, const int4& nb, const double4& U, Ld h_of) {
+  if (!(nb.w && dbits_hd(U.x) == 0 && finite_u(dbits_hd(M.gp)))) return false;
+  return (dbits_hd(h_of(nb.x)) | dbits_hd(h_of(nb.y)) | dbits_hd(h_of(nb.z))) == 0;
+}
+
 /* Fluxes (times the edge length) and bed sources of edge e into its two slots, from the
  * state U of step n: the body of the edge kernel. */
 template <int IFLUX, class S = double>
@@ -1137,42 +1180,6 @@ CF_HD CF_INLINE void element_core(const MemberDev& M, double area, double yarea,
     hu = T(0.);
     hv = T(0.);
   }
-}
-
-/* The conditions on the element itself under which a dry element's update is (+0, +0, +0, +0):
- * its depth is +-0, its discharges are finite, its area is a positive normal number, dt is finite
- * and tolisec >= 0. */
-CF_HD CF_INLINE bool dry_element_state(const MemberDev& M, const double4& U, const double4& st, double dt) {
-  const uint64_t ba = dbits_hd(st.x);
-  const bool area_ok = (ba >> 52) - 1u < 2046u;   /* positive normal (the sign bit fails the test) */
-  const uint64_t btol = dbits_hd(M.tolisec);
-  const bool tol_ok = (btol >> 63) == 0 && (btol & 0x7fffffffffffffffull) <= 0x7ff0000000000000ull;  /* +0..+inf */
-  return (dbits_hd(U.x) << 1) == 0 && area_ok && tol_ok && finite_u(dbits_hd(U.y)) && finite_u(dbits_hd(U.z)) &&
-         finite_u(dbits_hd(dt));
-}
-
-/* True when the general update of an element provably returns the state (+0, +0, +0, +0) without
- * flagging it non-finite: dry_element_state holds and every flux and bed-source component of its
- * three slots is +-0.  Then every residual (0 + 0 - rc) / area and (sb + sf - rc) / area is +0 (the
- * friction source of a dry element is +0), each new component is the old one plus +-0 (finite),
- * and the new depth +-0 <= tolisec clamps the state to +0. */
-CF_HD CF_INLINE bool dry_element(const MemberDev& M, const double4& U, const double4& st, const Slot& s0,
-                                 const Slot& s1, const Slot& s2, double dt) {
-  const uint64_t z = (dbits_hd(s0.f1) | dbits_hd(s0.f2) | dbits_hd(s0.f3) | dbits_hd(s0.bx) | dbits_hd(s0.by) |
-                      dbits_hd(s1.f1) | dbits_hd(s1.f2) | dbits_hd(s1.f3) | dbits_hd(s1.bx) | dbits_hd(s1.by) |
-                      dbits_hd(s2.f1) | dbits_hd(s2.f2) | dbits_hd(s2.f3) | dbits_hd(s2.bx) | dbits_hd(s2.by)) << 1;
-  return z == 0 && dry_element_state(M, U, st, dt);
-}
-
-/* True when an element's three slots are signed zeros without reading them: nb (cnbr) flags three
- * interior edges with finite normals and lengths, the member's g is finite, and the element and
- * its three neighbours have depth +0 (bits 0), so that every one of its edges took the edge
- * kernel's dry shortcut (edge_body, dry_edge_slots; the element kernel reads the same state and
- * dt).  With dry_element_state it gives dry_element's answer. */
-template <class Ld>
-CF_HD CF_INLINE bool dry_neighbourhood(const MemberDev& M, const int4& nb, const double4& U, Ld h_of) {
-  if (!(nb.w && dbits_hd(U.x) == 0 && finite_u(dbits_hd(M.gp)))) return false;
-  return (dbits_hd(h_of(nb.x)) | dbits_hd(h_of(nb.y)) | dbits_hd(h_of(nb.z))) == 0;
 }
 
 /* The element kernel's general body (element_update without its dry-region shortcut). */

@@ -195,17 +195,18 @@ __global__ void __launch_bounds__(BC, 768 / BC) k_cells(StepArgs a) {
   double cflL = 0.0;
   if (c < cend) {
     const double4 U = ld4(a.Uin + c);
-    const double4 st = ld4(a.cstat + c);   /* area, manning n, cfl L, - */
-    const int4 sl = __ldg(a.cslot + c);
     /* a dry element amid dry ones (most of an unflooded plain): its slots are signed zeros and
-     * its update is +0, known from four depths instead of its three slots */
+     * its update is +0, known from four depths and its neighbour entry, without its slots or its
+     * statics (a dry element's CFL value does not use its length) */
     bool dry = false;
     if (!SUMS) {
       const int4 nb = __ldg(a.cnbr + c);
-      dry = dry_element_state(M, U, st, dt) &&
+      dry = dry_state_ok(M, U, dt) &&
             dry_neighbourhood(M, nb, U, [&](int k) { return ldro(reinterpret_cast<const double*>(a.Uin + k)); });
     }
     if (!dry) {
+      const double4 st = ld4(a.cstat + c);   /* area, manning n, cfl L, - */
+      const int4 sl = __ldg(a.cslot + c);
       const Slot s0 = load_slot(a.slots + sl.x);
       const Slot s1 = load_slot(a.slots + sl.y);
       const Slot s2 = load_slot(a.slots + sl.z);
@@ -221,11 +222,11 @@ __global__ void __launch_bounds__(BC, 768 / BC) k_cells(StepArgs a) {
       if (a.xd_cmp && (a.xd_mul_mask & XD_CELLS)) V = element_update<XD<true>>(M, U, st, s0, s1, s2, dt, nonfinite);
       else V = element_update(M, U, st, s0, s1, s2, dt, nonfinite);
       if (nonfinite) atomicOr(&S->status, CF_STATUS_NONFINITE);
+      cflL = st.z;
     }
     double4* o = a.Uout + c;
     reinterpret_cast<double2*>(o)[0] = make_double2(V.x, V.y);
     reinterpret_cast<double2*>(o)[1] = make_double2(V.z, V.w);
-    cflL = st.z;
   }
   block_cfl_min<BC>(M, c < cend, cflL, V, &S->dt[1 - p]);
 }

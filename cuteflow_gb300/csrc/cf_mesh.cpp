@@ -417,8 +417,9 @@ int prepare_mesh(const cf_mesh* m, const cf_params* p, Prep& P, std::string& err
     P.egeo[e] = make_double4(n1, n2, ln, inv_d);
   }
   /* the elements across each element's edges, and whether all three are interior edges with
-   * finite geometry (those edges between two elements of depth +0 take the edge kernel's dry
-   * shortcut, so the element kernel knows their slots without reading them) */
+   * finite geometry and the element's area is one for which a dry update is exact zeros (then the
+   * edges between two elements of depth +0 take the edge kernel's dry shortcut, and the element
+   * kernel knows their slots without reading them) */
   P.cnbr.assign(n, make_int4(-1, -1, -1, 1));
   for (size_t e = 0; e < ne; ++e) {
     const HostEdge& E = P.edges[e];
@@ -433,7 +434,7 @@ int prepare_mesh(const cf_mesh* m, const cf_params* p, Prep& P, std::string& err
     if (!fin) P.cnbr[E.a].w = P.cnbr[E.b].w = 0;
   }
   for (int c = 0; c < n; ++c)
-    if (P.cnbr[c].x < 0 || P.cnbr[c].y < 0 || P.cnbr[c].z < 0) P.cnbr[c].w = 0;
+    if (P.cnbr[c].x < 0 || P.cnbr[c].y < 0 || P.cnbr[c].z < 0 || !area_ok(P.cstat[c].x)) P.cnbr[c].w = 0;
   /* the beds an edge reads: its elements' and, second order, its upwind reconstructions' (the
    * distance-weighted bed of two upwind elements, flux_riemann.cuf:320-366; static) */
   P.ez.resize(ne);

@@ -187,8 +187,7 @@ extern "C" int harness_run(const cf_mesh* m, const cf_params* p, const double* U
     for (int c = 0; c < n; ++c) {
       const int* sl = &P.cslot[c].x;
       bool nf = false;
-      if (dry_element_state(M, cur[c], P.cstat[c], dt) &&
-          dry_neighbourhood(M, P.cnbr[c], cur[c], [&](int k) { return cur[k].x; })) {
+      if (dry_state_ok(M, cur[c], dt) && dry_neighbourhood(M, P.cnbr[c], cur[c], [&](int k) { return cur[k].x; })) {
         ++g_nbhd_took;
         if (!dry_element(M, cur[c], P.cstat[c], slots[sl[0]], slots[sl[1]], slots[sl[2]], dt)) ++g_nbhd_bad;
         nxt[c] = make_double4(0.0, 0.0, 0.0, 0.0);
