@@ -167,16 +167,18 @@ __device__ __forceinline__ void block_cfl_min(const MemberDev& M, bool active, d
   block_min_atomic<BC>(dti, target);
 }
 
-/* 768 threads per SM (at most 85 registers; 80 used, 8 bytes spilled): the element update is a chain
- * of dependent integer-pipe quotients and products, and the extra warps hide its latency
- * (1M elements, tuned, 256-thread blocks: 0.152 -> 0.130 ms).  A block of BC threads (128 or 256,
- * the launch shape) lies within one tile of TILE_C elements, so within one member; each block
- * folds its dt minimum into the member's with one atomic.  SUMS (the recording forward) also
- * stores the element's slot sums; it is a separate instantiation because the compiler shares
- * those sums with the general update's and then forms them ahead of the dry-element test, for
- * every element (1M WAF step: 9 -> 19 FP64 sums per element, 0.088 -> 0.098 ms). */
+/* 1024 threads per SM (at most 64 registers; 116 bytes spilled): the element update is a chain of
+ * dependent integer-pipe quotients and products, and since the dry-region shortcuts most of the
+ * kernel's time is memory latency, which more warps hide (1M WAF step, tuned, 256-thread blocks:
+ * 0.152 -> 0.130 ms from two to three blocks per SM before the shortcuts; 0.088 -> 0.082 ms from
+ * three to four after them).  A block of BC threads (128 or 256, the launch shape) lies within one
+ * tile of TILE_C elements, so within one member; each block folds its dt minimum into the member's
+ * with one atomic.  SUMS (the recording forward) also stores the element's slot sums; it is a
+ * separate instantiation because the compiler shares those sums with the general update's and then
+ * forms them ahead of the dry-element test, for every element (1M WAF step: 9 -> 19 FP64 sums per
+ * element, 0.088 -> 0.098 ms). */
 template <int BC, bool SUMS>
-__global__ void __launch_bounds__(BC, 768 / BC) k_cells(StepArgs a) {
+__global__ void __launch_bounds__(BC, 1024 / BC) k_cells(StepArgs a) {
   const int c0 = a.c_lo + blockIdx.x * BC;   /* the block's first element (c_lo: a part's phase) */
   const int tile = c0 / TILE_C;
   const int m = __ldg(a.ctile_mem + tile);
