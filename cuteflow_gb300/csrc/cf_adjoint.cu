@@ -61,8 +61,10 @@ __device__ __forceinline__ Dual<D> seed(double v, int k, int base) {
 /* The recorded dt and start time of step n of member m: histories are [N][members]. */
 __device__ __forceinline__ size_t hidx(int n, int m, int nm) { return (size_t)n * nm + m; }
 
+/* The replays keep the forward kernels' occupancy: eight edge blocks and four element blocks per SM
+ * (64 registers), where the latency of the integer-pipe chains is hidden by more warps. */
 template <int IFLUX>
-__global__ void __launch_bounds__(TILE_E) k_rep_edges(StepArgs a, const double* dt_hist, const double* t_hist, int n) {
+__global__ void __launch_bounds__(TILE_E, 8) k_rep_edges(StepArgs a, const double* dt_hist, const double* t_hist, int n) {
   const int tile = blockIdx.x;
   const int m = __ldg(a.etile_mem + tile);
   const MemberDev& M = a.mdev[m];
@@ -78,8 +80,8 @@ __global__ void __launch_bounds__(TILE_E) k_rep_edges(StepArgs a, const double* 
   }
 }
 
-__global__ void __launch_bounds__(TILE_C) k_rep_cells(StepArgs a, const double* dt_hist, int n, uint32_t* flag,
-                                                      Slot* sums) {
+__global__ void __launch_bounds__(TILE_C, 4) k_rep_cells(StepArgs a, const double* dt_hist, int n, uint32_t* flag,
+                                                         Slot* sums) {
   const int tile = blockIdx.x;
   const int m = __ldg(a.ctile_mem + tile);
   const MemberDev& M = a.mdev[m];
@@ -153,13 +155,14 @@ __device__ __forceinline__ double4 gather_lambda(const AdjArgs& A, int c, const 
  * / area (R = I, or the semi-implicit matrix of rows (1, 0, 0), (m4, m5, m6), (m7, m8, m9)),
  * then the wet/dry clamp.  Its transpose is applied by hand; only the friction block
  * (q1, q2, q3, n) -> (sf2, sf3, m4..m9) is differentiated with Dual<4> numbers of the step's own
- * friction_terms. */
-__global__ void __launch_bounds__(TILE_C) k_adj_cells(AdjArgs A) {
+ * friction_terms.  128-thread blocks capped at 168 registers: three blocks per SM (a 256-thread
+ * block at its 170 registers left room for one). */
+constexpr int ADJ_CELLS_BLOCK = 128;
+__global__ void __launch_bounds__(ADJ_CELLS_BLOCK, 3) k_adj_cells(AdjArgs A) {
   const StepArgs& a = A.s;
-  const int tile = blockIdx.x;
-  const int mem = __ldg(a.ctile_mem + tile);
+  const int c = blockIdx.x * ADJ_CELLS_BLOCK + threadIdx.x;
+  const int mem = __ldg(a.ctile_mem + c / TILE_C);
   const MemberDev& M = a.mdev[mem];
-  const int c = tile * TILE_C + threadIdx.x;
   if (c >= M.cell_end) return;
   const double4 L = A.gather ? gather_lambda(A, c, A.gw) : ld4(A.lam_init + c);
   const double dt = __ldg(A.dt_hist + hidx(A.n, mem, a.nmembers));
@@ -464,7 +467,7 @@ int launch_record(const double4* Unew, const double* zcell, const MemberState* S
 int launch_adjoint_step(const AdjArgs& A, stream_t s) {
   cudaStream_t st = reinterpret_cast<cudaStream_t>(s);
   const StepArgs& a = A.s;
-  k_adj_cells<<<a.n_ctiles, TILE_C, 0, st>>>(A);
+  k_adj_cells<<<a.n_ctiles * (TILE_C / ADJ_CELLS_BLOCK), ADJ_CELLS_BLOCK, 0, st>>>(A);
   switch (a.iflux) {
     case 1:
       if (a.flux_mode == 0 && A.pend && A.npend) {
