@@ -314,7 +314,7 @@ int cf_get_tuning(cf_ctx* ctx, int32_t* int_compare, int32_t* int_mul_warps);
 /* Launch shape of the step (no counterpart in the reference, whose launch shapes are fixed,
  * finite_volumes_method.cuf:85-109): threads per block of the edge kernel (64, 128 or 256), edges
  * each of its threads evaluates (1 or 2), threads per block of the element kernel (128 or 256).
- * Default (128, 1, 256).  Results are identical bit for bit in every shape. */
+ * Default (256, 1, 128).  Results are identical bit for bit in every shape. */
 int cf_set_launch_shape(cf_ctx* ctx, int32_t edge_block, int32_t edges_per_thread, int32_t cell_block);
 int cf_get_launch_shape(cf_ctx* ctx, int32_t* edge_block, int32_t* edges_per_thread, int32_t* cell_block);
 /* Autotuner: times steps_per_trial steps on the context's own state and keeps the fastest
