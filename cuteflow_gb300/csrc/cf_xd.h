@@ -126,8 +126,9 @@ XD_NOINLINE double em_div(double a, double b) {
   const uint32_t ea = (uint32_t)(ua >> 52) & 0x7ffu, eb = (uint32_t)(ub >> 52) & 0x7ffu;
   const uint64_t S = (ua ^ ub) & 0x8000000000000000ull;
   if (eb - 1u >= 2046u) return xdiv_slow(a, b);
-  if ((ua << 1) == 0) return xdbl(S);  /* +-0 / normal */
-  if (ea - 1u >= 2046u) return xdiv_slow(a, b);
+  /* the zero test only behind the exponent test: the compiler turns a test of (bits << 1) into an
+   * FP64 comparison with zero, an FP64-pipe instruction on every call (measured: one per call) */
+  if (ea - 1u >= 2046u) return ((ua << 1) == 0) ? xdbl(S) : xdiv_slow(a, b);  /* +-0 / normal: +-0 */
   const uint64_t M = (1ull << 52) - 1;
   const uint64_t A = (ua & M) | (1ull << 52), B = (ub & M) | (1ull << 52);
   const uint32_t t = (A < B) ? 1u : 0u;
@@ -202,9 +203,9 @@ XD_HD uint32_t xrsqrt_seed(float f, uint64_t salt) {
  * Every result is the IEEE root's bits. */
 XD_NOINLINE double em_sqrt(double x) {
   const uint64_t ux = xbits(x);
-  if ((ux << 1) == 0) return x;
   const uint32_t ex = (uint32_t)(ux >> 52);  /* sign bit included: negative x fails the test */
-  if (ex - 1u >= 2046u) return xsqrt_slow(x);
+  /* +-0 is its own root; its test only behind the exponent test (see em_div) */
+  if (ex - 1u >= 2046u) return ((ux << 1) == 0) ? x : xsqrt_slow(x);
   const uint64_t X = (ux & ((1ull << 52) - 1)) | (1ull << 52);
   const uint32_t p = (ex & 1u) ^ 1u;
   const int er = (((int)ex - 1023 - (int)p) >> 1) + 1023;  /* the result's exponent field */
