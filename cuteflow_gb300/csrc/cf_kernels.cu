@@ -114,7 +114,7 @@ __device__ __forceinline__ float block_min_f32(float v) {
 __device__ __forceinline__ bool f32_trunc(double x, float& f) {
   const unsigned long long b = dbits(x);
   const unsigned sign = (unsigned)(b >> 32) & 0x80000000u;
-  if ((b << 1) == 0) {
+  if (zero_u(b)) {
     f = __uint_as_float(sign);
     return true;
   }

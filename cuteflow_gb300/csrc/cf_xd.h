@@ -126,9 +126,9 @@ XD_NOINLINE double em_div(double a, double b) {
   const uint32_t ea = (uint32_t)(ua >> 52) & 0x7ffu, eb = (uint32_t)(ub >> 52) & 0x7ffu;
   const uint64_t S = (ua ^ ub) & 0x8000000000000000ull;
   if (eb - 1u >= 2046u) return xdiv_slow(a, b);
-  /* the zero test only behind the exponent test: the compiler turns a test of (bits << 1) into an
-   * FP64 comparison with zero, an FP64-pipe instruction on every call (measured: one per call) */
-  if (ea - 1u >= 2046u) return ((ua << 1) == 0) ? xdbl(S) : xdiv_slow(a, b);  /* +-0 / normal: +-0 */
+  /* a zero numerator has a zero exponent field: its test runs behind the exponent test (written
+   * on the whole pattern ahead of it, the compiler made it an FP64 comparison on every call) */
+  if (ea - 1u >= 2046u) return zero_u(ua) ? xdbl(S) : xdiv_slow(a, b);  /* +-0 / normal: +-0 */
   const uint64_t M = (1ull << 52) - 1;
   const uint64_t A = (ua & M) | (1ull << 52), B = (ub & M) | (1ull << 52);
   const uint32_t t = (A < B) ? 1u : 0u;
@@ -204,8 +204,8 @@ XD_HD uint32_t xrsqrt_seed(float f, uint64_t salt) {
 XD_NOINLINE double em_sqrt(double x) {
   const uint64_t ux = xbits(x);
   const uint32_t ex = (uint32_t)(ux >> 52);  /* sign bit included: negative x fails the test */
-  /* +-0 is its own root; its test only behind the exponent test (see em_div) */
-  if (ex - 1u >= 2046u) return ((ux << 1) == 0) ? x : xsqrt_slow(x);
+  /* +-0 is its own root (tested behind the exponent test, as in em_div) */
+  if (ex - 1u >= 2046u) return zero_u(ux) ? x : xsqrt_slow(x);
   const uint64_t X = (ux & ((1ull << 52) - 1)) | (1ull << 52);
   const uint32_t p = (ex & 1u) ^ 1u;
   const int er = (((int)ex - 1023 - (int)p) >> 1) + 1023;  /* the result's exponent field */
@@ -317,7 +317,7 @@ XD_HD double xscale(double x) {
   const uint32_t lo = (K < 0) ? (uint32_t)(1 - K) : 1u;          /* lowest exponent field handled */
   const uint32_t n = (K < 0) ? (uint32_t)(2046 + K) : (uint32_t)(2046 - K);  /* fields handled */
   if (e - lo < n) return xdbl(b + ((uint64_t)(int64_t)K << 52));
-  if ((b << 1) == 0) return x;
+  if (zero_u(b)) return x;
   return xmul_slow(x, (K == -2) ? 0.25 : ((K == -1) ? 0.5 : 2.0));
 }
 template <bool MUL> XD_HD XD<MUL> halve(const XD<MUL>& x) { return XD<MUL>(MUL ? xscale<-1>(x.v) : x.v * 0.5); }
@@ -332,7 +332,7 @@ XD_HD XD<MUL> div_rn(const XD<MUL>& a, double d, double y) {
   const double q = a.v * y;
   const double r = fma(-d, q, a.v);
   const double q1 = fma(r, y, q);
-  return XD<MUL>(((xbits(a.v) << 1) == 0) ? q : q1);
+  return XD<MUL>(zero_u(xbits(a.v)) ? q : q1);
 }
 template <bool MUL>
 XD_HD XD<MUL> div_rn(const XD<MUL>& a, const XD<MUL>& d, const XD<MUL>& y) {
