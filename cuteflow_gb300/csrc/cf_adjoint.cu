@@ -73,8 +73,9 @@ __global__ void __launch_bounds__(TILE_E, 8) k_rep_edges(StepArgs a, const doubl
   const size_t h = hidx(n, m, a.nmembers);
   const double dt = __ldg(dt_hist + h), t = __ldg(t_hist + h);
   if (a.xd_cmp) {   /* the context's integer-pipe setting, as the step's edge kernel (same results) */
-    if ((a.xd_mul_mask >> (threadIdx.x >> 5)) & 1) edge_body<IFLUX, XD<true>>(a, M, e, dt, t);
-    else edge_body<IFLUX, XD<false>>(a, M, e, dt, t);
+    constexpr bool OC = IFLUX != 3;   /* as the forward edge kernel */
+    if ((a.xd_mul_mask >> (threadIdx.x >> 5)) & 1) edge_body<IFLUX, XD<true, OC>>(a, M, e, dt, t);
+    else edge_body<IFLUX, XD<false, OC>>(a, M, e, dt, t);
   } else {
     edge_body<IFLUX>(a, M, e, dt, t);
   }

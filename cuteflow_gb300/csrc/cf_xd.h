@@ -18,7 +18,7 @@
  * subnormal, infinite or NaN operand (a zero numerator of em_div is covered), a result outside
  * the normal range, and, for em_div and em_sqrt, a remainder check that fails.
  *
- * XD<MUL> is a double that compares on integer keys and, with MUL, multiplies, divides (div_rn
+ * XD<MUL, OC> is a double that compares on integer keys and, with MUL, multiplies, divides (div_rn
  * included) and takes square roots with em_mul, em_div and em_sqrt; sums stay FP64
  * instructions.  Every result is the IEEE binary64 result of the same operation, so code
  * instantiated on XD<...> rounds exactly like the same code on double; which warps use the
@@ -234,34 +234,52 @@ XD_NOINLINE double em_sqrt(double x) {
   return xdbl(((uint64_t)(er - 1) << 52) + S);
 }
 
+/* The bit pattern a comparison keys on.  On the device an opaque register move: when a value that
+ * an FP64 sum has just formed is compared on its bits, the compiler otherwise forms the sum twice,
+ * once for the double and once for its bits (measured: 16 key comparisons of running sums took 35
+ * FP64 additions instead of 18).  (The same move in every bit operation of this file made the WAF
+ * edge slower: it also blocks the folding of its sign flips and scalings.) */
+XD_HD uint64_t xbits_cmp(double x) {
+  uint64_t b;
+#ifdef __CUDA_ARCH__
+  asm("mov.b64 %0, %1;" : "=l"(b) : "d"(x));
+#else
+  memcpy(&b, &x, sizeof(b));
+#endif
+  return b;
+}
+
 /* ordered integer key of a non-NaN double: order of the values, -0 and +0 equal */
 XD_HD long long xkey(uint64_t b) {
   const long long s = (long long)b >> 63;
   return (long long)((b & 0x7fffffffffffffffull) ^ (uint64_t)s) - s;
 }
 XD_HD bool xnan(uint64_t b) { return (b & 0x7fffffffffffffffull) > 0x7ff0000000000000ull; }
-XD_HD bool xlt(double a, double b) {
-  const uint64_t ua = xbits(a), ub = xbits(b);
+/* a < b, a <= b, a == b (IEEE results, NaN compares false) on ordered keys; OC: the keys of the
+ * opaque bit patterns (xbits_cmp), else of the plain ones */
+template <bool OC> XD_HD uint64_t xbits_key(double x) { return OC ? xbits_cmp(x) : xbits(x); }
+template <bool OC = true> XD_HD bool xlt(double a, double b) {
+  const uint64_t ua = xbits_key<OC>(a), ub = xbits_key<OC>(b);
   return !(xnan(ua) | xnan(ub)) & (xkey(ua) < xkey(ub));
 }
-XD_HD bool xle(double a, double b) {
-  const uint64_t ua = xbits(a), ub = xbits(b);
+template <bool OC = true> XD_HD bool xle(double a, double b) {
+  const uint64_t ua = xbits_key<OC>(a), ub = xbits_key<OC>(b);
   return !(xnan(ua) | xnan(ub)) & (xkey(ua) <= xkey(ub));
 }
-XD_HD bool xeq(double a, double b) {
-  const uint64_t ua = xbits(a), ub = xbits(b);
+template <bool OC = true> XD_HD bool xeq(double a, double b) {
+  const uint64_t ua = xbits_key<OC>(a), ub = xbits_key<OC>(b);
   return !(xnan(ua) | xnan(ub)) & (xkey(ua) == xkey(ub));
 }
 
-template <bool MUL>
+template <bool MUL, bool OC = true>
 struct XD {
   double v;
   XD_HD XD() : v(0.0) {}
   XD_HD XD(double x) : v(x) {}  // NOLINT: constants promote implicitly
 };
 
-template <bool MUL>
-XD_HD double val(const XD<MUL>& x) { return x.v; }
+template <bool MUL, bool OC>
+XD_HD double val(const XD<MUL, OC>& x) { return x.v; }
 
 template <bool MUL>
 XD_HD double xd_mul(double a, double b) {
@@ -275,9 +293,9 @@ XD_HD double xd_div(double a, double b) {
 }
 
 #define CF_XD_BIN(op, expr)                                                                               \
-  template <bool MUL> XD_HD XD<MUL> operator op(const XD<MUL>& a, const XD<MUL>& b) { double x = a.v, y = b.v; return XD<MUL>(expr); } \
-  template <bool MUL> XD_HD XD<MUL> operator op(const XD<MUL>& a, double y) { double x = a.v; return XD<MUL>(expr); } \
-  template <bool MUL> XD_HD XD<MUL> operator op(double x, const XD<MUL>& b) { double y = b.v; return XD<MUL>(expr); }
+  template <bool MUL, bool OC> XD_HD XD<MUL, OC> operator op(const XD<MUL, OC>& a, const XD<MUL, OC>& b) { double x = a.v, y = b.v; return XD<MUL, OC>(expr); } \
+  template <bool MUL, bool OC> XD_HD XD<MUL, OC> operator op(const XD<MUL, OC>& a, double y) { double x = a.v; return XD<MUL, OC>(expr); } \
+  template <bool MUL, bool OC> XD_HD XD<MUL, OC> operator op(double x, const XD<MUL, OC>& b) { double y = b.v; return XD<MUL, OC>(expr); }
 CF_XD_BIN(+, x + y)
 CF_XD_BIN(-, x - y)
 CF_XD_BIN(*, xd_mul<MUL>(x, y))
@@ -286,25 +304,25 @@ CF_XD_BIN(/, xd_div<MUL>(x, y))
 
 /* negation as a sign-bit flip: an FP64 negation that is not folded into its consumer is an FP64
  * instruction, and most consumers here are integer code (products, comparisons) */
-template <bool MUL> XD_HD XD<MUL> operator-(const XD<MUL>& a) { return XD<MUL>(xdbl(xbits(a.v) ^ 0x8000000000000000ull)); }
+template <bool MUL, bool OC> XD_HD XD<MUL, OC> operator-(const XD<MUL, OC>& a) { return XD<MUL, OC>(xdbl(xbits(a.v) ^ 0x8000000000000000ull)); }
 
 #define CF_XD_CMP(op, expr)                                                                               \
-  template <bool MUL> XD_HD bool operator op(const XD<MUL>& a, const XD<MUL>& b) { double x = a.v, y = b.v; return expr; } \
-  template <bool MUL> XD_HD bool operator op(const XD<MUL>& a, double y) { double x = a.v; return expr; } \
-  template <bool MUL> XD_HD bool operator op(double x, const XD<MUL>& b) { double y = b.v; return expr; }
-CF_XD_CMP(<, xlt(x, y))
-CF_XD_CMP(>, xlt(y, x))
-CF_XD_CMP(<=, xle(x, y))
-CF_XD_CMP(>=, xle(y, x))
-CF_XD_CMP(==, xeq(x, y))
-CF_XD_CMP(!=, !xeq(x, y))
+  template <bool MUL, bool OC> XD_HD bool operator op(const XD<MUL, OC>& a, const XD<MUL, OC>& b) { double x = a.v, y = b.v; return expr; } \
+  template <bool MUL, bool OC> XD_HD bool operator op(const XD<MUL, OC>& a, double y) { double x = a.v; return expr; } \
+  template <bool MUL, bool OC> XD_HD bool operator op(double x, const XD<MUL, OC>& b) { double y = b.v; return expr; }
+CF_XD_CMP(<, xlt<OC>(x, y))
+CF_XD_CMP(>, xlt<OC>(y, x))
+CF_XD_CMP(<=, xle<OC>(x, y))
+CF_XD_CMP(>=, xle<OC>(y, x))
+CF_XD_CMP(==, xeq<OC>(x, y))
+CF_XD_CMP(!=, !xeq<OC>(x, y))
 #undef CF_XD_CMP
 
-template <bool MUL> XD_HD XD<MUL> sqrt(const XD<MUL>& a) { return XD<MUL>(MUL ? em_sqrt(a.v) : ::sqrt(a.v)); }
-template <bool MUL> XD_HD XD<MUL> rcbrt(const XD<MUL>& a) { return XD<MUL>(rcbrt(a.v)); }
-template <bool MUL> XD_HD XD<MUL> fabs(const XD<MUL>& a) { return XD<MUL>(xdbl(xbits(a.v) & 0x7fffffffffffffffull)); }
-template <bool MUL> XD_HD XD<MUL> sgnmul(const XD<MUL>& x, const XD<MUL>& y) {
-  return XD<MUL>(xdbl(xbits(y.v) ^ (xbits(x.v) & 0x8000000000000000ull)));
+template <bool MUL, bool OC> XD_HD XD<MUL, OC> sqrt(const XD<MUL, OC>& a) { return XD<MUL, OC>(MUL ? em_sqrt(a.v) : ::sqrt(a.v)); }
+template <bool MUL, bool OC> XD_HD XD<MUL, OC> rcbrt(const XD<MUL, OC>& a) { return XD<MUL, OC>(rcbrt(a.v)); }
+template <bool MUL, bool OC> XD_HD XD<MUL, OC> fabs(const XD<MUL, OC>& a) { return XD<MUL, OC>(xdbl(xbits(a.v) & 0x7fffffffffffffffull)); }
+template <bool MUL, bool OC> XD_HD XD<MUL, OC> sgnmul(const XD<MUL, OC>& x, const XD<MUL, OC>& y) {
+  return XD<MUL, OC>(xdbl(xbits(y.v) ^ (xbits(x.v) & 0x8000000000000000ull)));
 }
 
 /* x * 2^K (K = -2, -1, 1) by a change of the exponent field, for a normal x whose result is
@@ -320,22 +338,22 @@ XD_HD double xscale(double x) {
   if (zero_u(b)) return x;
   return xmul_slow(x, (K == -2) ? 0.25 : ((K == -1) ? 0.5 : 2.0));
 }
-template <bool MUL> XD_HD XD<MUL> halve(const XD<MUL>& x) { return XD<MUL>(MUL ? xscale<-1>(x.v) : x.v * 0.5); }
-template <bool MUL> XD_HD XD<MUL> quarter(const XD<MUL>& x) { return XD<MUL>(MUL ? xscale<-2>(x.v) : x.v * 0.25); }
-template <bool MUL> XD_HD XD<MUL> twice(const XD<MUL>& x) { return XD<MUL>(MUL ? xscale<1>(x.v) : x.v * 2.0); }
+template <bool MUL, bool OC> XD_HD XD<MUL, OC> halve(const XD<MUL, OC>& x) { return XD<MUL, OC>(MUL ? xscale<-1>(x.v) : x.v * 0.5); }
+template <bool MUL, bool OC> XD_HD XD<MUL, OC> quarter(const XD<MUL, OC>& x) { return XD<MUL, OC>(MUL ? xscale<-2>(x.v) : x.v * 0.25); }
+template <bool MUL, bool OC> XD_HD XD<MUL, OC> twice(const XD<MUL, OC>& x) { return XD<MUL, OC>(MUL ? xscale<1>(x.v) : x.v * 2.0); }
 
 /* The quotient a / d that div_rn in cf_flux.h forms from y = RN(1/d) by Markstein's step: on the
  * integer path the division itself (the same bits, y unused), otherwise Markstein's step. */
-template <bool MUL>
-XD_HD XD<MUL> div_rn(const XD<MUL>& a, double d, double y) {
-  if (MUL) return XD<MUL>(em_div(a.v, d));
+template <bool MUL, bool OC>
+XD_HD XD<MUL, OC> div_rn(const XD<MUL, OC>& a, double d, double y) {
+  if (MUL) return XD<MUL, OC>(em_div(a.v, d));
   const double q = a.v * y;
   const double r = fma(-d, q, a.v);
   const double q1 = fma(r, y, q);
-  return XD<MUL>(zero_u(xbits(a.v)) ? q : q1);
+  return XD<MUL, OC>(zero_u(xbits(a.v)) ? q : q1);
 }
-template <bool MUL>
-XD_HD XD<MUL> div_rn(const XD<MUL>& a, const XD<MUL>& d, const XD<MUL>& y) {
+template <bool MUL, bool OC>
+XD_HD XD<MUL, OC> div_rn(const XD<MUL, OC>& a, const XD<MUL, OC>& d, const XD<MUL, OC>& y) {
   return div_rn(a, d.v, y.v);
 }
 
