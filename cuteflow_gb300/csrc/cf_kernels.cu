@@ -578,7 +578,9 @@ __global__ void __launch_bounds__(256) k_selftest_xd(long long n, unsigned long 
     nbad += !st_same(em_div(a, b), a / b);
     nbad += !st_same(xscale<-2>(a), a * 0.25) + !st_same(xscale<-1>(a), a * 0.5) + !st_same(xscale<1>(a), a * 2.0);
     nbad += !st_same(val(-XD<true>(a)), -a);
+    /* the key comparisons on opaque and on plain bit patterns */
     nbad += (xlt(a, b) != (a < b)) + (xle(a, b) != (a <= b)) + (xeq(a, b) != (a == b));
+    nbad += (xlt<false>(a, b) != (a < b)) + (xle<false>(a, b) != (a <= b)) + (xeq<false>(a, b) != (a == b));
   }
   if (nbad) atomicAdd(bad, nbad);
 }
