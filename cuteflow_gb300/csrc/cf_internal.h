@@ -7,7 +7,8 @@
  *                  U[n & 1]); the bed elevations live in zcell and, per edge, in ez
  *          cslot : int4 {slot of local edge 0, 1, 2, -}   (local edges in the reference's order)
  *          cnbr  : int4 {element across local edge 0, 1, 2 (-1: boundary), 1 when all three edges
- *                  are interior with finite normals and lengths, else 0}
+ *                  are interior with finite normals and lengths and the area passes area_ok,
+ *                  else 0}
  *          cstat : double4 {area, Manning n, cfl*L_cfl, RN(1/area)}
  *   edges  ecell : int2 {A, B}; B >= 0 another element, B < 0 the boundary kind (-1/-2/-3)
  *          egeo  : double4 {nx, ny, len, d_AB}, normal pointing out of A, centroid distance
