@@ -220,21 +220,26 @@ CFD_HD Dual<N> rcbrt(const Dual<N>& x) {
 CFD_HD bool adj_edge_hllc(const MemberDev& M, const EdgeGeo& G, const double4& UA, const double4& UB, double zml,
                           double zmr, const double w[10], double lamA[3], double lamB[3]) {
   const double g = M.gp, tolisec = M.tolisec, nx = G.nx, ny = G.ny, len = G.len;
-  const double zij = dmax(zml, zmr);
-  double hautl, vitul, vitvl, hautr, vitur, vitvr;
-  to_frame(UA.x, UA.y, UA.z, UA.w, nx, ny, tolisec, hautl, vitul, vitvl);
-  to_frame(UB.x, UB.y, UB.z, UB.w, nx, ny, tolisec, hautr, vitur, vitvr);
-  if (hautl != UA.x || hautr != UB.x) return false;
+  /* the comparisons on integer keys (xlt, xeq, and XD<false> for the frame change: the same IEEE
+   * results and the same double arithmetic) keep them off the FP64 pipe that bounds this kernel */
+  const auto kmax = [](double a, double b) { return xlt(a, b) ? b : a; };   /* Fortran max */
+  const double zij = kmax(zml, zmr);
+  XD<false> hl_, ul_, vl_, hr_, ur_, vr_;
+  to_frame(XD<false>(UA.x), XD<false>(UA.y), XD<false>(UA.z), UA.w, nx, ny, tolisec, hl_, ul_, vl_);
+  to_frame(XD<false>(UB.x), XD<false>(UB.y), XD<false>(UB.z), UB.w, nx, ny, tolisec, hr_, ur_, vr_);
+  const double hautl = val(hl_), vitul = val(ul_), vitvl = val(vl_);
+  const double hautr = val(hr_), vitur = val(ur_), vitvr = val(vr_);
+  if (!xeq(hautl, UA.x) || !xeq(hautr, UB.x)) return false;
   /* hydrostatic reconstruction (flux_riemann.cuf:176-181, :200-210); which variables carry a
    * derivative (a clamped or masked one is a constant of the inputs) */
   const double el = hautl + zml - zij, er = UB.x + zmr - zij;
-  double hl = dmax(0.0, el), hr = dmax(0.0, er);
+  double hl = kmax(0.0, el), hr = kmax(0.0, er);
   double ul = vitul, vl = vitvl, ur = vitur, vr = vitvr;
-  const bool pl = !(hl < tolisec), pr = !(hr < tolisec);
+  const bool pl = !xlt(hl, tolisec), pr = !xlt(hr, tolisec);
   if (!pl) { hl = 0.; ul = 0.; vl = 0.; }
   if (!pr) { hr = 0.; ur = 0.; vr = 0.; }
-  const bool wa = UA.x > tolisec, wb = UB.x > tolisec;   /* frame velocities differentiable */
-  const bool s_hl = pl && 0.0 < el, s_ul = pl && wa, s_hr = pr && 0.0 < er, s_ur = pr && wb;
+  const bool wa = xlt(tolisec, UA.x), wb = xlt(tolisec, UB.x);   /* frame velocities differentiable */
+  const bool s_hl = pl && xlt(0.0, el), s_ul = pl && wa, s_hr = pr && xlt(0.0, er), s_ur = pr && wb;
   const Dual<4> Hl = s_hl ? Dual<4>::var(hl, 0) : Dual<4>(hl), Ul = s_ul ? Dual<4>::var(ul, 1) : Dual<4>(ul);
   const Dual<4> Hr = s_hr ? Dual<4>::var(hr, 2) : Dual<4>(hr), Ur = s_ur ? Dual<4>::var(ur, 3) : Dual<4>(ur);
   TwoFluxT<Dual<4>> F;
@@ -281,9 +286,9 @@ CFD_HD bool adj_edge_hllc(const MemberDev& M, const EdgeGeo& G, const double4& U
    * side A, tb likewise into -(tb nx, tb ny) of side B */
   {
     const double ea = UA.x + zml - zij, eb = UB.x + zmr - zij;
-    const double ha = dmax(0.0, ea), hb = dmax(0.0, eb);
-    const double dta = g / 2.0 * (2.0 * (0.0 < ea ? ha : 0.0) - 2.0 * UA.x) * len;
-    const double dtb = g / 2.0 * (2.0 * (0.0 < eb ? hb : 0.0) - 2.0 * UB.x) * len;
+    const double ha = kmax(0.0, ea), hb = kmax(0.0, eb);
+    const double dta = g / 2.0 * (2.0 * (xlt(0.0, ea) ? ha : 0.0) - 2.0 * UA.x) * len;
+    const double dtb = g / 2.0 * (2.0 * (xlt(0.0, eb) ? hb : 0.0) - 2.0 * UB.x) * len;
     lamA[0] += (w[3] * nx + w[4] * ny) * dta;
     lamB[0] -= (w[8] * nx + w[9] * ny) * dtb;
   }
